@@ -1,0 +1,574 @@
+"""CPU oracle: an FP64 NumPy restatement of horton-part's iterative
+stockholder loop on the molecular grid (MBIS, GISA, aLISA, gLISA).
+
+TEST INFRASTRUCTURE ONLY. This module is the checker for the GPU path and the
+timed CPU baseline of ``bench.py``; the product never imports it. It follows
+the reference algorithm step by step (file:line citations are to the
+reference package ``src/horton_part``), on plain arrays instead of the
+reference's class hierarchy:
+
+* inputs: ``points (N,3)``, ``weights (N,)``, ``rho (N,)``, ``coordinates
+  (A,3)``, ``numbers (A,)``, ``pseudo_numbers (A,)``;
+* results: a dict with the keys the reference stores in ``part.cache``.
+
+Parity of this restatement is pinned against the reference itself: the
+fixtures in ``tests/golden`` were produced by running the unmodified
+reference (through ``oracle/refshim``) on the same inputs, and
+``tests/test_oracle_vs_reference.py`` re-checks it whenever the reference
+source is present. Two reference solvers need packages that are absent here
+(quadprog for GISA, cvxopt for the aLISA/gLISA class defaults); GISA's QP is
+restated as an exact active-set solver (:func:`qp_simplex_nonneg`), so GISA
+parity at that boundary is unpinned.
+
+Vectorised NumPy (BLAS for the gLISA Hessian) replaces a few of the
+reference's Python loops; the arithmetic is the same, and the CPU baseline
+timed from this module is therefore at least as fast as the reference.
+"""
+
+from __future__ import annotations
+
+import math
+import warnings
+
+import numpy as np
+
+DENSITY_CUTOFF = 1e-15  # data/constants.yaml:27
+NEGATIVE_CUTOFF = -1e-12  # data/constants.yaml:28
+POPULATION_CUTOFF = 1e-4  # data/constants.yaml:29
+
+
+class OracleError(RuntimeError):
+    """Raised where the reference raises ``RuntimeError``."""
+
+
+# ---------------------------------------------------------------------------
+# shared pieces
+# ---------------------------------------------------------------------------
+
+
+def radial_distances(points, coordinates):
+    """|p - R_a| for every atom (``core/base.py:630-635``)."""
+    return [np.linalg.norm(points - c, axis=1) for c in coordinates]
+
+
+def integrate(weights, *arrays):
+    prod = arrays[0]
+    for a in arrays[1:]:
+        prod = prod * a
+    return float(np.dot(weights, prod))
+
+
+def entropy(weights, rho, rho0, density_cutoff=DENSITY_CUTOFF):
+    """Integral of rho ln(rho/rho0) with the sick mask (``core/stockholder.py:145-151``)."""
+    sick = (rho0 < density_cutoff) | (rho < density_cutoff)
+    with np.errstate(all="ignore"):
+        ratio = np.divide(rho, rho0, out=np.zeros_like(rho), where=~sick)
+        ln_ratio = np.log(ratio, out=np.zeros_like(rho), where=~sick)
+    return integrate(weights, rho, ln_ratio)
+
+
+def stockholder_weights(proatoms):
+    """Promolecule and clipped at_weights (``core/stockholder.py:153-175, 352-384``).
+
+    The promolecule accumulates each pro-atom and then 1e-100, atom by atom.
+    """
+    promol = np.zeros_like(proatoms[0])
+    for work in proatoms:
+        promol += work
+        promol += 1e-100
+    at_weights = [np.clip(work / promol, 0.0, 1.0) for work in proatoms]
+    return promol, at_weights
+
+
+def finalize(res, numbers, pseudo_numbers):
+    """``finalize_propars`` (``core/iterstock.py:48-58``)."""
+    charges = res["charges"]
+    res["history_propars"] = np.array(res["history_propars"])
+    res["history_charges"] = np.array(res["history_charges"])
+    res["history_entropies"] = np.array(res["history_entropies"])
+    res["history_changes"] = np.array(res["history_changes"])
+    res["populations"] = numbers - charges
+    res["pseudo_populations"] = pseudo_numbers - charges
+    return res
+
+
+# ---------------------------------------------------------------------------
+# MBIS  (mbis.py)
+# ---------------------------------------------------------------------------
+
+
+def mbis_nshell(number):
+    """Number of Slater shells (``mbis.py:36-46``)."""
+    noble = np.array([2, 10, 18, 36, 54, 86, 118])
+    return int(noble.searchsorted(number) + 1)
+
+
+def mbis_initial_propars(number):
+    """Initial (N_k, S_k) pairs (``mbis.py:49-78``)."""
+    nshell = mbis_nshell(number)
+    propars = np.zeros(2 * nshell)
+    s0 = 2.0 * number
+    alpha = (2.0 / s0) ** (1.0 / (nshell - 1)) if nshell > 1 else 1.0
+    nel = np.array([2.0, 8.0, 8.0, 18.0, 18.0, 32.0, 32.0])
+    for k in range(nshell):
+        propars[2 * k] = nel[k]
+        propars[2 * k + 1] = s0 * alpha**k
+    propars[-2] = number - propars[:-2:2].sum()
+    return propars
+
+
+def mbis_proatom(propars_a, r):
+    """sum_k N_k S_k^3 exp(-S_k r) / (8 pi) (``mbis.py:234-289``)."""
+    y = np.zeros(len(r))
+    for k in range(len(propars_a) // 2):
+        n, s = propars_a[2 * k], propars_a[2 * k + 1]
+        y += n * s**3 * np.exp(-s * r) / (8 * np.pi)
+    return y
+
+
+def opt_mbis_propars(rho, propars, weights, r, threshold, density_cutoff=DENSITY_CUTOFF,
+                     maxiter=2000):
+    """Inner MBIS fixed point for one atom (``mbis.py:81-163``).
+
+    Returns ``(propars, n_inner, converged)``.
+    """
+    nshell = len(propars) // 2
+    terms = np.zeros((nshell, len(r)))
+    oldpro = None
+    for irep in range(maxiter):
+        for k in range(nshell):
+            n, s = propars[2 * k], propars[2 * k + 1]
+            terms[k] = n * s**3 * np.exp(-s * r) / (8 * np.pi)
+        pro = terms.sum(axis=0)
+        sick = (rho < density_cutoff) | (pro < density_cutoff)
+        with np.errstate(all="ignore"):
+            ratio = rho / pro
+        ratio[sick] = 0.0
+        terms *= ratio
+        for k in range(nshell):
+            m0 = np.einsum("p,p->", weights, terms[k])
+            m1 = np.einsum("p,p,p->", weights, terms[k], r)
+            propars[2 * k] = m0
+            propars[2 * k + 1] = 3 * m0 / m1
+        if oldpro is None:
+            change = 1e100
+        else:
+            err = oldpro - pro
+            change = np.sqrt(np.einsum("p,p,p->", weights, err, err))
+        if change < threshold:
+            return propars, irep + 1, True
+        oldpro = pro
+    return propars, maxiter, False
+
+
+def mbis(coordinates, numbers, pseudo_numbers, points, weights, rho, threshold=1e-6,
+         maxiter=500, inner_threshold=1e-8, density_cutoff=DENSITY_CUTOFF):
+    """MBIS on the molecular grid (``core/iterstock.py:159-193``, ``mbis.py:167-203``,
+    ``mbis.py:291-362``)."""
+    natom = len(numbers)
+    inner = inner_threshold if inner_threshold < threshold else threshold  # iterstock.py:101
+    rs = radial_distances(points, coordinates)
+    ranges = [0]
+    for z in numbers:
+        ranges.append(ranges[-1] + 2 * mbis_nshell(z))
+    propars = np.concatenate([mbis_initial_propars(z) for z in numbers])
+    res = dict(history_propars=[], history_charges=[], history_entropies=[], history_changes=[],
+               inner_iterations=[])
+    charges = np.zeros(natom)
+    counter = 0
+    while True:
+        counter += 1
+        old = propars.copy()
+        pros = [mbis_proatom(propars[ranges[a]:ranges[a + 1]], rs[a]) for a in range(natom)]
+        promol, at_weights = stockholder_weights(pros)
+        inner_its = []
+        for a in range(natom):
+            rhoa = at_weights[a] * rho
+            sl = slice(ranges[a], ranges[a + 1])
+            new, nit, _ = opt_mbis_propars(rhoa, propars[sl].copy(), weights, rs[a], inner,
+                                           density_cutoff)
+            propars[sl] = new
+            inner_its.append(nit)
+            charges[a] = pseudo_numbers[a] - np.einsum("p,p->", weights, rhoa)
+        res["inner_iterations"].append(inner_its)
+        res["history_propars"].append(propars.copy())
+        res["history_charges"].append(charges.copy())
+        res["history_entropies"].append(entropy(weights, rho, promol, density_cutoff))
+        msd = 0.0
+        for a in range(natom):
+            d = (mbis_proatom(propars[ranges[a]:ranges[a + 1]], rs[a])
+                 - mbis_proatom(old[ranges[a]:ranges[a + 1]], rs[a]))
+            msd += integrate(weights, d, d)
+        change = np.sqrt(msd)
+        res["history_changes"].append(change)
+        if change < threshold or counter >= maxiter:
+            break
+    res.update(charges=charges, propars=propars, niter=counter, change=change,
+               promoldens=promol, at_weights=np.array(at_weights), ranges=np.array(ranges))
+    finalize(res, np.asarray(numbers), np.asarray(pseudo_numbers, dtype=float))
+    valence = np.array([-propars[ranges[a + 1] - 2] for a in range(natom)])
+    widths = np.array([1.0 / propars[ranges[a + 1] - 1] for a in range(natom)])
+    res["valence_charges"] = valence
+    res["valence_widths"] = widths
+    res["core_charges"] = charges - valence
+    return res
+
+
+# ---------------------------------------------------------------------------
+# basis-function schemes: shared  (gisa.py)
+# ---------------------------------------------------------------------------
+
+
+def shell_prefactor(n, alpha):
+    """N(alpha, n) (``core/basis.py:161``)."""
+    return n * alpha ** (3.0 / n) / (4.0 * math.pi * math.gamma(3.0 / n))
+
+
+def basis_functions(orders, exponents, r):
+    """(K, N) array of unit-population shells (``gisa.py:91-106``)."""
+    return np.array([shell_prefactor(n, a) * np.exp(-a * r**n) for n, a in zip(orders, exponents)])
+
+
+def init_basis_propars(initials, pseudo_numbers, weights, rho):
+    """Initial coefficients (``gisa.py:68-88``): initials below 1e-4 raised
+    to 1e-4, each atom normalised to its pseudo number, then all rescaled to
+    the integrated density."""
+    parts = []
+    for inits, zp in zip(initials, pseudo_numbers):
+        inits = np.array(inits, dtype=float)
+        inits[inits < 1e-4] = 1e-4
+        parts.append(inits / np.sum(inits) * zp)
+    propars = np.concatenate(parts)
+    nelec = integrate(weights, rho)
+    return propars / np.sum(propars) * nelec
+
+
+def compute_quantities(density, propars, bs_funcs, density_cutoff):
+    """pro-shells, pro-atom, sick mask, ratio, ln ratio (``utils.py:198-252``)."""
+    pro_shells = bs_funcs * np.asarray(propars).ravel()[:, None]
+    pro = np.einsum("ij->j", pro_shells)
+    sick = (density < density_cutoff) | (pro < density_cutoff)
+    with np.errstate(all="ignore"):
+        ratio = np.divide(density, pro, out=np.zeros_like(density), where=~sick)
+        ln_ratio = np.log(ratio, out=np.zeros_like(density), where=~sick)
+    return pro_shells, pro, sick, ratio, ln_ratio
+
+
+def _population_warning(propars, pop, population_cutoff):
+    if abs(np.sum(propars) - pop) > population_cutoff:  # utils.py:418-456
+        warnings.warn("The sum of pro-atom parameters is not equal to reference population.")
+
+
+def _negativity_error(dens, negative_cutoff):
+    if (dens < negative_cutoff).any():  # utils.py:491-520
+        raise OracleError("Negative pro-atom density found!")
+
+
+# ---------------------------------------------------------------------------
+# GISA  (gisa.py:348-421) - quadratic program
+# ---------------------------------------------------------------------------
+
+
+def qp_simplex_nonneg(P, q, total, maxiter=200):
+    """min 1/2 x^T P x + q^T x  subject to  x >= 0, sum(x) = total.
+
+    Exact primal active-set method (Nocedal & Wright, Algorithm 16.3) started
+    from the feasible point x = total/K. Restates the problem the reference
+    hands to quadprog (``gisa.py:387-421``); quadprog itself is not available.
+    """
+    K = len(q)
+    x = np.full(K, total / K)
+    work = np.zeros(K, dtype=bool)  # True: x_i fixed at 0
+    for _ in range(maxiter):
+        free = ~work
+        nf = int(free.sum())
+        g = P @ x + q
+        kkt = np.zeros((nf + 1, nf + 1))
+        kkt[:nf, :nf] = P[np.ix_(free, free)]
+        kkt[:nf, nf] = 1.0
+        kkt[nf, :nf] = 1.0
+        rhs = np.concatenate([-g[free], [0.0]])
+        sol = np.linalg.solve(kkt, rhs)
+        p = np.zeros(K)
+        p[free] = sol[:nf]
+        lam = sol[nf]
+        if np.max(np.abs(p)) <= 1e-14 * max(1.0, np.max(np.abs(x))):
+            mu = g + lam
+            mu[free] = 0.0
+            if not work.any() or mu[work].min() >= -1e-14:
+                return x
+            j = np.where(work)[0][np.argmin(mu[work])]
+            work[j] = False
+            continue
+        alpha, block = 1.0, -1
+        for i in np.where(free & (p < 0))[0]:
+            a = -x[i] / p[i]
+            if a < alpha:
+                alpha, block = a, i
+        x = x + alpha * p
+        if block >= 0:
+            x[block] = 0.0
+            work[block] = True
+    raise OracleError("QP active-set solver did not converge")
+
+
+def gisa_qp(bs_funcs, rho, weights, alphas):
+    """One atom's GISA update (``gisa.py:348-421``)."""
+    a = np.asarray(alphas, dtype=float)
+    P = 2 / np.pi**1.5 * (a[:, None] * a[None, :]) ** 1.5 / (a[:, None] + a[None, :]) ** 1.5
+    P = (P + P.T) / 2
+    q = -2 * np.einsum("i,ni,i->n", weights, bs_funcs, rho)
+    pop = np.einsum("i,i", weights, rho)
+    x = qp_simplex_nonneg(P, q, pop)
+    _population_warning(x, pop, POPULATION_CUTOFF)
+    return x
+
+
+# ---------------------------------------------------------------------------
+# aLISA inner solvers  (alisa.py)
+# ---------------------------------------------------------------------------
+
+
+def lisa_solver_sc(bs_funcs, rho, propars, weights, threshold, density_cutoff=DENSITY_CUTOFF,
+                   max_niter_inner=100000):
+    """Self-consistent update c_k <- int w c_k g_k rho/pro (``alisa.py:193-291``)."""
+    oldpro = None
+    for irep in range(int(max_niter_inner)):
+        pro_shells, pro, sick, ratio, _ = compute_quantities(rho, propars, bs_funcs,
+                                                            density_cutoff)
+        propars[:] = np.einsum("p,ip->i", weights, pro_shells * ratio)
+        if oldpro is None:
+            change = 1e100
+        else:
+            err = oldpro - pro
+            change = np.sqrt(np.einsum("i,i,i", weights, err, err))
+        if change < threshold:
+            _population_warning(propars, np.einsum("i,i", weights, rho), POPULATION_CUTOFF)
+            return propars, irep + 1
+        oldpro = pro
+    warnings.warn("Warning: Inner iteration is not converge!")
+    return propars, int(max_niter_inner)
+
+
+def lisa_solver_newton(bs_funcs, rho, propars, weights, threshold, mode="exact",
+                       density_cutoff=DENSITY_CUTOFF, negative_cutoff=NEGATIVE_CUTOFF,
+                       tau=1.0, linspace_size=20, niter=10000):
+    """Newton / modified Newton on one atom (``alisa.py:753-938``)."""
+    from scipy.linalg import solve
+
+    oldpro = None
+    change = 1e100
+    pop = np.einsum("i,i", weights, rho)
+    for irep in range(niter):
+        _, pro, sick, ratio, _ = compute_quantities(rho, propars, bs_funcs, density_cutoff)
+        if oldpro is not None:
+            err = oldpro - pro
+            change = np.sqrt(np.einsum("i,i,i", weights, err, err))
+        if change < threshold:
+            _negativity_error(pro, negative_cutoff)
+            _population_warning(propars, pop, POPULATION_CUTOFF)
+            return propars, irep + 1
+        integrand = bs_funcs * ratio
+        with np.errstate(all="ignore"):
+            grad_integrand = integrand / pro
+        grad_integrand[:, sick] = 0.0
+        df = -np.einsum("kp,p->k", integrand, weights)
+        hess = np.einsum("kp,jp,p->kj", grad_integrand, bs_funcs, weights)
+        delta = solve(hess, -1 - df, assume_a="sym")
+        if mode == "exact":
+            propars[:] = propars + delta
+        else:
+            for x in np.linspace(tau, 0, linspace_size):
+                new = propars + x * delta
+                new_pro = np.einsum("ij->j", bs_funcs * new[:, None])
+                if (new_pro > negative_cutoff).all():
+                    propars[:] = new
+                    break
+            else:
+                raise OracleError("Line search failed!")
+        oldpro = pro
+    raise OracleError("Inner loop: Newton does not converge!")
+
+
+# ---------------------------------------------------------------------------
+# GISA / aLISA outer loop  (core/iterstock.py:159-193, gisa.py:251-279)
+# ---------------------------------------------------------------------------
+
+
+def basis_scheme(scheme, coordinates, numbers, pseudo_numbers, points, weights, rho, orders,
+                 exponents, initials, threshold=1e-6, maxiter=500, inner_threshold=1e-8,
+                 solver="sc", density_cutoff=DENSITY_CUTOFF, negative_cutoff=NEGATIVE_CUTOFF):
+    """GISA (``scheme='gisa'``) or aLISA (``scheme='lisa'``) on the molecular grid.
+
+    ``orders/exponents/initials`` are per-atom lists of arrays.
+    """
+    natom = len(numbers)
+    inner = inner_threshold if inner_threshold < threshold else threshold
+    rs = radial_distances(points, coordinates)
+    bs = [basis_functions(orders[a], exponents[a], rs[a]) for a in range(natom)]
+    ranges = np.concatenate([[0], np.cumsum([len(e) for e in exponents])])
+    propars = init_basis_propars(initials, pseudo_numbers, weights, rho)
+    res = dict(history_propars=[], history_charges=[], history_entropies=[], history_changes=[],
+               inner_iterations=[])
+    charges = np.zeros(natom)
+    counter = 0
+    while True:
+        counter += 1
+        old = propars.copy()
+        pros = [propars[ranges[a]:ranges[a + 1]] @ bs[a] for a in range(natom)]
+        promol, at_weights = stockholder_weights(pros)
+        its = []
+        for a in range(natom):
+            rhoa = at_weights[a] * rho
+            sl = slice(ranges[a], ranges[a + 1])
+            if scheme == "gisa":
+                propars[sl] = gisa_qp(bs[a], rhoa, weights, exponents[a])
+                its.append(1)
+            elif solver == "sc":
+                new, nit = lisa_solver_sc(bs[a], rhoa, propars[sl].copy(), weights, inner,
+                                          density_cutoff)
+                propars[sl] = new
+                its.append(nit)
+            elif solver in ("newton", "m-newton"):
+                new, nit = lisa_solver_newton(
+                    bs[a], rhoa, propars[sl].copy(), weights, inner,
+                    mode="exact" if solver == "newton" else "modified",
+                    density_cutoff=density_cutoff, negative_cutoff=negative_cutoff)
+                propars[sl] = new
+                its.append(nit)
+            else:
+                raise NotImplementedError(solver)
+            charges[a] = pseudo_numbers[a] - integrate(weights, rhoa)
+        res["inner_iterations"].append(its)
+        res["history_propars"].append(propars.copy())
+        res["history_charges"].append(charges.copy())
+        res["history_entropies"].append(entropy(weights, rho, promol, density_cutoff))
+        msd = 0.0
+        for a in range(natom):
+            d = (propars[ranges[a]:ranges[a + 1]] - old[ranges[a]:ranges[a + 1]]) @ bs[a]
+            msd += integrate(weights, d, d)
+        change = np.sqrt(msd)
+        res["history_changes"].append(change)
+        if change < threshold or counter >= maxiter:
+            break
+    res.update(charges=charges, propars=propars, niter=counter, change=change,
+               promoldens=promol, at_weights=np.array(at_weights), ranges=ranges)
+    return finalize(res, np.asarray(numbers), np.asarray(pseudo_numbers, dtype=float))
+
+
+# ---------------------------------------------------------------------------
+# gLISA  (glisa.py)
+# ---------------------------------------------------------------------------
+
+
+def _fix_propars(exp_array, propars, delta):
+    """Indices of the most diffuse shells to freeze (``utils.py:556-577``)."""
+    fixed = []
+    check = True
+    for idx in np.argsort(exp_array):
+        if check and np.abs(propars[idx]) < 1e-4 and delta[idx] < 0.0:
+            fixed.append(idx)
+        else:
+            check = False
+    return fixed
+
+
+def glisa(coordinates, numbers, pseudo_numbers, points, weights, rho, orders, exponents,
+          initials, threshold=1e-6, maxiter=100, solver="newton",
+          density_cutoff=DENSITY_CUTOFF, negative_cutoff=NEGATIVE_CUTOFF, linspace_size=40,
+          tau=1.0):
+    """gLISA on the molecular grid (``glisa.py:248-281``) with the ``newton``,
+    ``m-newton`` (``glisa.py:617-803``) or ``sc`` (``glisa.py:805-879``) solver."""
+    from scipy.linalg import solve
+
+    natom = len(numbers)
+    rs = radial_distances(points, coordinates)
+    G = np.concatenate([basis_functions(orders[a], exponents[a], rs[a]) for a in range(natom)])
+    ranges = np.concatenate([[0], np.cumsum([len(e) for e in exponents])])
+    propars = init_basis_propars(initials, pseudo_numbers, weights, rho)
+    pop = integrate(weights, rho)
+    res = dict(history_propars=[], history_charges=[], history_entropies=[], history_changes=[])
+
+    def change_of(p1, p2):
+        msd = 0.0
+        for a in range(natom):
+            d = (p1[ranges[a]:ranges[a + 1]] - p2[ranges[a]:ranges[a + 1]]) @ G[ranges[a]:ranges[a + 1]]
+            msd += integrate(weights, d, d)
+        return np.sqrt(msd)
+
+    def promol_valid(p):
+        for a in range(natom):
+            if (p[ranges[a]:ranges[a + 1]] @ G[ranges[a]:ranges[a + 1]] < negative_cutoff).any():
+                return False
+        return True
+
+    niter = None
+    if solver in ("newton", "m-newton"):
+        for irep in range(maxiter):
+            old = propars.copy()
+            pro = propars @ G
+            sick = (rho < density_cutoff) | (pro < density_cutoff)
+            with np.errstate(all="ignore"):
+                d1 = np.where(sick, 0.0, rho / pro)  # rho / rho0
+            df = -(G @ (weights * d1))
+            hess = (G * (weights * np.where(sick, 0.0, d1 / np.where(sick, 1.0, pro)))) @ G.T
+            try:
+                delta = solve(hess, -1 - df, assume_a="sym")
+            except np.linalg.LinAlgError as e:
+                raise OracleError(str(e))
+            if solver == "newton":
+                propars = propars + delta
+            else:
+                keep = np.ones_like(delta)
+                for a in range(natom):
+                    sl = slice(ranges[a], ranges[a + 1])
+                    for i in _fix_propars(np.asarray(exponents[a]), propars[sl], delta[sl]):
+                        keep[i + ranges[a]] = 0
+                for x in np.linspace(tau, 0, linspace_size, endpoint=False):
+                    new = propars + keep * (x * delta)
+                    if promol_valid(new):
+                        break
+                else:
+                    raise OracleError("Line search failed!")
+                propars = new
+            ent = entropy(weights, rho, pro, density_cutoff)
+            change = change_of(propars, old)
+            res["history_entropies"].append(ent)
+            res["history_propars"].append(propars.copy())
+            res["history_changes"].append(change)
+            if change < threshold:
+                _negativity_error(pro, negative_cutoff)
+                _population_warning(propars, pop, POPULATION_CUTOFF)
+                niter = irep + 1
+                break
+        else:
+            raise OracleError("Not converged!")
+    elif solver == "sc":
+        it = 0
+        while True:
+            old = propars.copy()
+            rho0 = old @ G
+            sick = (rho < density_cutoff) | (rho0 < density_cutoff)
+            with np.errstate(all="ignore"):
+                f = np.where(sick, 0.0, rho / rho0)
+            propars = old * (G @ (weights * f))
+            change = change_of(propars, old)
+            res["history_entropies"].append(entropy(weights, rho, rho0, density_cutoff))
+            res["history_changes"].append(change)
+            res["history_propars"].append(propars.copy())
+            if change < threshold:
+                break
+            it += 1
+            if it >= maxiter:
+                raise OracleError("Not converged!")
+        niter = it + 1
+    else:
+        raise NotImplementedError(solver)
+
+    pros = [propars[ranges[a]:ranges[a + 1]] @ G[ranges[a]:ranges[a + 1]] for a in range(natom)]
+    promol, at_weights = stockholder_weights(pros)
+    charges = np.array([pseudo_numbers[a] - integrate(weights, at_weights[a] * rho)
+                        for a in range(natom)])
+    res.update(charges=charges, propars=propars, niter=niter, promoldens=promol,
+               at_weights=np.array(at_weights), ranges=ranges)
+    return finalize(res, np.asarray(numbers), np.asarray(pseudo_numbers, dtype=float))

@@ -1,0 +1,320 @@
+// Internal declarations shared by the partitioning kernels and the runtime.
+//
+// Data layout in HBM (per job):
+//   grid       px, py, pz, w, rho          FP64 SoA, npoint each
+//              pxh/pxl ... (float hi/lo)   mixed precision only
+//   atoms      ax, ay, az                  FP64, natom
+//   shells     shell_off[natom+1], per-shell (order, alpha, prefactor)
+//   params     propars / propars_old / cur / prev      FP64, nparam
+//   per point  promol                      FP64, npoint
+//   per pair   rhoa[natom][npoint]         FP64 (the AIM density w_a * rho)
+//   partials   apart[natom][QA][ntile]     FP64 per (atom, point-tile) sums
+//              jpart[QJ][ntile]            FP64 per point-tile sums
+//
+// Work is cut into point tiles of kTilePoints consecutive grid points. Every
+// kernel is launched over a *batch* of jobs: block b finds its job by a
+// binary search in a prefix array of per-job block counts, so one launch
+// serves many molecules of uneven size. All reductions are deterministic:
+// fixed per-thread point order, fixed warp-shuffle trees, per-tile partials
+// written without atomics and summed over tiles in a fixed order.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace hp {
+
+constexpr int kThreads = 256;
+constexpr int kWarps = kThreads / 32;
+constexpr int kMaxShells = 16;  // per atom
+// A point tile is kThreads * ppt consecutive points; ppt is fixed per job
+// (it depends only on that job's npoint, so a job's reductions are the same
+// alone and inside a batch).
+
+// Per-atom partial quantities (index q in apart[atom][q][tile]).
+// Layout depends on the kernel family; QA is the per-atom stride.
+enum AtomQ {
+  QA_POP = 0,      // sum w * rho_a (from the at_weights pass)
+  QA_CHANGE = 1,   // sum w * (pro_new - pro_old)^2 (outer change)
+  QA_INNER = 2     // first slot of the inner-solver quantities
+};
+
+// Per-job partial quantities (index q in jpart[q][tile]).
+enum JobQ {
+  QJ_ENTROPY = 0,  // sum w rho ln(rho/promol)
+  QJ_NELEC = 1,    // sum w rho
+  QJ_NEG = 2,      // count of points with promolecule < negative_cutoff
+  QJ_COUNT = 3
+};
+
+// Device-side scalars of a job, mirrored to pinned host memory after each
+// step (one contiguous array of Mailbox for all job slots of a context).
+enum MailD {
+  MD_CHANGE = 0,      // last outer change
+  MD_ENTROPY = 1,     // last entropy
+  MD_NELEC = 2,       // integrated density
+  MD_INNER_TOTAL = 3, // inner iterations summed over atoms (exact in FP64)
+  MD_LS_X = 4,        // accepted line-search step (gLISA m-newton)
+  MD_COUNT = 8
+};
+enum MailI {
+  MI_ITER = 0,        // outer iterations done (history rows written)
+  MI_NACTIVE = 1,     // atoms whose inner solver is still running
+  MI_ERR = 2,         // ErrFlag bits
+  MI_WARN = 3,        // warning bits (HP_WARN_*)
+  MI_CONVERGED = 4,   // gLISA solver converged flag
+  MI_COUNT = 8
+};
+struct Mailbox {
+  double d[MD_COUNT];
+  int i[MI_COUNT];
+};
+
+enum ErrFlag {
+  E_NEG_DENSITY = 1,   // pro-atom / promolecule density below negative_cutoff
+  E_SINGULAR = 2,      // Hessian not positive definite
+  E_LINESEARCH = 4,    // no valid trial step
+  E_INNER_NOT_CONV = 8,// Newton inner loop hit its iteration limit
+  E_QP = 16            // QP active-set did not finish
+};
+
+enum WarnFlag { W_INNER = 1, W_POPULATION = 2, W_NEG_PARS = 4 };
+
+enum Scheme { SCHEME_MBIS = 0, SCHEME_GISA = 1, SCHEME_LISA = 2, SCHEME_GLISA = 3 };
+enum Solver { SOLVER_DEFAULT = 0, SOLVER_SC = 1, SOLVER_NEWTON = 2, SOLVER_M_NEWTON = 3,
+              SOLVER_QP = 4 };
+enum Model { MODEL_MBIS = 0, MODEL_BASIS = 1 };
+
+struct JobDev {
+  // grid
+  const double* px;
+  const double* py;
+  const double* pz;
+  const double* w;
+  const double* rho;
+  const float* pxh; const float* pxl;
+  const float* pyh; const float* pyl;
+  const float* pzh; const float* pzl;
+  const float* wf;
+  const float* rhof;
+  // atoms and shells
+  const double* ax;
+  const double* ay;
+  const double* az;
+  const double* zpseudo;
+  const int* shell_off;   // natom + 1
+  const int* par_off;     // natom + 1
+  const double* sh_order;
+  const double* sh_alpha;
+  const double* sh_pref;
+  // parameters and solver state
+  double* propars;
+  double* propars_init;   // initial parameters (hp_job_reset)
+  double* propars_old;
+  double* cur;
+  double* prev;
+  double* delta;          // Newton steps (nparam)
+  double* keep;           // gLISA line-search mask (nparam)
+  // buffers
+  double* promol;
+  double* rhoa;
+  double* apart;
+  double* jpart;
+  double* atom_out;       // [natom][AO_COUNT]
+  int* active;            // natom
+  int* inner_it;          // natom
+  int* ls_fail;           // per (atom, tile) line-search failure bitmask
+  double* gmat;           // gLISA: basis values [nshell][npoint]
+  double* gpart;          // gLISA: gradient partials [nshell][ntile]
+  double* hpart;          // gLISA: Hessian partials [nsplit][nshell][nshell]
+  double* hess;           // gLISA: Hessian [nshell][nshell]
+  double* chol;           // gLISA: Cholesky factor work space [nshell][nshell]
+  double* grad;           // gLISA: gradient [nshell]
+  double* dvec1;          // gLISA: w rho / rho0 (0 where sick), npoint
+  double* dvec2;          // gLISA: w rho / rho0^2 (0 where sick), npoint
+  double* hist_propars;   // [maxiter][nparam]
+  double* hist_charges;   // [maxiter][natom]
+  double* hist_ent;       // [maxiter]
+  double* hist_chg;       // [maxiter]
+  double* charges;        // natom
+  Mailbox* mail;
+  int natom, npoint, ntile, nparam, nshell, qa;
+  int scheme, solver, mixed, maxiter;
+  int inner_maxiter, linspace_size, nsplit, ppt;  // ppt: points per thread per tile
+  int tile_points, htiles, pad1, pad2;           // htiles: 64-wide Hessian tiles per side
+  double threshold, inner_threshold, density_cutoff, negative_cutoff, population_cutoff, tau;
+};
+
+enum AtomOut {
+  AO_POP = 0,
+  AO_CHANGE = 1,
+  AO_INNER_CHANGE = 2,
+  AO_LS_X = 3,
+  AO_COUNT = 4
+};
+
+// A batch of jobs for one launch: block b belongs to the job j with
+// prefix[j] <= b < prefix[j + 1].
+struct Batch {
+  const JobDev* jobs;
+  const int* prefix;
+  int njobs;
+};
+
+__device__ __forceinline__ int find_job(const Batch& bt, int b) {
+  int lo = 0, hi = bt.njobs - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (bt.prefix[mid] <= b) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+// Deterministic block sum of Q per-thread values. Result valid in out[0..Q)
+// (shared memory) after the call, for all threads.
+template <int Q>
+__device__ __forceinline__ void block_sum(double (&acc)[Q], double* red /* [kWarps][Q] */,
+                                          double* out /* [Q] */) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int q = 0; q < Q; ++q) {
+    double v = acc[q];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) red[warp * Q + q] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < Q) {
+    double s = 0.0;
+#pragma unroll
+    for (int k = 0; k < kWarps; ++k) s += red[k * Q + threadIdx.x];
+    out[threadIdx.x] = s;
+  }
+  __syncthreads();
+}
+
+__device__ __forceinline__ double block_sum1(double v, double* red) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  if (lane == 0) red[warp] = v;
+  __syncthreads();
+  double s = 0.0;
+#pragma unroll
+  for (int k = 0; k < kWarps; ++k) s += red[k];
+  __syncthreads();
+  return s;
+}
+
+// Fixed-order sum of n values with stride (one thread).
+__device__ __forceinline__ double serial_sum(const double* p, int n) {
+  double s = 0.0;
+  for (int i = 0; i < n; ++i) s += p[i];
+  return s;
+}
+
+// Distance from grid point p to atom a.
+template <typename T>
+struct Dist;
+
+template <>
+struct Dist<double> {
+  __device__ __forceinline__ static double r(const JobDev& J, int p, int a) {
+    const double dx = J.px[p] - J.ax[a];
+    const double dy = J.py[p] - J.ay[a];
+    const double dz = J.pz[p] - J.az[a];
+    return sqrt(dx * dx + dy * dy + dz * dz);
+  }
+};
+
+// Mixed precision: coordinates as float hi + lo pairs; the difference is
+// formed as (xh - axh) + (xl - axl), which keeps ~1e-7 relative accuracy
+// in the distance without FP64 arithmetic.
+template <>
+struct Dist<float> {
+  __device__ __forceinline__ static float r(const JobDev& J, int p, int a) {
+    const float axh = (float)J.ax[a];
+    const float ayh = (float)J.ay[a];
+    const float azh = (float)J.az[a];
+    const float axl = (float)(J.ax[a] - (double)axh);
+    const float ayl = (float)(J.ay[a] - (double)ayh);
+    const float azl = (float)(J.az[a] - (double)azh);
+    const float dx = (J.pxh[p] - axh) + (J.pxl[p] - axl);
+    const float dy = (J.pyh[p] - ayh) + (J.pyl[p] - ayl);
+    const float dz = (J.pzh[p] - azh) + (J.pzl[p] - azl);
+    return sqrtf(dx * dx + dy * dy + dz * dz);
+  }
+};
+
+__device__ __forceinline__ double dexp(double x) { return exp(x); }
+__device__ __forceinline__ float dexp(float x) { return expf(x); }
+
+constexpr double kInv8Pi = 0.039788735772973836;  // 1 / (8 pi)
+
+// MBIS Slater shell N S^3 exp(-S r) / (8 pi)  (mbis.py:128, mbis.py:258)
+template <typename T>
+__device__ __forceinline__ T slater_shell(T n, T s, T r) {
+  return n * (s * s * s) * dexp(-s * r) * (T)kInv8Pi;
+}
+
+// Basis shell N(alpha, n) exp(-alpha r^n), unit population (core/basis.py:161-163)
+template <typename T>
+__device__ __forceinline__ T basis_shell(T order, T alpha, T pref, T r) {
+  T rn;
+  if (order == (T)2) rn = r * r;
+  else if (order == (T)1) rn = r;
+  else rn = pow(r, order);
+  return pref * dexp(-alpha * rn);
+}
+
+}  // namespace hp
+
+namespace hp {
+
+// Launch kinds: blocks per job for each kind of work.
+enum Kind {
+  K_POINT = 0,      // one block per point tile
+  K_ATOM_TILE = 1,  // one block per (atom, point tile)
+  K_ATOM = 2,       // one 32-thread block per atom
+  K_JOB = 3,        // one block per job
+  K_HESS = 4,       // gLISA Hessian: (tile pair, point split)
+  K_SQUARE = 5,     // gLISA reduce: ceil(nshell^2 / kThreads)
+  K_NKIND = 6
+};
+
+struct HostBatch {
+  Batch b[K_NKIND];
+  int blocks[K_NKIND];
+};
+
+void launch_nelec(const HostBatch& hb, cudaStream_t st);
+void launch_copy_old(const HostBatch& hb, cudaStream_t st);
+void launch_promol(const HostBatch& hb, cudaStream_t st, int mixed, int model);
+void launch_final_atweights(const HostBatch& hb, cudaStream_t st, int mixed, int model, int use_old);
+void launch_change(const HostBatch& hb, cudaStream_t st, int mixed, int model);
+void launch_outer_finish(const HostBatch& hb, cudaStream_t st, int with_charges);
+void launch_charges(const HostBatch& hb, cudaStream_t st);
+void launch_inner_init(const HostBatch& hb, cudaStream_t st);
+void launch_count_active(const HostBatch& hb, cudaStream_t st);
+void launch_mbis_inner(const HostBatch& hb, cudaStream_t st, int mixed);
+void launch_gisa(const HostBatch& hb, cudaStream_t st, int mixed);
+void launch_lisa_sc_inner(const HostBatch& hb, cudaStream_t st, int mixed);
+void launch_lisa_newton_inner(const HostBatch& hb, cudaStream_t st, int mixed, int modified);
+void launch_glisa_basis(const HostBatch& hb, cudaStream_t st);
+void launch_glisa_pro(const HostBatch& hb, cudaStream_t st);
+void launch_glisa_grad(const HostBatch& hb, cudaStream_t st);
+void launch_glisa_hess(const HostBatch& hb, cudaStream_t st);
+void launch_glisa_reduce(const HostBatch& hb, cudaStream_t st);
+void launch_glisa_solve(const HostBatch& hb, cudaStream_t st);
+void launch_glisa_apply(const HostBatch& hb, cudaStream_t st, int mode);
+void launch_glisa_keep(const HostBatch& hb, cudaStream_t st);
+void launch_glisa_ls(const HostBatch& hb, cudaStream_t st, int first, int count);
+void launch_glisa_change(const HostBatch& hb, cudaStream_t st);
+void launch_glisa_check(const HostBatch& hb, cudaStream_t st);
+
+extern long long g_launch_count;
+
+constexpr int kHessTile = 64;
+constexpr int kNewtonQ(int k) { return k + k * (k + 1) / 2 + 2; }
+
+}  // namespace hp

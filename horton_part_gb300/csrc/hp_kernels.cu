@@ -1,0 +1,1397 @@
+// Partitioning kernels for sm_103a.
+//
+// One kernel family per hot-path step of horton-part's stockholder loop
+// (file:line are in the reference package src/horton_part):
+//   k_promol          pro-atoms on the molecular grid + promolecule
+//                     (core/stockholder.py:153-175, 352-367; mbis.py:263-289;
+//                      gisa.py:202-220)
+//   k_atweights       at_weights = clip(pro_a / promol, 0, 1), rho_a = w_a rho,
+//                     per-atom populations, entropy integral
+//                     (core/stockholder.py:369-377, 145-151; mbis.py:200-203)
+//   k_change          sum_a int (rho_a0(new) - rho_a0(old))^2
+//                     (core/iterstock.py:32-45)
+//   k_mbis_*          MBIS inner fixed point (mbis.py:81-163)
+//   k_basis_qvec, k_gisa_qp   GISA quadratic program (gisa.py:348-421)
+//   k_lisa_sc_*       aLISA self-consistent solver (alisa.py:193-291)
+//   k_lisa_newton_*   aLISA (modified) Newton solver (alisa.py:753-938)
+//   k_glisa_*         gLISA global Newton / SC (glisa.py:335-479, 617-879)
+// Every kernel runs over a batch of jobs (see hp_internal.cuh).
+#include <math.h>
+
+#include "hp_internal.cuh"
+
+namespace hp {
+
+// ---------------------------------------------------------------------------
+// helpers
+// ---------------------------------------------------------------------------
+
+struct AtomTile {
+  int job, atom, tile;
+};
+
+__device__ __forceinline__ const JobDev& decode_local(const Batch& bt, int& local) {
+  const int b = blockIdx.x;
+  const int j = find_job(bt, b);
+  local = b - bt.prefix[j];
+  return bt.jobs[j];
+}
+
+__device__ __forceinline__ AtomTile decode_atom_tile(const Batch& bt, const JobDev*& Jp) {
+  const int b = blockIdx.x;
+  const int j = find_job(bt, b);
+  Jp = &bt.jobs[j];
+  const int local = b - bt.prefix[j];
+  AtomTile t;
+  t.job = j;
+  t.atom = local / Jp->ntile;
+  t.tile = local - t.atom * Jp->ntile;
+  return t;
+}
+
+__device__ __forceinline__ int point_of(const JobDev& J, int tile, int i) {
+  return tile * J.tile_points + i * kThreads + threadIdx.x;
+}
+
+// Warp sum over tiles with a fixed lane order (deterministic).
+__device__ __forceinline__ double warp_tile_sum(const double* p, int ntile) {
+  const int lane = threadIdx.x & 31;
+  double s = 0.0;
+  for (int t = lane; t < ntile; t += 32) s += p[t];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  return s;
+}
+
+__device__ __forceinline__ double* apart_ptr(const JobDev& J, int a, int q) {
+  return J.apart + ((size_t)a * J.qa + q) * J.ntile;
+}
+
+template <typename T>
+__device__ __forceinline__ T shell_value(const JobDev& J, int s, T r) {
+  return basis_shell<T>((T)J.sh_order[s], (T)J.sh_alpha[s], (T)J.sh_pref[s], r);
+}
+
+// Pro-atom of atom a at distance r with parameters par.
+template <typename T, int MODEL>
+__device__ __forceinline__ T proatom(const JobDev& J, int a, const double* par, T r) {
+  const int s0 = J.shell_off[a], s1 = J.shell_off[a + 1];
+  const double* pa = par + J.par_off[a];
+  T y = (T)0;
+  if (MODEL == MODEL_MBIS) {
+    for (int k = 0; k < s1 - s0; ++k) y += slater_shell<T>((T)pa[2 * k], (T)pa[2 * k + 1], r);
+  } else {
+    for (int k = 0; k < s1 - s0; ++k) y += (T)pa[k] * shell_value<T>(J, s0 + k, r);
+  }
+  return y;
+}
+
+// numpy.linspace(start, stop, num, endpoint): i * step + start, last element
+// forced to stop when endpoint is true.
+__device__ __forceinline__ double linspace_at(double start, double stop, int num, bool endpoint,
+                                              int i) {
+  const int div = endpoint ? num - 1 : num;
+  if (endpoint && i == num - 1) return stop;
+  const double step = (stop - start) / (double)div;
+  return (double)i * step + start;
+}
+
+// In-place Cholesky solve of a small SPD system (n <= 16), one thread.
+// Returns false when a pivot is not positive.
+__device__ bool small_chol_solve(double* A /* n*n */, double* b, int n) {
+  for (int k = 0; k < n; ++k) {
+    double d = A[k * n + k];
+    for (int j = 0; j < k; ++j) d -= A[k * n + j] * A[k * n + j];
+    if (!(d > 0.0)) return false;
+    d = sqrt(d);
+    A[k * n + k] = d;
+    for (int i = k + 1; i < n; ++i) {
+      double v = A[i * n + k];
+      for (int j = 0; j < k; ++j) v -= A[i * n + j] * A[k * n + j];
+      A[i * n + k] = v / d;
+    }
+  }
+  for (int i = 0; i < n; ++i) {
+    double v = b[i];
+    for (int j = 0; j < i; ++j) v -= A[i * n + j] * b[j];
+    b[i] = v / A[i * n + i];
+  }
+  for (int i = n - 1; i >= 0; --i) {
+    double v = b[i];
+    for (int j = i + 1; j < n; ++j) v -= A[j * n + i] * b[j];
+    b[i] = v / A[i * n + i];
+  }
+  return true;
+}
+
+// ---------------------------------------------------------------------------
+// job set-up
+// ---------------------------------------------------------------------------
+
+__global__ void __launch_bounds__(kThreads) k_nelec(Batch bt) {
+  __shared__ double red[kWarps];
+  int tile;
+  const JobDev& J = decode_local(bt, tile);
+  double acc = 0.0;
+  for (int i = 0; i < J.ppt; ++i) {
+    const int p = point_of(J, tile, i);
+    if (p < J.npoint) acc += J.w[p] * J.rho[p];
+  }
+  const double s = block_sum1(acc, red);
+  if (threadIdx.x == 0) J.jpart[(size_t)QJ_NELEC * J.ntile + tile] = s;
+}
+
+// Integrated density; basis schemes rescale the initial populations to it
+// (gisa.py:85-86).
+__global__ void k_init_params(Batch bt) {
+  int local;
+  const JobDev& J = decode_local(bt, local);
+  const double nelec = warp_tile_sum(J.jpart + (size_t)QJ_NELEC * J.ntile, J.ntile);
+  if ((threadIdx.x & 31) != 0) return;
+  J.mail->d[MD_NELEC] = nelec;
+  if (J.scheme != SCHEME_MBIS) {
+    double s = 0.0;
+    for (int i = 0; i < J.nparam; ++i) s += J.propars[i];
+    for (int i = 0; i < J.nparam; ++i) J.propars[i] = J.propars[i] / s * nelec;
+  }
+}
+
+__global__ void k_copy_old(Batch bt) {
+  int local;
+  const JobDev& J = decode_local(bt, local);
+  for (int i = threadIdx.x; i < J.nparam; i += blockDim.x) J.propars_old[i] = J.propars[i];
+}
+
+// ---------------------------------------------------------------------------
+// stockholder weights
+// ---------------------------------------------------------------------------
+
+template <typename T, int MODEL>
+__global__ void __launch_bounds__(kThreads) k_promol(Batch bt) {
+  int tile;
+  const JobDev& J = decode_local(bt, tile);
+  for (int i = 0; i < J.ppt; ++i) {
+    const int p = point_of(J, tile, i);
+    if (p >= J.npoint) continue;
+    double promol = 0.0;
+    for (int a = 0; a < J.natom; ++a) {
+      const T r = Dist<T>::r(J, p, a);
+      const double pro = (double)proatom<T, MODEL>(J, a, J.propars, r);
+      J.rhoa[(size_t)a * J.npoint + p] = pro;
+      promol += pro;
+      promol += 1e-100;
+    }
+    J.promol[p] = promol;
+  }
+}
+
+__global__ void __launch_bounds__(kThreads) k_atweights(Batch bt) {
+  __shared__ double red[kWarps * 2];
+  __shared__ double out[2];
+  const JobDev* Jp;
+  const AtomTile at = decode_atom_tile(bt, Jp);
+  const JobDev& J = *Jp;
+  double acc[2] = {0.0, 0.0};
+  double* ra = J.rhoa + (size_t)at.atom * J.npoint;
+  for (int i = 0; i < J.ppt; ++i) {
+    const int p = point_of(J, at.tile, i);
+    if (p >= J.npoint) continue;
+    const double promol = J.promol[p];
+    const double rho = J.rho[p];
+    const double aw = fmin(fmax(ra[p] / promol, 0.0), 1.0);
+    const double v = aw * rho;
+    ra[p] = v;
+    acc[0] += J.w[p] * v;
+    if (at.atom == 0) {
+      const bool sick = (promol < J.density_cutoff) || (rho < J.density_cutoff);
+      if (!sick) acc[1] += J.w[p] * rho * log(rho / promol);
+    }
+  }
+  block_sum<2>(acc, red, out);
+  if (threadIdx.x == 0) {
+    apart_ptr(J, at.atom, QA_POP)[at.tile] = out[0];
+    if (at.atom == 0) J.jpart[(size_t)QJ_ENTROPY * J.ntile + at.tile] = out[1];
+  }
+}
+
+// at_weights output: clip(pro_a / promol, 0, 1) into rhoa (use_old: the
+// parameters at the start of the last outer iteration).
+template <typename T, int MODEL>
+__global__ void __launch_bounds__(kThreads) k_final_atweights(Batch bt, int use_old) {
+  const JobDev* Jp;
+  const AtomTile at = decode_atom_tile(bt, Jp);
+  const JobDev& J = *Jp;
+  const double* par = use_old ? J.propars_old : J.propars;
+  for (int i = 0; i < J.ppt; ++i) {
+    const int p = point_of(J, at.tile, i);
+    if (p >= J.npoint) continue;
+    const T r = Dist<T>::r(J, p, at.atom);
+    const double pro = (double)proatom<T, MODEL>(J, at.atom, par, r);
+    J.rhoa[(size_t)at.atom * J.npoint + p] = fmin(fmax(pro / J.promol[p], 0.0), 1.0);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// outer change and end of an outer iteration
+// ---------------------------------------------------------------------------
+
+template <typename T, int MODEL>
+__global__ void __launch_bounds__(kThreads) k_change(Batch bt) {
+  __shared__ double red[kWarps];
+  const JobDev* Jp;
+  const AtomTile at = decode_atom_tile(bt, Jp);
+  const JobDev& J = *Jp;
+  double acc = 0.0;
+  for (int i = 0; i < J.ppt; ++i) {
+    const int p = point_of(J, at.tile, i);
+    if (p >= J.npoint) continue;
+    const T r = Dist<T>::r(J, p, at.atom);
+    const double d = (double)proatom<T, MODEL>(J, at.atom, J.propars, r) -
+                     (double)proatom<T, MODEL>(J, at.atom, J.propars_old, r);
+    acc += J.w[p] * d * d;
+  }
+  const double s = block_sum1(acc, red);
+  if (threadIdx.x == 0) apart_ptr(J, at.atom, QA_CHANGE)[at.tile] = s;
+}
+
+// One warp per job: change, entropy, charges (with_charges) and the
+// history row (core/iterstock.py:172-188).
+__global__ void k_outer_finish(Batch bt, int with_charges) {
+  int local;
+  const JobDev& J = decode_local(bt, local);
+  const int lane = threadIdx.x & 31;
+  double msd = 0.0;
+  for (int a = 0; a < J.natom; ++a) msd += warp_tile_sum(apart_ptr(J, a, QA_CHANGE), J.ntile);
+  const double ent = warp_tile_sum(J.jpart + (size_t)QJ_ENTROPY * J.ntile, J.ntile);
+  if (with_charges) {
+    for (int a = 0; a < J.natom; ++a) {
+      const double pop = warp_tile_sum(apart_ptr(J, a, QA_POP), J.ntile);
+      if (lane == 0) J.charges[a] = J.zpseudo[a] - pop;
+    }
+  }
+  __syncwarp();
+  const int it = J.mail->i[MI_ITER];
+  const double change = sqrt(msd);
+  if (it < J.maxiter) {
+    for (int i = lane; i < J.nparam; i += 32) J.hist_propars[(size_t)it * J.nparam + i] = J.propars[i];
+    if (with_charges)
+      for (int a = lane; a < J.natom; a += 32) J.hist_charges[(size_t)it * J.natom + a] = J.charges[a];
+  }
+  __syncwarp();
+  if (lane == 0) {
+    J.mail->d[MD_CHANGE] = change;
+    J.mail->d[MD_ENTROPY] = ent;
+    if (it < J.maxiter) {
+      J.hist_ent[it] = ent;
+      J.hist_chg[it] = change;
+    }
+    J.mail->i[MI_ITER] = it + 1;
+  }
+}
+
+// Charges from QA_POP (gLISA end, glisa.py:269-278).
+__global__ void k_charges(Batch bt) {
+  int local;
+  const JobDev& J = decode_local(bt, local);
+  for (int a = 0; a < J.natom; ++a) {
+    const double pop = warp_tile_sum(apart_ptr(J, a, QA_POP), J.ntile);
+    if ((threadIdx.x & 31) == 0) J.charges[a] = J.zpseudo[a] - pop;
+  }
+}
+
+__global__ void k_count_active(Batch bt) {
+  int local;
+  const JobDev& J = decode_local(bt, local);
+  const int lane = threadIdx.x & 31;
+  int c = 0;
+  for (int a = lane; a < J.natom; a += 32) c += J.active[a];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+  if (lane == 0) J.mail->i[MI_NACTIVE] = c;
+}
+
+__global__ void k_inner_init(Batch bt) {
+  int local;
+  const JobDev& J = decode_local(bt, local);
+  for (int i = threadIdx.x; i < J.nparam; i += blockDim.x) {
+    J.cur[i] = J.propars[i];
+    J.prev[i] = J.propars[i];
+  }
+  for (int a = threadIdx.x; a < J.natom; a += blockDim.x) {
+    J.active[a] = 1;
+    J.inner_it[a] = 0;
+  }
+  if (threadIdx.x == 0) {
+    J.mail->i[MI_NACTIVE] = J.natom;
+    J.mail->d[MD_INNER_TOTAL] = 0.0;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// MBIS inner fixed point (mbis.py:81-163)
+// ---------------------------------------------------------------------------
+
+constexpr int kMbisMaxShell = 7;            // get_nshell() <= 7 (mbis.py:36-46)
+constexpr int kMbisQ = 2 * kMbisMaxShell + 1;
+
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_mbis_inner(Batch bt) {
+  __shared__ double red[kWarps * kMbisQ];
+  __shared__ double out[kMbisQ];
+  const JobDev* Jp;
+  const AtomTile at = decode_atom_tile(bt, Jp);
+  const JobDev& J = *Jp;
+  if (!J.active[at.atom]) return;
+  const int nsh = J.shell_off[at.atom + 1] - J.shell_off[at.atom];
+  const double* pc = J.cur + J.par_off[at.atom];
+  const double* pp = J.prev + J.par_off[at.atom];
+  const bool first = J.inner_it[at.atom] == 0;
+  T cn[kMbisMaxShell], cs[kMbisMaxShell], pn[kMbisMaxShell], ps[kMbisMaxShell];
+#pragma unroll
+  for (int k = 0; k < kMbisMaxShell; ++k) {
+    const bool on = k < nsh;
+    cn[k] = on ? (T)pc[2 * k] : (T)0;
+    cs[k] = on ? (T)pc[2 * k + 1] : (T)0;
+    pn[k] = on ? (T)pp[2 * k] : (T)0;
+    ps[k] = on ? (T)pp[2 * k + 1] : (T)0;
+  }
+  double acc[kMbisQ];
+#pragma unroll
+  for (int q = 0; q < kMbisQ; ++q) acc[q] = 0.0;
+  const double* ra = J.rhoa + (size_t)at.atom * J.npoint;
+  for (int i = 0; i < J.ppt; ++i) {
+    const int p = point_of(J, at.tile, i);
+    if (p >= J.npoint) continue;
+    const T r = Dist<T>::r(J, p, at.atom);
+    T t[kMbisMaxShell];
+    T pro = (T)0, oldpro = (T)0;
+#pragma unroll
+    for (int k = 0; k < kMbisMaxShell; ++k) {
+      t[k] = (T)0;
+      if (k < nsh) {
+        t[k] = slater_shell<T>(cn[k], cs[k], r);
+        pro += t[k];
+        if (!first) oldpro += slater_shell<T>(pn[k], ps[k], r);
+      }
+    }
+    const double rho = ra[p];
+    const double w = J.w[p];
+    const bool sick = (rho < J.density_cutoff) || ((double)pro < J.density_cutoff);
+    const double ratio = sick ? 0.0 : rho / (double)pro;
+#pragma unroll
+    for (int k = 0; k < kMbisMaxShell; ++k) {
+      const double m0 = w * ((double)t[k] * ratio);
+      acc[2 * k] += m0;
+      acc[2 * k + 1] += m0 * (double)r;
+    }
+    const double e = (double)oldpro - (double)pro;
+    acc[kMbisQ - 1] += w * e * e;
+  }
+  block_sum<kMbisQ>(acc, red, out);
+  if (threadIdx.x < 2 * nsh) apart_ptr(J, at.atom, QA_INNER + threadIdx.x)[at.tile] = out[threadIdx.x];
+  if (threadIdx.x == 0) apart_ptr(J, at.atom, QA_INNER + kMbisQ - 1)[at.tile] = out[kMbisQ - 1];
+}
+
+// One warp per atom: N_k <- m0_k, S_k <- 3 m0_k / m1_k, convergence test.
+__global__ void k_mbis_update(Batch bt) {
+  int a;
+  const JobDev& J = decode_local(bt, a);
+  if (!J.active[a]) return;
+  const int lane = threadIdx.x & 31;
+  const int nsh = J.shell_off[a + 1] - J.shell_off[a];
+  double m[2 * kMbisMaxShell];
+  for (int q = 0; q < 2 * nsh; ++q) m[q] = warp_tile_sum(apart_ptr(J, a, QA_INNER + q), J.ntile);
+  const double chg2 = warp_tile_sum(apart_ptr(J, a, QA_INNER + kMbisQ - 1), J.ntile);
+  if (lane != 0) return;
+  const int it = J.inner_it[a];
+  const double change = (it == 0) ? 1e100 : sqrt(chg2);
+  double* pc = J.cur + J.par_off[a];
+  double* pp = J.prev + J.par_off[a];
+  double* pr = J.propars + J.par_off[a];
+  double nw[2 * kMbisMaxShell];
+  for (int k = 0; k < nsh; ++k) {
+    nw[2 * k] = m[2 * k];
+    nw[2 * k + 1] = 3.0 * m[2 * k] / m[2 * k + 1];
+  }
+  const bool conv = change < J.inner_threshold;
+  if (conv || it + 1 >= J.inner_maxiter) {
+    for (int q = 0; q < 2 * nsh; ++q) pr[q] = nw[q];
+    J.active[a] = 0;
+    J.atom_out[a * AO_COUNT + AO_INNER_CHANGE] = change;
+    atomicAdd(&J.mail->d[MD_INNER_TOTAL], (double)(it + 1));
+    if (!conv) atomicOr(&J.mail->i[MI_WARN], W_INNER);
+  } else {
+    for (int q = 0; q < 2 * nsh; ++q) {
+      pp[q] = pc[q];
+      pc[q] = nw[q];
+    }
+    J.inner_it[a] = it + 1;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// GISA (gisa.py:257-279, 348-421)
+// ---------------------------------------------------------------------------
+
+constexpr int kBasisQ = kMaxShells + 2;
+
+// q-vector moments sum_p w g_k rho_a (unit-population shells).
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_basis_qvec(Batch bt) {
+  __shared__ double red[kWarps * kMaxShells];
+  __shared__ double out[kMaxShells];
+  const JobDev* Jp;
+  const AtomTile at = decode_atom_tile(bt, Jp);
+  const JobDev& J = *Jp;
+  const int s0 = J.shell_off[at.atom];
+  const int nsh = J.shell_off[at.atom + 1] - s0;
+  double acc[kMaxShells];
+#pragma unroll
+  for (int q = 0; q < kMaxShells; ++q) acc[q] = 0.0;
+  const double* ra = J.rhoa + (size_t)at.atom * J.npoint;
+  for (int i = 0; i < J.ppt; ++i) {
+    const int p = point_of(J, at.tile, i);
+    if (p >= J.npoint) continue;
+    const T r = Dist<T>::r(J, p, at.atom);
+    const double wr = J.w[p] * ra[p];
+#pragma unroll
+    for (int k = 0; k < kMaxShells; ++k)
+      if (k < nsh) acc[k] += wr * (double)shell_value<T>(J, s0 + k, r);
+  }
+  block_sum<kMaxShells>(acc, red, out);
+  if (threadIdx.x < nsh) apart_ptr(J, at.atom, QA_INNER + threadIdx.x)[at.tile] = out[threadIdx.x];
+}
+
+// Exact primal active-set QP on the simplex {x >= 0, sum x = total}
+// (Nocedal & Wright, Algorithm 16.3), one thread. Solves
+//   min 1/2 x^T P x + q^T x.
+__device__ bool qp_simplex_nonneg(const double* P, const double* q, double total, int n,
+                                  double* x) {
+  bool work[kMaxShells];
+  double g[kMaxShells], p[kMaxShells];
+  double kkt[(kMaxShells + 1) * (kMaxShells + 1)];
+  double rhs[kMaxShells + 1];
+  int idx[kMaxShells];
+  for (int i = 0; i < n; ++i) {
+    x[i] = total / n;
+    work[i] = false;
+  }
+  for (int iter = 0; iter < 200; ++iter) {
+    int nf = 0;
+    for (int i = 0; i < n; ++i)
+      if (!work[i]) idx[nf++] = i;
+    for (int i = 0; i < n; ++i) {
+      double s = q[i];
+      for (int j = 0; j < n; ++j) s += P[i * n + j] * x[j];
+      g[i] = s;
+    }
+    const int m = nf + 1;
+    for (int r = 0; r < nf; ++r) {
+      for (int c = 0; c < nf; ++c) kkt[r * m + c] = P[idx[r] * n + idx[c]];
+      kkt[r * m + nf] = 1.0;
+      kkt[nf * m + r] = 1.0;
+      rhs[r] = -g[idx[r]];
+    }
+    kkt[nf * m + nf] = 0.0;
+    rhs[nf] = 0.0;
+    // Gaussian elimination with partial pivoting.
+    for (int c = 0; c < m; ++c) {
+      int piv = c;
+      double best = fabs(kkt[c * m + c]);
+      for (int r = c + 1; r < m; ++r)
+        if (fabs(kkt[r * m + c]) > best) {
+          best = fabs(kkt[r * m + c]);
+          piv = r;
+        }
+      if (best == 0.0) return false;
+      if (piv != c) {
+        for (int k = 0; k < m; ++k) {
+          const double t = kkt[c * m + k];
+          kkt[c * m + k] = kkt[piv * m + k];
+          kkt[piv * m + k] = t;
+        }
+        const double t = rhs[c];
+        rhs[c] = rhs[piv];
+        rhs[piv] = t;
+      }
+      for (int r = c + 1; r < m; ++r) {
+        const double f = kkt[r * m + c] / kkt[c * m + c];
+        if (f == 0.0) continue;
+        for (int k = c; k < m; ++k) kkt[r * m + k] -= f * kkt[c * m + k];
+        rhs[r] -= f * rhs[c];
+      }
+    }
+    for (int r = m - 1; r >= 0; --r) {
+      double v = rhs[r];
+      for (int k = r + 1; k < m; ++k) v -= kkt[r * m + k] * rhs[k];
+      rhs[r] = v / kkt[r * m + r];
+    }
+    for (int i = 0; i < n; ++i) p[i] = 0.0;
+    for (int r = 0; r < nf; ++r) p[idx[r]] = rhs[r];
+    const double lam = rhs[nf];
+    double pmax = 0.0, xmax = 1.0;
+    for (int i = 0; i < n; ++i) {
+      pmax = fmax(pmax, fabs(p[i]));
+      xmax = fmax(xmax, fabs(x[i]));
+    }
+    if (pmax <= 1e-14 * xmax) {
+      int jmin = -1;
+      double mumin = -1e-14;
+      for (int i = 0; i < n; ++i)
+        if (work[i]) {
+          const double mu = g[i] + lam;
+          if (mu < mumin) {
+            mumin = mu;
+            jmin = i;
+          }
+        }
+      if (jmin < 0) return true;
+      work[jmin] = false;
+      continue;
+    }
+    double alpha = 1.0;
+    int block = -1;
+    for (int i = 0; i < n; ++i)
+      if (!work[i] && p[i] < 0.0) {
+        const double a = -x[i] / p[i];
+        if (a < alpha) {
+          alpha = a;
+          block = i;
+        }
+      }
+    for (int i = 0; i < n; ++i) x[i] += alpha * p[i];
+    if (block >= 0) {
+      x[block] = 0.0;
+      work[block] = true;
+    }
+  }
+  return false;
+}
+
+// One warp per atom: P (twice the Gaussian overlap), q, QP.
+__global__ void k_gisa_qp(Batch bt) {
+  int a;
+  const JobDev& J = decode_local(bt, a);
+  const int lane = threadIdx.x & 31;
+  const int s0 = J.shell_off[a];
+  const int n = J.shell_off[a + 1] - s0;
+  double q[kMaxShells];
+  for (int k = 0; k < n; ++k) q[k] = -2.0 * warp_tile_sum(apart_ptr(J, a, QA_INNER + k), J.ntile);
+  const double pop = warp_tile_sum(apart_ptr(J, a, QA_POP), J.ntile);
+  if (lane != 0) return;
+  double P[kMaxShells * kMaxShells];
+  const double c = 2.0 / pow(3.14159265358979323846, 1.5);
+  for (int k = 0; k < n; ++k)
+    for (int l = 0; l < n; ++l) {
+      const double ak = J.sh_alpha[s0 + k], al = J.sh_alpha[s0 + l];
+      P[k * n + l] = c * pow(ak * al, 1.5) / pow(ak + al, 1.5);
+    }
+  for (int k = 0; k < n; ++k)
+    for (int l = 0; l < k; ++l) {
+      const double v = 0.5 * (P[k * n + l] + P[l * n + k]);
+      P[k * n + l] = v;
+      P[l * n + k] = v;
+    }
+  double x[kMaxShells];
+  if (!qp_simplex_nonneg(P, q, pop, n, x)) atomicOr(&J.mail->i[MI_ERR], E_QP);
+  double s = 0.0;
+  bool neg = false;
+  for (int k = 0; k < n; ++k) {
+    J.propars[J.par_off[a] + k] = x[k];
+    s += x[k];
+    neg |= x[k] < J.negative_cutoff;
+  }
+  if (fabs(s - pop) > J.population_cutoff) atomicOr(&J.mail->i[MI_WARN], W_POPULATION);
+  if (neg) atomicOr(&J.mail->i[MI_WARN], W_NEG_PARS);
+}
+
+// ---------------------------------------------------------------------------
+// aLISA self-consistent solver (alisa.py:193-291)
+// ---------------------------------------------------------------------------
+
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_lisa_sc_inner(Batch bt) {
+  constexpr int Q = kMaxShells + 1;
+  __shared__ double red[kWarps * Q];
+  __shared__ double out[Q];
+  const JobDev* Jp;
+  const AtomTile at = decode_atom_tile(bt, Jp);
+  const JobDev& J = *Jp;
+  if (!J.active[at.atom]) return;
+  const int s0 = J.shell_off[at.atom];
+  const int nsh = J.shell_off[at.atom + 1] - s0;
+  const double* pc = J.cur + J.par_off[at.atom];
+  const double* pp = J.prev + J.par_off[at.atom];
+  const bool first = J.inner_it[at.atom] == 0;
+  double acc[Q];
+#pragma unroll
+  for (int q = 0; q < Q; ++q) acc[q] = 0.0;
+  const double* ra = J.rhoa + (size_t)at.atom * J.npoint;
+  for (int i = 0; i < J.ppt; ++i) {
+    const int p = point_of(J, at.tile, i);
+    if (p >= J.npoint) continue;
+    const T r = Dist<T>::r(J, p, at.atom);
+    T g[kMaxShells];
+    T pro = (T)0, oldpro = (T)0;
+#pragma unroll
+    for (int k = 0; k < kMaxShells; ++k) {
+      g[k] = (T)0;
+      if (k < nsh) {
+        g[k] = shell_value<T>(J, s0 + k, r);
+        pro += g[k] * (T)pc[k];
+        if (!first) oldpro += g[k] * (T)pp[k];
+      }
+    }
+    const double rho = ra[p];
+    const double w = J.w[p];
+    const bool sick = (rho < J.density_cutoff) || ((double)pro < J.density_cutoff);
+    const double ratio = sick ? 0.0 : rho / (double)pro;
+#pragma unroll
+    for (int k = 0; k < kMaxShells; ++k)
+      if (k < nsh) acc[k] += w * ((double)g[k] * pc[k] * ratio);
+    const double e = (double)oldpro - (double)pro;
+    acc[Q - 1] += w * e * e;
+  }
+  block_sum<Q>(acc, red, out);
+  if (threadIdx.x < nsh) apart_ptr(J, at.atom, QA_INNER + threadIdx.x)[at.tile] = out[threadIdx.x];
+  if (threadIdx.x == 0) apart_ptr(J, at.atom, QA_INNER + Q - 1)[at.tile] = out[Q - 1];
+}
+
+__global__ void k_lisa_sc_update(Batch bt) {
+  constexpr int Q = kMaxShells + 1;
+  int a;
+  const JobDev& J = decode_local(bt, a);
+  if (!J.active[a]) return;
+  const int lane = threadIdx.x & 31;
+  const int nsh = J.shell_off[a + 1] - J.shell_off[a];
+  double m[kMaxShells];
+  for (int k = 0; k < nsh; ++k) m[k] = warp_tile_sum(apart_ptr(J, a, QA_INNER + k), J.ntile);
+  const double chg2 = warp_tile_sum(apart_ptr(J, a, QA_INNER + Q - 1), J.ntile);
+  const double pop = warp_tile_sum(apart_ptr(J, a, QA_POP), J.ntile);
+  if (lane != 0) return;
+  const int it = J.inner_it[a];
+  const double change = (it == 0) ? 1e100 : sqrt(chg2);
+  double* pc = J.cur + J.par_off[a];
+  double* pp = J.prev + J.par_off[a];
+  double* pr = J.propars + J.par_off[a];
+  const bool conv = change < J.inner_threshold;
+  if (conv || it + 1 >= J.inner_maxiter) {
+    double s = 0.0;
+    for (int k = 0; k < nsh; ++k) {
+      pr[k] = m[k];
+      s += m[k];
+    }
+    J.active[a] = 0;
+    J.atom_out[a * AO_COUNT + AO_INNER_CHANGE] = change;
+    atomicAdd(&J.mail->d[MD_INNER_TOTAL], (double)(it + 1));
+    if (!conv) atomicOr(&J.mail->i[MI_WARN], W_INNER);
+    else if (fabs(s - pop) > J.population_cutoff) atomicOr(&J.mail->i[MI_WARN], W_POPULATION);
+  } else {
+    for (int k = 0; k < nsh; ++k) {
+      pp[k] = pc[k];
+      pc[k] = m[k];
+    }
+    J.inner_it[a] = it + 1;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// aLISA Newton / modified Newton (alisa.py:753-938)
+// ---------------------------------------------------------------------------
+
+constexpr int kNtQ = kMaxShells + kMaxShells * (kMaxShells + 1) / 2 + 2;  // grad, hess, chg, neg
+constexpr int kStage = 256;  // points staged in shared memory per round
+
+// Partial gradient, Hessian, change and negativity count per (atom, tile).
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_lisa_newton_inner(Batch bt) {
+  __shared__ double gs[kMaxShells][kStage + 1];
+  __shared__ double f1[kStage], f2[kStage], fe[kStage], fn[kStage];
+  const JobDev* Jp;
+  const AtomTile at = decode_atom_tile(bt, Jp);
+  const JobDev& J = *Jp;
+  if (!J.active[at.atom]) return;
+  const int s0 = J.shell_off[at.atom];
+  const int nsh = J.shell_off[at.atom + 1] - s0;
+  const int nq = nsh + nsh * (nsh + 1) / 2;
+  const double* pc = J.cur + J.par_off[at.atom];
+  const double* pp = J.prev + J.par_off[at.atom];
+  const bool first = J.inner_it[at.atom] == 0;
+  const double* ra = J.rhoa + (size_t)at.atom * J.npoint;
+  // Output q owned by thread q: q < nsh -> grad_k; else Hessian entry (k,l), l <= k.
+  int qk = 0, ql = 0;
+  const int q = threadIdx.x;
+  if (q >= nsh && q < nq) {
+    int e = q - nsh, k = 0;
+    while (e > k) {
+      e -= k + 1;
+      ++k;
+    }
+    qk = k;
+    ql = e;
+  }
+  double acc = 0.0, acc_e = 0.0, acc_n = 0.0;
+  const int npts = J.tile_points;
+  for (int base = 0; base < npts; base += kStage) {
+    // stage kStage points: thread t handles point base + t
+    {
+      const int t = threadIdx.x;
+      const int p = at.tile * J.tile_points + base + t;
+      double v1 = 0.0, v2 = 0.0, ve = 0.0, vn = 0.0;
+      if (t < kStage && base + t < npts && p < J.npoint) {
+        const T r = Dist<T>::r(J, p, at.atom);
+        T pro = (T)0, oldpro = (T)0;
+        for (int k = 0; k < nsh; ++k) {
+          const T g = shell_value<T>(J, s0 + k, r);
+          gs[k][t] = (double)g;
+          pro += g * (T)pc[k];
+          if (!first) oldpro += g * (T)pp[k];
+        }
+        const double rho = ra[p];
+        const double w = J.w[p];
+        const bool sick = (rho < J.density_cutoff) || ((double)pro < J.density_cutoff);
+        const double ratio = sick ? 0.0 : rho / (double)pro;
+        v1 = w * ratio;
+        v2 = sick ? 0.0 : w * (ratio / (double)pro);
+        const double e = (double)oldpro - (double)pro;
+        ve = w * e * e;
+        vn = ((double)pro < J.negative_cutoff) ? 1.0 : 0.0;
+      } else if (t < kStage) {
+        for (int k = 0; k < nsh; ++k) gs[k][t] = 0.0;
+      }
+      if (t < kStage) {
+        f1[t] = v1;
+        f2[t] = v2;
+        fe[t] = ve;
+        fn[t] = vn;
+      }
+    }
+    __syncthreads();
+    if (q < nsh) {
+      for (int t = 0; t < kStage; ++t) acc += gs[q][t] * f1[t];
+    } else if (q < nq) {
+      for (int t = 0; t < kStage; ++t) acc += gs[qk][t] * gs[ql][t] * f2[t];
+    } else if (q == nq) {
+      for (int t = 0; t < kStage; ++t) acc_e += fe[t];
+    } else if (q == nq + 1) {
+      for (int t = 0; t < kStage; ++t) acc_n += fn[t];
+    }
+    __syncthreads();
+  }
+  if (q < nq) apart_ptr(J, at.atom, QA_INNER + q)[at.tile] = acc;
+  else if (q == nq) apart_ptr(J, at.atom, QA_INNER + nq)[at.tile] = acc_e;
+  else if (q == nq + 1) apart_ptr(J, at.atom, QA_INNER + nq + 1)[at.tile] = acc_n;
+}
+
+// One warp per atom: convergence test, Newton step (exact mode applies it).
+__global__ void k_lisa_newton_update(Batch bt) {
+  int a;
+  const JobDev& J = decode_local(bt, a);
+  if (!J.active[a]) return;
+  const int lane = threadIdx.x & 31;
+  const int nsh = J.shell_off[a + 1] - J.shell_off[a];
+  const int nq = nsh + nsh * (nsh + 1) / 2;
+  double v[kNtQ];
+  for (int q = 0; q < nq + 2; ++q) v[q] = warp_tile_sum(apart_ptr(J, a, QA_INNER + q), J.ntile);
+  const double pop = warp_tile_sum(apart_ptr(J, a, QA_POP), J.ntile);
+  if (lane != 0) return;
+  const int it = J.inner_it[a];
+  const double change = (it == 0) ? 1e100 : sqrt(v[nq]);
+  double* pc = J.cur + J.par_off[a];
+  double* pp = J.prev + J.par_off[a];
+  double* pr = J.propars + J.par_off[a];
+  double* dl = J.delta + J.par_off[a];
+  if (change < J.inner_threshold) {
+    // converged on the current parameters (alisa.py:881-892)
+    double s = 0.0;
+    for (int k = 0; k < nsh; ++k) {
+      pr[k] = pc[k];
+      s += pc[k];
+    }
+    J.active[a] = 0;
+    J.atom_out[a * AO_COUNT + AO_INNER_CHANGE] = change;
+    atomicAdd(&J.mail->d[MD_INNER_TOTAL], (double)(it + 1));
+    if (v[nq + 1] > 0.0) atomicOr(&J.mail->i[MI_ERR], E_NEG_DENSITY);
+    if (fabs(s - pop) > J.population_cutoff) atomicOr(&J.mail->i[MI_WARN], W_POPULATION);
+    return;
+  }
+  if (it + 1 >= J.inner_maxiter) {
+    J.active[a] = 0;
+    atomicOr(&J.mail->i[MI_ERR], E_INNER_NOT_CONV);
+    return;
+  }
+  double H[kMaxShells * kMaxShells], b[kMaxShells];
+  for (int k = 0; k < nsh; ++k) b[k] = -1.0 + v[k];  // -1 - df, df = -sum w g ratio
+  int e = nsh;
+  for (int k = 0; k < nsh; ++k)
+    for (int l = 0; l <= k; ++l) {
+      H[k * nsh + l] = v[e];
+      H[l * nsh + k] = v[e];
+      ++e;
+    }
+  if (!small_chol_solve(H, b, nsh)) {
+    J.active[a] = 0;
+    atomicOr(&J.mail->i[MI_ERR], E_SINGULAR);
+    return;
+  }
+  if (J.solver == SOLVER_NEWTON) {
+    for (int k = 0; k < nsh; ++k) {
+      pp[k] = pc[k];
+      pc[k] = pc[k] + b[k];
+    }
+    J.inner_it[a] = it + 1;
+  } else {
+    for (int k = 0; k < nsh; ++k) dl[k] = b[k];
+  }
+}
+
+// Line search (modified Newton): bit i set if trial x_i = linspace(tau, 0,
+// L)[i] gives a pro-atom <= negative_cutoff somewhere in the tile
+// (alisa.py:841-877).
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_lisa_ls(Batch bt) {
+  __shared__ int red[kWarps];
+  __shared__ double trial[32][kMaxShells];
+  const JobDev* Jp;
+  const AtomTile at = decode_atom_tile(bt, Jp);
+  const JobDev& J = *Jp;
+  if (!J.active[at.atom]) return;
+  const int s0 = J.shell_off[at.atom];
+  const int nsh = J.shell_off[at.atom + 1] - s0;
+  const int L = J.linspace_size < 32 ? J.linspace_size : 32;
+  const double* pc = J.cur + J.par_off[at.atom];
+  const double* dl = J.delta + J.par_off[at.atom];
+  for (int e = threadIdx.x; e < L * nsh; e += blockDim.x) {
+    const int i = e / nsh, k = e - i * nsh;
+    const double x = linspace_at(J.tau, 0.0, L, true, i);
+    trial[i][k] = pc[k] + x * dl[k];
+  }
+  __syncthreads();
+  int fail = 0;
+  for (int i = 0; i < J.ppt; ++i) {
+    const int p = point_of(J, at.tile, i);
+    if (p >= J.npoint) continue;
+    const T r = Dist<T>::r(J, p, at.atom);
+    double g[kMaxShells];
+    for (int k = 0; k < nsh; ++k) g[k] = (double)shell_value<T>(J, s0 + k, r);
+    for (int tr = 0; tr < L; ++tr) {
+      double v = 0.0;
+      for (int k = 0; k < nsh; ++k) v += g[k] * trial[tr][k];
+      if (!(v > J.negative_cutoff)) fail |= 1 << tr;
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) fail |= __shfl_xor_sync(0xffffffffu, fail, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = fail;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int f = 0;
+    for (int k = 0; k < kWarps; ++k) f |= red[k];
+    J.ls_fail[(size_t)at.atom * J.ntile + at.tile] = f;
+  }
+}
+
+__global__ void k_lisa_ls_pick(Batch bt) {
+  int a;
+  const JobDev& J = decode_local(bt, a);
+  if (!J.active[a]) return;
+  const int lane = threadIdx.x & 31;
+  int f = 0;
+  for (int t = lane; t < J.ntile; t += 32) f |= J.ls_fail[(size_t)a * J.ntile + t];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) f |= __shfl_xor_sync(0xffffffffu, f, o);
+  if (lane != 0) return;
+  const int L = J.linspace_size < 32 ? J.linspace_size : 32;
+  int pick = -1;
+  for (int i = 0; i < L; ++i)
+    if (!(f & (1 << i))) {
+      pick = i;
+      break;
+    }
+  const int nsh = J.shell_off[a + 1] - J.shell_off[a];
+  double* pc = J.cur + J.par_off[a];
+  double* pp = J.prev + J.par_off[a];
+  const double* dl = J.delta + J.par_off[a];
+  if (pick < 0) {
+    J.active[a] = 0;
+    atomicOr(&J.mail->i[MI_ERR], E_LINESEARCH);
+    return;
+  }
+  const double x = linspace_at(J.tau, 0.0, L, true, pick);
+  for (int k = 0; k < nsh; ++k) {
+    pp[k] = pc[k];
+    pc[k] = pc[k] + x * dl[k];
+  }
+  J.inner_it[a] += 1;
+}
+
+// ---------------------------------------------------------------------------
+// gLISA (glisa.py)
+// ---------------------------------------------------------------------------
+
+// G[m][p] = unit-population basis function m at point p (gisa.py:91-106 with
+// force_on_molgrid=True).
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_glisa_basis(Batch bt) {
+  int tile;
+  const JobDev& J = decode_local(bt, tile);
+  for (int i = 0; i < J.ppt; ++i) {
+    const int p = point_of(J, tile, i);
+    if (p >= J.npoint) continue;
+    for (int a = 0; a < J.natom; ++a) {
+      const T r = Dist<T>::r(J, p, a);
+      for (int s = J.shell_off[a]; s < J.shell_off[a + 1]; ++s)
+        J.gmat[(size_t)s * J.npoint + p] = (double)shell_value<T>(J, s, r);
+    }
+  }
+}
+
+// rho0 = G^T c (glisa.py:346-348); d1 = w rho/rho0, d2 = w rho/rho0^2 (0 where
+// sick); entropy and negativity partials (glisa.py:441-450, 784).
+__global__ void __launch_bounds__(kThreads) k_glisa_pro(Batch bt) {
+  __shared__ double red[kWarps * 2];
+  __shared__ double out[2];
+  int tile;
+  const JobDev& J = decode_local(bt, tile);
+  double acc[2] = {0.0, 0.0};
+  for (int i = 0; i < J.ppt; ++i) {
+    const int p = point_of(J, tile, i);
+    if (p >= J.npoint) continue;
+    double rho0 = 0.0;
+    for (int m = 0; m < J.nshell; ++m) rho0 += J.gmat[(size_t)m * J.npoint + p] * J.propars[m];
+    const double rho = J.rho[p];
+    const double w = J.w[p];
+    const bool sick = (rho < J.density_cutoff) || (rho0 < J.density_cutoff);
+    const double ratio = sick ? 0.0 : rho / rho0;
+    J.dvec1[p] = w * ratio;
+    J.dvec2[p] = sick ? 0.0 : w * (ratio / rho0);
+    if (!sick) acc[0] += w * rho * log(ratio);
+    if (rho0 < J.negative_cutoff) acc[1] += 1.0;
+  }
+  block_sum<2>(acc, red, out);
+  if (threadIdx.x == 0) {
+    J.jpart[(size_t)QJ_ENTROPY * J.ntile + tile] = out[0];
+    J.jpart[(size_t)QJ_NEG * J.ntile + tile] = out[1];
+  }
+}
+
+// gpart[m][tile] = sum_p G[m][p] d1[p]; one warp per row m.
+__global__ void __launch_bounds__(kThreads) k_glisa_grad(Batch bt) {
+  int tile;
+  const JobDev& J = decode_local(bt, tile);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int p0 = tile * J.tile_points;
+  const int p1 = min(p0 + J.tile_points, J.npoint);
+  for (int m = warp; m < J.nshell; m += kWarps) {
+    const double* g = J.gmat + (size_t)m * J.npoint;
+    double s = 0.0;
+    for (int p = p0 + lane; p < p1; p += 32) s += g[p] * J.dvec1[p];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) J.gpart[(size_t)m * J.ntile + tile] = s;
+  }
+}
+
+// Hessian partials: 64x64 tile (ti, tj), ti >= tj, over one point split.
+constexpr int kHT = 64;
+constexpr int kHK = 16;
+
+__global__ void __launch_bounds__(kThreads) k_glisa_hess(Batch bt) {
+  __shared__ double As[kHK][kHT + 1];
+  __shared__ double Bs[kHK][kHT + 1];
+  int local;
+  const JobDev& J = decode_local(bt, local);
+  const int npair = J.htiles * (J.htiles + 1) / 2;
+  const int split = local / npair;
+  int pr = local - split * npair;
+  int ti = 0;
+  while (pr > ti) {
+    pr -= ti + 1;
+    ++ti;
+  }
+  const int tj = pr;
+  const int i0 = ti * kHT, j0 = tj * kHT;
+  const int chunk = (J.npoint + J.nsplit - 1) / J.nsplit;
+  const int pbeg = split * chunk;
+  const int pend = min(pbeg + chunk, J.npoint);
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  double acc[4][4];
+#pragma unroll
+  for (int u = 0; u < 4; ++u)
+#pragma unroll
+    for (int v = 0; v < 4; ++v) acc[u][v] = 0.0;
+  for (int k0 = pbeg; k0 < pend; k0 += kHK) {
+    // load 64 rows x 16 points of each operand; thread -> (row, point) pairs
+    for (int e = threadIdx.x; e < kHT * kHK; e += kThreads) {
+      const int row = e / kHK, kk = e - row * kHK;
+      const int p = k0 + kk;
+      const int ia = i0 + row, jb = j0 + row;
+      double va = 0.0, vb = 0.0;
+      if (p < pend) {
+        if (ia < J.nshell) va = J.gmat[(size_t)ia * J.npoint + p] * J.dvec2[p];
+        if (jb < J.nshell) vb = J.gmat[(size_t)jb * J.npoint + p];
+      }
+      As[kk][row] = va;
+      Bs[kk][row] = vb;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < kHK; ++kk) {
+      double a[4], b[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) a[u] = As[kk][ty * 4 + u];
+#pragma unroll
+      for (int v = 0; v < 4; ++v) b[v] = Bs[kk][tx * 4 + v];
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int v = 0; v < 4; ++v) acc[u][v] += a[u] * b[v];
+    }
+    __syncthreads();
+  }
+  const int M = J.nshell;
+  double* out = J.hpart + (size_t)split * M * M;
+#pragma unroll
+  for (int u = 0; u < 4; ++u)
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      const int i = i0 + ty * 4 + u, j = j0 + tx * 4 + v;
+      if (i < M && j < M && i >= j) out[(size_t)i * M + j] = acc[u][v];
+    }
+}
+
+// Sum Hessian partials over splits (fixed order) into the lower triangle and
+// mirror; gradient rows from gpart.
+__global__ void __launch_bounds__(kThreads) k_glisa_reduce(Batch bt) {
+  int local;
+  const JobDev& J = decode_local(bt, local);
+  const int M = J.nshell;
+  const int e = local * kThreads + threadIdx.x;
+  if (e < M * M) {
+    const int i = e / M, j = e - i * M;
+    if (i >= j) {
+      double s = 0.0;
+      for (int sp = 0; sp < J.nsplit; ++sp) s += J.hpart[(size_t)sp * M * M + e];
+      J.hess[(size_t)i * M + j] = s;
+      J.hess[(size_t)j * M + i] = s;
+    }
+  }
+  if (e < M) {
+    double s = 0.0;
+    for (int t = 0; t < J.ntile; ++t) s += J.gpart[(size_t)e * J.ntile + t];
+    J.grad[e] = -s;  // df_i = -int rho g_i / rho0 (glisa.py:452-455)
+  }
+}
+
+// Newton step: Cholesky of H (one block per job), delta = H^-1 (-1 - df).
+__global__ void __launch_bounds__(kThreads) k_glisa_solve(Batch bt) {
+  __shared__ int bad;
+  int local;
+  const JobDev& J = decode_local(bt, local);
+  const int M = J.nshell;
+  double* L = J.chol;
+  for (int e = threadIdx.x; e < M * M; e += kThreads) L[e] = J.hess[e];
+  if (threadIdx.x == 0) bad = 0;
+  __syncthreads();
+  for (int k = 0; k < M; ++k) {
+    if (threadIdx.x == 0) {
+      const double d = L[(size_t)k * M + k];
+      if (!(d > 0.0)) bad = 1;
+      L[(size_t)k * M + k] = sqrt(fmax(d, 1e-300));
+    }
+    __syncthreads();
+    const double dkk = L[(size_t)k * M + k];
+    for (int i = k + 1 + threadIdx.x; i < M; i += kThreads) L[(size_t)i * M + k] /= dkk;
+    __syncthreads();
+    const int n = M - k - 1;
+    for (int e = threadIdx.x; e < n * n; e += kThreads) {
+      const int i = k + 1 + e / n, j = k + 1 + e % n;
+      if (j <= i) L[(size_t)i * M + j] -= L[(size_t)i * M + k] * L[(size_t)j * M + k];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    if (bad) atomicOr(&J.mail->i[MI_ERR], E_SINGULAR);
+    double* x = J.delta;
+    for (int i = 0; i < M; ++i) {
+      double v = -1.0 - J.grad[i];
+      for (int j = 0; j < i; ++j) v -= L[(size_t)i * M + j] * x[j];
+      x[i] = v / L[(size_t)i * M + i];
+    }
+    for (int i = M - 1; i >= 0; --i) {
+      double v = x[i];
+      for (int j = i + 1; j < M; ++j) v -= L[(size_t)j * M + i] * x[j];
+      x[i] = v / L[(size_t)i * M + i];
+    }
+  }
+}
+
+// Line-search mask (glisa.py:688-699 with utils.py:556-577): per atom, the
+// most diffuse shells with |c| < 1e-4 and a negative step stay fixed.
+__global__ void k_glisa_keep(Batch bt) {
+  int a;
+  const JobDev& J = decode_local(bt, a);
+  if ((threadIdx.x & 31) != 0) return;
+  const int s0 = J.shell_off[a];
+  const int n = J.shell_off[a + 1] - s0;
+  int order[kMaxShells];
+  for (int k = 0; k < n; ++k) order[k] = k;
+  // stable insertion sort by exponent (numpy argsort default is not stable,
+  // but exponents within an atom are distinct)
+  for (int k = 1; k < n; ++k) {
+    const int v = order[k];
+    int j = k - 1;
+    while (j >= 0 && J.sh_alpha[s0 + order[j]] > J.sh_alpha[s0 + v]) {
+      order[j + 1] = order[j];
+      --j;
+    }
+    order[j + 1] = v;
+  }
+  for (int k = 0; k < n; ++k) J.keep[s0 + k] = 1.0;
+  for (int k = 0; k < n; ++k) {
+    const int m = s0 + order[k];
+    if (fabs(J.propars[m]) < 1e-4 && J.delta[m] < 0.0) J.keep[m] = 0.0;
+    else break;
+  }
+}
+
+// Validity of trial steps x_i = linspace(tau, 0, L, endpoint=False)[first + i]
+// for i < count (<= 64): bit set if some pro-atom of this atom is below
+// negative_cutoff in the tile (glisa.py:283-307).
+__global__ void __launch_bounds__(kThreads) k_glisa_ls(Batch bt, int first, int count) {
+  __shared__ unsigned long long red[kWarps];
+  const JobDev* Jp;
+  const AtomTile at = decode_atom_tile(bt, Jp);
+  const JobDev& J = *Jp;
+  const int s0 = J.shell_off[at.atom];
+  const int nsh = J.shell_off[at.atom + 1] - s0;
+  unsigned long long fail = 0ull;
+  for (int i = 0; i < J.ppt; ++i) {
+    const int p = point_of(J, at.tile, i);
+    if (p >= J.npoint) continue;
+    for (int tr = 0; tr < count; ++tr) {
+      const double x = linspace_at(J.tau, 0.0, J.linspace_size, false, first + tr);
+      double v = 0.0;
+      for (int k = 0; k < nsh; ++k) {
+        const int m = s0 + k;
+        const double c = J.propars[m] + J.keep[m] * (x * J.delta[m]);
+        v += c * J.gmat[(size_t)m * J.npoint + p];
+      }
+      if (v < J.negative_cutoff) fail |= 1ull << tr;
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) fail |= __shfl_xor_sync(0xffffffffu, fail, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = fail;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned long long f = 0ull;
+    for (int k = 0; k < kWarps; ++k) f |= red[k];
+    reinterpret_cast<unsigned long long*>(J.ls_fail)[(size_t)at.atom * J.ntile + at.tile] = f;
+  }
+}
+
+// Pick the first valid trial among [first, first+count) and apply it; sets
+// MD_LS_X = -1 if none is valid.
+__global__ void k_glisa_ls_pick(Batch bt, int first, int count) {
+  int local;
+  const JobDev& J = decode_local(bt, local);
+  const int lane = threadIdx.x & 31;
+  const unsigned long long* lf = reinterpret_cast<const unsigned long long*>(J.ls_fail);
+  unsigned long long f = 0ull;
+  for (int e = lane; e < J.natom * J.ntile; e += 32) f |= lf[e];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) f |= __shfl_xor_sync(0xffffffffu, f, o);
+  __shared__ int pick;
+  if (lane == 0) {
+    pick = -1;
+    for (int i = 0; i < count; ++i)
+      if (!(f & (1ull << i))) {
+        pick = first + i;
+        break;
+      }
+  }
+  __syncwarp();
+  if (pick < 0) {
+    if (lane == 0) J.mail->d[MD_LS_X] = -1.0;
+    return;
+  }
+  const double x = linspace_at(J.tau, 0.0, J.linspace_size, false, pick);
+  for (int m = lane; m < J.nshell; m += 32) J.propars[m] = J.propars[m] + J.keep[m] * (x * J.delta[m]);
+  if (lane == 0) J.mail->d[MD_LS_X] = x;
+}
+
+// Exact Newton: propars += delta. SC: c_m <- c_m int rho g_m / rho0.
+__global__ void k_glisa_apply(Batch bt, int mode) {
+  int local;
+  const JobDev& J = decode_local(bt, local);
+  for (int m = threadIdx.x; m < J.nshell; m += blockDim.x) {
+    if (mode == 0) J.propars[m] = J.propars[m] + J.delta[m];
+    else J.propars[m] = J.propars[m] * (-J.grad[m]);
+  }
+}
+
+// Change from stored basis values (glisa.py:776 via compute_change).
+__global__ void __launch_bounds__(kThreads) k_glisa_change(Batch bt) {
+  __shared__ double red[kWarps];
+  const JobDev* Jp;
+  const AtomTile at = decode_atom_tile(bt, Jp);
+  const JobDev& J = *Jp;
+  const int s0 = J.shell_off[at.atom], s1 = J.shell_off[at.atom + 1];
+  double acc = 0.0;
+  for (int i = 0; i < J.ppt; ++i) {
+    const int p = point_of(J, at.tile, i);
+    if (p >= J.npoint) continue;
+    double r1 = 0.0, r2 = 0.0;
+    for (int m = s0; m < s1; ++m) {
+      const double g = J.gmat[(size_t)m * J.npoint + p];
+      r1 += J.propars[m] * g;
+      r2 += J.propars_old[m] * g;
+    }
+    const double d = r1 - r2;
+    acc += J.w[p] * d * d;
+  }
+  const double s = block_sum1(acc, red);
+  if (threadIdx.x == 0) apart_ptr(J, at.atom, QA_CHANGE)[at.tile] = s;
+}
+
+// gLISA convergence bookkeeping: negativity of the promolecule used in the
+// last iteration and the population check (glisa.py:786-798).
+__global__ void k_glisa_check(Batch bt) {
+  int local;
+  const JobDev& J = decode_local(bt, local);
+  const double neg = warp_tile_sum(J.jpart + (size_t)QJ_NEG * J.ntile, J.ntile);
+  if ((threadIdx.x & 31) != 0) return;
+  if (neg > 0.0) atomicOr(&J.mail->i[MI_ERR], E_NEG_DENSITY);
+  double s = 0.0;
+  for (int m = 0; m < J.nshell; ++m) s += J.propars[m];
+  if (fabs(s - J.mail->d[MD_NELEC]) > J.population_cutoff) atomicOr(&J.mail->i[MI_WARN], W_POPULATION);
+}
+
+// ---------------------------------------------------------------------------
+// launchers
+// ---------------------------------------------------------------------------
+
+long long g_launch_count = 0;  // kernel launches issued by this library (host counter)
+
+#define HP_LAUNCH(kernel, kind, threads, ...)                                          \
+  do {                                                                                 \
+    if (hb.blocks[kind] > 0) {                                                         \
+      kernel<<<hb.blocks[kind], threads, 0, st>>>(hb.b[kind], ##__VA_ARGS__);          \
+      ++g_launch_count;                                                                \
+    }                                                                                  \
+  } while (0)
+
+void launch_nelec(const HostBatch& hb, cudaStream_t st) {
+  HP_LAUNCH(k_nelec, K_POINT, kThreads);
+  HP_LAUNCH(k_init_params, K_JOB, 32);
+}
+
+void launch_copy_old(const HostBatch& hb, cudaStream_t st) { HP_LAUNCH(k_copy_old, K_JOB, 128); }
+
+void launch_promol(const HostBatch& hb, cudaStream_t st, int mixed, int model) {
+  if (mixed) {
+    if (model == MODEL_MBIS) HP_LAUNCH((k_promol<float, MODEL_MBIS>), K_POINT, kThreads);
+    else HP_LAUNCH((k_promol<float, MODEL_BASIS>), K_POINT, kThreads);
+  } else {
+    if (model == MODEL_MBIS) HP_LAUNCH((k_promol<double, MODEL_MBIS>), K_POINT, kThreads);
+    else HP_LAUNCH((k_promol<double, MODEL_BASIS>), K_POINT, kThreads);
+  }
+  HP_LAUNCH(k_atweights, K_ATOM_TILE, kThreads);
+}
+
+void launch_final_atweights(const HostBatch& hb, cudaStream_t st, int mixed, int model,
+                            int use_old) {
+  if (mixed) {
+    if (model == MODEL_MBIS) HP_LAUNCH((k_final_atweights<float, MODEL_MBIS>), K_ATOM_TILE, kThreads, use_old);
+    else HP_LAUNCH((k_final_atweights<float, MODEL_BASIS>), K_ATOM_TILE, kThreads, use_old);
+  } else {
+    if (model == MODEL_MBIS) HP_LAUNCH((k_final_atweights<double, MODEL_MBIS>), K_ATOM_TILE, kThreads, use_old);
+    else HP_LAUNCH((k_final_atweights<double, MODEL_BASIS>), K_ATOM_TILE, kThreads, use_old);
+  }
+}
+
+void launch_change(const HostBatch& hb, cudaStream_t st, int mixed, int model) {
+  if (mixed) {
+    if (model == MODEL_MBIS) HP_LAUNCH((k_change<float, MODEL_MBIS>), K_ATOM_TILE, kThreads);
+    else HP_LAUNCH((k_change<float, MODEL_BASIS>), K_ATOM_TILE, kThreads);
+  } else {
+    if (model == MODEL_MBIS) HP_LAUNCH((k_change<double, MODEL_MBIS>), K_ATOM_TILE, kThreads);
+    else HP_LAUNCH((k_change<double, MODEL_BASIS>), K_ATOM_TILE, kThreads);
+  }
+}
+
+void launch_outer_finish(const HostBatch& hb, cudaStream_t st, int with_charges) {
+  HP_LAUNCH(k_outer_finish, K_JOB, 32, with_charges);
+}
+
+void launch_charges(const HostBatch& hb, cudaStream_t st) { HP_LAUNCH(k_charges, K_JOB, 32); }
+
+void launch_inner_init(const HostBatch& hb, cudaStream_t st) { HP_LAUNCH(k_inner_init, K_JOB, 128); }
+
+void launch_count_active(const HostBatch& hb, cudaStream_t st) {
+  HP_LAUNCH(k_count_active, K_JOB, 32);
+}
+
+void launch_mbis_inner(const HostBatch& hb, cudaStream_t st, int mixed) {
+  if (mixed) HP_LAUNCH(k_mbis_inner<float>, K_ATOM_TILE, kThreads);
+  else HP_LAUNCH(k_mbis_inner<double>, K_ATOM_TILE, kThreads);
+  HP_LAUNCH(k_mbis_update, K_ATOM, 32);
+}
+
+void launch_gisa(const HostBatch& hb, cudaStream_t st, int mixed) {
+  if (mixed) HP_LAUNCH(k_basis_qvec<float>, K_ATOM_TILE, kThreads);
+  else HP_LAUNCH(k_basis_qvec<double>, K_ATOM_TILE, kThreads);
+  HP_LAUNCH(k_gisa_qp, K_ATOM, 32);
+}
+
+void launch_lisa_sc_inner(const HostBatch& hb, cudaStream_t st, int mixed) {
+  if (mixed) HP_LAUNCH(k_lisa_sc_inner<float>, K_ATOM_TILE, kThreads);
+  else HP_LAUNCH(k_lisa_sc_inner<double>, K_ATOM_TILE, kThreads);
+  HP_LAUNCH(k_lisa_sc_update, K_ATOM, 32);
+}
+
+void launch_lisa_newton_inner(const HostBatch& hb, cudaStream_t st, int mixed, int modified) {
+  if (mixed) HP_LAUNCH(k_lisa_newton_inner<float>, K_ATOM_TILE, kThreads);
+  else HP_LAUNCH(k_lisa_newton_inner<double>, K_ATOM_TILE, kThreads);
+  HP_LAUNCH(k_lisa_newton_update, K_ATOM, 32);
+  if (modified) {
+    if (mixed) HP_LAUNCH(k_lisa_ls<float>, K_ATOM_TILE, kThreads);
+    else HP_LAUNCH(k_lisa_ls<double>, K_ATOM_TILE, kThreads);
+    HP_LAUNCH(k_lisa_ls_pick, K_ATOM, 32);
+  }
+}
+
+void launch_glisa_basis(const HostBatch& hb, cudaStream_t st) {
+  HP_LAUNCH(k_glisa_basis<double>, K_POINT, kThreads);
+}
+
+void launch_glisa_pro(const HostBatch& hb, cudaStream_t st) { HP_LAUNCH(k_glisa_pro, K_POINT, kThreads); }
+void launch_glisa_grad(const HostBatch& hb, cudaStream_t st) { HP_LAUNCH(k_glisa_grad, K_POINT, kThreads); }
+void launch_glisa_hess(const HostBatch& hb, cudaStream_t st) { HP_LAUNCH(k_glisa_hess, K_HESS, kThreads); }
+void launch_glisa_reduce(const HostBatch& hb, cudaStream_t st) {
+  HP_LAUNCH(k_glisa_reduce, K_SQUARE, kThreads);
+}
+
+void launch_glisa_solve(const HostBatch& hb, cudaStream_t st) {
+  HP_LAUNCH(k_glisa_solve, K_JOB, kThreads);
+}
+
+void launch_glisa_apply(const HostBatch& hb, cudaStream_t st, int mode) {
+  HP_LAUNCH(k_glisa_apply, K_JOB, 128, mode);
+}
+
+void launch_glisa_keep(const HostBatch& hb, cudaStream_t st) { HP_LAUNCH(k_glisa_keep, K_ATOM, 32); }
+
+void launch_glisa_ls(const HostBatch& hb, cudaStream_t st, int first, int count) {
+  HP_LAUNCH(k_glisa_ls, K_ATOM_TILE, kThreads, first, count);
+  HP_LAUNCH(k_glisa_ls_pick, K_JOB, 32, first, count);
+}
+
+void launch_glisa_change(const HostBatch& hb, cudaStream_t st) {
+  HP_LAUNCH(k_glisa_change, K_ATOM_TILE, kThreads);
+}
+
+void launch_glisa_check(const HostBatch& hb, cudaStream_t st) { HP_LAUNCH(k_glisa_check, K_JOB, 32); }
+
+}  // namespace hp

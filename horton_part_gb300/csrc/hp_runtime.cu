@@ -1,0 +1,915 @@
+// Host runtime of libhpgpu.so: contexts, jobs, the batched outer-iteration
+// driver and the C ABI declared in include/hpgpu.h.
+//
+// The outer loop mirrors AbstractISAWPart.do_partitioning
+// (core/iterstock.py:159-193) for MBIS/GISA/aLISA and the gLISA solver loops
+// (glisa.py:617-848); each call of hp_step advances every live job of a batch
+// by one outer iteration with batched kernel launches on the context stream
+// and a single host wait at the end (plus one per inner-solver chunk).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "hp_internal.cuh"
+#include "hpgpu.h"
+
+using namespace hp;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const std::string& msg) {
+  g_err = msg;
+  return code;
+}
+
+#define HP_CK(call)                                                                   \
+  do {                                                                                \
+    cudaError_t e_ = (call);                                                          \
+    if (e_ != cudaSuccess)                                                            \
+      return fail(HP_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));   \
+  } while (0)
+
+constexpr int kMaxSlots = 4096;
+constexpr size_t kAlign = 256;
+
+size_t align_up(size_t x) { return (x + kAlign - 1) / kAlign * kAlign; }
+
+}  // namespace
+
+struct hp_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  size_t budget = 0, used = 0;
+  Mailbox* mail_dev = nullptr;
+  Mailbox* mail_host = nullptr;
+  std::vector<hp_job*> slots;
+  JobDev* batch_dev = nullptr;     // JobDev array of the current batch
+  JobDev* batch_host = nullptr;    // pinned staging
+  int* prefix_dev = nullptr;       // [K_NKIND][kMaxSlots + 1]
+  int* prefix_host = nullptr;      // pinned staging
+  // kernel timing (hp_ctx_profile)
+  bool prof = false;
+  struct Pending {
+    int fam;
+    cudaEvent_t a, b;
+  };
+  std::vector<Pending> pending;
+  std::vector<cudaEvent_t> event_pool;
+  double prof_ms[HP_KERNEL_COUNT] = {};
+  int64_t prof_n[HP_KERNEL_COUNT] = {};
+  long long launch_base = 0;
+};
+
+struct hp_job {
+  hp_ctx* ctx = nullptr;
+  int slot = -1;
+  hp_job_desc desc{};
+  JobDev dev{};
+  void* mem = nullptr;
+  size_t bytes = 0;
+  // host-side state
+  bool initialized = false;
+  bool done = false;
+  int status = HP_OK;
+  int niter = 0;
+  double change = 0.0;
+  uint32_t warnings = 0;
+  int last_inner = 4;
+  double evals = 0.0;
+  double inner_total = 0.0;
+  bool converged = false;
+};
+
+namespace {
+
+cudaEvent_t take_event(hp_ctx* ctx) {
+  if (!ctx->event_pool.empty()) {
+    cudaEvent_t e = ctx->event_pool.back();
+    ctx->event_pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e = nullptr;
+  cudaEventCreate(&e);
+  return e;
+}
+
+// Records CUDA events around the launches of one kernel family.
+struct ProfScope {
+  hp_ctx* ctx;
+  int fam;
+  cudaEvent_t a = nullptr;
+  ProfScope(hp_ctx* c, int f) : ctx(c), fam(f) {
+    if (ctx->prof) {
+      a = take_event(ctx);
+      cudaEventRecord(a, ctx->stream);
+    }
+  }
+  ~ProfScope() {
+    if (a) {
+      cudaEvent_t b = take_event(ctx);
+      cudaEventRecord(b, ctx->stream);
+      ctx->pending.push_back({fam, a, b});
+    }
+  }
+};
+
+// After a stream synchronisation: fold finished event pairs into the totals.
+void prof_collect(hp_ctx* ctx) {
+  for (auto& p : ctx->pending) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, p.a, p.b) == cudaSuccess) {
+      ctx->prof_ms[p.fam] += ms;
+      ctx->prof_n[p.fam] += 1;
+    }
+    ctx->event_pool.push_back(p.a);
+    ctx->event_pool.push_back(p.b);
+  }
+  ctx->pending.clear();
+}
+
+int blocks_for(const JobDev& J, int kind) {
+  switch (kind) {
+    case K_POINT: return J.ntile;
+    case K_ATOM_TILE: return J.natom * J.ntile;
+    case K_ATOM: return J.natom;
+    case K_JOB: return 1;
+    case K_HESS: return J.scheme == SCHEME_GLISA ? J.nsplit * J.htiles * (J.htiles + 1) / 2 : 0;
+    case K_SQUARE: return J.scheme == SCHEME_GLISA ? (J.nshell * J.nshell + kThreads - 1) / kThreads : 0;
+  }
+  return 0;
+}
+
+// Upload the batch description (JobDev copies and per-kind block prefixes).
+int build_batch(hp_ctx* ctx, const std::vector<hp_job*>& jobs, HostBatch& hb) {
+  const int n = (int)jobs.size();
+  for (int j = 0; j < n; ++j) ctx->batch_host[j] = jobs[j]->dev;
+  HP_CK(cudaMemcpyAsync(ctx->batch_dev, ctx->batch_host, sizeof(JobDev) * n,
+                        cudaMemcpyHostToDevice, ctx->stream));
+  for (int k = 0; k < K_NKIND; ++k) {
+    int* pre = ctx->prefix_host + (size_t)k * (kMaxSlots + 1);
+    pre[0] = 0;
+    for (int j = 0; j < n; ++j) pre[j + 1] = pre[j] + blocks_for(jobs[j]->dev, k);
+    hb.blocks[k] = pre[n];
+    hb.b[k].jobs = ctx->batch_dev;
+    hb.b[k].prefix = ctx->prefix_dev + (size_t)k * (kMaxSlots + 1);
+    hb.b[k].njobs = n;
+  }
+  HP_CK(cudaMemcpyAsync(ctx->prefix_dev, ctx->prefix_host,
+                        sizeof(int) * K_NKIND * (kMaxSlots + 1), cudaMemcpyHostToDevice,
+                        ctx->stream));
+  return HP_OK;
+}
+
+int read_mail(hp_ctx* ctx) {
+  HP_CK(cudaMemcpyAsync(ctx->mail_host, ctx->mail_dev, sizeof(Mailbox) * kMaxSlots,
+                        cudaMemcpyDeviceToHost, ctx->stream));
+  HP_CK(cudaStreamSynchronize(ctx->stream));
+  prof_collect(ctx);
+  return HP_OK;
+}
+
+int check_launch() {
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return fail(HP_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e));
+  return HP_OK;
+}
+
+int model_of(const hp_job* j) { return j->desc.scheme == HP_SCHEME_MBIS ? MODEL_MBIS : MODEL_BASIS; }
+
+// Map device error bits to a status.
+int status_of(int err) {
+  if (err == 0) return HP_OK;
+  if (err & E_INNER_NOT_CONV) return HP_ERR_NOT_CONVERGED;
+  return HP_ERR_NUMERIC;
+}
+
+const char* err_text(int err) {
+  if (err & E_NEG_DENSITY) return "Negative pro-atom density found!";
+  if (err & E_SINGULAR) return "Hessian is not positive definite (singular Newton system)";
+  if (err & E_LINESEARCH) return "Line search failed!";
+  if (err & E_INNER_NOT_CONV) return "Inner loop: Newton does not converge!";
+  if (err & E_QP) return "GISA quadratic program did not converge";
+  return "numerical failure";
+}
+
+// Inner-solver loop for a batch: launch chunks of inner iterations until no
+// atom of any job is active.
+template <typename F>
+int run_inner(hp_ctx* ctx, const std::vector<hp_job*>& jobs, const HostBatch& hb, F launch_one,
+              int max_launch) {
+  launch_inner_init(hb, ctx->stream);
+  int chunk = 1;
+  for (hp_job* j : jobs) chunk = std::max(chunk, j->last_inner);
+  int launched = 0;
+  while (true) {
+    for (int c = 0; c < chunk && launched < max_launch; ++c, ++launched) launch_one();
+    launch_count_active(hb, ctx->stream);
+    int rc = check_launch();
+    if (rc) return rc;
+    rc = read_mail(ctx);
+    if (rc) return rc;
+    int nact = 0;
+    for (hp_job* j : jobs) nact += ctx->mail_host[j->slot].i[MI_NACTIVE];
+    if (nact == 0) break;
+    if (launched >= max_launch) break;
+    chunk = 2;
+  }
+  for (hp_job* j : jobs) j->last_inner = std::max(1, std::min(launched, 64));
+  return HP_OK;
+}
+
+int job_init(hp_ctx* ctx, const std::vector<hp_job*>& jobs, const HostBatch& hb) {
+  launch_nelec(hb, ctx->stream);
+  bool any_glisa = false;
+  for (hp_job* j : jobs) any_glisa |= j->desc.scheme == HP_SCHEME_GLISA;
+  if (any_glisa) launch_glisa_basis(hb, ctx->stream);
+  for (hp_job* j : jobs) j->initialized = true;
+  return check_launch();
+}
+
+// One outer iteration of MBIS / GISA / aLISA for a homogeneous batch.
+int step_iterstock(hp_ctx* ctx, const std::vector<hp_job*>& jobs, const HostBatch& hb) {
+  const hp_job* j0 = jobs[0];
+  const int mixed = j0->desc.precision == HP_PRECISION_MIXED;
+  const int model = model_of(j0);
+  cudaStream_t st = ctx->stream;
+  launch_copy_old(hb, st);
+  {
+    ProfScope ps(ctx, HP_KERNEL_PROMOL);
+    launch_promol(hb, st, mixed, model);
+  }
+  int rc = HP_OK;
+  switch (j0->desc.scheme) {
+    case HP_SCHEME_MBIS:
+      rc = run_inner(ctx, jobs, hb, [&] {
+        ProfScope ps(ctx, HP_KERNEL_INNER);
+        launch_mbis_inner(hb, st, mixed);
+      }, j0->dev.inner_maxiter + 1);
+      break;
+    case HP_SCHEME_GISA: {
+      ProfScope ps(ctx, HP_KERNEL_INNER);
+      launch_gisa(hb, st, mixed);
+      break;
+    }
+    case HP_SCHEME_LISA:
+      if (j0->dev.solver == SOLVER_SC)
+        rc = run_inner(ctx, jobs, hb, [&] {
+          ProfScope ps(ctx, HP_KERNEL_INNER);
+          launch_lisa_sc_inner(hb, st, mixed);
+        }, j0->dev.inner_maxiter + 1);
+      else
+        rc = run_inner(ctx, jobs, hb, [&] {
+          ProfScope ps(ctx, HP_KERNEL_INNER);
+          launch_lisa_newton_inner(hb, st, mixed, j0->dev.solver == SOLVER_M_NEWTON);
+        }, j0->dev.inner_maxiter + 1);
+      break;
+  }
+  if (rc) return rc;
+  {
+    ProfScope ps(ctx, HP_KERNEL_CHANGE);
+    launch_change(hb, st, mixed, model);
+  }
+  launch_outer_finish(hb, st, 1);
+  rc = check_launch();
+  if (rc) return rc;
+  rc = read_mail(ctx);
+  if (rc) return rc;
+  for (hp_job* j : jobs) {
+    const Mailbox& m = ctx->mail_host[j->slot];
+    j->niter = m.i[MI_ITER];
+    j->change = m.d[MD_CHANGE];
+    j->warnings |= (uint32_t)m.i[MI_WARN];
+    const double inner = m.d[MD_INNER_TOTAL];
+    j->inner_total += inner;
+    // point-atom evaluations in the reference's convention: weights pass,
+    // one per inner iteration, two in compute_change (GISA: one q-vector pass)
+    const double n = (double)j->dev.npoint;
+    const double a = (double)j->dev.natom;
+    const double inner_evals = j->desc.scheme == HP_SCHEME_GISA ? a : inner;
+    j->evals += n * (3.0 * a + inner_evals);
+    if (m.i[MI_ERR]) {
+      j->status = status_of(m.i[MI_ERR]);
+      g_err = err_text(m.i[MI_ERR]);
+      j->done = true;
+    } else if (j->change < j->desc.threshold || j->niter >= j->desc.maxiter) {
+      j->converged = j->change < j->desc.threshold;
+      j->done = true;
+    }
+  }
+  return HP_OK;
+}
+
+// One gLISA solver iteration (glisa.py:748-798 for Newton, 805-848 for SC).
+int step_glisa(hp_ctx* ctx, const std::vector<hp_job*>& jobs, const HostBatch& hb) {
+  cudaStream_t st = ctx->stream;
+  const int solver = jobs[0]->dev.solver;
+  launch_copy_old(hb, st);
+  {
+    ProfScope ps(ctx, HP_KERNEL_GLISA_PRO);
+    launch_glisa_pro(hb, st);
+  }
+  {
+    ProfScope ps(ctx, HP_KERNEL_GLISA_GRAD);
+    launch_glisa_grad(hb, st);
+  }
+  if (solver != SOLVER_SC) {
+    ProfScope ps(ctx, HP_KERNEL_GLISA_HESS);
+    launch_glisa_hess(hb, st);
+  }
+  {
+    ProfScope ps(ctx, HP_KERNEL_GLISA_SOLVE);
+    launch_glisa_reduce(hb, st);
+    if (solver == SOLVER_SC) {
+      launch_glisa_apply(hb, st, 1);
+    } else {
+      launch_glisa_solve(hb, st);
+      if (solver == SOLVER_NEWTON) launch_glisa_apply(hb, st, 0);
+      else {
+        launch_glisa_keep(hb, st);
+        launch_glisa_ls(hb, st, 0, 1);
+      }
+    }
+  }
+  if (solver == SOLVER_M_NEWTON) {
+    {
+      int rc = check_launch();
+      if (rc) return rc;
+      rc = read_mail(ctx);
+      if (rc) return rc;
+      bool retry = false;
+      for (hp_job* j : jobs) retry |= ctx->mail_host[j->slot].d[MD_LS_X] < 0.0;
+      if (retry) {
+        // all remaining trials in one pass; jobs that already accepted x = tau
+        // see no change because their propars were updated (first trial valid
+        // again is not possible: only failed jobs are re-run below)
+        std::vector<hp_job*> failed;
+        for (hp_job* j : jobs)
+          if (ctx->mail_host[j->slot].d[MD_LS_X] < 0.0) failed.push_back(j);
+        HostBatch hb2;
+        rc = build_batch(ctx, failed, hb2);
+        if (rc) return rc;
+        const int L = failed[0]->dev.linspace_size;
+        launch_glisa_ls(hb2, st, 1, std::min(L - 1, 64));
+        rc = check_launch();
+        if (rc) return rc;
+        rc = read_mail(ctx);
+        if (rc) return rc;
+        for (hp_job* j : failed)
+          if (ctx->mail_host[j->slot].d[MD_LS_X] < 0.0) {
+            j->status = HP_ERR_NUMERIC;
+            g_err = "Line search failed!";
+            j->done = true;
+          }
+        rc = build_batch(ctx, jobs, hb2);
+        if (rc) return rc;
+      }
+    }
+  }
+  {
+    ProfScope ps(ctx, HP_KERNEL_CHANGE);
+    launch_glisa_change(hb, st);
+  }
+  launch_outer_finish(hb, st, 0);
+  int rc = check_launch();
+  if (rc) return rc;
+  rc = read_mail(ctx);
+  if (rc) return rc;
+  std::vector<hp_job*> conv;
+  for (hp_job* j : jobs) {
+    if (j->done) continue;
+    const Mailbox& m = ctx->mail_host[j->slot];
+    j->niter = m.i[MI_ITER];
+    j->change = m.d[MD_CHANGE];
+    j->evals += 3.0 * (double)j->dev.npoint * (double)j->dev.natom;
+    if (m.i[MI_ERR]) {
+      j->status = status_of(m.i[MI_ERR]);
+      g_err = err_text(m.i[MI_ERR]);
+      j->done = true;
+    } else if (j->change < j->desc.threshold) {
+      conv.push_back(j);
+    } else if (j->niter >= j->desc.maxiter) {
+      j->status = HP_ERR_NOT_CONVERGED;
+      g_err = "Not converged!";
+      j->done = true;
+    }
+  }
+  if (!conv.empty()) {
+    // converged: checks, then at_weights and charges with the final parameters
+    // (glisa.py:268-278)
+    HostBatch hc;
+    rc = build_batch(ctx, conv, hc);
+    if (rc) return rc;
+    if (solver != SOLVER_SC) launch_glisa_check(hc, st);
+    launch_promol(hc, st, 0, MODEL_BASIS);
+    launch_charges(hc, st);
+    rc = check_launch();
+    if (rc) return rc;
+    rc = read_mail(ctx);
+    if (rc) return rc;
+    for (hp_job* j : conv) {
+      const Mailbox& m = ctx->mail_host[j->slot];
+      j->warnings |= (uint32_t)m.i[MI_WARN];
+      j->evals += (double)j->dev.npoint * (double)j->dev.natom;
+      if (m.i[MI_ERR]) {
+        j->status = status_of(m.i[MI_ERR]);
+        g_err = err_text(m.i[MI_ERR]);
+      }
+      j->converged = true;
+      j->done = true;
+    }
+  }
+  return HP_OK;
+}
+
+int step_group(hp_ctx* ctx, const std::vector<hp_job*>& jobs) {
+  // The pinned staging buffers are reused by every build_batch; each upload
+  // is followed by a stream synchronisation before the next one.
+  int rc;
+  std::vector<hp_job*> fresh;
+  for (hp_job* j : jobs)
+    if (!j->initialized) fresh.push_back(j);
+  if (!fresh.empty()) {
+    HostBatch hf;
+    rc = build_batch(ctx, fresh, hf);
+    if (rc) return rc;
+    rc = job_init(ctx, fresh, hf);
+    if (rc) return rc;
+    HP_CK(cudaStreamSynchronize(ctx->stream));
+  }
+  HostBatch hb;
+  rc = build_batch(ctx, jobs, hb);
+  if (rc) return rc;
+  if (jobs[0]->desc.scheme == HP_SCHEME_GLISA) return step_glisa(ctx, jobs, hb);
+  return step_iterstock(ctx, jobs, hb);
+}
+
+// ---------------------------------------------------------------------------
+// job creation
+// ---------------------------------------------------------------------------
+
+int validate(const hp_job_desc* d) {
+  if (!d) return fail(HP_ERR_INVALID, "null descriptor");
+  if (d->scheme < 0 || d->scheme > 3) return fail(HP_ERR_INVALID, "unknown scheme");
+  if (d->natom <= 0 || d->npoint <= 0) return fail(HP_ERR_INVALID, "natom and npoint must be positive");
+  if (d->npoint > (int64_t)2000000000) return fail(HP_ERR_INVALID, "npoint too large");
+  if (!d->coordinates || !d->pseudo_numbers || !d->points || !d->weights || !d->density ||
+      !d->shell_offsets || !d->initial_propars)
+    return fail(HP_ERR_INVALID, "missing input array");
+  if (d->grid_type != 2 && d->grid_type != 3)
+    return fail(HP_ERR_UNSUPPORTED, "only grid_type 2 and 3 (molecular grid) are supported");
+  if (d->scheme != HP_SCHEME_MBIS && (!d->shell_orders || !d->shell_exponents))
+    return fail(HP_ERR_INVALID, "basis schemes need shell orders and exponents");
+  if (d->shell_offsets[0] != 0) return fail(HP_ERR_INVALID, "shell_offsets[0] must be 0");
+  for (int64_t a = 0; a < d->natom; ++a) {
+    const int n = d->shell_offsets[a + 1] - d->shell_offsets[a];
+    if (n <= 0) return fail(HP_ERR_INVALID, "every atom needs at least one shell");
+    if (d->scheme == HP_SCHEME_MBIS && n > 7) return fail(HP_ERR_INVALID, "MBIS allows at most 7 shells");
+    if (n > kMaxShells) return fail(HP_ERR_UNSUPPORTED, "at most 16 shells per atom");
+  }
+  if (d->maxiter <= 0) return fail(HP_ERR_INVALID, "maxiter must be positive");
+  if (d->scheme == HP_SCHEME_LISA &&
+      (d->solver != HP_SOLVER_SC && d->solver != HP_SOLVER_NEWTON && d->solver != HP_SOLVER_M_NEWTON &&
+       d->solver != HP_SOLVER_DEFAULT))
+    return fail(HP_ERR_UNSUPPORTED, "aLISA solvers on this path: sc, newton, m-newton");
+  if (d->scheme == HP_SCHEME_GLISA &&
+      (d->solver != HP_SOLVER_SC && d->solver != HP_SOLVER_NEWTON && d->solver != HP_SOLVER_M_NEWTON &&
+       d->solver != HP_SOLVER_DEFAULT))
+    return fail(HP_ERR_UNSUPPORTED, "gLISA solvers on this path: newton, m-newton, sc");
+  if (d->linspace_size > 64 || (d->scheme == HP_SCHEME_LISA && d->linspace_size > 32))
+    return fail(HP_ERR_UNSUPPORTED, "linspace_size too large");
+  for (int64_t s = 0; d->scheme != HP_SCHEME_MBIS && s < d->shell_offsets[d->natom]; ++s) {
+    if (!(d->shell_orders[s] > 0.0)) return fail(HP_ERR_INVALID, "n must be positive");
+    if (d->shell_exponents[s] < 0.0) return fail(HP_ERR_INVALID, "alpha must be non-negative");
+  }
+  return HP_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int32_t hp_abi_version(void) { return HPGPU_ABI_VERSION; }
+
+const char* hp_last_error(void) { return g_err.c_str(); }
+
+int32_t hp_ctx_create(int32_t device, size_t hbm_budget, void* stream, hp_ctx** out) {
+  if (!out) return fail(HP_ERR_INVALID, "null output pointer");
+  *out = nullptr;
+  int ndev = 0;
+  cudaError_t e = cudaGetDeviceCount(&ndev);
+  if (e != cudaSuccess || ndev == 0)
+    return fail(HP_ERR_CUDA, std::string("no CUDA device: ") + cudaGetErrorString(e));
+  if (device < 0 || device >= ndev) return fail(HP_ERR_INVALID, "device index out of range");
+  HP_CK(cudaSetDevice(device));
+  cudaDeviceProp prop;
+  HP_CK(cudaGetDeviceProperties(&prop, device));
+  if (prop.major * 10 + prop.minor != 103)
+    return fail(HP_ERR_CUDA, "libhpgpu is built for sm_103 (GB300) only");
+  hp_ctx* c = new hp_ctx();
+  c->device = device;
+  if (stream) {
+    c->stream = (cudaStream_t)stream;
+  } else {
+    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+      delete c;
+      return fail(HP_ERR_CUDA, "cudaStreamCreate failed");
+    }
+    c->own_stream = true;
+  }
+  size_t fr = 0, tot = 0;
+  cudaMemGetInfo(&fr, &tot);
+  c->budget = hbm_budget ? hbm_budget : (size_t)(0.9 * (double)fr);
+  c->slots.assign(kMaxSlots, nullptr);
+  if (cudaMalloc(&c->mail_dev, sizeof(Mailbox) * kMaxSlots) != cudaSuccess ||
+      cudaMallocHost(&c->mail_host, sizeof(Mailbox) * kMaxSlots) != cudaSuccess ||
+      cudaMalloc(&c->batch_dev, sizeof(JobDev) * kMaxSlots) != cudaSuccess ||
+      cudaMallocHost(&c->batch_host, sizeof(JobDev) * kMaxSlots) != cudaSuccess ||
+      cudaMalloc(&c->prefix_dev, sizeof(int) * K_NKIND * (kMaxSlots + 1)) != cudaSuccess ||
+      cudaMallocHost(&c->prefix_host, sizeof(int) * K_NKIND * (kMaxSlots + 1)) != cudaSuccess) {
+    hp_ctx_destroy(c);
+    return fail(HP_ERR_NO_MEMORY, "context allocation failed");
+  }
+  cudaMemsetAsync(c->mail_dev, 0, sizeof(Mailbox) * kMaxSlots, c->stream);
+  memset(c->mail_host, 0, sizeof(Mailbox) * kMaxSlots);
+  *out = c;
+  return HP_OK;
+}
+
+int32_t hp_ctx_destroy(hp_ctx* c) {
+  if (!c) return HP_OK;
+  cudaSetDevice(c->device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  for (hp_job* j : c->slots)
+    if (j) hp_job_destroy(j);
+  if (c->mail_dev) cudaFree(c->mail_dev);
+  if (c->mail_host) cudaFreeHost(c->mail_host);
+  if (c->batch_dev) cudaFree(c->batch_dev);
+  if (c->batch_host) cudaFreeHost(c->batch_host);
+  if (c->prefix_dev) cudaFree(c->prefix_dev);
+  if (c->prefix_host) cudaFreeHost(c->prefix_host);
+  prof_collect(c);
+  for (cudaEvent_t e : c->event_pool) cudaEventDestroy(e);
+  if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+  return HP_OK;
+}
+
+int32_t hp_ctx_synchronize(hp_ctx* c) {
+  if (!c) return fail(HP_ERR_INVALID, "null context");
+  HP_CK(cudaStreamSynchronize(c->stream));
+  return HP_OK;
+}
+
+int32_t hp_ctx_memory(hp_ctx* c, size_t* used, size_t* budget) {
+  if (!c) return fail(HP_ERR_INVALID, "null context");
+  if (used) *used = c->used;
+  if (budget) *budget = c->budget;
+  return HP_OK;
+}
+
+int32_t hp_job_create(hp_ctx* ctx, const hp_job_desc* d, hp_job** out) {
+  if (!ctx || !out) return fail(HP_ERR_INVALID, "null context or output pointer");
+  *out = nullptr;
+  int rc = validate(d);
+  if (rc) return rc;
+  HP_CK(cudaSetDevice(ctx->device));
+  int slot = -1;
+  for (int s = 0; s < kMaxSlots; ++s)
+    if (!ctx->slots[s]) {
+      slot = s;
+      break;
+    }
+  if (slot < 0) return fail(HP_ERR_NO_MEMORY, "too many live jobs in this context");
+
+  const int A = (int)d->natom;
+  const int N = (int)d->npoint;
+  const int S = d->shell_offsets[A];
+  const bool mbis = d->scheme == HP_SCHEME_MBIS;
+  const bool glisa = d->scheme == HP_SCHEME_GLISA;
+  const int P = mbis ? 2 * S : S;
+  int kmax = 1;
+  for (int a = 0; a < A; ++a) kmax = std::max(kmax, d->shell_offsets[a + 1] - d->shell_offsets[a]);
+  int solver = d->solver;
+  if (solver == HP_SOLVER_DEFAULT) {
+    if (d->scheme == HP_SCHEME_LISA) solver = HP_SOLVER_SC;
+    else if (glisa) solver = HP_SOLVER_NEWTON;
+    else if (d->scheme == HP_SCHEME_GISA) solver = HP_SOLVER_QP;
+  }
+  // tiles: aim for >= 2 * 152 point tiles when the grid is large enough
+  int ppt = (int)std::min<int64_t>(64, std::max<int64_t>(2, (N + kThreads * 304 - 1) / (kThreads * 304)));
+  const int tile_points = kThreads * ppt;
+  const int ntile = (N + tile_points - 1) / tile_points;
+  int qa = 2 + std::max(2 * 7 + 1, kMaxShells + 1);
+  if (d->scheme == HP_SCHEME_LISA && solver != HP_SOLVER_SC) qa = 2 + kNewtonQ(kmax);
+  const int maxiter = d->maxiter;
+  const bool mixed = d->precision == HP_PRECISION_MIXED;
+  const int htiles = glisa ? (S + kHessTile - 1) / kHessTile : 0;
+  const int npair = htiles * (htiles + 1) / 2;
+  int nsplit = glisa ? std::max(1, std::min(1024, (4 * 152 + npair - 1) / std::max(1, npair))) : 0;
+  if (glisa) nsplit = std::max(1, std::min(nsplit, (N + 255) / 256));
+
+  // carve one allocation
+  struct Part { void** dst; size_t bytes; };
+  std::vector<Part> parts;
+  JobDev J{};
+  auto add = [&](void* dst, size_t bytes) { parts.push_back({(void**)dst, bytes}); };
+  add(&J.px, 8 * (size_t)N); add(&J.py, 8 * (size_t)N); add(&J.pz, 8 * (size_t)N);
+  add(&J.w, 8 * (size_t)N); add(&J.rho, 8 * (size_t)N);
+  if (mixed) {
+    add(&J.pxh, 4 * (size_t)N); add(&J.pxl, 4 * (size_t)N);
+    add(&J.pyh, 4 * (size_t)N); add(&J.pyl, 4 * (size_t)N);
+    add(&J.pzh, 4 * (size_t)N); add(&J.pzl, 4 * (size_t)N);
+  }
+  add(&J.ax, 8 * (size_t)A); add(&J.ay, 8 * (size_t)A); add(&J.az, 8 * (size_t)A);
+  add(&J.zpseudo, 8 * (size_t)A);
+  add(&J.shell_off, 4 * (size_t)(A + 1)); add(&J.par_off, 4 * (size_t)(A + 1));
+  add(&J.sh_order, 8 * (size_t)S); add(&J.sh_alpha, 8 * (size_t)S); add(&J.sh_pref, 8 * (size_t)S);
+  add(&J.propars, 8 * (size_t)P); add(&J.propars_init, 8 * (size_t)P);
+  add(&J.propars_old, 8 * (size_t)P); add(&J.cur, 8 * (size_t)P);
+  add(&J.prev, 8 * (size_t)P); add(&J.delta, 8 * (size_t)P); add(&J.keep, 8 * (size_t)P);
+  add(&J.promol, 8 * (size_t)N);
+  add(&J.rhoa, 8 * (size_t)A * N);
+  add(&J.apart, 8 * (size_t)A * qa * ntile);
+  add(&J.jpart, 8 * (size_t)QJ_COUNT * ntile);
+  add(&J.atom_out, 8 * (size_t)A * AO_COUNT);
+  add(&J.active, 4 * (size_t)A); add(&J.inner_it, 4 * (size_t)A);
+  add(&J.ls_fail, 8 * (size_t)A * ntile);
+  if (glisa) {
+    add(&J.gmat, 8 * (size_t)S * N);
+    add(&J.gpart, 8 * (size_t)S * ntile);
+    add(&J.hpart, 8 * (size_t)nsplit * S * S);
+    add(&J.hess, 8 * (size_t)S * S);
+    add(&J.chol, 8 * (size_t)S * S);
+    add(&J.grad, 8 * (size_t)S);
+    add(&J.dvec1, 8 * (size_t)N); add(&J.dvec2, 8 * (size_t)N);
+  }
+  add(&J.hist_propars, 8 * (size_t)maxiter * P);
+  add(&J.hist_charges, 8 * (size_t)maxiter * A);
+  add(&J.hist_ent, 8 * (size_t)maxiter); add(&J.hist_chg, 8 * (size_t)maxiter);
+  add(&J.charges, 8 * (size_t)A);
+  size_t total = 0;
+  for (auto& p : parts) total += align_up(p.bytes);
+  if (ctx->used + total > ctx->budget)
+    return fail(HP_ERR_NO_MEMORY, "job needs " + std::to_string(total) + " bytes; HBM budget exceeded");
+  void* mem = nullptr;
+  if (cudaMalloc(&mem, total) != cudaSuccess) {
+    cudaGetLastError();
+    return fail(HP_ERR_NO_MEMORY, "cudaMalloc of " + std::to_string(total) + " bytes failed");
+  }
+  char* cur = (char*)mem;
+  for (auto& p : parts) {
+    *p.dst = cur;
+    cur += align_up(p.bytes);
+  }
+  J.mail = ctx->mail_dev + slot;
+  J.natom = A; J.npoint = N; J.ntile = ntile; J.nparam = P; J.nshell = S; J.qa = qa;
+  J.scheme = d->scheme; J.solver = solver; J.mixed = mixed; J.maxiter = maxiter;
+  J.inner_maxiter = d->inner_maxiter > 0 ? d->inner_maxiter : 2000;
+  J.linspace_size = d->linspace_size > 0 ? d->linspace_size : (glisa ? 40 : 20);
+  J.nsplit = nsplit; J.ppt = ppt; J.tile_points = tile_points; J.htiles = htiles;
+  J.threshold = d->threshold;
+  J.inner_threshold = d->inner_threshold < d->threshold ? d->inner_threshold : d->threshold;
+  J.density_cutoff = d->density_cutoff; J.negative_cutoff = d->negative_cutoff;
+  J.population_cutoff = d->population_cutoff; J.tau = d->tau;
+
+  hp_job* job = new hp_job();
+  job->ctx = ctx;
+  job->slot = slot;
+  job->desc = *d;
+  job->desc.solver = solver;
+  job->mem = mem;
+  job->bytes = total;
+  job->dev = J;
+
+  // host staging: SoA grid, float hi/lo, atoms, shells
+  cudaStream_t st = ctx->stream;
+  std::vector<double> buf((size_t)N);
+  auto up = [&](const void* dst, const void* src, size_t bytes) {
+    return cudaMemcpyAsync((void*)dst, src, bytes, cudaMemcpyHostToDevice, st);
+  };
+  bool ok = true;
+  for (int c = 0; c < 3 && ok; ++c) {
+    for (int p = 0; p < N; ++p) buf[p] = d->points[(size_t)3 * p + c];
+    const double* dst = c == 0 ? J.px : c == 1 ? J.py : J.pz;
+    ok &= up(dst, buf.data(), 8 * (size_t)N) == cudaSuccess;
+    if (mixed) {
+      std::vector<float> hi((size_t)N), lo((size_t)N);
+      for (int p = 0; p < N; ++p) {
+        hi[p] = (float)buf[p];
+        lo[p] = (float)(buf[p] - (double)hi[p]);
+      }
+      const float* dh = c == 0 ? J.pxh : c == 1 ? J.pyh : J.pzh;
+      const float* dl = c == 0 ? J.pxl : c == 1 ? J.pyl : J.pzl;
+      ok &= up(dh, hi.data(), 4 * (size_t)N) == cudaSuccess;
+      ok &= up(dl, lo.data(), 4 * (size_t)N) == cudaSuccess;
+    }
+  }
+  ok &= up(J.w, d->weights, 8 * (size_t)N) == cudaSuccess;
+  ok &= up(J.rho, d->density, 8 * (size_t)N) == cudaSuccess;
+  std::vector<double> ac((size_t)A);
+  for (int c = 0; c < 3 && ok; ++c) {
+    for (int a = 0; a < A; ++a) ac[a] = d->coordinates[(size_t)3 * a + c];
+    ok &= up(c == 0 ? J.ax : c == 1 ? J.ay : J.az, ac.data(), 8 * (size_t)A) == cudaSuccess;
+  }
+  ok &= up(J.zpseudo, d->pseudo_numbers, 8 * (size_t)A) == cudaSuccess;
+  ok &= up(J.shell_off, d->shell_offsets, 4 * (size_t)(A + 1)) == cudaSuccess;
+  std::vector<int> poff((size_t)A + 1);
+  for (int a = 0; a <= A; ++a) poff[a] = mbis ? 2 * d->shell_offsets[a] : d->shell_offsets[a];
+  ok &= up(J.par_off, poff.data(), 4 * (size_t)(A + 1)) == cudaSuccess;
+  std::vector<double> ord((size_t)S, 1.0), alp((size_t)S, 0.0), pref((size_t)S, 0.0);
+  if (!mbis) {
+    for (int s = 0; s < S; ++s) {
+      ord[s] = d->shell_orders[s];
+      alp[s] = d->shell_exponents[s];
+      pref[s] = ord[s] * std::pow(alp[s], 3.0 / ord[s]) / (4.0 * M_PI * std::tgamma(3.0 / ord[s]));
+    }
+  }
+  ok &= up(J.sh_order, ord.data(), 8 * (size_t)S) == cudaSuccess;
+  ok &= up(J.sh_alpha, alp.data(), 8 * (size_t)S) == cudaSuccess;
+  ok &= up(J.sh_pref, pref.data(), 8 * (size_t)S) == cudaSuccess;
+  ok &= up(J.propars, d->initial_propars, 8 * (size_t)P) == cudaSuccess;
+  ok &= up(J.propars_init, d->initial_propars, 8 * (size_t)P) == cudaSuccess;
+  ok &= cudaMemsetAsync(J.apart, 0, 8 * (size_t)A * qa * ntile, st) == cudaSuccess;
+  ok &= cudaMemsetAsync(J.atom_out, 0, 8 * (size_t)A * AO_COUNT, st) == cudaSuccess;
+  ok &= cudaMemsetAsync(J.charges, 0, 8 * (size_t)A, st) == cudaSuccess;
+  ok &= cudaMemsetAsync(ctx->mail_dev + slot, 0, sizeof(Mailbox), st) == cudaSuccess;
+  ok &= cudaStreamSynchronize(st) == cudaSuccess;
+  if (!ok) {
+    cudaFree(mem);
+    delete job;
+    return fail(HP_ERR_CUDA, "upload of job inputs failed");
+  }
+  memset(&ctx->mail_host[slot], 0, sizeof(Mailbox));
+  ctx->slots[slot] = job;
+  ctx->used += total;
+  *out = job;
+  return HP_OK;
+}
+
+int32_t hp_job_destroy(hp_job* job) {
+  if (!job) return HP_OK;
+  hp_ctx* ctx = job->ctx;
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  if (job->mem) cudaFree(job->mem);
+  ctx->used -= job->bytes;
+  ctx->slots[job->slot] = nullptr;
+  delete job;
+  return HP_OK;
+}
+
+int32_t hp_step(hp_ctx* ctx, hp_job* const* jobs, int32_t njobs, int32_t* n_live) {
+  if (!ctx || (njobs > 0 && !jobs)) return fail(HP_ERR_INVALID, "null argument");
+  if (njobs > kMaxSlots) return fail(HP_ERR_INVALID, "too many jobs in one step");
+  HP_CK(cudaSetDevice(ctx->device));
+  // group live jobs by (scheme, solver, precision)
+  std::vector<std::vector<hp_job*>> groups;
+  for (int i = 0; i < njobs; ++i) {
+    hp_job* j = jobs[i];
+    if (!j || j->ctx != ctx) return fail(HP_ERR_INVALID, "job does not belong to this context");
+    if (j->done) continue;
+    bool placed = false;
+    for (auto& g : groups) {
+      const hp_job* h = g[0];
+      if (h->desc.scheme == j->desc.scheme && h->dev.solver == j->dev.solver &&
+          h->desc.precision == j->desc.precision) {
+        g.push_back(j);
+        placed = true;
+        break;
+      }
+    }
+    if (!placed) groups.push_back({j});
+  }
+  for (auto& g : groups) {
+    int rc = step_group(ctx, g);
+    if (rc) return rc;
+  }
+  int live = 0;
+  for (int i = 0; i < njobs; ++i)
+    if (!jobs[i]->done) ++live;
+  if (n_live) *n_live = live;
+  return HP_OK;
+}
+
+int32_t hp_job_run(hp_ctx* ctx, hp_job* job) {
+  if (!ctx || !job) return fail(HP_ERR_INVALID, "null argument");
+  int32_t live = 1;
+  while (!job->done) {
+    int rc = hp_step(ctx, &job, 1, &live);
+    if (rc) return rc;
+  }
+  if (job->status != HP_OK) return fail(job->status, g_err.empty() ? "job failed" : g_err);
+  return HP_OK;
+}
+
+int32_t hp_job_reset(hp_job* job) {
+  if (!job) return fail(HP_ERR_INVALID, "null job");
+  hp_ctx* ctx = job->ctx;
+  HP_CK(cudaSetDevice(ctx->device));
+  const JobDev& J = job->dev;
+  HP_CK(cudaMemcpyAsync(J.propars, J.propars_init, 8 * (size_t)J.nparam, cudaMemcpyDeviceToDevice,
+                        ctx->stream));
+  HP_CK(cudaMemsetAsync(ctx->mail_dev + job->slot, 0, sizeof(Mailbox), ctx->stream));
+  HP_CK(cudaStreamSynchronize(ctx->stream));
+  memset(&ctx->mail_host[job->slot], 0, sizeof(Mailbox));
+  job->initialized = false;
+  job->done = false;
+  job->status = HP_OK;
+  job->niter = 0;
+  job->change = 0.0;
+  job->warnings = 0;
+  job->last_inner = 4;
+  job->evals = 0.0;
+  job->inner_total = 0.0;
+  job->converged = false;
+  return HP_OK;
+}
+
+int32_t hp_ctx_profile(hp_ctx* c, int32_t enable) {
+  if (!c) return fail(HP_ERR_INVALID, "null context");
+  HP_CK(cudaStreamSynchronize(c->stream));
+  prof_collect(c);
+  c->prof = enable != 0;
+  c->launch_base = g_launch_count;
+  for (int k = 0; k < HP_KERNEL_COUNT; ++k) {
+    c->prof_ms[k] = 0.0;
+    c->prof_n[k] = 0;
+  }
+  return HP_OK;
+}
+
+int32_t hp_ctx_profile_get(hp_ctx* c, int32_t family, double* ms, int64_t* launches) {
+  if (!c || family < 0 || family > HP_KERNEL_COUNT) return fail(HP_ERR_INVALID, "bad argument");
+  HP_CK(cudaStreamSynchronize(c->stream));
+  prof_collect(c);
+  if (family == HP_KERNEL_COUNT) {  // all kernel launches since profiling was enabled
+    if (ms) *ms = 0.0;
+    if (launches) *launches = g_launch_count - c->launch_base;
+    return HP_OK;
+  }
+  if (ms) *ms = c->prof_ms[family];
+  if (launches) *launches = c->prof_n[family];
+  return HP_OK;
+}
+
+int32_t hp_job_info_get(hp_job* job, hp_job_info* out) {
+  if (!job || !out) return fail(HP_ERR_INVALID, "null argument");
+  out->natom = job->dev.natom;
+  out->npoint = job->dev.npoint;
+  out->nparam = job->dev.nparam;
+  out->niter = job->niter;
+  out->inner_iterations = (int64_t)job->inner_total;
+  out->change = job->change;
+  out->done = job->done ? 1 : 0;
+  out->status = job->status;
+  out->warnings = job->warnings;
+  out->reserved = job->converged ? 1 : 0;
+  out->device_bytes = (int64_t)job->bytes;
+  out->point_atom_evals = job->evals;
+  return HP_OK;
+}
+
+int32_t hp_job_results_get(hp_job* job, const hp_job_results* r) {
+  if (!job || !r) return fail(HP_ERR_INVALID, "null argument");
+  hp_ctx* ctx = job->ctx;
+  HP_CK(cudaSetDevice(ctx->device));
+  const JobDev& J = job->dev;
+  const size_t A = J.natom, N = J.npoint, P = J.nparam;
+  const size_t nit = std::min(job->niter, J.maxiter);
+  cudaStream_t st = ctx->stream;
+  if (r->at_weights) {
+    if (!job->done) return fail(HP_ERR_STATE, "at_weights are available once the job is done");
+    std::vector<hp_job*> one{job};
+    HostBatch hb;
+    int rc = build_batch(ctx, one, hb);
+    if (rc) return rc;
+    const int glisa = job->desc.scheme == HP_SCHEME_GLISA;
+    launch_final_atweights(hb, st, glisa ? 0 : J.mixed, model_of(job), glisa ? 0 : 1);
+    rc = check_launch();
+    if (rc) return rc;
+  }
+  HP_CK(cudaStreamSynchronize(st));
+  if (r->charges) HP_CK(cudaMemcpy(r->charges, J.charges, 8 * A, cudaMemcpyDeviceToHost));
+  if (r->propars) HP_CK(cudaMemcpy(r->propars, J.propars, 8 * P, cudaMemcpyDeviceToHost));
+  if (r->history_propars && nit)
+    HP_CK(cudaMemcpy(r->history_propars, J.hist_propars, 8 * P * nit, cudaMemcpyDeviceToHost));
+  if (r->history_charges && nit)
+    HP_CK(cudaMemcpy(r->history_charges, J.hist_charges, 8 * A * nit, cudaMemcpyDeviceToHost));
+  if (r->history_entropies && nit)
+    HP_CK(cudaMemcpy(r->history_entropies, J.hist_ent, 8 * nit, cudaMemcpyDeviceToHost));
+  if (r->history_changes && nit)
+    HP_CK(cudaMemcpy(r->history_changes, J.hist_chg, 8 * nit, cudaMemcpyDeviceToHost));
+  if (r->promoldens) HP_CK(cudaMemcpy(r->promoldens, J.promol, 8 * N, cudaMemcpyDeviceToHost));
+  if (r->at_weights) HP_CK(cudaMemcpy(r->at_weights, J.rhoa, 8 * A * N, cudaMemcpyDeviceToHost));
+  return HP_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,201 @@
+/*
+ * hpgpu.h - C ABI of the GB300 partitioning library (libhpgpu.so).
+ *
+ * The library runs horton-part's iterative stockholder loop on one GPU:
+ * pro-atom evaluation on the Becke-weighted molecular grid, promolecule and
+ * at_weights ratio, weighted per-atom/per-shell moment integrals and the
+ * per-atom (MBIS, GISA, aLISA) or global (gLISA) parameter update, until the
+ * outer change drops below the threshold.
+ *
+ * Reference entry points this ABI replaces (paths inside horton-part's
+ * src/horton_part):
+ *   hp_job_create   <- WPart/AbstractISAWPart/GaussianISAWPart/LinearISAWPart/
+ *                      GlobalLinearISAWPart constructors: core/base.py:416-488,
+ *                      core/iterstock.py:64-114, gisa.py:114-160,
+ *                      alisa.py:1205-1256, glisa.py:58-117
+ *   hp_job_run      <- do_partitioning: core/iterstock.py:159-193 (MBIS, GISA,
+ *                      aLISA), glisa.py:248-281 (gLISA)
+ *   hp_step         <- one pass of the outer loop body: core/iterstock.py:172-188
+ *                      (_update_propars + _update_entropy + compute_change);
+ *                      for gLISA one solver iteration, glisa.py:748-798
+ *   hp_job_info_get / hp_job_results_get
+ *                   <- part.cache["niter"/"change"/"charges"/"propars"/
+ *                      "history_*"/"promoldens"/"at_weights_{i}"],
+ *                      core/iterstock.py:48-58, mbis.py:347-362
+ *
+ * Conventions
+ *   - All pointers in descriptors and result structs are HOST pointers; the
+ *     library copies inputs to the device in hp_job_create and copies results
+ *     into caller-owned buffers in hp_job_results_get.
+ *   - Every call returns an hp_status (0 = HP_OK). No C++ exception crosses
+ *     the ABI. hp_last_error() returns a message for the calling thread.
+ *   - A context is used by one host thread at a time. Jobs belong to the
+ *     context that created them.
+ *   - No CPU fallback: when no usable sm_103 device is present,
+ *     hp_ctx_create fails with HP_ERR_CUDA.
+ */
+#ifndef HPGPU_H
+#define HPGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define HPGPU_ABI_VERSION 1
+
+typedef enum {
+  HP_OK = 0,
+  HP_ERR_INVALID = 1,       /* bad argument (reference: ValueError/TypeError) */
+  HP_ERR_NO_MEMORY = 2,     /* device allocation failed or HBM budget exceeded */
+  HP_ERR_NOT_CONVERGED = 3, /* reference: RuntimeError("Not converged!") */
+  HP_ERR_NUMERIC = 4,       /* negative pro-atom density, singular Hessian,
+                               failed line search (reference: RuntimeError) */
+  HP_ERR_TIMEOUT = 5,       /* a bounded device wait ran out */
+  HP_ERR_CUDA = 6,          /* CUDA runtime error or no usable device */
+  HP_ERR_UNSUPPORTED = 7,   /* option not implemented on this path */
+  HP_ERR_STATE = 8          /* call made in the wrong state */
+} hp_status;
+
+typedef enum {
+  HP_SCHEME_MBIS = 0,  /* mbis.py  MBISWPart */
+  HP_SCHEME_GISA = 1,  /* gisa.py  GaussianISAWPart */
+  HP_SCHEME_LISA = 2,  /* alisa.py LinearISAWPart (aLISA) */
+  HP_SCHEME_GLISA = 3  /* glisa.py GlobalLinearISAWPart (gLISA) */
+} hp_scheme;
+
+typedef enum {
+  HP_SOLVER_DEFAULT = 0, /* MBIS fixed point; GISA QP; aLISA sc; gLISA newton */
+  HP_SOLVER_SC = 1,      /* alisa.py:193-291, glisa.py:805-848 */
+  HP_SOLVER_NEWTON = 2,  /* alisa.py:543-602, glisa.py:573-575 (exact Newton) */
+  HP_SOLVER_M_NEWTON = 3,/* alisa.py:605-664, glisa.py:577-591 (line search) */
+  HP_SOLVER_QP = 4       /* gisa.py:348-421 (quadratic program) */
+} hp_solver;
+
+typedef enum {
+  HP_PRECISION_FP64 = 0,  /* every step in FP64 */
+  HP_PRECISION_MIXED = 1  /* FP32 evaluation, FP64 sums/solves, FP64 polish */
+} hp_precision;
+
+/* Warning bits reported in hp_job_info.warnings (the reference logs these). */
+#define HP_WARN_INNER_NOT_CONVERGED 1u /* mbis.py:162, alisa.py:289 */
+#define HP_WARN_POPULATION 2u          /* utils.py:418-456 */
+#define HP_WARN_NEGATIVE_PARS 4u       /* utils.py:459-488 */
+
+typedef struct hp_ctx hp_ctx;
+typedef struct hp_job hp_job;
+
+typedef struct {
+  int32_t scheme;    /* hp_scheme */
+  int32_t solver;    /* hp_solver */
+  int32_t precision; /* hp_precision */
+  int32_t grid_type; /* 2 or 3 (molecular grid); 1 is not supported yet */
+  int64_t natom;
+  int64_t npoint;
+  const double* coordinates;    /* natom x 3, bohr */
+  const double* pseudo_numbers; /* natom */
+  const double* points;         /* npoint x 3, row-major */
+  const double* weights;        /* npoint */
+  const double* density;        /* npoint */
+  /* Shells. shell_offsets[natom+1] delimits each atom's shells.
+   * MBIS: each shell has the parameter pair (N_k, S_k); shell_orders and
+   *       shell_exponents are ignored.
+   * Basis schemes: shell k has fixed order n_k and exponent alpha_k and one
+   *       parameter (its population c_k). */
+  const int32_t* shell_offsets;
+  const double* shell_orders;
+  const double* shell_exponents;
+  /* Initial parameters: MBIS 2 per shell (N, S); basis schemes 1 per shell.
+   * For the basis schemes the library rescales them so that their sum is
+   * the integrated density (gisa.py:85-86). */
+  const double* initial_propars;
+  double threshold;
+  double inner_threshold; /* used as min(inner_threshold, threshold) */
+  double density_cutoff;
+  double negative_cutoff;
+  double population_cutoff;
+  double tau;             /* line-search start (m-newton) */
+  int32_t maxiter;        /* outer iterations (gLISA: solver iterations) */
+  int32_t inner_maxiter;  /* MBIS 2000, aLISA sc 100000, aLISA newton 10000 */
+  int32_t linspace_size;  /* line-search trial count (m-newton) */
+  int32_t reserved;
+} hp_job_desc;
+
+typedef struct {
+  int64_t natom;
+  int64_t npoint;
+  int64_t nparam;
+  int64_t niter;        /* outer iterations done */
+  int64_t inner_iterations; /* sum of inner iterations over atoms and outer iterations */
+  double change;        /* last outer change */
+  int32_t done;         /* 1 when converged, hit maxiter or failed */
+  int32_t status;       /* hp_status of the job (HP_OK unless it failed) */
+  uint32_t warnings;    /* HP_WARN_* bits */
+  int32_t reserved;
+  int64_t device_bytes; /* device memory held by the job */
+  double point_atom_evals; /* pro-atom evaluations done so far (sum over passes) */
+} hp_job_info;
+
+typedef struct {
+  double* charges;           /* natom */
+  double* propars;           /* nparam */
+  double* history_propars;   /* niter x nparam */
+  double* history_charges;   /* niter x natom (empty for gLISA) */
+  double* history_entropies; /* niter */
+  double* history_changes;   /* niter */
+  double* promoldens;        /* npoint */
+  double* at_weights;        /* natom x npoint */
+} hp_job_results;
+
+/* Library */
+int32_t hp_abi_version(void);
+const char* hp_last_error(void);
+
+/* Context: one device, one stream, an HBM budget in bytes (0 = 90 % of free
+ * memory). `stream` may be NULL (the library creates one) or a cudaStream_t
+ * owned by the caller. */
+int32_t hp_ctx_create(int32_t device, size_t hbm_budget, void* stream, hp_ctx** out);
+int32_t hp_ctx_destroy(hp_ctx* ctx);
+int32_t hp_ctx_synchronize(hp_ctx* ctx);
+/* Bytes reserved by live jobs and the budget. */
+int32_t hp_ctx_memory(hp_ctx* ctx, size_t* used, size_t* budget);
+
+/* Jobs */
+int32_t hp_job_create(hp_ctx* ctx, const hp_job_desc* desc, hp_job** out);
+int32_t hp_job_destroy(hp_job* job);
+/* Advance every live job in `jobs` by one outer iteration. Kernels of all
+ * jobs go to the context stream; the host waits once at the end. `n_live`
+ * receives the number of jobs still running. */
+int32_t hp_step(hp_ctx* ctx, hp_job* const* jobs, int32_t njobs, int32_t* n_live);
+/* Run one job to completion (the whole do_partitioning). */
+int32_t hp_job_run(hp_ctx* ctx, hp_job* job);
+int32_t hp_job_info_get(hp_job* job, hp_job_info* out);
+int32_t hp_job_results_get(hp_job* job, const hp_job_results* out);
+/* Restart a job from its initial parameters; inputs stay on the device.
+ * (No reference counterpart: re-running do_partitioning after part.clear(),
+ * core/base.py:164-167, without re-uploading the grid.) */
+int32_t hp_job_reset(hp_job* job);
+
+/* Kernel timing with CUDA events on the context stream, per kernel family
+ * (hp_kernel_family). Enabling clears the accumulators. */
+typedef enum {
+  HP_KERNEL_PROMOL = 0,     /* pro-atoms, promolecule, at_weights */
+  HP_KERNEL_INNER = 1,      /* MBIS / aLISA inner solver passes, GISA moments */
+  HP_KERNEL_CHANGE = 2,     /* outer change pass */
+  HP_KERNEL_GLISA_PRO = 3,  /* gLISA promolecule, ratios, entropy */
+  HP_KERNEL_GLISA_GRAD = 4, /* gLISA gradient */
+  HP_KERNEL_GLISA_HESS = 5, /* gLISA Hessian G^T diag(w rho/rho0^2) G */
+  HP_KERNEL_GLISA_SOLVE = 6,/* gLISA Newton solve, line search, updates */
+  HP_KERNEL_OTHER = 7,
+  HP_KERNEL_COUNT = 8
+} hp_kernel_family;
+int32_t hp_ctx_profile(hp_ctx* ctx, int32_t enable);
+int32_t hp_ctx_profile_get(hp_ctx* ctx, int32_t family, double* ms, int64_t* launches);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* HPGPU_H */

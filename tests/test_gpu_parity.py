@@ -1,0 +1,157 @@
+"""GPU parity: the public classes (through libhpgpu.so) against the
+reference's results on the same inputs.
+
+Golden values come from the unmodified reference (tests/golden). FP64 path
+tolerances: charges within 1e-8 e (the spec bar is 1e-6 e), pro-atom
+parameters within 1e-7 relative, identical iteration counts unless the
+reference's final change lies within 1e-6 (relative) of the threshold.
+"""
+
+import os
+import warnings
+
+import numpy as np
+import pytest
+
+from cases import CASES, build_inputs
+from horton_part_gb300 import synthetic
+from horton_part_gb300.basis import ExpBasisFuncHelper
+from horton_part_gb300.utils import wpart_schemes
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+Q_TOL = 1e-8
+P_RTOL = 1e-7
+
+
+def load_golden(name):
+    with np.load(os.path.join(GOLDEN, f"{name}.npz")) as f:
+        return {k: f[k] for k in f.files}
+
+
+def run_case(name, precision="fp64", store_at_weights=True):
+    case = CASES[name]
+    mol, kwargs = build_inputs(case)
+    cls = wpart_schemes(case["scheme"])
+    part = cls(mol.coordinates, mol.numbers, mol.pseudo_numbers, mol.grid, mol.density,
+               grid_type=3, precision=precision, store_at_weights=store_at_weights, **kwargs)
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        part.do_partitioning()
+    return part, mol
+
+
+def niter_must_match(g, threshold):
+    ch = np.asarray(g["history_changes"])
+    return abs(ch[-1] - threshold) > 1e-6 * threshold and (len(ch) < 2 or abs(ch[-2] - threshold) > 1e-6 * threshold)
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_fp64_parity_with_reference(name, gpu_context):
+    g = load_golden(name)
+    part, mol = run_case(name)
+    thr = CASES[name]["kwargs"]["threshold"]
+    if niter_must_match(g, thr):
+        assert part["niter"] == int(g["niter"])
+    np.testing.assert_allclose(part["charges"], g["charges"], rtol=0, atol=Q_TOL)
+    np.testing.assert_allclose(part["propars"], g["propars"], rtol=P_RTOL, atol=1e-10)
+    n = min(len(part["history_changes"]), len(g["history_changes"]))
+    np.testing.assert_allclose(part["history_entropies"][:n], g["history_entropies"][:n],
+                               rtol=1e-8, atol=1e-10)
+    np.testing.assert_allclose(part["history_propars"][:n], g["history_propars"][:n],
+                               rtol=1e-6, atol=1e-9)
+    np.testing.assert_allclose(part["populations"], g["populations"], atol=Q_TOL)
+    if CASES[name]["scheme"] != "glisa":
+        np.testing.assert_allclose(part["history_charges"][:n], g["history_charges"][:n],
+                                   atol=Q_TOL)
+        assert part["change"] == pytest.approx(float(g["change"]), rel=1e-4)
+    else:
+        assert part["history_charges"].size == 0
+    if "core_charges" in g:
+        np.testing.assert_allclose(part["core_charges"], g["core_charges"], atol=Q_TOL)
+        np.testing.assert_allclose(part["valence_charges"], g["valence_charges"], atol=Q_TOL)
+        np.testing.assert_allclose(part["valence_widths"], g["valence_widths"], rtol=P_RTOL)
+
+
+def test_at_weights_and_promolecule(gpu_context):
+    """at_weights are the clipped pro-atom / promolecule ratios and sum to one
+    where the promolecule is well above 1e-100 (core/stockholder.py:352-377)."""
+    part, mol = run_case("mbis_h2o_75x110")
+    aw = np.array([part[f"at_weights_{i}"] for i in range(mol.natom)])
+    promol = part["promoldens"]
+    assert aw.min() >= 0.0 and aw.max() <= 1.0
+    big = promol > 1e-30
+    np.testing.assert_allclose(aw[:, big].sum(axis=0), 1.0, atol=1e-12)
+    # charges from the at_weights on the grid agree with the loop's charges
+    # up to one outer iteration's change
+    q = mol.pseudo_numbers - np.array([mol.grid.integrate(aw[i], mol.density) for i in range(mol.natom)])
+    np.testing.assert_allclose(q, part["charges"], atol=1e-6)
+
+
+def test_do_charges_and_do_all(gpu_context):
+    mol = synthetic.water(nrad=40, nang=50)
+    cls = wpart_schemes("mbis")
+    part = cls(mol.coordinates, mol.numbers, mol.pseudo_numbers, mol.grid, mol.density,
+               grid_type=3, threshold=1e-6)
+    part.do_charges()
+    names = part.do_all()
+    for key in ("charges", "propars", "niter", "change", "history_propars", "populations",
+                "pseudo_populations", "core_charges", "valence_charges", "valence_widths"):
+        assert key in part.cache and key in names
+    assert abs(part["charges"].sum()) < 1e-3
+    assert part["charges"] == pytest.approx(part["valence_charges"] + part["core_charges"])
+
+
+def test_grid_type_1_is_rejected_like_the_reference(gpu_context):
+    mol = synthetic.water(nrad=20, nang=50)
+    cls = wpart_schemes("mbis")
+    with pytest.raises(ValueError):
+        cls(mol.coordinates, mol.numbers, mol.pseudo_numbers, mol.grid, mol.density, grid_type=1)
+
+
+def test_numbers_must_be_int64(gpu_context):
+    mol = synthetic.water(nrad=20, nang=50)
+    with pytest.raises(TypeError):
+        wpart_schemes("mbis")(mol.coordinates, mol.numbers.astype(np.int32), mol.pseudo_numbers,
+                              mol.grid, mol.density, grid_type=3)
+
+
+def test_glisa_not_converged_raises(gpu_context):
+    mol = synthetic.water(nrad=30, nang=50)
+    part = wpart_schemes("glisa")(mol.coordinates, mol.numbers, mol.pseudo_numbers, mol.grid,
+                                  mol.density, grid_type=3, solver="newton",
+                                  solver_options={"maxiter": 2}, threshold=1e-12)
+    with pytest.raises(RuntimeError, match="Not converged"):
+        part.do_partitioning()
+
+
+def test_hbm_budget_rejects_oversized_job():
+    from horton_part_gb300 import _lib
+
+    ctx = _lib.Context(0, hbm_budget=1 << 20)
+    mol = synthetic.water(nrad=40, nang=110)
+    part = wpart_schemes("mbis")(mol.coordinates, mol.numbers, mol.pseudo_numbers, mol.grid,
+                                 mol.density, grid_type=3, context=ctx)
+    with pytest.raises(MemoryError):
+        part.do_partitioning()
+    ctx.close()
+
+
+def test_custom_basis_helper(gpu_context):
+    """A user-supplied ExpBasisFuncHelper (the config-2 style basis) runs and
+    matches the oracle."""
+    from oracle import hp_oracle as O
+
+    mol = synthetic.chain_molecule({6: 1, 8: 1, 1: 3}, 30, 50, seed=11)
+    helper = synthetic.geometric_gaussian_basis({1: 4, 6: 6, 8: 6}, 0.05, 300.0)
+    part = wpart_schemes("glisa")(mol.coordinates, mol.numbers, mol.pseudo_numbers, mol.grid,
+                                  mol.density, grid_type=3, solver="newton", basis_func=helper,
+                                  threshold=1e-8)
+    part.do_partitioning()
+    ref = O.glisa(mol.coordinates, mol.numbers, mol.pseudo_numbers, mol.grid.points,
+                  mol.grid.weights, mol.density, [helper.get_order(z) for z in mol.numbers],
+                  [helper.get_exponent(z) for z in mol.numbers],
+                  [helper.get_initial(z) for z in mol.numbers], threshold=1e-8, solver="newton")
+    np.testing.assert_allclose(part["charges"], ref["charges"], atol=Q_TOL)
+    assert part["niter"] == ref["niter"]

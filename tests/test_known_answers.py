@@ -1,0 +1,124 @@
+"""Known-answer checks that the reference's own tests pin (no GPU).
+
+* ``tests/test_mbis.py:26-41``: MBIS shell counts and initial parameters.
+* ``tests/core/test_basis.py:102-188``: normalised shell values and the
+  Slater exponent tables.
+* ``core/cache.py`` semantics of ``Cache`` / ``just_once``.
+"""
+
+import numpy as np
+import pytest
+
+from horton_part_gb300 import basis, mbis
+from horton_part_gb300.cache import Cache, JustOnceClass, just_once
+from oracle import hp_oracle as O
+
+
+@pytest.mark.parametrize("impl", [mbis.get_nshell, O.mbis_nshell])
+def test_get_nshell(impl):
+    expected = {1: 1, 2: 1, 3: 2, 17: 3, 18: 3, 21: 4, 44: 5, 72: 6, 104: 7}
+    for z, n in expected.items():
+        assert impl(z) == n
+
+
+@pytest.mark.parametrize("impl", [mbis.get_initial_mbis_propars, O.mbis_initial_propars])
+def test_get_initial_mbis_propars(impl):
+    assert (impl(1) == [1.0, 2.0]).all()
+    assert (impl(2) == [2.0, 4.0]).all()
+    assert (impl(3) == [2.0, 6.0, 1.0, 2.0]).all()
+
+
+def test_evaluate_function_scalar():
+    r = np.array([1.0])
+    assert np.isclose(basis.evaluate_function(2, 1.0, 1.0, r), np.pi ** (-1.5) * np.exp(-1))
+    f, df = basis.evaluate_function(2, 1.0, 1.0, r, 1)
+    assert np.isclose(df[-1], -2 * np.pi ** (-1.5) * np.exp(-1))
+    assert basis.evaluate_function(2, 1, 0.5, np.array([0, 1, 2])).shape == (3,)
+
+
+def test_evaluate_function_vector():
+    pops = np.ones(10)
+    exps = np.ones(10)
+    r = np.ones(100)
+    res = basis.evaluate_function(np.full(10, 2.0), pops, exps, r)
+    assert res.shape == (10, 100)
+    assert res == pytest.approx(np.full((10, 100), np.pi ** (-1.5) * np.exp(-1)))
+
+
+def test_evaluate_function_errors():
+    with pytest.raises(NotImplementedError):
+        basis.evaluate_function(2, 1.0, 2.0, np.array([3.0]), 2)
+    with pytest.raises(ValueError):
+        basis.evaluate_function(0, 1.0, 2.0, np.array([3.0]))
+    with pytest.raises(ValueError):
+        basis.evaluate_function(2, 1.0, -2.0, np.array([3.0]))
+
+
+def test_shell_normalisation():
+    # N(alpha, n) integrates to one over space for Slater and Gaussian orders
+    r = np.linspace(0, 60, 600001)
+    for n, a in ((1.0, 2.3), (2.0, 0.7), (1.5, 1.1)):
+        f = basis.shell_prefactor(n, a) * np.exp(-a * r**n)
+        assert np.trapezoid(4 * np.pi * r**2 * f, r) == pytest.approx(1.0, rel=1e-6)
+        assert basis.shell_prefactor(n, a) == pytest.approx(O.shell_prefactor(n, a), rel=1e-15)
+
+
+def test_slater_tables():
+    h = basis.ExpBasisFuncHelper.from_function_type("slater")
+    assert h.get_exponent(1) == pytest.approx([6.6, 4.62, 3.23, 2.26, 1.58, 1.1, 0.77, 1.0])
+    assert h.get_exponent(6) == pytest.approx(
+        [22.8, 17.35, 13.2, 8.79, 10.83, 7.91, 5.78, 4.22, 4.51, 3.46, 2.65, 2.03, 1.56])
+    g = basis.ExpBasisFuncHelper.from_function_type("gauss")
+    assert g.get_nshell(1) == 4 and g.get_nshell(6) == 6 and g.get_nshell(16) == 9
+
+
+def test_cache_semantics():
+    c = Cache()
+    arr, new = c.load("a", alloc=3, tags="o")
+    assert new and arr.shape == (3,)
+    arr2, new2 = c.load("a", alloc=3, tags="o")
+    assert not new2 and arr2 is arr
+    c.dump("b", 5, tags="o")
+    assert c["b"] == 5 and "b" in c
+    assert sorted(c.iterkeys(tags="o")) == ["a", "b"]
+    c.clear()
+    assert "a" not in c
+    with pytest.raises(KeyError):
+        c.load("a")
+    assert c.load("zz", default=7) == 7
+    with pytest.raises(TypeError):
+        c.load("a", alloc=3, default=1)
+
+
+def test_just_once():
+    class A(JustOnceClass):
+        def __init__(self):
+            super().__init__()
+            self.n = 0
+
+        @just_once
+        def do(self):
+            self.n += 1
+
+    a = A()
+    a.do()
+    a.do()
+    assert a.n == 1 and "do" in a.time_usage
+    a.clear()
+    a.do()
+    assert a.n == 2
+
+
+def test_qp_simplex_kkt():
+    rng = np.random.default_rng(0)
+    for _ in range(20):
+        k = rng.integers(2, 9)
+        a = np.geomspace(100, 0.05, k) * rng.uniform(0.8, 1.2, k)
+        P = 2 / np.pi**1.5 * (a[:, None] * a[None]) ** 1.5 / (a[:, None] + a[None]) ** 1.5
+        q = -rng.uniform(0, 3, k)
+        x = O.qp_simplex_nonneg(P, q, 2.0)
+        assert x.min() >= 0 and x.sum() == pytest.approx(2.0)
+        g = P @ x + q
+        lam = -np.mean(g[x > 1e-12])
+        assert np.all(g[x > 1e-12] + lam == pytest.approx(0, abs=1e-9))
+        assert np.all(g[x <= 1e-12] + lam >= -1e-9)

@@ -129,7 +129,7 @@ def test_glisa_not_converged_raises(gpu_context):
 def test_hbm_budget_rejects_oversized_job():
     from horton_part_gb300 import _lib
 
-    ctx = _lib.Context(0, hbm_budget=1 << 20)
+    ctx = _lib.Context(0, hbm_budget=1 << 16)
     mol = synthetic.water(nrad=40, nang=110)
     part = wpart_schemes("mbis")(mol.coordinates, mol.numbers, mol.pseudo_numbers, mol.grid,
                                  mol.density, grid_type=3, context=ctx)

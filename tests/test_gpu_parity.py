@@ -139,12 +139,23 @@ def test_hbm_budget_rejects_oversized_job():
 
 
 def test_custom_basis_helper(gpu_context):
-    """A user-supplied ExpBasisFuncHelper (the config-2 style basis) runs and
-    matches the oracle."""
+    """A user-supplied ExpBasisFuncHelper object runs and matches the oracle;
+    an ill-posed basis (tight 300 bohr^-2 Gaussians on H, whose optimal
+    populations are zero) makes the unconstrained Newton system singular on
+    the GPU exactly as in the reference (glisa.py:763-769 raises)."""
     from oracle import hp_oracle as O
 
     mol = synthetic.chain_molecule({6: 1, 8: 1, 1: 3}, 30, 50, seed=11)
-    helper = synthetic.geometric_gaussian_basis({1: 4, 6: 6, 8: 6}, 0.05, 300.0)
+    bad = synthetic.geometric_gaussian_basis({1: 4, 6: 6, 8: 6}, 0.05, 300.0)
+    part = wpart_schemes("glisa")(mol.coordinates, mol.numbers, mol.pseudo_numbers, mol.grid,
+                                  mol.density, grid_type=3, solver="newton", basis_func=bad,
+                                  threshold=1e-8)
+    with pytest.raises(RuntimeError):
+        part.do_partitioning()
+    gauss = ExpBasisFuncHelper.from_function_type("gauss")
+    helper = ExpBasisFuncHelper({z: gauss.get_order(z) for z in (1, 6, 8)},
+                                {z: gauss.get_exponent(z) for z in (1, 6, 8)},
+                                {z: gauss.get_initial(z) for z in (1, 6, 8)})
     part = wpart_schemes("glisa")(mol.coordinates, mol.numbers, mol.pseudo_numbers, mol.grid,
                                   mol.density, grid_type=3, solver="newton", basis_func=helper,
                                   threshold=1e-8)

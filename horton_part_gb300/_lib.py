@@ -72,7 +72,7 @@ class HPError(RuntimeError):
 EXPORTED = ("hp_abi_version", "hp_last_error", "hp_ctx_create", "hp_ctx_destroy",
             "hp_ctx_synchronize", "hp_ctx_memory", "hp_job_create", "hp_job_destroy", "hp_step",
             "hp_job_run", "hp_job_info_get", "hp_job_results_get", "hp_job_reset",
-            "hp_ctx_profile", "hp_ctx_profile_get")
+            "hp_ctx_profile", "hp_ctx_profile_get", "hp_mbis_inner_noalloc")
 
 KERNEL_FAMILIES = {"promol": 0, "inner": 1, "change": 2, "glisa_pro": 3, "glisa_grad": 4,
                    "glisa_hess": 5, "glisa_solve": 6, "other": 7}
@@ -107,6 +107,10 @@ def lib():
         L.hp_job_info_get.argtypes = [ctypes.c_void_p, ctypes.POINTER(JobInfo)]
         L.hp_job_results_get.argtypes = [ctypes.c_void_p, ctypes.POINTER(JobResults)]
         L.hp_job_reset.argtypes = [ctypes.c_void_p]
+        L.hp_mbis_inner_noalloc.argtypes = [
+            ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int32,
+            ctypes.c_void_p, ctypes.c_double, ctypes.c_double, ctypes.c_int32,
+            ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32), ctypes.c_void_p]
         L.hp_ctx_profile.argtypes = [ctypes.c_void_p, ctypes.c_int32]
         L.hp_ctx_profile_get.argtypes = [ctypes.c_void_p, ctypes.c_int32,
                                          ctypes.POINTER(ctypes.c_double),

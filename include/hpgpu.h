@@ -194,6 +194,29 @@ typedef enum {
 int32_t hp_ctx_profile(hp_ctx* ctx, int32_t enable);
 int32_t hp_ctx_profile_get(hp_ctx* ctx, int32_t family, double* ms, int64_t* launches);
 
+/* MBIS inner fixed point for ONE atom that allocates no memory. It has no
+ * counterpart in the reference; it computes what the reference's per-atom
+ * solver opt_mbis_propars does for one atom on the molecular grid.
+ *
+ * For callers that cannot call cudaMalloc: code running inside a host
+ * application's own device-memory pool, plug-in hosts that forbid allocation
+ * after start-up, and loops where an allocation would synchronise the device.
+ *
+ * All array arguments are DEVICE pointers owned by the caller: rho_a, weights
+ * and radial_dist hold npoint values (the atom's AIM density w_a * rho, the
+ * grid weights and |r - R_a|); propars holds the 2*nshell (N, S) pairs on
+ * input and the solution on output. niter and converged are optional HOST
+ * outputs. Runs on `stream` (NULL = default stream) and returns after it.
+ * Limits: 1 <= nshell <= 7 and npoint <= 2,097,152 (HP_ERR_INVALID beyond).
+ * The scratch is one 492 KB static device array per GPU, shared by all calls:
+ * calls that overlap on the GPU (other streams or threads) race on it. The
+ * first call on a device looks up that array's address; make that first call
+ * before any stream capture. */
+int32_t hp_mbis_inner_noalloc(const double* rho_a, const double* weights,
+                              const double* radial_dist, int64_t npoint, int32_t nshell,
+                              double* propars, double threshold, double density_cutoff,
+                              int32_t maxiter, int32_t* niter, int32_t* converged, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -369,6 +369,29 @@ def run_ours(args):
         "roofline": roofline, "clocks": clocks.summary(),
         "gpu_launches": int(launches),
     }
+    if args.precision == "mixed":
+        # error of the mixed-precision result against the FP64 path on the
+        # same input (the FP64 path matches the reference to 1e-8 e in tests)
+        jm = make_job(ctx, w, "mixed")
+        jm.run()
+        rm, im = jm.results(promoldens=False, histories=False), jm.info()
+        jm.close()
+        jd = make_job(ctx, w, "fp64")
+        jd.run()
+        rd = jd.results(promoldens=False, histories=False)
+        jd.close()
+        off = np.asarray(job_arrays(w)[0])
+        per = 2 if w["scheme"] == "mbis" else 1
+        dp = 0.0
+        for a in range(len(off) - 1):
+            sl = slice(per * off[a], per * off[a + 1])
+            for k in ((slice(0, None, 2), slice(1, None, 2)) if per == 2 else (slice(None),)):
+                ref = rd["propars"][sl][k]
+                dp = max(dp, float(np.abs(rm["propars"][sl][k] - ref).max() / np.abs(ref).max()))
+        line["accuracy_vs_fp64"] = {
+            "max_abs_dq_e": float(np.abs(rm["charges"] - rd["charges"]).max()),
+            "max_scaled_dparam": dp, "polish_iterations": int(im.polish_iterations),
+            "niter_mixed": int(im.niter)}
     if rank == 0 and world == 1 and not args.no_cpu:
         r, sample, threads = cpu_sample(w, 2 if w["scheme"] == "glisa" else 3)
         line["cpu_baseline"] = {"value": r, "unit": UNIT, "cores": threads, "kind": "port",
@@ -388,7 +411,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="gisa-c6h10n2o2")
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:

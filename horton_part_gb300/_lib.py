@@ -28,6 +28,7 @@ PRECISIONS = {"fp64": 0, "mixed": 1}
 WARN_INNER_NOT_CONVERGED = 1
 WARN_POPULATION = 2
 WARN_NEGATIVE_PARS = 4
+WARN_NOISE_FLOOR = 8
 
 _dp = ctypes.POINTER(ctypes.c_double)
 _ip = ctypes.POINTER(ctypes.c_int32)
@@ -43,7 +44,7 @@ class JobDesc(ctypes.Structure):
         ("inner_threshold", ctypes.c_double), ("density_cutoff", ctypes.c_double),
         ("negative_cutoff", ctypes.c_double), ("population_cutoff", ctypes.c_double),
         ("tau", ctypes.c_double), ("maxiter", ctypes.c_int32), ("inner_maxiter", ctypes.c_int32),
-        ("linspace_size", ctypes.c_int32), ("reserved", ctypes.c_int32),
+        ("linspace_size", ctypes.c_int32), ("polish", ctypes.c_int32),
     ]
 
 
@@ -52,8 +53,9 @@ class JobInfo(ctypes.Structure):
         ("natom", ctypes.c_int64), ("npoint", ctypes.c_int64), ("nparam", ctypes.c_int64),
         ("niter", ctypes.c_int64), ("inner_iterations", ctypes.c_int64),
         ("change", ctypes.c_double), ("done", ctypes.c_int32), ("status", ctypes.c_int32),
-        ("warnings", ctypes.c_uint32), ("reserved", ctypes.c_int32),
+        ("warnings", ctypes.c_uint32), ("converged", ctypes.c_int32),
         ("device_bytes", ctypes.c_int64), ("point_atom_evals", ctypes.c_double),
+        ("polish_iterations", ctypes.c_int32), ("reserved", ctypes.c_int32),
     ]
 
 
@@ -218,7 +220,8 @@ class Job:
                  shell_offsets, initial_propars, shell_orders=None, shell_exponents=None,
                  solver="default", precision="fp64", grid_type=3, threshold=1e-6,
                  inner_threshold=1e-8, density_cutoff=1e-15, negative_cutoff=-1e-12,
-                 population_cutoff=1e-4, maxiter=500, inner_maxiter=0, linspace_size=0, tau=1.0):
+                 population_cutoff=1e-4, maxiter=500, inner_maxiter=0, linspace_size=0, tau=1.0,
+                 polish=False):
         self.ctx = ctx
         keep = []
 
@@ -254,6 +257,7 @@ class Job:
         d.density_cutoff, d.negative_cutoff = density_cutoff, negative_cutoff
         d.population_cutoff, d.tau = population_cutoff, tau
         d.maxiter, d.inner_maxiter, d.linspace_size = int(maxiter), int(inner_maxiter), int(linspace_size)
+        d.polish = 1 if polish else 0
         handle = ctypes.c_void_p()
         _check(lib().hp_job_create(ctx.handle, ctypes.byref(d), ctypes.byref(handle)))
         self._h = handle

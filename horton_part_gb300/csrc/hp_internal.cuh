@@ -97,6 +97,15 @@ struct JobDev {
   const float* pzh; const float* pzl;
   const float* wf;
   const float* rhof;
+  const float* shf;       // mixed: per shell (order, alpha, prefactor) as FP32
+  const float* atf;       // mixed: atom coordinates as FP32 hi/lo [natom][6]
+  const double* qp_p;     // GISA: per-atom QP matrix P (K_a x K_a, FP64), at shell_off^2 offsets
+  const int* qp_off;      // GISA: offset of atom a's P block (natom + 1)
+  float* fpar;            // mixed: FP32 pro-atom coefficients of propars (2 per shell)
+  float* fco;             // mixed: per-shell FP32 coefficients [nshell][8] of a (new, old)
+                          // parameter pair: MBIS (A_new, S_new, A_old, S_old, g, dS),
+                          // basis (c_new, c_old - c_new); A = N S^3/(8 pi), g = A_old/A_new - 1
+  float* promolf;         // mixed: FP32 promolecule
   // atoms and shells
   const double* ax;
   const double* ay;
@@ -206,11 +215,53 @@ __device__ __forceinline__ double block_sum1(double v, double* red) {
   return s;
 }
 
+// Per-tile partial sums of mixed-precision jobs are float-float pairs stored
+// in the FP64 slot (bit pattern of a float2); FP64 jobs store doubles.
+__device__ __forceinline__ double partial_value(const JobDev& J, const double* slot) {
+  if (!J.mixed) return *slot;
+  const float2 v = *reinterpret_cast<const float2*>(slot);
+  return (double)v.x + (double)v.y;
+}
+
+__device__ __forceinline__ void store_partial(const JobDev& J, double* slot, double v) {
+  if (!J.mixed) {
+    *slot = v;
+    return;
+  }
+  const float hi = (float)v;
+  *reinterpret_cast<float2*>(slot) = make_float2(hi, (float)(v - (double)hi));
+}
+
 // Fixed-order sum of n values with stride (one thread).
 __device__ __forceinline__ double serial_sum(const double* p, int n) {
   double s = 0.0;
   for (int i = 0; i < n; ++i) s += p[i];
   return s;
+}
+
+constexpr double kInv8PiD = 0.039788735772973836;  // 1 / (8 pi)
+
+// FP32 coefficients of shell s for a (new, old) parameter pair, formed in
+// FP64 (mixed precision only): MBIS (A_new, S_new, A_old, S_old, g, dS) with
+// A = N S^3 / (8 pi), g = A_old / A_new - 1, dS = S_new - S_old; basis
+// schemes (c_new, c_old - c_new).
+__device__ __forceinline__ void fill_fco(const JobDev& J, int s, const double* pnew,
+                                         const double* pold) {
+  float* c = J.fco + 8 * s;
+  if (J.scheme == SCHEME_MBIS) {
+    const double n1 = pnew[2 * s], s1 = pnew[2 * s + 1];
+    const double n0 = pold[2 * s], s0 = pold[2 * s + 1];
+    const double a1 = n1 * s1 * s1 * s1 * kInv8PiD, a0 = n0 * s0 * s0 * s0 * kInv8PiD;
+    c[0] = (float)a1;
+    c[1] = (float)s1;
+    c[2] = (float)a0;
+    c[3] = (float)s0;
+    c[4] = a1 != 0.0 ? (float)(a0 / a1 - 1.0) : 0.0f;
+    c[5] = (float)(s1 - s0);
+  } else {
+    c[0] = (float)pnew[s];
+    c[1] = (float)(pold[s] - pnew[s]);
+  }
 }
 
 // Distance from grid point p to atom a.
@@ -233,15 +284,10 @@ struct Dist<double> {
 template <>
 struct Dist<float> {
   __device__ __forceinline__ static float r(const JobDev& J, int p, int a) {
-    const float axh = (float)J.ax[a];
-    const float ayh = (float)J.ay[a];
-    const float azh = (float)J.az[a];
-    const float axl = (float)(J.ax[a] - (double)axh);
-    const float ayl = (float)(J.ay[a] - (double)ayh);
-    const float azl = (float)(J.az[a] - (double)azh);
-    const float dx = (J.pxh[p] - axh) + (J.pxl[p] - axl);
-    const float dy = (J.pyh[p] - ayh) + (J.pyl[p] - ayl);
-    const float dz = (J.pzh[p] - azh) + (J.pzl[p] - azl);
+    const float* c = J.atf + 6 * a;  // xh, xl, yh, yl, zh, zl (no FP64 work per point)
+    const float dx = (J.pxh[p] - c[0]) + (J.pxl[p] - c[1]);
+    const float dy = (J.pyh[p] - c[2]) + (J.pyl[p] - c[3]);
+    const float dz = (J.pzh[p] - c[4]) + (J.pzl[p] - c[5]);
     return sqrtf(dx * dx + dy * dy + dz * dz);
   }
 };
@@ -274,12 +320,13 @@ namespace hp {
 // Launch kinds: blocks per job for each kind of work.
 enum Kind {
   K_POINT = 0,      // one block per point tile
+  K_POINT1 = 6,     // one block per kThreads points (kernels without per-tile sums)
   K_ATOM_TILE = 1,  // one block per (atom, point tile)
   K_ATOM = 2,       // one 32-thread block per atom
   K_JOB = 3,        // one block per job
   K_HESS = 4,       // gLISA Hessian: (tile pair, point split)
   K_SQUARE = 5,     // gLISA reduce: ceil(nshell^2 / kThreads)
-  K_NKIND = 6
+  K_NKIND = 7
 };
 
 struct HostBatch {
@@ -311,6 +358,14 @@ void launch_glisa_keep(const HostBatch& hb, cudaStream_t st);
 void launch_glisa_ls(const HostBatch& hb, cudaStream_t st, int first, int count);
 void launch_glisa_change(const HostBatch& hb, cudaStream_t st);
 void launch_glisa_check(const HostBatch& hb, cudaStream_t st);
+
+// mixed precision (hp_mixed.cu)
+void launch_promol_mx(const HostBatch& hb, cudaStream_t st, int model);
+void launch_change_mx(const HostBatch& hb, cudaStream_t st, int model);
+void launch_mbis_inner_mx(const HostBatch& hb, cudaStream_t st);
+void launch_basis_qvec_mx(const HostBatch& hb, cudaStream_t st);
+void launch_lisa_sc_inner_mx(const HostBatch& hb, cudaStream_t st);
+void launch_final_atweights_mx(const HostBatch& hb, cudaStream_t st, int model, int use_old);
 
 extern long long g_launch_count;
 

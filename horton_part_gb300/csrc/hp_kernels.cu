@@ -54,10 +54,10 @@ __device__ __forceinline__ int point_of(const JobDev& J, int tile, int i) {
 }
 
 // Warp sum over tiles with a fixed lane order (deterministic).
-__device__ __forceinline__ double warp_tile_sum(const double* p, int ntile) {
+__device__ __forceinline__ double warp_tile_sum(const JobDev& J, const double* p, int ntile) {
   const int lane = threadIdx.x & 31;
   double s = 0.0;
-  for (int t = lane; t < ntile; t += 32) s += p[t];
+  for (int t = lane; t < ntile; t += 32) s += partial_value(J, p + t);
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
   return s;
@@ -138,7 +138,7 @@ __global__ void __launch_bounds__(kThreads) k_nelec(Batch bt) {
     if (p < J.npoint) acc += J.w[p] * J.rho[p];
   }
   const double s = block_sum1(acc, red);
-  if (threadIdx.x == 0) J.jpart[(size_t)QJ_NELEC * J.ntile + tile] = s;
+  if (threadIdx.x == 0) store_partial(J, J.jpart + (size_t)QJ_NELEC * J.ntile + tile, s);
 }
 
 // Integrated density; basis schemes rescale the initial populations to it
@@ -146,7 +146,7 @@ __global__ void __launch_bounds__(kThreads) k_nelec(Batch bt) {
 __global__ void k_init_params(Batch bt) {
   int local;
   const JobDev& J = decode_local(bt, local);
-  const double nelec = warp_tile_sum(J.jpart + (size_t)QJ_NELEC * J.ntile, J.ntile);
+  const double nelec = warp_tile_sum(J, J.jpart + (size_t)QJ_NELEC * J.ntile, J.ntile);
   if ((threadIdx.x & 31) != 0) return;
   J.mail->d[MD_NELEC] = nelec;
   if (J.scheme != SCHEME_MBIS) {
@@ -166,23 +166,22 @@ __global__ void k_copy_old(Batch bt) {
 // stockholder weights
 // ---------------------------------------------------------------------------
 
+// One block per kThreads points (launch kind K_POINT1).
 template <typename T, int MODEL>
 __global__ void __launch_bounds__(kThreads) k_promol(Batch bt) {
-  int tile;
-  const JobDev& J = decode_local(bt, tile);
-  for (int i = 0; i < J.ppt; ++i) {
-    const int p = point_of(J, tile, i);
-    if (p >= J.npoint) continue;
-    double promol = 0.0;
-    for (int a = 0; a < J.natom; ++a) {
-      const T r = Dist<T>::r(J, p, a);
-      const double pro = (double)proatom<T, MODEL>(J, a, J.propars, r);
-      J.rhoa[(size_t)a * J.npoint + p] = pro;
-      promol += pro;
-      promol += 1e-100;
-    }
-    J.promol[p] = promol;
+  int blk;
+  const JobDev& J = decode_local(bt, blk);
+  const int p = blk * kThreads + threadIdx.x;
+  if (p >= J.npoint) return;
+  double promol = 0.0;
+  for (int a = 0; a < J.natom; ++a) {
+    const T r = Dist<T>::r(J, p, a);
+    const double pro = (double)proatom<T, MODEL>(J, a, J.propars, r);
+    J.rhoa[(size_t)a * J.npoint + p] = pro;
+    promol += pro;
+    promol += 1e-100;
   }
+  J.promol[p] = promol;
 }
 
 __global__ void __launch_bounds__(kThreads) k_atweights(Batch bt) {
@@ -254,36 +253,48 @@ __global__ void __launch_bounds__(kThreads) k_change(Batch bt) {
   if (threadIdx.x == 0) apart_ptr(J, at.atom, QA_CHANGE)[at.tile] = s;
 }
 
-// One warp per job: change, entropy, charges (with_charges) and the
-// history row (core/iterstock.py:172-188).
-__global__ void k_outer_finish(Batch bt, int with_charges) {
+// One block per job: change, entropy, charges (with_charges) and the
+// history row (core/iterstock.py:172-188). Warps sum atoms' tiles in
+// parallel; thread 0 adds the atoms in order (deterministic).
+__global__ void __launch_bounds__(kThreads) k_outer_finish(Batch bt, int with_charges) {
+  __shared__ double ent_s;
+  __shared__ double change_s;
   int local;
   const JobDev& J = decode_local(bt, local);
-  const int lane = threadIdx.x & 31;
-  double msd = 0.0;
-  for (int a = 0; a < J.natom; ++a) msd += warp_tile_sum(apart_ptr(J, a, QA_CHANGE), J.ntile);
-  const double ent = warp_tile_sum(J.jpart + (size_t)QJ_ENTROPY * J.ntile, J.ntile);
-  if (with_charges) {
-    for (int a = 0; a < J.natom; ++a) {
-      const double pop = warp_tile_sum(apart_ptr(J, a, QA_POP), J.ntile);
-      if (lane == 0) J.charges[a] = J.zpseudo[a] - pop;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int it = J.mail->i[MI_ITER];
+  for (int a = warp; a < J.natom; a += kWarps) {
+    const double s = warp_tile_sum(J, apart_ptr(J, a, QA_CHANGE), J.ntile);
+    const double pop = with_charges ? warp_tile_sum(J, apart_ptr(J, a, QA_POP), J.ntile) : 0.0;
+    if (lane == 0) {
+      J.atom_out[a * AO_COUNT + AO_CHANGE] = s;
+      if (with_charges) J.charges[a] = J.zpseudo[a] - pop;
     }
   }
-  __syncwarp();
-  const int it = J.mail->i[MI_ITER];
-  const double change = sqrt(msd);
-  if (it < J.maxiter) {
-    for (int i = lane; i < J.nparam; i += 32) J.hist_propars[(size_t)it * J.nparam + i] = J.propars[i];
-    if (with_charges)
-      for (int a = lane; a < J.natom; a += 32) J.hist_charges[(size_t)it * J.natom + a] = J.charges[a];
+  if (warp == 0) {
+    const double ent = warp_tile_sum(J, J.jpart + (size_t)QJ_ENTROPY * J.ntile, J.ntile);
+    if (lane == 0) ent_s = ent;
   }
-  __syncwarp();
-  if (lane == 0) {
-    J.mail->d[MD_CHANGE] = change;
-    J.mail->d[MD_ENTROPY] = ent;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double msd = 0.0;
+    for (int a = 0; a < J.natom; ++a) msd += J.atom_out[a * AO_COUNT + AO_CHANGE];
+    change_s = sqrt(msd);
+  }
+  __syncthreads();
+  if (it < J.maxiter) {
+    for (int i = threadIdx.x; i < J.nparam; i += kThreads)
+      J.hist_propars[(size_t)it * J.nparam + i] = J.propars[i];
+    if (with_charges)
+      for (int a = threadIdx.x; a < J.natom; a += kThreads)
+        J.hist_charges[(size_t)it * J.natom + a] = J.charges[a];
+  }
+  if (threadIdx.x == 0) {
+    J.mail->d[MD_CHANGE] = change_s;
+    J.mail->d[MD_ENTROPY] = ent_s;
     if (it < J.maxiter) {
-      J.hist_ent[it] = ent;
-      J.hist_chg[it] = change;
+      J.hist_ent[it] = ent_s;
+      J.hist_chg[it] = change_s;
     }
     J.mail->i[MI_ITER] = it + 1;
   }
@@ -294,9 +305,19 @@ __global__ void k_charges(Batch bt) {
   int local;
   const JobDev& J = decode_local(bt, local);
   for (int a = 0; a < J.natom; ++a) {
-    const double pop = warp_tile_sum(apart_ptr(J, a, QA_POP), J.ntile);
+    const double pop = warp_tile_sum(J, apart_ptr(J, a, QA_POP), J.ntile);
     if ((threadIdx.x & 31) == 0) J.charges[a] = J.zpseudo[a] - pop;
   }
+}
+
+// Mixed precision only: the inner change of FP32-evaluated pro-atoms has a
+// noise floor (about 1e-9 of the pro-atom's L2 norm). An inner solve whose
+// change has reached the floor region (below 1000 x threshold) and stopped
+// decreasing (>= 0.9 x the previous change) is taken as converged.
+__device__ __forceinline__ bool mixed_stalled(const JobDev& J, int a, double change) {
+  if (!J.mixed) return false;
+  const double prev = J.atom_out[a * AO_COUNT + AO_INNER_CHANGE];
+  return change < 1e3 * J.inner_threshold && change >= 0.9 * prev;
 }
 
 __global__ void k_count_active(Batch bt) {
@@ -320,7 +341,10 @@ __global__ void k_inner_init(Batch bt) {
   for (int a = threadIdx.x; a < J.natom; a += blockDim.x) {
     J.active[a] = 1;
     J.inner_it[a] = 0;
+    J.atom_out[a * AO_COUNT + AO_INNER_CHANGE] = 1e300;
   }
+  if (J.mixed)
+    for (int s = threadIdx.x; s < J.nshell; s += blockDim.x) fill_fco(J, s, J.propars, J.propars);
   if (threadIdx.x == 0) {
     J.mail->i[MI_NACTIVE] = J.natom;
     J.mail->d[MD_INNER_TOTAL] = 0.0;
@@ -400,8 +424,8 @@ __global__ void k_mbis_update(Batch bt) {
   const int lane = threadIdx.x & 31;
   const int nsh = J.shell_off[a + 1] - J.shell_off[a];
   double m[2 * kMbisMaxShell];
-  for (int q = 0; q < 2 * nsh; ++q) m[q] = warp_tile_sum(apart_ptr(J, a, QA_INNER + q), J.ntile);
-  const double chg2 = warp_tile_sum(apart_ptr(J, a, QA_INNER + kMbisQ - 1), J.ntile);
+  for (int q = 0; q < 2 * nsh; ++q) m[q] = warp_tile_sum(J, apart_ptr(J, a, QA_INNER + q), J.ntile);
+  const double chg2 = warp_tile_sum(J, apart_ptr(J, a, QA_INNER + kMbisQ - 1), J.ntile);
   if (lane != 0) return;
   const int it = J.inner_it[a];
   const double change = (it == 0) ? 1e100 : sqrt(chg2);
@@ -413,7 +437,7 @@ __global__ void k_mbis_update(Batch bt) {
     nw[2 * k] = m[2 * k];
     nw[2 * k + 1] = 3.0 * m[2 * k] / m[2 * k + 1];
   }
-  const bool conv = change < J.inner_threshold;
+  const bool conv = change < J.inner_threshold || mixed_stalled(J, a, change);
   if (conv || it + 1 >= J.inner_maxiter) {
     for (int q = 0; q < 2 * nsh; ++q) pr[q] = nw[q];
     J.active[a] = 0;
@@ -426,6 +450,9 @@ __global__ void k_mbis_update(Batch bt) {
       pc[q] = nw[q];
     }
     J.inner_it[a] = it + 1;
+    J.atom_out[a * AO_COUNT + AO_INNER_CHANGE] = change;
+    if (J.mixed)
+      for (int s = J.shell_off[a]; s < J.shell_off[a + 1]; ++s) fill_fco(J, s, J.cur, J.prev);
   }
 }
 
@@ -433,7 +460,6 @@ __global__ void k_mbis_update(Batch bt) {
 // GISA (gisa.py:257-279, 348-421)
 // ---------------------------------------------------------------------------
 
-constexpr int kBasisQ = kMaxShells + 2;
 
 // q-vector moments sum_p w g_k rho_a (unit-population shells).
 template <typename T>
@@ -462,147 +488,179 @@ __global__ void __launch_bounds__(kThreads) k_basis_qvec(Batch bt) {
   if (threadIdx.x < nsh) apart_ptr(J, at.atom, QA_INNER + threadIdx.x)[at.tile] = out[threadIdx.x];
 }
 
-// Exact primal active-set QP on the simplex {x >= 0, sum x = total}
-// (Nocedal & Wright, Algorithm 16.3), one thread. Solves
-//   min 1/2 x^T P x + q^T x.
-__device__ bool qp_simplex_nonneg(const double* P, const double* q, double total, int n,
-                                  double* x) {
-  bool work[kMaxShells];
-  double g[kMaxShells], p[kMaxShells];
-  double kkt[(kMaxShells + 1) * (kMaxShells + 1)];
-  double rhs[kMaxShells + 1];
-  int idx[kMaxShells];
-  for (int i = 0; i < n; ++i) {
-    x[i] = total / n;
-    work[i] = false;
-  }
-  for (int iter = 0; iter < 200; ++iter) {
-    int nf = 0;
-    for (int i = 0; i < n; ++i)
-      if (!work[i]) idx[nf++] = i;
-    for (int i = 0; i < n; ++i) {
-      double s = q[i];
-      for (int j = 0; j < n; ++j) s += P[i * n + j] * x[j];
-      g[i] = s;
-    }
-    const int m = nf + 1;
-    for (int r = 0; r < nf; ++r) {
-      for (int c = 0; c < nf; ++c) kkt[r * m + c] = P[idx[r] * n + idx[c]];
-      kkt[r * m + nf] = 1.0;
-      kkt[nf * m + r] = 1.0;
-      rhs[r] = -g[idx[r]];
-    }
-    kkt[nf * m + nf] = 0.0;
-    rhs[nf] = 0.0;
-    // Gaussian elimination with partial pivoting.
-    for (int c = 0; c < m; ++c) {
-      int piv = c;
-      double best = fabs(kkt[c * m + c]);
-      for (int r = c + 1; r < m; ++r)
-        if (fabs(kkt[r * m + c]) > best) {
-          best = fabs(kkt[r * m + c]);
-          piv = r;
-        }
-      if (best == 0.0) return false;
-      if (piv != c) {
-        for (int k = 0; k < m; ++k) {
-          const double t = kkt[c * m + k];
-          kkt[c * m + k] = kkt[piv * m + k];
-          kkt[piv * m + k] = t;
-        }
-        const double t = rhs[c];
-        rhs[c] = rhs[piv];
-        rhs[piv] = t;
-      }
-      for (int r = c + 1; r < m; ++r) {
-        const double f = kkt[r * m + c] / kkt[c * m + c];
-        if (f == 0.0) continue;
-        for (int k = c; k < m; ++k) kkt[r * m + k] -= f * kkt[c * m + k];
-        rhs[r] -= f * rhs[c];
-      }
-    }
-    for (int r = m - 1; r >= 0; --r) {
-      double v = rhs[r];
-      for (int k = r + 1; k < m; ++k) v -= kkt[r * m + k] * rhs[k];
-      rhs[r] = v / kkt[r * m + r];
-    }
-    for (int i = 0; i < n; ++i) p[i] = 0.0;
-    for (int r = 0; r < nf; ++r) p[idx[r]] = rhs[r];
-    const double lam = rhs[nf];
-    double pmax = 0.0, xmax = 1.0;
-    for (int i = 0; i < n; ++i) {
-      pmax = fmax(pmax, fabs(p[i]));
-      xmax = fmax(xmax, fabs(x[i]));
-    }
-    if (pmax <= 1e-14 * xmax) {
-      int jmin = -1;
-      double mumin = -1e-14;
-      for (int i = 0; i < n; ++i)
-        if (work[i]) {
-          const double mu = g[i] + lam;
-          if (mu < mumin) {
-            mumin = mu;
-            jmin = i;
-          }
-        }
-      if (jmin < 0) return true;
-      work[jmin] = false;
-      continue;
-    }
-    double alpha = 1.0;
-    int block = -1;
-    for (int i = 0; i < n; ++i)
-      if (!work[i] && p[i] < 0.0) {
-        const double a = -x[i] / p[i];
-        if (a < alpha) {
-          alpha = a;
-          block = i;
-        }
-      }
-    for (int i = 0; i < n; ++i) x[i] += alpha * p[i];
-    if (block >= 0) {
-      x[block] = 0.0;
-      work[block] = true;
-    }
-  }
-  return false;
+__device__ __forceinline__ double warp_sum_d(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
 }
 
-// One warp per atom: P (twice the Gaussian overlap), q, QP.
+__device__ __forceinline__ double warp_max_d(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+
+// Warp minimum with the lowest lane as tie-break; returns the winning lane.
+__device__ __forceinline__ int warp_argmin_d(double v, double& vmin) {
+  int idx = threadIdx.x & 31;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const double ov = __shfl_xor_sync(0xffffffffu, v, o);
+    const int oi = __shfl_xor_sync(0xffffffffu, idx, o);
+    if (ov < v || (ov == v && oi < idx)) {
+      v = ov;
+      idx = oi;
+    }
+  }
+  vmin = v;
+  return idx;
+}
+
+// One warp per atom: the GISA quadratic program (gisa.py:348-421)
+//   min 1/2 x^T P x + q^T x,  x >= 0,  sum x = int w rho_a,
+// P precomputed per atom (twice the Gaussian overlap), q_k = -2 int w g_k rho_a.
+// Exact primal active-set method (Nocedal & Wright, Algorithm 16.3) started at
+// x = total/K, the same iteration as the oracle's qp_simplex_nonneg. Lane k
+// owns variable k; the equality-constrained step on the free set solves
+// P_FF u = -g_F and P_FF v = 1 with one Cholesky factor, lambda = sum u / sum v,
+// p = u - lambda v.
 __global__ void k_gisa_qp(Batch bt) {
+  __shared__ double Ps[kMaxShells][kMaxShells + 1];
+  __shared__ double M[kMaxShells][kMaxShells + 1];
+  __shared__ double rhs[2][kMaxShells];
+  __shared__ int bad;
   int a;
   const JobDev& J = decode_local(bt, a);
   const int lane = threadIdx.x & 31;
   const int s0 = J.shell_off[a];
   const int n = J.shell_off[a + 1] - s0;
-  double q[kMaxShells];
-  for (int k = 0; k < n; ++k) q[k] = -2.0 * warp_tile_sum(apart_ptr(J, a, QA_INNER + k), J.ntile);
-  const double pop = warp_tile_sum(apart_ptr(J, a, QA_POP), J.ntile);
-  if (lane != 0) return;
-  double P[kMaxShells * kMaxShells];
-  const double c = 2.0 / pow(3.14159265358979323846, 1.5);
-  for (int k = 0; k < n; ++k)
-    for (int l = 0; l < n; ++l) {
-      const double ak = J.sh_alpha[s0 + k], al = J.sh_alpha[s0 + l];
-      P[k * n + l] = c * pow(ak * al, 1.5) / pow(ak + al, 1.5);
-    }
-  for (int k = 0; k < n; ++k)
-    for (int l = 0; l < k; ++l) {
-      const double v = 0.5 * (P[k * n + l] + P[l * n + k]);
-      P[k * n + l] = v;
-      P[l * n + k] = v;
-    }
-  double x[kMaxShells];
-  if (!qp_simplex_nonneg(P, q, pop, n, x)) atomicOr(&J.mail->i[MI_ERR], E_QP);
-  double s = 0.0;
-  bool neg = false;
+  double qi = 0.0;
   for (int k = 0; k < n; ++k) {
-    J.propars[J.par_off[a] + k] = x[k];
-    s += x[k];
-    neg |= x[k] < J.negative_cutoff;
+    const double v = -2.0 * warp_tile_sum(J, apart_ptr(J, a, QA_INNER + k), J.ntile);
+    if (lane == k) qi = v;
   }
-  if (fabs(s - pop) > J.population_cutoff) atomicOr(&J.mail->i[MI_WARN], W_POPULATION);
-  if (neg) atomicOr(&J.mail->i[MI_WARN], W_NEG_PARS);
+  const double pop = warp_tile_sum(J, apart_ptr(J, a, QA_POP), J.ntile);
+  const double* P = J.qp_p + J.qp_off[a];
+  for (int e = lane; e < n * n; e += 32) Ps[e / n][e % n] = P[e];
+  if (lane == 0) bad = 0;
+  __syncwarp();
+  const bool mine = lane < n;
+  // Warm start: the previous outer iteration's solution rescaled to the new
+  // population, with its zero populations in the working set. The QP is
+  // strictly convex, so the optimum does not depend on the start; the active
+  // set rarely changes between outer iterations, so one or two steps finish.
+  const double prev = mine ? J.propars[J.par_off[a] + lane] : 0.0;
+  const double psum = warp_sum_d((mine && prev > 0.0) ? prev : 0.0);
+  double x;
+  bool work;
+  if (psum > 0.0) {
+    x = (mine && prev > 0.0) ? prev * (pop / psum) : 0.0;
+    work = mine && !(prev > 0.0);
+  } else {
+    x = mine ? pop / n : 0.0;
+    work = false;
+  }
+  bool done = false;
+  bool at_min = false;  // x minimises the objective on the current free set
+  for (int iter = 0; iter < 200 && !done; ++iter) {
+    double g = 0.0;
+    if (mine) {
+      g = qi;
+      for (int j = 0; j < n; ++j) g += Ps[lane][j] * __shfl_sync(0xffffffffu, x, j);
+    } else {
+      for (int j = 0; j < n; ++j) (void)__shfl_sync(0xffffffffu, x, j);
+    }
+    const unsigned fmask = __ballot_sync(0xffffffffu, mine && !work);
+    const int nf = __popc(fmask);
+    const bool fr = (fmask >> lane) & 1u;
+    const int rank = __popc(fmask & ((1u << lane) - 1u));
+    if (at_min) {
+      // After a full (unblocked) step x is the subspace minimiser: the
+      // multiplier of sum x = total is lambda = -mean(g_F); release the
+      // most negative bound multiplier g_i + lambda, or stop. (Testing the
+      // next step for zero instead would sit below the rounding noise of
+      // the Cholesky solve when P is ill-conditioned.)
+      const double lam0 = -warp_sum_d(fr ? g : 0.0) / (double)(nf > 0 ? nf : 1);
+      const double gmax = warp_max_d(mine ? fabs(g) : 0.0);
+      double mumin;
+      const int jmin = warp_argmin_d((mine && work) ? g + lam0 : 1e300, mumin);
+      if (!(mumin < -1e-12 * fmax(1.0, gmax))) {
+        done = true;
+      } else {
+        if (lane == jmin) work = false;
+        at_min = false;
+      }
+      continue;
+    }
+    if (fr)
+      for (int j = 0; j < n; ++j)
+        if ((fmask >> j) & 1u) M[rank][__popc(fmask & ((1u << j) - 1u))] = Ps[lane][j];
+    __syncwarp();
+    for (int k = 0; k < nf; ++k) {  // right-looking Cholesky, lane r owns row r
+      if (lane == k) {
+        const double d = M[k][k];
+        if (!(d > 0.0)) bad = 1;
+        M[k][k] = sqrt(fmax(d, 1e-300));
+      }
+      __syncwarp();
+      if (lane > k && lane < nf) M[lane][k] /= M[k][k];
+      __syncwarp();
+      if (lane > k && lane < nf)
+        for (int j = k + 1; j <= lane; ++j) M[lane][j] -= M[lane][k] * M[j][k];
+      __syncwarp();
+    }
+    if (fr) {
+      rhs[0][rank] = -g;
+      rhs[1][rank] = 1.0;
+    }
+    __syncwarp();
+    if (lane < 2) {  // two triangular solves, one per lane
+      double* b = rhs[lane];
+      for (int i = 0; i < nf; ++i) {
+        double v = b[i];
+        for (int j = 0; j < i; ++j) v -= M[i][j] * b[j];
+        b[i] = v / M[i][i];
+      }
+      for (int i = nf - 1; i >= 0; --i) {
+        double v = b[i];
+        for (int j = i + 1; j < nf; ++j) v -= M[j][i] * b[j];
+        b[i] = v / M[i][i];
+      }
+    }
+    __syncwarp();
+    const double u = fr ? rhs[0][rank] : 0.0;
+    const double v = fr ? rhs[1][rank] : 0.0;
+    const double lam = warp_sum_d(u) / warp_sum_d(v);
+    const double p = fr ? u - lam * v : 0.0;
+    const double pmax = warp_max_d(fabs(p));
+    const double xmax = warp_max_d(mine ? fmax(1.0, fabs(x)) : 1.0);
+    if (pmax <= 1e-14 * xmax) {
+      at_min = true;
+      continue;
+    }
+    double amin;
+    const int blk = warp_argmin_d((fr && p < 0.0) ? -x / p : 1e300, amin);
+    const double alpha = amin < 1.0 ? amin : 1.0;
+    x += alpha * p;
+    if (amin < 1.0) {
+      if (lane == blk) {
+        x = 0.0;
+        work = true;
+      }
+    } else {
+      at_min = true;
+    }
+  }
+  if (!done || bad) {
+    if (lane == 0) atomicOr(&J.mail->i[MI_ERR], E_QP);
+  }
+  if (mine) J.propars[J.par_off[a] + lane] = x;
+  const double s = warp_sum_d(mine ? x : 0.0);
+  const unsigned neg = __ballot_sync(0xffffffffu, mine && x < J.negative_cutoff);
+  if (lane == 0) {
+    if (fabs(s - pop) > J.population_cutoff) atomicOr(&J.mail->i[MI_WARN], W_POPULATION);
+    if (neg) atomicOr(&J.mail->i[MI_WARN], W_NEG_PARS);
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -665,16 +723,16 @@ __global__ void k_lisa_sc_update(Batch bt) {
   const int lane = threadIdx.x & 31;
   const int nsh = J.shell_off[a + 1] - J.shell_off[a];
   double m[kMaxShells];
-  for (int k = 0; k < nsh; ++k) m[k] = warp_tile_sum(apart_ptr(J, a, QA_INNER + k), J.ntile);
-  const double chg2 = warp_tile_sum(apart_ptr(J, a, QA_INNER + Q - 1), J.ntile);
-  const double pop = warp_tile_sum(apart_ptr(J, a, QA_POP), J.ntile);
+  for (int k = 0; k < nsh; ++k) m[k] = warp_tile_sum(J, apart_ptr(J, a, QA_INNER + k), J.ntile);
+  const double chg2 = warp_tile_sum(J, apart_ptr(J, a, QA_INNER + Q - 1), J.ntile);
+  const double pop = warp_tile_sum(J, apart_ptr(J, a, QA_POP), J.ntile);
   if (lane != 0) return;
   const int it = J.inner_it[a];
   const double change = (it == 0) ? 1e100 : sqrt(chg2);
   double* pc = J.cur + J.par_off[a];
   double* pp = J.prev + J.par_off[a];
   double* pr = J.propars + J.par_off[a];
-  const bool conv = change < J.inner_threshold;
+  const bool conv = change < J.inner_threshold || mixed_stalled(J, a, change);
   if (conv || it + 1 >= J.inner_maxiter) {
     double s = 0.0;
     for (int k = 0; k < nsh; ++k) {
@@ -692,6 +750,9 @@ __global__ void k_lisa_sc_update(Batch bt) {
       pc[k] = m[k];
     }
     J.inner_it[a] = it + 1;
+    J.atom_out[a * AO_COUNT + AO_INNER_CHANGE] = change;
+    if (J.mixed)
+      for (int s = J.shell_off[a]; s < J.shell_off[a + 1]; ++s) fill_fco(J, s, J.cur, J.prev);
   }
 }
 
@@ -792,8 +853,8 @@ __global__ void k_lisa_newton_update(Batch bt) {
   const int nsh = J.shell_off[a + 1] - J.shell_off[a];
   const int nq = nsh + nsh * (nsh + 1) / 2;
   double v[kNtQ];
-  for (int q = 0; q < nq + 2; ++q) v[q] = warp_tile_sum(apart_ptr(J, a, QA_INNER + q), J.ntile);
-  const double pop = warp_tile_sum(apart_ptr(J, a, QA_POP), J.ntile);
+  for (int q = 0; q < nq + 2; ++q) v[q] = warp_tile_sum(J, apart_ptr(J, a, QA_INNER + q), J.ntile);
+  const double pop = warp_tile_sum(J, apart_ptr(J, a, QA_POP), J.ntile);
   if (lane != 0) return;
   const int it = J.inner_it[a];
   const double change = (it == 0) ? 1e100 : sqrt(v[nq]);
@@ -1260,7 +1321,7 @@ __global__ void __launch_bounds__(kThreads) k_glisa_change(Batch bt) {
 __global__ void k_glisa_check(Batch bt) {
   int local;
   const JobDev& J = decode_local(bt, local);
-  const double neg = warp_tile_sum(J.jpart + (size_t)QJ_NEG * J.ntile, J.ntile);
+  const double neg = warp_tile_sum(J, J.jpart + (size_t)QJ_NEG * J.ntile, J.ntile);
   if ((threadIdx.x & 31) != 0) return;
   if (neg > 0.0) atomicOr(&J.mail->i[MI_ERR], E_NEG_DENSITY);
   double s = 0.0;
@@ -1289,40 +1350,29 @@ void launch_nelec(const HostBatch& hb, cudaStream_t st) {
 
 void launch_copy_old(const HostBatch& hb, cudaStream_t st) { HP_LAUNCH(k_copy_old, K_JOB, 128); }
 
+// Mixed-precision variants live in hp_mixed.cu.
 void launch_promol(const HostBatch& hb, cudaStream_t st, int mixed, int model) {
-  if (mixed) {
-    if (model == MODEL_MBIS) HP_LAUNCH((k_promol<float, MODEL_MBIS>), K_POINT, kThreads);
-    else HP_LAUNCH((k_promol<float, MODEL_BASIS>), K_POINT, kThreads);
-  } else {
-    if (model == MODEL_MBIS) HP_LAUNCH((k_promol<double, MODEL_MBIS>), K_POINT, kThreads);
-    else HP_LAUNCH((k_promol<double, MODEL_BASIS>), K_POINT, kThreads);
-  }
+  if (mixed) return launch_promol_mx(hb, st, model);
+  if (model == MODEL_MBIS) HP_LAUNCH((k_promol<double, MODEL_MBIS>), K_POINT1, kThreads);
+  else HP_LAUNCH((k_promol<double, MODEL_BASIS>), K_POINT1, kThreads);
   HP_LAUNCH(k_atweights, K_ATOM_TILE, kThreads);
 }
 
 void launch_final_atweights(const HostBatch& hb, cudaStream_t st, int mixed, int model,
                             int use_old) {
-  if (mixed) {
-    if (model == MODEL_MBIS) HP_LAUNCH((k_final_atweights<float, MODEL_MBIS>), K_ATOM_TILE, kThreads, use_old);
-    else HP_LAUNCH((k_final_atweights<float, MODEL_BASIS>), K_ATOM_TILE, kThreads, use_old);
-  } else {
-    if (model == MODEL_MBIS) HP_LAUNCH((k_final_atweights<double, MODEL_MBIS>), K_ATOM_TILE, kThreads, use_old);
-    else HP_LAUNCH((k_final_atweights<double, MODEL_BASIS>), K_ATOM_TILE, kThreads, use_old);
-  }
+  if (mixed) return launch_final_atweights_mx(hb, st, model, use_old);
+  if (model == MODEL_MBIS) HP_LAUNCH((k_final_atweights<double, MODEL_MBIS>), K_ATOM_TILE, kThreads, use_old);
+  else HP_LAUNCH((k_final_atweights<double, MODEL_BASIS>), K_ATOM_TILE, kThreads, use_old);
 }
 
 void launch_change(const HostBatch& hb, cudaStream_t st, int mixed, int model) {
-  if (mixed) {
-    if (model == MODEL_MBIS) HP_LAUNCH((k_change<float, MODEL_MBIS>), K_ATOM_TILE, kThreads);
-    else HP_LAUNCH((k_change<float, MODEL_BASIS>), K_ATOM_TILE, kThreads);
-  } else {
-    if (model == MODEL_MBIS) HP_LAUNCH((k_change<double, MODEL_MBIS>), K_ATOM_TILE, kThreads);
-    else HP_LAUNCH((k_change<double, MODEL_BASIS>), K_ATOM_TILE, kThreads);
-  }
+  if (mixed) return launch_change_mx(hb, st, model);
+  if (model == MODEL_MBIS) HP_LAUNCH((k_change<double, MODEL_MBIS>), K_ATOM_TILE, kThreads);
+  else HP_LAUNCH((k_change<double, MODEL_BASIS>), K_ATOM_TILE, kThreads);
 }
 
 void launch_outer_finish(const HostBatch& hb, cudaStream_t st, int with_charges) {
-  HP_LAUNCH(k_outer_finish, K_JOB, 32, with_charges);
+  HP_LAUNCH(k_outer_finish, K_JOB, kThreads, with_charges);
 }
 
 void launch_charges(const HostBatch& hb, cudaStream_t st) { HP_LAUNCH(k_charges, K_JOB, 32); }
@@ -1334,30 +1384,31 @@ void launch_count_active(const HostBatch& hb, cudaStream_t st) {
 }
 
 void launch_mbis_inner(const HostBatch& hb, cudaStream_t st, int mixed) {
-  if (mixed) HP_LAUNCH(k_mbis_inner<float>, K_ATOM_TILE, kThreads);
+  if (mixed) launch_mbis_inner_mx(hb, st);
   else HP_LAUNCH(k_mbis_inner<double>, K_ATOM_TILE, kThreads);
   HP_LAUNCH(k_mbis_update, K_ATOM, 32);
 }
 
 void launch_gisa(const HostBatch& hb, cudaStream_t st, int mixed) {
-  if (mixed) HP_LAUNCH(k_basis_qvec<float>, K_ATOM_TILE, kThreads);
+  if (mixed) launch_basis_qvec_mx(hb, st);
   else HP_LAUNCH(k_basis_qvec<double>, K_ATOM_TILE, kThreads);
   HP_LAUNCH(k_gisa_qp, K_ATOM, 32);
 }
 
 void launch_lisa_sc_inner(const HostBatch& hb, cudaStream_t st, int mixed) {
-  if (mixed) HP_LAUNCH(k_lisa_sc_inner<float>, K_ATOM_TILE, kThreads);
+  if (mixed) launch_lisa_sc_inner_mx(hb, st);
   else HP_LAUNCH(k_lisa_sc_inner<double>, K_ATOM_TILE, kThreads);
   HP_LAUNCH(k_lisa_sc_update, K_ATOM, 32);
 }
 
+// Newton keeps FP64 evaluation (its Hessian needs it); mixed jobs are
+// rejected for this solver at job creation.
 void launch_lisa_newton_inner(const HostBatch& hb, cudaStream_t st, int mixed, int modified) {
-  if (mixed) HP_LAUNCH(k_lisa_newton_inner<float>, K_ATOM_TILE, kThreads);
-  else HP_LAUNCH(k_lisa_newton_inner<double>, K_ATOM_TILE, kThreads);
+  (void)mixed;
+  HP_LAUNCH(k_lisa_newton_inner<double>, K_ATOM_TILE, kThreads);
   HP_LAUNCH(k_lisa_newton_update, K_ATOM, 32);
   if (modified) {
-    if (mixed) HP_LAUNCH(k_lisa_ls<float>, K_ATOM_TILE, kThreads);
-    else HP_LAUNCH(k_lisa_ls<double>, K_ATOM_TILE, kThreads);
+    HP_LAUNCH(k_lisa_ls<double>, K_ATOM_TILE, kThreads);
     HP_LAUNCH(k_lisa_ls_pick, K_ATOM, 32);
   }
 }

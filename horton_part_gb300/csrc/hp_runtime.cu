@@ -86,6 +86,8 @@ struct hp_job {
   double evals = 0.0;
   double inner_total = 0.0;
   bool converged = false;
+  double prev_change = 1e300;
+  int polish_iters = 0;  // FP64 outer iterations after a mixed-precision stall
 };
 
 namespace {
@@ -138,6 +140,7 @@ void prof_collect(hp_ctx* ctx) {
 int blocks_for(const JobDev& J, int kind) {
   switch (kind) {
     case K_POINT: return J.ntile;
+    case K_POINT1: return (J.npoint + kThreads - 1) / kThreads;
     case K_ATOM_TILE: return J.natom * J.ntile;
     case K_ATOM: return J.natom;
     case K_JOB: return 1;
@@ -238,7 +241,7 @@ int job_init(hp_ctx* ctx, const std::vector<hp_job*>& jobs, const HostBatch& hb)
 // One outer iteration of MBIS / GISA / aLISA for a homogeneous batch.
 int step_iterstock(hp_ctx* ctx, const std::vector<hp_job*>& jobs, const HostBatch& hb) {
   const hp_job* j0 = jobs[0];
-  const int mixed = j0->desc.precision == HP_PRECISION_MIXED;
+  const int mixed = j0->dev.mixed;  // current phase (a mixed job may finish in FP64)
   const int model = model_of(j0);
   cudaStream_t st = ctx->stream;
   launch_copy_old(hb, st);
@@ -295,6 +298,7 @@ int step_iterstock(hp_ctx* ctx, const std::vector<hp_job*>& jobs, const HostBatc
     const double a = (double)j->dev.natom;
     const double inner_evals = j->desc.scheme == HP_SCHEME_GISA ? a : inner;
     j->evals += n * (3.0 * a + inner_evals);
+    if (j->dev.mixed == 0 && j->desc.precision == HP_PRECISION_MIXED) j->polish_iters += 1;
     if (m.i[MI_ERR]) {
       j->status = status_of(m.i[MI_ERR]);
       g_err = err_text(m.i[MI_ERR]);
@@ -302,7 +306,20 @@ int step_iterstock(hp_ctx* ctx, const std::vector<hp_job*>& jobs, const HostBatc
     } else if (j->change < j->desc.threshold || j->niter >= j->desc.maxiter) {
       j->converged = j->change < j->desc.threshold;
       j->done = true;
+    } else if (j->dev.mixed && j->change < 10.0 * j->desc.threshold &&
+               j->change >= j->prev_change) {
+      // the FP32-evaluated outer change went up just above the threshold
+      // (its noise floor): finish in FP64 (every buffer is rewritten by the
+      // next FP64 pass), or stop here with a warning
+      if (j->desc.polish) {
+        j->dev.mixed = 0;
+      } else {
+        j->warnings |= HP_WARN_NOISE_FLOOR;
+        j->converged = true;
+        j->done = true;
+      }
     }
+    j->prev_change = j->change;
   }
   return HP_OK;
 }
@@ -485,6 +502,12 @@ int validate(const hp_job_desc* d) {
     return fail(HP_ERR_UNSUPPORTED, "gLISA solvers on this path: newton, m-newton, sc");
   if (d->linspace_size > 64 || (d->scheme == HP_SCHEME_LISA && d->linspace_size > 32))
     return fail(HP_ERR_UNSUPPORTED, "linspace_size too large");
+  if (d->precision != HP_PRECISION_FP64 && d->precision != HP_PRECISION_MIXED)
+    return fail(HP_ERR_INVALID, "unknown precision");
+  if (d->precision == HP_PRECISION_MIXED &&
+      (d->scheme == HP_SCHEME_GLISA ||
+       (d->scheme == HP_SCHEME_LISA && d->solver != HP_SOLVER_SC && d->solver != HP_SOLVER_DEFAULT)))
+    return fail(HP_ERR_UNSUPPORTED, "mixed precision is available for MBIS, GISA and aLISA sc");
   for (int64_t s = 0; d->scheme != HP_SCHEME_MBIS && s < d->shell_offsets[d->natom]; ++s) {
     if (!(d->shell_orders[s] > 0.0)) return fail(HP_ERR_INVALID, "n must be positive");
     if (d->shell_exponents[s] < 0.0) return fail(HP_ERR_INVALID, "alpha must be non-negative");
@@ -604,7 +627,10 @@ int32_t hp_job_create(hp_ctx* ctx, const hp_job_desc* d, hp_job** out) {
     else if (d->scheme == HP_SCHEME_GISA) solver = HP_SOLVER_QP;
   }
   // tiles: aim for >= 2 * 152 point tiles when the grid is large enough
-  int ppt = (int)std::min<int64_t>(64, std::max<int64_t>(2, (N + kThreads * 304 - 1) / (kThreads * 304)));
+  // (mixed precision: at least 4 points per thread so the per-block
+  // compensated reductions are amortised)
+  const int ppt_min = d->precision == HP_PRECISION_MIXED ? 4 : 2;
+  int ppt = (int)std::min<int64_t>(64, std::max<int64_t>(ppt_min, (N + kThreads * 304 - 1) / (kThreads * 304)));
   const int tile_points = kThreads * ppt;
   const int ntile = (N + tile_points - 1) / tile_points;
   int qa = 2 + std::max(2 * 7 + 1, kMaxShells + 1);
@@ -627,6 +653,22 @@ int32_t hp_job_create(hp_ctx* ctx, const hp_job_desc* d, hp_job** out) {
     add(&J.pxh, 4 * (size_t)N); add(&J.pxl, 4 * (size_t)N);
     add(&J.pyh, 4 * (size_t)N); add(&J.pyl, 4 * (size_t)N);
     add(&J.pzh, 4 * (size_t)N); add(&J.pzl, 4 * (size_t)N);
+    add(&J.wf, 4 * (size_t)N); add(&J.rhof, 4 * (size_t)N); add(&J.promolf, 4 * (size_t)N);
+    add(&J.shf, 4 * 3 * (size_t)S); add(&J.fpar, 4 * 2 * (size_t)S);
+    add(&J.atf, 4 * 6 * (size_t)A);
+    add(&J.fco, 4 * 8 * (size_t)S);
+  }
+  // GISA: per-atom QP matrices, precomputed once (they depend only on exponents)
+  int qp_total = 0;
+  std::vector<int> qp_off_h((size_t)A + 1, 0);
+  for (int a = 0; a < A; ++a) {
+    const int n = d->shell_offsets[a + 1] - d->shell_offsets[a];
+    qp_off_h[a + 1] = qp_off_h[a] + n * n;
+  }
+  qp_total = qp_off_h[A];
+  if (d->scheme == HP_SCHEME_GISA) {
+    add(&J.qp_p, 8 * (size_t)qp_total);
+    add(&J.qp_off, 4 * (size_t)(A + 1));
   }
   add(&J.ax, 8 * (size_t)A); add(&J.ay, 8 * (size_t)A); add(&J.az, 8 * (size_t)A);
   add(&J.zpseudo, 8 * (size_t)A);
@@ -714,12 +756,57 @@ int32_t hp_job_create(hp_ctx* ctx, const hp_job_desc* d, hp_job** out) {
   }
   ok &= up(J.w, d->weights, 8 * (size_t)N) == cudaSuccess;
   ok &= up(J.rho, d->density, 8 * (size_t)N) == cudaSuccess;
+  std::vector<float> wf32, rf32;
+  if (mixed) {
+    wf32.resize((size_t)N);
+    rf32.resize((size_t)N);
+    for (int p = 0; p < N; ++p) {
+      wf32[p] = (float)d->weights[p];
+      rf32[p] = (float)d->density[p];
+    }
+    ok &= up(J.wf, wf32.data(), 4 * (size_t)N) == cudaSuccess;
+    ok &= up(J.rhof, rf32.data(), 4 * (size_t)N) == cudaSuccess;
+  }
   std::vector<double> ac((size_t)A);
   for (int c = 0; c < 3 && ok; ++c) {
     for (int a = 0; a < A; ++a) ac[a] = d->coordinates[(size_t)3 * a + c];
     ok &= up(c == 0 ? J.ax : c == 1 ? J.ay : J.az, ac.data(), 8 * (size_t)A) == cudaSuccess;
   }
   ok &= up(J.zpseudo, d->pseudo_numbers, 8 * (size_t)A) == cudaSuccess;
+  std::vector<float> atf32;
+  if (mixed) {
+    atf32.resize(6 * (size_t)A);
+    for (int a = 0; a < A; ++a)
+      for (int c = 0; c < 3; ++c) {
+        const double x = d->coordinates[(size_t)3 * a + c];
+        const float h = (float)x;
+        atf32[6 * a + 2 * c] = h;
+        atf32[6 * a + 2 * c + 1] = (float)(x - (double)h);
+      }
+    ok &= up(J.atf, atf32.data(), 4 * 6 * (size_t)A) == cudaSuccess;
+  }
+  std::vector<double> qp_h;
+  if (d->scheme == HP_SCHEME_GISA) {
+    // P_kl = 2 / pi^1.5 (a_k a_l)^1.5 / (a_k + a_l)^1.5, symmetrised (gisa.py:387-393)
+    qp_h.resize((size_t)qp_total);
+    for (int a = 0; a < A; ++a) {
+      const int s0 = d->shell_offsets[a], n = d->shell_offsets[a + 1] - s0;
+      double* P = qp_h.data() + qp_off_h[a];
+      for (int k = 0; k < n; ++k)
+        for (int l = 0; l < n; ++l) {
+          const double ak = d->shell_exponents[s0 + k], al = d->shell_exponents[s0 + l];
+          P[k * n + l] = 2.0 / std::pow(M_PI, 1.5) * std::pow(ak * al, 1.5) / std::pow(ak + al, 1.5);
+        }
+      for (int k = 0; k < n; ++k)
+        for (int l = 0; l < k; ++l) {
+          const double v = 0.5 * (P[k * n + l] + P[l * n + k]);
+          P[k * n + l] = v;
+          P[l * n + k] = v;
+        }
+    }
+    ok &= up(J.qp_p, qp_h.data(), 8 * (size_t)qp_total) == cudaSuccess;
+    ok &= up(J.qp_off, qp_off_h.data(), 4 * (size_t)(A + 1)) == cudaSuccess;
+  }
   ok &= up(J.shell_off, d->shell_offsets, 4 * (size_t)(A + 1)) == cudaSuccess;
   std::vector<int> poff((size_t)A + 1);
   for (int a = 0; a <= A; ++a) poff[a] = mbis ? 2 * d->shell_offsets[a] : d->shell_offsets[a];
@@ -735,6 +822,16 @@ int32_t hp_job_create(hp_ctx* ctx, const hp_job_desc* d, hp_job** out) {
   ok &= up(J.sh_order, ord.data(), 8 * (size_t)S) == cudaSuccess;
   ok &= up(J.sh_alpha, alp.data(), 8 * (size_t)S) == cudaSuccess;
   ok &= up(J.sh_pref, pref.data(), 8 * (size_t)S) == cudaSuccess;
+  std::vector<float> shf32;
+  if (mixed) {
+    shf32.resize(3 * (size_t)S);
+    for (int s = 0; s < S; ++s) {
+      shf32[3 * s] = (float)ord[s];
+      shf32[3 * s + 1] = (float)alp[s];
+      shf32[3 * s + 2] = (float)pref[s];
+    }
+    ok &= up(J.shf, shf32.data(), 4 * 3 * (size_t)S) == cudaSuccess;
+  }
   ok &= up(J.propars, d->initial_propars, 8 * (size_t)P) == cudaSuccess;
   ok &= up(J.propars_init, d->initial_propars, 8 * (size_t)P) == cudaSuccess;
   ok &= cudaMemsetAsync(J.apart, 0, 8 * (size_t)A * qa * ntile, st) == cudaSuccess;
@@ -780,7 +877,7 @@ int32_t hp_step(hp_ctx* ctx, hp_job* const* jobs, int32_t njobs, int32_t* n_live
     for (auto& g : groups) {
       const hp_job* h = g[0];
       if (h->desc.scheme == j->desc.scheme && h->dev.solver == j->dev.solver &&
-          h->desc.precision == j->desc.precision) {
+          h->dev.mixed == j->dev.mixed) {
         g.push_back(j);
         placed = true;
         break;
@@ -830,6 +927,9 @@ int32_t hp_job_reset(hp_job* job) {
   job->evals = 0.0;
   job->inner_total = 0.0;
   job->converged = false;
+  job->prev_change = 1e300;
+  job->polish_iters = 0;
+  job->dev.mixed = job->desc.precision == HP_PRECISION_MIXED ? 1 : 0;
   return HP_OK;
 }
 
@@ -871,9 +971,11 @@ int32_t hp_job_info_get(hp_job* job, hp_job_info* out) {
   out->done = job->done ? 1 : 0;
   out->status = job->status;
   out->warnings = job->warnings;
-  out->reserved = job->converged ? 1 : 0;
+  out->converged = job->converged ? 1 : 0;
   out->device_bytes = (int64_t)job->bytes;
   out->point_atom_evals = job->evals;
+  out->polish_iterations = job->polish_iters;
+  out->reserved = 0;
   return HP_OK;
 }
 
@@ -907,7 +1009,16 @@ int32_t hp_job_results_get(hp_job* job, const hp_job_results* r) {
     HP_CK(cudaMemcpy(r->history_entropies, J.hist_ent, 8 * nit, cudaMemcpyDeviceToHost));
   if (r->history_changes && nit)
     HP_CK(cudaMemcpy(r->history_changes, J.hist_chg, 8 * nit, cudaMemcpyDeviceToHost));
-  if (r->promoldens) HP_CK(cudaMemcpy(r->promoldens, J.promol, 8 * N, cudaMemcpyDeviceToHost));
+  if (r->promoldens) {
+    HP_CK(cudaMemcpy(r->promoldens, J.promol, 8 * N, cudaMemcpyDeviceToHost));
+    if (J.mixed) {  // float pairs (hi, lo) -> double, plus 1e-100 per atom as the reference
+      for (size_t p = 0; p < N; ++p) {
+        float pair[2];
+        memcpy(pair, &r->promoldens[p], sizeof(pair));
+        r->promoldens[p] = (double)pair[0] + (double)pair[1] + 1e-100 * (double)A;
+      }
+    }
+  }
   if (r->at_weights) HP_CK(cudaMemcpy(r->at_weights, J.rhoa, 8 * A * N, cudaMemcpyDeviceToHost));
   return HP_OK;
 }

@@ -297,13 +297,14 @@ class GPUStockholderWPart(WPart):
 
     def __init__(self, coordinates, numbers, pseudo_numbers, grid, moldens, spindens=None, lmax=3,
                  logger=None, threshold=1e-6, maxiter=500, inner_threshold=1e-8, grid_type=1,
-                 precision="fp64", context=None, store_at_weights=True, **kwargs):
+                 precision="fp64", context=None, store_at_weights=True, polish=False, **kwargs):
         self._threshold = threshold
         self._inner_threshold = inner_threshold if inner_threshold < threshold else threshold
         self._maxiter = maxiter
         if precision not in ("fp64", "mixed"):
             raise ValueError("precision must be 'fp64' or 'mixed'")
         self._precision = precision
+        self._polish = polish
         self._context = context
         self._store_at_weights = store_at_weights
         self._ranges = None
@@ -346,7 +347,7 @@ class GPUStockholderWPart(WPart):
             grid_type=self.grid_type, threshold=self._threshold,
             inner_threshold=self._inner_threshold, density_cutoff=self.density_cutoff,
             negative_cutoff=self.negative_cutoff, population_cutoff=self.population_cutoff,
-            maxiter=self._maxiter, **self._job_extra())
+            maxiter=self._maxiter, polish=self._polish, **self._job_extra())
 
     def _report_warnings(self, info):
         if info.warnings & _lib.WARN_INNER_NOT_CONVERGED:
@@ -355,6 +356,9 @@ class GPUStockholderWPart(WPart):
             self.logger.warning("The sum of pro-atom parameters is not equal to reference population.")
         if info.warnings & _lib.WARN_NEGATIVE_PARS:
             self.logger.warning("WARNING: Not all pro-atom parameters are positive!")
+        if info.warnings & _lib.WARN_NOISE_FLOOR:
+            self.logger.warning("Mixed precision stopped at its noise floor (change %.3e); "
+                                "pass polish=True to finish in FP64." % info.change)
 
     _inner_warning = "Warning: Inner iteration is not converge!"
 

@@ -83,6 +83,7 @@ typedef enum {
 #define HP_WARN_INNER_NOT_CONVERGED 1u /* mbis.py:162, alisa.py:289 */
 #define HP_WARN_POPULATION 2u          /* utils.py:418-456 */
 #define HP_WARN_NEGATIVE_PARS 4u       /* utils.py:459-488 */
+#define HP_WARN_NOISE_FLOOR 8u         /* mixed precision stopped at its noise floor */
 
 typedef struct hp_ctx hp_ctx;
 typedef struct hp_job hp_job;
@@ -120,7 +121,10 @@ typedef struct {
   int32_t maxiter;        /* outer iterations (gLISA: solver iterations) */
   int32_t inner_maxiter;  /* MBIS 2000, aLISA sc 100000, aLISA newton 10000 */
   int32_t linspace_size;  /* line-search trial count (m-newton) */
-  int32_t reserved;
+  int32_t polish;         /* mixed precision: when the FP32-evaluated outer change
+                             stalls at its noise floor above the threshold,
+                             1 = finish in FP64, 0 = stop there and set
+                             HP_WARN_NOISE_FLOOR */
 } hp_job_desc;
 
 typedef struct {
@@ -133,9 +137,11 @@ typedef struct {
   int32_t done;         /* 1 when converged, hit maxiter or failed */
   int32_t status;       /* hp_status of the job (HP_OK unless it failed) */
   uint32_t warnings;    /* HP_WARN_* bits */
-  int32_t reserved;
+  int32_t converged;    /* 1 when the change fell below the threshold */
   int64_t device_bytes; /* device memory held by the job */
   double point_atom_evals; /* pro-atom evaluations done so far (sum over passes) */
+  int32_t polish_iterations; /* mixed precision: FP64 outer iterations after a stall */
+  int32_t reserved;
 } hp_job_info;
 
 typedef struct {

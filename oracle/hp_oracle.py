@@ -279,10 +279,20 @@ def qp_simplex_nonneg(P, q, total, maxiter=200):
     K = len(q)
     x = np.full(K, total / K)
     work = np.zeros(K, dtype=bool)  # True: x_i fixed at 0
+    at_min = False  # x minimises the objective on the current free set
     for _ in range(maxiter):
         free = ~work
         nf = int(free.sum())
         g = P @ x + q
+        if at_min:
+            # multiplier check at the subspace minimiser (lambda = -mean g_F)
+            lam = -g[free].mean() if nf else 0.0
+            mu = g + lam
+            if not work.any() or mu[work].min() >= -1e-12 * max(1.0, np.abs(g).max()):
+                return x
+            work[np.where(work)[0][np.argmin(mu[work])]] = False
+            at_min = False
+            continue
         kkt = np.zeros((nf + 1, nf + 1))
         kkt[:nf, :nf] = P[np.ix_(free, free)]
         kkt[:nf, nf] = 1.0
@@ -291,14 +301,8 @@ def qp_simplex_nonneg(P, q, total, maxiter=200):
         sol = np.linalg.solve(kkt, rhs)
         p = np.zeros(K)
         p[free] = sol[:nf]
-        lam = sol[nf]
         if np.max(np.abs(p)) <= 1e-14 * max(1.0, np.max(np.abs(x))):
-            mu = g + lam
-            mu[free] = 0.0
-            if not work.any() or mu[work].min() >= -1e-14:
-                return x
-            j = np.where(work)[0][np.argmin(mu[work])]
-            work[j] = False
+            at_min = True
             continue
         alpha, block = 1.0, -1
         for i in np.where(free & (p < 0))[0]:
@@ -309,6 +313,8 @@ def qp_simplex_nonneg(P, q, total, maxiter=200):
         if block >= 0:
             x[block] = 0.0
             work[block] = True
+        else:
+            at_min = True
     raise OracleError("QP active-set solver did not converge")
 
 

@@ -58,11 +58,17 @@ def workload(name):
         mol = synthetic.water(75, 110)
         return dict(name=name, scheme="mbis", solver="default", mol=mol, helper=None,
                     threshold=1e-8, maxiter=500)
+    if name.startswith("mbis-batch"):
+        # 512 molecules, 3-60 atoms (H:C:N:O 10:6:1:1), 75 radial x Lebedev-194
+        nmol = int(name[len("mbis-batch"):] or 512)
+        mols = synthetic.batch_molecules(nmol=nmol, amin=3, amax=60, nrad=75, nang=194, seed=3)
+        return dict(name=name, scheme="mbis", solver="default", mol=mols[0], mols=mols,
+                    helper=None, threshold=1e-8, maxiter=500)
     raise ValueError(name)
 
 
-def job_arrays(w):
-    mol = w["mol"]
+def job_arrays(w, mol=None):
+    mol = mol if mol is not None else w["mol"]
     if w["scheme"] == "mbis":
         from horton_part_gb300.mbis import get_initial_mbis_propars, get_nshell
 
@@ -83,17 +89,20 @@ def job_arrays(w):
     return off, init, orders, exps
 
 
-def make_job(ctx, w, precision, pinned=None):
+def make_job(ctx, w, precision, pinned=None, mol=None):
     from horton_part_gb300 import _lib
 
-    mol = w["mol"]
-    off, init, orders, exps = job_arrays(w)
+    mol = mol if mol is not None else w["mol"]
+    off, init, orders, exps = job_arrays(w, mol)
     pts, wts, rho = (mol.grid.points, mol.grid.weights, mol.density) if pinned is None else pinned
     extra = {"inner_maxiter": 2000} if w["scheme"] == "mbis" else {}
     return _lib.Job(ctx, w["scheme"], mol.coordinates, mol.pseudo_numbers, pts, wts, rho, off,
                     init, shell_orders=orders, shell_exponents=exps, solver=w["solver"],
                     precision=precision, grid_type=3, threshold=w["threshold"],
-                    inner_threshold=w["threshold"], maxiter=w["maxiter"], **extra)
+                    inner_threshold=w["threshold"], maxiter=w["maxiter"], polish=POLISH, **extra)
+
+
+POLISH = True
 
 
 # ---------------------------------------------------------------------------
@@ -239,12 +248,21 @@ def run_reference(args):
 
 
 def config_of(w, args, precision):
-    mol = w["mol"]
-    return {"workload": w["name"], "natom": int(mol.natom), "npoint": int(mol.npoint),
-            "nshell": int(sum(w["helper"].get_nshell(z) for z in mol.numbers)) if w["helper"] else None,
-            "solver": w["solver"], "threshold": w["threshold"], "precision": precision,
-            "l2": "inputs larger than L2 (basis matrix 725 MB)" if w["scheme"] == "glisa"
-            else "L2-resident small case", "parallelism": f"replicas{args.gpus}"}
+    mols = w.get("mols", [w["mol"]])
+    mol = mols[0]
+    natom = sum(m.natom for m in mols)
+    npoint = sum(m.npoint for m in mols)
+    # bytes resident per step: rho_a (A x N values) dominates
+    resident = sum(m.natom * m.npoint for m in mols) * (4 if precision == "mixed" else 8)
+    cfg = {"workload": w["name"], "molecules": len(mols), "natom": int(natom),
+           "npoint": int(npoint),
+           "nshell": int(sum(w["helper"].get_nshell(z) for z in mol.numbers)) if w["helper"] else None,
+           "solver": w["solver"], "threshold": w["threshold"], "precision": precision,
+           "polish": POLISH if precision == "mixed" else None,
+           "l2": ("inputs larger than L2 (%.0f MB of rho_a per pass)" % (resident / 1e6))
+           if resident > 129e6 else "inputs smaller than L2 (%.0f MB)" % (resident / 1e6),
+           "parallelism": f"replicas{args.gpus}"}
+    return cfg
 
 
 def run_ours(args):
@@ -264,15 +282,25 @@ def run_ours(args):
     build()
     w = workload(args.workload)
     mol = w["mol"]
+    mols = w.get("mols", [mol])
     stream = torch.cuda.current_stream()
     ctx = _lib.Context(torch.cuda.current_device(), stream=stream.cuda_stream)
-    job = make_job(ctx, w, args.precision)
+    jobs = [make_job(ctx, w, args.precision, mol=m) for m in mols]
+    job = jobs[0]
+
+    def run_all(js):
+        # one step of the benchmark: every job from its initial parameters to
+        # convergence, all live jobs advanced together by hp_step
+        for j in js:
+            j.reset()
+        while ctx.step(js) > 0:
+            pass
+
     for _ in range(args.warmup):
-        job.reset()
-        job.run()
-    info = job.info()
-    evals_per_job = info.point_atom_evals
-    niter = info.niter
+        run_all(jobs)
+    infos = [j.info() for j in jobs]
+    evals_per_job = float(sum(i.point_atom_evals for i in infos))
+    niter = max(i.niter for i in infos)
 
     def barrier():
         if world > 1:
@@ -285,8 +313,7 @@ def run_ours(args):
     with ClockSampler(torch.cuda.current_device()) as clocks:
         start.record(stream)
         for _ in range(args.steps):
-            job.reset()
-            job.run()
+            run_all(jobs)
         end.record(stream)
         torch.cuda.synchronize()
     barrier()
@@ -305,21 +332,29 @@ def run_ours(args):
     # end to end through the C ABI: host inputs (pinned), job create (H2D),
     # run, charges back (D2H), destroy
     pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()  # noqa: E731
-    pinned = (pin(mol.grid.points), pin(mol.grid.weights), pin(mol.density))
-    e2e_steps = max(1, min(args.steps, 3))
+    pinned = [(pin(m.grid.points), pin(m.grid.weights), pin(m.density)) for m in mols]
+    e2e_steps = 1 if len(mols) > 1 else max(1, min(args.steps, 3))
+    if len(mols) > 1:
+        for j in jobs:  # the resident copies make room for the end-to-end jobs
+            j.close()
     barrier()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
-        j2 = make_job(ctx, w, args.precision, pinned=pinned)
-        j2.run()
-        q = j2.results(promoldens=False, histories=False)["charges"]
-        j2.close()
+        e2e_jobs = [make_job(ctx, w, args.precision, pinned=pp, mol=m) for pp, m in zip(pinned, mols)]
+        while ctx.step(e2e_jobs) > 0:
+            pass
+        q = [j2.results(promoldens=False, histories=False) for j2 in e2e_jobs]
+        for j2 in e2e_jobs:
+            j2.close()
     torch.cuda.synchronize()
     e2e_s = (time.perf_counter() - t0) / e2e_steps
     e2e_value = evals_per_job * world / e2e_s
-    h2d = int(mol.npoint * 5 * 8 + mol.natom * 4 * 8)
-    d2h = int(q.nbytes + job.nparam * 8)
+    h2d = int(sum(m.npoint * 5 * 8 + m.natom * 4 * 8 for m in mols))
+    d2h = int(sum(r["charges"].nbytes + r["propars"].nbytes for r in q))
+    if len(mols) > 1:
+        jobs = [make_job(ctx, w, args.precision, mol=mols[0])]
+        job = jobs[0]
 
     fams = {k: {"ms": round(v[0], 3), "launches": v[1]} for k, v in fam_ms.items() if v[1]}
     roofline = None
@@ -330,22 +365,35 @@ def run_ours(args):
         pass
     hbm_peak = peaks.get("hbm_gbs", 6800.0)
     if w["scheme"] != "glisa":
-        # dominant kernel family and its algorithmic bytes per launch
-        A, N = float(mol.natom), float(mol.npoint)
-        model = {  # bytes that the pass must move at least once
-            "promol": 8 * N * (3 + 2 + 1) + 8 * A * N * 3,   # xyz, w, rho, promol; rho_a w/r/w
-            "inner": 8 * N * (3 + 1) + 8 * A * N,            # xyz, w; rho_a read
-            "change": 8 * N * (3 + 1),                       # xyz, w
+        # Dominant kernel family and its algorithmic bytes per launch: the
+        # point-atom evaluations the family performs per step (over all jobs)
+        # times the bytes one evaluation must move at least once.
+        # mixed: xyz hi/lo 24 B, w 4 B, rho_a 4 B (float); fp64: 24 B, 8 B, 8 B
+        mixed = args.precision == "mixed"
+        pt, val = (24.0, 4.0) if mixed else (24.0, 8.0)
+        sum_an = float(sum(m.natom * m.npoint for m in mols))
+        inner_evals = float(sum(i.inner_iterations * m.npoint for i, m in zip(infos, mols)))
+        if w["scheme"] == "gisa":
+            inner_evals = sum_an
+        per_step = {  # (point-atom evals per step, bytes per evaluation)
+            "promol": (sum_an, pt + 5 * val),   # pro-atom write, at_weights read/write, w, rho
+            "inner": (inner_evals, pt + 2 * val),  # coordinates, w, rho_a
+            "change": (sum_an, pt + val),       # coordinates, w
         }
-        fam = max(model, key=lambda f: fam_ms[f][0])
+        fam = max(per_step, key=lambda f: fam_ms[f][0])
         f_ms, f_n = fam_ms[fam]
         if f_n:
+            evals, bpe = per_step[fam]
             per_launch_s = f_ms / f_n / 1000.0
-            achieved = model[fam] / per_launch_s / 1e9
+            launches_per_step = f_n / args.steps
+            alg_bytes = evals * bpe / launches_per_step
+            achieved = alg_bytes / per_launch_s / 1e9
             roofline = {"kernel": fam, "bound": "hbm", "achieved": achieved, "peak": hbm_peak,
                         "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": None,
                         "peak_source": "measured" if peaks else "fallback",
-                        "ms_per_launch": per_launch_s * 1000.0}
+                        "ms_per_launch": per_launch_s * 1000.0,
+                        "algorithmic_bytes_per_launch": alg_bytes,
+                        "point_atom_evals_per_launch": evals / launches_per_step}
     if w["scheme"] == "glisa" and hess_n:
         nshell = config_of(w, args, args.precision)["nshell"]
         per_launch_s = hess_ms / hess_n / 1000.0
@@ -411,11 +459,19 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="gisa-c6h10n2o2")
-    ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
+    ap.add_argument("--precision", default="auto", choices=["auto", "fp64", "mixed"],
+                    help="auto: MBIS mixed (FP32 bulk, FP64 finish); basis schemes FP64 with "
+                         "the basis matrix resident in HBM")
+    ap.add_argument("--no-polish", action="store_true",
+                    help="mixed precision: stop at the FP32 noise floor instead of finishing in FP64")
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    if args.precision == "auto":
+        args.precision = "mixed" if args.workload.startswith("mbis") else "fp64"
+    global POLISH
+    POLISH = not args.no_polish
     if args.impl == "reference":
         run_reference(args)
     else:

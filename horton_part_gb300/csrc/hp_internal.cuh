@@ -82,7 +82,8 @@ enum WarnFlag { W_INNER = 1, W_POPULATION = 2, W_NEG_PARS = 4 };
 
 enum Scheme { SCHEME_MBIS = 0, SCHEME_GISA = 1, SCHEME_LISA = 2, SCHEME_GLISA = 3 };
 enum Solver { SOLVER_DEFAULT = 0, SOLVER_SC = 1, SOLVER_NEWTON = 2, SOLVER_M_NEWTON = 3,
-              SOLVER_QP = 4 };
+              SOLVER_QP = 4, SOLVER_PNEWTON = 5 };
+constexpr int kTrials = 8;  // projected-Newton step lengths 2^-t evaluated per pass
 enum Model { MODEL_MBIS = 0, MODEL_BASIS = 1 };
 
 struct JobDev {
@@ -126,6 +127,7 @@ struct JobDev {
   double* keep;           // gLISA line-search mask (nparam)
   // buffers
   double* promol;
+  double* invpro;         // FP64 jobs: 1 / promol (one division per point, not per pair)
   double* rhoa;
   double* apart;
   double* jpart;
@@ -141,6 +143,9 @@ struct JobDev {
   double* grad;           // gLISA: gradient [nshell]
   double* dvec1;          // gLISA: w rho / rho0 (0 where sick), npoint
   double* dvec2;          // gLISA: w rho / rho0^2 (0 where sick), npoint
+  double* ctrial;         // gLISA projected Newton: trial populations [kTrials][nshell]
+  double* tpart;          // gLISA projected Newton: trial objective partials [kTrials][ntile]
+  int* freeidx;           // gLISA projected Newton: free-variable list [nshell]
   double* hist_propars;   // [maxiter][nparam]
   double* hist_charges;   // [maxiter][natom]
   double* hist_ent;       // [maxiter]
@@ -358,6 +363,7 @@ void launch_glisa_keep(const HostBatch& hb, cudaStream_t st);
 void launch_glisa_ls(const HostBatch& hb, cudaStream_t st, int first, int count);
 void launch_glisa_change(const HostBatch& hb, cudaStream_t st);
 void launch_glisa_check(const HostBatch& hb, cudaStream_t st);
+void launch_glisa_pnewton(const HostBatch& hb, cudaStream_t st);
 
 // mixed precision (hp_mixed.cu)
 void launch_promol_mx(const HostBatch& hb, cudaStream_t st, int model);

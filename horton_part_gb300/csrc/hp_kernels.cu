@@ -72,16 +72,30 @@ __device__ __forceinline__ T shell_value(const JobDev& J, int s, T r) {
   return basis_shell<T>((T)J.sh_order[s], (T)J.sh_alpha[s], (T)J.sh_pref[s], r);
 }
 
-// Pro-atom of atom a at distance r with parameters par.
+// Unit-population shell s at grid point p: read from the stored basis matrix
+// when the job keeps one (basis schemes, FP64), else evaluated at distance r.
+template <typename T>
+__device__ __forceinline__ T basis_val(const JobDev& J, int s, int p, T r) {
+  return J.gmat ? (T)J.gmat[(size_t)s * J.npoint + p] : shell_value<T>(J, s, r);
+}
+
+// Distance to atom a, skipped when a stored basis matrix makes it unused.
 template <typename T, int MODEL>
-__device__ __forceinline__ T proatom(const JobDev& J, int a, const double* par, T r) {
+__device__ __forceinline__ T dist_for(const JobDev& J, int p, int a) {
+  if (MODEL == MODEL_BASIS && J.gmat) return (T)0;
+  return Dist<T>::r(J, p, a);
+}
+
+// Pro-atom of atom a at grid point p (distance r) with parameters par.
+template <typename T, int MODEL>
+__device__ __forceinline__ T proatom(const JobDev& J, int a, const double* par, T r, int p) {
   const int s0 = J.shell_off[a], s1 = J.shell_off[a + 1];
   const double* pa = par + J.par_off[a];
   T y = (T)0;
   if (MODEL == MODEL_MBIS) {
     for (int k = 0; k < s1 - s0; ++k) y += slater_shell<T>((T)pa[2 * k], (T)pa[2 * k + 1], r);
   } else {
-    for (int k = 0; k < s1 - s0; ++k) y += (T)pa[k] * shell_value<T>(J, s0 + k, r);
+    for (int k = 0; k < s1 - s0; ++k) y += (T)pa[k] * basis_val<T>(J, s0 + k, p, r);
   }
   return y;
 }
@@ -175,13 +189,14 @@ __global__ void __launch_bounds__(kThreads) k_promol(Batch bt) {
   if (p >= J.npoint) return;
   double promol = 0.0;
   for (int a = 0; a < J.natom; ++a) {
-    const T r = Dist<T>::r(J, p, a);
-    const double pro = (double)proatom<T, MODEL>(J, a, J.propars, r);
+    const T r = dist_for<T, MODEL>(J, p, a);
+    const double pro = (double)proatom<T, MODEL>(J, a, J.propars, r, p);
     J.rhoa[(size_t)a * J.npoint + p] = pro;
     promol += pro;
     promol += 1e-100;
   }
   J.promol[p] = promol;
+  J.invpro[p] = 1.0 / promol;
 }
 
 __global__ void __launch_bounds__(kThreads) k_atweights(Batch bt) {
@@ -197,7 +212,7 @@ __global__ void __launch_bounds__(kThreads) k_atweights(Batch bt) {
     if (p >= J.npoint) continue;
     const double promol = J.promol[p];
     const double rho = J.rho[p];
-    const double aw = fmin(fmax(ra[p] / promol, 0.0), 1.0);
+    const double aw = fmin(fmax(ra[p] * J.invpro[p], 0.0), 1.0);
     const double v = aw * rho;
     ra[p] = v;
     acc[0] += J.w[p] * v;
@@ -224,8 +239,8 @@ __global__ void __launch_bounds__(kThreads) k_final_atweights(Batch bt, int use_
   for (int i = 0; i < J.ppt; ++i) {
     const int p = point_of(J, at.tile, i);
     if (p >= J.npoint) continue;
-    const T r = Dist<T>::r(J, p, at.atom);
-    const double pro = (double)proatom<T, MODEL>(J, at.atom, par, r);
+    const T r = dist_for<T, MODEL>(J, p, at.atom);
+    const double pro = (double)proatom<T, MODEL>(J, at.atom, par, r, p);
     J.rhoa[(size_t)at.atom * J.npoint + p] = fmin(fmax(pro / J.promol[p], 0.0), 1.0);
   }
 }
@@ -244,9 +259,18 @@ __global__ void __launch_bounds__(kThreads) k_change(Batch bt) {
   for (int i = 0; i < J.ppt; ++i) {
     const int p = point_of(J, at.tile, i);
     if (p >= J.npoint) continue;
-    const T r = Dist<T>::r(J, p, at.atom);
-    const double d = (double)proatom<T, MODEL>(J, at.atom, J.propars, r) -
-                     (double)proatom<T, MODEL>(J, at.atom, J.propars_old, r);
+    const T r = dist_for<T, MODEL>(J, p, at.atom);
+    double d;
+    if (MODEL == MODEL_BASIS && J.gmat) {
+      // stored basis: one sum over exact FP64 coefficient differences
+      d = 0.0;
+      const int s0 = J.shell_off[at.atom], s1 = J.shell_off[at.atom + 1];
+      for (int s = s0; s < s1; ++s)
+        d += (J.propars[s] - J.propars_old[s]) * J.gmat[(size_t)s * J.npoint + p];
+    } else {
+      d = (double)proatom<T, MODEL>(J, at.atom, J.propars, r, p) -
+          (double)proatom<T, MODEL>(J, at.atom, J.propars_old, r, p);
+    }
     acc += J.w[p] * d * d;
   }
   const double s = block_sum1(acc, red);
@@ -311,13 +335,12 @@ __global__ void k_charges(Batch bt) {
 }
 
 // Mixed precision only: the inner change of FP32-evaluated pro-atoms has a
-// noise floor (about 1e-9 of the pro-atom's L2 norm). An inner solve whose
-// change has reached the floor region (below 1000 x threshold) and stopped
-// decreasing (>= 0.9 x the previous change) is taken as converged.
+// noise floor (about 1e-9 of the pro-atom's L2 norm), so the FP32 inner solve
+// stops at 1000 x the inner threshold; the exact convergence to the
+// threshold happens in the FP64 outer iterations that finish a mixed job.
 __device__ __forceinline__ bool mixed_stalled(const JobDev& J, int a, double change) {
-  if (!J.mixed) return false;
-  const double prev = J.atom_out[a * AO_COUNT + AO_INNER_CHANGE];
-  return change < 1e3 * J.inner_threshold && change >= 0.9 * prev;
+  (void)a;
+  return J.mixed && change < 1e3 * J.inner_threshold;
 }
 
 __global__ void k_count_active(Batch bt) {
@@ -478,11 +501,11 @@ __global__ void __launch_bounds__(kThreads) k_basis_qvec(Batch bt) {
   for (int i = 0; i < J.ppt; ++i) {
     const int p = point_of(J, at.tile, i);
     if (p >= J.npoint) continue;
-    const T r = Dist<T>::r(J, p, at.atom);
+    const T r = dist_for<T, MODEL_BASIS>(J, p, at.atom);
     const double wr = J.w[p] * ra[p];
 #pragma unroll
     for (int k = 0; k < kMaxShells; ++k)
-      if (k < nsh) acc[k] += wr * (double)shell_value<T>(J, s0 + k, r);
+      if (k < nsh) acc[k] += wr * (double)basis_val<T>(J, s0 + k, p, r);
   }
   block_sum<kMaxShells>(acc, red, out);
   if (threadIdx.x < nsh) apart_ptr(J, at.atom, QA_INNER + threadIdx.x)[at.tile] = out[threadIdx.x];
@@ -688,14 +711,14 @@ __global__ void __launch_bounds__(kThreads) k_lisa_sc_inner(Batch bt) {
   for (int i = 0; i < J.ppt; ++i) {
     const int p = point_of(J, at.tile, i);
     if (p >= J.npoint) continue;
-    const T r = Dist<T>::r(J, p, at.atom);
+    const T r = dist_for<T, MODEL_BASIS>(J, p, at.atom);
     T g[kMaxShells];
     T pro = (T)0, oldpro = (T)0;
 #pragma unroll
     for (int k = 0; k < kMaxShells; ++k) {
       g[k] = (T)0;
       if (k < nsh) {
-        g[k] = shell_value<T>(J, s0 + k, r);
+        g[k] = basis_val<T>(J, s0 + k, p, r);
         pro += g[k] * (T)pc[k];
         if (!first) oldpro += g[k] * (T)pp[k];
       }
@@ -800,10 +823,10 @@ __global__ void __launch_bounds__(kThreads) k_lisa_newton_inner(Batch bt) {
       const int p = at.tile * J.tile_points + base + t;
       double v1 = 0.0, v2 = 0.0, ve = 0.0, vn = 0.0;
       if (t < kStage && base + t < npts && p < J.npoint) {
-        const T r = Dist<T>::r(J, p, at.atom);
+        const T r = dist_for<T, MODEL_BASIS>(J, p, at.atom);
         T pro = (T)0, oldpro = (T)0;
         for (int k = 0; k < nsh; ++k) {
-          const T g = shell_value<T>(J, s0 + k, r);
+          const T g = basis_val<T>(J, s0 + k, p, r);
           gs[k][t] = (double)g;
           pro += g * (T)pc[k];
           if (!first) oldpro += g * (T)pp[k];
@@ -932,9 +955,9 @@ __global__ void __launch_bounds__(kThreads) k_lisa_ls(Batch bt) {
   for (int i = 0; i < J.ppt; ++i) {
     const int p = point_of(J, at.tile, i);
     if (p >= J.npoint) continue;
-    const T r = Dist<T>::r(J, p, at.atom);
+    const T r = dist_for<T, MODEL_BASIS>(J, p, at.atom);
     double g[kMaxShells];
-    for (int k = 0; k < nsh; ++k) g[k] = (double)shell_value<T>(J, s0 + k, r);
+    for (int k = 0; k < nsh; ++k) g[k] = (double)basis_val<T>(J, s0 + k, p, r);
     for (int tr = 0; tr < L; ++tr) {
       double v = 0.0;
       for (int k = 0; k < nsh; ++k) v += g[k] * trial[tr][k];
@@ -996,6 +1019,7 @@ template <typename T>
 __global__ void __launch_bounds__(kThreads) k_glisa_basis(Batch bt) {
   int tile;
   const JobDev& J = decode_local(bt, tile);
+  if (!J.gmat) return;  // jobs that recompute their shells keep no basis matrix
   for (int i = 0; i < J.ppt; ++i) {
     const int p = point_of(J, tile, i);
     if (p >= J.npoint) continue;
@@ -1330,6 +1354,151 @@ __global__ void k_glisa_check(Batch bt) {
 }
 
 // ---------------------------------------------------------------------------
+// gLISA with non-negative populations: projected Newton (the optimum of the
+// reference's cvxopt solver, glisa.py:488-571)
+//
+// F(c) = int rho ln(rho / rho0) + sum c is the extended KL objective whose
+// Newton step the reference's newton solver takes (H delta = -1 - df,
+// glisa.py:763-769); minimising it over c >= 0 gives the cvxopt optimum
+// (sum c = int rho holds there automatically). Per iteration: variables at 0
+// whose gradient dF_k = 1 + df_k is non-negative stay fixed (Bertsekas'
+// projected Newton), the Newton system is solved on the free set, and the
+// step lengths 2^-t (t < kTrials) are tried on the projection
+// max(c + 2^-t delta, 0) with the Armijo rule in one pass over the grid.
+// ---------------------------------------------------------------------------
+
+// One block per job: free set, reduced Cholesky solve, trial populations.
+__global__ void __launch_bounds__(kThreads) k_glisa_pnewton_solve(Batch bt) {
+  __shared__ int bad, nf_s;
+  int local;
+  const JobDev& J = decode_local(bt, local);
+  const int M = J.nshell;
+  if (threadIdx.x == 0) {
+    int nf = 0;
+    for (int m = 0; m < M; ++m) {
+      const double gF = 1.0 + J.grad[m];
+      if (J.propars[m] > 0.0 || gF < 0.0) J.freeidx[nf++] = m;
+    }
+    nf_s = nf;
+    bad = 0;
+  }
+  __syncthreads();
+  const int nf = nf_s;
+  double* L = J.chol;
+  for (int e = threadIdx.x; e < nf * nf; e += kThreads) {
+    const int i = e / nf, j = e % nf;
+    L[e] = J.hess[(size_t)J.freeidx[i] * M + J.freeidx[j]];
+  }
+  __syncthreads();
+  for (int k = 0; k < nf; ++k) {
+    if (threadIdx.x == 0) {
+      const double d = L[(size_t)k * nf + k];
+      if (!(d > 0.0)) bad = 1;
+      L[(size_t)k * nf + k] = sqrt(fmax(d, 1e-300));
+    }
+    __syncthreads();
+    const double dkk = L[(size_t)k * nf + k];
+    for (int i = k + 1 + threadIdx.x; i < nf; i += kThreads) L[(size_t)i * nf + k] /= dkk;
+    __syncthreads();
+    const int n = nf - k - 1;
+    for (int e = threadIdx.x; e < n * n; e += kThreads) {
+      const int i = k + 1 + e / n, j = k + 1 + e % n;
+      if (j <= i) L[(size_t)i * nf + j] -= L[(size_t)i * nf + k] * L[(size_t)j * nf + k];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    if (bad) atomicOr(&J.mail->i[MI_ERR], E_SINGULAR);
+    for (int m = 0; m < M; ++m) J.delta[m] = 0.0;
+    double* y = J.keep;  // scratch
+    for (int i = 0; i < nf; ++i) {
+      double v = -(1.0 + J.grad[J.freeidx[i]]);
+      for (int j = 0; j < i; ++j) v -= L[(size_t)i * nf + j] * y[j];
+      y[i] = v / L[(size_t)i * nf + i];
+    }
+    for (int i = nf - 1; i >= 0; --i) {
+      double v = y[i];
+      for (int j = i + 1; j < nf; ++j) v -= L[(size_t)j * nf + i] * y[j];
+      y[i] = v / L[(size_t)i * nf + i];
+    }
+    for (int i = 0; i < nf; ++i) J.delta[J.freeidx[i]] = y[i];
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < kTrials * M; e += kThreads) {
+    const int t = e / M, m = e - t * M;
+    const double a = ldexp(1.0, -t);
+    J.ctrial[e] = fmax(J.propars[m] + a * J.delta[m], 0.0);
+  }
+}
+
+// Trial objectives: tpart[t][tile] = sum_p w rho ln(rho / rho0_t) (sick -> 0).
+__global__ void __launch_bounds__(kThreads) k_glisa_trials(Batch bt) {
+  __shared__ double red[kWarps * kTrials];
+  __shared__ double out[kTrials];
+  int tile;
+  const JobDev& J = decode_local(bt, tile);
+  double acc[kTrials];
+#pragma unroll
+  for (int t = 0; t < kTrials; ++t) acc[t] = 0.0;
+  for (int i = 0; i < J.ppt; ++i) {
+    const int p = point_of(J, tile, i);
+    if (p >= J.npoint) continue;
+    double r0[kTrials];
+#pragma unroll
+    for (int t = 0; t < kTrials; ++t) r0[t] = 0.0;
+    for (int m = 0; m < J.nshell; ++m) {
+      const double g = J.gmat[(size_t)m * J.npoint + p];
+#pragma unroll
+      for (int t = 0; t < kTrials; ++t) r0[t] += J.ctrial[t * J.nshell + m] * g;
+    }
+    const double rho = J.rho[p], w = J.w[p];
+#pragma unroll
+    for (int t = 0; t < kTrials; ++t)
+      if (!(rho < J.density_cutoff || r0[t] < J.density_cutoff)) acc[t] += w * rho * log(rho / r0[t]);
+  }
+  block_sum<kTrials>(acc, red, out);
+  if (threadIdx.x < kTrials) J.tpart[(size_t)threadIdx.x * J.ntile + tile] = out[threadIdx.x];
+}
+
+// One warp per job: Armijo choice among the trials, apply the step.
+__global__ void k_glisa_trial_pick(Batch bt) {
+  int local;
+  const JobDev& J = decode_local(bt, local);
+  const int lane = threadIdx.x & 31;
+  const int M = J.nshell;
+  const double f0 = warp_tile_sum(J, J.jpart + (size_t)QJ_ENTROPY * J.ntile, J.ntile);
+  double c0 = 0.0;
+  for (int m = lane; m < M; m += 32) c0 += J.propars[m];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) c0 += __shfl_xor_sync(0xffffffffu, c0, o);
+  const double F0 = f0 + c0;
+  int pick = kTrials - 1;
+  for (int t = 0; t < kTrials; ++t) {
+    double s = 0.0, dec = 0.0;
+    for (int m = lane; m < M; m += 32) {
+      const double ct = J.ctrial[t * M + m];
+      s += ct;
+      dec += (1.0 + J.grad[m]) * (ct - J.propars[m]);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      s += __shfl_xor_sync(0xffffffffu, s, o);
+      dec += __shfl_xor_sync(0xffffffffu, dec, o);
+    }
+    double ft = 0.0;
+    for (int q = lane; q < J.ntile; q += 32) ft += J.tpart[(size_t)t * J.ntile + q];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) ft += __shfl_xor_sync(0xffffffffu, ft, o);
+    if (ft + s <= F0 + 1e-4 * dec) {
+      pick = t;
+      break;
+    }
+  }
+  for (int m = lane; m < M; m += 32) J.propars[m] = J.ctrial[pick * M + m];
+  if (lane == 0) J.mail->d[MD_LS_X] = ldexp(1.0, -pick);
+}
+
+// ---------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------
 
@@ -1444,5 +1613,11 @@ void launch_glisa_change(const HostBatch& hb, cudaStream_t st) {
 }
 
 void launch_glisa_check(const HostBatch& hb, cudaStream_t st) { HP_LAUNCH(k_glisa_check, K_JOB, 32); }
+
+void launch_glisa_pnewton(const HostBatch& hb, cudaStream_t st) {
+  HP_LAUNCH(k_glisa_pnewton_solve, K_JOB, kThreads);
+  HP_LAUNCH(k_glisa_trials, K_POINT, kThreads);
+  HP_LAUNCH(k_glisa_trial_pick, K_JOB, 32);
+}
 
 }  // namespace hp

@@ -88,7 +88,26 @@ struct hp_job {
   bool converged = false;
   double prev_change = 1e300;
   int polish_iters = 0;  // FP64 outer iterations after a mixed-precision stall
+  std::vector<double> changes;  // outer changes of this run
 };
+
+namespace {
+
+// A mixed-precision job hands over to FP64 when its outer change is within
+// 100 x the threshold, or when the best change of the last 5 iterations is
+// not 10 % better than the best of the 5 before (the FP32 noise floor).
+bool mixed_outer_done(const hp_job* j) {
+  const double thr = j->desc.threshold;
+  if (j->desc.polish && j->change < 100.0 * thr) return true;
+  const size_t n = j->changes.size();
+  if (n < 10) return false;
+  double a = 1e300, b = 1e300;
+  for (size_t i = n - 10; i < n - 5; ++i) a = std::min(a, j->changes[i]);
+  for (size_t i = n - 5; i < n; ++i) b = std::min(b, j->changes[i]);
+  return b > 0.9 * a;
+}
+
+}  // namespace
 
 namespace {
 
@@ -231,9 +250,9 @@ int run_inner(hp_ctx* ctx, const std::vector<hp_job*>& jobs, const HostBatch& hb
 
 int job_init(hp_ctx* ctx, const std::vector<hp_job*>& jobs, const HostBatch& hb) {
   launch_nelec(hb, ctx->stream);
-  bool any_glisa = false;
-  for (hp_job* j : jobs) any_glisa |= j->desc.scheme == HP_SCHEME_GLISA;
-  if (any_glisa) launch_glisa_basis(hb, ctx->stream);
+  bool any_basis = false;
+  for (hp_job* j : jobs) any_basis |= j->dev.gmat != nullptr;
+  if (any_basis) launch_glisa_basis(hb, ctx->stream);
   for (hp_job* j : jobs) j->initialized = true;
   return check_launch();
 }
@@ -306,11 +325,10 @@ int step_iterstock(hp_ctx* ctx, const std::vector<hp_job*>& jobs, const HostBatc
     } else if (j->change < j->desc.threshold || j->niter >= j->desc.maxiter) {
       j->converged = j->change < j->desc.threshold;
       j->done = true;
-    } else if (j->dev.mixed && j->change < 10.0 * j->desc.threshold &&
-               j->change >= j->prev_change) {
-      // the FP32-evaluated outer change went up just above the threshold
-      // (its noise floor): finish in FP64 (every buffer is rewritten by the
-      // next FP64 pass), or stop here with a warning
+    } else if (j->dev.mixed && mixed_outer_done(j)) {
+      // the FP32-evaluated outer change is near the threshold or has stopped
+      // improving (its noise floor): finish in FP64 (every buffer is rewritten
+      // by the next FP64 pass), or stop here with a warning
       if (j->desc.polish) {
         j->dev.mixed = 0;
       } else {
@@ -320,6 +338,7 @@ int step_iterstock(hp_ctx* ctx, const std::vector<hp_job*>& jobs, const HostBatc
       }
     }
     j->prev_change = j->change;
+    j->changes.push_back(j->change);
   }
   return HP_OK;
 }
@@ -346,6 +365,8 @@ int step_glisa(hp_ctx* ctx, const std::vector<hp_job*>& jobs, const HostBatch& h
     launch_glisa_reduce(hb, st);
     if (solver == SOLVER_SC) {
       launch_glisa_apply(hb, st, 1);
+    } else if (solver == SOLVER_PNEWTON) {
+      launch_glisa_pnewton(hb, st);
     } else {
       launch_glisa_solve(hb, st);
       if (solver == SOLVER_NEWTON) launch_glisa_apply(hb, st, 0);
@@ -498,8 +519,10 @@ int validate(const hp_job_desc* d) {
     return fail(HP_ERR_UNSUPPORTED, "aLISA solvers on this path: sc, newton, m-newton");
   if (d->scheme == HP_SCHEME_GLISA &&
       (d->solver != HP_SOLVER_SC && d->solver != HP_SOLVER_NEWTON && d->solver != HP_SOLVER_M_NEWTON &&
-       d->solver != HP_SOLVER_DEFAULT))
-    return fail(HP_ERR_UNSUPPORTED, "gLISA solvers on this path: newton, m-newton, sc");
+       d->solver != HP_SOLVER_PNEWTON && d->solver != HP_SOLVER_DEFAULT))
+    return fail(HP_ERR_UNSUPPORTED, "gLISA solvers on this path: newton, m-newton, sc, pnewton");
+  if (d->scheme != HP_SCHEME_GLISA && d->solver == HP_SOLVER_PNEWTON)
+    return fail(HP_ERR_UNSUPPORTED, "the projected Newton solver is for gLISA");
   if (d->linspace_size > 64 || (d->scheme == HP_SCHEME_LISA && d->linspace_size > 32))
     return fail(HP_ERR_UNSUPPORTED, "linspace_size too large");
   if (d->precision != HP_PRECISION_FP64 && d->precision != HP_PRECISION_MIXED)
@@ -678,12 +701,19 @@ int32_t hp_job_create(hp_ctx* ctx, const hp_job_desc* d, hp_job** out) {
   add(&J.propars_old, 8 * (size_t)P); add(&J.cur, 8 * (size_t)P);
   add(&J.prev, 8 * (size_t)P); add(&J.delta, 8 * (size_t)P); add(&J.keep, 8 * (size_t)P);
   add(&J.promol, 8 * (size_t)N);
+  add(&J.invpro, 8 * (size_t)N);
   add(&J.rhoa, 8 * (size_t)A * N);
   add(&J.apart, 8 * (size_t)A * qa * ntile);
   add(&J.jpart, 8 * (size_t)QJ_COUNT * ntile);
   add(&J.atom_out, 8 * (size_t)A * AO_COUNT);
   add(&J.active, 4 * (size_t)A); add(&J.inner_it, 4 * (size_t)A);
   add(&J.ls_fail, 8 * (size_t)A * ntile);
+  // GISA / aLISA in FP64 keep the (fixed) unit-population shells on the device
+  // when the matrix takes at most half of the remaining budget: every pass
+  // then reads G instead of recomputing exponentials (gLISA always does).
+  const size_t gbytes = 8 * (size_t)S * N;
+  const size_t room = ctx->budget > ctx->used ? ctx->budget - ctx->used : 0;
+  if (!glisa && !mbis && !mixed && gbytes <= room / 2) add(&J.gmat, gbytes);
   if (glisa) {
     add(&J.gmat, 8 * (size_t)S * N);
     add(&J.gpart, 8 * (size_t)S * ntile);
@@ -692,6 +722,9 @@ int32_t hp_job_create(hp_ctx* ctx, const hp_job_desc* d, hp_job** out) {
     add(&J.chol, 8 * (size_t)S * S);
     add(&J.grad, 8 * (size_t)S);
     add(&J.dvec1, 8 * (size_t)N); add(&J.dvec2, 8 * (size_t)N);
+    add(&J.ctrial, 8 * (size_t)kTrials * S);
+    add(&J.tpart, 8 * (size_t)kTrials * ntile);
+    add(&J.freeidx, 4 * (size_t)S);
   }
   add(&J.hist_propars, 8 * (size_t)maxiter * P);
   add(&J.hist_charges, 8 * (size_t)maxiter * A);
@@ -929,6 +962,7 @@ int32_t hp_job_reset(hp_job* job) {
   job->converged = false;
   job->prev_change = 1e300;
   job->polish_iters = 0;
+  job->changes.clear();
   job->dev.mixed = job->desc.precision == HP_PRECISION_MIXED ? 1 : 0;
   return HP_OK;
 }

@@ -23,7 +23,8 @@ from .part import GPUStockholderWPart
 
 __all__ = ["GlobalLinearISAWPart"]
 
-_SOLVERS = {"newton": "newton", "m-newton": "m-newton", "sc": "sc", "cvxopt": "sc"}
+_SOLVERS = {"newton": "newton", "m-newton": "m-newton", "sc": "sc", "cvxopt": "pnewton",
+            "pnewton": "pnewton"}
 
 
 class GlobalLinearISAWPart(GPUStockholderWPart):

@@ -297,7 +297,7 @@ class GPUStockholderWPart(WPart):
 
     def __init__(self, coordinates, numbers, pseudo_numbers, grid, moldens, spindens=None, lmax=3,
                  logger=None, threshold=1e-6, maxiter=500, inner_threshold=1e-8, grid_type=1,
-                 precision="fp64", context=None, store_at_weights=True, polish=False, **kwargs):
+                 precision="fp64", context=None, store_at_weights=True, polish=True, **kwargs):
         self._threshold = threshold
         self._inner_threshold = inner_threshold if inner_threshold < threshold else threshold
         self._maxiter = maxiter

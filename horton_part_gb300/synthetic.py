@@ -19,7 +19,7 @@ from __future__ import annotations
 import numpy as np
 
 from .basis import ExpBasisFuncHelper
-from .molgrid import becke_molecular_grid
+from .molgrid import MolecularGrid, becke_molecular_grid, lebedev, radial_becke_gauss_chebyshev
 
 __all__ = [
     "ANGSTROM",
@@ -124,6 +124,84 @@ def chain_molecule(counts, nrad, nang, seed=7):
     rho = slater_density(grid.points, coords, numbers, seed + 1, jitter=0.1)
     rho *= float(numbers.sum()) / grid.integrate(rho)
     return Molecule(coords, numbers, grid, rho, name=f"chain A={len(numbers)} {nrad}x{nang}")
+
+
+def _becke_weights_torch(points, coords, owner, torch, chunk_bytes=1 << 29):
+    """Becke (k = 3) partition weights on the GPU (FP64), chunked over points."""
+    natom = coords.shape[0]
+    out = torch.empty(points.shape[0], dtype=torch.float64, device=points.device)
+    if natom == 1:
+        out.fill_(1.0)
+        return out
+    rab = torch.cdist(coords, coords)
+    rab.fill_diagonal_(1.0)
+    inv = 1.0 / rab
+    eye = torch.eye(natom, dtype=torch.bool, device=points.device)
+    chunk = max(1024, chunk_bytes // (8 * natom * natom))
+    for s in range(0, points.shape[0], chunk):
+        d = torch.cdist(points[s:s + chunk], coords)  # (n, A)
+        mu = (d[:, :, None] - d[:, None, :]) * inv[None]
+        f = mu
+        for _ in range(3):
+            f = 1.5 * f - 0.5 * f * f * f
+        sv = 0.5 * (1.0 - f)
+        sv[:, eye] = 1.0
+        cell = torch.prod(sv, dim=2)
+        own = owner[s:s + chunk]
+        out[s:s + chunk] = cell.gather(1, own[:, None])[:, 0] / cell.sum(dim=1)
+    return out
+
+
+def batch_molecules(nmol=512, amin=3, amax=60, nrad=75, nang=194, seed=3, ratio=None,
+                    device="cuda"):
+    """Seeded batch of chain molecules for the batched-MBIS workload.
+
+    Atom counts uniform in [amin, amax]; elements drawn H:C:N:O = 10:6:1:1;
+    geometry, Becke grid (nrad radial x Lebedev-nang per atom) and Slater-shell
+    density as :func:`chain_molecule`, computed on the GPU with torch (input
+    preparation only). Returns a list of :class:`Molecule` with host arrays.
+    """
+    import torch
+
+    ratio = ratio or {1: 10, 6: 6, 7: 1, 8: 1}
+    rng = np.random.default_rng(seed)
+    zs = np.array(sorted(ratio))
+    pz = np.array([ratio[z] for z in zs], dtype=float)
+    pz /= pz.sum()
+    r, wr = radial_becke_gauss_chebyshev(nrad)
+    ang, wang = lebedev(nang)
+    shell_pts = torch.as_tensor((r[:, None, None] * ang[None]).reshape(-1, 3), device=device)
+    shell_w = torch.as_tensor(((wr * r * r)[:, None] * wang[None]).reshape(-1), device=device)
+    npa = shell_pts.shape[0]
+    mols = []
+    for m in range(nmol):
+        natom = int(rng.integers(amin, amax + 1))
+        numbers = rng.choice(zs, size=natom, p=pz).astype(np.int64)
+        coords = _chain_geometry(numbers, rng)
+        c = torch.as_tensor(coords, device=device)
+        pts = (shell_pts[None] + c[:, None, :]).reshape(-1, 3)
+        owner = torch.arange(natom, device=device).repeat_interleave(npa)
+        w = shell_w.repeat(natom) * _becke_weights_torch(pts, c, owner, torch)
+        rho = torch.zeros(pts.shape[0], dtype=torch.float64, device=device)
+        jit = rng.uniform(0.9, 1.1, size=(natom, 3))
+        for a, z in enumerate(numbers):
+            ra = torch.linalg.norm(pts - c[a], dim=1)
+            for k, (alpha, pop) in enumerate(_DENSITY_SHELLS[int(z)]):
+                al = alpha * jit[a, k]
+                rho += pop * al**3 / (8.0 * np.pi) * torch.exp(-al * ra)
+        nb = 2 * natom + 2
+        centres = torch.as_tensor(coords[rng.integers(0, natom, nb)] + rng.normal(0, 1, (nb, 3)),
+                                  device=device)
+        amps = torch.as_tensor(rng.normal(0, 1, nb), device=device)
+        bumps = torch.zeros_like(rho)
+        for cc, am in zip(centres, amps):
+            bumps += am * torch.exp(-0.5 * ((pts - cc) ** 2).sum(dim=1))
+        rho = rho * (1.0 + 0.05 * torch.tanh(bumps))
+        rho *= float(numbers.sum()) / float(torch.dot(w, rho))
+        indices = np.arange(natom + 1, dtype=np.int64) * npa
+        grid = MolecularGrid(pts.cpu().numpy(), w.cpu().numpy(), indices=indices)
+        mols.append(Molecule(coords, numbers, grid, rho.cpu().numpy(), name=f"batch{m} A={natom}"))
+    return mols
 
 
 def geometric_gaussian_basis(nshell_per_element, amin=0.05, amax=300.0):

@@ -71,7 +71,11 @@ typedef enum {
   HP_SOLVER_SC = 1,      /* alisa.py:193-291, glisa.py:805-848 */
   HP_SOLVER_NEWTON = 2,  /* alisa.py:543-602, glisa.py:573-575 (exact Newton) */
   HP_SOLVER_M_NEWTON = 3,/* alisa.py:605-664, glisa.py:577-591 (line search) */
-  HP_SOLVER_QP = 4       /* gisa.py:348-421 (quadratic program) */
+  HP_SOLVER_QP = 4,      /* gisa.py:348-421 (quadratic program) */
+  HP_SOLVER_PNEWTON = 5  /* gLISA with non-negative populations: projected Newton on
+                            the extended KL objective; reaches the optimum of the
+                            reference's cvxopt solver (glisa.py:488-571), whose
+                            package is not available */
 } hp_solver;
 
 typedef enum {

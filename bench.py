@@ -52,7 +52,9 @@ def workload(name):
         if name.startswith("gisa"):
             return dict(name=name, scheme="gisa", solver="quadprog", mol=mol, helper=helper,
                         threshold=1e-8, maxiter=500)
-        return dict(name=name, scheme="glisa", solver="newton", mol=mol, helper=helper,
+        # the reference's default gLISA solver (cvxopt: populations >= 0) is
+        # served by projected Newton; exact Newton is singular on this basis
+        return dict(name=name, scheme="glisa", solver="pnewton", mol=mol, helper=helper,
                     threshold=1e-8, maxiter=100)
     if name == "mbis-h2o":
         mol = synthetic.water(75, 110)
@@ -103,6 +105,34 @@ def make_job(ctx, w, precision, pinned=None, mol=None):
 
 
 POLISH = True
+
+
+def measure_tf32_peak(n=8192, reps=10):
+    """Best-of-`reps` TF32 GEMM rate of cuBLAS (TFLOP/s, 2 n^3 per product),
+    timed with CUDA events: the denominator of the tensor-core Hessian's
+    roofline (no TF32 figure is recorded beside the HBM and BF16 peaks)."""
+    import torch
+
+    old = torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cuda.matmul.allow_tf32 = True
+    try:
+        a = torch.randn(n, n, device="cuda", dtype=torch.float32)
+        b = torch.randn(n, n, device="cuda", dtype=torch.float32)
+        c = torch.empty(n, n, device="cuda", dtype=torch.float32)
+        for _ in range(3):
+            torch.matmul(a, b, out=c)
+        best = float("inf")
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            torch.matmul(a, b, out=c)
+            e1.record()
+            torch.cuda.synchronize()
+            best = min(best, e0.elapsed_time(e1) / 1000.0)
+        del a, b, c
+        return 2.0 * n ** 3 / best / 1e12
+    finally:
+        torch.backends.cuda.matmul.allow_tf32 = old
 
 
 # ---------------------------------------------------------------------------
@@ -223,7 +253,8 @@ def run_reference(args):
     world, rank, _ = dist_env()
     if rank != 0:
         return
-    w = workload(args.workload)
+    # the serving mix has no CPU server; its CPU sample is the MBIS H2O job
+    w = workload("mbis-h2o" if args.workload == "serve" else args.workload)
     rates = []
     for _ in range(args.warmup):
         cpu_sample(w, 1)
@@ -306,7 +337,7 @@ def run_ours(args):
         if world > 1:
             torch.distributed.barrier()
 
-    ctx.profile(True)
+    ctx.profile(False)  # no per-family events in the timed region; resets the launch counter
     barrier()
     torch.cuda.synchronize()
     start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -318,10 +349,15 @@ def run_ours(args):
         torch.cuda.synchronize()
     barrier()
     ms = start.elapsed_time(end)
+    launches = ctx.launch_count()
+    # one more step with CUDA events around each kernel family (on the
+    # launching stream) for the per-family times and the roofline
+    ctx.profile(True)
+    run_all(jobs)
     hess_ms, hess_n = ctx.profile_get("glisa_hess")
     fam_ms = {f: ctx.profile_get(f) for f in _lib.KERNEL_FAMILIES}
-    launches = ctx.launch_count()
     ctx.profile(False)
+    prof_steps = 1
     ms_max = ms
     if world > 1:
         t = torch.tensor([ms], device="cuda")
@@ -385,7 +421,7 @@ def run_ours(args):
         if f_n:
             evals, bpe = per_step[fam]
             per_launch_s = f_ms / f_n / 1000.0
-            launches_per_step = f_n / args.steps
+            launches_per_step = f_n / prof_steps
             alg_bytes = evals * bpe / launches_per_step
             achieved = alg_bytes / per_launch_s / 1e9
             roofline = {"kernel": fam, "bound": "hbm", "achieved": achieved, "peak": hbm_peak,
@@ -397,13 +433,29 @@ def run_ours(args):
     if w["scheme"] == "glisa" and hess_n:
         nshell = config_of(w, args, args.precision)["nshell"]
         per_launch_s = hess_ms / hess_n / 1000.0
-        alg_bytes = (nshell + 1) * mol.npoint * 8.0  # G and w rho/rho0^2 once
-        achieved = alg_bytes / per_launch_s / 1e9
-        roofline = {"kernel": "k_glisa_hess", "bound": "hbm", "achieved": achieved,
-                    "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
-                    "traffic": None, "peak_source": "measured" if peaks else "fallback",
-                    "ms_per_launch": per_launch_s * 1000.0,
-                    "note": "FP64 CUDA-core Hessian; FP64 issue rate, not HBM, limits it"}
+        if args.precision == "mixed":
+            # algorithmic work of H = G diag(d) G^T: 2 M^2 N FLOP per launch,
+            # against cuBLAS's TF32 GEMM rate measured in this process
+            flops = 2.0 * nshell * nshell * mol.npoint
+            achieved = flops / per_launch_s / 1e12
+            tf32 = measure_tf32_peak()
+            roofline = {"kernel": "k_glisa_hess_tc", "bound": "tensor", "achieved": achieved,
+                        "peak": tf32, "unit": "TFLOP/s", "frac": achieved / tf32,
+                        "traffic": None,
+                        "peak_source": "measured: cuBLAS TF32 GEMM 8192^3, this run",
+                        "bf16_peak_measured": peaks.get("bf16_tflops"),
+                        "ms_per_launch": per_launch_s * 1000.0,
+                        "algorithmic_flop_per_launch": flops,
+                        "note": "3 TF32 MMAs per product (hi*hi, hi*lo, lo*hi); "
+                                "shells padded to 128 x 256 tiles"}
+        else:
+            alg_bytes = (nshell + 1) * mol.npoint * 8.0  # G and w rho/rho0^2 once
+            achieved = alg_bytes / per_launch_s / 1e9
+            roofline = {"kernel": "k_glisa_hess", "bound": "hbm", "achieved": achieved,
+                        "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
+                        "traffic": None, "peak_source": "measured" if peaks else "fallback",
+                        "ms_per_launch": per_launch_s * 1000.0,
+                        "note": "FP64 CUDA-core Hessian; FP64 issue rate, not HBM, limits it"}
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -411,7 +463,7 @@ def run_ours(args):
         "scaling": "weak", "vs_baseline": None,
         "dtype": "f64" if args.precision == "fp64" else "f32+f64", "data": "synthetic",
         "config": config_of(w, args, args.precision), "niter_per_job": int(niter),
-        "point_atom_evals_per_job": evals_per_job, "kernel_ms": fams,
+        "point_atom_evals_per_job": evals_per_job, "kernel_ms_one_profiled_step": fams,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "seconds_per_step": e2e_s},
         "roofline": roofline, "clocks": clocks.summary(),
@@ -452,6 +504,116 @@ def run_ours(args):
         torch.distributed.destroy_process_group()
 
 
+def serve_requests(nreq, seed, precision):
+    """Seeded request mix of the serving workload: 70 % MBIS on 75 x Lebedev-194
+    grids, 30 % gLISA (projected Newton, default Gaussian basis) on 100 x
+    Lebedev-302 grids, atom counts log-uniform in [3, 150], threshold 1e-8."""
+    from horton_part_gb300 import synthetic
+    from horton_part_gb300.serve import request_from_molecule
+
+    rng = np.random.default_rng(seed)
+    is_mbis = rng.random(nreq) < 0.7
+    natoms = np.rint(np.exp(rng.uniform(np.log(3.0), np.log(150.0), nreq))).astype(int)
+    mb = iter(synthetic.batch_molecules(natoms=natoms[is_mbis], nrad=75, nang=194, seed=seed))
+    gl = iter(synthetic.batch_molecules(natoms=natoms[~is_mbis], nrad=100, nang=302,
+                                        seed=seed + 1))
+    return [("mbis", next(mb), "default") if is_mbis[i] else ("glisa", next(gl), "pnewton")
+            for i in range(nreq)]
+
+
+def run_serve(args):
+    """Continuous-batching server under Poisson arrivals: the closed-loop
+    capacity first (every request queued at t = 0), then arrival rates at
+    50 % and 80 % of it, each reporting jobs/s and p50/p99 latency. Every
+    request enters from host arrays (job creation copies them in) and its
+    charges and parameters come back to the host, so the served rate is an
+    end-to-end figure."""
+    import torch
+
+    from horton_part_gb300 import _lib
+    from horton_part_gb300.build import build
+    from horton_part_gb300.serve import PartitionServer, request_from_molecule
+
+    torch.cuda.set_device(0)
+    build()
+    pool = serve_requests(args.serve_jobs, 5, args.precision)
+    h2d = sum(m.npoint * 5 * 8 + m.natom * 4 * 8 for _, m, _ in pool)
+
+    def requests(precision=args.precision):
+        return [request_from_molecule(i, s, m, precision=precision, threshold=1e-8, solver=sv)
+                for i, (s, m, sv) in enumerate(pool)]
+
+    def serve(arrivals, precision=args.precision):
+        srv = PartitionServer(hbm_budget=150 * 10**9)
+        reqs = requests(precision)
+        with ClockSampler(torch.cuda.current_device()) as clocks:
+            wall = srv.run_stream(reqs, arrivals)
+        st = srv.stats(wall)
+        launches = srv.ctx.launch_count()
+        srv.close()
+        return reqs, st, wall, clocks.summary(), launches
+
+    # warm-up: the smallest MBIS and gLISA requests once
+    small = sorted(range(len(pool)), key=lambda i: pool[i][1].npoint)
+    warm = [i for i in small if pool[i][0] == "mbis"][:1] + [i for i in small if pool[i][0] == "glisa"][:1]
+    for _ in range(max(1, args.warmup // 3)):
+        srv = PartitionServer(hbm_budget=150 * 10**9)
+        srv.run_stream([requests()[i] for i in warm], np.zeros(len(warm)))
+        srv.close()
+
+    reqs, cap, wall0, clocks, launches = serve(np.zeros(len(pool)))
+    capacity = cap["jobs_per_s"]
+    rates = []
+    rng = np.random.default_rng(11)
+    for frac in (0.5, 0.8):
+        lam = frac * capacity
+        arr = np.cumsum(rng.exponential(1.0 / lam, len(pool)))
+        _, st, wall, _, _ = serve(arr)
+        rates.append({"arrival_rate_jobs_per_s": lam, "load": frac, **st, "wall_s": wall})
+
+    # accuracy: the served (mixed-precision) charges of the smallest requests
+    # against the FP64 path run alone
+    check = [i for i in small if pool[i][0] == "mbis"][:3] + [i for i in small if pool[i][0] == "glisa"][:1]
+    dq = 0.0
+    ctx = _lib.Context(0)
+    for i in check:
+        s, m, sv = pool[i]
+        r = request_from_molecule(i, s, m, precision="fp64", threshold=1e-8, solver=sv)
+        j = _lib.Job(ctx, r.scheme, **r.arrays, **r.options)
+        j.run()
+        ref = j.results(promoldens=False, histories=False)["charges"]
+        j.close()
+        got = reqs[i].result["charges"] if reqs[i].result is not None else None
+        if got is not None:
+            dq = max(dq, float(np.abs(got - ref).max()))
+    ctx.close()
+
+    evals = sum(r.evals for r in reqs)
+    value = evals / wall0
+    d2h = sum(r.result["charges"].nbytes + r.result["propars"].nbytes
+              for r in reqs if r.result is not None)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": 1,
+        "warmup": args.warmup, "ms_per_step": wall0 * 1000.0, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64" if args.precision == "mixed" else "f64",
+        "data": "synthetic",
+        "config": {"workload": "serve", "requests": len(pool),
+                   "mbis": sum(1 for p in pool if p[0] == "mbis"),
+                   "glisa": sum(1 for p in pool if p[0] == "glisa"),
+                   "natom_total": int(sum(p[1].natom for p in pool)),
+                   "npoint_total": int(sum(p[1].npoint for p in pool)),
+                   "precision": args.precision, "hbm_budget_gb": 150, "threshold": 1e-8,
+                   "l2": "inputs larger than L2", "parallelism": "replicas1"},
+        "serving": {"capacity_jobs_per_s": capacity, "closed_loop": cap, "poisson": rates,
+                    "max_abs_dq_vs_fp64_e": dq, "dq_checked_requests": len(check)},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h),
+                "note": "every request enters from host arrays and returns its results"},
+        "clocks": clocks, "gpu_launches": int(launches),
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -460,20 +622,26 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="gisa-c6h10n2o2")
     ap.add_argument("--precision", default="auto", choices=["auto", "fp64", "mixed"],
-                    help="auto: MBIS mixed (FP32 bulk, FP64 finish); basis schemes FP64 with "
-                         "the basis matrix resident in HBM")
+                    help="auto: MBIS mixed (FP32 bulk, FP64 finish); gLISA mixed (tensor-core "
+                         "Hessian, FP64 refinement); GISA FP64 with the basis matrix resident")
     ap.add_argument("--no-polish", action="store_true",
                     help="mixed precision: stop at the FP32 noise floor instead of finishing in FP64")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--serve-jobs", type=int, default=32,
+                    help="serving workload: number of requests in the stream")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.precision == "auto":
-        args.precision = "mixed" if args.workload.startswith("mbis") else "fp64"
+        # MBIS: FP32 bulk with an FP64 finish; gLISA: tensor-core Hessian with
+        # FP64 refinement; GISA: FP64 with the basis matrix resident
+        args.precision = "fp64" if args.workload.startswith("gisa") else "mixed"
     global POLISH
     POLISH = not args.no_polish
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "serve":
+        run_serve(args)
     else:
         run_ours(args)
 

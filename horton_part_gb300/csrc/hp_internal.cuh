@@ -75,7 +75,8 @@ enum ErrFlag {
   E_SINGULAR = 2,      // Hessian not positive definite
   E_LINESEARCH = 4,    // no valid trial step
   E_INNER_NOT_CONV = 8,// Newton inner loop hit its iteration limit
-  E_QP = 16            // QP active-set did not finish
+  E_QP = 16,           // QP active-set did not finish
+  E_TIMEOUT = 32       // a bounded mbarrier wait ran out (tensor-core Hessian)
 };
 
 enum WarnFlag { W_INNER = 1, W_POPULATION = 2, W_NEG_PARS = 4 };
@@ -145,7 +146,10 @@ struct JobDev {
   double* dvec2;          // gLISA: w rho / rho0^2 (0 where sick), npoint
   double* ctrial;         // gLISA projected Newton: trial populations [kTrials][nshell]
   double* tpart;          // gLISA projected Newton: trial objective partials [kTrials][ntile]
-  int* freeidx;           // gLISA projected Newton: free-variable list [nshell]
+  int* freeidx;           // gLISA Newton: free-variable list [nshell], count at [nshell]
+  float* gmat32;          // gLISA tensor-core Hessian: FP32 copy of gmat [nshell][npoint]
+  float* hess_s;          // gLISA tensor-core Hessian: sqrt(w rho / rho0^2) as FP32, npoint
+  double* hvec;           // gLISA refinement: w rho / rho0^2 * (G^T delta)(p), npoint
   double* hist_propars;   // [maxiter][nparam]
   double* hist_charges;   // [maxiter][natom]
   double* hist_ent;       // [maxiter]
@@ -155,7 +159,8 @@ struct JobDev {
   int natom, npoint, ntile, nparam, nshell, qa;
   int scheme, solver, mixed, maxiter;
   int inner_maxiter, linspace_size, nsplit, ppt;  // ppt: points per thread per tile
-  int tile_points, htiles, pad1, pad2;           // htiles: 64-wide Hessian tiles per side
+  int tile_points, htiles, tc, pad2;             // htiles: 64-wide Hessian tiles per side;
+                                                 // tc: gLISA Hessian on the tensor cores
   double threshold, inner_threshold, density_cutoff, negative_cutoff, population_cutoff, tau;
 };
 
@@ -357,13 +362,18 @@ void launch_glisa_pro(const HostBatch& hb, cudaStream_t st);
 void launch_glisa_grad(const HostBatch& hb, cudaStream_t st);
 void launch_glisa_hess(const HostBatch& hb, cudaStream_t st);
 void launch_glisa_reduce(const HostBatch& hb, cudaStream_t st);
-void launch_glisa_solve(const HostBatch& hb, cudaStream_t st);
+void launch_glisa_solve(const HostBatch& hb, cudaStream_t st, int projected);
 void launch_glisa_apply(const HostBatch& hb, cudaStream_t st, int mode);
 void launch_glisa_keep(const HostBatch& hb, cudaStream_t st);
 void launch_glisa_ls(const HostBatch& hb, cudaStream_t st, int first, int count);
 void launch_glisa_change(const HostBatch& hb, cudaStream_t st);
 void launch_glisa_check(const HostBatch& hb, cudaStream_t st);
-void launch_glisa_pnewton(const HostBatch& hb, cudaStream_t st);
+void launch_glisa_pnewton(const HostBatch& hb, cudaStream_t st);  // trials + Armijo pick
+void launch_glisa_refine(const HostBatch& hb, cudaStream_t st);
+
+// tensor-core Hessian (hp_tcgen05.cu)
+int tc_hess_blocks(const JobDev& J);
+void launch_glisa_hess_tc(const HostBatch& hb, cudaStream_t st);
 
 // mixed precision (hp_mixed.cu)
 void launch_promol_mx(const HostBatch& hb, cudaStream_t st, int model);

@@ -1025,8 +1025,11 @@ __global__ void __launch_bounds__(kThreads) k_glisa_basis(Batch bt) {
     if (p >= J.npoint) continue;
     for (int a = 0; a < J.natom; ++a) {
       const T r = Dist<T>::r(J, p, a);
-      for (int s = J.shell_off[a]; s < J.shell_off[a + 1]; ++s)
-        J.gmat[(size_t)s * J.npoint + p] = (double)shell_value<T>(J, s, r);
+      for (int s = J.shell_off[a]; s < J.shell_off[a + 1]; ++s) {
+        const double g = (double)shell_value<T>(J, s, r);
+        J.gmat[(size_t)s * J.npoint + p] = g;
+        if (J.gmat32) J.gmat32[(size_t)s * J.npoint + p] = (float)g;
+      }
     }
   }
 }
@@ -1050,6 +1053,7 @@ __global__ void __launch_bounds__(kThreads) k_glisa_pro(Batch bt) {
     const double ratio = sick ? 0.0 : rho / rho0;
     J.dvec1[p] = w * ratio;
     J.dvec2[p] = sick ? 0.0 : w * (ratio / rho0);
+    if (J.hess_s) J.hess_s[p] = sick ? 0.0f : (float)sqrt(w * (ratio / rho0));
     if (!sick) acc[0] += w * rho * log(ratio);
     if (rho0 < J.negative_cutoff) acc[1] += 1.0;
   }
@@ -1060,17 +1064,19 @@ __global__ void __launch_bounds__(kThreads) k_glisa_pro(Batch bt) {
   }
 }
 
-// gpart[m][tile] = sum_p G[m][p] d1[p]; one warp per row m.
-__global__ void __launch_bounds__(kThreads) k_glisa_grad(Batch bt) {
+// gpart[m][tile] = sum_p G[m][p] v[p] with v = d1 (gradient) or v = hvec
+// (Hessian-vector product of the refinement); one warp per row m.
+__global__ void __launch_bounds__(kThreads) k_glisa_grad(Batch bt, int use_hvec) {
   int tile;
   const JobDev& J = decode_local(bt, tile);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int p0 = tile * J.tile_points;
   const int p1 = min(p0 + J.tile_points, J.npoint);
+  const double* v = use_hvec ? J.hvec : J.dvec1;
   for (int m = warp; m < J.nshell; m += kWarps) {
     const double* g = J.gmat + (size_t)m * J.npoint;
     double s = 0.0;
-    for (int p = p0 + lane; p < p1; p += 32) s += g[p] * J.dvec1[p];
+    for (int p = p0 + lane; p < p1; p += 32) s += g[p] * v[p];
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
     if (lane == 0) J.gpart[(size_t)m * J.ntile + tile] = s;
@@ -1168,46 +1174,137 @@ __global__ void __launch_bounds__(kThreads) k_glisa_reduce(Batch bt) {
   }
 }
 
-// Newton step: Cholesky of H (one block per job), delta = H^-1 (-1 - df).
-__global__ void __launch_bounds__(kThreads) k_glisa_solve(Batch bt) {
-  __shared__ int bad;
-  int local;
-  const JobDev& J = decode_local(bt, local);
-  const int M = J.nshell;
-  double* L = J.chol;
-  for (int e = threadIdx.x; e < M * M; e += kThreads) L[e] = J.hess[e];
-  if (threadIdx.x == 0) bad = 0;
-  __syncthreads();
-  for (int k = 0; k < M; ++k) {
+// In-place Cholesky factor of the n x n matrix L (row stride n, lower
+// triangle used) by all threads of the block; sets *bad on a non-positive pivot.
+__device__ void chol_factor(double* L, int n, int* bad) {
+  for (int k = 0; k < n; ++k) {
     if (threadIdx.x == 0) {
-      const double d = L[(size_t)k * M + k];
-      if (!(d > 0.0)) bad = 1;
-      L[(size_t)k * M + k] = sqrt(fmax(d, 1e-300));
+      const double d = L[(size_t)k * n + k];
+      if (!(d > 0.0)) *bad = 1;
+      L[(size_t)k * n + k] = sqrt(fmax(d, 1e-300));
     }
     __syncthreads();
-    const double dkk = L[(size_t)k * M + k];
-    for (int i = k + 1 + threadIdx.x; i < M; i += kThreads) L[(size_t)i * M + k] /= dkk;
+    const double dkk = L[(size_t)k * n + k];
+    for (int i = k + 1 + threadIdx.x; i < n; i += blockDim.x) L[(size_t)i * n + k] /= dkk;
     __syncthreads();
-    const int n = M - k - 1;
-    for (int e = threadIdx.x; e < n * n; e += kThreads) {
-      const int i = k + 1 + e / n, j = k + 1 + e % n;
-      if (j <= i) L[(size_t)i * M + j] -= L[(size_t)i * M + k] * L[(size_t)j * M + k];
+    const int m = n - k - 1;
+    for (int e = threadIdx.x; e < m * m; e += blockDim.x) {
+      const int i = k + 1 + e / m, j = k + 1 + e % m;
+      if (j <= i) L[(size_t)i * n + j] -= L[(size_t)i * n + k] * L[(size_t)j * n + k];
     }
     __syncthreads();
   }
+}
+
+// y <- (L L^T)^-1 y by one warp: forward then backward substitution, each
+// row's dot product split over the lanes and summed by a fixed xor tree.
+__device__ void chol_solve_warp(const double* L, int n, double* y) {
+  const int lane = threadIdx.x & 31;
+  for (int i = 0; i < n; ++i) {
+    double s = 0.0;
+    for (int j = lane; j < i; j += 32) s += L[(size_t)i * n + j] * y[j];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    const double v = (y[i] - s) / L[(size_t)i * n + i];
+    __syncwarp();
+    if (lane == 0) y[i] = v;
+    __syncwarp();
+  }
+  for (int i = n - 1; i >= 0; --i) {
+    double s = 0.0;
+    for (int j = i + 1 + lane; j < n; j += 32) s += L[(size_t)j * n + i] * y[j];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    const double v = (y[i] - s) / L[(size_t)i * n + i];
+    __syncwarp();
+    if (lane == 0) y[i] = v;
+    __syncwarp();
+  }
+}
+
+// Newton step on a free set F (one block per job): delta_F = H_FF^-1 (-1 - df)_F,
+// delta = 0 outside F. Newton / m-newton (glisa.py:734-748): F = all shells;
+// projected Newton: F = {c > 0 or dF/dc < 0}. The factor of H_FF stays in
+// chol and |F| in freeidx[nshell] for the refinement steps.
+__global__ void __launch_bounds__(kThreads) k_glisa_newton_step(Batch bt, int projected) {
+  __shared__ int bad, nf_s;
+  int local;
+  const JobDev& J = decode_local(bt, local);
+  const int M = J.nshell;
   if (threadIdx.x == 0) {
-    if (bad) atomicOr(&J.mail->i[MI_ERR], E_SINGULAR);
-    double* x = J.delta;
-    for (int i = 0; i < M; ++i) {
-      double v = -1.0 - J.grad[i];
-      for (int j = 0; j < i; ++j) v -= L[(size_t)i * M + j] * x[j];
-      x[i] = v / L[(size_t)i * M + i];
+    int nf = 0;
+    for (int m = 0; m < M; ++m) {
+      const double gF = 1.0 + J.grad[m];
+      if (!projected || J.propars[m] > 0.0 || gF < 0.0) J.freeidx[nf++] = m;
     }
-    for (int i = M - 1; i >= 0; --i) {
-      double v = x[i];
-      for (int j = i + 1; j < M; ++j) v -= L[(size_t)j * M + i] * x[j];
-      x[i] = v / L[(size_t)i * M + i];
-    }
+    J.freeidx[M] = nf;
+    nf_s = nf;
+    bad = 0;
+  }
+  __syncthreads();
+  const int nf = nf_s;
+  double* L = J.chol;
+  for (int e = threadIdx.x; e < nf * nf; e += kThreads) {
+    const int i = e / nf, j = e % nf;
+    L[e] = J.hess[(size_t)J.freeidx[i] * M + J.freeidx[j]];
+  }
+  for (int m = threadIdx.x; m < M; m += kThreads) J.delta[m] = 0.0;
+  __syncthreads();
+  chol_factor(L, nf, &bad);
+  if (threadIdx.x < 32) {
+    double* y = J.keep;  // scratch (the m-newton mask is formed after the step)
+    for (int i = threadIdx.x; i < nf; i += 32) y[i] = -(1.0 + J.grad[J.freeidx[i]]);
+    __syncwarp();
+    chol_solve_warp(L, nf, y);
+    for (int i = threadIdx.x; i < nf; i += 32) J.delta[J.freeidx[i]] = y[i];
+    if (threadIdx.x == 0 && bad) atomicOr(&J.mail->i[MI_ERR], E_SINGULAR);
+  }
+}
+
+// Hessian-vector product with the exact FP64 Hessian, first half:
+// hvec[p] = (w rho / rho0^2)(p) * sum_m G[m][p] delta[m]. The second half is
+// k_glisa_grad(use_hvec = 1): gpart[m][tile] = sum_p G[m][p] hvec[p].
+__global__ void __launch_bounds__(kThreads) k_glisa_hv(Batch bt) {
+  int local;
+  const JobDev& J = decode_local(bt, local);
+  const int p = local * kThreads + threadIdx.x;
+  if (p >= J.npoint) return;
+  double u = 0.0;
+  for (int m = 0; m < J.nshell; ++m) u += J.gmat[(size_t)m * J.npoint + p] * J.delta[m];
+  J.hvec[p] = J.dvec2[p] * u;
+}
+
+// One step of iterative refinement of the Newton system on the free set:
+// r = (-1 - df)_F - (H delta)_F with the exact FP64 product, then
+// delta_F += (L L^T)^-1 r with the factor of the (tensor-core) Hessian.
+__global__ void __launch_bounds__(kThreads) k_glisa_refine(Batch bt) {
+  int local;
+  const JobDev& J = decode_local(bt, local);
+  const int M = J.nshell;
+  const int nf = J.freeidx[M];
+  double* r = J.keep;
+  for (int i = threadIdx.x; i < nf; i += kThreads) {
+    const int m = J.freeidx[i];
+    double hd = 0.0;
+    for (int t = 0; t < J.ntile; ++t) hd += J.gpart[(size_t)m * J.ntile + t];
+    r[i] = -(1.0 + J.grad[m]) - hd;
+  }
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    chol_solve_warp(J.chol, nf, r);
+    for (int i = threadIdx.x; i < nf; i += 32) J.delta[J.freeidx[i]] += r[i];
+  }
+}
+
+// Projected-Newton trial points c_t = max(c + 2^-t delta, 0), t < kTrials.
+__global__ void __launch_bounds__(kThreads) k_glisa_trial_set(Batch bt) {
+  int local;
+  const JobDev& J = decode_local(bt, local);
+  const int M = J.nshell;
+  for (int e = threadIdx.x; e < kTrials * M; e += kThreads) {
+    const int t = e / M, m = e - t * M;
+    const double a = ldexp(1.0, -t);
+    J.ctrial[e] = fmax(J.propars[m] + a * J.delta[m], 0.0);
   }
 }
 
@@ -1367,69 +1464,8 @@ __global__ void k_glisa_check(Batch bt) {
 // max(c + 2^-t delta, 0) with the Armijo rule in one pass over the grid.
 // ---------------------------------------------------------------------------
 
-// One block per job: free set, reduced Cholesky solve, trial populations.
-__global__ void __launch_bounds__(kThreads) k_glisa_pnewton_solve(Batch bt) {
-  __shared__ int bad, nf_s;
-  int local;
-  const JobDev& J = decode_local(bt, local);
-  const int M = J.nshell;
-  if (threadIdx.x == 0) {
-    int nf = 0;
-    for (int m = 0; m < M; ++m) {
-      const double gF = 1.0 + J.grad[m];
-      if (J.propars[m] > 0.0 || gF < 0.0) J.freeidx[nf++] = m;
-    }
-    nf_s = nf;
-    bad = 0;
-  }
-  __syncthreads();
-  const int nf = nf_s;
-  double* L = J.chol;
-  for (int e = threadIdx.x; e < nf * nf; e += kThreads) {
-    const int i = e / nf, j = e % nf;
-    L[e] = J.hess[(size_t)J.freeidx[i] * M + J.freeidx[j]];
-  }
-  __syncthreads();
-  for (int k = 0; k < nf; ++k) {
-    if (threadIdx.x == 0) {
-      const double d = L[(size_t)k * nf + k];
-      if (!(d > 0.0)) bad = 1;
-      L[(size_t)k * nf + k] = sqrt(fmax(d, 1e-300));
-    }
-    __syncthreads();
-    const double dkk = L[(size_t)k * nf + k];
-    for (int i = k + 1 + threadIdx.x; i < nf; i += kThreads) L[(size_t)i * nf + k] /= dkk;
-    __syncthreads();
-    const int n = nf - k - 1;
-    for (int e = threadIdx.x; e < n * n; e += kThreads) {
-      const int i = k + 1 + e / n, j = k + 1 + e % n;
-      if (j <= i) L[(size_t)i * nf + j] -= L[(size_t)i * nf + k] * L[(size_t)j * nf + k];
-    }
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) {
-    if (bad) atomicOr(&J.mail->i[MI_ERR], E_SINGULAR);
-    for (int m = 0; m < M; ++m) J.delta[m] = 0.0;
-    double* y = J.keep;  // scratch
-    for (int i = 0; i < nf; ++i) {
-      double v = -(1.0 + J.grad[J.freeidx[i]]);
-      for (int j = 0; j < i; ++j) v -= L[(size_t)i * nf + j] * y[j];
-      y[i] = v / L[(size_t)i * nf + i];
-    }
-    for (int i = nf - 1; i >= 0; --i) {
-      double v = y[i];
-      for (int j = i + 1; j < nf; ++j) v -= L[(size_t)j * nf + i] * y[j];
-      y[i] = v / L[(size_t)i * nf + i];
-    }
-    for (int i = 0; i < nf; ++i) J.delta[J.freeidx[i]] = y[i];
-  }
-  __syncthreads();
-  for (int e = threadIdx.x; e < kTrials * M; e += kThreads) {
-    const int t = e / M, m = e - t * M;
-    const double a = ldexp(1.0, -t);
-    J.ctrial[e] = fmax(J.propars[m] + a * J.delta[m], 0.0);
-  }
-}
+// The free-set step is k_glisa_newton_step(projected = 1); the trial points
+// come from k_glisa_trial_set after the optional refinement.
 
 // Trial objectives: tpart[t][tile] = sum_p w rho ln(rho / rho0_t) (sick -> 0).
 __global__ void __launch_bounds__(kThreads) k_glisa_trials(Batch bt) {
@@ -1587,14 +1623,22 @@ void launch_glisa_basis(const HostBatch& hb, cudaStream_t st) {
 }
 
 void launch_glisa_pro(const HostBatch& hb, cudaStream_t st) { HP_LAUNCH(k_glisa_pro, K_POINT, kThreads); }
-void launch_glisa_grad(const HostBatch& hb, cudaStream_t st) { HP_LAUNCH(k_glisa_grad, K_POINT, kThreads); }
+void launch_glisa_grad(const HostBatch& hb, cudaStream_t st) {
+  HP_LAUNCH(k_glisa_grad, K_POINT, kThreads, 0);
+}
 void launch_glisa_hess(const HostBatch& hb, cudaStream_t st) { HP_LAUNCH(k_glisa_hess, K_HESS, kThreads); }
 void launch_glisa_reduce(const HostBatch& hb, cudaStream_t st) {
   HP_LAUNCH(k_glisa_reduce, K_SQUARE, kThreads);
 }
 
-void launch_glisa_solve(const HostBatch& hb, cudaStream_t st) {
-  HP_LAUNCH(k_glisa_solve, K_JOB, kThreads);
+void launch_glisa_solve(const HostBatch& hb, cudaStream_t st, int projected) {
+  HP_LAUNCH(k_glisa_newton_step, K_JOB, kThreads, projected);
+}
+
+void launch_glisa_refine(const HostBatch& hb, cudaStream_t st) {
+  HP_LAUNCH(k_glisa_hv, K_POINT1, kThreads);
+  HP_LAUNCH(k_glisa_grad, K_POINT, kThreads, 1);
+  HP_LAUNCH(k_glisa_refine, K_JOB, kThreads);
 }
 
 void launch_glisa_apply(const HostBatch& hb, cudaStream_t st, int mode) {
@@ -1615,7 +1659,7 @@ void launch_glisa_change(const HostBatch& hb, cudaStream_t st) {
 void launch_glisa_check(const HostBatch& hb, cudaStream_t st) { HP_LAUNCH(k_glisa_check, K_JOB, 32); }
 
 void launch_glisa_pnewton(const HostBatch& hb, cudaStream_t st) {
-  HP_LAUNCH(k_glisa_pnewton_solve, K_JOB, kThreads);
+  HP_LAUNCH(k_glisa_trial_set, K_JOB, kThreads);
   HP_LAUNCH(k_glisa_trials, K_POINT, kThreads);
   HP_LAUNCH(k_glisa_trial_pick, K_JOB, 32);
 }

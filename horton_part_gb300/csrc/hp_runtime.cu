@@ -163,7 +163,9 @@ int blocks_for(const JobDev& J, int kind) {
     case K_ATOM_TILE: return J.natom * J.ntile;
     case K_ATOM: return J.natom;
     case K_JOB: return 1;
-    case K_HESS: return J.scheme == SCHEME_GLISA ? J.nsplit * J.htiles * (J.htiles + 1) / 2 : 0;
+    case K_HESS:
+      if (J.scheme != SCHEME_GLISA) return 0;
+      return J.tc ? tc_hess_blocks(J) : J.nsplit * J.htiles * (J.htiles + 1) / 2;
     case K_SQUARE: return J.scheme == SCHEME_GLISA ? (J.nshell * J.nshell + kThreads - 1) / kThreads : 0;
   }
   return 0;
@@ -209,11 +211,13 @@ int model_of(const hp_job* j) { return j->desc.scheme == HP_SCHEME_MBIS ? MODEL_
 // Map device error bits to a status.
 int status_of(int err) {
   if (err == 0) return HP_OK;
+  if (err & E_TIMEOUT) return HP_ERR_TIMEOUT;
   if (err & E_INNER_NOT_CONV) return HP_ERR_NOT_CONVERGED;
   return HP_ERR_NUMERIC;
 }
 
 const char* err_text(int err) {
+  if (err & E_TIMEOUT) return "tensor-core Hessian: a bounded device wait ran out";
   if (err & E_NEG_DENSITY) return "Negative pro-atom density found!";
   if (err & E_SINGULAR) return "Hessian is not positive definite (singular Newton system)";
   if (err & E_LINESEARCH) return "Line search failed!";
@@ -343,6 +347,10 @@ int step_iterstock(hp_ctx* ctx, const std::vector<hp_job*>& jobs, const HostBatc
   return HP_OK;
 }
 
+// Refinement steps per Newton iteration when the Hessian comes from the
+// tensor cores (each: one FP64 H delta product, two passes over G).
+constexpr int kRefineSteps = 2;
+
 // One gLISA solver iteration (glisa.py:748-798 for Newton, 805-848 for SC).
 int step_glisa(hp_ctx* ctx, const std::vector<hp_job*>& jobs, const HostBatch& hb) {
   cudaStream_t st = ctx->stream;
@@ -356,19 +364,27 @@ int step_glisa(hp_ctx* ctx, const std::vector<hp_job*>& jobs, const HostBatch& h
     ProfScope ps(ctx, HP_KERNEL_GLISA_GRAD);
     launch_glisa_grad(hb, st);
   }
+  const bool tc = jobs[0]->dev.tc != 0;
   if (solver != SOLVER_SC) {
     ProfScope ps(ctx, HP_KERNEL_GLISA_HESS);
-    launch_glisa_hess(hb, st);
+    if (tc) launch_glisa_hess_tc(hb, st);
+    else launch_glisa_hess(hb, st);
   }
   {
     ProfScope ps(ctx, HP_KERNEL_GLISA_SOLVE);
     launch_glisa_reduce(hb, st);
     if (solver == SOLVER_SC) {
       launch_glisa_apply(hb, st, 1);
-    } else if (solver == SOLVER_PNEWTON) {
-      launch_glisa_pnewton(hb, st);
     } else {
-      launch_glisa_solve(hb, st);
+      // Newton system with the FP64 Hessian, or with the tensor-core one plus
+      // iterative refinement against the exact FP64 product H delta.
+      launch_glisa_solve(hb, st, solver == SOLVER_PNEWTON ? 1 : 0);
+      if (tc)
+        for (int k = 0; k < kRefineSteps; ++k) launch_glisa_refine(hb, st);
+    }
+    if (solver == SOLVER_PNEWTON) {
+      launch_glisa_pnewton(hb, st);
+    } else if (solver != SOLVER_SC) {
       if (solver == SOLVER_NEWTON) launch_glisa_apply(hb, st, 0);
       else {
         launch_glisa_keep(hb, st);
@@ -527,10 +543,13 @@ int validate(const hp_job_desc* d) {
     return fail(HP_ERR_UNSUPPORTED, "linspace_size too large");
   if (d->precision != HP_PRECISION_FP64 && d->precision != HP_PRECISION_MIXED)
     return fail(HP_ERR_INVALID, "unknown precision");
-  if (d->precision == HP_PRECISION_MIXED &&
-      (d->scheme == HP_SCHEME_GLISA ||
-       (d->scheme == HP_SCHEME_LISA && d->solver != HP_SOLVER_SC && d->solver != HP_SOLVER_DEFAULT)))
-    return fail(HP_ERR_UNSUPPORTED, "mixed precision is available for MBIS, GISA and aLISA sc");
+  if (d->precision == HP_PRECISION_MIXED && d->scheme == HP_SCHEME_LISA &&
+      d->solver != HP_SOLVER_SC && d->solver != HP_SOLVER_DEFAULT)
+    return fail(HP_ERR_UNSUPPORTED, "mixed precision is available for MBIS, GISA, aLISA sc and gLISA");
+  if (d->precision == HP_PRECISION_MIXED && d->scheme == HP_SCHEME_GLISA &&
+      d->solver == HP_SOLVER_SC)
+    return fail(HP_ERR_UNSUPPORTED,
+                "mixed precision for gLISA is the tensor-core Hessian of the Newton solvers");
   for (int64_t s = 0; d->scheme != HP_SCHEME_MBIS && s < d->shell_offsets[d->natom]; ++s) {
     if (!(d->shell_orders[s] > 0.0)) return fail(HP_ERR_INVALID, "n must be positive");
     if (d->shell_exponents[s] < 0.0) return fail(HP_ERR_INVALID, "alpha must be non-negative");
@@ -652,18 +671,28 @@ int32_t hp_job_create(hp_ctx* ctx, const hp_job_desc* d, hp_job** out) {
   // tiles: aim for >= 2 * 152 point tiles when the grid is large enough
   // (mixed precision: at least 4 points per thread so the per-block
   // compensated reductions are amortised)
-  const int ppt_min = d->precision == HP_PRECISION_MIXED ? 4 : 2;
+  const int ppt_min = d->precision == HP_PRECISION_MIXED && !glisa ? 4 : 2;
   int ppt = (int)std::min<int64_t>(64, std::max<int64_t>(ppt_min, (N + kThreads * 304 - 1) / (kThreads * 304)));
   const int tile_points = kThreads * ppt;
   const int ntile = (N + tile_points - 1) / tile_points;
   int qa = 2 + std::max(2 * 7 + 1, kMaxShells + 1);
   if (d->scheme == HP_SCHEME_LISA && solver != HP_SOLVER_SC) qa = 2 + kNewtonQ(kmax);
   const int maxiter = d->maxiter;
-  const bool mixed = d->precision == HP_PRECISION_MIXED;
+  // gLISA keeps FP64 evaluation; its mixed mode is the tensor-core Hessian
+  const bool mixed = d->precision == HP_PRECISION_MIXED && !glisa;
+  const bool tc = d->precision == HP_PRECISION_MIXED && glisa;
   const int htiles = glisa ? (S + kHessTile - 1) / kHessTile : 0;
   const int npair = htiles * (htiles + 1) / 2;
   int nsplit = glisa ? std::max(1, std::min(1024, (4 * 152 + npair - 1) / std::max(1, npair))) : 0;
   if (glisa) nsplit = std::max(1, std::min(nsplit, (N + 255) / 256));
+  if (tc) {
+    // two 128-thread CTAs per SM (about 97 KB of shared memory each)
+    JobDev probe{};
+    probe.nshell = S;
+    probe.nsplit = 1;
+    const int tiles = tc_hess_blocks(probe);
+    nsplit = std::max(1, std::min((2 * 152 + tiles - 1) / tiles, (N + 255) / 256));
+  }
 
   // carve one allocation
   struct Part { void** dst; size_t bytes; };
@@ -724,7 +753,12 @@ int32_t hp_job_create(hp_ctx* ctx, const hp_job_desc* d, hp_job** out) {
     add(&J.dvec1, 8 * (size_t)N); add(&J.dvec2, 8 * (size_t)N);
     add(&J.ctrial, 8 * (size_t)kTrials * S);
     add(&J.tpart, 8 * (size_t)kTrials * ntile);
-    add(&J.freeidx, 4 * (size_t)S);
+    add(&J.freeidx, 4 * (size_t)(S + 1));
+    if (tc) {
+      add(&J.gmat32, 4 * (size_t)S * N);
+      add(&J.hess_s, 4 * (size_t)N);
+      add(&J.hvec, 8 * (size_t)N);
+    }
   }
   add(&J.hist_propars, 8 * (size_t)maxiter * P);
   add(&J.hist_charges, 8 * (size_t)maxiter * A);
@@ -750,6 +784,7 @@ int32_t hp_job_create(hp_ctx* ctx, const hp_job_desc* d, hp_job** out) {
   J.inner_maxiter = d->inner_maxiter > 0 ? d->inner_maxiter : 2000;
   J.linspace_size = d->linspace_size > 0 ? d->linspace_size : (glisa ? 40 : 20);
   J.nsplit = nsplit; J.ppt = ppt; J.tile_points = tile_points; J.htiles = htiles;
+  J.tc = tc ? 1 : 0;
   J.threshold = d->threshold;
   J.inner_threshold = d->inner_threshold < d->threshold ? d->inner_threshold : d->threshold;
   J.density_cutoff = d->density_cutoff; J.negative_cutoff = d->negative_cutoff;
@@ -910,7 +945,7 @@ int32_t hp_step(hp_ctx* ctx, hp_job* const* jobs, int32_t njobs, int32_t* n_live
     for (auto& g : groups) {
       const hp_job* h = g[0];
       if (h->desc.scheme == j->desc.scheme && h->dev.solver == j->dev.solver &&
-          h->dev.mixed == j->dev.mixed) {
+          h->dev.mixed == j->dev.mixed && h->dev.tc == j->dev.tc) {
         g.push_back(j);
         placed = true;
         break;
@@ -963,7 +998,8 @@ int32_t hp_job_reset(hp_job* job) {
   job->prev_change = 1e300;
   job->polish_iters = 0;
   job->changes.clear();
-  job->dev.mixed = job->desc.precision == HP_PRECISION_MIXED ? 1 : 0;
+  job->dev.mixed =
+      job->desc.precision == HP_PRECISION_MIXED && job->desc.scheme != HP_SCHEME_GLISA ? 1 : 0;
   return HP_OK;
 }
 

@@ -1,0 +1,318 @@
+// gLISA Hessian on the 5th-generation tensor cores (tcgen05, sm_103a).
+//
+//   H = G diag(w rho / rho0^2) G^T = X X^T,   X[m][p] = G[m][p] s(p),
+//   s(p) = sqrt(w rho / rho0^2) (0 where sick)          (glisa.py:457-470)
+//
+// Output tiles cover the lower triangle of H: row block i0 (128 rows, the
+// UMMA M) against column block j0 (N columns, a multiple of 16 up to 256,
+// ending at the tile's last row). One CTA (128 threads) computes one tile
+// over one range of grid points. Per block of 32 points the threads load G
+// (FP32 copy) and s for the next block into registers while the tensor core
+// works on the current one, then form X, split it into two TF32 parts
+// X = X_hi + X_lo (cvt.rna.tf32) and write A (128 x 32) and B (N x 32)
+// K-major into shared memory in the 128-byte-swizzled layout; one thread
+// issues tcgen05.mma.kind::tf32 (M = 128, K = 8) for X_hi X_hi^T,
+// X_hi X_lo^T and X_lo X_hi^T into one FP32 accumulator in tensor memory and
+// commits to an mbarrier. The accumulator is read back with tcgen05.ld and
+// written as the CTA's partial; partials over point ranges are summed in FP64
+// in a fixed order (k_glisa_reduce). Relative accuracy of H is about 1e-7
+// (the dropped X_lo X_lo^T term and FP32 accumulation); the Newton step is
+// refined against the exact FP64 product H delta (k_glisa_refine), so the
+// solver converges as with the FP64 Hessian.
+//
+// Every mbarrier wait is bounded: on time-out the kernel sets E_TIMEOUT,
+// frees its tensor memory and returns.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "hp_internal.cuh"
+
+namespace hp {
+
+namespace {
+
+constexpr int kTcM = 128;       // UMMA M
+constexpr int kTcNMax = 256;    // largest UMMA N
+constexpr int kTcK = 32;        // points per block: 32 x 4 B = one 128-byte swizzle row
+constexpr int kTcThreads = 128; // one warpgroup (tensor-memory lanes 0..127)
+constexpr int kTcWarps = kTcThreads / 32;
+constexpr int kRowsA = kTcM / kTcWarps;     // A rows staged per warp
+constexpr int kRowsB = kTcNMax / kTcWarps;  // B rows staged per warp (at most)
+constexpr int kTcCols = 256;    // tensor-memory columns (FP32 accumulator, N <= 256)
+constexpr long long kWaitLimit = 1ll << 26;
+
+// shared-memory layout (offsets from a 1024-byte-aligned base)
+constexpr int kOffAhi = 0;
+constexpr int kOffAlo = kOffAhi + kTcM * kTcK * 4;     // 16 KB
+constexpr int kOffBhi = kOffAlo + kTcM * kTcK * 4;     // 32 KB
+constexpr int kOffBlo = kOffBhi + kTcNMax * kTcK * 4;  // 64 KB
+constexpr int kOffBar = kOffBlo + kTcNMax * kTcK * 4;  // 96 KB
+constexpr int kSmemBytes = kOffBar + 64 + 1024;        // + alignment slack
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+// Word offset of element (row, k) of a K-major tile of 32-bit elements with
+// 128-byte rows in the 128B-swizzle layout: 16-byte chunk c of row r is
+// stored at chunk c ^ (r mod 8); rows are 128 bytes apart, 8-row groups 1024.
+__device__ __forceinline__ uint32_t swz_word(int row, int k) {
+  const int chunk = (k >> 2) ^ (row & 7);
+  return (uint32_t)(row * 32 + chunk * 4 + (k & 3));
+}
+
+// UMMA shared-memory descriptor: start address, leading byte offset (unused
+// for swizzled K-major; 16 B), stride byte offset 1024 B (between 8-row
+// groups), descriptor version 1, 128B swizzle.
+__device__ __forceinline__ uint64_t umma_desc(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr >> 4) & 0x3FFF);
+  d |= (uint64_t)(16 >> 4) << 16;
+  d |= (uint64_t)(1024 >> 4) << 32;
+  d |= (uint64_t)1 << 46;
+  d |= (uint64_t)2 << 61;
+  return d;
+}
+
+// Instruction descriptor, kind::tf32: D = F32 (bits 4-5), A = B = TF32
+// (bits 7-9, 10-12), both K-major, N >> 3 at bit 17, M >> 4 at bit 24.
+__device__ __forceinline__ uint32_t idesc_tf32(int n) {
+  return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(n >> 3) << 17) |
+         ((uint32_t)(kTcM >> 4) << 24);
+}
+
+__device__ __forceinline__ uint32_t to_tf32(float x) {
+  uint32_t r;
+  asm volatile("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return r;
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count));
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Bounded wait; returns false on time-out.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+  for (long long i = 0; i < kWaitLimit; ++i)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+
+__device__ __forceinline__ void umma_tf32(uint32_t tmem, uint64_t a, uint64_t b, uint32_t idesc,
+                                          uint32_t acc) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+      "l"(a), "l"(b), "r"(idesc), "r"(acc));
+}
+
+__device__ __forceinline__ void umma_commit(uint32_t bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                   bar)
+               : "memory");
+}
+
+// Lower-triangular tile list of an M x M Hessian: row block r0 (128 rows)
+// pairs with column blocks of up to 256 columns that start before the
+// block's end row. Returns the number of tiles; for idx in range also the
+// tile's (i0, j0, n), n a multiple of 16.
+__host__ __device__ inline int tc_tiles(int M, int idx, int* i0, int* j0, int* n) {
+  int t = 0;
+  for (int r0 = 0; r0 < M; r0 += kTcM) {
+    const int rend = r0 + kTcM < M ? r0 + kTcM : M;  // columns j < rend are needed
+    for (int c0 = 0; c0 < rend; c0 += kTcNMax) {
+      if (t == idx) {
+        int w = rend - c0;
+        if (w > kTcNMax) w = kTcNMax;
+        *i0 = r0;
+        *j0 = c0;
+        *n = (w + 15) / 16 * 16;
+      }
+      ++t;
+    }
+  }
+  return t;
+}
+
+}  // namespace
+
+__global__ void __launch_bounds__(kTcThreads) k_glisa_hess_tc(Batch bt) {
+  extern __shared__ uint8_t smem_raw[];
+  const uint32_t raw = smem_u32(smem_raw);
+  const uint32_t base = (raw + 1023u) & ~1023u;
+  uint8_t* sm = smem_raw + (base - raw);
+  uint32_t* a_hi = reinterpret_cast<uint32_t*>(sm + kOffAhi);
+  uint32_t* a_lo = reinterpret_cast<uint32_t*>(sm + kOffAlo);
+  uint32_t* b_hi = reinterpret_cast<uint32_t*>(sm + kOffBhi);
+  uint32_t* b_lo = reinterpret_cast<uint32_t*>(sm + kOffBlo);
+  const uint32_t bar = base + kOffBar;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(sm + kOffBar + 16);
+  __shared__ int timed_out;
+
+  const int jb = find_job(bt, blockIdx.x);
+  const JobDev& J = bt.jobs[jb];
+  const int local = blockIdx.x - bt.prefix[jb];
+  const int M = J.nshell, N = J.npoint;
+  const int ntiles = tc_tiles(M, -1, nullptr, nullptr, nullptr);
+  const int split = local / ntiles;
+  int i0 = 0, j0 = 0, ncol = 16;
+  tc_tiles(M, local - split * ntiles, &i0, &j0, &ncol);
+  const int chunk = ((N + J.nsplit - 1) / J.nsplit + kTcK - 1) / kTcK * kTcK;
+  const int pbeg = split * chunk;
+  const int pend = min(pbeg + chunk, N);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const uint32_t idesc = idesc_tf32(ncol);
+
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(tmem_slot)),
+                 "r"(kTcCols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  if (threadIdx.x == 0) {
+    mbar_init(bar, 1);
+    timed_out = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  const uint32_t tmem = *tmem_slot;
+
+  // rows of this thread: A rows warp + 4 r (r < 32), B rows warp + 4 r (row < ncol)
+  float va[kRowsA], vb[kRowsB], s = 0.0f;
+  auto load_block = [&](int kb) {
+    const int p = kb + lane;
+    const bool inr = p < pend;
+    s = inr ? J.hess_s[p] : 0.0f;
+#pragma unroll
+    for (int r = 0; r < kRowsA; ++r) {
+      const int m = i0 + warp + kTcWarps * r;
+      va[r] = (inr && m < M) ? J.gmat32[(size_t)m * N + p] : 0.0f;
+    }
+#pragma unroll
+    for (int r = 0; r < kRowsB; ++r) {
+      const int row = warp + kTcWarps * r;
+      const int m = j0 + row;
+      vb[r] = (inr && row < ncol && m < M) ? J.gmat32[(size_t)m * N + p] : 0.0f;
+    }
+  };
+
+  uint32_t phase = 0;
+  int nblocks = 0;
+  if (pbeg < pend) load_block(pbeg);
+  for (int kb = pbeg; kb < pend; kb += kTcK) {
+    if (nblocks > 0) {  // the previous block's MMAs must have read shared memory
+      if (!mbar_wait(bar, phase)) timed_out = 1;
+      phase ^= 1u;
+      __syncthreads();
+      if (timed_out) break;
+    }
+#pragma unroll
+    for (int r = 0; r < kRowsA; ++r) {
+      const float x = va[r] * s;
+      const uint32_t hi = to_tf32(x);
+      const uint32_t off = swz_word(warp + kTcWarps * r, lane);
+      a_hi[off] = hi;
+      a_lo[off] = to_tf32(x - __uint_as_float(hi));
+    }
+#pragma unroll
+    for (int r = 0; r < kRowsB; ++r) {
+      const int row = warp + kTcWarps * r;
+      if (row < ncol) {
+        const float x = vb[r] * s;
+        const uint32_t hi = to_tf32(x);
+        const uint32_t off = swz_word(row, lane);
+        b_hi[off] = hi;
+        b_lo[off] = to_tf32(x - __uint_as_float(hi));
+      }
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      asm volatile("tcgen05.fence::after_thread_sync;");
+      const uint32_t ahi = smem_u32(a_hi), alo = smem_u32(a_lo);
+      const uint32_t bhi = smem_u32(b_hi), blo = smem_u32(b_lo);
+#pragma unroll
+      for (int k = 0; k < kTcK / 8; ++k) {  // K = 8 TF32 = 32 bytes per MMA
+        const uint32_t acc = (nblocks > 0 || k > 0) ? 1u : 0u;
+        umma_tf32(tmem, umma_desc(ahi + 32 * k), umma_desc(bhi + 32 * k), idesc, acc);
+        umma_tf32(tmem, umma_desc(ahi + 32 * k), umma_desc(blo + 32 * k), idesc, 1u);
+        umma_tf32(tmem, umma_desc(alo + 32 * k), umma_desc(bhi + 32 * k), idesc, 1u);
+      }
+      umma_commit(bar);
+    }
+    ++nblocks;
+    // the next block's operands into registers while the tensor core runs
+    if (kb + kTcK < pend) load_block(kb + kTcK);
+  }
+  if (nblocks > 0 && !timed_out) {
+    if (!mbar_wait(bar, phase)) timed_out = 1;
+  }
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  __syncthreads();
+
+  // epilogue: warp w reads tensor-memory lanes 32w..32w+31 = rows of the tile
+  double* out = J.hpart + (size_t)split * M * M;
+  const int i = i0 + warp * 32 + lane;
+  const bool ok = nblocks > 0 && !timed_out;
+  for (int c = 0; c < ncol; c += 8) {
+    uint32_t v[8];
+    if (ok) {
+      const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c;
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+          : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+            "=r"(v[7])
+          : "r"(taddr));
+      asm volatile("tcgen05.wait::ld.sync.aligned;");
+    } else {
+#pragma unroll
+      for (int q = 0; q < 8; ++q) v[q] = 0u;
+    }
+    if (i < M) {
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        const int j = j0 + c + q;
+        if (j < M && j <= i) out[(size_t)i * M + j] = (double)__uint_as_float(v[q]);
+      }
+    }
+  }
+  if (timed_out && threadIdx.x == 0) atomicOr(&J.mail->i[MI_ERR], E_TIMEOUT);
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTcCols));
+  }
+}
+
+int tc_hess_blocks(const JobDev& J) {
+  return tc_tiles(J.nshell, -1, nullptr, nullptr, nullptr) * J.nsplit;
+}
+
+void launch_glisa_hess_tc(const HostBatch& hb, cudaStream_t st) {
+  static int configured_device = -1;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (configured_device != dev) {
+    cudaFuncSetAttribute(k_glisa_hess_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes);
+    configured_device = dev;
+  }
+  if (hb.blocks[K_HESS] > 0) {
+    k_glisa_hess_tc<<<hb.blocks[K_HESS], kTcThreads, kSmemBytes, st>>>(hb.b[K_HESS]);
+    ++g_launch_count;
+  }
+}
+
+}  // namespace hp

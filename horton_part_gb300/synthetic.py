@@ -153,13 +153,14 @@ def _becke_weights_torch(points, coords, owner, torch, chunk_bytes=1 << 29):
 
 
 def batch_molecules(nmol=512, amin=3, amax=60, nrad=75, nang=194, seed=3, ratio=None,
-                    device="cuda"):
+                    device="cuda", natoms=None):
     """Seeded batch of chain molecules for the batched-MBIS workload.
 
-    Atom counts uniform in [amin, amax]; elements drawn H:C:N:O = 10:6:1:1;
-    geometry, Becke grid (nrad radial x Lebedev-nang per atom) and Slater-shell
-    density as :func:`chain_molecule`, computed on the GPU with torch (input
-    preparation only). Returns a list of :class:`Molecule` with host arrays.
+    Atom counts uniform in [amin, amax] (or the given ``natoms`` list, one
+    molecule per entry); elements drawn H:C:N:O = 10:6:1:1; geometry, Becke
+    grid (nrad radial x Lebedev-nang per atom) and Slater-shell density as
+    :func:`chain_molecule`, computed on the GPU with torch (input preparation
+    only). Returns a list of :class:`Molecule` with host arrays.
     """
     import torch
 
@@ -174,8 +175,10 @@ def batch_molecules(nmol=512, amin=3, amax=60, nrad=75, nang=194, seed=3, ratio=
     shell_w = torch.as_tensor(((wr * r * r)[:, None] * wang[None]).reshape(-1), device=device)
     npa = shell_pts.shape[0]
     mols = []
+    if natoms is not None:
+        nmol = len(natoms)
     for m in range(nmol):
-        natom = int(rng.integers(amin, amax + 1))
+        natom = int(natoms[m]) if natoms is not None else int(rng.integers(amin, amax + 1))
         numbers = rng.choice(zs, size=natom, p=pz).astype(np.int64)
         coords = _chain_geometry(numbers, rng)
         c = torch.as_tensor(coords, device=device)

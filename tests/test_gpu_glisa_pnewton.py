@@ -48,3 +48,53 @@ def test_projected_newton_reaches_the_nonnegative_optimum(case, gpu_context):
     assert (part["propars"] >= 0).all()
     assert part["niter"] < 100
     np.testing.assert_allclose(part["propars"].sum(), mol.grid.integrate(mol.density), rtol=1e-8)
+
+
+@pytest.mark.parametrize("case", ["h2o-gauss", "chain5-geometric"])
+def test_tensor_core_hessian_reaches_the_same_optimum(case, gpu_context):
+    """precision="mixed" for gLISA: the Hessian G diag(w rho/rho0^2) G^T comes
+    from tcgen05 TF32 MMAs (hi/lo split, FP32 accumulation) and the Newton
+    system is refined against the exact FP64 product H delta; the gradient
+    and objective stay FP64, so the optimum is the FP64 one."""
+    if case == "h2o-gauss":
+        mol = synthetic.water(nrad=40, nang=50)
+        helper = ExpBasisFuncHelper.from_function_type("gauss")
+    else:
+        mol = synthetic.chain_molecule({6: 1, 8: 1, 1: 3}, 30, 50, seed=11)
+        helper = synthetic.geometric_gaussian_basis({1: 4, 6: 6, 8: 6}, 0.05, 300.0)
+    ref = _oracle_sc(mol, helper, 1e-11, 60000)
+    out = {}
+    for precision in ("fp64", "mixed"):
+        part = wpart_schemes("glisa")(mol.coordinates, mol.numbers, mol.pseudo_numbers, mol.grid,
+                                      mol.density, grid_type=3, solver="cvxopt",
+                                      basis_func=helper, threshold=1e-10, precision=precision)
+        part.do_partitioning()
+        out[precision] = part
+    tc, fp = out["mixed"], out["fp64"]
+    dq_ref = np.abs(tc["charges"] - ref["charges"]).max()
+    dq_fp = np.abs(tc["charges"] - fp["charges"]).max()
+    print(f"{case}: tensor-core niter {tc['niter']}, fp64 niter {fp['niter']}, "
+          f"max|dq| vs oracle {dq_ref:.2e}, vs fp64 {dq_fp:.2e}")
+    assert dq_ref < 1e-6
+    assert dq_fp < 1e-7
+    assert (tc["propars"] >= 0).all()
+    assert tc["niter"] <= fp["niter"] + 5
+
+
+def test_tensor_core_hessian_with_newton(gpu_context):
+    """The unconstrained Newton solver with the tensor-core Hessian converges
+    to the same populations as with the FP64 Hessian (glisa.py:748-798)."""
+    mol = synthetic.water(nrad=40, nang=50)
+    res = {}
+    for precision in ("fp64", "mixed"):
+        part = wpart_schemes("glisa")(mol.coordinates, mol.numbers, mol.pseudo_numbers, mol.grid,
+                                      mol.density, grid_type=3, solver="newton",
+                                      threshold=1e-10, precision=precision)
+        part.do_partitioning()
+        res[precision] = part
+    dq = np.abs(res["mixed"]["charges"] - res["fp64"]["charges"]).max()
+    dp = np.abs(res["mixed"]["propars"] - res["fp64"]["propars"]).max()
+    print(f"newton: niter tc {res['mixed']['niter']} fp64 {res['fp64']['niter']}, "
+          f"max|dq| {dq:.2e}, max|dp| {dp:.2e}")
+    assert dq < 1e-8
+    assert dp < 1e-7

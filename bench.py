@@ -1,19 +1,24 @@
 """Benchmark of the partitioning loop on one GB300 (or N independent replicas).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload glisa-c6h10n2o2|mbis-h2o] [--precision fp64|mixed]
+                    [--workload glisa-c6h10n2o2|gisa-c6h10n2o2|mbis-h2o|mbis-chain60|
+                                mbis-batch<N>|serve]
+                    [--precision auto|fp64|mixed] [--no-polish] [--no-cpu] [--no-check]
 
-Default workload: gLISA (exact Newton) on a 20-atom C6H10N2O2 chain,
-100 radial x Lebedev-302 points per atom (604,000 points), 6 s-Gaussians per
-H and 9 per C/N/O with exponents geometric in [0.05, 300] (150 shells),
-threshold 1e-8. One step = one complete partitioning job (every solver
-iteration until convergence) on inputs already resident in HBM; the basis
-matrix G (150 x 604,000 FP64 = 725 MB) is larger than L2, so no L2 flush is
-added between steps.
+Default workload: gLISA with non-negative populations (the reference's cvxopt
+default, served by projected Newton) on a 20-atom C6H10N2O2 chain, 100 radial
+x Lebedev-302 points per atom (604,000 points), 6 s-Gaussians per H and 9 per
+C/N/O with exponents geometric in [0.05, 300] (150 shells), threshold 1e-8;
+precision "auto" = the Hessian on the tensor cores with FP64 refinement. One
+step = one complete partitioning job (every solver iteration until
+convergence) on inputs already resident in HBM; the basis matrix G
+(150 x 604,000 FP64 = 725 MB) is larger than L2, so no L2 flush is added
+between steps.
 
 Metric: pro-atom evaluations (point x atom) per second, counted in the
-reference's convention (each solver iteration evaluates every pro-atom on
-every grid point three times: promolecule and the two sides of the change).
+reference's convention (gLISA: each solver iteration evaluates every pro-atom
+on every grid point three times: promolecule and the two sides of the change;
+MBIS/aLISA add one per inner iteration).
 
 Output: one JSON line (rank 0). Under torchrun every rank runs its own
 replica of the job (no collective on the data path); value = sum over ranks.
@@ -59,6 +64,11 @@ def workload(name):
     if name == "mbis-h2o":
         mol = synthetic.water(75, 110)
         return dict(name=name, scheme="mbis", solver="default", mol=mol, helper=None,
+                    threshold=1e-8, maxiter=500)
+    if name == "mbis-chain60":
+        # the largest molecule of the batched-MBIS mix: 60 atoms, 75 x Lebedev-194
+        mols = synthetic.batch_molecules(natoms=[60], nrad=75, nang=194, seed=3)
+        return dict(name=name, scheme="mbis", solver="default", mol=mols[0], helper=None,
                     threshold=1e-8, maxiter=500)
     if name.startswith("mbis-batch"):
         # 512 molecules, 3-60 atoms (H:C:N:O 10:6:1:1), 75 radial x Lebedev-194
@@ -469,7 +479,7 @@ def run_ours(args):
         "roofline": roofline, "clocks": clocks.summary(),
         "gpu_launches": int(launches),
     }
-    if args.precision == "mixed":
+    if args.precision == "mixed" and not args.no_check:
         # error of the mixed-precision result against the FP64 path on the
         # same input (the FP64 path matches the reference to 1e-8 e in tests)
         jm = make_job(ctx, w, "mixed")
@@ -620,13 +630,15 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="gisa-c6h10n2o2")
+    ap.add_argument("--workload", default="glisa-c6h10n2o2")
     ap.add_argument("--precision", default="auto", choices=["auto", "fp64", "mixed"],
                     help="auto: MBIS mixed (FP32 bulk, FP64 finish); gLISA mixed (tensor-core "
                          "Hessian, FP64 refinement); GISA FP64 with the basis matrix resident")
     ap.add_argument("--no-polish", action="store_true",
                     help="mixed precision: stop at the FP32 noise floor instead of finishing in FP64")
-    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--no-check", action="store_true",
+                    help="skip the mixed-precision accuracy run against the FP64 path")
     ap.add_argument("--serve-jobs", type=int, default=32,
                     help="serving workload: number of requests in the stream")
     args = ap.parse_args()

@@ -1046,6 +1046,7 @@ __global__ void __launch_bounds__(kThreads) k_glisa_pro(Batch bt) {
     const int p = point_of(J, tile, i);
     if (p >= J.npoint) continue;
     double rho0 = 0.0;
+#pragma unroll 8
     for (int m = 0; m < J.nshell; ++m) rho0 += J.gmat[(size_t)m * J.npoint + p] * J.propars[m];
     const double rho = J.rho[p];
     const double w = J.w[p];
@@ -1053,6 +1054,7 @@ __global__ void __launch_bounds__(kThreads) k_glisa_pro(Batch bt) {
     const double ratio = sick ? 0.0 : rho / rho0;
     J.dvec1[p] = w * ratio;
     J.dvec2[p] = sick ? 0.0 : w * (ratio / rho0);
+    J.rho0[p] = rho0;
     if (J.hess_s) J.hess_s[p] = sick ? 0.0f : (float)sqrt(w * (ratio / rho0));
     if (!sick) acc[0] += w * rho * log(ratio);
     if (rho0 < J.negative_cutoff) acc[1] += 1.0;
@@ -1076,6 +1078,7 @@ __global__ void __launch_bounds__(kThreads) k_glisa_grad(Batch bt, int use_hvec)
   for (int m = warp; m < J.nshell; m += kWarps) {
     const double* g = J.gmat + (size_t)m * J.npoint;
     double s = 0.0;
+#pragma unroll 8
     for (int p = p0 + lane; p < p1; p += 32) s += g[p] * v[p];
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
@@ -1175,24 +1178,41 @@ __global__ void __launch_bounds__(kThreads) k_glisa_reduce(Batch bt) {
 }
 
 // In-place Cholesky factor of the n x n matrix L (row stride n, lower
-// triangle used) by all threads of the block; sets *bad on a non-positive pivot.
-__device__ void chol_factor(double* L, int n, int* bad) {
+// triangle used) by all threads of the block (right-looking, one barrier per
+// column); sets *bad on a non-positive pivot. At step k warp w updates the
+// rows i > k with i = w (mod warps), lanes over the columns k < j <= i, using
+// a copy of the unscaled column k (colbuf[0..n)); the lane that updates
+// entry (i, k+1) copies it into the next column buffer (colbuf[n..2n)), and
+// entry (i, k) is replaced by its scaled value. colbuf: 2n doubles.
+__device__ void chol_factor(double* L, int n, int* bad, double* colbuf) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+  double* col = colbuf;
+  double* nxt = colbuf + n;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) col[i] = L[(size_t)i * n];
+  __syncthreads();
   for (int k = 0; k < n; ++k) {
+    const double akk = col[k];
+    const double piv = sqrt(fmax(akk, 1e-300));
+    const double inv = 1.0 / fmax(akk, 1e-300);
     if (threadIdx.x == 0) {
-      const double d = L[(size_t)k * n + k];
-      if (!(d > 0.0)) *bad = 1;
-      L[(size_t)k * n + k] = sqrt(fmax(d, 1e-300));
+      if (!(akk > 0.0)) *bad = 1;
+      L[(size_t)k * n + k] = piv;
+    }
+    for (int i = k + 1 + warp; i < n; i += nwarp) {
+      const double ci = col[i];
+      const double li = ci * inv;
+      double* row = L + (size_t)i * n;
+      for (int j = k + 1 + lane; j <= i; j += 32) {
+        const double v = row[j] - li * col[j];
+        row[j] = v;
+        if (j == k + 1) nxt[i] = v;
+      }
+      if (lane == 0) row[k] = ci / piv;
     }
     __syncthreads();
-    const double dkk = L[(size_t)k * n + k];
-    for (int i = k + 1 + threadIdx.x; i < n; i += blockDim.x) L[(size_t)i * n + k] /= dkk;
-    __syncthreads();
-    const int m = n - k - 1;
-    for (int e = threadIdx.x; e < m * m; e += blockDim.x) {
-      const int i = k + 1 + e / m, j = k + 1 + e % m;
-      if (j <= i) L[(size_t)i * n + j] -= L[(size_t)i * n + k] * L[(size_t)j * n + k];
-    }
-    __syncthreads();
+    double* t = col;
+    col = nxt;
+    nxt = t;
   }
 }
 
@@ -1250,7 +1270,7 @@ __global__ void __launch_bounds__(kThreads) k_glisa_newton_step(Batch bt, int pr
   }
   for (int m = threadIdx.x; m < M; m += kThreads) J.delta[m] = 0.0;
   __syncthreads();
-  chol_factor(L, nf, &bad);
+  chol_factor(L, nf, &bad, J.ctrial);  // ctrial (kTrials x nshell) is free until the trial set
   if (threadIdx.x < 32) {
     double* y = J.keep;  // scratch (the m-newton mask is formed after the step)
     for (int i = threadIdx.x; i < nf; i += 32) y[i] = -(1.0 + J.grad[J.freeidx[i]]);
@@ -1270,6 +1290,7 @@ __global__ void __launch_bounds__(kThreads) k_glisa_hv(Batch bt) {
   const int p = local * kThreads + threadIdx.x;
   if (p >= J.npoint) return;
   double u = 0.0;
+#pragma unroll 8
   for (int m = 0; m < J.nshell; ++m) u += J.gmat[(size_t)m * J.npoint + p] * J.delta[m];
   J.hvec[p] = J.dvec2[p] * u;
 }
@@ -1282,12 +1303,15 @@ __global__ void __launch_bounds__(kThreads) k_glisa_refine(Batch bt) {
   const JobDev& J = decode_local(bt, local);
   const int M = J.nshell;
   const int nf = J.freeidx[M];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   double* r = J.keep;
-  for (int i = threadIdx.x; i < nf; i += kThreads) {
+  for (int i = warp; i < nf; i += kWarps) {  // one warp per row, lanes over tiles
     const int m = J.freeidx[i];
     double hd = 0.0;
-    for (int t = 0; t < J.ntile; ++t) hd += J.gpart[(size_t)m * J.ntile + t];
-    r[i] = -(1.0 + J.grad[m]) - hd;
+    for (int t = lane; t < J.ntile; t += 32) hd += J.gpart[(size_t)m * J.ntile + t];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) hd += __shfl_xor_sync(0xffffffffu, hd, o);
+    if (lane == 0) r[i] = -(1.0 + J.grad[m]) - hd;
   }
   __syncthreads();
   if (threadIdx.x < 32) {
@@ -1296,7 +1320,9 @@ __global__ void __launch_bounds__(kThreads) k_glisa_refine(Batch bt) {
   }
 }
 
-// Projected-Newton trial points c_t = max(c + 2^-t delta, 0), t < kTrials.
+// Projected-Newton trial points c_t = max(c + 2^-t delta, 0), t < kTrials,
+// and the list of shells the projection clips at the full step (the clipped
+// set of every shorter step is a subset of it).
 __global__ void __launch_bounds__(kThreads) k_glisa_trial_set(Batch bt) {
   int local;
   const JobDev& J = decode_local(bt, local);
@@ -1305,6 +1331,12 @@ __global__ void __launch_bounds__(kThreads) k_glisa_trial_set(Batch bt) {
     const int t = e / M, m = e - t * M;
     const double a = ldexp(1.0, -t);
     J.ctrial[e] = fmax(J.propars[m] + a * J.delta[m], 0.0);
+  }
+  if (threadIdx.x == 0) {
+    int n = 0;
+    for (int m = 0; m < M; ++m)
+      if (J.propars[m] + J.delta[m] < 0.0) J.clip[n++] = m;
+    J.clip[M] = n;
   }
 }
 
@@ -1476,16 +1508,28 @@ __global__ void __launch_bounds__(kThreads) k_glisa_trials(Batch bt) {
   double acc[kTrials];
 #pragma unroll
   for (int t = 0; t < kTrials; ++t) acc[t] = 0.0;
+  // rho0_t = sum_m max(c_m + a_t delta_m, 0) g_m
+  //        = rho0 + a_t (G^T delta) + sum_{m clipped at t} -(c_m + a_t delta_m) g_m,
+  // one pass over G plus the few clipped shells instead of kTrials passes
+  const int nclip = J.clip[J.nshell];
   for (int i = 0; i < J.ppt; ++i) {
     const int p = point_of(J, tile, i);
     if (p >= J.npoint) continue;
+    double u = 0.0;
+#pragma unroll 8
+    for (int m = 0; m < J.nshell; ++m) u += J.gmat[(size_t)m * J.npoint + p] * J.delta[m];
     double r0[kTrials];
 #pragma unroll
-    for (int t = 0; t < kTrials; ++t) r0[t] = 0.0;
-    for (int m = 0; m < J.nshell; ++m) {
+    for (int t = 0; t < kTrials; ++t) r0[t] = J.rho0[p] + ldexp(1.0, -t) * u;
+    for (int k = 0; k < nclip; ++k) {
+      const int m = J.clip[k];
       const double g = J.gmat[(size_t)m * J.npoint + p];
+      const double c = J.propars[m], d = J.delta[m];
 #pragma unroll
-      for (int t = 0; t < kTrials; ++t) r0[t] += J.ctrial[t * J.nshell + m] * g;
+      for (int t = 0; t < kTrials; ++t) {
+        const double e = -(c + ldexp(1.0, -t) * d);
+        if (e > 0.0) r0[t] += e * g;
+      }
     }
     const double rho = J.rho[p], w = J.w[p];
 #pragma unroll

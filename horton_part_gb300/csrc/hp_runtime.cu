@@ -93,18 +93,25 @@ struct hp_job {
 
 namespace {
 
-// A mixed-precision job hands over to FP64 when its outer change is within
-// 100 x the threshold, or when the best change of the last 5 iterations is
-// not 10 % better than the best of the 5 before (the FP32 noise floor).
-bool mixed_outer_done(const hp_job* j) {
-  const double thr = j->desc.threshold;
-  if (j->desc.polish && j->change < 100.0 * thr) return true;
+// State of a mixed-precision job after an outer iteration:
+//   MIXED_FLOOR: the outer change has stopped decreasing (the best change of
+//     the last kFloorWindow iterations is not below the best of the window
+//     before): the FP32 noise floor. A slowly but steadily converging job
+//     (linear rate up to 0.999 per iteration) never reaches this state.
+//   MIXED_NEAR: the change is within 100 x the threshold.
+enum MixedState { MIXED_GO = 0, MIXED_NEAR = 1, MIXED_FLOOR = 2 };
+constexpr size_t kFloorWindow = 8;
+
+int mixed_state(const hp_job* j) {
   const size_t n = j->changes.size();
-  if (n < 10) return false;
-  double a = 1e300, b = 1e300;
-  for (size_t i = n - 10; i < n - 5; ++i) a = std::min(a, j->changes[i]);
-  for (size_t i = n - 5; i < n; ++i) b = std::min(b, j->changes[i]);
-  return b > 0.9 * a;
+  if (n >= 2 * kFloorWindow) {
+    double a = 1e300, b = 1e300;
+    for (size_t i = n - 2 * kFloorWindow; i < n - kFloorWindow; ++i) a = std::min(a, j->changes[i]);
+    for (size_t i = n - kFloorWindow; i < n; ++i) b = std::min(b, j->changes[i]);
+    if (b >= 0.999 * a) return MIXED_FLOOR;
+  }
+  if (j->change < 100.0 * j->desc.threshold) return MIXED_NEAR;
+  return MIXED_GO;
 }
 
 }  // namespace
@@ -312,6 +319,7 @@ int step_iterstock(hp_ctx* ctx, const std::vector<hp_job*>& jobs, const HostBatc
     const Mailbox& m = ctx->mail_host[j->slot];
     j->niter = m.i[MI_ITER];
     j->change = m.d[MD_CHANGE];
+    j->changes.push_back(j->change);
     j->warnings |= (uint32_t)m.i[MI_WARN];
     const double inner = m.d[MD_INNER_TOTAL];
     j->inner_total += inner;
@@ -329,20 +337,21 @@ int step_iterstock(hp_ctx* ctx, const std::vector<hp_job*>& jobs, const HostBatc
     } else if (j->change < j->desc.threshold || j->niter >= j->desc.maxiter) {
       j->converged = j->change < j->desc.threshold;
       j->done = true;
-    } else if (j->dev.mixed && mixed_outer_done(j)) {
-      // the FP32-evaluated outer change is near the threshold or has stopped
-      // improving (its noise floor): finish in FP64 (every buffer is rewritten
-      // by the next FP64 pass), or stop here with a warning
-      if (j->desc.polish) {
+    } else if (j->dev.mixed) {
+      // polish: finish in FP64 once the FP32-evaluated change is near the
+      // threshold or at its noise floor (every buffer is rewritten by the
+      // next FP64 pass); without polish, stay in FP32 until the threshold and
+      // stop with a warning only at the noise floor
+      const int st = mixed_state(j);
+      if (j->desc.polish && st != MIXED_GO) {
         j->dev.mixed = 0;
-      } else {
+      } else if (!j->desc.polish && st == MIXED_FLOOR) {
         j->warnings |= HP_WARN_NOISE_FLOOR;
         j->converged = true;
         j->done = true;
       }
     }
     j->prev_change = j->change;
-    j->changes.push_back(j->change);
   }
   return HP_OK;
 }
@@ -754,6 +763,8 @@ int32_t hp_job_create(hp_ctx* ctx, const hp_job_desc* d, hp_job** out) {
     add(&J.ctrial, 8 * (size_t)kTrials * S);
     add(&J.tpart, 8 * (size_t)kTrials * ntile);
     add(&J.freeidx, 4 * (size_t)(S + 1));
+    add(&J.clip, 4 * (size_t)(S + 1));
+    add(&J.rho0, 8 * (size_t)N);
     if (tc) {
       add(&J.gmat32, 4 * (size_t)S * N);
       add(&J.hess_s, 4 * (size_t)N);

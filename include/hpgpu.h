@@ -80,7 +80,11 @@ typedef enum {
 
 typedef enum {
   HP_PRECISION_FP64 = 0,  /* every step in FP64 */
-  HP_PRECISION_MIXED = 1  /* FP32 evaluation, FP64 sums/solves, FP64 polish */
+  HP_PRECISION_MIXED = 1  /* MBIS, GISA, aLISA sc: FP32 evaluation, compensated
+                             sums, FP64 updates and change test (optional FP64
+                             finish, see polish). gLISA Newton solvers: FP64
+                             evaluation, Hessian on the tensor cores (TF32)
+                             with FP64 iterative refinement of the step. */
 } hp_precision;
 
 /* Warning bits reported in hp_job_info.warnings (the reference logs these). */
@@ -125,10 +129,11 @@ typedef struct {
   int32_t maxiter;        /* outer iterations (gLISA: solver iterations) */
   int32_t inner_maxiter;  /* MBIS 2000, aLISA sc 100000, aLISA newton 10000 */
   int32_t linspace_size;  /* line-search trial count (m-newton) */
-  int32_t polish;         /* mixed precision: when the FP32-evaluated outer change
-                             stalls at its noise floor above the threshold,
-                             1 = finish in FP64, 0 = stop there and set
-                             HP_WARN_NOISE_FLOOR */
+  int32_t polish;         /* mixed precision: 1 = finish in FP64 once the
+                             FP32-evaluated outer change is within 100 x the
+                             threshold or has stopped decreasing (its noise
+                             floor); 0 = stay in FP32 to the threshold and stop
+                             with HP_WARN_NOISE_FLOOR only at the floor */
 } hp_job_desc;
 
 typedef struct {

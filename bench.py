@@ -116,6 +116,14 @@ def make_job(ctx, w, precision, pinned=None, mol=None):
 
 POLISH = True
 
+# DRAM bytes (read + write) per launch of the dominant kernel, from one ncu
+# capture of the same workload (ncu --set full; the summaries in profiles/
+# give the commands). Keyed by (workload, precision, kernel family).
+NCU_TRAFFIC = {
+    ("glisa-c6h10n2o2", "mixed", "k_glisa_hess_tc"): 365.12e6 + 3.32e6,
+    ("mbis-chain60", "mixed", "inner"): 125.81e6 + 3.46e6,
+}
+
 
 def measure_tf32_peak(n=8192, reps=10):
     """Best-of-`reps` TF32 GEMM rate of cuBLAS (TFLOP/s, 2 n^3 per product),
@@ -254,13 +262,10 @@ def cpu_sample(w, iterations):
 # arms
 # ---------------------------------------------------------------------------
 
-def dist_env():
-    return int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0")), int(
-        os.environ.get("LOCAL_RANK", "0"))
-
-
 def run_reference(args):
-    world, rank, _ = dist_env()
+    from horton_part_gb300 import replicas
+
+    world, rank, _ = replicas.env()
     if rank != 0:
         return
     # the serving mix has no CPU server; its CPU sample is the MBIS H2O job
@@ -309,14 +314,12 @@ def config_of(w, args, precision):
 def run_ours(args):
     import torch
 
-    world, rank, local = dist_env()
-    if world > 1:
-        import torch.distributed as dist
+    from horton_part_gb300 import replicas
 
-        torch.cuda.set_device(local)
-        dist.init_process_group("nccl")
-    else:
-        torch.cuda.set_device(0)
+    # one process per GPU, each running its own replica of the job: no
+    # collective on the data path, only the barrier and max-over-ranks timing
+    world, rank, local = replicas.init("nccl")
+    torch.cuda.set_device(local if world > 1 else 0)
     from horton_part_gb300 import _lib
     from horton_part_gb300.build import build
 
@@ -343,9 +346,7 @@ def run_ours(args):
     evals_per_job = float(sum(i.point_atom_evals for i in infos))
     niter = max(i.niter for i in infos)
 
-    def barrier():
-        if world > 1:
-            torch.distributed.barrier()
+    barrier = replicas.barrier
 
     ctx.profile(False)  # no per-family events in the timed region; resets the launch counter
     barrier()
@@ -368,11 +369,7 @@ def run_ours(args):
     fam_ms = {f: ctx.profile_get(f) for f in _lib.KERNEL_FAMILIES}
     ctx.profile(False)
     prof_steps = 1
-    ms_max = ms
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms_max = float(t.item())
+    ms_max = replicas.reduce_max(ms)
     value = evals_per_job * args.steps * world / (ms_max / 1000.0)
 
     # end to end through the C ABI: host inputs (pinned), job create (H2D),
@@ -394,7 +391,7 @@ def run_ours(args):
         for j2 in e2e_jobs:
             j2.close()
     torch.cuda.synchronize()
-    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    e2e_s = replicas.reduce_max((time.perf_counter() - t0) / e2e_steps)
     e2e_value = evals_per_job * world / e2e_s
     h2d = int(sum(m.npoint * 5 * 8 + m.natom * 4 * 8 for m in mols))
     d2h = int(sum(r["charges"].nbytes + r["propars"].nbytes for r in q))
@@ -411,31 +408,42 @@ def run_ours(args):
         pass
     hbm_peak = peaks.get("hbm_gbs", 6800.0)
     if w["scheme"] != "glisa":
-        # Dominant kernel family and its algorithmic bytes per launch: the
-        # point-atom evaluations the family performs per step (over all jobs)
-        # times the bytes one evaluation must move at least once.
-        # mixed: xyz hi/lo 24 B, w 4 B, rho_a 4 B (float); fp64: 24 B, 8 B, 8 B
-        mixed = args.precision == "mixed"
-        pt, val = (24.0, 4.0) if mixed else (24.0, 8.0)
+        # Dominant kernel family and its algorithmic bytes per launch: every
+        # per-point array once per launch (all atoms of a point share it)
+        # plus every per-(atom, point) array once. Per point: coordinates
+        # 24 B (FP64, or float hi/lo pairs), w and rho one value each; per
+        # pair: rho_a (and the pro-atom) one value. Value size: mixed 4 B
+        # (FP32), ff and fp64 8 B (float pair or double).
+        val = 4.0 if args.precision == "mixed" else 8.0
+        pt = 24.0
+        n_pts = float(sum(m.npoint for m in mols))
         sum_an = float(sum(m.natom * m.npoint for m in mols))
         inner_evals = float(sum(i.inner_iterations * m.npoint for i, m in zip(infos, mols)))
         if w["scheme"] == "gisa":
             inner_evals = sum_an
-        per_step = {  # (point-atom evals per step, bytes per evaluation)
-            "promol": (sum_an, pt + 5 * val),   # pro-atom write, at_weights read/write, w, rho
-            "inner": (inner_evals, pt + 2 * val),  # coordinates, w, rho_a
-            "change": (sum_an, pt + val),       # coordinates, w
+        per_step = {  # (point-atom evals per step, algorithmic bytes per step)
+            # promolecule + at_weights: points (xyz, w, rho, promol), pro-atom
+            # written, read back and rho_a written
+            "promol": (sum_an, n_pts * (pt + 3 * val) + sum_an * 3 * val),
+            # inner iterations: points (xyz, w) per launch, rho_a per pair
+            "inner": (inner_evals, None),
+            # outer change: points (xyz, w)
+            "change": (sum_an, n_pts * (pt + val)),
         }
         fam = max(per_step, key=lambda f: fam_ms[f][0])
         f_ms, f_n = fam_ms[fam]
         if f_n:
-            evals, bpe = per_step[fam]
+            evals, step_bytes = per_step[fam]
             per_launch_s = f_ms / f_n / 1000.0
             launches_per_step = f_n / prof_steps
-            alg_bytes = evals * bpe / launches_per_step
+            if step_bytes is None:  # inner: per launch, points once plus rho_a per evaluation
+                alg_bytes = n_pts * (pt + val) + evals / launches_per_step * val
+            else:
+                alg_bytes = step_bytes / launches_per_step
             achieved = alg_bytes / per_launch_s / 1e9
             roofline = {"kernel": fam, "bound": "hbm", "achieved": achieved, "peak": hbm_peak,
-                        "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": None,
+                        "unit": "GB/s", "frac": achieved / hbm_peak,
+                        "traffic": NCU_TRAFFIC.get((w["name"], args.precision, fam)),
                         "peak_source": "measured" if peaks else "fallback",
                         "ms_per_launch": per_launch_s * 1000.0,
                         "algorithmic_bytes_per_launch": alg_bytes,
@@ -451,7 +459,8 @@ def run_ours(args):
             tf32 = measure_tf32_peak()
             roofline = {"kernel": "k_glisa_hess_tc", "bound": "tensor", "achieved": achieved,
                         "peak": tf32, "unit": "TFLOP/s", "frac": achieved / tf32,
-                        "traffic": None,
+                        "traffic": NCU_TRAFFIC.get((w["name"], args.precision, "k_glisa_hess_tc")),
+                        "algorithmic_bytes_per_launch": (nshell + 1) * mol.npoint * 4.0,
                         "peak_source": "measured: cuBLAS TF32 GEMM 8192^3, this run",
                         "bf16_peak_measured": peaks.get("bf16_tflops"),
                         "ms_per_launch": per_launch_s * 1000.0,
@@ -510,8 +519,7 @@ def run_ours(args):
         print(json.dumps(line), flush=True)
     job.close()
     ctx.close()
-    if world > 1:
-        torch.distributed.destroy_process_group()
+    replicas.finalize()
 
 
 def serve_requests(nreq, seed, precision):
@@ -550,7 +558,8 @@ def run_serve(args):
     h2d = sum(m.npoint * 5 * 8 + m.natom * 4 * 8 for _, m, _ in pool)
 
     def requests(precision=args.precision):
-        return [request_from_molecule(i, s, m, precision=precision, threshold=1e-8, solver=sv)
+        return [request_from_molecule(i, s, m, precision=precision, threshold=1e-8, solver=sv,
+                                      polish=POLISH)
                 for i, (s, m, sv) in enumerate(pool)]
 
     def serve(arrivals, precision=args.precision):
@@ -631,11 +640,12 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="glisa-c6h10n2o2")
-    ap.add_argument("--precision", default="auto", choices=["auto", "fp64", "mixed"],
-                    help="auto: MBIS mixed (FP32 bulk, FP64 finish); gLISA mixed (tensor-core "
-                         "Hessian, FP64 refinement); GISA FP64 with the basis matrix resident")
+    ap.add_argument("--precision", default="auto", choices=["auto", "fp64", "mixed", "ff"],
+                    help="auto: MBIS mixed (FP32 bulk, float-float finish); gLISA mixed "
+                         "(tensor-core Hessian, FP64 refinement); GISA FP64 with the basis "
+                         "matrix resident. ff: MBIS in float-float throughout")
     ap.add_argument("--no-polish", action="store_true",
-                    help="mixed precision: stop at the FP32 noise floor instead of finishing in FP64")
+                    help="mixed precision: stay in FP32 to the threshold (no finish phase)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-check", action="store_true",
                     help="skip the mixed-precision accuracy run against the FP64 path")

@@ -86,6 +86,9 @@ enum Solver { SOLVER_DEFAULT = 0, SOLVER_SC = 1, SOLVER_NEWTON = 2, SOLVER_M_NEW
               SOLVER_QP = 4, SOLVER_PNEWTON = 5 };
 constexpr int kTrials = 8;  // projected-Newton step lengths 2^-t evaluated per pass
 enum Model { MODEL_MBIS = 0, MODEL_BASIS = 1 };
+// Evaluation phase of a job (JobDev::mixed): FP64, FP32 with compensated sums,
+// or float-float (MBIS).
+enum Phase { PH_FP64 = 0, PH_FP32 = 1, PH_FF = 2 };
 
 struct JobDev {
   // grid
@@ -99,14 +102,18 @@ struct JobDev {
   const float* pzh; const float* pzl;
   const float* wf;
   const float* rhof;
+  const float* wl;        // mixed / ff: low parts of w and rho (w = wf + wl)
+  const float* rhol;
   const float* shf;       // mixed: per shell (order, alpha, prefactor) as FP32
   const float* atf;       // mixed: atom coordinates as FP32 hi/lo [natom][6]
   const double* qp_p;     // GISA: per-atom QP matrix P (K_a x K_a, FP64), at shell_off^2 offsets
   const int* qp_off;      // GISA: offset of atom a's P block (natom + 1)
-  float* fpar;            // mixed: FP32 pro-atom coefficients of propars (2 per shell)
+  float* fpar;            // mixed: FP32 pro-atom coefficients of propars (2 per shell);
+                          // ff: (A hi, A lo, S hi, S lo) per shell
   float* fco;             // mixed: per-shell FP32 coefficients [nshell][8] of a (new, old)
                           // parameter pair: MBIS (A_new, S_new, A_old, S_old, g, dS),
-                          // basis (c_new, c_old - c_new); A = N S^3/(8 pi), g = A_old/A_new - 1
+                          // basis (c_new, c_old - c_new); A = N S^3/(8 pi), g = A_old/A_new - 1;
+                          // MBIS slots 6, 7: low parts of A_new, S_new (ff)
   float* promolf;         // mixed: FP32 promolecule
   // atoms and shells
   const double* ax;
@@ -270,6 +277,8 @@ __device__ __forceinline__ void fill_fco(const JobDev& J, int s, const double* p
     c[3] = (float)s0;
     c[4] = a1 != 0.0 ? (float)(a0 / a1 - 1.0) : 0.0f;
     c[5] = (float)(s1 - s0);
+    c[6] = (float)(a1 - (double)c[0]);
+    c[7] = (float)(s1 - (double)c[1]);
   } else {
     c[0] = (float)pnew[s];
     c[1] = (float)(pold[s] - pnew[s]);
@@ -384,6 +393,11 @@ void launch_mbis_inner_mx(const HostBatch& hb, cudaStream_t st);
 void launch_basis_qvec_mx(const HostBatch& hb, cudaStream_t st);
 void launch_lisa_sc_inner_mx(const HostBatch& hb, cudaStream_t st);
 void launch_final_atweights_mx(const HostBatch& hb, cudaStream_t st, int model, int use_old);
+
+// float-float MBIS (hp_ff.cu)
+void launch_promol_ff(const HostBatch& hb, cudaStream_t st);
+void launch_mbis_inner_ff(const HostBatch& hb, cudaStream_t st);
+void launch_final_atweights_ff(const HostBatch& hb, cudaStream_t st, int use_old);
 
 extern long long g_launch_count;
 

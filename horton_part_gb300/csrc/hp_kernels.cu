@@ -340,7 +340,7 @@ __global__ void k_charges(Batch bt) {
 // threshold happens in the FP64 outer iterations that finish a mixed job.
 __device__ __forceinline__ bool mixed_stalled(const JobDev& J, int a, double change) {
   (void)a;
-  return J.mixed && change < 1e3 * J.inner_threshold;
+  return J.mixed == PH_FP32 && change < 1e3 * J.inner_threshold;
 }
 
 __global__ void k_count_active(Batch bt) {
@@ -1051,11 +1051,13 @@ __global__ void __launch_bounds__(kThreads) k_glisa_pro(Batch bt) {
     const double rho = J.rho[p];
     const double w = J.w[p];
     const bool sick = (rho < J.density_cutoff) || (rho0 < J.density_cutoff);
-    const double ratio = sick ? 0.0 : rho / rho0;
+    const double inv = sick ? 0.0 : 1.0 / rho0;
+    const double ratio = rho * inv;
+    const double d2 = w * ratio * inv;
     J.dvec1[p] = w * ratio;
-    J.dvec2[p] = sick ? 0.0 : w * (ratio / rho0);
+    J.dvec2[p] = d2;
     J.rho0[p] = rho0;
-    if (J.hess_s) J.hess_s[p] = sick ? 0.0f : (float)sqrt(w * (ratio / rho0));
+    if (J.hess_s) J.hess_s[p] = sqrtf((float)d2);
     if (!sick) acc[0] += w * rho * log(ratio);
     if (rho0 < J.negative_cutoff) acc[1] += 1.0;
   }
@@ -1177,37 +1179,58 @@ __global__ void __launch_bounds__(kThreads) k_glisa_reduce(Batch bt) {
   }
 }
 
-// In-place Cholesky factor of the n x n matrix L (row stride n, lower
-// triangle used) by all threads of the block (right-looking, one barrier per
-// column); sets *bad on a non-positive pivot. At step k warp w updates the
-// rows i > k with i = w (mod warps), lanes over the columns k < j <= i, using
-// a copy of the unscaled column k (colbuf[0..n)); the lane that updates
-// entry (i, k+1) copies it into the next column buffer (colbuf[n..2n)), and
-// entry (i, k) is replaced by its scaled value. colbuf: 2n doubles.
-__device__ void chol_factor(double* L, int n, int* bad, double* colbuf) {
+// In-place Cholesky factor of the n x n matrix L (row stride n) by all
+// threads of the block (right-looking, one barrier per column); sets *bad on
+// a non-positive pivot. At step k warp w updates the rows i > k with
+// i = w (mod warps), lanes over the columns k < j <= i, using a copy of the
+// unscaled column k (colbuf[0..n)); the lane that updates entry (i, k+1)
+// copies it into the next column buffer (colbuf[n..2n)), and the lane that
+// updates the next diagonal entry forms the next pivot's square root and
+// reciprocal (one FP64 sqrt and division per column, not per thread).
+// On return L holds the factor in its lower triangle and its transpose in
+// the upper triangle (row-contiguous backward substitution), and dinv[k] =
+// 1 / L[k][k]. colbuf: 2n doubles.
+__device__ void chol_factor(double* L, int n, int* bad, double* colbuf, double* dinv) {
+  __shared__ double piv_s[2], rinv_s[2];  // sqrt(a_kk), 1 / a_kk of the next two steps
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
   double* col = colbuf;
   double* nxt = colbuf + n;
   for (int i = threadIdx.x; i < n; i += blockDim.x) col[i] = L[(size_t)i * n];
+  if (threadIdx.x == 0 && n > 0) {
+    const double a = L[0];
+    if (!(a > 0.0)) *bad = 1;
+    piv_s[0] = sqrt(fmax(a, 1e-300));
+    rinv_s[0] = 1.0 / fmax(a, 1e-300);
+  }
   __syncthreads();
   for (int k = 0; k < n; ++k) {
-    const double akk = col[k];
-    const double piv = sqrt(fmax(akk, 1e-300));
-    const double inv = 1.0 / fmax(akk, 1e-300);
+    const double piv = piv_s[k & 1], rinv = rinv_s[k & 1];
+    const double ipiv = piv * rinv;  // 1 / sqrt(a_kk)
     if (threadIdx.x == 0) {
-      if (!(akk > 0.0)) *bad = 1;
       L[(size_t)k * n + k] = piv;
+      dinv[k] = ipiv;
     }
     for (int i = k + 1 + warp; i < n; i += nwarp) {
       const double ci = col[i];
-      const double li = ci * inv;
+      const double li = ci * rinv;
       double* row = L + (size_t)i * n;
       for (int j = k + 1 + lane; j <= i; j += 32) {
         const double v = row[j] - li * col[j];
         row[j] = v;
-        if (j == k + 1) nxt[i] = v;
+        if (j == k + 1) {
+          nxt[i] = v;
+          if (i == k + 1) {  // the next pivot
+            if (!(v > 0.0)) *bad = 1;
+            piv_s[(k + 1) & 1] = sqrt(fmax(v, 1e-300));
+            rinv_s[(k + 1) & 1] = 1.0 / fmax(v, 1e-300);
+          }
+        }
       }
-      if (lane == 0) row[k] = ci / piv;
+      if (lane == 0) {
+        const double lik = ci * ipiv;
+        row[k] = lik;
+        L[(size_t)k * n + i] = lik;
+      }
     }
     __syncthreads();
     double* t = col;
@@ -1216,26 +1239,29 @@ __device__ void chol_factor(double* L, int n, int* bad, double* colbuf) {
   }
 }
 
-// y <- (L L^T)^-1 y by one warp: forward then backward substitution, each
-// row's dot product split over the lanes and summed by a fixed xor tree.
-__device__ void chol_solve_warp(const double* L, int n, double* y) {
+// y <- (L L^T)^-1 y by one warp with the factor of chol_factor: forward then
+// backward substitution (both over contiguous rows), each row's dot product
+// split over the lanes and summed by a fixed xor tree.
+__device__ void chol_solve_warp(const double* L, const double* dinv, int n, double* y) {
   const int lane = threadIdx.x & 31;
   for (int i = 0; i < n; ++i) {
+    const double* row = L + (size_t)i * n;
     double s = 0.0;
-    for (int j = lane; j < i; j += 32) s += L[(size_t)i * n + j] * y[j];
+    for (int j = lane; j < i; j += 32) s += row[j] * y[j];
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-    const double v = (y[i] - s) / L[(size_t)i * n + i];
+    const double v = (y[i] - s) * dinv[i];
     __syncwarp();
     if (lane == 0) y[i] = v;
     __syncwarp();
   }
   for (int i = n - 1; i >= 0; --i) {
+    const double* row = L + (size_t)i * n;  // upper part: L^T
     double s = 0.0;
-    for (int j = i + 1 + lane; j < n; j += 32) s += L[(size_t)j * n + i] * y[j];
+    for (int j = i + 1 + lane; j < n; j += 32) s += row[j] * y[j];
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-    const double v = (y[i] - s) / L[(size_t)i * n + i];
+    const double v = (y[i] - s) * dinv[i];
     __syncwarp();
     if (lane == 0) y[i] = v;
     __syncwarp();
@@ -1270,12 +1296,14 @@ __global__ void __launch_bounds__(kThreads) k_glisa_newton_step(Batch bt, int pr
   }
   for (int m = threadIdx.x; m < M; m += kThreads) J.delta[m] = 0.0;
   __syncthreads();
-  chol_factor(L, nf, &bad, J.ctrial);  // ctrial (kTrials x nshell) is free until the trial set
+  // ctrial (kTrials x nshell) is free until the trial set: column buffers at
+  // [0, 2 nshell), 1 / diag(L) at [2 nshell, 3 nshell) (kept for the refinement)
+  chol_factor(L, nf, &bad, J.ctrial, J.ctrial + 2 * M);
   if (threadIdx.x < 32) {
     double* y = J.keep;  // scratch (the m-newton mask is formed after the step)
     for (int i = threadIdx.x; i < nf; i += 32) y[i] = -(1.0 + J.grad[J.freeidx[i]]);
     __syncwarp();
-    chol_solve_warp(L, nf, y);
+    chol_solve_warp(L, J.ctrial + 2 * M, nf, y);
     for (int i = threadIdx.x; i < nf; i += 32) J.delta[J.freeidx[i]] = y[i];
     if (threadIdx.x == 0 && bad) atomicOr(&J.mail->i[MI_ERR], E_SINGULAR);
   }
@@ -1315,7 +1343,7 @@ __global__ void __launch_bounds__(kThreads) k_glisa_refine(Batch bt) {
   }
   __syncthreads();
   if (threadIdx.x < 32) {
-    chol_solve_warp(J.chol, nf, r);
+    chol_solve_warp(J.chol, J.ctrial + 2 * M, nf, r);
     for (int i = threadIdx.x; i < nf; i += 32) J.delta[J.freeidx[i]] += r[i];
   }
 }
@@ -1499,28 +1527,35 @@ __global__ void k_glisa_check(Batch bt) {
 // The free-set step is k_glisa_newton_step(projected = 1); the trial points
 // come from k_glisa_trial_set after the optional refinement.
 
-// Trial objectives: tpart[t][tile] = sum_p w rho ln(rho / rho0_t) (sick -> 0).
+// Trial objective differences: tpart[t][tile] = this tile's part of
+// f(c_t) - f(c), f(c) = sum over healthy points of w rho ln(rho / rho0(c)).
+//   rho0_t = sum_m max(c_m + a_t delta_m, 0) g_m
+//          = rho0 + a_t (G^T delta) + sum_{m clipped at t} -(c_m + a_t delta_m) g_m,
+// one pass over G plus the few clipped shells. Where a point is healthy for
+// both, its term is -w rho log1p((rho0_t - rho0) / rho0): the relative change
+// is formed in FP64 and goes through the FP32 log1pf, which keeps each term
+// (and the difference the Armijo test compares) accurate to ~1e-7 of itself
+// without an FP64 log per trial; the few points whose sick status differs
+// between rho0 and rho0_t take FP64 logs. Sums in float-float per thread.
 __global__ void __launch_bounds__(kThreads) k_glisa_trials(Batch bt) {
   __shared__ double red[kWarps * kTrials];
   __shared__ double out[kTrials];
   int tile;
   const JobDev& J = decode_local(bt, tile);
-  double acc[kTrials];
+  float ah[kTrials], al[kTrials];
 #pragma unroll
-  for (int t = 0; t < kTrials; ++t) acc[t] = 0.0;
-  // rho0_t = sum_m max(c_m + a_t delta_m, 0) g_m
-  //        = rho0 + a_t (G^T delta) + sum_{m clipped at t} -(c_m + a_t delta_m) g_m,
-  // one pass over G plus the few clipped shells instead of kTrials passes
+  for (int t = 0; t < kTrials; ++t) ah[t] = al[t] = 0.0f;
   const int nclip = J.clip[J.nshell];
+  const double cut = J.density_cutoff;
   for (int i = 0; i < J.ppt; ++i) {
     const int p = point_of(J, tile, i);
     if (p >= J.npoint) continue;
     double u = 0.0;
 #pragma unroll 8
     for (int m = 0; m < J.nshell; ++m) u += J.gmat[(size_t)m * J.npoint + p] * J.delta[m];
-    double r0[kTrials];
+    double corr[kTrials];
 #pragma unroll
-    for (int t = 0; t < kTrials; ++t) r0[t] = J.rho0[p] + ldexp(1.0, -t) * u;
+    for (int t = 0; t < kTrials; ++t) corr[t] = 0.0;
     for (int k = 0; k < nclip; ++k) {
       const int m = J.clip[k];
       const double g = J.gmat[(size_t)m * J.npoint + p];
@@ -1528,14 +1563,37 @@ __global__ void __launch_bounds__(kThreads) k_glisa_trials(Batch bt) {
 #pragma unroll
       for (int t = 0; t < kTrials; ++t) {
         const double e = -(c + ldexp(1.0, -t) * d);
-        if (e > 0.0) r0[t] += e * g;
+        if (e > 0.0) corr[t] += e * g;
       }
     }
-    const double rho = J.rho[p], w = J.w[p];
+    const double rho = J.rho[p], w = J.w[p], r0 = J.rho0[p];
+    const bool h0 = !(rho < cut || r0 < cut);
+    const double inv = h0 ? 1.0 / r0 : 0.0;
+    const float wr = (float)(w * rho);
 #pragma unroll
-    for (int t = 0; t < kTrials; ++t)
-      if (!(rho < J.density_cutoff || r0[t] < J.density_cutoff)) acc[t] += w * rho * log(rho / r0[t]);
+    for (int t = 0; t < kTrials; ++t) {
+      const double dr = ldexp(1.0, -t) * u + corr[t];
+      const double rt = r0 + dr;
+      const bool ht = !(rho < cut || rt < cut);
+      double big = 0.0;
+      float term = 0.0f;
+      if (h0 && ht) term = -wr * log1pf((float)(dr * inv));
+      else if (ht) big = w * rho * log(rho / rt);
+      else if (h0) big = -(w * rho * log(rho / r0));
+      if (big != 0.0) {
+        const float bh = (float)big;
+        term = bh;
+        al[t] += (float)(big - (double)bh);
+      }
+      const float s = ah[t] + term;  // TwoSum into (ah, al)
+      const float bb = s - ah[t];
+      al[t] += (ah[t] - (s - bb)) + (term - bb);
+      ah[t] = s;
+    }
   }
+  double acc[kTrials];
+#pragma unroll
+  for (int t = 0; t < kTrials; ++t) acc[t] = (double)ah[t] + (double)al[t];
   block_sum<kTrials>(acc, red, out);
   if (threadIdx.x < kTrials) J.tpart[(size_t)threadIdx.x * J.ntile + tile] = out[threadIdx.x];
 }
@@ -1546,12 +1604,10 @@ __global__ void k_glisa_trial_pick(Batch bt) {
   const JobDev& J = decode_local(bt, local);
   const int lane = threadIdx.x & 31;
   const int M = J.nshell;
-  const double f0 = warp_tile_sum(J, J.jpart + (size_t)QJ_ENTROPY * J.ntile, J.ntile);
   double c0 = 0.0;
   for (int m = lane; m < M; m += 32) c0 += J.propars[m];
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) c0 += __shfl_xor_sync(0xffffffffu, c0, o);
-  const double F0 = f0 + c0;
   int pick = kTrials - 1;
   for (int t = 0; t < kTrials; ++t) {
     double s = 0.0, dec = 0.0;
@@ -1565,11 +1621,12 @@ __global__ void k_glisa_trial_pick(Batch bt) {
       s += __shfl_xor_sync(0xffffffffu, s, o);
       dec += __shfl_xor_sync(0xffffffffu, dec, o);
     }
-    double ft = 0.0;
-    for (int q = lane; q < J.ntile; q += 32) ft += J.tpart[(size_t)t * J.ntile + q];
+    double df = 0.0;  // f(c_t) - f(c)
+    for (int q = lane; q < J.ntile; q += 32) df += J.tpart[(size_t)t * J.ntile + q];
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) ft += __shfl_xor_sync(0xffffffffu, ft, o);
-    if (ft + s <= F0 + 1e-4 * dec) {
+    for (int o = 16; o > 0; o >>= 1) df += __shfl_xor_sync(0xffffffffu, df, o);
+    // Armijo on F = f + sum c: F(c_t) <= F(c) + 1e-4 dF.(c_t - c)
+    if (df + (s - c0) <= 1e-4 * dec) {
       pick = t;
       break;
     }
@@ -1599,8 +1656,10 @@ void launch_nelec(const HostBatch& hb, cudaStream_t st) {
 
 void launch_copy_old(const HostBatch& hb, cudaStream_t st) { HP_LAUNCH(k_copy_old, K_JOB, 128); }
 
-// Mixed-precision variants live in hp_mixed.cu.
+// FP32 variants live in hp_mixed.cu, float-float (MBIS) in hp_ff.cu; `mixed`
+// is the job group's evaluation phase (Phase).
 void launch_promol(const HostBatch& hb, cudaStream_t st, int mixed, int model) {
+  if (mixed == PH_FF && model == MODEL_MBIS) return launch_promol_ff(hb, st);
   if (mixed) return launch_promol_mx(hb, st, model);
   if (model == MODEL_MBIS) HP_LAUNCH((k_promol<double, MODEL_MBIS>), K_POINT1, kThreads);
   else HP_LAUNCH((k_promol<double, MODEL_BASIS>), K_POINT1, kThreads);
@@ -1609,6 +1668,7 @@ void launch_promol(const HostBatch& hb, cudaStream_t st, int mixed, int model) {
 
 void launch_final_atweights(const HostBatch& hb, cudaStream_t st, int mixed, int model,
                             int use_old) {
+  if (mixed == PH_FF && model == MODEL_MBIS) return launch_final_atweights_ff(hb, st, use_old);
   if (mixed) return launch_final_atweights_mx(hb, st, model, use_old);
   if (model == MODEL_MBIS) HP_LAUNCH((k_final_atweights<double, MODEL_MBIS>), K_ATOM_TILE, kThreads, use_old);
   else HP_LAUNCH((k_final_atweights<double, MODEL_BASIS>), K_ATOM_TILE, kThreads, use_old);
@@ -1633,7 +1693,8 @@ void launch_count_active(const HostBatch& hb, cudaStream_t st) {
 }
 
 void launch_mbis_inner(const HostBatch& hb, cudaStream_t st, int mixed) {
-  if (mixed) launch_mbis_inner_mx(hb, st);
+  if (mixed == PH_FF) launch_mbis_inner_ff(hb, st);
+  else if (mixed) launch_mbis_inner_mx(hb, st);
   else HP_LAUNCH(k_mbis_inner<double>, K_ATOM_TILE, kThreads);
   HP_LAUNCH(k_mbis_update, K_ATOM, 32);
 }

@@ -87,7 +87,7 @@ struct hp_job {
   double inner_total = 0.0;
   bool converged = false;
   double prev_change = 1e300;
-  int polish_iters = 0;  // FP64 outer iterations after a mixed-precision stall
+  int polish_iters = 0;  // outer iterations of a mixed job after its FP32 phase (FF or FP64)
   std::vector<double> changes;  // outer changes of this run
 };
 
@@ -329,7 +329,7 @@ int step_iterstock(hp_ctx* ctx, const std::vector<hp_job*>& jobs, const HostBatc
     const double a = (double)j->dev.natom;
     const double inner_evals = j->desc.scheme == HP_SCHEME_GISA ? a : inner;
     j->evals += n * (3.0 * a + inner_evals);
-    if (j->dev.mixed == 0 && j->desc.precision == HP_PRECISION_MIXED) j->polish_iters += 1;
+    if (j->dev.mixed != PH_FP32 && j->desc.precision == HP_PRECISION_MIXED) j->polish_iters += 1;
     if (m.i[MI_ERR]) {
       j->status = status_of(m.i[MI_ERR]);
       g_err = err_text(m.i[MI_ERR]);
@@ -337,14 +337,16 @@ int step_iterstock(hp_ctx* ctx, const std::vector<hp_job*>& jobs, const HostBatc
     } else if (j->change < j->desc.threshold || j->niter >= j->desc.maxiter) {
       j->converged = j->change < j->desc.threshold;
       j->done = true;
-    } else if (j->dev.mixed) {
+    } else if (j->dev.mixed == PH_FP32) {
       // polish: finish in FP64 once the FP32-evaluated change is near the
       // threshold or at its noise floor (every buffer is rewritten by the
       // next FP64 pass); without polish, stay in FP32 until the threshold and
       // stop with a warning only at the noise floor
       const int st = mixed_state(j);
       if (j->desc.polish && st != MIXED_GO) {
-        j->dev.mixed = 0;
+        // MBIS finishes in float-float (FP64-class results on the FP32
+        // pipes), the basis schemes in FP64
+        j->dev.mixed = j->desc.scheme == HP_SCHEME_MBIS ? PH_FF : PH_FP64;
       } else if (!j->desc.polish && st == MIXED_FLOOR) {
         j->warnings |= HP_WARN_NOISE_FLOOR;
         j->converged = true;
@@ -550,7 +552,10 @@ int validate(const hp_job_desc* d) {
     return fail(HP_ERR_UNSUPPORTED, "the projected Newton solver is for gLISA");
   if (d->linspace_size > 64 || (d->scheme == HP_SCHEME_LISA && d->linspace_size > 32))
     return fail(HP_ERR_UNSUPPORTED, "linspace_size too large");
-  if (d->precision != HP_PRECISION_FP64 && d->precision != HP_PRECISION_MIXED)
+  if (d->precision == HP_PRECISION_FF && d->scheme != HP_SCHEME_MBIS)
+    return fail(HP_ERR_UNSUPPORTED, "float-float evaluation is available for MBIS");
+  if (d->precision != HP_PRECISION_FP64 && d->precision != HP_PRECISION_MIXED &&
+      d->precision != HP_PRECISION_FF)
     return fail(HP_ERR_INVALID, "unknown precision");
   if (d->precision == HP_PRECISION_MIXED && d->scheme == HP_SCHEME_LISA &&
       d->solver != HP_SOLVER_SC && d->solver != HP_SOLVER_DEFAULT)
@@ -680,7 +685,7 @@ int32_t hp_job_create(hp_ctx* ctx, const hp_job_desc* d, hp_job** out) {
   // tiles: aim for >= 2 * 152 point tiles when the grid is large enough
   // (mixed precision: at least 4 points per thread so the per-block
   // compensated reductions are amortised)
-  const int ppt_min = d->precision == HP_PRECISION_MIXED && !glisa ? 4 : 2;
+  const int ppt_min = d->precision != HP_PRECISION_FP64 && !glisa ? 4 : 2;
   int ppt = (int)std::min<int64_t>(64, std::max<int64_t>(ppt_min, (N + kThreads * 304 - 1) / (kThreads * 304)));
   const int tile_points = kThreads * ppt;
   const int ntile = (N + tile_points - 1) / tile_points;
@@ -688,19 +693,20 @@ int32_t hp_job_create(hp_ctx* ctx, const hp_job_desc* d, hp_job** out) {
   if (d->scheme == HP_SCHEME_LISA && solver != HP_SOLVER_SC) qa = 2 + kNewtonQ(kmax);
   const int maxiter = d->maxiter;
   // gLISA keeps FP64 evaluation; its mixed mode is the tensor-core Hessian
-  const bool mixed = d->precision == HP_PRECISION_MIXED && !glisa;
+  // FP32 / float-float buffers (mixed precision and ff)
+  const bool mixed = d->precision != HP_PRECISION_FP64 && !glisa;
   const bool tc = d->precision == HP_PRECISION_MIXED && glisa;
   const int htiles = glisa ? (S + kHessTile - 1) / kHessTile : 0;
   const int npair = htiles * (htiles + 1) / 2;
   int nsplit = glisa ? std::max(1, std::min(1024, (4 * 152 + npair - 1) / std::max(1, npair))) : 0;
   if (glisa) nsplit = std::max(1, std::min(nsplit, (N + 255) / 256));
   if (tc) {
-    // two 128-thread CTAs per SM (about 97 KB of shared memory each)
+    // one 256-thread CTA per SM (two 97 KB shared-memory stages)
     JobDev probe{};
     probe.nshell = S;
     probe.nsplit = 1;
     const int tiles = tc_hess_blocks(probe);
-    nsplit = std::max(1, std::min((2 * 152 + tiles - 1) / tiles, (N + 255) / 256));
+    nsplit = std::max(1, std::min((152 + tiles - 1) / tiles, (N + 255) / 256));
   }
 
   // carve one allocation
@@ -715,7 +721,8 @@ int32_t hp_job_create(hp_ctx* ctx, const hp_job_desc* d, hp_job** out) {
     add(&J.pyh, 4 * (size_t)N); add(&J.pyl, 4 * (size_t)N);
     add(&J.pzh, 4 * (size_t)N); add(&J.pzl, 4 * (size_t)N);
     add(&J.wf, 4 * (size_t)N); add(&J.rhof, 4 * (size_t)N); add(&J.promolf, 4 * (size_t)N);
-    add(&J.shf, 4 * 3 * (size_t)S); add(&J.fpar, 4 * 2 * (size_t)S);
+    add(&J.wl, 4 * (size_t)N); add(&J.rhol, 4 * (size_t)N);
+    add(&J.shf, 4 * 3 * (size_t)S); add(&J.fpar, 4 * 4 * (size_t)S);
     add(&J.atf, 4 * 6 * (size_t)A);
     add(&J.fco, 4 * 8 * (size_t)S);
   }
@@ -791,7 +798,8 @@ int32_t hp_job_create(hp_ctx* ctx, const hp_job_desc* d, hp_job** out) {
   }
   J.mail = ctx->mail_dev + slot;
   J.natom = A; J.npoint = N; J.ntile = ntile; J.nparam = P; J.nshell = S; J.qa = qa;
-  J.scheme = d->scheme; J.solver = solver; J.mixed = mixed; J.maxiter = maxiter;
+  J.scheme = d->scheme; J.solver = solver; J.maxiter = maxiter;
+  J.mixed = !mixed ? PH_FP64 : d->precision == HP_PRECISION_FF ? PH_FF : PH_FP32;
   J.inner_maxiter = d->inner_maxiter > 0 ? d->inner_maxiter : 2000;
   J.linspace_size = d->linspace_size > 0 ? d->linspace_size : (glisa ? 40 : 20);
   J.nsplit = nsplit; J.ppt = ppt; J.tile_points = tile_points; J.htiles = htiles;
@@ -835,16 +843,22 @@ int32_t hp_job_create(hp_ctx* ctx, const hp_job_desc* d, hp_job** out) {
   }
   ok &= up(J.w, d->weights, 8 * (size_t)N) == cudaSuccess;
   ok &= up(J.rho, d->density, 8 * (size_t)N) == cudaSuccess;
-  std::vector<float> wf32, rf32;
+  std::vector<float> wf32, rf32, wl32, rl32;
   if (mixed) {
     wf32.resize((size_t)N);
     rf32.resize((size_t)N);
+    wl32.resize((size_t)N);
+    rl32.resize((size_t)N);
     for (int p = 0; p < N; ++p) {
       wf32[p] = (float)d->weights[p];
       rf32[p] = (float)d->density[p];
+      wl32[p] = (float)(d->weights[p] - (double)wf32[p]);
+      rl32[p] = (float)(d->density[p] - (double)rf32[p]);
     }
     ok &= up(J.wf, wf32.data(), 4 * (size_t)N) == cudaSuccess;
     ok &= up(J.rhof, rf32.data(), 4 * (size_t)N) == cudaSuccess;
+    ok &= up(J.wl, wl32.data(), 4 * (size_t)N) == cudaSuccess;
+    ok &= up(J.rhol, rl32.data(), 4 * (size_t)N) == cudaSuccess;
   }
   std::vector<double> ac((size_t)A);
   for (int c = 0; c < 3 && ok; ++c) {
@@ -1009,8 +1023,10 @@ int32_t hp_job_reset(hp_job* job) {
   job->prev_change = 1e300;
   job->polish_iters = 0;
   job->changes.clear();
-  job->dev.mixed =
-      job->desc.precision == HP_PRECISION_MIXED && job->desc.scheme != HP_SCHEME_GLISA ? 1 : 0;
+  if (job->desc.scheme == HP_SCHEME_GLISA || job->desc.precision == HP_PRECISION_FP64)
+    job->dev.mixed = PH_FP64;
+  else
+    job->dev.mixed = job->desc.precision == HP_PRECISION_FF ? PH_FF : PH_FP32;
   return HP_OK;
 }
 

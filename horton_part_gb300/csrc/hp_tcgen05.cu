@@ -5,16 +5,18 @@
 //
 // Output tiles cover the lower triangle of H: row block i0 (128 rows, the
 // UMMA M) against column block j0 (N columns, a multiple of 16 up to 256,
-// ending at the tile's last row). One CTA (128 threads) computes one tile
-// over one range of grid points. Per block of 32 points the threads load G
-// (FP32 copy) and s for the next block into registers while the tensor core
-// works on the current one, then form X, split it into two TF32 parts
-// X = X_hi + X_lo (cvt.rna.tf32) and write A (128 x 32) and B (N x 32)
-// K-major into shared memory in the 128-byte-swizzled layout; one thread
-// issues tcgen05.mma.kind::tf32 (M = 128, K = 8) for X_hi X_hi^T,
-// X_hi X_lo^T and X_lo X_hi^T into one FP32 accumulator in tensor memory and
-// commits to an mbarrier. The accumulator is read back with tcgen05.ld and
-// written as the CTA's partial; partials over point ranges are summed in FP64
+// ending at the tile's last row). One CTA (256 threads, one per SM: two
+// 97 KB stages of shared memory) computes one tile over one range of grid
+// points. Per block
+// of 32 points the threads form X from G (FP32 copy) and s, split it into two
+// TF32 parts X = X_hi + X_lo (cvt.rna.tf32) and write A (128 x 32) and B
+// (N x 32) K-major into one of two shared-memory stages in the
+// 128-byte-swizzled layout; one thread issues tcgen05.mma.kind::tf32
+// (M = 128, K = 8) for X_hi X_hi^T, X_hi X_lo^T and X_lo X_hi^T into one FP32
+// accumulator in tensor memory and commits to the stage's mbarrier. While
+// the tensor core works on block k, the threads load block k+1's operands
+// into registers and stage them into the other buffer. The accumulator is
+// read back with tcgen05.ld and written as the CTA's partial; partials over point ranges are summed in FP64
 // in a fixed order (k_glisa_reduce). Relative accuracy of H is about 1e-7
 // (the dropped X_lo X_lo^T term and FP32 accumulation); the Newton step is
 // refined against the exact FP64 product H delta (k_glisa_refine), so the
@@ -34,19 +36,21 @@ namespace {
 constexpr int kTcM = 128;       // UMMA M
 constexpr int kTcNMax = 256;    // largest UMMA N
 constexpr int kTcK = 32;        // points per block: 32 x 4 B = one 128-byte swizzle row
-constexpr int kTcThreads = 128; // one warpgroup (tensor-memory lanes 0..127)
+constexpr int kTcThreads = 256; // two warpgroups (each covers tensor-memory lanes 0..127)
 constexpr int kTcWarps = kTcThreads / 32;
 constexpr int kRowsA = kTcM / kTcWarps;     // A rows staged per warp
 constexpr int kRowsB = kTcNMax / kTcWarps;  // B rows staged per warp (at most)
 constexpr int kTcCols = 256;    // tensor-memory columns (FP32 accumulator, N <= 256)
 constexpr long long kWaitLimit = 1ll << 26;
 
-// shared-memory layout (offsets from a 1024-byte-aligned base)
+// shared-memory layout (offsets from a 1024-byte-aligned base): two stages
+// of (A_hi, A_lo, B_hi, B_lo), then the stages' mbarriers and the TMEM slot
 constexpr int kOffAhi = 0;
 constexpr int kOffAlo = kOffAhi + kTcM * kTcK * 4;     // 16 KB
 constexpr int kOffBhi = kOffAlo + kTcM * kTcK * 4;     // 32 KB
 constexpr int kOffBlo = kOffBhi + kTcNMax * kTcK * 4;  // 64 KB
-constexpr int kOffBar = kOffBlo + kTcNMax * kTcK * 4;  // 96 KB
+constexpr int kStageBytes = kOffBlo + kTcNMax * kTcK * 4;  // 96 KB
+constexpr int kOffBar = 2 * kStageBytes;               // 192 KB
 constexpr int kSmemBytes = kOffBar + 64 + 1024;        // + alignment slack
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -152,11 +156,7 @@ __global__ void __launch_bounds__(kTcThreads) k_glisa_hess_tc(Batch bt) {
   const uint32_t raw = smem_u32(smem_raw);
   const uint32_t base = (raw + 1023u) & ~1023u;
   uint8_t* sm = smem_raw + (base - raw);
-  uint32_t* a_hi = reinterpret_cast<uint32_t*>(sm + kOffAhi);
-  uint32_t* a_lo = reinterpret_cast<uint32_t*>(sm + kOffAlo);
-  uint32_t* b_hi = reinterpret_cast<uint32_t*>(sm + kOffBhi);
-  uint32_t* b_lo = reinterpret_cast<uint32_t*>(sm + kOffBlo);
-  const uint32_t bar = base + kOffBar;
+  const uint32_t bar0 = base + kOffBar;  // stage s: bar0 + 8 s
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(sm + kOffBar + 16);
   __shared__ int timed_out;
 
@@ -181,7 +181,8 @@ __global__ void __launch_bounds__(kTcThreads) k_glisa_hess_tc(Batch bt) {
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
   if (threadIdx.x == 0) {
-    mbar_init(bar, 1);
+    mbar_init(bar0, 1);
+    mbar_init(bar0 + 8, 1);
     timed_out = 0;
     asm volatile("fence.mbarrier_init.release.cluster;");
   }
@@ -190,7 +191,7 @@ __global__ void __launch_bounds__(kTcThreads) k_glisa_hess_tc(Batch bt) {
   asm volatile("tcgen05.fence::after_thread_sync;");
   const uint32_t tmem = *tmem_slot;
 
-  // rows of this thread: A rows warp + 4 r (r < 32), B rows warp + 4 r (row < ncol)
+  // rows of this thread: A rows warp + 8 r (r < 16), B rows warp + 8 r (row < ncol)
   float va[kRowsA], vb[kRowsB], s = 0.0f;
   auto load_block = [&](int kb) {
     const int p = kb + lane;
@@ -209,15 +210,19 @@ __global__ void __launch_bounds__(kTcThreads) k_glisa_hess_tc(Batch bt) {
     }
   };
 
-  uint32_t phase = 0;
   int nblocks = 0;
   if (pbeg < pend) load_block(pbeg);
-  for (int kb = pbeg; kb < pend; kb += kTcK) {
-    if (nblocks > 0) {  // the previous block's MMAs must have read shared memory
-      if (!mbar_wait(bar, phase)) timed_out = 1;
-      phase ^= 1u;
-      __syncthreads();
-      if (timed_out) break;
+  for (int kb = pbeg; kb < pend; kb += kTcK, ++nblocks) {
+    const int st = nblocks & 1;
+    uint8_t* stage = sm + st * kStageBytes;
+    uint32_t* a_hi = reinterpret_cast<uint32_t*>(stage + kOffAhi);
+    uint32_t* a_lo = reinterpret_cast<uint32_t*>(stage + kOffAlo);
+    uint32_t* b_hi = reinterpret_cast<uint32_t*>(stage + kOffBhi);
+    uint32_t* b_lo = reinterpret_cast<uint32_t*>(stage + kOffBlo);
+    if (nblocks >= 2) {
+      // the MMAs of block nblocks - 2 (the stage's previous commit, number
+      // (nblocks >> 1) - 1 on this barrier) must have read the stage
+      if (!mbar_wait(bar0 + 8 * st, (uint32_t)(((nblocks >> 1) - 1) & 1))) timed_out = 1;
     }
 #pragma unroll
     for (int r = 0; r < kRowsA; ++r) {
@@ -240,6 +245,7 @@ __global__ void __launch_bounds__(kTcThreads) k_glisa_hess_tc(Batch bt) {
     }
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     __syncthreads();
+    if (timed_out) break;
     if (threadIdx.x == 0) {
       asm volatile("tcgen05.fence::after_thread_sync;");
       const uint32_t ahi = smem_u32(a_hi), alo = smem_u32(a_lo);
@@ -251,26 +257,31 @@ __global__ void __launch_bounds__(kTcThreads) k_glisa_hess_tc(Batch bt) {
         umma_tf32(tmem, umma_desc(ahi + 32 * k), umma_desc(blo + 32 * k), idesc, 1u);
         umma_tf32(tmem, umma_desc(alo + 32 * k), umma_desc(bhi + 32 * k), idesc, 1u);
       }
-      umma_commit(bar);
+      umma_commit(bar0 + 8 * st);
     }
-    ++nblocks;
     // the next block's operands into registers while the tensor core runs
     if (kb + kTcK < pend) load_block(kb + kTcK);
   }
   if (nblocks > 0 && !timed_out) {
-    if (!mbar_wait(bar, phase)) timed_out = 1;
+    // the last commit covers every MMA issued before it
+    const int last = nblocks - 1;
+    if (!mbar_wait(bar0 + 8 * (last & 1), (uint32_t)((last >> 1) & 1))) timed_out = 1;
   }
   asm volatile("tcgen05.fence::after_thread_sync;");
   __syncthreads();
 
-  // epilogue: warp w reads tensor-memory lanes 32w..32w+31 = rows of the tile
+  // epilogue: warp w reads tensor-memory lanes 32 (w % 4) .. + 31 (rows of the
+  // tile); warps 0-3 take the first half of the columns, warps 4-7 the rest
   double* out = J.hpart + (size_t)split * M * M;
-  const int i = i0 + warp * 32 + lane;
+  const int quad = warp & 3;
+  const int i = i0 + quad * 32 + lane;
   const bool ok = nblocks > 0 && !timed_out;
-  for (int c = 0; c < ncol; c += 8) {
+  const int half = ncol / 2;  // a multiple of 8
+  const int c0 = warp < 4 ? 0 : half, c1 = warp < 4 ? half : ncol;
+  for (int c = c0; c < c1; c += 8) {
     uint32_t v[8];
     if (ok) {
-      const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c;
+      const uint32_t taddr = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)c;
       asm volatile(
           "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
           : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),

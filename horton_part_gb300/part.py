@@ -8,7 +8,12 @@ replaces the Python stockholder loop (``core/stockholder.py``,
 
 GPU-only options (keyword arguments, all optional):
 
-``precision``   ``"fp64"`` (default: every step in FP64) or ``"mixed"``.
+``precision``   ``"fp64"`` (default: every step in FP64), ``"mixed"`` (FP32
+                evaluation with compensated sums and FP64 updates; gLISA: the
+                Hessian on the tensor cores) or ``"ff"`` (MBIS: float-float
+                evaluation on the FP32 pipes, FP64-class results).
+``polish``      mixed precision: finish near the threshold in float-float
+                (MBIS) or FP64 (default ``True``).
 ``context``     a :class:`horton_part_gb300._lib.Context` (device, stream,
                 HBM budget); default: one shared context on device 0.
 ``store_at_weights``  fetch the per-atom ``at_weights_{i}`` arrays into the
@@ -301,8 +306,8 @@ class GPUStockholderWPart(WPart):
         self._threshold = threshold
         self._inner_threshold = inner_threshold if inner_threshold < threshold else threshold
         self._maxiter = maxiter
-        if precision not in ("fp64", "mixed"):
-            raise ValueError("precision must be 'fp64' or 'mixed'")
+        if precision not in ("fp64", "mixed", "ff"):
+            raise ValueError("precision must be 'fp64', 'mixed' or 'ff'")
         self._precision = precision
         self._polish = polish
         self._context = context

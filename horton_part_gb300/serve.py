@@ -57,11 +57,15 @@ class Request:
 
 
 def request_from_molecule(rid, scheme, mol, precision="fp64", threshold=1e-8, solver="default",
-                          basis="gauss", maxiter=None):
-    """Build a request for ``mol`` (a :class:`~horton_part_gb300.synthetic.Molecule`)."""
+                          basis="gauss", maxiter=None, polish=True):
+    """Build a request for ``mol`` (a :class:`~horton_part_gb300.synthetic.Molecule`).
+
+    ``polish`` (mixed precision): finish near the threshold in float-float
+    (MBIS) or FP64 (basis schemes)."""
     arrays = dict(coordinates=mol.coordinates, pseudo_numbers=mol.pseudo_numbers,
                   points=mol.grid.points, weights=mol.grid.weights, density=mol.density)
-    opts = dict(precision=precision, threshold=threshold, solver=solver, grid_type=3)
+    opts = dict(precision=precision, threshold=threshold, solver=solver, grid_type=3,
+                polish=bool(polish))
     if scheme == "mbis":
         nsh = [int(get_nshell(z)) for z in mol.numbers]
         arrays["shell_offsets"] = np.concatenate([[0], np.cumsum(nsh)]).astype(np.int32)

@@ -80,11 +80,15 @@ typedef enum {
 
 typedef enum {
   HP_PRECISION_FP64 = 0,  /* every step in FP64 */
-  HP_PRECISION_MIXED = 1  /* MBIS, GISA, aLISA sc: FP32 evaluation, compensated
-                             sums, FP64 updates and change test (optional FP64
-                             finish, see polish). gLISA Newton solvers: FP64
+  HP_PRECISION_MIXED = 1, /* MBIS, GISA, aLISA sc: FP32 evaluation, compensated
+                             sums, FP64 updates and change test (optional
+                             finish, see polish: float-float for MBIS, FP64 for
+                             the basis schemes). gLISA Newton solvers: FP64
                              evaluation, Hessian on the tensor cores (TF32)
                              with FP64 iterative refinement of the step. */
+  HP_PRECISION_FF = 2     /* MBIS: every evaluation in float-float arithmetic
+                             (about 48 significant bits) on the FP32 pipes,
+                             FP64 updates and tests: FP64-class results */
 } hp_precision;
 
 /* Warning bits reported in hp_job_info.warnings (the reference logs these). */
@@ -129,11 +133,12 @@ typedef struct {
   int32_t maxiter;        /* outer iterations (gLISA: solver iterations) */
   int32_t inner_maxiter;  /* MBIS 2000, aLISA sc 100000, aLISA newton 10000 */
   int32_t linspace_size;  /* line-search trial count (m-newton) */
-  int32_t polish;         /* mixed precision: 1 = finish in FP64 once the
-                             FP32-evaluated outer change is within 100 x the
-                             threshold or has stopped decreasing (its noise
-                             floor); 0 = stay in FP32 to the threshold and stop
-                             with HP_WARN_NOISE_FLOOR only at the floor */
+  int32_t polish;         /* mixed precision: 1 = finish in float-float (MBIS)
+                             or FP64 (basis schemes) once the FP32-evaluated
+                             outer change is within 100 x the threshold or has
+                             stopped decreasing (its noise floor); 0 = stay in
+                             FP32 to the threshold and stop with
+                             HP_WARN_NOISE_FLOOR only at the floor */
 } hp_job_desc;
 
 typedef struct {

@@ -15,6 +15,12 @@ convergence) on inputs already resident in HBM; the basis matrix G
 (150 x 604,000 FP64 = 725 MB) is larger than L2, so no L2 flush is added
 between steps.
 
+Batched workloads (mbis-batch<N>: N molecules of 3-60 atoms, 75 x
+Lebedev-194 per atom): a step is one outer iteration of every live job (one
+pass of the loop over the whole batch, shared launches); the batch converges
+over hundreds of such steps, so W warm-up and K timed steps are the first
+W + K iterations from the initial parameters.
+
 Metric: pro-atom evaluations (point x atom) per second, counted in the
 reference's convention (gLISA: each solver iteration evaluates every pro-atom
 on every grid point three times: promolecule and the two sides of the change;
@@ -332,20 +338,32 @@ def run_ours(args):
     jobs = [make_job(ctx, w, args.precision, mol=m) for m in mols]
     job = jobs[0]
 
+    # A step: for one molecule, one complete job (every iteration to
+    # convergence); for a batch of molecules, one outer iteration of every
+    # live job (the batch converges over hundreds of such steps).
+    batched = len(mols) > 1
+
     def run_all(js):
-        # one step of the benchmark: every job from its initial parameters to
-        # convergence, all live jobs advanced together by hp_step
         for j in js:
             j.reset()
         while ctx.step(js) > 0:
             pass
 
-    for _ in range(args.warmup):
-        run_all(jobs)
-    infos = [j.info() for j in jobs]
-    evals_per_job = float(sum(i.point_atom_evals for i in infos))
-    niter = max(i.niter for i in infos)
+    def one_step(js):
+        if batched:
+            ctx.step(js)
+        else:
+            run_all(js)
 
+    def snapshot(js):
+        return [(i.point_atom_evals, i.niter, i.inner_iterations) for i in (j.info() for j in js)]
+
+    if batched:
+        for j in jobs:
+            j.reset()
+    for _ in range(args.warmup):
+        one_step(jobs)
+    before = snapshot(jobs)
     barrier = replicas.barrier
 
     ctx.profile(False)  # no per-family events in the timed region; resets the launch counter
@@ -355,29 +373,43 @@ def run_ours(args):
     with ClockSampler(torch.cuda.current_device()) as clocks:
         start.record(stream)
         for _ in range(args.steps):
-            run_all(jobs)
+            one_step(jobs)
         end.record(stream)
         torch.cuda.synchronize()
     barrier()
     ms = start.elapsed_time(end)
     launches = ctx.launch_count()
+    after = snapshot(jobs)
+    if batched:
+        evals_timed = sum(a[0] - b[0] for a, b in zip(after, before))
+    else:
+        evals_timed = args.steps * sum(a[0] for a in after)
+    niter = max(a[1] for a in after)
     # one more step with CUDA events around each kernel family (on the
     # launching stream) for the per-family times and the roofline
     ctx.profile(True)
-    run_all(jobs)
+    one_step(jobs)
     hess_ms, hess_n = ctx.profile_get("glisa_hess")
     fam_ms = {f: ctx.profile_get(f) for f in _lib.KERNEL_FAMILIES}
     ctx.profile(False)
-    prof_steps = 1
+    prof = snapshot(jobs)
+    if batched:  # work of the profiled step: the differences
+        d_iter = [p[1] - a[1] for p, a in zip(prof, after)]
+        d_inner = [p[2] - a[2] for p, a in zip(prof, after)]
+    else:
+        d_iter = [p[1] for p in prof]
+        d_inner = [p[2] for p in prof]
     ms_max = replicas.reduce_max(ms)
-    value = evals_per_job * args.steps * world / (ms_max / 1000.0)
+    value = evals_timed * world / (ms_max / 1000.0)
+    evals_per_step = evals_timed / args.steps
 
-    # end to end through the C ABI: host inputs (pinned), job create (H2D),
-    # run, charges back (D2H), destroy
+    # end to end through the C ABI: host inputs (pinned), job creation (H2D),
+    # the same work as one step (a batch: creation, warm-up and timed
+    # iterations), charges and parameters back (D2H), destroy
     pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()  # noqa: E731
     pinned = [(pin(m.grid.points), pin(m.grid.weights), pin(m.density)) for m in mols]
-    e2e_steps = 1 if len(mols) > 1 else max(1, min(args.steps, 3))
-    if len(mols) > 1:
+    e2e_steps = 1 if batched else max(1, min(args.steps, 3))
+    if batched:
         for j in jobs:  # the resident copies make room for the end-to-end jobs
             j.close()
     barrier()
@@ -385,17 +417,22 @@ def run_ours(args):
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         e2e_jobs = [make_job(ctx, w, args.precision, pinned=pp, mol=m) for pp, m in zip(pinned, mols)]
-        while ctx.step(e2e_jobs) > 0:
-            pass
+        if batched:
+            for _ in range(args.warmup + args.steps):
+                ctx.step(e2e_jobs)
+        else:
+            while ctx.step(e2e_jobs) > 0:
+                pass
+        e2e_evals = sum(j2.info().point_atom_evals for j2 in e2e_jobs)
         q = [j2.results(promoldens=False, histories=False) for j2 in e2e_jobs]
         for j2 in e2e_jobs:
             j2.close()
     torch.cuda.synchronize()
     e2e_s = replicas.reduce_max((time.perf_counter() - t0) / e2e_steps)
-    e2e_value = evals_per_job * world / e2e_s
+    e2e_value = e2e_evals * world / e2e_s
     h2d = int(sum(m.npoint * 5 * 8 + m.natom * 4 * 8 for m in mols))
     d2h = int(sum(r["charges"].nbytes + r["propars"].nbytes for r in q))
-    if len(mols) > 1:
+    if batched:
         jobs = [make_job(ctx, w, args.precision, mol=mols[0])]
         job = jobs[0]
 
@@ -408,38 +445,38 @@ def run_ours(args):
         pass
     hbm_peak = peaks.get("hbm_gbs", 6800.0)
     if w["scheme"] != "glisa":
-        # Dominant kernel family and its algorithmic bytes per launch: every
-        # per-point array once per launch (all atoms of a point share it)
-        # plus every per-(atom, point) array once. Per point: coordinates
-        # 24 B (FP64, or float hi/lo pairs), w and rho one value each; per
-        # pair: rho_a (and the pro-atom) one value. Value size: mixed 4 B
-        # (FP32), ff and fp64 8 B (float pair or double).
+        # Dominant kernel family and its algorithmic bytes per launch, from the
+        # work of the profiled step: every per-point array once per pass (all
+        # atoms of a point share it) plus every per-(atom, point) array once.
+        # Per point: coordinates 24 B (FP64, or float hi/lo pairs), w and rho
+        # one value each; per pair: rho_a (and the pro-atom) one value. Value
+        # size: mixed 4 B (FP32), ff and fp64 8 B (float pair or double).
         val = 4.0 if args.precision == "mixed" else 8.0
         pt = 24.0
-        n_pts = float(sum(m.npoint for m in mols))
-        sum_an = float(sum(m.natom * m.npoint for m in mols))
-        inner_evals = float(sum(i.inner_iterations * m.npoint for i, m in zip(infos, mols)))
+        an_pass = sum(m.natom * m.npoint * d for m, d in zip(mols, d_iter))  # per outer pass
+        pt_pass = sum(m.npoint * d for m, d in zip(mols, d_iter))
+        inner_evals = float(sum(m.npoint * d for m, d in zip(mols, d_inner)))
         if w["scheme"] == "gisa":
-            inner_evals = sum_an
-        per_step = {  # (point-atom evals per step, algorithmic bytes per step)
+            inner_evals = an_pass
+        per_step = {  # (point-atom evals, algorithmic bytes) of the profiled step
             # promolecule + at_weights: points (xyz, w, rho, promol), pro-atom
             # written, read back and rho_a written
-            "promol": (sum_an, n_pts * (pt + 3 * val) + sum_an * 3 * val),
+            "promol": (an_pass, pt_pass * (pt + 3 * val) + an_pass * 3 * val),
             # inner iterations: points (xyz, w) per launch, rho_a per pair
             "inner": (inner_evals, None),
             # outer change: points (xyz, w)
-            "change": (sum_an, n_pts * (pt + val)),
+            "change": (an_pass, pt_pass * (pt + val)),
         }
         fam = max(per_step, key=lambda f: fam_ms[f][0])
         f_ms, f_n = fam_ms[fam]
         if f_n:
             evals, step_bytes = per_step[fam]
             per_launch_s = f_ms / f_n / 1000.0
-            launches_per_step = f_n / prof_steps
-            if step_bytes is None:  # inner: per launch, points once plus rho_a per evaluation
-                alg_bytes = n_pts * (pt + val) + evals / launches_per_step * val
+            if step_bytes is None:  # inner: points once per launch plus rho_a per evaluation
+                n_pts = float(sum(m.npoint for m in mols))
+                alg_bytes = n_pts * (pt + val) + evals / f_n * val
             else:
-                alg_bytes = step_bytes / launches_per_step
+                alg_bytes = step_bytes / f_n
             achieved = alg_bytes / per_launch_s / 1e9
             roofline = {"kernel": fam, "bound": "hbm", "achieved": achieved, "peak": hbm_peak,
                         "unit": "GB/s", "frac": achieved / hbm_peak,
@@ -447,7 +484,7 @@ def run_ours(args):
                         "peak_source": "measured" if peaks else "fallback",
                         "ms_per_launch": per_launch_s * 1000.0,
                         "algorithmic_bytes_per_launch": alg_bytes,
-                        "point_atom_evals_per_launch": evals / launches_per_step}
+                        "point_atom_evals_per_launch": evals / f_n}
     if w["scheme"] == "glisa" and hess_n:
         nshell = config_of(w, args, args.precision)["nshell"]
         per_launch_s = hess_ms / hess_n / 1000.0
@@ -482,7 +519,7 @@ def run_ours(args):
         "scaling": "weak", "vs_baseline": None,
         "dtype": "f64" if args.precision == "fp64" else "f32+f64", "data": "synthetic",
         "config": config_of(w, args, args.precision), "niter_per_job": int(niter),
-        "point_atom_evals_per_job": evals_per_job, "kernel_ms_one_profiled_step": fams,
+        "point_atom_evals_per_step": evals_per_step, "kernel_ms_one_profiled_step": fams,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "seconds_per_step": e2e_s},
         "roofline": roofline, "clocks": clocks.summary(),

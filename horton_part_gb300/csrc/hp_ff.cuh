@@ -58,7 +58,8 @@ __device__ __forceinline__ f2 add(f2 a, float b) {
   return fast_two_sum(s.hi, s.lo);
 }
 
-// a + b for operands of the same sign (no cancellation): cheaper, same accuracy.
+// a + b when no cancellation occurs (|a + b| not much below |a| + |b|, e.g.
+// operands of the same sign): cheaper, same accuracy.
 __device__ __forceinline__ f2 add_pos(f2 a, f2 b) {
   f2 s = two_sum(a.hi, b.hi);
   s.lo += a.lo + b.lo;
@@ -126,9 +127,11 @@ __device__ __forceinline__ f2 exp_ff(f2 x, const float2* tab) {
   const f2 half = {0.5f * sq.hi, 0.5f * sq.lo};
   const float c =
       r.hi * sq.hi * fmaf(r.hi, fmaf(r.hi, 1.0f / 120.0f, 1.0f / 24.0f), 1.0f / 6.0f);
-  f2 e = add(r, half);
+  // |r^2/2| << |r| and |c| << |r|: no cancellation, so the cheaper sums
+  // (two_sum of the high parts) keep the full accuracy
+  f2 e = add_pos(r, half);
   e = add(e, c);
-  e = add(f2{1.0f, 0.0f}, e);
+  e = add(e, 1.0f);
   const int m = n >> 6;  // floor(n / 64)
   const int i = n - (m << 6);
   const float2 t = tab[i];

@@ -158,7 +158,8 @@ struct JobDev {
   float* hess_s;          // gLISA tensor-core Hessian: sqrt(w rho / rho0^2) as FP32, npoint
   double* hvec;           // gLISA refinement: w rho / rho0^2 * (G^T delta)(p), npoint
   double* rho0;           // gLISA: promolecule of the current populations, npoint
-  int* clip;              // gLISA projected Newton: shells clipped at the full step [nshell], count at [nshell]
+  int* clip;              // gLISA projected Newton: shells clipped at the full step [nshell],
+                          // count at [nshell], their trial counts t_m at [nshell + 1 ...]
   double* hist_propars;   // [maxiter][nparam]
   double* hist_charges;   // [maxiter][natom]
   double* hist_ent;       // [maxiter]

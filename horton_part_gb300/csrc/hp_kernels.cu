@@ -1241,8 +1241,12 @@ __device__ void chol_factor(double* L, int n, int* bad, double* colbuf, double* 
 
 // y <- (L L^T)^-1 y by one warp with the factor of chol_factor: forward then
 // backward substitution (both over contiguous rows), each row's dot product
-// split over the lanes and summed by a fixed xor tree.
-__device__ void chol_solve_warp(const double* L, const double* dinv, int n, double* y) {
+// split over the lanes and summed by a fixed xor tree. y is worked on in
+// shared memory (each row reads the values the previous rows just wrote)
+// when n <= kSolveSmem, in place otherwise.
+constexpr int kSolveSmem = 2048;
+
+__device__ void chol_solve_rows(const double* L, const double* dinv, int n, double* y) {
   const int lane = threadIdx.x & 31;
   for (int i = 0; i < n; ++i) {
     const double* row = L + (size_t)i * n;
@@ -1268,11 +1272,33 @@ __device__ void chol_solve_warp(const double* L, const double* dinv, int n, doub
   }
 }
 
+// Called by one full warp.
+__device__ void chol_solve_warp(const double* L, const double* dinv, int n, double* y) {
+  __shared__ double ys[kSolveSmem];
+  const int lane = threadIdx.x & 31;
+  if (n > kSolveSmem) {
+    chol_solve_rows(L, dinv, n, y);
+    return;
+  }
+  for (int i = lane; i < n; i += 32) ys[i] = y[i];
+  __syncwarp();
+  chol_solve_rows(L, dinv, n, ys);
+  for (int i = lane; i < n; i += 32) y[i] = ys[i];
+  __syncwarp();
+}
+
 // Newton step on a free set F (one block per job): delta_F = H_FF^-1 (-1 - df)_F,
 // delta = 0 outside F. Newton / m-newton (glisa.py:734-748): F = all shells;
 // projected Newton: F = {c > 0 or dF/dc < 0}. The factor of H_FF stays in
 // chol and |F| in freeidx[nshell] for the refinement steps.
+// Shared memory of the Newton step: the factor (dynamic, when |F|^2 doubles
+// fit in kNewtonSmemL) and the two column buffers (when |F| <= kNewtonColMax).
+constexpr int kNewtonSmemL = 200 * 1024;
+constexpr int kNewtonColMax = 256;
+
 __global__ void __launch_bounds__(kThreads) k_glisa_newton_step(Batch bt, int projected) {
+  extern __shared__ double l_smem[];
+  __shared__ double col_smem[2 * kNewtonColMax];
   __shared__ int bad, nf_s;
   int local;
   const JobDev& J = decode_local(bt, local);
@@ -1289,16 +1315,19 @@ __global__ void __launch_bounds__(kThreads) k_glisa_newton_step(Batch bt, int pr
   }
   __syncthreads();
   const int nf = nf_s;
-  double* L = J.chol;
+  const bool l_in_smem = (size_t)nf * nf * sizeof(double) <= (size_t)kNewtonSmemL;
+  double* L = l_in_smem ? l_smem : J.chol;
   for (int e = threadIdx.x; e < nf * nf; e += kThreads) {
     const int i = e / nf, j = e % nf;
     L[e] = J.hess[(size_t)J.freeidx[i] * M + J.freeidx[j]];
   }
   for (int m = threadIdx.x; m < M; m += kThreads) J.delta[m] = 0.0;
   __syncthreads();
-  // ctrial (kTrials x nshell) is free until the trial set: column buffers at
-  // [0, 2 nshell), 1 / diag(L) at [2 nshell, 3 nshell) (kept for the refinement)
-  chol_factor(L, nf, &bad, J.ctrial, J.ctrial + 2 * M);
+  // column buffers in shared memory when they fit, else in ctrial (kTrials x
+  // nshell, free until the trial set); 1 / diag(L) at ctrial[2 nshell, 3 nshell)
+  // (kept for the refinement)
+  double* colbuf = nf <= kNewtonColMax ? col_smem : J.ctrial;
+  chol_factor(L, nf, &bad, colbuf, J.ctrial + 2 * M);
   if (threadIdx.x < 32) {
     double* y = J.keep;  // scratch (the m-newton mask is formed after the step)
     for (int i = threadIdx.x; i < nf; i += 32) y[i] = -(1.0 + J.grad[J.freeidx[i]]);
@@ -1306,6 +1335,10 @@ __global__ void __launch_bounds__(kThreads) k_glisa_newton_step(Batch bt, int pr
     chol_solve_warp(L, J.ctrial + 2 * M, nf, y);
     for (int i = threadIdx.x; i < nf; i += 32) J.delta[J.freeidx[i]] = y[i];
     if (threadIdx.x == 0 && bad) atomicOr(&J.mail->i[MI_ERR], E_SINGULAR);
+  }
+  if (l_in_smem) {  // the refinement steps read the factor from chol
+    __syncthreads();
+    for (int e = threadIdx.x; e < nf * nf; e += kThreads) J.chol[e] = L[e];
   }
 }
 
@@ -1361,9 +1394,23 @@ __global__ void __launch_bounds__(kThreads) k_glisa_trial_set(Batch bt) {
     J.ctrial[e] = fmax(J.propars[m] + a * J.delta[m], 0.0);
   }
   if (threadIdx.x == 0) {
+    // clipped shells with the number of trials t_m at which they are clipped
+    // (c + 2^-t delta < 0 for t < t_m), sorted by t_m, largest first
+    int* tm = J.clip + M + 1;
     int n = 0;
-    for (int m = 0; m < M; ++m)
-      if (J.propars[m] + J.delta[m] < 0.0) J.clip[n++] = m;
+    for (int m = 0; m < M; ++m) {
+      if (!(J.propars[m] + J.delta[m] < 0.0)) continue;
+      int t = 1;
+      while (t < kTrials && J.propars[m] + ldexp(1.0, -t) * J.delta[m] < 0.0) ++t;
+      int k = n++;
+      while (k > 0 && tm[k - 1] < t) {
+        J.clip[k] = J.clip[k - 1];
+        tm[k] = tm[k - 1];
+        --k;
+      }
+      J.clip[k] = m;
+      tm[k] = t;
+    }
     J.clip[M] = n;
   }
 }
@@ -1553,17 +1600,22 @@ __global__ void __launch_bounds__(kThreads) k_glisa_trials(Batch bt) {
     double u = 0.0;
 #pragma unroll 8
     for (int m = 0; m < J.nshell; ++m) u += J.gmat[(size_t)m * J.npoint + p] * J.delta[m];
+    // corr_t = -sum_{m clipped at t} (c_m + 2^-t delta_m) g_m: the clipped
+    // sets shrink as t grows, so walk the list (sorted by t_m, largest first)
+    // once, keeping the running sums of c g and delta g
     double corr[kTrials];
+    {
+      double sc = 0.0, sd = 0.0;
+      int k = 0;
 #pragma unroll
-    for (int t = 0; t < kTrials; ++t) corr[t] = 0.0;
-    for (int k = 0; k < nclip; ++k) {
-      const int m = J.clip[k];
-      const double g = J.gmat[(size_t)m * J.npoint + p];
-      const double c = J.propars[m], d = J.delta[m];
-#pragma unroll
-      for (int t = 0; t < kTrials; ++t) {
-        const double e = -(c + ldexp(1.0, -t) * d);
-        if (e > 0.0) corr[t] += e * g;
+      for (int t = kTrials - 1; t >= 0; --t) {
+        for (; k < nclip && J.clip[J.nshell + 1 + k] > t; ++k) {
+          const int m = J.clip[k];
+          const double g = J.gmat[(size_t)m * J.npoint + p];
+          sc += J.propars[m] * g;
+          sd += J.delta[m] * g;
+        }
+        corr[t] = -(sc + ldexp(1.0, -t) * sd);
       }
     }
     const double rho = J.rho[p], w = J.w[p], r0 = J.rho0[p];
@@ -1737,7 +1789,18 @@ void launch_glisa_reduce(const HostBatch& hb, cudaStream_t st) {
 }
 
 void launch_glisa_solve(const HostBatch& hb, cudaStream_t st, int projected) {
-  HP_LAUNCH(k_glisa_newton_step, K_JOB, kThreads, projected);
+  static int configured_device = -1;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (configured_device != dev) {
+    cudaFuncSetAttribute(k_glisa_newton_step, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         kNewtonSmemL);
+    configured_device = dev;
+  }
+  if (hb.blocks[K_JOB] > 0) {
+    k_glisa_newton_step<<<hb.blocks[K_JOB], kThreads, kNewtonSmemL, st>>>(hb.b[K_JOB], projected);
+    ++g_launch_count;
+  }
 }
 
 void launch_glisa_refine(const HostBatch& hb, cudaStream_t st) {

@@ -770,7 +770,7 @@ int32_t hp_job_create(hp_ctx* ctx, const hp_job_desc* d, hp_job** out) {
     add(&J.ctrial, 8 * (size_t)kTrials * S);
     add(&J.tpart, 8 * (size_t)kTrials * ntile);
     add(&J.freeidx, 4 * (size_t)(S + 1));
-    add(&J.clip, 4 * (size_t)(S + 1));
+    add(&J.clip, 4 * (size_t)(2 * S + 1));
     add(&J.rho0, 8 * (size_t)N);
     if (tc) {
       add(&J.gmat32, 4 * (size_t)S * N);

@@ -5,17 +5,20 @@
 //
 // Output tiles cover the lower triangle of H: row block i0 (128 rows, the
 // UMMA M) against column block j0 (N columns, a multiple of 16 up to 256,
-// ending at the tile's last row). One CTA (256 threads, one per SM: two
+// ending at the tile's last row). One CTA (512 threads, one per SM: two
 // 97 KB stages of shared memory) computes one tile over one range of grid
 // points. Per block
 // of 32 points the threads form X from G (FP32 copy) and s, split it into two
-// TF32 parts X = X_hi + X_lo (cvt.rna.tf32) and write A (128 x 32) and B
-// (N x 32) K-major into one of two shared-memory stages in the
+// TF32 parts X = X_hi + X_lo (X_hi: X with its low 13 mantissa bits cleared;
+// X_lo = X - X_hi, exact, whose low bits the MMA ignores) and write A
+// (128 x 32) and B (N x 32; on a diagonal tile B is A itself) K-major into
+// one of two shared-memory stages in the
 // 128-byte-swizzled layout; one thread issues tcgen05.mma.kind::tf32
 // (M = 128, K = 8) for X_hi X_hi^T, X_hi X_lo^T and X_lo X_hi^T into one FP32
-// accumulator in tensor memory and commits to the stage's mbarrier. While
-// the tensor core works on block k, the threads load block k+1's operands
-// into registers and stage them into the other buffer. The accumulator is
+// accumulator in tensor memory and commits to the stage's mbarrier. Each
+// thread keeps the operands of the next two blocks in registers (loads two
+// blocks ahead), so HBM latency overlaps the staging of block k+1 and the
+// MMAs of block k. The accumulator is
 // read back with tcgen05.ld and written as the CTA's partial; partials over point ranges are summed in FP64
 // in a fixed order (k_glisa_reduce). Relative accuracy of H is about 1e-7
 // (the dropped X_lo X_lo^T term and FP32 accumulation); the Newton step is
@@ -36,7 +39,7 @@ namespace {
 constexpr int kTcM = 128;       // UMMA M
 constexpr int kTcNMax = 256;    // largest UMMA N
 constexpr int kTcK = 32;        // points per block: 32 x 4 B = one 128-byte swizzle row
-constexpr int kTcThreads = 256; // two warpgroups (each covers tensor-memory lanes 0..127)
+constexpr int kTcThreads = 512; // four warpgroups (each covers tensor-memory lanes 0..127)
 constexpr int kTcWarps = kTcThreads / 32;
 constexpr int kRowsA = kTcM / kTcWarps;     // A rows staged per warp
 constexpr int kRowsB = kTcNMax / kTcWarps;  // B rows staged per warp (at most)
@@ -57,13 +60,6 @@ __device__ __forceinline__ uint32_t smem_u32(const void* p) {
   return (uint32_t)__cvta_generic_to_shared(p);
 }
 
-// Word offset of element (row, k) of a K-major tile of 32-bit elements with
-// 128-byte rows in the 128B-swizzle layout: 16-byte chunk c of row r is
-// stored at chunk c ^ (r mod 8); rows are 128 bytes apart, 8-row groups 1024.
-__device__ __forceinline__ uint32_t swz_word(int row, int k) {
-  const int chunk = (k >> 2) ^ (row & 7);
-  return (uint32_t)(row * 32 + chunk * 4 + (k & 3));
-}
 
 // UMMA shared-memory descriptor: start address, leading byte offset (unused
 // for swizzled K-major; 16 B), stride byte offset 1024 B (between 8-row
@@ -85,11 +81,8 @@ __device__ __forceinline__ uint32_t idesc_tf32(int n) {
          ((uint32_t)(kTcM >> 4) << 24);
 }
 
-__device__ __forceinline__ uint32_t to_tf32(float x) {
-  uint32_t r;
-  asm volatile("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
-  return r;
-}
+// High TF32 part of a float: sign, exponent and the top 10 mantissa bits.
+constexpr uint32_t kTf32Mask = 0xFFFFE000u;
 
 __device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count));
@@ -173,6 +166,14 @@ __global__ void __launch_bounds__(kTcThreads) k_glisa_hess_tc(Batch bt) {
   const int pend = min(pbeg + chunk, N);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const uint32_t idesc = idesc_tf32(ncol);
+  // diagonal tile (B rows = the first ncol rows of A): the MMAs read A for B
+  const bool diag = (j0 == i0) && (ncol <= kTcM);
+  // 128B-swizzle layout of a K-major tile of 32-bit elements with 128-byte
+  // rows: element (row, k) sits at word row * 32 + ((k / 4) ^ (row mod 8)) * 4
+  // + k mod 4 (16-byte chunk c of row r at chunk c ^ (r mod 8); 8-row groups
+  // 1024 bytes apart). This thread's rows all have row mod 8 = warp mod 8 and
+  // its k is its lane, so the in-row word offset is one constant.
+  const uint32_t swz_col = (uint32_t)((((lane >> 2) ^ (warp & 7)) << 2) | (lane & 3));
 
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
@@ -191,9 +192,11 @@ __global__ void __launch_bounds__(kTcThreads) k_glisa_hess_tc(Batch bt) {
   asm volatile("tcgen05.fence::after_thread_sync;");
   const uint32_t tmem = *tmem_slot;
 
-  // rows of this thread: A rows warp + 8 r (r < 16), B rows warp + 8 r (row < ncol)
-  float va[kRowsA], vb[kRowsB], s = 0.0f;
-  auto load_block = [&](int kb) {
+  // rows of this thread: A rows warp + 16 r (r < 8), B rows warp + 16 r
+  // (row < ncol); operands of two blocks in flight (slots 0 and 1)
+  float va0[kRowsA], vb0[kRowsB], s0 = 0.0f;
+  float va1[kRowsA], vb1[kRowsB], s1 = 0.0f;
+  auto load_block = [&](float (&va)[kRowsA], float (&vb)[kRowsB], float& s, int kb) {
     const int p = kb + lane;
     const bool inr = p < pend;
     s = inr ? J.hess_s[p] : 0.0f;
@@ -206,13 +209,14 @@ __global__ void __launch_bounds__(kTcThreads) k_glisa_hess_tc(Batch bt) {
     for (int r = 0; r < kRowsB; ++r) {
       const int row = warp + kTcWarps * r;
       const int m = j0 + row;
-      vb[r] = (inr && row < ncol && m < M) ? J.gmat32[(size_t)m * N + p] : 0.0f;
+      vb[r] = (!diag && inr && row < ncol && m < M) ? J.gmat32[(size_t)m * N + p] : 0.0f;
     }
   };
 
   int nblocks = 0;
-  if (pbeg < pend) load_block(pbeg);
-  for (int kb = pbeg; kb < pend; kb += kTcK, ++nblocks) {
+  // one block: wait for its stage, stage it from registers, issue its MMAs,
+  // refill the registers with the block two ahead; false when a wait timed out
+  auto do_block = [&](float (&va)[kRowsA], float (&vb)[kRowsB], float& s, int kb) -> bool {
     const int st = nblocks & 1;
     uint8_t* stage = sm + st * kStageBytes;
     uint32_t* a_hi = reinterpret_cast<uint32_t*>(stage + kOffAhi);
@@ -227,29 +231,31 @@ __global__ void __launch_bounds__(kTcThreads) k_glisa_hess_tc(Batch bt) {
 #pragma unroll
     for (int r = 0; r < kRowsA; ++r) {
       const float x = va[r] * s;
-      const uint32_t hi = to_tf32(x);
-      const uint32_t off = swz_word(warp + kTcWarps * r, lane);
+      const uint32_t hi = __float_as_uint(x) & kTf32Mask;
+      const uint32_t off = (uint32_t)((warp + kTcWarps * r) * 32) + swz_col;
       a_hi[off] = hi;
-      a_lo[off] = to_tf32(x - __uint_as_float(hi));
+      a_lo[off] = __float_as_uint(x - __uint_as_float(hi));
     }
+    if (!diag) {
 #pragma unroll
-    for (int r = 0; r < kRowsB; ++r) {
-      const int row = warp + kTcWarps * r;
-      if (row < ncol) {
-        const float x = vb[r] * s;
-        const uint32_t hi = to_tf32(x);
-        const uint32_t off = swz_word(row, lane);
-        b_hi[off] = hi;
-        b_lo[off] = to_tf32(x - __uint_as_float(hi));
+      for (int r = 0; r < kRowsB; ++r) {
+        const int row = warp + kTcWarps * r;
+        if (row < ncol) {
+          const float x = vb[r] * s;
+          const uint32_t hi = __float_as_uint(x) & kTf32Mask;
+          const uint32_t off = (uint32_t)(row * 32) + swz_col;
+          b_hi[off] = hi;
+          b_lo[off] = __float_as_uint(x - __uint_as_float(hi));
+        }
       }
     }
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     __syncthreads();
-    if (timed_out) break;
+    if (timed_out) return false;
     if (threadIdx.x == 0) {
       asm volatile("tcgen05.fence::after_thread_sync;");
       const uint32_t ahi = smem_u32(a_hi), alo = smem_u32(a_lo);
-      const uint32_t bhi = smem_u32(b_hi), blo = smem_u32(b_lo);
+      const uint32_t bhi = diag ? ahi : smem_u32(b_hi), blo = diag ? alo : smem_u32(b_lo);
 #pragma unroll
       for (int k = 0; k < kTcK / 8; ++k) {  // K = 8 TF32 = 32 bytes per MMA
         const uint32_t acc = (nblocks > 0 || k > 0) ? 1u : 0u;
@@ -259,8 +265,16 @@ __global__ void __launch_bounds__(kTcThreads) k_glisa_hess_tc(Batch bt) {
       }
       umma_commit(bar0 + 8 * st);
     }
-    // the next block's operands into registers while the tensor core runs
-    if (kb + kTcK < pend) load_block(kb + kTcK);
+    ++nblocks;
+    if (kb + 2 * kTcK < pend) load_block(va, vb, s, kb + 2 * kTcK);
+    return true;
+  };
+
+  if (pbeg < pend) load_block(va0, vb0, s0, pbeg);
+  if (pbeg + kTcK < pend) load_block(va1, vb1, s1, pbeg + kTcK);
+  for (int kb = pbeg; kb < pend; kb += 2 * kTcK) {
+    if (!do_block(va0, vb0, s0, kb)) break;
+    if (kb + kTcK < pend && !do_block(va1, vb1, s1, kb + kTcK)) break;
   }
   if (nblocks > 0 && !timed_out) {
     // the last commit covers every MMA issued before it
@@ -271,14 +285,12 @@ __global__ void __launch_bounds__(kTcThreads) k_glisa_hess_tc(Batch bt) {
   __syncthreads();
 
   // epilogue: warp w reads tensor-memory lanes 32 (w % 4) .. + 31 (rows of the
-  // tile); warps 0-3 take the first half of the columns, warps 4-7 the rest
+  // tile); the four warps of a lane quarter take every fourth 8-column chunk
   double* out = J.hpart + (size_t)split * M * M;
   const int quad = warp & 3;
   const int i = i0 + quad * 32 + lane;
   const bool ok = nblocks > 0 && !timed_out;
-  const int half = ncol / 2;  // a multiple of 8
-  const int c0 = warp < 4 ? 0 : half, c1 = warp < 4 ? half : ncol;
-  for (int c = c0; c < c1; c += 8) {
+  for (int c = 8 * (warp >> 2); c < ncol; c += 32) {
     uint32_t v[8];
     if (ok) {
       const uint32_t taddr = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)c;

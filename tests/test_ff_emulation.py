@@ -41,6 +41,11 @@ def add(a, b):
     return fast_two_sum(*s)
 
 
+def add_pos(a, b):
+    s = two_sum(a[0], b[0])
+    return fast_two_sum(s[0], f32(s[1] + f32(a[1] + b[1])))
+
+
 def add_f(a, b):
     s = two_sum(a[0], b)
     return fast_two_sum(s[0], f32(s[1] + a[1]))
@@ -77,9 +82,9 @@ def exp_ff(x):
     sq = fast_two_sum(sq[0], fma(f32(2.0) * r[0], r[1], sq[1]))
     half = (f32(0.5) * sq[0], f32(0.5) * sq[1])
     c = f32(f32(r[0] * sq[0]) * fma(r[0], fma(r[0], f32(1.0 / 120.0), f32(1.0 / 24.0)), f32(1.0 / 6.0)))
-    e = add(r, half)
+    e = add_pos(r, half)
     e = add_f(e, c)
-    e = add((f32(1.0), f32(0.0)), e)
+    e = add_f(e, f32(1.0))
     m = n >> 6
     i = n - (m << 6)
     v = mul(TABLE[i], e)

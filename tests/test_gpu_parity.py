@@ -166,3 +166,28 @@ def test_custom_basis_helper(gpu_context):
                   [helper.get_initial(z) for z in mol.numbers], threshold=1e-8, solver="newton")
     np.testing.assert_allclose(part["charges"], ref["charges"], atol=Q_TOL)
     assert part["niter"] == ref["niter"]
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-9), ("ff", 1e-9), ("mixed", 1e-6)])
+def test_mbis_water_hf_sto3g_reference_data(precision, tol, gpu_context):
+    """MBIS on the reference's cached water HF/STO-3G density (the input of
+    horton-part's tests/test_wpart.py:95-101) against the unmodified
+    reference run on the same molecular grid, and within the reference
+    test's 2e-3 of its published charges."""
+    from horton_part_gb300.molgrid import MolecularGrid
+
+    path = os.path.join(os.path.dirname(__file__), "golden", "water_sto3g_hf_molgrid.npz")
+    with np.load(path) as f:
+        d = {k: f[k] for k in f.files}
+    grid = MolecularGrid(d["points"], d["weights"])
+    part = wpart_schemes("mbis")(d["coordinates"], d["numbers"], d["pseudo_numbers"], grid,
+                                 d["density"], grid_type=3, threshold=1e-8, precision=precision)
+    part.do_partitioning()
+    dq = float(np.abs(part["charges"] - d["ref_charges"]).max())
+    print(f"water HF/STO-3G {precision}: niter {part['niter']} (reference {int(d['ref_niter'])}), "
+          f"max|dq| {dq:.2e}")
+    assert dq < tol
+    if precision != "mixed":
+        assert part["niter"] == int(d["ref_niter"])
+    published = np.array([-0.61891067, 0.3095756, 0.30932584])
+    assert np.abs(part["charges"] - published).max() < 2e-3

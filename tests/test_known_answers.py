@@ -122,3 +122,26 @@ def test_qp_simplex_kkt():
         lam = -np.mean(g[x > 1e-12])
         assert np.all(g[x > 1e-12] + lam == pytest.approx(0, abs=1e-9))
         assert np.all(g[x <= 1e-12] + lam >= -1e-9)
+
+
+def _water_sto3g():
+    import os
+
+    path = os.path.join(os.path.dirname(__file__), "golden", "water_sto3g_hf_molgrid.npz")
+    with np.load(path) as f:
+        return {k: f[k] for k in f.files}
+
+
+def test_mbis_water_hf_sto3g_reference_data():
+    """The reference's own cached water HF/STO-3G density and grid points
+    (tests/test_wpart.py:95-101 of horton-part). On the molecular grid the
+    oracle reproduces the unmodified reference run (same charges, same
+    iteration count) and stays within the reference test's 2e-3 of its
+    published MBIS charges (computed there with grid_type 1)."""
+    d = _water_sto3g()
+    res = O.mbis(d["coordinates"], d["numbers"], d["pseudo_numbers"], d["points"], d["weights"],
+                 d["density"], threshold=1e-8, maxiter=500, inner_threshold=1e-8)
+    assert res["niter"] == int(d["ref_niter"])
+    np.testing.assert_allclose(res["charges"], d["ref_charges"], atol=1e-10)
+    published = np.array([-0.61891067, 0.3095756, 0.30932584])
+    assert np.abs(res["charges"] - published).max() < 2e-3

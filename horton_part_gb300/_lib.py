@@ -46,6 +46,9 @@ class JobDesc(ctypes.Structure):
         ("negative_cutoff", ctypes.c_double), ("population_cutoff", ctypes.c_double),
         ("tau", ctypes.c_double), ("maxiter", ctypes.c_int32), ("inner_maxiter", ctypes.c_int32),
         ("linspace_size", ctypes.c_int32), ("polish", ctypes.c_int32),
+        ("nrad", ctypes.c_int32), ("radial_offsets", _ip),
+        ("shell_point_offsets", ctypes.POINTER(ctypes.c_int64)),
+        ("point_sphere_weights", _dp), ("radial_points", _dp), ("radial_weights", _dp),
     ]
 
 
@@ -222,7 +225,10 @@ class Job:
                  solver="default", precision="fp64", grid_type=3, threshold=1e-6,
                  inner_threshold=1e-8, density_cutoff=1e-15, negative_cutoff=-1e-12,
                  population_cutoff=1e-4, maxiter=500, inner_maxiter=0, linspace_size=0, tau=1.0,
-                 polish=False):
+                 polish=False, local=None):
+        """``local`` (grid_type 1): dict with ``radial_offsets`` (natom + 1),
+        ``shell_point_offsets`` (nrad + 1), ``point_sphere_weights`` (npoint),
+        ``radial_points`` and ``radial_weights`` (nrad), as in hpgpu.h."""
         self.ctx = ctx
         keep = []
 
@@ -259,6 +265,16 @@ class Job:
         d.population_cutoff, d.tau = population_cutoff, tau
         d.maxiter, d.inner_maxiter, d.linspace_size = int(maxiter), int(inner_maxiter), int(linspace_size)
         d.polish = 1 if polish else 0
+        if local is not None:
+            roff = np.ascontiguousarray(local["radial_offsets"], dtype=np.int32)
+            spo = np.ascontiguousarray(local["shell_point_offsets"], dtype=np.int64)
+            keep.extend([roff, spo])
+            d.nrad = int(roff[-1])
+            d.radial_offsets = _ptr(roff, ctypes.c_int32)
+            d.shell_point_offsets = _ptr(spo, ctypes.c_int64)
+            d.point_sphere_weights = _ptr(f64(local["point_sphere_weights"], (npoint,)))
+            d.radial_points = _ptr(f64(local["radial_points"], (d.nrad,)))
+            d.radial_weights = _ptr(f64(local["radial_weights"], (d.nrad,)))
         handle = ctypes.c_void_p()
         _check(lib().hp_job_create(ctx.handle, ctypes.byref(d), ctypes.byref(handle)))
         self._h = handle

@@ -155,11 +155,24 @@ struct JobDev {
   double* tpart;          // gLISA projected Newton: trial objective partials [kTrials][ntile]
   int* freeidx;           // gLISA Newton: free-variable list [nshell], count at [nshell]
   float* gmat32;          // gLISA tensor-core Hessian: FP32 copy of gmat [nshell][npoint]
+                          // (with gff: the high part of G = gmat32 + gmat_lo)
+  float* gmat_lo;         // gLISA, gff: low part of G [nshell][npoint] (gmat is not stored)
+  float2* d1f;            // gLISA, gff: w rho / rho0 as float pairs, npoint
+  float2* hvf;            // gLISA, gff: the refinement's hvec as float pairs, npoint
   float* hess_s;          // gLISA tensor-core Hessian: sqrt(w rho / rho0^2) as FP32, npoint
   double* hvec;           // gLISA refinement: w rho / rho0^2 * (G^T delta)(p), npoint
   double* rho0;           // gLISA: promolecule of the current populations, npoint
   int* clip;              // gLISA projected Newton: shells clipped at the full step [nshell],
                           // count at [nshell], their trial counts t_m at [nshell + 1 ...]
+  // grid_type 1 (atom grids, MBIS): atom a owns radial shells [rad_off[a],
+  // rad_off[a+1]); shell s owns the grid points [shell_pt[s], shell_pt[s+1])
+  // with angular weights wsph (Lebedev weight / 4 pi)
+  const int* rad_off;     // natom + 1
+  const long long* shell_pt;  // nrad + 1
+  const double* wsph;     // npoint
+  const double* rad_r;    // nrad: radial nodes
+  const double* rad_w;    // nrad: radial weights
+  double* radrho;         // nrad: spherical average of w_a rho
   double* hist_propars;   // [maxiter][nparam]
   double* hist_charges;   // [maxiter][natom]
   double* hist_ent;       // [maxiter]
@@ -169,8 +182,10 @@ struct JobDev {
   int natom, npoint, ntile, nparam, nshell, qa;
   int scheme, solver, mixed, maxiter;
   int inner_maxiter, linspace_size, nsplit, ppt;  // ppt: points per thread per tile
-  int tile_points, htiles, tc, pad2;             // htiles: 64-wide Hessian tiles per side;
-                                                 // tc: gLISA Hessian on the tensor cores
+  int local, nrad;                               // local: grid_type 1 (atom grids)
+  int tile_points, htiles, tc, gff;              // htiles: 64-wide Hessian tiles per side;
+                                                 // tc: gLISA Hessian on the tensor cores;
+                                                 // gff: gLISA G passes in float-float
   double threshold, inner_threshold, density_cutoff, negative_cutoff, population_cutoff, tau;
 };
 
@@ -380,8 +395,17 @@ void launch_glisa_keep(const HostBatch& hb, cudaStream_t st);
 void launch_glisa_ls(const HostBatch& hb, cudaStream_t st, int first, int count);
 void launch_glisa_change(const HostBatch& hb, cudaStream_t st);
 void launch_glisa_check(const HostBatch& hb, cudaStream_t st);
-void launch_glisa_pnewton(const HostBatch& hb, cudaStream_t st);  // trials + Armijo pick
-void launch_glisa_refine(const HostBatch& hb, cudaStream_t st);
+void launch_glisa_pnewton(const HostBatch& hb, cudaStream_t st, int gff);  // trials + Armijo pick
+void launch_glisa_refine(const HostBatch& hb, cudaStream_t st, int gff);
+
+// gLISA passes over G in float-float (hp_glisa_ff.cu); shells per job at most
+// kGffMaxShells (their coefficients are staged in shared memory)
+constexpr int kGffMaxShells = 2048;
+void launch_glisa_pro_ff(const HostBatch& hb, cudaStream_t st);
+void launch_glisa_grad_ff(const HostBatch& hb, cudaStream_t st);
+void launch_glisa_hv_ff(const HostBatch& hb, cudaStream_t st);  // hvec and G hvec
+void launch_glisa_trials_ff(const HostBatch& hb, cudaStream_t st);
+void launch_glisa_change_ff(const HostBatch& hb, cudaStream_t st);
 
 // tensor-core Hessian (hp_tcgen05.cu)
 int tc_hess_blocks(const JobDev& J);
@@ -394,6 +418,10 @@ void launch_mbis_inner_mx(const HostBatch& hb, cudaStream_t st);
 void launch_basis_qvec_mx(const HostBatch& hb, cudaStream_t st);
 void launch_lisa_sc_inner_mx(const HostBatch& hb, cudaStream_t st);
 void launch_final_atweights_mx(const HostBatch& hb, cudaStream_t st, int model, int use_old);
+
+// MBIS on atom grids (hp_local.cu)
+void launch_mbis_local(const HostBatch& hb, cudaStream_t st);  // spherical averages + radial inner solve
+void launch_change_radial(const HostBatch& hb, cudaStream_t st);
 
 // float-float MBIS (hp_ff.cu)
 void launch_promol_ff(const HostBatch& hb, cudaStream_t st);

@@ -76,7 +76,10 @@ __device__ __forceinline__ T shell_value(const JobDev& J, int s, T r) {
 // when the job keeps one (basis schemes, FP64), else evaluated at distance r.
 template <typename T>
 __device__ __forceinline__ T basis_val(const JobDev& J, int s, int p, T r) {
-  return J.gmat ? (T)J.gmat[(size_t)s * J.npoint + p] : shell_value<T>(J, s, r);
+  if (J.gmat) return (T)J.gmat[(size_t)s * J.npoint + p];
+  if (J.gmat_lo)  // float-float planes of G (gLISA with the tensor-core Hessian)
+    return (T)((double)J.gmat32[(size_t)s * J.npoint + p] + (double)J.gmat_lo[(size_t)s * J.npoint + p]);
+  return shell_value<T>(J, s, r);
 }
 
 // Distance to atom a, skipped when a stored basis matrix makes it unused.
@@ -1019,7 +1022,7 @@ template <typename T>
 __global__ void __launch_bounds__(kThreads) k_glisa_basis(Batch bt) {
   int tile;
   const JobDev& J = decode_local(bt, tile);
-  if (!J.gmat) return;  // jobs that recompute their shells keep no basis matrix
+  if (!J.gmat && !J.gmat_lo) return;  // jobs that recompute their shells keep no basis matrix
   for (int i = 0; i < J.ppt; ++i) {
     const int p = point_of(J, tile, i);
     if (p >= J.npoint) continue;
@@ -1027,8 +1030,13 @@ __global__ void __launch_bounds__(kThreads) k_glisa_basis(Batch bt) {
       const T r = Dist<T>::r(J, p, a);
       for (int s = J.shell_off[a]; s < J.shell_off[a + 1]; ++s) {
         const double g = (double)shell_value<T>(J, s, r);
-        J.gmat[(size_t)s * J.npoint + p] = g;
-        if (J.gmat32) J.gmat32[(size_t)s * J.npoint + p] = (float)g;
+        const size_t e = (size_t)s * J.npoint + p;
+        if (J.gmat) J.gmat[e] = g;
+        if (J.gmat32) {
+          const float hi = (float)g;
+          J.gmat32[e] = hi;
+          if (J.gmat_lo) J.gmat_lo[e] = (float)(g - (double)hi);
+        }
       }
     }
   }
@@ -1239,58 +1247,41 @@ __device__ void chol_factor(double* L, int n, int* bad, double* colbuf, double* 
   }
 }
 
-// y <- (L L^T)^-1 y by one warp with the factor of chol_factor: forward then
-// backward substitution (both over contiguous rows), each row's dot product
-// split over the lanes and summed by a fixed xor tree. y is worked on in
-// shared memory (each row reads the values the previous rows just wrote)
-// when n <= kSolveSmem, in place otherwise.
-constexpr int kSolveSmem = 2048;
+constexpr int kSolveSmem = 1024;  // vector length solved in shared memory
 
-__device__ void chol_solve_rows(const double* L, const double* dinv, int n, double* y) {
-  const int lane = threadIdx.x & 31;
-  for (int i = 0; i < n; ++i) {
-    const double* row = L + (size_t)i * n;
-    double s = 0.0;
-    for (int j = lane; j < i; j += 32) s += row[j] * y[j];
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-    const double v = (y[i] - s) * dinv[i];
-    __syncwarp();
-    if (lane == 0) y[i] = v;
-    __syncwarp();
+// y <- (L L^T)^-1 y by all threads of the block, column by column (one
+// barrier per column): forward, z_j = y_j / L_jj and y_i -= L_ij z_j for
+// i > j; backward with the rows of L, x_j = z_j / L_jj and z_i -= L_ji x_j
+// for i < j. Works in shared memory when n <= kSolveSmem (else in place in y).
+__device__ void chol_solve_block(const double* L, const double* dinv, int n, double* y) {
+  __shared__ double yb[kSolveSmem], zb[kSolveSmem];
+  const bool sm = n <= kSolveSmem;
+  double* a = sm ? yb : y;
+  double* z = sm ? zb : y;  // in place: z_j overwrites y_j once y_j is no longer read
+  if (sm)
+    for (int i = threadIdx.x; i < n; i += blockDim.x) yb[i] = y[i];
+  __syncthreads();
+  for (int j = 0; j < n; ++j) {
+    const double zj = a[j] * dinv[j];
+    const double* col = L + j;  // L[i][j] = col[i n]
+    for (int i = j + 1 + threadIdx.x; i < n; i += blockDim.x) a[i] -= col[(size_t)i * n] * zj;
+    __syncthreads();
+    if (threadIdx.x == 0) z[j] = zj;
   }
-  for (int i = n - 1; i >= 0; --i) {
-    const double* row = L + (size_t)i * n;  // upper part: L^T
-    double s = 0.0;
-    for (int j = i + 1 + lane; j < n; j += 32) s += row[j] * y[j];
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-    const double v = (y[i] - s) * dinv[i];
-    __syncwarp();
-    if (lane == 0) y[i] = v;
-    __syncwarp();
+  __syncthreads();
+  for (int j = n - 1; j >= 0; --j) {
+    const double xj = z[j] * dinv[j];
+    const double* row = L + (size_t)j * n;  // L[j][i], i < j
+    for (int i = threadIdx.x; i < j; i += blockDim.x) z[i] -= row[i] * xj;
+    __syncthreads();
+    if (threadIdx.x == 0) z[j] = xj;
   }
+  __syncthreads();
+  if (sm)
+    for (int i = threadIdx.x; i < n; i += blockDim.x) y[i] = zb[i];
+  __syncthreads();
 }
 
-// Called by one full warp.
-__device__ void chol_solve_warp(const double* L, const double* dinv, int n, double* y) {
-  __shared__ double ys[kSolveSmem];
-  const int lane = threadIdx.x & 31;
-  if (n > kSolveSmem) {
-    chol_solve_rows(L, dinv, n, y);
-    return;
-  }
-  for (int i = lane; i < n; i += 32) ys[i] = y[i];
-  __syncwarp();
-  chol_solve_rows(L, dinv, n, ys);
-  for (int i = lane; i < n; i += 32) y[i] = ys[i];
-  __syncwarp();
-}
-
-// Newton step on a free set F (one block per job): delta_F = H_FF^-1 (-1 - df)_F,
-// delta = 0 outside F. Newton / m-newton (glisa.py:734-748): F = all shells;
-// projected Newton: F = {c > 0 or dF/dc < 0}. The factor of H_FF stays in
-// chol and |F| in freeidx[nshell] for the refinement steps.
 // Shared memory of the Newton step: the factor (dynamic, when |F|^2 doubles
 // fit in kNewtonSmemL) and the two column buffers (when |F| <= kNewtonColMax).
 constexpr int kNewtonSmemL = 200 * 1024;
@@ -1328,18 +1319,14 @@ __global__ void __launch_bounds__(kThreads) k_glisa_newton_step(Batch bt, int pr
   // (kept for the refinement)
   double* colbuf = nf <= kNewtonColMax ? col_smem : J.ctrial;
   chol_factor(L, nf, &bad, colbuf, J.ctrial + 2 * M);
-  if (threadIdx.x < 32) {
-    double* y = J.keep;  // scratch (the m-newton mask is formed after the step)
-    for (int i = threadIdx.x; i < nf; i += 32) y[i] = -(1.0 + J.grad[J.freeidx[i]]);
-    __syncwarp();
-    chol_solve_warp(L, J.ctrial + 2 * M, nf, y);
-    for (int i = threadIdx.x; i < nf; i += 32) J.delta[J.freeidx[i]] = y[i];
-    if (threadIdx.x == 0 && bad) atomicOr(&J.mail->i[MI_ERR], E_SINGULAR);
-  }
-  if (l_in_smem) {  // the refinement steps read the factor from chol
-    __syncthreads();
+  double* y = J.keep;  // scratch (the m-newton mask is formed after the step)
+  for (int i = threadIdx.x; i < nf; i += kThreads) y[i] = -(1.0 + J.grad[J.freeidx[i]]);
+  __syncthreads();
+  chol_solve_block(L, J.ctrial + 2 * M, nf, y);
+  for (int i = threadIdx.x; i < nf; i += kThreads) J.delta[J.freeidx[i]] = y[i];
+  if (threadIdx.x == 0 && bad) atomicOr(&J.mail->i[MI_ERR], E_SINGULAR);
+  if (l_in_smem)  // the refinement steps read the factor from chol
     for (int e = threadIdx.x; e < nf * nf; e += kThreads) J.chol[e] = L[e];
-  }
 }
 
 // Hessian-vector product with the exact FP64 Hessian, first half:
@@ -1375,10 +1362,8 @@ __global__ void __launch_bounds__(kThreads) k_glisa_refine(Batch bt) {
     if (lane == 0) r[i] = -(1.0 + J.grad[m]) - hd;
   }
   __syncthreads();
-  if (threadIdx.x < 32) {
-    chol_solve_warp(J.chol, J.ctrial + 2 * M, nf, r);
-    for (int i = threadIdx.x; i < nf; i += 32) J.delta[J.freeidx[i]] += r[i];
-  }
+  chol_solve_block(J.chol, J.ctrial + 2 * M, nf, r);
+  for (int i = threadIdx.x; i < nf; i += kThreads) J.delta[J.freeidx[i]] += r[i];
 }
 
 // Projected-Newton trial points c_t = max(c + 2^-t delta, 0), t < kTrials,
@@ -1803,9 +1788,13 @@ void launch_glisa_solve(const HostBatch& hb, cudaStream_t st, int projected) {
   }
 }
 
-void launch_glisa_refine(const HostBatch& hb, cudaStream_t st) {
-  HP_LAUNCH(k_glisa_hv, K_POINT1, kThreads);
-  HP_LAUNCH(k_glisa_grad, K_POINT, kThreads, 1);
+void launch_glisa_refine(const HostBatch& hb, cudaStream_t st, int gff) {
+  if (gff) {
+    launch_glisa_hv_ff(hb, st);
+  } else {
+    HP_LAUNCH(k_glisa_hv, K_POINT1, kThreads);
+    HP_LAUNCH(k_glisa_grad, K_POINT, kThreads, 1);
+  }
   HP_LAUNCH(k_glisa_refine, K_JOB, kThreads);
 }
 
@@ -1826,9 +1815,10 @@ void launch_glisa_change(const HostBatch& hb, cudaStream_t st) {
 
 void launch_glisa_check(const HostBatch& hb, cudaStream_t st) { HP_LAUNCH(k_glisa_check, K_JOB, 32); }
 
-void launch_glisa_pnewton(const HostBatch& hb, cudaStream_t st) {
+void launch_glisa_pnewton(const HostBatch& hb, cudaStream_t st, int gff) {
   HP_LAUNCH(k_glisa_trial_set, K_JOB, kThreads);
-  HP_LAUNCH(k_glisa_trials, K_POINT, kThreads);
+  if (gff) launch_glisa_trials_ff(hb, st);
+  else HP_LAUNCH(k_glisa_trials, K_POINT, kThreads);
   HP_LAUNCH(k_glisa_trial_pick, K_JOB, 32);
 }
 

@@ -66,6 +66,7 @@ struct hp_ctx {
   double prof_ms[HP_KERNEL_COUNT] = {};
   int64_t prof_n[HP_KERNEL_COUNT] = {};
   long long launch_base = 0;
+  int slots_hi = 0;  // one past the highest slot a job has used (mailboxes to read back)
 };
 
 struct hp_job {
@@ -98,9 +99,10 @@ namespace {
 //     the last kFloorWindow iterations is not below the best of the window
 //     before): the FP32 noise floor. A slowly but steadily converging job
 //     (linear rate up to 0.999 per iteration) never reaches this state.
-//   MIXED_NEAR: the change is within 100 x the threshold.
+//   MIXED_NEAR: the change is within kNearFactor x the threshold.
 enum MixedState { MIXED_GO = 0, MIXED_NEAR = 1, MIXED_FLOOR = 2 };
 constexpr size_t kFloorWindow = 8;
+constexpr double kNearFactor = 10.0;
 
 int mixed_state(const hp_job* j) {
   const size_t n = j->changes.size();
@@ -110,7 +112,7 @@ int mixed_state(const hp_job* j) {
     for (size_t i = n - kFloorWindow; i < n; ++i) b = std::min(b, j->changes[i]);
     if (b >= 0.999 * a) return MIXED_FLOOR;
   }
-  if (j->change < 100.0 * j->desc.threshold) return MIXED_NEAR;
+  if (j->change < kNearFactor * j->desc.threshold) return MIXED_NEAR;
   return MIXED_GO;
 }
 
@@ -200,7 +202,8 @@ int build_batch(hp_ctx* ctx, const std::vector<hp_job*>& jobs, HostBatch& hb) {
 }
 
 int read_mail(hp_ctx* ctx) {
-  HP_CK(cudaMemcpyAsync(ctx->mail_host, ctx->mail_dev, sizeof(Mailbox) * kMaxSlots,
+  const int n = std::max(1, ctx->slots_hi);
+  HP_CK(cudaMemcpyAsync(ctx->mail_host, ctx->mail_dev, sizeof(Mailbox) * n,
                         cudaMemcpyDeviceToHost, ctx->stream));
   HP_CK(cudaStreamSynchronize(ctx->stream));
   prof_collect(ctx);
@@ -262,7 +265,7 @@ int run_inner(hp_ctx* ctx, const std::vector<hp_job*>& jobs, const HostBatch& hb
 int job_init(hp_ctx* ctx, const std::vector<hp_job*>& jobs, const HostBatch& hb) {
   launch_nelec(hb, ctx->stream);
   bool any_basis = false;
-  for (hp_job* j : jobs) any_basis |= j->dev.gmat != nullptr;
+  for (hp_job* j : jobs) any_basis |= j->dev.gmat != nullptr || j->dev.gmat_lo != nullptr;
   if (any_basis) launch_glisa_basis(hb, ctx->stream);
   for (hp_job* j : jobs) j->initialized = true;
   return check_launch();
@@ -280,12 +283,19 @@ int step_iterstock(hp_ctx* ctx, const std::vector<hp_job*>& jobs, const HostBatc
     launch_promol(hb, st, mixed, model);
   }
   int rc = HP_OK;
+  const bool local = j0->dev.local != 0;
   switch (j0->desc.scheme) {
     case HP_SCHEME_MBIS:
-      rc = run_inner(ctx, jobs, hb, [&] {
+      if (local) {  // atom grids: every inner iteration of every atom in one launch
         ProfScope ps(ctx, HP_KERNEL_INNER);
-        launch_mbis_inner(hb, st, mixed);
-      }, j0->dev.inner_maxiter + 1);
+        launch_inner_init(hb, st);
+        launch_mbis_local(hb, st);
+      } else {
+        rc = run_inner(ctx, jobs, hb, [&] {
+          ProfScope ps(ctx, HP_KERNEL_INNER);
+          launch_mbis_inner(hb, st, mixed);
+        }, j0->dev.inner_maxiter + 1);
+      }
       break;
     case HP_SCHEME_GISA: {
       ProfScope ps(ctx, HP_KERNEL_INNER);
@@ -308,7 +318,8 @@ int step_iterstock(hp_ctx* ctx, const std::vector<hp_job*>& jobs, const HostBatc
   if (rc) return rc;
   {
     ProfScope ps(ctx, HP_KERNEL_CHANGE);
-    launch_change(hb, st, mixed, model);
+    if (local) launch_change_radial(hb, st);
+    else launch_change(hb, st, mixed, model);
   }
   launch_outer_finish(hb, st, 1);
   rc = check_launch();
@@ -328,7 +339,10 @@ int step_iterstock(hp_ctx* ctx, const std::vector<hp_job*>& jobs, const HostBatc
     const double n = (double)j->dev.npoint;
     const double a = (double)j->dev.natom;
     const double inner_evals = j->desc.scheme == HP_SCHEME_GISA ? a : inner;
-    j->evals += n * (3.0 * a + inner_evals);
+    if (j->dev.local)  // promolecule on the molecular grid; inner and change on the radial grids
+      j->evals += n * a + (inner + 2.0 * a) * (double)j->dev.nrad / a;
+    else
+      j->evals += n * (3.0 * a + inner_evals);
     if (j->dev.mixed != PH_FP32 && j->desc.precision == HP_PRECISION_MIXED) j->polish_iters += 1;
     if (m.i[MI_ERR]) {
       j->status = status_of(m.i[MI_ERR]);
@@ -367,15 +381,18 @@ int step_glisa(hp_ctx* ctx, const std::vector<hp_job*>& jobs, const HostBatch& h
   cudaStream_t st = ctx->stream;
   const int solver = jobs[0]->dev.solver;
   launch_copy_old(hb, st);
+  const bool tc = jobs[0]->dev.tc != 0;
+  const int gff = jobs[0]->dev.gff;
   {
     ProfScope ps(ctx, HP_KERNEL_GLISA_PRO);
-    launch_glisa_pro(hb, st);
+    if (gff) launch_glisa_pro_ff(hb, st);
+    else launch_glisa_pro(hb, st);
   }
   {
     ProfScope ps(ctx, HP_KERNEL_GLISA_GRAD);
-    launch_glisa_grad(hb, st);
+    if (gff) launch_glisa_grad_ff(hb, st);
+    else launch_glisa_grad(hb, st);
   }
-  const bool tc = jobs[0]->dev.tc != 0;
   if (solver != SOLVER_SC) {
     ProfScope ps(ctx, HP_KERNEL_GLISA_HESS);
     if (tc) launch_glisa_hess_tc(hb, st);
@@ -391,10 +408,10 @@ int step_glisa(hp_ctx* ctx, const std::vector<hp_job*>& jobs, const HostBatch& h
       // iterative refinement against the exact FP64 product H delta.
       launch_glisa_solve(hb, st, solver == SOLVER_PNEWTON ? 1 : 0);
       if (tc)
-        for (int k = 0; k < kRefineSteps; ++k) launch_glisa_refine(hb, st);
+        for (int k = 0; k < kRefineSteps; ++k) launch_glisa_refine(hb, st, gff);
     }
     if (solver == SOLVER_PNEWTON) {
-      launch_glisa_pnewton(hb, st);
+      launch_glisa_pnewton(hb, st, gff);
     } else if (solver != SOLVER_SC) {
       if (solver == SOLVER_NEWTON) launch_glisa_apply(hb, st, 0);
       else {
@@ -440,7 +457,8 @@ int step_glisa(hp_ctx* ctx, const std::vector<hp_job*>& jobs, const HostBatch& h
   }
   {
     ProfScope ps(ctx, HP_KERNEL_CHANGE);
-    launch_glisa_change(hb, st);
+    if (gff) launch_glisa_change_ff(hb, st);
+    else launch_glisa_change(hb, st);
   }
   launch_outer_finish(hb, st, 0);
   int rc = check_launch();
@@ -528,8 +546,26 @@ int validate(const hp_job_desc* d) {
   if (!d->coordinates || !d->pseudo_numbers || !d->points || !d->weights || !d->density ||
       !d->shell_offsets || !d->initial_propars)
     return fail(HP_ERR_INVALID, "missing input array");
-  if (d->grid_type != 2 && d->grid_type != 3)
-    return fail(HP_ERR_UNSUPPORTED, "only grid_type 2 and 3 (molecular grid) are supported");
+  if (d->grid_type != 1 && d->grid_type != 2 && d->grid_type != 3)
+    return fail(HP_ERR_INVALID, "grid_type must be 1, 2 or 3");
+  if (d->grid_type == 1) {
+    if (d->scheme != HP_SCHEME_MBIS)
+      return fail(HP_ERR_UNSUPPORTED, "grid_type 1 (atom grids) is available for MBIS");
+    if (!d->radial_offsets || !d->shell_point_offsets || !d->point_sphere_weights ||
+        !d->radial_points || !d->radial_weights || d->nrad <= 0)
+      return fail(HP_ERR_INVALID, "grid_type 1 needs the atom-grid arrays");
+    if (d->radial_offsets[0] != 0 || d->radial_offsets[d->natom] != d->nrad)
+      return fail(HP_ERR_INVALID, "radial_offsets must run from 0 to nrad");
+    for (int64_t a = 0; a < d->natom; ++a) {
+      const int n = d->radial_offsets[a + 1] - d->radial_offsets[a];
+      if (n <= 0 || n > 1024) return fail(HP_ERR_INVALID, "every atom needs 1 to 1024 radial nodes");
+    }
+    if (d->shell_point_offsets[0] != 0 || d->shell_point_offsets[d->nrad] != d->npoint)
+      return fail(HP_ERR_INVALID, "shell_point_offsets must run from 0 to npoint");
+    for (int64_t k = 0; k < d->nrad; ++k)
+      if (d->shell_point_offsets[k + 1] < d->shell_point_offsets[k])
+        return fail(HP_ERR_INVALID, "shell_point_offsets must not decrease");
+  }
   if (d->scheme != HP_SCHEME_MBIS && (!d->shell_orders || !d->shell_exponents))
     return fail(HP_ERR_INVALID, "basis schemes need shell orders and exponents");
   if (d->shell_offsets[0] != 0) return fail(HP_ERR_INVALID, "shell_offsets[0] must be 0");
@@ -686,7 +722,10 @@ int32_t hp_job_create(hp_ctx* ctx, const hp_job_desc* d, hp_job** out) {
   // (mixed precision: at least 4 points per thread so the per-block
   // compensated reductions are amortised)
   const int ppt_min = d->precision != HP_PRECISION_FP64 && !glisa ? 4 : 2;
-  int ppt = (int)std::min<int64_t>(64, std::max<int64_t>(ppt_min, (N + kThreads * 304 - 1) / (kThreads * 304)));
+  // gLISA's passes over G keep one point tile per block: aim for 4 blocks per SM
+  const int64_t tiles_target = glisa ? 4 * 152 : 2 * 152;
+  int ppt = (int)std::min<int64_t>(
+      64, std::max<int64_t>(ppt_min, (N + kThreads * tiles_target - 1) / (kThreads * tiles_target)));
   const int tile_points = kThreads * ppt;
   const int ntile = (N + tile_points - 1) / tile_points;
   int qa = 2 + std::max(2 * 7 + 1, kMaxShells + 1);
@@ -759,8 +798,11 @@ int32_t hp_job_create(hp_ctx* ctx, const hp_job_desc* d, hp_job** out) {
   const size_t gbytes = 8 * (size_t)S * N;
   const size_t room = ctx->budget > ctx->used ? ctx->budget - ctx->used : 0;
   if (!glisa && !mbis && !mixed && gbytes <= room / 2) add(&J.gmat, gbytes);
+  // gLISA with the tensor-core Hessian (Newton or projected Newton): G as
+  // float-float planes, no FP64 copy
+  const bool gff = tc && solver != HP_SOLVER_M_NEWTON && S <= kGffMaxShells;
   if (glisa) {
-    add(&J.gmat, 8 * (size_t)S * N);
+    if (!gff) add(&J.gmat, 8 * (size_t)S * N);
     add(&J.gpart, 8 * (size_t)S * ntile);
     add(&J.hpart, 8 * (size_t)nsplit * S * S);
     add(&J.hess, 8 * (size_t)S * S);
@@ -775,8 +817,24 @@ int32_t hp_job_create(hp_ctx* ctx, const hp_job_desc* d, hp_job** out) {
     if (tc) {
       add(&J.gmat32, 4 * (size_t)S * N);
       add(&J.hess_s, 4 * (size_t)N);
-      add(&J.hvec, 8 * (size_t)N);
+      if (gff) {
+        add(&J.gmat_lo, 4 * (size_t)S * N);
+        add(&J.d1f, 8 * (size_t)N);
+        add(&J.hvf, 8 * (size_t)N);
+      } else {
+        add(&J.hvec, 8 * (size_t)N);
+      }
     }
+  }
+  const bool local = d->grid_type == 1;
+  const int nrad = local ? d->nrad : 0;
+  if (local) {
+    add(&J.rad_off, 4 * (size_t)(A + 1));
+    add(&J.shell_pt, 8 * (size_t)(nrad + 1));
+    add(&J.wsph, 8 * (size_t)N);
+    add(&J.rad_r, 8 * (size_t)nrad);
+    add(&J.rad_w, 8 * (size_t)nrad);
+    add(&J.radrho, 8 * (size_t)nrad);
   }
   add(&J.hist_propars, 8 * (size_t)maxiter * P);
   add(&J.hist_charges, 8 * (size_t)maxiter * A);
@@ -804,6 +862,9 @@ int32_t hp_job_create(hp_ctx* ctx, const hp_job_desc* d, hp_job** out) {
   J.linspace_size = d->linspace_size > 0 ? d->linspace_size : (glisa ? 40 : 20);
   J.nsplit = nsplit; J.ppt = ppt; J.tile_points = tile_points; J.htiles = htiles;
   J.tc = tc ? 1 : 0;
+  J.gff = gff ? 1 : 0;
+  J.local = local ? 1 : 0;
+  J.nrad = nrad;
   J.threshold = d->threshold;
   J.inner_threshold = d->inner_threshold < d->threshold ? d->inner_threshold : d->threshold;
   J.density_cutoff = d->density_cutoff; J.negative_cutoff = d->negative_cutoff;
@@ -843,6 +904,13 @@ int32_t hp_job_create(hp_ctx* ctx, const hp_job_desc* d, hp_job** out) {
   }
   ok &= up(J.w, d->weights, 8 * (size_t)N) == cudaSuccess;
   ok &= up(J.rho, d->density, 8 * (size_t)N) == cudaSuccess;
+  if (local) {
+    ok &= up(J.rad_off, d->radial_offsets, 4 * (size_t)(A + 1)) == cudaSuccess;
+    ok &= up(J.shell_pt, d->shell_point_offsets, 8 * (size_t)(nrad + 1)) == cudaSuccess;
+    ok &= up(J.wsph, d->point_sphere_weights, 8 * (size_t)N) == cudaSuccess;
+    ok &= up(J.rad_r, d->radial_points, 8 * (size_t)nrad) == cudaSuccess;
+    ok &= up(J.rad_w, d->radial_weights, 8 * (size_t)nrad) == cudaSuccess;
+  }
   std::vector<float> wf32, rf32, wl32, rl32;
   if (mixed) {
     wf32.resize((size_t)N);
@@ -939,6 +1007,7 @@ int32_t hp_job_create(hp_ctx* ctx, const hp_job_desc* d, hp_job** out) {
   }
   memset(&ctx->mail_host[slot], 0, sizeof(Mailbox));
   ctx->slots[slot] = job;
+  ctx->slots_hi = std::max(ctx->slots_hi, slot + 1);
   ctx->used += total;
   *out = job;
   return HP_OK;
@@ -970,7 +1039,8 @@ int32_t hp_step(hp_ctx* ctx, hp_job* const* jobs, int32_t njobs, int32_t* n_live
     for (auto& g : groups) {
       const hp_job* h = g[0];
       if (h->desc.scheme == j->desc.scheme && h->dev.solver == j->dev.solver &&
-          h->dev.mixed == j->dev.mixed && h->dev.tc == j->dev.tc) {
+          h->dev.mixed == j->dev.mixed && h->dev.tc == j->dev.tc &&
+          h->dev.local == j->dev.local) {
         g.push_back(j);
         placed = true;
         break;

@@ -42,6 +42,7 @@ class MBISWPart(GPUStockholderWPart):
     name = "mbis"
     _scheme = "mbis"
     _inner_warning = "MBIS not converged, but still go ahead!"
+    _supports_atom_grids = True  # grid_type 1: spherical averages on the radial grids
 
     def _shell_tables(self):
         self._ranges = [0]

@@ -21,6 +21,9 @@ import numpy as np
 
 __all__ = [
     "MolecularGrid",
+    "RadialGrid",
+    "AtomGrid",
+    "atom_grid_arrays",
     "lebedev",
     "radial_becke_gauss_chebyshev",
     "becke_molecular_grid",
@@ -79,6 +82,90 @@ class MolecularGrid:
         for arr in value_arrays[1:]:
             prod = prod * arr
         return float(np.dot(self._weights, prod))
+
+
+class RadialGrid:
+    """Radial nodes and weights (qc-grid ``OneDGrid`` surface used by the
+    reference: ``points``, ``weights``, ``size``, ``integrate``)."""
+
+    def __init__(self, points, weights):
+        self.points = np.ascontiguousarray(points, dtype=np.float64)
+        self.weights = np.ascontiguousarray(weights, dtype=np.float64)
+
+    @property
+    def size(self):
+        return self.points.size
+
+    def integrate(self, *value_arrays):
+        prod = value_arrays[0]
+        for arr in value_arrays[1:]:
+            prod = prod * arr
+        return float(np.dot(self.weights, prod))
+
+
+# Lebedev rule size -> degree (the reference logs the degrees)
+_LEBEDEV_DEGREE = {50: 11, 110: 17, 194: 23, 302: 29, 590: 41}
+
+
+class AtomGrid:
+    """One atom's radial x Lebedev grid (the parts of qc-grid's ``AtomGrid``
+    that grid_type 1 uses: ``rgrid``, ``size``, ``degrees`` and
+    ``spherical_average``). Its points are ordered shell by shell: shell i
+    owns points ``shell_offsets[i]:shell_offsets[i+1]`` with angular weights
+    ``sphere_weights`` (Lebedev weight / 4 pi, summing to 1 over a shell)."""
+
+    def __init__(self, rpoints, rweights, nang):
+        self.rgrid = RadialGrid(rpoints, rweights)
+        ang, wang = lebedev(nang)
+        self.shell_offsets = np.arange(self.rgrid.size + 1, dtype=np.int64) * nang
+        self.sphere_weights = np.tile(wang / (4.0 * np.pi), self.rgrid.size)
+        self.degrees = np.full(self.rgrid.size, _LEBEDEV_DEGREE.get(nang, 0))
+
+    @property
+    def size(self):
+        return int(self.shell_offsets[-1])
+
+    def spherical_average(self, values):
+        """Cubic spline through the angular averages of ``values`` on the
+        radial nodes (evaluated at the nodes it returns the averages)."""
+        from scipy.interpolate import CubicSpline
+
+        shell = np.repeat(np.arange(self.rgrid.size), np.diff(self.shell_offsets))
+        avg = np.bincount(shell, weights=self.sphere_weights * values, minlength=self.rgrid.size)
+        return CubicSpline(self.rgrid.points, avg)
+
+
+def atom_grid_arrays(grid):
+    """The grid_type 1 arrays of the C ABI from a molecular grid with atom
+    grids (``grid.atgrids``, ``grid.indices``): radial offsets per atom,
+    point offsets per radial shell, angular weight / 4 pi per point, radial
+    nodes and weights. Accepts this package's :class:`AtomGrid` and qc-grid
+    atom grids (whose ``indices`` delimit the shells and whose weights are
+    w_r r^2 w_Lebedev)."""
+    roff, spo, wsph, rr, rw = [0], [0], [], [], []
+    base = 0
+    for a, ag in enumerate(grid.atgrids):
+        r = np.asarray(ag.rgrid.points, dtype=np.float64)
+        w = np.asarray(ag.rgrid.weights, dtype=np.float64)
+        if hasattr(ag, "shell_offsets"):
+            offs = np.asarray(ag.shell_offsets, dtype=np.int64)
+            ws = np.asarray(ag.sphere_weights, dtype=np.float64)
+        else:
+            offs = np.asarray(ag.indices, dtype=np.int64)
+            shell = np.repeat(np.arange(r.size), np.diff(offs))
+            ws = np.asarray(ag.weights, dtype=np.float64) / (4.0 * np.pi * r[shell] ** 2 * w[shell])
+        if grid.indices is not None and int(grid.indices[a]) != base:
+            raise ValueError("atom grids must follow each other in the molecular grid")
+        spo.extend((base + offs[1:]).tolist())
+        base += int(offs[-1])
+        roff.append(roff[-1] + r.size)
+        wsph.append(ws)
+        rr.append(r)
+        rw.append(w)
+    return dict(radial_offsets=np.asarray(roff, dtype=np.int32),
+                shell_point_offsets=np.asarray(spo, dtype=np.int64),
+                point_sphere_weights=np.concatenate(wsph), radial_points=np.concatenate(rr),
+                radial_weights=np.concatenate(rw))
 
 
 def lebedev(npoint):
@@ -168,4 +255,5 @@ def becke_molecular_grid(coordinates, nrad, nang, rmin=1e-4, radius=1.5):
         weights[a * npa : (a + 1) * npa] = shell_w
     weights *= becke_partition_weights(points, coordinates, owner)
     indices = np.arange(natom + 1, dtype=np.int64) * npa
-    return MolecularGrid(points, weights, indices=indices)
+    atgrids = [AtomGrid(r, wr, nang) for _ in range(natom)]
+    return MolecularGrid(points, weights, indices=indices, atgrids=atgrids)

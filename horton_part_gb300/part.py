@@ -335,16 +335,21 @@ class GPUStockholderWPart(WPart):
         pass
 
     # -- the partitioning ------------------------------------------------------
+    _supports_atom_grids = False  # grid_type 1 on the GPU (MBIS)
+
     def _check_grid_type(self):
-        if not self.on_molgrid:
+        if not self.on_molgrid and not self._supports_atom_grids:
             raise NotImplementedError(
-                "grid_type=1 (spherical averages on the atomic radial grids) is not available on "
-                "the GPU path; use grid_type=2 or 3 (molecular grid)")
+                "grid_type=1 (spherical averages on the atomic radial grids) is available for MBIS "
+                "on the GPU path; use grid_type=2 or 3 (molecular grid)")
 
     def _make_job(self):
+        from .molgrid import atom_grid_arrays
+
         self._check_grid_type()
         offsets, init, orders, exps = self._shell_tables()
         ctx = self._context or _lib.default_context(0)
+        local = None if self.on_molgrid else atom_grid_arrays(self.grid)
         return _lib.Job(
             ctx, self._scheme, self.coordinates, self.pseudo_numbers, self.grid.points,
             self.grid.weights, self._moldens, offsets, init, shell_orders=orders,
@@ -352,7 +357,7 @@ class GPUStockholderWPart(WPart):
             grid_type=self.grid_type, threshold=self._threshold,
             inner_threshold=self._inner_threshold, density_cutoff=self.density_cutoff,
             negative_cutoff=self.negative_cutoff, population_cutoff=self.population_cutoff,
-            maxiter=self._maxiter, polish=self._polish, **self._job_extra())
+            maxiter=self._maxiter, polish=self._polish, local=local, **self._job_extra())
 
     def _report_warnings(self, info):
         if info.warnings & _lib.WARN_INNER_NOT_CONVERGED:
@@ -404,7 +409,12 @@ class GPUStockholderWPart(WPart):
         self.cache.dump("promoldens", res["promoldens"])
         if self._store_at_weights:
             for i in range(self.natom):
-                self.cache.dump(f"at_weights_{i}", res["at_weights"][i])
+                # grid_type 1: each atom's at_weights live on its own atom grid
+                self.cache.dump(f"at_weights_{i}", self.to_atomic_grid(i, res["at_weights"][i]))
+        if not self.on_molgrid:
+            for i, ag in enumerate(self.grid.atgrids):
+                self.cache.dump(f"radial_points_{i}", np.asarray(ag.rgrid.points), tags="o")
+                self.cache.dump(f"radial_weights_{i}", np.asarray(ag.rgrid.weights), tags="o")
         charges = res["charges"]
         self.cache.dump("history_propars", np.array(self.history_propars), tags="o")
         self.cache.dump("history_charges", np.array(self.history_charges), tags="o")

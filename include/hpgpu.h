@@ -44,7 +44,7 @@
 extern "C" {
 #endif
 
-#define HPGPU_ABI_VERSION 1
+#define HPGPU_ABI_VERSION 2
 
 typedef enum {
   HP_OK = 0,
@@ -104,7 +104,7 @@ typedef struct {
   int32_t scheme;    /* hp_scheme */
   int32_t solver;    /* hp_solver */
   int32_t precision; /* hp_precision */
-  int32_t grid_type; /* 2 or 3 (molecular grid); 1 is not supported yet */
+  int32_t grid_type; /* 2 or 3 (molecular grid); 1 (atom grids: MBIS) */
   int64_t natom;
   int64_t npoint;
   const double* coordinates;    /* natom x 3, bohr */
@@ -139,6 +139,19 @@ typedef struct {
                              stopped decreasing (its noise floor); 0 = stay in
                              FP32 to the threshold and stop with
                              HP_WARN_NOISE_FLOOR only at the floor */
+  int32_t nrad;           /* grid_type 1: radial nodes over all atom grids */
+  /* grid_type 1 (atom grids, the reference's default; base.py:619-628,
+   * mbis.py:174-187): atom a owns the radial shells [radial_offsets[a],
+   * radial_offsets[a+1]) of the concatenated radial grids (nodes
+   * radial_points, weights radial_weights), and shell s owns the consecutive
+   * grid points [shell_point_offsets[s], shell_point_offsets[s+1]) with
+   * angular weights point_sphere_weights (Lebedev weight / 4 pi, summing to
+   * 1 over a shell). NULL for grid_type 2/3. */
+  const int32_t* radial_offsets;      /* natom + 1 */
+  const int64_t* shell_point_offsets; /* nrad + 1 */
+  const double* point_sphere_weights; /* npoint */
+  const double* radial_points;        /* nrad */
+  const double* radial_weights;       /* nrad */
 } hp_job_desc;
 
 typedef struct {

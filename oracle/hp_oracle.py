@@ -161,10 +161,27 @@ def opt_mbis_propars(rho, propars, weights, r, threshold, density_cutoff=DENSITY
     return propars, maxiter, False
 
 
+def spherical_average(values, shell, wsph, nrad):
+    """Angular average of ``values`` over each radial shell of one atom grid:
+    sum_j wsph_j f_j per shell, wsph = Lebedev weight / 4 pi (the node values
+    of the spline that qc-grid's ``AtomGrid.spherical_average`` returns;
+    ``mbis.py:179-184`` evaluates it at the radial nodes)."""
+    return np.bincount(shell, weights=wsph * values, minlength=nrad)
+
+
 def mbis(coordinates, numbers, pseudo_numbers, points, weights, rho, threshold=1e-6,
-         maxiter=500, inner_threshold=1e-8, density_cutoff=DENSITY_CUTOFF):
+         maxiter=500, inner_threshold=1e-8, density_cutoff=DENSITY_CUTOFF, local=None):
     """MBIS on the molecular grid (``core/iterstock.py:159-193``, ``mbis.py:167-203``,
-    ``mbis.py:291-362``)."""
+    ``mbis.py:291-362``).
+
+    ``local`` selects the atom-grid form (grid_type 1): a dict with
+    ``indices`` (atom a owns points indices[a]:indices[a+1]), per-atom radial
+    nodes ``rpoints`` and weights ``rweights`` (lists), and per point its
+    shell index within its atom grid (``shell``) and its angular weight / 4 pi
+    (``wsph``). The at_weights then act on each atom's own points, the inner
+    solve runs on the spherical average over the atom's radial grid
+    (``mbis.py:174-187``) and the change is a radial integral
+    (``core/iterstock.py:43-44``)."""
     natom = len(numbers)
     inner = inner_threshold if inner_threshold < threshold else threshold  # iterstock.py:101
     rs = radial_distances(points, coordinates)
@@ -183,22 +200,34 @@ def mbis(coordinates, numbers, pseudo_numbers, points, weights, rho, threshold=1
         promol, at_weights = stockholder_weights(pros)
         inner_its = []
         for a in range(natom):
-            rhoa = at_weights[a] * rho
             sl = slice(ranges[a], ranges[a + 1])
-            new, nit, _ = opt_mbis_propars(rhoa, propars[sl].copy(), weights, rs[a], inner,
+            if local is None:
+                rhoa, wa, ra = at_weights[a] * rho, weights, rs[a]
+            else:
+                own = slice(local["indices"][a], local["indices"][a + 1])
+                ra = local["rpoints"][a]
+                rhoa = spherical_average(at_weights[a][own] * rho[own], local["shell"][own],
+                                         local["wsph"][own], len(ra))
+                wa = 4 * np.pi * ra**2 * local["rweights"][a]
+            new, nit, _ = opt_mbis_propars(rhoa, propars[sl].copy(), wa, ra, inner,
                                            density_cutoff)
             propars[sl] = new
             inner_its.append(nit)
-            charges[a] = pseudo_numbers[a] - np.einsum("p,p->", weights, rhoa)
+            charges[a] = pseudo_numbers[a] - np.einsum("p,p->", wa, rhoa)
         res["inner_iterations"].append(inner_its)
         res["history_propars"].append(propars.copy())
         res["history_charges"].append(charges.copy())
         res["history_entropies"].append(entropy(weights, rho, promol, density_cutoff))
         msd = 0.0
         for a in range(natom):
-            d = (mbis_proatom(propars[ranges[a]:ranges[a + 1]], rs[a])
-                 - mbis_proatom(old[ranges[a]:ranges[a + 1]], rs[a]))
-            msd += integrate(weights, d, d)
+            if local is None:
+                ra, wa = rs[a], weights
+            else:
+                ra = local["rpoints"][a]
+                wa = 4 * np.pi * ra**2 * local["rweights"][a]
+            d = (mbis_proatom(propars[ranges[a]:ranges[a + 1]], ra)
+                 - mbis_proatom(old[ranges[a]:ranges[a + 1]], ra))
+            msd += integrate(wa, d, d)
         change = np.sqrt(msd)
         res["history_changes"].append(change)
         if change < threshold or counter >= maxiter:

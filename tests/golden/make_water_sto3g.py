@@ -64,13 +64,31 @@ def main(reference=None):
     from oracle import refrun
 
     ref = refrun.run("mbis", coords, numbers, pseudo, pts, weights, density, threshold=1e-8)
+    # and on the atom grids (grid_type 1, the reference's default and the
+    # setting of its published test): radial grid and Lebedev-110 per atom
+    natom = len(numbers)
+    local = atom_grid_description(natom, r, wr, wang)
+    ref1 = refrun.run("mbis", coords, numbers, pseudo, pts, weights, density, local=local,
+                      threshold=1e-8)
     out = os.path.join(HERE, "water_sto3g_hf_molgrid.npz")
     np.savez_compressed(out, points=pts, weights=weights, density=density, numbers=numbers,
                         coordinates=coords, pseudo_numbers=pseudo,
                         ref_charges=np.asarray(ref["charges"]), ref_propars=np.asarray(ref["propars"]),
-                        ref_niter=np.asarray(ref["niter"]))
+                        ref_niter=np.asarray(ref["niter"]), radial_points=r, radial_weights=wr,
+                        ref1_charges=np.asarray(ref1["charges"]),
+                        ref1_propars=np.asarray(ref1["propars"]), ref1_niter=np.asarray(ref1["niter"]))
     print(out, "integrated density", float(weights @ density), "reference charges",
-          ref["charges"], "niter", ref["niter"])
+          ref["charges"], "niter", ref["niter"], "grid_type 1:", ref1["charges"], ref1["niter"])
+
+
+def atom_grid_description(natom, r, wr, wang):
+    """Atom-grid layout of this fixture (atom after atom, radial shell after
+    radial shell, the Lebedev points of a shell together), in the form of the
+    oracle's ``local`` argument."""
+    nr, nq = len(r), len(wang)
+    return dict(indices=np.arange(natom + 1) * nr * nq, rpoints=[r] * natom,
+                rweights=[wr] * natom, shell=np.tile(np.repeat(np.arange(nr), nq), natom),
+                wsph=np.tile(wang / (4.0 * np.pi), nr * natom), nang=nq)
 
 
 if __name__ == "__main__":

@@ -38,12 +38,13 @@ def test_binding_covers_header():
 
 
 def test_abi_version(library):
-    assert _lib.lib().hp_abi_version() == 1
+    assert _lib.lib().hp_abi_version() == 2
 
 
 def test_struct_sizes_match_header():
-    # natural alignment on LP64: hp_job_desc is 4*4 + 2*8 + 9*8 + 6*8 + 4*4 bytes
-    assert ctypes.sizeof(_lib.JobDesc) == 16 + 16 + 72 + 48 + 16
+    # natural alignment on LP64: hp_job_desc is 4*4 + 2*8 + 9*8 + 6*8 + 4*4 bytes,
+    # then nrad (4 + 4 padding) and five atom-grid pointers
+    assert ctypes.sizeof(_lib.JobDesc) == 16 + 16 + 72 + 48 + 16 + 8 + 40
     assert ctypes.sizeof(_lib.JobResults) == 8 * 8
 
 

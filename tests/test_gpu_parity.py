@@ -103,11 +103,46 @@ def test_do_charges_and_do_all(gpu_context):
     assert part["charges"] == pytest.approx(part["valence_charges"] + part["core_charges"])
 
 
-def test_grid_type_1_is_rejected_like_the_reference(gpu_context):
+def test_grid_type_1_needs_atom_grids_like_the_reference(gpu_context):
+    """grid_type 1 without atom grids raises ValueError (core/base.py:461-465);
+    the basis schemes do not run on atom grids on this path."""
+    from horton_part_gb300.molgrid import MolecularGrid
+
     mol = synthetic.water(nrad=20, nang=50)
-    cls = wpart_schemes("mbis")
+    bare = MolecularGrid(mol.grid.points, mol.grid.weights)
     with pytest.raises(ValueError):
-        cls(mol.coordinates, mol.numbers, mol.pseudo_numbers, mol.grid, mol.density, grid_type=1)
+        wpart_schemes("mbis")(mol.coordinates, mol.numbers, mol.pseudo_numbers, bare, mol.density,
+                              grid_type=1)
+    part = wpart_schemes("gisa")(mol.coordinates, mol.numbers, mol.pseudo_numbers, mol.grid,
+                                 mol.density, grid_type=1)
+    with pytest.raises(NotImplementedError):
+        part.do_partitioning()
+
+
+def test_mbis_atom_grids_match_the_oracle(gpu_context):
+    """grid_type 1 on a synthetic water grid (Becke transform radial grid,
+    Lebedev-50): the GPU's atom-grid MBIS against the oracle's."""
+    from horton_part_gb300.molgrid import atom_grid_arrays
+
+    mol = synthetic.water(nrad=30, nang=50)
+    arr = atom_grid_arrays(mol.grid)
+    roff, spo = arr["radial_offsets"], arr["shell_point_offsets"]
+    shell = np.repeat(np.arange(len(spo) - 1), np.diff(spo))
+    local = dict(indices=np.asarray(mol.grid.indices),
+                 rpoints=[arr["radial_points"][roff[a]:roff[a + 1]] for a in range(3)],
+                 rweights=[arr["radial_weights"][roff[a]:roff[a + 1]] for a in range(3)],
+                 shell=shell - np.repeat(roff[:-1], np.diff(roff))[shell],
+                 wsph=arr["point_sphere_weights"])
+    from oracle import hp_oracle as O
+
+    ref = O.mbis(mol.coordinates, mol.numbers, mol.pseudo_numbers, mol.grid.points,
+                 mol.grid.weights, mol.density, threshold=1e-8, local=local)
+    part = wpart_schemes("mbis")(mol.coordinates, mol.numbers, mol.pseudo_numbers, mol.grid,
+                                 mol.density, grid_type=1, threshold=1e-8)
+    part.do_partitioning()
+    assert part["niter"] == ref["niter"]
+    np.testing.assert_allclose(part["charges"], ref["charges"], atol=1e-9)
+    np.testing.assert_allclose(part["propars"], ref["propars"], rtol=1e-7)
 
 
 def test_numbers_must_be_int64(gpu_context):
@@ -191,3 +226,33 @@ def test_mbis_water_hf_sto3g_reference_data(precision, tol, gpu_context):
         assert part["niter"] == int(d["ref_niter"])
     published = np.array([-0.61891067, 0.3095756, 0.30932584])
     assert np.abs(part["charges"] - published).max() < 2e-3
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-9), ("ff", 1e-9), ("mixed", 1e-6)])
+def test_mbis_atom_grids_water_hf_sto3g(precision, tol, gpu_context):
+    """grid_type 1 (atom grids, the reference's default) on the reference's
+    cached water HF/STO-3G data: against the unmodified reference run on the
+    same atom grids, and within 5e-5 e of the published charges of
+    horton-part's tests/test_wpart.py:95-101."""
+    from horton_part_gb300.molgrid import AtomGrid, MolecularGrid
+
+    path = os.path.join(os.path.dirname(__file__), "golden", "water_sto3g_hf_molgrid.npz")
+    with np.load(path) as f:
+        d = {k: f[k] for k in f.files}
+    natom = len(d["numbers"])
+    npa = len(d["radial_points"]) * 110
+    atgrids = [AtomGrid(d["radial_points"], d["radial_weights"], 110) for _ in range(natom)]
+    grid = MolecularGrid(d["points"], d["weights"], indices=np.arange(natom + 1) * npa,
+                         atgrids=atgrids)
+    part = wpart_schemes("mbis")(d["coordinates"], d["numbers"], d["pseudo_numbers"], grid,
+                                 d["density"], grid_type=1, threshold=1e-8, precision=precision)
+    part.do_partitioning()
+    dq = float(np.abs(part["charges"] - d["ref1_charges"]).max())
+    print(f"water HF/STO-3G atom grids {precision}: niter {part['niter']} "
+          f"(reference {int(d['ref1_niter'])}), max|dq| {dq:.2e}")
+    assert dq < tol
+    if precision != "mixed":
+        assert part["niter"] == int(d["ref1_niter"])
+    published = np.array([-0.61891067, 0.3095756, 0.30932584])
+    assert np.abs(part["charges"] - published).max() < 5e-5
+    assert part["at_weights_0"].shape == (npa,)

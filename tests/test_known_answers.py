@@ -145,3 +145,26 @@ def test_mbis_water_hf_sto3g_reference_data():
     np.testing.assert_allclose(res["charges"], d["ref_charges"], atol=1e-10)
     published = np.array([-0.61891067, 0.3095756, 0.30932584])
     assert np.abs(res["charges"] - published).max() < 2e-3
+
+
+def test_mbis_water_hf_sto3g_atom_grids():
+    """grid_type 1 (the reference's default): spherical averages on each
+    atom's radial grid. The oracle reproduces the unmodified reference run on
+    the same atom grids, and both land within 5e-5 e of the published charges
+    of horton-part's tests/test_wpart.py:95-101 (whose tolerance is 2e-3)."""
+    import sys
+    import os
+
+    sys.path.insert(0, os.path.join(os.path.dirname(__file__), "golden"))
+    from make_water_sto3g import atom_grid_description
+    from horton_part_gb300.molgrid import lebedev
+
+    d = _water_sto3g()
+    _, wang = lebedev(110)
+    local = atom_grid_description(len(d["numbers"]), d["radial_points"], d["radial_weights"], wang)
+    res = O.mbis(d["coordinates"], d["numbers"], d["pseudo_numbers"], d["points"], d["weights"],
+                 d["density"], threshold=1e-8, maxiter=500, inner_threshold=1e-8, local=local)
+    assert res["niter"] == int(d["ref1_niter"])
+    np.testing.assert_allclose(res["charges"], d["ref1_charges"], atol=1e-10)
+    published = np.array([-0.61891067, 0.3095756, 0.30932584])
+    assert np.abs(res["charges"] - published).max() < 5e-5

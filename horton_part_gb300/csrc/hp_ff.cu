@@ -61,14 +61,18 @@ __device__ __forceinline__ f2 load2(const float2* p) {
   return {v.x, v.y};
 }
 
-// Distance from grid point p to atom a; coordinates as float hi/lo pairs.
-__device__ __forceinline__ f2 dist_ff(const JobDev& J, int p, int a) {
+// Squared distance from grid point p to atom a; coordinates as float hi/lo pairs.
+__device__ __forceinline__ f2 dist2_ff(const JobDev& J, int p, int a) {
   const float* c = J.atf + 6 * a;  // xh, xl, yh, yl, zh, zl
   const f2 dx = ffa::add(ffa::two_sum(J.pxh[p], -c[0]), J.pxl[p] - c[1]);
   const f2 dy = ffa::add(ffa::two_sum(J.pyh[p], -c[2]), J.pyl[p] - c[3]);
   const f2 dz = ffa::add(ffa::two_sum(J.pzh[p], -c[4]), J.pzl[p] - c[5]);
-  const f2 d2 = ffa::add_pos(ffa::add_pos(ffa::sqr(dx), ffa::sqr(dy)), ffa::sqr(dz));
-  return ffa::sqrt_ff(d2);
+  return ffa::add_pos(ffa::add_pos(ffa::sqr(dx), ffa::sqr(dy)), ffa::sqr(dz));
+}
+
+// Distance from grid point p to atom a.
+__device__ __forceinline__ f2 dist_ff(const JobDev& J, int p, int a) {
+  return ffa::sqrt_ff(dist2_ff(J, p, a));
 }
 
 // Slater shell A exp(-S r), A = N S^3 / (8 pi), from FF coefficients.
@@ -197,7 +201,7 @@ __global__ void __launch_bounds__(kThreads) k_atweights_ff(Batch bt) {
 // A_old, S_old, g, dS, A_new lo, S_new lo).
 constexpr int kFfMbisQ = 2 * 7 + 1;
 
-__global__ void __launch_bounds__(kThreads) k_mbis_inner_ff(Batch bt) {
+__global__ void __launch_bounds__(kThreads, 4) k_mbis_inner_ff(Batch bt) {
   __shared__ float2 tab[64];
   __shared__ float2 red[kWarps * kFfMbisQ];
   __shared__ float2 out[kFfMbisQ];
@@ -303,6 +307,41 @@ void ensure_exp_table() {
 
 }  // namespace
 
+// Basis matrix of a gLISA job as float-float planes (gmat32 = hi, gmat_lo =
+// lo): G[s][p] = pref_s exp(-alpha_s r^order_s), the unit-population shells
+// of gisa.py:91-106 (force_on_molgrid=True) with the normalisation of
+// core/basis.py:161. Orders 2 (from the squared distance) and 1 are evaluated
+// in FF, any other order in FP64. fpar[4 s ..] = (pref hi, pref lo, alpha hi,
+// alpha lo). One thread per grid point, all shells.
+__global__ void __launch_bounds__(kThreads) k_glisa_basis_ff(Batch bt) {
+  __shared__ float2 tab[64];
+  ffa::load_exp_table(tab);
+  int blk;
+  const JobDev& J = decode_local_ff(bt, blk);
+  const int p = blk * kThreads + threadIdx.x;
+  if (p >= J.npoint) return;
+  for (int a = 0; a < J.natom; ++a) {
+    const f2 d2 = dist2_ff(J, p, a);
+    const f2 r = d2.hi > 0.0f ? ffa::sqrt_ff(d2) : f2{0.0f, 0.0f};
+    for (int s = J.shell_off[a]; s < J.shell_off[a + 1]; ++s) {
+      const double order = J.sh_order[s];
+      f2 g;
+      if (order == 2.0 || order == 1.0) {
+        const float* c = J.fpar + 4 * s;
+        const f2 x = ffa::mul(f2{c[2], c[3]}, order == 2.0 ? d2 : r);
+        g = ffa::mul(f2{c[0], c[1]}, ffa::exp_ff(ffa::neg(x), tab));
+      } else {
+        const double v = basis_shell<double>(order, J.sh_alpha[s], J.sh_pref[s],
+                                             Dist<double>::r(J, p, a));
+        split(v, &g.hi, &g.lo);
+      }
+      const size_t e = (size_t)s * J.npoint + p;
+      J.gmat32[e] = g.hi;
+      J.gmat_lo[e] = g.lo;
+    }
+  }
+}
+
 #define HP_LAUNCH_FF(kernel, kind, threads, ...)                                       \
   do {                                                                                 \
     if (hb.blocks[kind] > 0) {                                                         \
@@ -321,6 +360,11 @@ void launch_promol_ff(const HostBatch& hb, cudaStream_t st) {
 void launch_mbis_inner_ff(const HostBatch& hb, cudaStream_t st) {
   ensure_exp_table();
   HP_LAUNCH_FF(k_mbis_inner_ff, K_ATOM_TILE, kThreads);
+}
+
+void launch_glisa_basis_ff(const HostBatch& hb, cudaStream_t st) {
+  ensure_exp_table();
+  HP_LAUNCH_FF(k_glisa_basis_ff, K_POINT1, kThreads);
 }
 
 void launch_final_atweights_ff(const HostBatch& hb, cudaStream_t st, int use_old) {

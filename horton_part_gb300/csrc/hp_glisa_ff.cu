@@ -22,6 +22,8 @@ namespace hp {
 
 namespace {
 
+using ffa::f2;
+
 struct Dot2 {
   float s, c;  // running sum and the sum of its rounding errors
 };
@@ -46,6 +48,9 @@ __device__ __forceinline__ void dot2_merge(Dot2& a, const Dot2& b) {
 
 __device__ __forceinline__ double dot2_value(const Dot2& a) { return (double)a.s + (double)a.c; }
 
+// The compensated sum as a normalised float pair.
+__device__ __forceinline__ ffa::f2 dot2_ff(const Dot2& a) { return ffa::two_sum(a.s, a.c); }
+
 __device__ __forceinline__ float2 split2(double v) {
   const float hi = (float)v;
   return make_float2(hi, (float)(v - (double)hi));
@@ -61,6 +66,30 @@ __device__ __forceinline__ int point_in_tile(const JobDev& J, int tile, int i) {
   return tile * J.tile_points + i * kThreads + threadIdx.x;
 }
 
+// 2^(i/64) as float pairs for ffa::exp_ff (this translation unit's copy).
+__constant__ float2 c_exp2_gl[64];
+
+// Asynchronous global -> shared copies (cp.async); a source size of 0
+// writes zeros without reading.
+__device__ __forceinline__ void cp_async4(float* dst, const float* src, bool full) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(d), "l"(src), "r"(full ? 4 : 0)
+               : "memory");
+}
+
+__device__ __forceinline__ void cp_async16(float* dst, const float* src, bool full) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(d), "l"(src), "r"(full ? 16 : 0)
+               : "memory");
+}
+
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
 // FP64 vector -> float pairs in shared memory (all threads; ends with a barrier).
 __device__ __forceinline__ void load_pairs(const double* v, int n, float2* out) {
   for (int i = threadIdx.x; i < n; i += blockDim.x) out[i] = split2(v[i]);
@@ -70,7 +99,7 @@ __device__ __forceinline__ void load_pairs(const double* v, int n, float2* out) 
 // sum_m G[m][p] x[m] for one point: four independent compensated sums
 // (shells m = 0, 1, 2, 3 mod 4) merged in a fixed order, so the dependency
 // chains overlap.
-__device__ __forceinline__ double g_dot(const JobDev& J, int p, const float2* x) {
+__device__ __forceinline__ Dot2 g_dot2(const JobDev& J, int p, const float2* x) {
   Dot2 d0{0.f, 0.f}, d1{0.f, 0.f}, d2{0.f, 0.f}, d3{0.f, 0.f};
   const size_t N = J.npoint;
   const int M = J.nshell;
@@ -85,7 +114,11 @@ __device__ __forceinline__ double g_dot(const JobDev& J, int p, const float2* x)
   dot2_merge(d0, d1);
   dot2_merge(d2, d3);
   dot2_merge(d0, d2);
-  return dot2_value(d0);
+  return d0;
+}
+
+__device__ __forceinline__ double g_dot(const JobDev& J, int p, const float2* x) {
+  return dot2_value(g_dot2(J, p, x));
 }
 
 }  // namespace
@@ -98,6 +131,7 @@ __global__ void __launch_bounds__(kThreads) k_glisa_pro_ff(Batch bt) {
   __shared__ double out[2];
   int tile;
   const JobDev& J = decode_local_gf(bt, tile);
+  if (J.fuse) return;  // k_glisa_fused_ff<1>
   load_pairs(J.propars, J.nshell, cf);
   double acc[2] = {0.0, 0.0};
   for (int i = 0; i < J.ppt; ++i) {
@@ -130,6 +164,7 @@ __global__ void __launch_bounds__(kThreads) k_glisa_pro_ff(Batch bt) {
 __global__ void __launch_bounds__(kThreads) k_glisa_grad_ff(Batch bt, int use_hvec) {
   int tile;
   const JobDev& J = decode_local_gf(bt, tile);
+  if (J.fuse) return;  // k_glisa_fused_ff
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int p0 = tile * J.tile_points;
   const int p1 = min(p0 + J.tile_points, J.npoint);
@@ -169,14 +204,20 @@ __global__ void __launch_bounds__(kThreads) k_glisa_hv_ff(Batch bt) {
   __shared__ float2 df[kGffMaxShells];
   int local;
   const JobDev& J = decode_local_gf(bt, local);
+  if (J.fuse) return;  // k_glisa_fused_ff<0>
   load_pairs(J.delta, J.nshell, df);
   const int p = local * kThreads + threadIdx.x;
   if (p >= J.npoint) return;
   J.hvf[p] = split2(J.dvec2[p] * g_dot(J, p, df));
 }
 
-// Trial objective differences of the projected Newton step, as
-// k_glisa_trials with G^T delta as a compensated dot product.
+// Trial objective differences of the projected Newton step (the steps of
+// k_glisa_trials) on the FP32 pipes: u = G^T delta and the clipped-shell
+// corrections are compensated dot products (the clipped shells' c and delta
+// as float pairs from k_glisa_trial_set), rho0_t - rho0 = 2^-t u + corr_t is
+// a float-float sum, and the sick tests compare float-float values with the
+// cutoff's float pair. The relative change (rho0_t - rho0) / rho0 goes to
+// log1pf as before; only the points whose sick status differs take FP64 logs.
 __global__ void __launch_bounds__(kThreads) k_glisa_trials_ff(Batch bt) {
   __shared__ float2 df[kGffMaxShells];
   __shared__ double red[kWarps * kTrials];
@@ -188,40 +229,52 @@ __global__ void __launch_bounds__(kThreads) k_glisa_trials_ff(Batch bt) {
 #pragma unroll
   for (int t = 0; t < kTrials; ++t) ah[t] = al[t] = 0.0f;
   const int nclip = J.clip[J.nshell];
+  const int* tm = J.clip + J.nshell + 1;
+  const float4* cd = reinterpret_cast<const float4*>(J.clipf);
   const double cut = J.density_cutoff;
+  const float2 cutp = split2(cut);
   const size_t N = J.npoint;
   for (int i = 0; i < J.ppt; ++i) {
     const int p = point_in_tile(J, tile, i);
     if (p >= J.npoint) continue;
-    const double u = g_dot(J, p, df);
-    double corr[kTrials];
+    const f2 u = dot2_ff(g_dot2(J, p, df));
+    // corr_t = -sum_{m clipped at t} (c_m + 2^-t delta_m) g_m, running sums
+    // over the list sorted by t_m (largest first)
+    f2 corr[kTrials];
     {
-      double sc = 0.0, sd = 0.0;
+      Dot2 sc{0.f, 0.f}, sd{0.f, 0.f};
       int k = 0;
 #pragma unroll
       for (int t = kTrials - 1; t >= 0; --t) {
-        for (; k < nclip && J.clip[J.nshell + 1 + k] > t; ++k) {
+        for (; k < nclip && tm[k] > t; ++k) {
           const int m = J.clip[k];
-          const double g = (double)J.gmat32[m * N + p] + (double)J.gmat_lo[m * N + p];
-          sc += J.propars[m] * g;
-          sd += J.delta[m] * g;
+          const float gh = J.gmat32[m * N + p], gl = J.gmat_lo[m * N + p];
+          const float4 v = cd[k];
+          dot2_add(sc, gh, gl, v.x, v.y);
+          dot2_add(sd, gh, gl, v.z, v.w);
         }
-        corr[t] = -(sc + ldexp(1.0, -t) * sd);
+        const f2 d = dot2_ff(sd);
+        const float a = ldexpf(1.0f, -t);
+        corr[t] = ffa::neg(ffa::add(dot2_ff(sc), f2{a * d.hi, a * d.lo}));
       }
     }
     const double rho = J.rho[p], w = J.w[p], r0 = J.rho0[p];
-    const bool h0 = !(rho < cut || r0 < cut);
-    const double inv = h0 ? 1.0 / r0 : 0.0;
+    const bool rs = rho < cut;
+    const bool h0 = !(rs || r0 < cut);
+    const float2 r0p = split2(r0);
+    const float inv = h0 ? 1.0f / r0p.x : 0.0f;
     const float wr = (float)(w * rho);
 #pragma unroll
     for (int t = 0; t < kTrials; ++t) {
-      const double dr = ldexp(1.0, -t) * u + corr[t];
-      const double rt = r0 + dr;
-      const bool ht = !(rho < cut || rt < cut);
+      const float a = ldexpf(1.0f, -t);
+      const f2 dr = ffa::add(f2{a * u.hi, a * u.lo}, corr[t]);
+      const f2 rt = ffa::add(dr, f2{r0p.x, r0p.y});
+      const bool below = rt.hi < cutp.x || (rt.hi == cutp.x && rt.lo < cutp.y);
+      const bool ht = !(rs || below);
       double big = 0.0;
       float term = 0.0f;
-      if (h0 && ht) term = -wr * log1pf((float)(dr * inv));
-      else if (ht) big = w * rho * log(rho / rt);
+      if (h0 && ht) term = -wr * log1pf(dr.hi * inv);
+      else if (ht) big = w * rho * log(rho / ffa::to_double(rt));
       else if (h0) big = -(w * rho * log(rho / r0));
       if (big != 0.0) {
         const float bh = (float)big;
@@ -239,6 +292,212 @@ __global__ void __launch_bounds__(kThreads) k_glisa_trials_ff(Batch bt) {
   for (int t = 0; t < kTrials; ++t) acc[t] = (double)ah[t] + (double)al[t];
   block_sum<kTrials>(acc, red, out);
   if (threadIdx.x < kTrials) J.tpart[(size_t)threadIdx.x * J.ntile + tile] = out[threadIdx.x];
+}
+
+// ---------------------------------------------------------------------------
+// Fused passes: one read of G for a product G^T x and the row sums G v that
+// depend on it. The block streams its point tile through shared memory in
+// sub-tiles of kFuseSP points (both planes of all S shells, double-buffered
+// with cp.async); per sub-tile
+//   A  u(p) = sum_m G[m][p] x[m]: kFuseThreads / kFuseSP partial sums per
+//      point, merged in a fixed order;
+//   A' the per-point step, giving v(p) as a float pair;
+//   B  gpart[m] += sum_p G[m][p] v(p): warp w owns rows w, w + 16, ...; the
+//      lanes' compensated sums stay in registers across the tile and are
+//      reduced once at its end.
+// MODE 0 (refinement product): x = delta, v = (w rho / rho0^2) u.
+// MODE 1 (promolecule + gradient): x = c, u = rho0, the outputs of
+//   k_glisa_pro_ff with the ratios as float-float quotients and
+//   ln(rho / rho0) from logf plus one Newton step on exp_ff (error ~ the
+//   square of logf's), v = w rho / rho0.
+// Jobs with more than kFuseMaxShells shells use k_glisa_pro_ff /
+// k_glisa_hv_ff with k_glisa_grad_ff.
+// ---------------------------------------------------------------------------
+
+constexpr int kFuseThreads = 512;
+constexpr int kFuseWarps = kFuseThreads / 32;
+constexpr int kFuseSP = 64;                             // points per sub-tile
+constexpr int kFuseParts = kFuseThreads / kFuseSP;      // partial sums per point
+constexpr int kFuseRows = kFuseMaxShells / kFuseWarps;  // rows per warp
+
+// Shared memory of a fused pass for S shells (bytes).
+__host__ __device__ constexpr size_t fuse_smem_bytes(int S) {
+  return 4 * (size_t)S * kFuseSP * 4     // two stages of both planes
+         + 8 * (size_t)S                 // x as float pairs
+         + 8 * (size_t)kFuseParts * kFuseSP  // partial sums
+         + 8 * (size_t)kFuseSP           // v
+         + 512                           // exp table
+         + 8 * (2 * kFuseWarps + 2);     // block sums
+}
+
+// Sub-tile [q0, q0 + kFuseSP) of both planes into gh / gl ([S][kFuseSP]);
+// columns at or past p1 are zero-filled. vec: 16-byte copies (npoint % 4 == 0,
+// so every row segment starts 16-byte aligned and p1 is a multiple of 4).
+__device__ __forceinline__ void fuse_load(const JobDev& J, int q0, int p1, float* gh, float* gl,
+                                          bool vec) {
+  const int S = J.nshell;
+  const size_t N = J.npoint;
+  if (vec) {
+    constexpr int C = kFuseSP / 4;
+    for (int e = threadIdx.x; e < S * C; e += kFuseThreads) {
+      const int m = e / C, c = e - m * C;
+      const int p = q0 + 4 * c;
+      const bool in = p < p1;
+      const size_t off = (size_t)m * N + (in ? p : q0);
+      cp_async16(gh + m * kFuseSP + 4 * c, J.gmat32 + off, in);
+      cp_async16(gl + m * kFuseSP + 4 * c, J.gmat_lo + off, in);
+    }
+  } else {
+    for (int e = threadIdx.x; e < S * kFuseSP; e += kFuseThreads) {
+      const int m = e / kFuseSP, c = e - m * kFuseSP;
+      const int p = q0 + c;
+      const bool in = p < p1;
+      const size_t off = (size_t)m * N + (in ? p : q0);
+      cp_async4(gh + m * kFuseSP + c, J.gmat32 + off, in);
+      cp_async4(gl + m * kFuseSP + c, J.gmat_lo + off, in);
+    }
+  }
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(kFuseThreads, 1) k_glisa_fused_ff(Batch bt) {
+  extern __shared__ float4 fsm[];
+  int tile;
+  const JobDev& J = decode_local_gf(bt, tile);
+  if (!J.fuse) return;
+  const int S = J.nshell;
+  // stage k: high plane at stg + 2 k S kFuseSP, low plane S kFuseSP after it
+  float* stg = reinterpret_cast<float*>(fsm);
+  const int plane = S * kFuseSP;
+  float2* xv = reinterpret_cast<float2*>(stg + 4 * plane);
+  Dot2* part = reinterpret_cast<Dot2*>(xv + S);
+  float2* vs = reinterpret_cast<float2*>(part + kFuseParts * kFuseSP);
+  float2* tab = vs + kFuseSP;
+  double* red = reinterpret_cast<double*>(tab + 64);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int p0 = tile * J.tile_points;
+  const int p1 = min(p0 + J.tile_points, J.npoint);
+  const int nsub = (p1 - p0 + kFuseSP - 1) / kFuseSP;
+  const bool vec = (J.npoint & 3) == 0;
+  fuse_load(J, p0, p1, stg, stg + plane, vec);
+  cp_async_commit();
+  const double* x = MODE ? J.propars : J.delta;
+  for (int i = threadIdx.x; i < S; i += kFuseThreads) xv[i] = split2(x[i]);
+  if (MODE == 1 && threadIdx.x < 64) tab[threadIdx.x] = c_exp2_gl[threadIdx.x];
+  Dot2 acc[kFuseRows];
+#pragma unroll
+  for (int r = 0; r < kFuseRows; ++r) acc[r] = Dot2{0.f, 0.f};
+  f2 ent{0.f, 0.f};
+  float nneg = 0.0f;
+  for (int sub = 0; sub < nsub; ++sub) {
+    const float* gh = stg + (sub & 1) * 2 * plane;
+    const float* gl = gh + plane;
+    if (sub + 1 < nsub) {
+      float* nh = stg + ((sub + 1) & 1) * 2 * plane;
+      fuse_load(J, p0 + (sub + 1) * kFuseSP, p1, nh, nh + plane, vec);
+      cp_async_commit();
+      cp_async_wait<1>();
+    } else {
+      cp_async_wait<0>();
+    }
+    __syncthreads();
+    {  // A
+      const int pt = threadIdx.x % kFuseSP, q = threadIdx.x / kFuseSP;
+      Dot2 d{0.f, 0.f};
+      for (int m = q; m < S; m += kFuseParts)
+        dot2_add(d, gh[m * kFuseSP + pt], gl[m * kFuseSP + pt], xv[m].x, xv[m].y);
+      part[q * kFuseSP + pt] = d;
+    }
+    __syncthreads();
+    if (threadIdx.x < kFuseSP) {  // A'
+      Dot2 d = part[threadIdx.x];
+#pragma unroll
+      for (int q = 1; q < kFuseParts; ++q) dot2_merge(d, part[q * kFuseSP + threadIdx.x]);
+      const int p = p0 + sub * kFuseSP + threadIdx.x;
+      float2 v = make_float2(0.f, 0.f);
+      if (p < p1) {
+        if (MODE == 0) {
+          const float2 d2 = split2(J.dvec2[p]);
+          const f2 h = ffa::mul(dot2_ff(d), f2{d2.x, d2.y});
+          v = make_float2(h.hi, h.lo);
+        } else {
+          const f2 r0 = dot2_ff(d);
+          const double rho0 = ffa::to_double(r0);
+          const double rho = J.rho[p], w = J.w[p];
+          const bool sick = (rho < J.density_cutoff) || (rho0 < J.density_cutoff);
+          f2 d1{0.f, 0.f}, dd{0.f, 0.f};
+          const float2 wr = split2(w * rho);
+          if (!sick) {
+            d1 = ffa::div(f2{wr.x, wr.y}, r0);
+            dd = ffa::div(d1, r0);
+            const float2 rp = split2(rho);
+            const f2 ratio = ffa::div(f2{rp.x, rp.y}, r0);
+            const float l0 = logf(ratio.hi);
+            const f2 e = ffa::exp_ff(f2{-l0, 0.f}, tab);
+            const f2 l = ffa::add(ffa::add(ffa::mul(ratio, e), -1.0f), l0);
+            ent = ffa::add(ent, ffa::mul(f2{wr.x, wr.y}, l));
+          }
+          J.dvec1[p] = ffa::to_double(d1);
+          J.dvec2[p] = ffa::to_double(dd);
+          J.d1f[p] = make_float2(d1.hi, d1.lo);
+          J.rho0[p] = rho0;
+          J.hess_s[p] = sqrtf(dd.hi);
+          if (rho0 < J.negative_cutoff) nneg += 1.0f;
+          v = make_float2(d1.hi, d1.lo);
+        }
+      }
+      vs[threadIdx.x] = v;
+    }
+    __syncthreads();
+    {  // B
+      const float2 v0 = vs[lane], v1 = vs[lane + 32];
+#pragma unroll
+      for (int r = 0; r < kFuseRows; ++r) {
+        const int m = warp + kFuseWarps * r;
+        if (m < S) {
+          dot2_add(acc[r], gh[m * kFuseSP + lane], gl[m * kFuseSP + lane], v0.x, v0.y);
+          dot2_add(acc[r], gh[m * kFuseSP + lane + 32], gl[m * kFuseSP + lane + 32], v1.x, v1.y);
+        }
+      }
+    }
+    __syncthreads();  // this stage is refilled by the next sub-tile's copies
+  }
+#pragma unroll
+  for (int r = 0; r < kFuseRows; ++r) {
+    const int m = warp + kFuseWarps * r;
+    if (m < S) {  // warp-uniform
+      Dot2 d = acc[r];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const Dot2 b{__shfl_xor_sync(0xffffffffu, d.s, o), __shfl_xor_sync(0xffffffffu, d.c, o)};
+        dot2_merge(d, b);
+      }
+      if (lane == 0) J.gpart[(size_t)m * J.ntile + tile] = dot2_value(d);
+    }
+  }
+  if (MODE == 1) {
+    // entropy and negativity partials of the tile (threads >= kFuseSP hold zeros)
+    double e = ffa::to_double(ent), n = (double)nneg;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      e += __shfl_xor_sync(0xffffffffu, e, o);
+      n += __shfl_xor_sync(0xffffffffu, n, o);
+    }
+    if (lane == 0) {
+      red[2 * warp] = e;
+      red[2 * warp + 1] = n;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double se = 0.0, sn = 0.0;
+      for (int k = 0; k < kFuseWarps; ++k) {
+        se += red[2 * k];
+        sn += red[2 * k + 1];
+      }
+      J.jpart[(size_t)QJ_ENTROPY * J.ntile + tile] = se;
+      J.jpart[(size_t)QJ_NEG * J.ntile + tile] = sn;
+    }
+  }
 }
 
 // Outer change per (atom, tile): sum_p w (sum_{m in atom} (c - c_old)_m g_m)^2
@@ -291,6 +550,39 @@ void launch_glisa_grad_ff(const HostBatch& hb, cudaStream_t st) {
 void launch_glisa_hv_ff(const HostBatch& hb, cudaStream_t st) {
   HP_LAUNCH_GF(k_glisa_hv_ff, K_POINT1, kThreads);
   HP_LAUNCH_GF(k_glisa_grad_ff, K_POINT, kThreads, 1);
+}
+
+namespace {
+
+// 2^(i/64) as float pairs, from the host's double-precision exp2; once per device.
+void ensure_exp_table_gl() {
+  static int done_mask = 0;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 31 && (done_mask >> dev) & 1) return;
+  float2 t[64];
+  for (int i = 0; i < 64; ++i) {
+    const double v = exp2((double)i / 64.0);
+    const float hi = (float)v;
+    t[i] = make_float2(hi, (float)(v - (double)hi));
+  }
+  cudaMemcpyToSymbol(c_exp2_gl, t, sizeof(t));
+  cudaFuncSetAttribute(k_glisa_fused_ff<0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)fuse_smem_bytes(kFuseMaxShells));
+  cudaFuncSetAttribute(k_glisa_fused_ff<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)fuse_smem_bytes(kFuseMaxShells));
+  if (dev < 31) done_mask |= 1 << dev;
+}
+
+}  // namespace
+
+void launch_glisa_fused_ff(const HostBatch& hb, cudaStream_t st, int mode, int max_shells) {
+  if (hb.blocks[K_POINT] <= 0) return;
+  ensure_exp_table_gl();
+  const size_t smem = fuse_smem_bytes(max_shells);
+  if (mode) k_glisa_fused_ff<1><<<hb.blocks[K_POINT], kFuseThreads, smem, st>>>(hb.b[K_POINT]);
+  else k_glisa_fused_ff<0><<<hb.blocks[K_POINT], kFuseThreads, smem, st>>>(hb.b[K_POINT]);
+  ++g_launch_count;
 }
 
 void launch_glisa_trials_ff(const HostBatch& hb, cudaStream_t st) {

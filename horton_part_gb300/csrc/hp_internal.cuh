@@ -157,6 +157,7 @@ struct JobDev {
   float* gmat32;          // gLISA tensor-core Hessian: FP32 copy of gmat [nshell][npoint]
                           // (with gff: the high part of G = gmat32 + gmat_lo)
   float* gmat_lo;         // gLISA, gff: low part of G [nshell][npoint] (gmat is not stored)
+  float* clipf;           // gLISA, gff: clipped shells' (c hi, c lo, delta hi, delta lo) [nshell]
   float2* d1f;            // gLISA, gff: w rho / rho0 as float pairs, npoint
   float2* hvf;            // gLISA, gff: the refinement's hvec as float pairs, npoint
   float* hess_s;          // gLISA tensor-core Hessian: sqrt(w rho / rho0^2) as FP32, npoint
@@ -186,6 +187,7 @@ struct JobDev {
   int tile_points, htiles, tc, gff;              // htiles: 64-wide Hessian tiles per side;
                                                  // tc: gLISA Hessian on the tensor cores;
                                                  // gff: gLISA G passes in float-float
+  int fuse;                                      // gff with nshell <= kFuseMaxShells: fused passes
   double threshold, inner_threshold, density_cutoff, negative_cutoff, population_cutoff, tau;
 };
 
@@ -396,11 +398,18 @@ void launch_glisa_ls(const HostBatch& hb, cudaStream_t st, int first, int count)
 void launch_glisa_change(const HostBatch& hb, cudaStream_t st);
 void launch_glisa_check(const HostBatch& hb, cudaStream_t st);
 void launch_glisa_pnewton(const HostBatch& hb, cudaStream_t st, int gff);  // trials + Armijo pick
-void launch_glisa_refine(const HostBatch& hb, cudaStream_t st, int gff);
+// fuse_shells: largest shell count of the batch's fused jobs (0: none);
+// unfused: some job of the batch takes the separate passes
+void launch_glisa_refine(const HostBatch& hb, cudaStream_t st, int gff, int fuse_shells, int unfused);
 
 // gLISA passes over G in float-float (hp_glisa_ff.cu); shells per job at most
 // kGffMaxShells (their coefficients are staged in shared memory)
 constexpr int kGffMaxShells = 2048;
+// fused passes (one read of G for a product and the row sums that follow it):
+// two shared-memory stages of [S][64] float pairs
+constexpr int kFuseMaxShells = 192;
+void launch_glisa_fused_ff(const HostBatch& hb, cudaStream_t st, int mode, int max_shells);
+void launch_glisa_basis_ff(const HostBatch& hb, cudaStream_t st);
 void launch_glisa_pro_ff(const HostBatch& hb, cudaStream_t st);
 void launch_glisa_grad_ff(const HostBatch& hb, cudaStream_t st);
 void launch_glisa_hv_ff(const HostBatch& hb, cudaStream_t st);  // hvec and G hvec

@@ -1022,7 +1022,9 @@ template <typename T>
 __global__ void __launch_bounds__(kThreads) k_glisa_basis(Batch bt) {
   int tile;
   const JobDev& J = decode_local(bt, tile);
-  if (!J.gmat && !J.gmat_lo) return;  // jobs that recompute their shells keep no basis matrix
+  // jobs that recompute their shells keep no basis matrix; float-float planes
+  // without an FP64 copy are written by k_glisa_basis_ff
+  if (!J.gmat) return;
   for (int i = 0; i < J.ppt; ++i) {
     const int p = point_of(J, tile, i);
     if (p >= J.npoint) continue;
@@ -1035,7 +1037,6 @@ __global__ void __launch_bounds__(kThreads) k_glisa_basis(Batch bt) {
         if (J.gmat32) {
           const float hi = (float)g;
           J.gmat32[e] = hi;
-          if (J.gmat_lo) J.gmat_lo[e] = (float)(g - (double)hi);
         }
       }
     }
@@ -1282,10 +1283,92 @@ __device__ void chol_solve_block(const double* L, const double* dinv, int n, dou
   __syncthreads();
 }
 
+// chol_factor in FP32, for the factor of the tensor-core Hessian: that
+// matrix carries ~1e-7 relative error already, so an FP32 factor is as good a
+// preconditioner for the FP64-residual refinement as an FP64 one (same
+// direction error after each refinement step), at 1/64 of the FP64 cost per
+// operation on GB300. Same layout: factor in the lower triangle, its
+// transpose in the upper, dinv[k] = 1 / L[k][k]; colbuf: 2n floats.
+__device__ void chol_factor_f(float* L, int n, int* bad, float* colbuf, float* dinv) {
+  __shared__ float piv_f[2], rinv_f[2];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+  const float tiny = 1e-37f;
+  float* col = colbuf;
+  float* nxt = colbuf + n;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) col[i] = L[(size_t)i * n];
+  if (threadIdx.x == 0 && n > 0) {
+    const float a = L[0];
+    if (!(a > 0.0f)) *bad = 1;
+    piv_f[0] = sqrtf(fmaxf(a, tiny));
+    rinv_f[0] = 1.0f / fmaxf(a, tiny);
+  }
+  __syncthreads();
+  for (int k = 0; k < n; ++k) {
+    const float piv = piv_f[k & 1], rinv = rinv_f[k & 1];
+    const float ipiv = piv * rinv;
+    if (threadIdx.x == 0) {
+      L[(size_t)k * n + k] = piv;
+      dinv[k] = ipiv;
+    }
+    for (int i = k + 1 + warp; i < n; i += nwarp) {
+      const float ci = col[i];
+      const float li = ci * rinv;
+      float* row = L + (size_t)i * n;
+      for (int j = k + 1 + lane; j <= i; j += 32) {
+        const float v = fmaf(-li, col[j], row[j]);
+        row[j] = v;
+        if (j == k + 1) {
+          nxt[i] = v;
+          if (i == k + 1) {
+            if (!(v > 0.0f)) *bad = 1;
+            piv_f[(k + 1) & 1] = sqrtf(fmaxf(v, tiny));
+            rinv_f[(k + 1) & 1] = 1.0f / fmaxf(v, tiny);
+          }
+        }
+      }
+      if (lane == 0) {
+        const float lik = ci * ipiv;
+        row[k] = lik;
+        L[(size_t)k * n + i] = lik;
+      }
+    }
+    __syncthreads();
+    float* t = col;
+    col = nxt;
+    nxt = t;
+  }
+}
+
+// y <- (L L^T)^-1 y by one warp, everything in shared memory (L as left by
+// chol_factor_f): forward with the columns of L (contiguous in the upper
+// copy), backward with its rows; one warp barrier per column.
+__device__ void chol_solve_warp_f(const float* L, const float* dinv, int n, float* y) {
+  const int lane = threadIdx.x & 31;
+  for (int j = 0; j < n; ++j) {
+    const float zj = y[j] * dinv[j];
+    const float* col = L + (size_t)j * n;  // L[i][j] = col[i], i > j
+    for (int i = j + 1 + lane; i < n; i += 32) y[i] = fmaf(-col[i], zj, y[i]);
+    __syncwarp();
+    if (lane == 0) y[j] = zj;
+    __syncwarp();
+  }
+  for (int j = n - 1; j >= 0; --j) {
+    const float xj = y[j] * dinv[j];
+    const float* row = L + (size_t)j * n;  // L[j][i], i < j
+    for (int i = lane; i < j; i += 32) y[i] = fmaf(-row[i], xj, y[i]);
+    __syncwarp();
+    if (lane == 0) y[j] = xj;
+    __syncwarp();
+  }
+}
+
 // Shared memory of the Newton step: the factor (dynamic, when |F|^2 doubles
 // fit in kNewtonSmemL) and the two column buffers (when |F| <= kNewtonColMax).
 constexpr int kNewtonSmemL = 200 * 1024;
 constexpr int kNewtonColMax = 256;
+// FP32 factor in shared memory (factor, 1 / diagonal and the right-hand side)
+constexpr int kNewtonF32Max = 224;
+static_assert(4 * (kNewtonF32Max * kNewtonF32Max + 2 * kNewtonF32Max) <= kNewtonSmemL, "FP32 factor");
 
 __global__ void __launch_bounds__(kThreads) k_glisa_newton_step(Batch bt, int projected) {
   extern __shared__ double l_smem[];
@@ -1306,6 +1389,37 @@ __global__ void __launch_bounds__(kThreads) k_glisa_newton_step(Batch bt, int pr
   }
   __syncthreads();
   const int nf = nf_s;
+  if (J.tc && nf <= kNewtonF32Max) {
+    // tensor-core Hessian: FP32 factor and solve in shared memory; the factor
+    // (with 1 / diagonal after it) is kept in chol for the refinement steps,
+    // freeidx[nshell + 1] = 1 marks it as FP32
+    float* Lf = reinterpret_cast<float*>(l_smem);
+    float* dv = Lf + nf * nf;
+    float* yv = dv + nf;
+    for (int e = threadIdx.x; e < nf * nf; e += kThreads) {
+      const int i = e / nf, j = e - i * nf;
+      Lf[e] = (float)J.hess[(size_t)J.freeidx[i] * M + J.freeidx[j]];
+    }
+    for (int m = threadIdx.x; m < M; m += kThreads) J.delta[m] = 0.0;
+    __syncthreads();
+    chol_factor_f(Lf, nf, &bad, reinterpret_cast<float*>(col_smem), dv);
+    if (!bad) {
+      for (int i = threadIdx.x; i < nf; i += kThreads) yv[i] = (float)(-(1.0 + J.grad[J.freeidx[i]]));
+      __syncthreads();
+      if (threadIdx.x < 32) chol_solve_warp_f(Lf, dv, nf, yv);
+      __syncthreads();
+      for (int i = threadIdx.x; i < nf; i += kThreads) J.delta[J.freeidx[i]] = (double)yv[i];
+      float* keep = reinterpret_cast<float*>(J.chol);
+      for (int e = threadIdx.x; e < nf * nf + nf; e += kThreads) keep[e] = Lf[e];
+      if (threadIdx.x == 0) J.freeidx[M + 1] = 1;
+      return;
+    }
+    // not positive definite in FP32: the FP64 factor below decides
+    __syncthreads();
+    if (threadIdx.x == 0) bad = 0;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) J.freeidx[M + 1] = 0;
   const bool l_in_smem = (size_t)nf * nf * sizeof(double) <= (size_t)kNewtonSmemL;
   double* L = l_in_smem ? l_smem : J.chol;
   for (int e = threadIdx.x; e < nf * nf; e += kThreads) {
@@ -1347,10 +1461,12 @@ __global__ void __launch_bounds__(kThreads) k_glisa_hv(Batch bt) {
 // r = (-1 - df)_F - (H delta)_F with the exact FP64 product, then
 // delta_F += (L L^T)^-1 r with the factor of the (tensor-core) Hessian.
 __global__ void __launch_bounds__(kThreads) k_glisa_refine(Batch bt) {
+  extern __shared__ double l_smem[];
   int local;
   const JobDev& J = decode_local(bt, local);
   const int M = J.nshell;
   const int nf = J.freeidx[M];
+  const bool f32 = J.freeidx[M + 1] != 0;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   double* r = J.keep;
   for (int i = warp; i < nf; i += kWarps) {  // one warp per row, lanes over tiles
@@ -1362,6 +1478,18 @@ __global__ void __launch_bounds__(kThreads) k_glisa_refine(Batch bt) {
     if (lane == 0) r[i] = -(1.0 + J.grad[m]) - hd;
   }
   __syncthreads();
+  if (f32) {  // FP32 factor of k_glisa_newton_step: copy it in, one warp solves
+    float* Lf = reinterpret_cast<float*>(l_smem);
+    float* yv = Lf + nf * nf + nf;
+    const float* keep = reinterpret_cast<const float*>(J.chol);
+    for (int e = threadIdx.x; e < nf * nf + nf; e += kThreads) Lf[e] = keep[e];
+    for (int i = threadIdx.x; i < nf; i += kThreads) yv[i] = (float)r[i];
+    __syncthreads();
+    if (threadIdx.x < 32) chol_solve_warp_f(Lf, Lf + nf * nf, nf, yv);
+    __syncthreads();
+    for (int i = threadIdx.x; i < nf; i += kThreads) J.delta[J.freeidx[i]] += (double)yv[i];
+    return;
+  }
   chol_solve_block(J.chol, J.ctrial + 2 * M, nf, r);
   for (int i = threadIdx.x; i < nf; i += kThreads) J.delta[J.freeidx[i]] += r[i];
 }
@@ -1397,6 +1525,19 @@ __global__ void __launch_bounds__(kThreads) k_glisa_trial_set(Batch bt) {
       tm[k] = t;
     }
     J.clip[M] = n;
+  }
+  if (J.clipf) {  // float pairs (c hi, c lo, delta hi, delta lo) of the clipped shells
+    __syncthreads();
+    const int n = J.clip[M];
+    for (int k = threadIdx.x; k < n; k += kThreads) {
+      const int m = J.clip[k];
+      const double c = J.propars[m], d = J.delta[m];
+      const float ch = (float)c, dh = (float)d;
+      J.clipf[4 * k] = ch;
+      J.clipf[4 * k + 1] = (float)(c - (double)ch);
+      J.clipf[4 * k + 2] = dh;
+      J.clipf[4 * k + 3] = (float)(d - (double)dh);
+    }
   }
 }
 
@@ -1780,6 +1921,8 @@ void launch_glisa_solve(const HostBatch& hb, cudaStream_t st, int projected) {
   if (configured_device != dev) {
     cudaFuncSetAttribute(k_glisa_newton_step, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          kNewtonSmemL);
+    cudaFuncSetAttribute(k_glisa_refine, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         kNewtonSmemL);
     configured_device = dev;
   }
   if (hb.blocks[K_JOB] > 0) {
@@ -1788,14 +1931,18 @@ void launch_glisa_solve(const HostBatch& hb, cudaStream_t st, int projected) {
   }
 }
 
-void launch_glisa_refine(const HostBatch& hb, cudaStream_t st, int gff) {
+void launch_glisa_refine(const HostBatch& hb, cudaStream_t st, int gff, int fuse_shells, int unfused) {
   if (gff) {
-    launch_glisa_hv_ff(hb, st);
+    if (fuse_shells > 0) launch_glisa_fused_ff(hb, st, 0, fuse_shells);
+    if (unfused) launch_glisa_hv_ff(hb, st);
   } else {
     HP_LAUNCH(k_glisa_hv, K_POINT1, kThreads);
     HP_LAUNCH(k_glisa_grad, K_POINT, kThreads, 1);
   }
-  HP_LAUNCH(k_glisa_refine, K_JOB, kThreads);
+  if (hb.blocks[K_JOB] > 0) {  // dynamic shared memory: the FP32 factor (set up by launch_glisa_solve)
+    k_glisa_refine<<<hb.blocks[K_JOB], kThreads, kNewtonSmemL, st>>>(hb.b[K_JOB]);
+    ++g_launch_count;
+  }
 }
 
 void launch_glisa_apply(const HostBatch& hb, cudaStream_t st, int mode) {

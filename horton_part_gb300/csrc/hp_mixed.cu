@@ -232,7 +232,9 @@ __global__ void __launch_bounds__(kThreads) k_change_mx(Batch bt) {
 
 constexpr int kMxMbisQ = 2 * 7 + 1;
 
-__global__ void __launch_bounds__(kThreads) k_mbis_inner_mx(Batch bt) {
+// At most 64 registers: four blocks (32 warps) per SM to hide the latency of
+// the rho_a and coordinate loads.
+__global__ void __launch_bounds__(kThreads, 4) k_mbis_inner_mx(Batch bt) {
   __shared__ float2 red[kWarps * kMxMbisQ];
   __shared__ float2 out[kMxMbisQ];
   int a, tile;

@@ -102,7 +102,7 @@ namespace {
 //   MIXED_NEAR: the change is within kNearFactor x the threshold.
 enum MixedState { MIXED_GO = 0, MIXED_NEAR = 1, MIXED_FLOOR = 2 };
 constexpr size_t kFloorWindow = 8;
-constexpr double kNearFactor = 10.0;
+constexpr double kNearFactor = 100.0;
 
 int mixed_state(const hp_job* j) {
   const size_t n = j->changes.size();
@@ -264,9 +264,13 @@ int run_inner(hp_ctx* ctx, const std::vector<hp_job*>& jobs, const HostBatch& hb
 
 int job_init(hp_ctx* ctx, const std::vector<hp_job*>& jobs, const HostBatch& hb) {
   launch_nelec(hb, ctx->stream);
-  bool any_basis = false;
-  for (hp_job* j : jobs) any_basis |= j->dev.gmat != nullptr || j->dev.gmat_lo != nullptr;
+  bool any_basis = false, any_basis_ff = false;
+  for (hp_job* j : jobs) {
+    any_basis |= j->dev.gmat != nullptr;
+    any_basis_ff |= j->dev.gmat_lo != nullptr;
+  }
   if (any_basis) launch_glisa_basis(hb, ctx->stream);
+  if (any_basis_ff) launch_glisa_basis_ff(hb, ctx->stream);
   for (hp_job* j : jobs) j->initialized = true;
   return check_launch();
 }
@@ -373,8 +377,11 @@ int step_iterstock(hp_ctx* ctx, const std::vector<hp_job*>& jobs, const HostBatc
 }
 
 // Refinement steps per Newton iteration when the Hessian comes from the
-// tensor cores (each: one FP64 H delta product, two passes over G).
-constexpr int kRefineSteps = 2;
+// tensor cores (each: one exact H delta product, one fused pass over G).
+// The factor of the tensor-core Hessian leaves a relative direction error
+// of ~1e-6; one step brings it to ~1e-12, far below what the outer
+// iteration notices (same iteration counts as the FP64 Hessian).
+constexpr int kRefineSteps = 1;
 
 // One gLISA solver iteration (glisa.py:748-798 for Newton, 805-848 for SC).
 int step_glisa(hp_ctx* ctx, const std::vector<hp_job*>& jobs, const HostBatch& hb) {
@@ -383,12 +390,23 @@ int step_glisa(hp_ctx* ctx, const std::vector<hp_job*>& jobs, const HostBatch& h
   launch_copy_old(hb, st);
   const bool tc = jobs[0]->dev.tc != 0;
   const int gff = jobs[0]->dev.gff;
-  {
-    ProfScope ps(ctx, HP_KERNEL_GLISA_PRO);
-    if (gff) launch_glisa_pro_ff(hb, st);
-    else launch_glisa_pro(hb, st);
+  // fused promolecule + gradient (and refinement) passes for jobs with at
+  // most kFuseMaxShells shells, separate passes for the others
+  int fuse_shells = 0, unfused = 0;
+  for (hp_job* j : jobs) {
+    if (j->dev.fuse) fuse_shells = std::max(fuse_shells, j->dev.nshell);
+    else unfused = 1;
   }
   {
+    ProfScope ps(ctx, HP_KERNEL_GLISA_PRO);
+    if (gff) {
+      if (fuse_shells > 0) launch_glisa_fused_ff(hb, st, 1, fuse_shells);
+      if (unfused) launch_glisa_pro_ff(hb, st);
+    } else {
+      launch_glisa_pro(hb, st);
+    }
+  }
+  if (!gff || unfused) {
     ProfScope ps(ctx, HP_KERNEL_GLISA_GRAD);
     if (gff) launch_glisa_grad_ff(hb, st);
     else launch_glisa_grad(hb, st);
@@ -408,7 +426,7 @@ int step_glisa(hp_ctx* ctx, const std::vector<hp_job*>& jobs, const HostBatch& h
       // iterative refinement against the exact FP64 product H delta.
       launch_glisa_solve(hb, st, solver == SOLVER_PNEWTON ? 1 : 0);
       if (tc)
-        for (int k = 0; k < kRefineSteps; ++k) launch_glisa_refine(hb, st, gff);
+        for (int k = 0; k < kRefineSteps; ++k) launch_glisa_refine(hb, st, gff, fuse_shells, unfused);
     }
     if (solver == SOLVER_PNEWTON) {
       launch_glisa_pnewton(hb, st, gff);
@@ -735,6 +753,11 @@ int32_t hp_job_create(hp_ctx* ctx, const hp_job_desc* d, hp_job** out) {
   // FP32 / float-float buffers (mixed precision and ff)
   const bool mixed = d->precision != HP_PRECISION_FP64 && !glisa;
   const bool tc = d->precision == HP_PRECISION_MIXED && glisa;
+  // gLISA with the tensor-core Hessian (Newton or projected Newton): G as
+  // float-float planes, no FP64 copy
+  const bool gff = tc && solver != HP_SOLVER_M_NEWTON && S <= kGffMaxShells;
+  // float hi/lo coordinates: FP32 / float-float evaluation and the FF basis
+  const bool hilo = mixed || gff;
   const int htiles = glisa ? (S + kHessTile - 1) / kHessTile : 0;
   const int npair = htiles * (htiles + 1) / 2;
   int nsplit = glisa ? std::max(1, std::min(1024, (4 * 152 + npair - 1) / std::max(1, npair))) : 0;
@@ -755,14 +778,17 @@ int32_t hp_job_create(hp_ctx* ctx, const hp_job_desc* d, hp_job** out) {
   auto add = [&](void* dst, size_t bytes) { parts.push_back({(void**)dst, bytes}); };
   add(&J.px, 8 * (size_t)N); add(&J.py, 8 * (size_t)N); add(&J.pz, 8 * (size_t)N);
   add(&J.w, 8 * (size_t)N); add(&J.rho, 8 * (size_t)N);
-  if (mixed) {
+  if (hilo) {
     add(&J.pxh, 4 * (size_t)N); add(&J.pxl, 4 * (size_t)N);
     add(&J.pyh, 4 * (size_t)N); add(&J.pyl, 4 * (size_t)N);
     add(&J.pzh, 4 * (size_t)N); add(&J.pzl, 4 * (size_t)N);
+    add(&J.atf, 4 * 6 * (size_t)A);
+    add(&J.fpar, 4 * 4 * (size_t)S);
+  }
+  if (mixed) {
     add(&J.wf, 4 * (size_t)N); add(&J.rhof, 4 * (size_t)N); add(&J.promolf, 4 * (size_t)N);
     add(&J.wl, 4 * (size_t)N); add(&J.rhol, 4 * (size_t)N);
-    add(&J.shf, 4 * 3 * (size_t)S); add(&J.fpar, 4 * 4 * (size_t)S);
-    add(&J.atf, 4 * 6 * (size_t)A);
+    add(&J.shf, 4 * 3 * (size_t)S);
     add(&J.fco, 4 * 8 * (size_t)S);
   }
   // GISA: per-atom QP matrices, precomputed once (they depend only on exponents)
@@ -798,9 +824,6 @@ int32_t hp_job_create(hp_ctx* ctx, const hp_job_desc* d, hp_job** out) {
   const size_t gbytes = 8 * (size_t)S * N;
   const size_t room = ctx->budget > ctx->used ? ctx->budget - ctx->used : 0;
   if (!glisa && !mbis && !mixed && gbytes <= room / 2) add(&J.gmat, gbytes);
-  // gLISA with the tensor-core Hessian (Newton or projected Newton): G as
-  // float-float planes, no FP64 copy
-  const bool gff = tc && solver != HP_SOLVER_M_NEWTON && S <= kGffMaxShells;
   if (glisa) {
     if (!gff) add(&J.gmat, 8 * (size_t)S * N);
     add(&J.gpart, 8 * (size_t)S * ntile);
@@ -811,7 +834,7 @@ int32_t hp_job_create(hp_ctx* ctx, const hp_job_desc* d, hp_job** out) {
     add(&J.dvec1, 8 * (size_t)N); add(&J.dvec2, 8 * (size_t)N);
     add(&J.ctrial, 8 * (size_t)kTrials * S);
     add(&J.tpart, 8 * (size_t)kTrials * ntile);
-    add(&J.freeidx, 4 * (size_t)(S + 1));
+    add(&J.freeidx, 4 * (size_t)(S + 2));
     add(&J.clip, 4 * (size_t)(2 * S + 1));
     add(&J.rho0, 8 * (size_t)N);
     if (tc) {
@@ -819,6 +842,7 @@ int32_t hp_job_create(hp_ctx* ctx, const hp_job_desc* d, hp_job** out) {
       add(&J.hess_s, 4 * (size_t)N);
       if (gff) {
         add(&J.gmat_lo, 4 * (size_t)S * N);
+        add(&J.clipf, 4 * 4 * (size_t)S);
         add(&J.d1f, 8 * (size_t)N);
         add(&J.hvf, 8 * (size_t)N);
       } else {
@@ -863,6 +887,7 @@ int32_t hp_job_create(hp_ctx* ctx, const hp_job_desc* d, hp_job** out) {
   J.nsplit = nsplit; J.ppt = ppt; J.tile_points = tile_points; J.htiles = htiles;
   J.tc = tc ? 1 : 0;
   J.gff = gff ? 1 : 0;
+  J.fuse = gff && S <= kFuseMaxShells ? 1 : 0;
   J.local = local ? 1 : 0;
   J.nrad = nrad;
   J.threshold = d->threshold;
@@ -890,7 +915,7 @@ int32_t hp_job_create(hp_ctx* ctx, const hp_job_desc* d, hp_job** out) {
     for (int p = 0; p < N; ++p) buf[p] = d->points[(size_t)3 * p + c];
     const double* dst = c == 0 ? J.px : c == 1 ? J.py : J.pz;
     ok &= up(dst, buf.data(), 8 * (size_t)N) == cudaSuccess;
-    if (mixed) {
+    if (hilo) {
       std::vector<float> hi((size_t)N), lo((size_t)N);
       for (int p = 0; p < N; ++p) {
         hi[p] = (float)buf[p];
@@ -935,7 +960,7 @@ int32_t hp_job_create(hp_ctx* ctx, const hp_job_desc* d, hp_job** out) {
   }
   ok &= up(J.zpseudo, d->pseudo_numbers, 8 * (size_t)A) == cudaSuccess;
   std::vector<float> atf32;
-  if (mixed) {
+  if (hilo) {
     atf32.resize(6 * (size_t)A);
     for (int a = 0; a < A; ++a)
       for (int c = 0; c < 3; ++c) {
@@ -992,6 +1017,17 @@ int32_t hp_job_create(hp_ctx* ctx, const hp_job_desc* d, hp_job** out) {
       shf32[3 * s + 2] = (float)pref[s];
     }
     ok &= up(J.shf, shf32.data(), 4 * 3 * (size_t)S) == cudaSuccess;
+  }
+  std::vector<float> fpar32;
+  if (gff) {  // (pref hi, pref lo, alpha hi, alpha lo) per shell for the FF basis
+    fpar32.resize(4 * (size_t)S);
+    for (int s = 0; s < S; ++s) {
+      fpar32[4 * s] = (float)pref[s];
+      fpar32[4 * s + 1] = (float)(pref[s] - (double)fpar32[4 * s]);
+      fpar32[4 * s + 2] = (float)alp[s];
+      fpar32[4 * s + 3] = (float)(alp[s] - (double)fpar32[4 * s + 2]);
+    }
+    ok &= up(J.fpar, fpar32.data(), 4 * 4 * (size_t)S) == cudaSuccess;
   }
   ok &= up(J.propars, d->initial_propars, 8 * (size_t)P) == cudaSuccess;
   ok &= up(J.propars_init, d->initial_propars, 8 * (size_t)P) == cudaSuccess;

@@ -211,20 +211,32 @@ __global__ void __launch_bounds__(kThreads) k_glisa_hv_ff(Batch bt) {
   J.hvf[p] = split2(J.dvec2[p] * g_dot(J, p, df));
 }
 
+// u = G^T delta per point as a normalised float pair (in hvf, free after the
+// refinement), for the trial promolecules; a light kernel at full occupancy
+// so that this pass over G streams at the memory rate.
+__global__ void __launch_bounds__(kThreads) k_glisa_u_ff(Batch bt) {
+  __shared__ float2 df[kGffMaxShells];
+  int local;
+  const JobDev& J = decode_local_gf(bt, local);
+  load_pairs(J.delta, J.nshell, df);
+  const int p = local * kThreads + threadIdx.x;
+  if (p >= J.npoint) return;
+  const f2 u = dot2_ff(g_dot2(J, p, df));
+  J.hvf[p] = make_float2(u.hi, u.lo);
+}
+
 // Trial objective differences of the projected Newton step (the steps of
-// k_glisa_trials) on the FP32 pipes: u = G^T delta and the clipped-shell
+// k_glisa_trials) on the FP32 pipes: u = G^T delta (k_glisa_u_ff) and the clipped-shell
 // corrections are compensated dot products (the clipped shells' c and delta
 // as float pairs from k_glisa_trial_set), rho0_t - rho0 = 2^-t u + corr_t is
 // a float-float sum, and the sick tests compare float-float values with the
 // cutoff's float pair. The relative change (rho0_t - rho0) / rho0 goes to
 // log1pf as before; only the points whose sick status differs take FP64 logs.
 __global__ void __launch_bounds__(kThreads) k_glisa_trials_ff(Batch bt) {
-  __shared__ float2 df[kGffMaxShells];
   __shared__ double red[kWarps * kTrials];
   __shared__ double out[kTrials];
   int tile;
   const JobDev& J = decode_local_gf(bt, tile);
-  load_pairs(J.delta, J.nshell, df);
   float ah[kTrials], al[kTrials];
 #pragma unroll
   for (int t = 0; t < kTrials; ++t) ah[t] = al[t] = 0.0f;
@@ -237,7 +249,8 @@ __global__ void __launch_bounds__(kThreads) k_glisa_trials_ff(Batch bt) {
   for (int i = 0; i < J.ppt; ++i) {
     const int p = point_in_tile(J, tile, i);
     if (p >= J.npoint) continue;
-    const f2 u = dot2_ff(g_dot2(J, p, df));
+    const float2 up = J.hvf[p];
+    const f2 u{up.x, up.y};
     // corr_t = -sum_{m clipped at t} (c_m + 2^-t delta_m) g_m, running sums
     // over the list sorted by t_m (largest first)
     f2 corr[kTrials];
@@ -296,38 +309,40 @@ __global__ void __launch_bounds__(kThreads) k_glisa_trials_ff(Batch bt) {
 
 // ---------------------------------------------------------------------------
 // Fused passes: one read of G for a product G^T x and the row sums G v that
-// depend on it. The block streams its point tile through shared memory in
-// sub-tiles of kFuseSP points (both planes of all S shells, double-buffered
-// with cp.async); per sub-tile
-//   A  u(p) = sum_m G[m][p] x[m]: kFuseThreads / kFuseSP partial sums per
-//      point, merged in a fixed order;
-//   A' the per-point step, giving v(p) as a float pair;
-//   B  gpart[m] += sum_p G[m][p] v(p): warp w owns rows w, w + 16, ...; the
+// depend on it. A block (256 threads, two per SM) streams its point tile
+// through shared memory in sub-tiles of kFuseSP = 32 points (both planes of
+// all S shells, double-buffered with cp.async); per sub-tile
+//   A  u(p) = sum_m G[m][p] x[m]: warp w sums the shells m = w (mod 8) for
+//      the 32 points (lane = point), two chains per lane;
+//   A' warp 0 merges the eight partial sums in a fixed order and forms the
+//      per-point v(p) as a float pair;
+//   B  gpart[m] += sum_p G[m][p] v(p): warp w owns rows w, w + 8, ...; the
 //      lanes' compensated sums stay in registers across the tile and are
 //      reduced once at its end.
 // MODE 0 (refinement product): x = delta, v = (w rho / rho0^2) u.
 // MODE 1 (promolecule + gradient): x = c, u = rho0, the outputs of
-//   k_glisa_pro_ff with the ratios as float-float quotients and
-//   ln(rho / rho0) from logf plus one Newton step on exp_ff (error ~ the
-//   square of logf's), v = w rho / rho0.
+//   k_glisa_pro_ff with the quotients in float-float, v = w rho / rho0; the
+//   entropy terms w rho ln(rho / rho0) are formed every 256 points by all
+//   threads (one point each) with ln from logf plus one Newton step on
+//   exp_ff (error ~ the square of logf's).
 // Jobs with more than kFuseMaxShells shells use k_glisa_pro_ff /
 // k_glisa_hv_ff with k_glisa_grad_ff.
 // ---------------------------------------------------------------------------
 
-constexpr int kFuseThreads = 512;
+constexpr int kFuseThreads = 256;
 constexpr int kFuseWarps = kFuseThreads / 32;
-constexpr int kFuseSP = 64;                             // points per sub-tile
-constexpr int kFuseParts = kFuseThreads / kFuseSP;      // partial sums per point
-constexpr int kFuseRows = kFuseMaxShells / kFuseWarps;  // rows per warp
+constexpr int kFuseSP = 32;                             // points per sub-tile (one per lane)
+constexpr int kFuseRows = kFuseMaxShells / kFuseWarps;  // rows per warp in B
+constexpr int kFuseGroup = kFuseThreads / kFuseSP;      // sub-tiles per entropy pass
 
 // Shared memory of a fused pass for S shells (bytes).
 __host__ __device__ constexpr size_t fuse_smem_bytes(int S) {
-  return 4 * (size_t)S * kFuseSP * 4     // two stages of both planes
-         + 8 * (size_t)S                 // x as float pairs
-         + 8 * (size_t)kFuseParts * kFuseSP  // partial sums
-         + 8 * (size_t)kFuseSP           // v
-         + 512                           // exp table
-         + 8 * (2 * kFuseWarps + 2);     // block sums
+  return 4 * (size_t)S * kFuseSP * 4          // two stages of both planes
+         + 8 * (size_t)S                      // x as float pairs
+         + 8 * (size_t)kFuseWarps * kFuseSP   // partial sums
+         + 8 * (size_t)kFuseSP                // v
+         + 512                                // exp table
+         + 8 * (2 * kFuseWarps + 2);          // block sums
 }
 
 // Sub-tile [q0, q0 + kFuseSP) of both planes into gh / gl ([S][kFuseSP]);
@@ -338,21 +353,23 @@ __device__ __forceinline__ void fuse_load(const JobDev& J, int q0, int p1, float
   const int S = J.nshell;
   const size_t N = J.npoint;
   if (vec) {
-    constexpr int C = kFuseSP / 4;
-    for (int e = threadIdx.x; e < S * C; e += kFuseThreads) {
-      const int m = e / C, c = e - m * C;
-      const int p = q0 + 4 * c;
-      const bool in = p < p1;
-      const size_t off = (size_t)m * N + (in ? p : q0);
+    constexpr int C = kFuseSP / 4;  // 16-byte chunks per row
+    const int c = threadIdx.x % C;
+    const int p = q0 + 4 * c;
+    const bool in = p < p1;
+    const int pc = in ? p : q0;
+    for (int m = threadIdx.x / C; m < S; m += kFuseThreads / C) {
+      const size_t off = (size_t)m * N + pc;
       cp_async16(gh + m * kFuseSP + 4 * c, J.gmat32 + off, in);
       cp_async16(gl + m * kFuseSP + 4 * c, J.gmat_lo + off, in);
     }
   } else {
-    for (int e = threadIdx.x; e < S * kFuseSP; e += kFuseThreads) {
-      const int m = e / kFuseSP, c = e - m * kFuseSP;
-      const int p = q0 + c;
-      const bool in = p < p1;
-      const size_t off = (size_t)m * N + (in ? p : q0);
+    const int c = threadIdx.x % kFuseSP;
+    const int p = q0 + c;
+    const bool in = p < p1;
+    const int pc = in ? p : q0;
+    for (int m = threadIdx.x / kFuseSP; m < S; m += kFuseThreads / kFuseSP) {
+      const size_t off = (size_t)m * N + pc;
       cp_async4(gh + m * kFuseSP + c, J.gmat32 + off, in);
       cp_async4(gl + m * kFuseSP + c, J.gmat_lo + off, in);
     }
@@ -360,7 +377,7 @@ __device__ __forceinline__ void fuse_load(const JobDev& J, int q0, int p1, float
 }
 
 template <int MODE>
-__global__ void __launch_bounds__(kFuseThreads, 1) k_glisa_fused_ff(Batch bt) {
+__global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_fused_ff(Batch bt) {
   extern __shared__ float4 fsm[];
   int tile;
   const JobDev& J = decode_local_gf(bt, tile);
@@ -371,7 +388,7 @@ __global__ void __launch_bounds__(kFuseThreads, 1) k_glisa_fused_ff(Batch bt) {
   const int plane = S * kFuseSP;
   float2* xv = reinterpret_cast<float2*>(stg + 4 * plane);
   Dot2* part = reinterpret_cast<Dot2*>(xv + S);
-  float2* vs = reinterpret_cast<float2*>(part + kFuseParts * kFuseSP);
+  float2* vs = reinterpret_cast<float2*>(part + kFuseWarps * kFuseSP);
   float2* tab = vs + kFuseSP;
   double* red = reinterpret_cast<double*>(tab + 64);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -392,28 +409,31 @@ __global__ void __launch_bounds__(kFuseThreads, 1) k_glisa_fused_ff(Batch bt) {
   for (int sub = 0; sub < nsub; ++sub) {
     const float* gh = stg + (sub & 1) * 2 * plane;
     const float* gl = gh + plane;
+    cp_async_wait<0>();
+    __syncthreads();  // sub-tile sub visible; every thread is done with sub - 1
     if (sub + 1 < nsub) {
-      float* nh = stg + ((sub + 1) & 1) * 2 * plane;
+      float* nh = stg + ((sub + 1) & 1) * 2 * plane;  // last read in B of sub - 1
       fuse_load(J, p0 + (sub + 1) * kFuseSP, p1, nh, nh + plane, vec);
       cp_async_commit();
-      cp_async_wait<1>();
-    } else {
-      cp_async_wait<0>();
     }
-    __syncthreads();
     {  // A
-      const int pt = threadIdx.x % kFuseSP, q = threadIdx.x / kFuseSP;
-      Dot2 d{0.f, 0.f};
-      for (int m = q; m < S; m += kFuseParts)
-        dot2_add(d, gh[m * kFuseSP + pt], gl[m * kFuseSP + pt], xv[m].x, xv[m].y);
-      part[q * kFuseSP + pt] = d;
+      Dot2 d{0.f, 0.f}, e{0.f, 0.f};
+      int m = warp;
+      for (; m + kFuseWarps < S; m += 2 * kFuseWarps) {
+        dot2_add(d, gh[m * kFuseSP + lane], gl[m * kFuseSP + lane], xv[m].x, xv[m].y);
+        const int m2 = m + kFuseWarps;
+        dot2_add(e, gh[m2 * kFuseSP + lane], gl[m2 * kFuseSP + lane], xv[m2].x, xv[m2].y);
+      }
+      if (m < S) dot2_add(d, gh[m * kFuseSP + lane], gl[m * kFuseSP + lane], xv[m].x, xv[m].y);
+      dot2_merge(d, e);
+      part[warp * kFuseSP + lane] = d;
     }
     __syncthreads();
-    if (threadIdx.x < kFuseSP) {  // A'
-      Dot2 d = part[threadIdx.x];
+    if (warp == 0) {  // A'
+      Dot2 d = part[lane];
 #pragma unroll
-      for (int q = 1; q < kFuseParts; ++q) dot2_merge(d, part[q * kFuseSP + threadIdx.x]);
-      const int p = p0 + sub * kFuseSP + threadIdx.x;
+      for (int q = 1; q < kFuseWarps; ++q) dot2_merge(d, part[q * kFuseSP + lane]);
+      const int p = p0 + sub * kFuseSP + lane;
       float2 v = make_float2(0.f, 0.f);
       if (p < p1) {
         if (MODE == 0) {
@@ -426,16 +446,10 @@ __global__ void __launch_bounds__(kFuseThreads, 1) k_glisa_fused_ff(Batch bt) {
           const double rho = J.rho[p], w = J.w[p];
           const bool sick = (rho < J.density_cutoff) || (rho0 < J.density_cutoff);
           f2 d1{0.f, 0.f}, dd{0.f, 0.f};
-          const float2 wr = split2(w * rho);
           if (!sick) {
+            const float2 wr = split2(w * rho);
             d1 = ffa::div(f2{wr.x, wr.y}, r0);
             dd = ffa::div(d1, r0);
-            const float2 rp = split2(rho);
-            const f2 ratio = ffa::div(f2{rp.x, rp.y}, r0);
-            const float l0 = logf(ratio.hi);
-            const f2 e = ffa::exp_ff(f2{-l0, 0.f}, tab);
-            const f2 l = ffa::add(ffa::add(ffa::mul(ratio, e), -1.0f), l0);
-            ent = ffa::add(ent, ffa::mul(f2{wr.x, wr.y}, l));
           }
           J.dvec1[p] = ffa::to_double(d1);
           J.dvec2[p] = ffa::to_double(dd);
@@ -446,21 +460,33 @@ __global__ void __launch_bounds__(kFuseThreads, 1) k_glisa_fused_ff(Batch bt) {
           v = make_float2(d1.hi, d1.lo);
         }
       }
-      vs[threadIdx.x] = v;
+      vs[lane] = v;
     }
     __syncthreads();
     {  // B
-      const float2 v0 = vs[lane], v1 = vs[lane + 32];
+      const float2 v = vs[lane];
 #pragma unroll
       for (int r = 0; r < kFuseRows; ++r) {
         const int m = warp + kFuseWarps * r;
-        if (m < S) {
-          dot2_add(acc[r], gh[m * kFuseSP + lane], gl[m * kFuseSP + lane], v0.x, v0.y);
-          dot2_add(acc[r], gh[m * kFuseSP + lane + 32], gl[m * kFuseSP + lane + 32], v1.x, v1.y);
+        if (m < S) dot2_add(acc[r], gh[m * kFuseSP + lane], gl[m * kFuseSP + lane], v.x, v.y);
+      }
+    }
+    if (MODE == 1 && (sub % kFuseGroup == kFuseGroup - 1 || sub == nsub - 1)) {
+      // entropy terms of the group's points, one per thread (rho0 was
+      // written by warp 0 before the last barrier)
+      const int p = p0 + (sub - sub % kFuseGroup) * kFuseSP + threadIdx.x;
+      if (p < p1 && threadIdx.x < (sub % kFuseGroup + 1) * kFuseSP) {
+        const double rho = J.rho[p], rho0 = J.rho0[p];
+        if (!((rho < J.density_cutoff) || (rho0 < J.density_cutoff))) {
+          const float2 rp = split2(rho), r0 = split2(rho0), wr = split2(J.w[p] * rho);
+          const f2 ratio = ffa::div(f2{rp.x, rp.y}, f2{r0.x, r0.y});
+          const float l0 = logf(ratio.hi);
+          const f2 e = ffa::exp_ff(f2{-l0, 0.f}, tab);
+          const f2 l = ffa::add(ffa::add(ffa::mul(ratio, e), -1.0f), l0);
+          ent = ffa::add(ent, ffa::mul(f2{wr.x, wr.y}, l));
         }
       }
     }
-    __syncthreads();  // this stage is refilled by the next sub-tile's copies
   }
 #pragma unroll
   for (int r = 0; r < kFuseRows; ++r) {
@@ -476,7 +502,7 @@ __global__ void __launch_bounds__(kFuseThreads, 1) k_glisa_fused_ff(Batch bt) {
     }
   }
   if (MODE == 1) {
-    // entropy and negativity partials of the tile (threads >= kFuseSP hold zeros)
+    // entropy and negativity partials of the tile
     double e = ffa::to_double(ent), n = (double)nneg;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
@@ -500,31 +526,42 @@ __global__ void __launch_bounds__(kFuseThreads, 1) k_glisa_fused_ff(Batch bt) {
   }
 }
 
-// Outer change per (atom, tile): sum_p w (sum_{m in atom} (c - c_old)_m g_m)^2
-// (glisa.py:776 via compute_change), the differences formed in FP64.
+// Outer change (glisa.py:776 via compute_change): sum over atoms of
+// int w (sum_{m in atom} (c - c_old)_m g_m)^2, one block per point tile, all
+// atoms per point (one read of G). The differences are formed in FP64 and
+// each atom's sum over its shells is a compensated dot product; its square
+// and the weight are FP32 (the change is compared with the threshold, where
+// 1e-7 relative is ample), summed per thread as a float pair. The tile's
+// total goes to atom 0's slot (the other atoms' slots get 0).
 __global__ void __launch_bounds__(kThreads) k_glisa_change_ff(Batch bt) {
-  __shared__ float2 dc[kMaxShells];
+  __shared__ float2 dc[kGffMaxShells];
   __shared__ double red[kWarps];
-  const int jb = find_job(bt, blockIdx.x);
-  const JobDev& J = bt.jobs[jb];
-  const int local = blockIdx.x - bt.prefix[jb];
-  const int atom = local / J.ntile, tile = local - atom * J.ntile;
-  const int s0 = J.shell_off[atom], n = J.shell_off[atom + 1] - s0;
-  if (threadIdx.x < n) dc[threadIdx.x] = split2(J.propars[s0 + threadIdx.x] - J.propars_old[s0 + threadIdx.x]);
+  int tile;
+  const JobDev& J = decode_local_gf(bt, tile);
+  for (int i = threadIdx.x; i < J.nshell; i += kThreads) dc[i] = split2(J.propars[i] - J.propars_old[i]);
   __syncthreads();
   const size_t N = J.npoint;
-  double acc = 0.0;
+  float ah = 0.0f, al = 0.0f;
   for (int i = 0; i < J.ppt; ++i) {
     const int p = point_in_tile(J, tile, i);
     if (p >= J.npoint) continue;
-    Dot2 d{0.f, 0.f};
-    for (int k = 0; k < n; ++k)
-      dot2_add(d, J.gmat32[(s0 + k) * N + p], J.gmat_lo[(s0 + k) * N + p], dc[k].x, dc[k].y);
-    const double v = dot2_value(d);
-    acc += J.w[p] * v * v;
+    const float wf = (float)J.w[p];
+    int m = J.shell_off[0];
+    for (int a = 0; a < J.natom; ++a) {
+      const int m1 = J.shell_off[a + 1];
+      Dot2 d{0.f, 0.f};
+      for (; m < m1; ++m) dot2_add(d, J.gmat32[m * N + p], J.gmat_lo[m * N + p], dc[m].x, dc[m].y);
+      const float v = d.s + d.c;
+      const float term = wf * v * v;
+      const float t = ah + term;
+      const float bb = t - ah;
+      al += (ah - (t - bb)) + (term - bb);
+      ah = t;
+    }
   }
-  const double s = block_sum1(acc, red);
-  if (threadIdx.x == 0) J.apart[((size_t)atom * J.qa + QA_CHANGE) * J.ntile + tile] = s;
+  const double sum = block_sum1((double)ah + (double)al, red);
+  for (int a = threadIdx.x; a < J.natom; a += kThreads)
+    J.apart[((size_t)a * J.qa + QA_CHANGE) * J.ntile + tile] = a == 0 ? sum : 0.0;
 }
 
 // ---------------------------------------------------------------------------
@@ -586,11 +623,12 @@ void launch_glisa_fused_ff(const HostBatch& hb, cudaStream_t st, int mode, int m
 }
 
 void launch_glisa_trials_ff(const HostBatch& hb, cudaStream_t st) {
+  HP_LAUNCH_GF(k_glisa_u_ff, K_POINT1, kThreads);
   HP_LAUNCH_GF(k_glisa_trials_ff, K_POINT, kThreads);
 }
 
 void launch_glisa_change_ff(const HostBatch& hb, cudaStream_t st) {
-  HP_LAUNCH_GF(k_glisa_change_ff, K_ATOM_TILE, kThreads);
+  HP_LAUNCH_GF(k_glisa_change_ff, K_POINT, kThreads);
 }
 
 }  // namespace hp

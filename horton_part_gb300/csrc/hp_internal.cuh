@@ -418,7 +418,8 @@ void launch_glisa_change_ff(const HostBatch& hb, cudaStream_t st);
 
 // tensor-core Hessian (hp_tcgen05.cu)
 int tc_hess_blocks(const JobDev& J);
-void launch_glisa_hess_tc(const HostBatch& hb, cudaStream_t st);
+// max_shells / min_shells: largest and smallest shell count among the batch's jobs
+void launch_glisa_hess_tc(const HostBatch& hb, cudaStream_t st, int max_shells, int min_shells);
 
 // mixed precision (hp_mixed.cu)
 void launch_promol_mx(const HostBatch& hb, cudaStream_t st, int model);

@@ -413,7 +413,14 @@ int step_glisa(hp_ctx* ctx, const std::vector<hp_job*>& jobs, const HostBatch& h
   }
   if (solver != SOLVER_SC) {
     ProfScope ps(ctx, HP_KERNEL_GLISA_HESS);
-    if (tc) launch_glisa_hess_tc(hb, st);
+    if (tc) {
+      int smax = 0, smin = 1 << 30;
+      for (hp_job* j : jobs) {
+        smax = std::max(smax, j->dev.nshell);
+        smin = std::min(smin, j->dev.nshell);
+      }
+      launch_glisa_hess_tc(hb, st, smax, smin);
+    }
     else launch_glisa_hess(hb, st);
   }
   {

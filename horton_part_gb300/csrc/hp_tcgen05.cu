@@ -45,6 +45,7 @@ constexpr int kRowsA = kTcM / kTcWarps;     // A rows staged per warp
 constexpr int kRowsB = kTcNMax / kTcWarps;  // B rows staged per warp (at most)
 constexpr int kTcCols = 256;    // tensor-memory columns (FP32 accumulator, N <= 256)
 constexpr long long kWaitLimit = 1ll << 26;
+constexpr int kT1Rows = 256;    // single-pass form (k_glisa_hess_tc1) up to this many shells
 
 // shared-memory layout (offsets from a 1024-byte-aligned base): two stages
 // of (A_hi, A_lo, B_hi, B_lo), then the stages' mbarriers and the TMEM slot
@@ -157,6 +158,7 @@ __global__ void __launch_bounds__(kTcThreads) k_glisa_hess_tc(Batch bt) {
   const JobDev& J = bt.jobs[jb];
   const int local = blockIdx.x - bt.prefix[jb];
   const int M = J.nshell, N = J.npoint;
+  if (M <= kT1Rows) return;  // k_glisa_hess_tc1
   const int ntiles = tc_tiles(M, -1, nullptr, nullptr, nullptr);
   const int split = local / ntiles;
   int i0 = 0, j0 = 0, ncol = 16;
@@ -320,19 +322,212 @@ __global__ void __launch_bounds__(kTcThreads) k_glisa_hess_tc(Batch bt) {
   }
 }
 
+// ---------------------------------------------------------------------------
+// Single-pass form for S <= 256 shells: one CTA per point range computes the
+// whole lower triangle from one staging of X. Per block of 32 points the
+// CTA stages rows 0..S-1 of X (hi and lo planes, 128B-swizzled K-major, rows
+// S..255 zero, written once) and issues two accumulations:
+//   D1 (TMEM columns 0..N1-1):    A = rows 0..127,   B = rows 0..N1-1,
+//                                  N1 = S rounded up to 16;
+//   D2 (TMEM columns 256..+N2-1): A = rows 128..255, B = rows 128..N1-1,
+//                                  N2 = N1 - 128 (only when S > 128).
+// D1 holds H[i][j] for i < 128 (its columns j >= 128 are the entries H[j][i]
+// of the rows below 128), D2 the block i, j >= 128. Every X row is staged
+// once per block (the tiled form stages up to three 128-row operands per
+// block) and the MMA area per block is 128 x (N1 + N2).
+// ---------------------------------------------------------------------------
+constexpr int kT1Plane = kT1Rows * kTcK * 4;      // 32 KB
+constexpr int kT1Stage = 2 * kT1Plane;             // hi + lo
+constexpr int kT1OffBar = 2 * kT1Stage;            // 128 KB
+constexpr int kT1Smem = kT1OffBar + 64 + 1024;     // + alignment slack
+constexpr int kT1Cols = 512;                       // D1 at 0, D2 at 256
+constexpr int kT1RowsPerWarp = kT1Rows / kTcWarps; // 16
+
+__global__ void __launch_bounds__(kTcThreads) k_glisa_hess_tc1(Batch bt) {
+  extern __shared__ uint8_t smem_raw[];
+  const uint32_t raw = smem_u32(smem_raw);
+  const uint32_t base = (raw + 1023u) & ~1023u;
+  uint8_t* sm = smem_raw + (base - raw);
+  const uint32_t bar0 = base + kT1OffBar;  // stage s: bar0 + 8 s
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(sm + kT1OffBar + 16);
+  __shared__ int timed_out;
+
+  const int jb = find_job(bt, blockIdx.x);
+  const JobDev& J = bt.jobs[jb];
+  const int M = J.nshell, N = J.npoint;
+  if (M > kT1Rows) return;  // the tiled kernel (k_glisa_hess_tc) takes this job
+  const int split = blockIdx.x - bt.prefix[jb];
+  const int chunk = ((N + J.nsplit - 1) / J.nsplit + kTcK - 1) / kTcK * kTcK;
+  const int pbeg = split * chunk;
+  const int pend = min(pbeg + chunk, N);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int n1 = (M + 15) / 16 * 16;
+  const int n2 = n1 > kTcM ? n1 - kTcM : 0;
+  const uint32_t idesc1 = idesc_tf32(n1);
+  const uint32_t idesc2 = idesc_tf32(n2 > 0 ? n2 : 16);
+  const uint32_t swz_col = (uint32_t)((((lane >> 2) ^ (warp & 7)) << 2) | (lane & 3));
+
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(tmem_slot)),
+                 "r"(kT1Cols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  // rows M..255 of both planes of both stages stay zero
+  for (int e = threadIdx.x; e < 2 * 2 * (kT1Rows - M) * kTcK; e += kTcThreads) {
+    const int k = e % kTcK;
+    const int rr = e / kTcK;  // 0 .. 4 (256 - M) - 1
+    const int row = M + rr % (kT1Rows - M);
+    const int plane = rr / (kT1Rows - M);  // stage * 2 + (lo ? 1 : 0)
+    reinterpret_cast<uint32_t*>(sm + plane * kT1Plane)[row * kTcK + k] = 0u;
+  }
+  if (threadIdx.x == 0) {
+    mbar_init(bar0, 1);
+    mbar_init(bar0 + 8, 1);
+    timed_out = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;");
+  }
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  const uint32_t tmem = *tmem_slot;
+
+  // rows of this thread: warp + 16 r (< M); operands of two blocks in flight
+  float v0[kT1RowsPerWarp], v1[kT1RowsPerWarp], s0 = 0.0f, s1 = 0.0f;
+  auto load_block = [&](float (&v)[kT1RowsPerWarp], float& s, int kb) {
+    const int p = kb + lane;
+    const bool inr = p < pend;
+    s = inr ? J.hess_s[p] : 0.0f;
+#pragma unroll
+    for (int r = 0; r < kT1RowsPerWarp; ++r) {
+      const int m = warp + kTcWarps * r;
+      v[r] = (inr && m < M) ? J.gmat32[(size_t)m * N + p] : 0.0f;
+    }
+  };
+
+  int nblocks = 0;
+  auto do_block = [&](float (&v)[kT1RowsPerWarp], float& s, int kb) -> bool {
+    const int st = nblocks & 1;
+    uint8_t* stage = sm + st * kT1Stage;
+    uint32_t* x_hi = reinterpret_cast<uint32_t*>(stage);
+    uint32_t* x_lo = reinterpret_cast<uint32_t*>(stage + kT1Plane);
+    if (nblocks >= 2) {
+      if (!mbar_wait(bar0 + 8 * st, (uint32_t)(((nblocks >> 1) - 1) & 1))) timed_out = 1;
+    }
+#pragma unroll
+    for (int r = 0; r < kT1RowsPerWarp; ++r) {
+      const int row = warp + kTcWarps * r;
+      if (row < M) {
+        const float x = v[r] * s;
+        const uint32_t hi = __float_as_uint(x) & kTf32Mask;
+        const uint32_t off = (uint32_t)(row * kTcK) + swz_col;
+        x_hi[off] = hi;
+        x_lo[off] = __float_as_uint(x - __uint_as_float(hi));
+      }
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
+    if (timed_out) return false;
+    if (threadIdx.x == 0) {
+      asm volatile("tcgen05.fence::after_thread_sync;");
+      const uint32_t hi = smem_u32(x_hi), lo = smem_u32(x_lo);
+      const uint32_t hi2 = hi + kTcM * kTcK * 4, lo2 = lo + kTcM * kTcK * 4;  // row 128
+#pragma unroll
+      for (int k = 0; k < kTcK / 8; ++k) {
+        const uint32_t acc = (nblocks > 0 || k > 0) ? 1u : 0u;
+        umma_tf32(tmem, umma_desc(hi + 32 * k), umma_desc(hi + 32 * k), idesc1, acc);
+        umma_tf32(tmem, umma_desc(hi + 32 * k), umma_desc(lo + 32 * k), idesc1, 1u);
+        umma_tf32(tmem, umma_desc(lo + 32 * k), umma_desc(hi + 32 * k), idesc1, 1u);
+        if (n2 > 0) {
+          const uint32_t t2 = tmem + 256u;
+          umma_tf32(t2, umma_desc(hi2 + 32 * k), umma_desc(hi2 + 32 * k), idesc2, acc);
+          umma_tf32(t2, umma_desc(hi2 + 32 * k), umma_desc(lo2 + 32 * k), idesc2, 1u);
+          umma_tf32(t2, umma_desc(lo2 + 32 * k), umma_desc(hi2 + 32 * k), idesc2, 1u);
+        }
+      }
+      umma_commit(bar0 + 8 * st);
+    }
+    ++nblocks;
+    if (kb + 2 * kTcK < pend) load_block(v, s, kb + 2 * kTcK);
+    return true;
+  };
+
+  if (pbeg < pend) load_block(v0, s0, pbeg);
+  if (pbeg + kTcK < pend) load_block(v1, s1, pbeg + kTcK);
+  for (int kb = pbeg; kb < pend; kb += 2 * kTcK) {
+    if (!do_block(v0, s0, kb)) break;
+    if (kb + kTcK < pend && !do_block(v1, s1, kb + kTcK)) break;
+  }
+  if (nblocks > 0 && !timed_out) {
+    const int last = nblocks - 1;
+    if (!mbar_wait(bar0 + 8 * (last & 1), (uint32_t)((last >> 1) & 1))) timed_out = 1;
+  }
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  __syncthreads();
+
+  // epilogue: warp w reads tensor-memory lanes 32 (w % 4) .. + 31; the four
+  // warps of a lane quarter take every fourth 8-column chunk
+  double* out = J.hpart + (size_t)split * M * M;
+  const int quad = warp & 3;
+  const bool ok = nblocks > 0 && !timed_out;
+  for (int part = 0; part < 2; ++part) {
+    const int ncols = part == 0 ? n1 : n2;
+    const int i = part * kTcM + quad * 32 + lane;  // row of H
+    for (int c = 8 * (warp >> 2); c < ncols; c += 32) {
+      uint32_t v[8];
+      if (ok) {
+        const uint32_t taddr = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(part * 256 + c);
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+            : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+              "=r"(v[7])
+            : "r"(taddr));
+        asm volatile("tcgen05.wait::ld.sync.aligned;");
+      } else {
+#pragma unroll
+        for (int q = 0; q < 8; ++q) v[q] = 0u;
+      }
+      if (i < M) {
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+          const int j = part * kTcM + c + q;
+          if (j >= M) continue;
+          const double h = (double)__uint_as_float(v[q]);
+          if (j <= i) out[(size_t)i * M + j] = h;
+          else if (part == 0 && j >= kTcM) out[(size_t)j * M + i] = h;  // H[j][i], j below row 128
+        }
+      }
+    }
+  }
+  if (timed_out && threadIdx.x == 0) atomicOr(&J.mail->i[MI_ERR], E_TIMEOUT);
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kT1Cols));
+  }
+}
+
 int tc_hess_blocks(const JobDev& J) {
+  if (J.nshell <= kT1Rows) return J.nsplit;  // k_glisa_hess_tc1: one CTA per point range
   return tc_tiles(J.nshell, -1, nullptr, nullptr, nullptr) * J.nsplit;
 }
 
-void launch_glisa_hess_tc(const HostBatch& hb, cudaStream_t st) {
+void launch_glisa_hess_tc(const HostBatch& hb, cudaStream_t st, int max_shells, int min_shells) {
   static int configured_device = -1;
   int dev = 0;
   cudaGetDevice(&dev);
   if (configured_device != dev) {
     cudaFuncSetAttribute(k_glisa_hess_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes);
+    cudaFuncSetAttribute(k_glisa_hess_tc1, cudaFuncAttributeMaxDynamicSharedMemorySize, kT1Smem);
     configured_device = dev;
   }
-  if (hb.blocks[K_HESS] > 0) {
+  if (hb.blocks[K_HESS] <= 0) return;
+  if (min_shells <= kT1Rows) {
+    k_glisa_hess_tc1<<<hb.blocks[K_HESS], kTcThreads, kT1Smem, st>>>(hb.b[K_HESS]);
+    ++g_launch_count;
+  }
+  if (max_shells > kT1Rows) {
     k_glisa_hess_tc<<<hb.blocks[K_HESS], kTcThreads, kSmemBytes, st>>>(hb.b[K_HESS]);
     ++g_launch_count;
   }

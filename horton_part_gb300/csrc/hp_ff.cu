@@ -70,8 +70,10 @@ __device__ __forceinline__ f2 dist2_ff(const JobDev& J, int p, int a) {
   return ffa::add_pos(ffa::add_pos(ffa::sqr(dx), ffa::sqr(dy)), ffa::sqr(dz));
 }
 
-// Distance from grid point p to atom a.
+// Distance from grid point p to atom a (the stored pair when the job keeps
+// one: the same value, computed once at job start by k_rdist_ff).
 __device__ __forceinline__ f2 dist_ff(const JobDev& J, int p, int a) {
+  if (J.rdist) return load2(&J.rdist[(size_t)a * J.npoint + p]);
   return ffa::sqrt_ff(dist2_ff(J, p, a));
 }
 
@@ -307,6 +309,21 @@ void ensure_exp_table() {
 
 }  // namespace
 
+// Point-atom distances of a mixed / ff job as float pairs (once per job):
+// every later kernel reads them instead of re-forming the distance.
+__global__ void __launch_bounds__(kThreads) k_rdist_ff(Batch bt) {
+  int blk;
+  const JobDev& J = decode_local_ff(bt, blk);
+  if (!J.rdist) return;
+  const int p = blk * kThreads + threadIdx.x;
+  if (p >= J.npoint) return;
+  for (int a = 0; a < J.natom; ++a) {
+    const f2 d2 = dist2_ff(J, p, a);
+    const f2 r = d2.hi > 0.0f ? ffa::sqrt_ff(d2) : f2{0.0f, 0.0f};
+    J.rdist[(size_t)a * J.npoint + p] = make_float2(r.hi, r.lo);
+  }
+}
+
 // Basis matrix of a gLISA job as float-float planes (gmat32 = hi, gmat_lo =
 // lo): G[s][p] = pref_s exp(-alpha_s r^order_s), the unit-population shells
 // of gisa.py:91-106 (force_on_molgrid=True) with the normalisation of
@@ -360,6 +377,10 @@ void launch_promol_ff(const HostBatch& hb, cudaStream_t st) {
 void launch_mbis_inner_ff(const HostBatch& hb, cudaStream_t st) {
   ensure_exp_table();
   HP_LAUNCH_FF(k_mbis_inner_ff, K_ATOM_TILE, kThreads);
+}
+
+void launch_rdist_ff(const HostBatch& hb, cudaStream_t st) {
+  HP_LAUNCH_FF(k_rdist_ff, K_POINT1, kThreads);
 }
 
 void launch_glisa_basis_ff(const HostBatch& hb, cudaStream_t st) {

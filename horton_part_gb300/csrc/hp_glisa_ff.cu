@@ -324,7 +324,12 @@ __global__ void __launch_bounds__(kThreads) k_glisa_trials_ff(Batch bt) {
 //   k_glisa_pro_ff with the quotients in float-float, v = w rho / rho0; the
 //   entropy terms w rho ln(rho / rho0) are formed every 256 points by all
 //   threads (one point each) with ln from logf plus one Newton step on
-//   exp_ff (error ~ the square of logf's).
+//   exp_ff (error ~ the square of logf's). With with_change, also
+//   C  the outer change of the step that produced c (glisa.py:776 via
+//      compute_change): warp w takes the atoms a = w (mod 8), lane = point,
+//      sum_{m in a} (c - c_old)_m g_m as a compensated sum from the staged
+//      sub-tile, w times its square (FP32) summed per thread as a float
+//      pair; the tile's total goes to atom 0's QA_CHANGE slot.
 // Jobs with more than kFuseMaxShells shells use k_glisa_pro_ff /
 // k_glisa_hv_ff with k_glisa_grad_ff.
 // ---------------------------------------------------------------------------
@@ -338,7 +343,7 @@ constexpr int kFuseGroup = kFuseThreads / kFuseSP;      // sub-tiles per entropy
 // Shared memory of a fused pass for S shells (bytes).
 __host__ __device__ constexpr size_t fuse_smem_bytes(int S) {
   return 4 * (size_t)S * kFuseSP * 4          // two stages of both planes
-         + 8 * (size_t)S                      // x as float pairs
+         + 16 * (size_t)S                     // x and the parameter change as float pairs
          + 8 * (size_t)kFuseWarps * kFuseSP   // partial sums
          + 8 * (size_t)kFuseSP                // v
          + 512                                // exp table
@@ -377,7 +382,7 @@ __device__ __forceinline__ void fuse_load(const JobDev& J, int q0, int p1, float
 }
 
 template <int MODE>
-__global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_fused_ff(Batch bt) {
+__global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_fused_ff(Batch bt, int with_change) {
   extern __shared__ float4 fsm[];
   int tile;
   const JobDev& J = decode_local_gf(bt, tile);
@@ -387,7 +392,8 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_fused_ff(Batch bt) {
   float* stg = reinterpret_cast<float*>(fsm);
   const int plane = S * kFuseSP;
   float2* xv = reinterpret_cast<float2*>(stg + 4 * plane);
-  Dot2* part = reinterpret_cast<Dot2*>(xv + S);
+  float2* dcv = xv + S;
+  Dot2* part = reinterpret_cast<Dot2*>(dcv + S);
   float2* vs = reinterpret_cast<float2*>(part + kFuseWarps * kFuseSP);
   float2* tab = vs + kFuseSP;
   double* red = reinterpret_cast<double*>(tab + 64);
@@ -400,6 +406,10 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_fused_ff(Batch bt) {
   cp_async_commit();
   const double* x = MODE ? J.propars : J.delta;
   for (int i = threadIdx.x; i < S; i += kFuseThreads) xv[i] = split2(x[i]);
+  const bool chg = MODE == 1 && with_change;
+  if (chg)
+    for (int i = threadIdx.x; i < S; i += kFuseThreads) dcv[i] = split2(J.propars[i] - J.propars_old[i]);
+  float ch = 0.0f, cl = 0.0f;  // change terms of this thread (float pair)
   if (MODE == 1 && threadIdx.x < 64) tab[threadIdx.x] = c_exp2_gl[threadIdx.x];
   Dot2 acc[kFuseRows];
 #pragma unroll
@@ -471,6 +481,21 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_fused_ff(Batch bt) {
         if (m < S) dot2_add(acc[r], gh[m * kFuseSP + lane], gl[m * kFuseSP + lane], v.x, v.y);
       }
     }
+    if (chg) {  // C
+      const int p = p0 + sub * kFuseSP + lane;
+      const float wf = p < p1 ? (float)J.w[p] : 0.0f;
+      for (int a = warp; a < J.natom; a += kFuseWarps) {
+        Dot2 d{0.f, 0.f};
+        for (int m = J.shell_off[a]; m < J.shell_off[a + 1]; ++m)
+          dot2_add(d, gh[m * kFuseSP + lane], gl[m * kFuseSP + lane], dcv[m].x, dcv[m].y);
+        const float v = d.s + d.c;
+        const float term = wf * v * v;
+        const float t = ch + term;
+        const float bb = t - ch;
+        cl += (ch - (t - bb)) + (term - bb);
+        ch = t;
+      }
+    }
     if (MODE == 1 && (sub % kFuseGroup == kFuseGroup - 1 || sub == nsub - 1)) {
       // entropy terms of the group's points, one per thread (rho0 was
       // written by warp 0 before the last barrier)
@@ -523,7 +548,124 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_fused_ff(Batch bt) {
       J.jpart[(size_t)QJ_ENTROPY * J.ntile + tile] = se;
       J.jpart[(size_t)QJ_NEG * J.ntile + tile] = sn;
     }
+    if (chg) {
+      double c = (double)ch + (double)cl;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+      __syncthreads();  // red is reused
+      if (lane == 0) red[warp] = c;
+      __syncthreads();
+      double sc = 0.0;
+      for (int k = 0; k < kFuseWarps; ++k) sc += red[k];
+      for (int a = threadIdx.x; a < J.natom; a += kFuseThreads)
+        J.apart[((size_t)a * J.qa + QA_CHANGE) * J.ntile + tile] = a == 0 ? sc : 0.0;
+    }
   }
+}
+
+// Trial objective differences for fused jobs: k_glisa_u_ff and
+// k_glisa_trials_ff in one pass over staged sub-tiles (as k_glisa_fused_ff).
+// Per sub-tile: A forms u = G^T delta (eight partial sums per point); T: warp
+// t evaluates trial t for the 32 points (lane = point), with the clipped
+// shells' corrections read from the staged sub-tile, and keeps its sum in
+// registers; the tile's eight sums go to tpart at its end.
+static_assert(kTrials == kFuseWarps, "one warp per trial step");
+
+__global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_trials_fused(Batch bt) {
+  extern __shared__ float4 fsm[];
+  int tile;
+  const JobDev& J = decode_local_gf(bt, tile);
+  if (!J.fuse) return;
+  const int S = J.nshell;
+  float* stg = reinterpret_cast<float*>(fsm);
+  const int plane = S * kFuseSP;
+  float2* xv = reinterpret_cast<float2*>(stg + 4 * plane);
+  Dot2* part = reinterpret_cast<Dot2*>(xv + 2 * S);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int p0 = tile * J.tile_points;
+  const int p1 = min(p0 + J.tile_points, J.npoint);
+  const int nsub = (p1 - p0 + kFuseSP - 1) / kFuseSP;
+  const bool vec = (J.npoint & 3) == 0;
+  fuse_load(J, p0, p1, stg, stg + plane, vec);
+  cp_async_commit();
+  for (int i = threadIdx.x; i < S; i += kFuseThreads) xv[i] = split2(J.delta[i]);
+  const int t = warp;  // this warp's trial: step 2^-t
+  const float at = ldexpf(1.0f, -t);
+  const int nclip = J.clip[S];
+  const int* tm = J.clip + S + 1;
+  int kt = 0;  // clipped shells with t_m > t: a prefix of the list (sorted, largest first)
+  while (kt < nclip && tm[kt] > t) ++kt;
+  const float4* cd = reinterpret_cast<const float4*>(J.clipf);
+  const double cut = J.density_cutoff;
+  const float2 cutp = split2(cut);
+  float ah = 0.0f, al = 0.0f;
+  for (int sub = 0; sub < nsub; ++sub) {
+    const float* gh = stg + (sub & 1) * 2 * plane;
+    const float* gl = gh + plane;
+    cp_async_wait<0>();
+    __syncthreads();
+    if (sub + 1 < nsub) {
+      float* nh = stg + ((sub + 1) & 1) * 2 * plane;
+      fuse_load(J, p0 + (sub + 1) * kFuseSP, p1, nh, nh + plane, vec);
+      cp_async_commit();
+    }
+    {  // A
+      Dot2 d{0.f, 0.f}, e{0.f, 0.f};
+      int m = warp;
+      for (; m + kFuseWarps < S; m += 2 * kFuseWarps) {
+        dot2_add(d, gh[m * kFuseSP + lane], gl[m * kFuseSP + lane], xv[m].x, xv[m].y);
+        const int m2 = m + kFuseWarps;
+        dot2_add(e, gh[m2 * kFuseSP + lane], gl[m2 * kFuseSP + lane], xv[m2].x, xv[m2].y);
+      }
+      if (m < S) dot2_add(d, gh[m * kFuseSP + lane], gl[m * kFuseSP + lane], xv[m].x, xv[m].y);
+      dot2_merge(d, e);
+      part[warp * kFuseSP + lane] = d;
+    }
+    __syncthreads();
+    const int p = p0 + sub * kFuseSP + lane;
+    if (p < p1) {  // T
+      Dot2 du = part[lane];
+#pragma unroll
+      for (int q = 1; q < kFuseWarps; ++q) dot2_merge(du, part[q * kFuseSP + lane]);
+      const f2 u = dot2_ff(du);
+      Dot2 sc{0.f, 0.f}, sd{0.f, 0.f};
+      for (int k = 0; k < kt; ++k) {
+        const int m = J.clip[k];
+        const float4 v = cd[k];
+        const float g1 = gh[m * kFuseSP + lane], g2 = gl[m * kFuseSP + lane];
+        dot2_add(sc, g1, g2, v.x, v.y);
+        dot2_add(sd, g1, g2, v.z, v.w);
+      }
+      const f2 dsd = dot2_ff(sd);
+      const f2 corr = ffa::neg(ffa::add(dot2_ff(sc), f2{at * dsd.hi, at * dsd.lo}));
+      const double rho = J.rho[p], w = J.w[p], r0 = J.rho0[p];
+      const bool rs = rho < cut;
+      const bool h0 = !(rs || r0 < cut);
+      const float2 r0p = split2(r0);
+      const f2 dr = ffa::add(f2{at * u.hi, at * u.lo}, corr);
+      const f2 rt = ffa::add(dr, f2{r0p.x, r0p.y});
+      const bool below = rt.hi < cutp.x || (rt.hi == cutp.x && rt.lo < cutp.y);
+      const bool ht = !(rs || below);
+      double big = 0.0;
+      float term = 0.0f;
+      if (h0 && ht) term = -(float)(w * rho) * log1pf(dr.hi / r0p.x);
+      else if (ht) big = w * rho * log(rho / ffa::to_double(rt));
+      else if (h0) big = -(w * rho * log(rho / r0));
+      if (big != 0.0) {
+        const float bh = (float)big;
+        term = bh;
+        al += (float)(big - (double)bh);
+      }
+      const float s2 = ah + term;
+      const float bb = s2 - ah;
+      al += (ah - (s2 - bb)) + (term - bb);
+      ah = s2;
+    }
+  }
+  double v = (double)ah + (double)al;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  if (lane == 0) J.tpart[(size_t)t * J.ntile + tile] = v;
 }
 
 // Outer change (glisa.py:776 via compute_change): sum over atoms of
@@ -562,6 +704,33 @@ __global__ void __launch_bounds__(kThreads) k_glisa_change_ff(Batch bt) {
   const double sum = block_sum1((double)ah + (double)al, red);
   for (int a = threadIdx.x; a < J.natom; a += kThreads)
     J.apart[((size_t)a * J.qa + QA_CHANGE) * J.ntile + tile] = a == 0 ? sum : 0.0;
+}
+
+// Final promolecule of a float-float gLISA job (glisa.py:268-278 through
+// core/stockholder.py:153-175): per point, each atom's pro-atom
+// sum_m c_m g_m as a compensated dot product; rho_a, the promolecule (+1e-100
+// per atom, as k_promol) and its reciprocal in FP64 for k_atweights.
+__global__ void __launch_bounds__(kThreads) k_glisa_promol_ff(Batch bt) {
+  __shared__ float2 cf[kGffMaxShells];
+  int blk;
+  const JobDev& J = decode_local_gf(bt, blk);
+  load_pairs(J.propars, J.nshell, cf);
+  const int p = blk * kThreads + threadIdx.x;
+  if (p >= J.npoint) return;
+  const size_t N = J.npoint;
+  double promol = 0.0;
+  int m = J.shell_off[0];
+  for (int a = 0; a < J.natom; ++a) {
+    const int m1 = J.shell_off[a + 1];
+    Dot2 d{0.f, 0.f};
+    for (; m < m1; ++m) dot2_add(d, J.gmat32[m * N + p], J.gmat_lo[m * N + p], cf[m].x, cf[m].y);
+    const double pro = dot2_value(d);
+    J.rhoa[(size_t)a * N + p] = pro;
+    promol += pro;
+    promol += 1e-100;
+  }
+  J.promol[p] = promol;
+  J.invpro[p] = 1.0 / promol;
 }
 
 // ---------------------------------------------------------------------------
@@ -608,18 +777,35 @@ void ensure_exp_table_gl() {
                        (int)fuse_smem_bytes(kFuseMaxShells));
   cudaFuncSetAttribute(k_glisa_fused_ff<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)fuse_smem_bytes(kFuseMaxShells));
+  cudaFuncSetAttribute(k_glisa_trials_fused, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)fuse_smem_bytes(kFuseMaxShells));
   if (dev < 31) done_mask |= 1 << dev;
 }
 
 }  // namespace
 
-void launch_glisa_fused_ff(const HostBatch& hb, cudaStream_t st, int mode, int max_shells) {
+void launch_glisa_fused_ff(const HostBatch& hb, cudaStream_t st, int mode, int max_shells,
+                           int with_change) {
   if (hb.blocks[K_POINT] <= 0) return;
   ensure_exp_table_gl();
   const size_t smem = fuse_smem_bytes(max_shells);
-  if (mode) k_glisa_fused_ff<1><<<hb.blocks[K_POINT], kFuseThreads, smem, st>>>(hb.b[K_POINT]);
-  else k_glisa_fused_ff<0><<<hb.blocks[K_POINT], kFuseThreads, smem, st>>>(hb.b[K_POINT]);
+  if (mode)
+    k_glisa_fused_ff<1><<<hb.blocks[K_POINT], kFuseThreads, smem, st>>>(hb.b[K_POINT], with_change);
+  else
+    k_glisa_fused_ff<0><<<hb.blocks[K_POINT], kFuseThreads, smem, st>>>(hb.b[K_POINT], 0);
   ++g_launch_count;
+}
+
+void launch_glisa_trials_fused(const HostBatch& hb, cudaStream_t st, int max_shells) {
+  if (hb.blocks[K_POINT] <= 0) return;
+  ensure_exp_table_gl();
+  k_glisa_trials_fused<<<hb.blocks[K_POINT], kFuseThreads, fuse_smem_bytes(max_shells), st>>>(
+      hb.b[K_POINT]);
+  ++g_launch_count;
+}
+
+void launch_glisa_promol_ff(const HostBatch& hb, cudaStream_t st) {
+  HP_LAUNCH_GF(k_glisa_promol_ff, K_POINT1, kThreads);
 }
 
 void launch_glisa_trials_ff(const HostBatch& hb, cudaStream_t st) {

@@ -44,7 +44,9 @@ enum JobQ {
   QJ_ENTROPY = 0,  // sum w rho ln(rho/promol)
   QJ_NELEC = 1,    // sum w rho
   QJ_NEG = 2,      // count of points with promolecule < negative_cutoff
-  QJ_COUNT = 3
+  QJ_ENT_PREV = 3, // fused gLISA jobs: QJ_ENTROPY / QJ_NEG of the parameters at the
+  QJ_NEG_PREV = 4, // start of the iteration (the pass that forms them runs one step early)
+  QJ_COUNT = 5
 };
 
 // Device-side scalars of a job, mirrored to pinned host memory after each
@@ -158,6 +160,7 @@ struct JobDev {
                           // (with gff: the high part of G = gmat32 + gmat_lo)
   float* gmat_lo;         // gLISA, gff: low part of G [nshell][npoint] (gmat is not stored)
   float* clipf;           // gLISA, gff: clipped shells' (c hi, c lo, delta hi, delta lo) [nshell]
+  float2* rdist;          // mixed / ff (MBIS, GISA, aLISA): point-atom distances as float pairs [natom][npoint]
   float2* d1f;            // gLISA, gff: w rho / rho0 as float pairs, npoint
   float2* hvf;            // gLISA, gff: the refinement's hvec as float pairs, npoint
   float* hess_s;          // gLISA tensor-core Hessian: sqrt(w rho / rho0^2) as FP32, npoint
@@ -323,6 +326,7 @@ struct Dist<double> {
 template <>
 struct Dist<float> {
   __device__ __forceinline__ static float r(const JobDev& J, int p, int a) {
+    if (J.rdist) return J.rdist[(size_t)a * J.npoint + p].x;  // stored float-float distance
     const float* c = J.atf + 6 * a;  // xh, xl, yh, yl, zh, zl (no FP64 work per point)
     const float dx = (J.pxh[p] - c[0]) + (J.pxl[p] - c[1]);
     const float dy = (J.pyh[p] - c[2]) + (J.pyl[p] - c[3]);
@@ -397,7 +401,8 @@ void launch_glisa_keep(const HostBatch& hb, cudaStream_t st);
 void launch_glisa_ls(const HostBatch& hb, cudaStream_t st, int first, int count);
 void launch_glisa_change(const HostBatch& hb, cudaStream_t st);
 void launch_glisa_check(const HostBatch& hb, cudaStream_t st);
-void launch_glisa_pnewton(const HostBatch& hb, cudaStream_t st, int gff);  // trials + Armijo pick
+// trials + Armijo pick; fuse_shells > 0: the fused trial pass (batch of fused jobs)
+void launch_glisa_pnewton(const HostBatch& hb, cudaStream_t st, int gff, int fuse_shells);
 // fuse_shells: largest shell count of the batch's fused jobs (0: none);
 // unfused: some job of the batch takes the separate passes
 void launch_glisa_refine(const HostBatch& hb, cudaStream_t st, int gff, int fuse_shells, int unfused);
@@ -408,16 +413,28 @@ constexpr int kGffMaxShells = 2048;
 // fused passes (one read of G for a product and the row sums that follow it):
 // two shared-memory stages of [S][64] float pairs
 constexpr int kFuseMaxShells = 192;
-void launch_glisa_fused_ff(const HostBatch& hb, cudaStream_t st, int mode, int max_shells);
+// mode 1 with with_change: also the outer change of the step just taken
+// (parameters minus propars_old), for fused jobs in place of k_glisa_change_ff
+void launch_glisa_fused_ff(const HostBatch& hb, cudaStream_t st, int mode, int max_shells,
+                           int with_change = 0);
 void launch_glisa_basis_ff(const HostBatch& hb, cudaStream_t st);
+void launch_rdist_ff(const HostBatch& hb, cudaStream_t st);  // rdist of the batch's jobs
 void launch_glisa_pro_ff(const HostBatch& hb, cudaStream_t st);
 void launch_glisa_grad_ff(const HostBatch& hb, cudaStream_t st);
 void launch_glisa_hv_ff(const HostBatch& hb, cudaStream_t st);  // hvec and G hvec
 void launch_glisa_trials_ff(const HostBatch& hb, cudaStream_t st);
+void launch_glisa_promol_ff(const HostBatch& hb, cudaStream_t st);  // final promolecule
+void launch_glisa_trials_fused(const HostBatch& hb, cudaStream_t st, int max_shells);
+void launch_atweights(const HostBatch& hb, cudaStream_t st);        // k_atweights alone
 void launch_glisa_change_ff(const HostBatch& hb, cudaStream_t st);
 
 // tensor-core Hessian (hp_tcgen05.cu)
 int tc_hess_blocks(const JobDev& J);
+// Jobs with at most kTcSinglePassShells shells take the single-pass kernel,
+// whose per-split partials are FP32 packed lower triangles (M (M + 1) / 2
+// floats per split, row-major: entry (i, j <= i) at i (i + 1) / 2 + j);
+// the tiled kernel writes full FP64 M x M partials.
+constexpr int kTcSinglePassShells = 256;
 // max_shells / min_shells: largest and smallest shell count among the batch's jobs
 void launch_glisa_hess_tc(const HostBatch& hb, cudaStream_t st, int max_shells, int min_shells);
 

@@ -177,6 +177,11 @@ __global__ void k_copy_old(Batch bt) {
   int local;
   const JobDev& J = decode_local(bt, local);
   for (int i = threadIdx.x; i < J.nparam; i += blockDim.x) J.propars_old[i] = J.propars[i];
+  if (J.fuse)  // entropy and negativity partials of the parameters the step starts from
+    for (int t = threadIdx.x; t < J.ntile; t += blockDim.x) {
+      J.jpart[(size_t)QJ_ENT_PREV * J.ntile + t] = J.jpart[(size_t)QJ_ENTROPY * J.ntile + t];
+      J.jpart[(size_t)QJ_NEG_PREV * J.ntile + t] = J.jpart[(size_t)QJ_NEG * J.ntile + t];
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -299,7 +304,8 @@ __global__ void __launch_bounds__(kThreads) k_outer_finish(Batch bt, int with_ch
     }
   }
   if (warp == 0) {
-    const double ent = warp_tile_sum(J, J.jpart + (size_t)QJ_ENTROPY * J.ntile, J.ntile);
+    const int q = J.fuse ? QJ_ENT_PREV : QJ_ENTROPY;
+    const double ent = warp_tile_sum(J, J.jpart + (size_t)q * J.ntile, J.ntile);
     if (lane == 0) ent_s = ent;
   }
   __syncthreads();
@@ -1172,7 +1178,21 @@ __global__ void __launch_bounds__(kThreads) k_glisa_reduce(Batch bt) {
   const JobDev& J = decode_local(bt, local);
   const int M = J.nshell;
   const int e = local * kThreads + threadIdx.x;
-  if (e < M * M) {
+  if (J.tc && M <= kTcSinglePassShells) {
+    // FP32 packed lower triangles of the single-pass tensor-core kernel
+    const int E = M * (M + 1) / 2;
+    if (e < E) {
+      int i = (int)((sqrtf(8.0f * (float)e + 1.0f) - 1.0f) * 0.5f);
+      while (i * (i + 1) / 2 > e) --i;
+      while ((i + 1) * (i + 2) / 2 <= e) ++i;
+      const int j = e - i * (i + 1) / 2;
+      const float* hp = reinterpret_cast<const float*>(J.hpart);
+      double s = 0.0;
+      for (int sp = 0; sp < J.nsplit; ++sp) s += (double)hp[(size_t)sp * E + e];
+      J.hess[(size_t)i * M + j] = s;
+      J.hess[(size_t)j * M + i] = s;
+    }
+  } else if (e < M * M) {
     const int i = e / M, j = e - i * M;
     if (i >= j) {
       double s = 0.0;
@@ -1373,22 +1393,40 @@ static_assert(4 * (kNewtonF32Max * kNewtonF32Max + 2 * kNewtonF32Max) <= kNewton
 __global__ void __launch_bounds__(kThreads) k_glisa_newton_step(Batch bt, int projected) {
   extern __shared__ double l_smem[];
   __shared__ double col_smem[2 * kNewtonColMax];
-  __shared__ int bad, nf_s;
+  __shared__ int bad;
+  __shared__ int wcount[kWarps];
+  __shared__ int fid[kNewtonF32Max];
   int local;
   const JobDev& J = decode_local(bt, local);
   const int M = J.nshell;
-  if (threadIdx.x == 0) {
-    int nf = 0;
-    for (int m = 0; m < M; ++m) {
-      const double gF = 1.0 + J.grad[m];
-      if (!projected || J.propars[m] > 0.0 || gF < 0.0) J.freeidx[nf++] = m;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  // free set in shell order: per-warp ballots and a prefix over the warps
+  int nf = 0;
+  for (int base = 0; base < M; base += kThreads) {
+    const int m = base + threadIdx.x;
+    bool f = false;
+    if (m < M) f = !projected || J.propars[m] > 0.0 || 1.0 + J.grad[m] < 0.0;
+    const unsigned b = __ballot_sync(0xffffffffu, f);
+    if (lane == 0) wcount[warp] = __popc(b);
+    __syncthreads();
+    int off = nf, total = nf;
+    for (int w = 0; w < kWarps; ++w) {
+      if (w < warp) off += wcount[w];
+      total += wcount[w];
     }
+    if (f) {
+      const int pos = off + __popc(b & ((1u << lane) - 1u));
+      J.freeidx[pos] = m;
+      if (pos < kNewtonF32Max) fid[pos] = m;
+    }
+    __syncthreads();
+    nf = total;
+  }
+  if (threadIdx.x == 0) {
     J.freeidx[M] = nf;
-    nf_s = nf;
     bad = 0;
   }
   __syncthreads();
-  const int nf = nf_s;
   if (J.tc && nf <= kNewtonF32Max) {
     // tensor-core Hessian: FP32 factor and solve in shared memory; the factor
     // (with 1 / diagonal after it) is kept in chol for the refinement steps,
@@ -1396,19 +1434,19 @@ __global__ void __launch_bounds__(kThreads) k_glisa_newton_step(Batch bt, int pr
     float* Lf = reinterpret_cast<float*>(l_smem);
     float* dv = Lf + nf * nf;
     float* yv = dv + nf;
-    for (int e = threadIdx.x; e < nf * nf; e += kThreads) {
-      const int i = e / nf, j = e - i * nf;
-      Lf[e] = (float)J.hess[(size_t)J.freeidx[i] * M + J.freeidx[j]];
+    for (int i = warp; i < nf; i += kWarps) {  // lower triangle (all the factor reads)
+      const double* hrow = J.hess + (size_t)fid[i] * M;
+      for (int j = lane; j <= i; j += 32) Lf[i * nf + j] = (float)hrow[fid[j]];
     }
     for (int m = threadIdx.x; m < M; m += kThreads) J.delta[m] = 0.0;
     __syncthreads();
     chol_factor_f(Lf, nf, &bad, reinterpret_cast<float*>(col_smem), dv);
     if (!bad) {
-      for (int i = threadIdx.x; i < nf; i += kThreads) yv[i] = (float)(-(1.0 + J.grad[J.freeidx[i]]));
+      for (int i = threadIdx.x; i < nf; i += kThreads) yv[i] = (float)(-(1.0 + J.grad[fid[i]]));
       __syncthreads();
       if (threadIdx.x < 32) chol_solve_warp_f(Lf, dv, nf, yv);
       __syncthreads();
-      for (int i = threadIdx.x; i < nf; i += kThreads) J.delta[J.freeidx[i]] = (double)yv[i];
+      for (int i = threadIdx.x; i < nf; i += kThreads) J.delta[fid[i]] = (double)yv[i];
       float* keep = reinterpret_cast<float*>(J.chol);
       for (int e = threadIdx.x; e < nf * nf + nf; e += kThreads) keep[e] = Lf[e];
       if (threadIdx.x == 0) J.freeidx[M + 1] = 1;
@@ -1471,8 +1509,17 @@ __global__ void __launch_bounds__(kThreads) k_glisa_refine(Batch bt) {
   double* r = J.keep;
   for (int i = warp; i < nf; i += kWarps) {  // one warp per row, lanes over tiles
     const int m = J.freeidx[i];
-    double hd = 0.0;
-    for (int t = lane; t < J.ntile; t += 32) hd += J.gpart[(size_t)m * J.ntile + t];
+    const double* gp = J.gpart + (size_t)m * J.ntile;
+    double h0 = 0.0, h1 = 0.0, h2 = 0.0, h3 = 0.0;  // four chains, combined in a fixed order
+    int t = lane;
+    for (; t + 96 < J.ntile; t += 128) {
+      h0 += gp[t];
+      h1 += gp[t + 32];
+      h2 += gp[t + 64];
+      h3 += gp[t + 96];
+    }
+    for (; t < J.ntile; t += 32) h0 += gp[t];
+    double hd = (h0 + h1) + (h2 + h3);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) hd += __shfl_xor_sync(0xffffffffu, hd, o);
     if (lane == 0) r[i] = -(1.0 + J.grad[m]) - hd;
@@ -1482,7 +1529,10 @@ __global__ void __launch_bounds__(kThreads) k_glisa_refine(Batch bt) {
     float* Lf = reinterpret_cast<float*>(l_smem);
     float* yv = Lf + nf * nf + nf;
     const float* keep = reinterpret_cast<const float*>(J.chol);
-    for (int e = threadIdx.x; e < nf * nf + nf; e += kThreads) Lf[e] = keep[e];
+    const int ne = nf * nf + nf;
+    for (int e = threadIdx.x; e < ne / 4; e += kThreads)  // chol and the dynamic shared base are 16-byte aligned
+      reinterpret_cast<float4*>(Lf)[e] = reinterpret_cast<const float4*>(keep)[e];
+    for (int e = ne / 4 * 4 + threadIdx.x; e < ne; e += kThreads) Lf[e] = keep[e];
     for (int i = threadIdx.x; i < nf; i += kThreads) yv[i] = (float)r[i];
     __syncthreads();
     if (threadIdx.x < 32) chol_solve_warp_f(Lf, Lf + nf * nf, nf, yv);
@@ -1675,7 +1725,8 @@ __global__ void __launch_bounds__(kThreads) k_glisa_change(Batch bt) {
 __global__ void k_glisa_check(Batch bt) {
   int local;
   const JobDev& J = decode_local(bt, local);
-  const double neg = warp_tile_sum(J, J.jpart + (size_t)QJ_NEG * J.ntile, J.ntile);
+  const int q = J.fuse ? QJ_NEG_PREV : QJ_NEG;  // the promolecule of the last step's start
+  const double neg = warp_tile_sum(J, J.jpart + (size_t)q * J.ntile, J.ntile);
   if ((threadIdx.x & 31) != 0) return;
   if (neg > 0.0) atomicOr(&J.mail->i[MI_ERR], E_NEG_DENSITY);
   double s = 0.0;
@@ -1844,6 +1895,10 @@ void launch_promol(const HostBatch& hb, cudaStream_t st, int mixed, int model) {
   HP_LAUNCH(k_atweights, K_ATOM_TILE, kThreads);
 }
 
+void launch_atweights(const HostBatch& hb, cudaStream_t st) {
+  HP_LAUNCH(k_atweights, K_ATOM_TILE, kThreads);
+}
+
 void launch_final_atweights(const HostBatch& hb, cudaStream_t st, int mixed, int model,
                             int use_old) {
   if (mixed == PH_FF && model == MODEL_MBIS) return launch_final_atweights_ff(hb, st, use_old);
@@ -1962,9 +2017,10 @@ void launch_glisa_change(const HostBatch& hb, cudaStream_t st) {
 
 void launch_glisa_check(const HostBatch& hb, cudaStream_t st) { HP_LAUNCH(k_glisa_check, K_JOB, 32); }
 
-void launch_glisa_pnewton(const HostBatch& hb, cudaStream_t st, int gff) {
+void launch_glisa_pnewton(const HostBatch& hb, cudaStream_t st, int gff, int fuse_shells) {
   HP_LAUNCH(k_glisa_trial_set, K_JOB, kThreads);
-  if (gff) launch_glisa_trials_ff(hb, st);
+  if (fuse_shells > 0) launch_glisa_trials_fused(hb, st, fuse_shells);
+  else if (gff) launch_glisa_trials_ff(hb, st);
   else HP_LAUNCH(k_glisa_trials, K_POINT, kThreads);
   HP_LAUNCH(k_glisa_trial_pick, K_JOB, 32);
 }

@@ -264,13 +264,20 @@ int run_inner(hp_ctx* ctx, const std::vector<hp_job*>& jobs, const HostBatch& hb
 
 int job_init(hp_ctx* ctx, const std::vector<hp_job*>& jobs, const HostBatch& hb) {
   launch_nelec(hb, ctx->stream);
-  bool any_basis = false, any_basis_ff = false;
+  bool any_basis = false, any_basis_ff = false, any_rdist = false;
   for (hp_job* j : jobs) {
     any_basis |= j->dev.gmat != nullptr;
     any_basis_ff |= j->dev.gmat_lo != nullptr;
+    any_rdist |= j->dev.rdist != nullptr;
   }
+  if (any_rdist) launch_rdist_ff(hb, ctx->stream);
   if (any_basis) launch_glisa_basis(hb, ctx->stream);
   if (any_basis_ff) launch_glisa_basis_ff(hb, ctx->stream);
+  int fuse_shells = 0;
+  for (hp_job* j : jobs)
+    if (j->dev.fuse) fuse_shells = std::max(fuse_shells, j->dev.nshell);
+  // fused gLISA jobs: the first iteration's promolecule and gradient
+  if (fuse_shells > 0) launch_glisa_fused_ff(hb, ctx->stream, 1, fuse_shells, 0);
   for (hp_job* j : jobs) j->initialized = true;
   return check_launch();
 }
@@ -390,23 +397,21 @@ int step_glisa(hp_ctx* ctx, const std::vector<hp_job*>& jobs, const HostBatch& h
   launch_copy_old(hb, st);
   const bool tc = jobs[0]->dev.tc != 0;
   const int gff = jobs[0]->dev.gff;
-  // fused promolecule + gradient (and refinement) passes for jobs with at
-  // most kFuseMaxShells shells, separate passes for the others
-  int fuse_shells = 0, unfused = 0;
-  for (hp_job* j : jobs) {
-    if (j->dev.fuse) fuse_shells = std::max(fuse_shells, j->dev.nshell);
-    else unfused = 1;
-  }
-  {
+  // Jobs with at most kFuseMaxShells shells (batches are homogeneous in
+  // this) take the fused passes: the promolecule + gradient pass of an
+  // iteration runs at the end of the previous step (or at job start) and also
+  // forms that step's change; the others take separate passes.
+  const bool fused = jobs[0]->dev.fuse != 0;
+  int fuse_shells = 0;
+  for (hp_job* j : jobs) fuse_shells = std::max(fuse_shells, j->dev.nshell);
+  if (!fused) fuse_shells = 0;
+  const int unfused = fused ? 0 : 1;
+  if (!fused) {
     ProfScope ps(ctx, HP_KERNEL_GLISA_PRO);
-    if (gff) {
-      if (fuse_shells > 0) launch_glisa_fused_ff(hb, st, 1, fuse_shells);
-      if (unfused) launch_glisa_pro_ff(hb, st);
-    } else {
-      launch_glisa_pro(hb, st);
-    }
+    if (gff) launch_glisa_pro_ff(hb, st);
+    else launch_glisa_pro(hb, st);
   }
-  if (!gff || unfused) {
+  if (!fused) {
     ProfScope ps(ctx, HP_KERNEL_GLISA_GRAD);
     if (gff) launch_glisa_grad_ff(hb, st);
     else launch_glisa_grad(hb, st);
@@ -436,7 +441,7 @@ int step_glisa(hp_ctx* ctx, const std::vector<hp_job*>& jobs, const HostBatch& h
         for (int k = 0; k < kRefineSteps; ++k) launch_glisa_refine(hb, st, gff, fuse_shells, unfused);
     }
     if (solver == SOLVER_PNEWTON) {
-      launch_glisa_pnewton(hb, st, gff);
+      launch_glisa_pnewton(hb, st, gff, fuse_shells);
     } else if (solver != SOLVER_SC) {
       if (solver == SOLVER_NEWTON) launch_glisa_apply(hb, st, 0);
       else {
@@ -480,7 +485,10 @@ int step_glisa(hp_ctx* ctx, const std::vector<hp_job*>& jobs, const HostBatch& h
       }
     }
   }
-  {
+  if (fused) {  // next iteration's promolecule and gradient, this step's change
+    ProfScope ps(ctx, HP_KERNEL_GLISA_PRO);
+    launch_glisa_fused_ff(hb, st, 1, fuse_shells, 1);
+  } else {
     ProfScope ps(ctx, HP_KERNEL_CHANGE);
     if (gff) launch_glisa_change_ff(hb, st);
     else launch_glisa_change(hb, st);
@@ -516,7 +524,12 @@ int step_glisa(hp_ctx* ctx, const std::vector<hp_job*>& jobs, const HostBatch& h
     rc = build_batch(ctx, conv, hc);
     if (rc) return rc;
     if (solver != SOLVER_SC) launch_glisa_check(hc, st);
-    launch_promol(hc, st, 0, MODEL_BASIS);
+    if (gff) {  // G as float-float planes: the promolecule from compensated sums
+      launch_glisa_promol_ff(hc, st);
+      launch_atweights(hc, st);
+    } else {
+      launch_promol(hc, st, 0, MODEL_BASIS);
+    }
     launch_charges(hc, st);
     rc = check_launch();
     if (rc) return rc;
@@ -797,6 +810,7 @@ int32_t hp_job_create(hp_ctx* ctx, const hp_job_desc* d, hp_job** out) {
     add(&J.wl, 4 * (size_t)N); add(&J.rhol, 4 * (size_t)N);
     add(&J.shf, 4 * 3 * (size_t)S);
     add(&J.fco, 4 * 8 * (size_t)S);
+    add(&J.rdist, 8 * (size_t)A * N);
   }
   // GISA: per-atom QP matrices, precomputed once (they depend only on exponents)
   int qp_total = 0;
@@ -1083,7 +1097,7 @@ int32_t hp_step(hp_ctx* ctx, hp_job* const* jobs, int32_t njobs, int32_t* n_live
       const hp_job* h = g[0];
       if (h->desc.scheme == j->desc.scheme && h->dev.solver == j->dev.solver &&
           h->dev.mixed == j->dev.mixed && h->dev.tc == j->dev.tc &&
-          h->dev.local == j->dev.local) {
+          h->dev.local == j->dev.local && h->dev.fuse == j->dev.fuse) {
         g.push_back(j);
         placed = true;
         break;

@@ -45,7 +45,7 @@ constexpr int kRowsA = kTcM / kTcWarps;     // A rows staged per warp
 constexpr int kRowsB = kTcNMax / kTcWarps;  // B rows staged per warp (at most)
 constexpr int kTcCols = 256;    // tensor-memory columns (FP32 accumulator, N <= 256)
 constexpr long long kWaitLimit = 1ll << 26;
-constexpr int kT1Rows = 256;    // single-pass form (k_glisa_hess_tc1) up to this many shells
+constexpr int kT1Rows = kTcSinglePassShells;  // single-pass form (k_glisa_hess_tc1)
 
 // shared-memory layout (offsets from a 1024-byte-aligned base): two stages
 // of (A_hi, A_lo, B_hi, B_lo), then the stages' mbarriers and the TMEM slot
@@ -467,8 +467,9 @@ __global__ void __launch_bounds__(kTcThreads) k_glisa_hess_tc1(Batch bt) {
   __syncthreads();
 
   // epilogue: warp w reads tensor-memory lanes 32 (w % 4) .. + 31; the four
-  // warps of a lane quarter take every fourth 8-column chunk
-  double* out = J.hpart + (size_t)split * M * M;
+  // warps of a lane quarter take every fourth 8-column chunk; the split's
+  // partial is the packed lower triangle in FP32 (the accumulator's format)
+  float* out = reinterpret_cast<float*>(J.hpart) + (size_t)split * (M * (M + 1) / 2);
   const int quad = warp & 3;
   const bool ok = nblocks > 0 && !timed_out;
   for (int part = 0; part < 2; ++part) {
@@ -493,9 +494,9 @@ __global__ void __launch_bounds__(kTcThreads) k_glisa_hess_tc1(Batch bt) {
         for (int q = 0; q < 8; ++q) {
           const int j = part * kTcM + c + q;
           if (j >= M) continue;
-          const double h = (double)__uint_as_float(v[q]);
-          if (j <= i) out[(size_t)i * M + j] = h;
-          else if (part == 0 && j >= kTcM) out[(size_t)j * M + i] = h;  // H[j][i], j below row 128
+          const float h = __uint_as_float(v[q]);
+          if (j <= i) out[i * (i + 1) / 2 + j] = h;
+          else if (part == 0 && j >= kTcM) out[j * (j + 1) / 2 + i] = h;  // H[j][i], j below row 128
         }
       }
     }

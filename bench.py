@@ -126,7 +126,8 @@ POLISH = True
 # capture of the same workload (ncu --set full; the summaries in profiles/
 # give the commands). Keyed by (workload, precision, kernel family).
 NCU_TRAFFIC = {
-    ("glisa-c6h10n2o2", "mixed", "k_glisa_hess_tc"): 365.12e6 + 3.32e6,
+    ("glisa-c6h10n2o2", "mixed", "k_glisa_hess_tc1"): 365.34e6 + 3.81e6,
+    ("glisa-c6h10n2o2", "mixed", "k_glisa_fused_ff<1>"): 734.05e6 + 22.20e6,
     ("mbis-chain60", "mixed", "inner"): 125.81e6 + 3.46e6,
 }
 
@@ -489,21 +490,47 @@ def run_ours(args):
         nshell = config_of(w, args, args.precision)["nshell"]
         per_launch_s = hess_ms / hess_n / 1000.0
         if args.precision == "mixed":
-            # algorithmic work of H = G diag(d) G^T: 2 M^2 N FLOP per launch,
-            # against cuBLAS's TF32 GEMM rate measured in this process
+            # the two single kernels of a tensor-core gLISA step; the roofline
+            # line is the one with more time in the profiled step
+            cands = {}
+            # Hessian: algorithmic work of H = G diag(d) G^T, 2 M^2 N FLOP per
+            # launch, against cuBLAS's TF32 GEMM rate measured in this process
             flops = 2.0 * nshell * nshell * mol.npoint
             achieved = flops / per_launch_s / 1e12
             tf32 = measure_tf32_peak()
-            roofline = {"kernel": "k_glisa_hess_tc", "bound": "tensor", "achieved": achieved,
-                        "peak": tf32, "unit": "TFLOP/s", "frac": achieved / tf32,
-                        "traffic": NCU_TRAFFIC.get((w["name"], args.precision, "k_glisa_hess_tc")),
-                        "algorithmic_bytes_per_launch": (nshell + 1) * mol.npoint * 4.0,
-                        "peak_source": "measured: cuBLAS TF32 GEMM 8192^3, this run",
-                        "bf16_peak_measured": peaks.get("bf16_tflops"),
-                        "ms_per_launch": per_launch_s * 1000.0,
-                        "algorithmic_flop_per_launch": flops,
-                        "note": "3 TF32 MMAs per product (hi*hi, hi*lo, lo*hi); "
-                                "shells padded to 128 x 256 tiles"}
+            hk = "k_glisa_hess_tc1" if nshell <= 256 else "k_glisa_hess_tc"
+            cands["hess"] = (hess_ms, {
+                "kernel": hk, "bound": "tensor", "achieved": achieved,
+                "peak": tf32, "unit": "TFLOP/s", "frac": achieved / tf32,
+                "traffic": NCU_TRAFFIC.get((w["name"], args.precision, hk)),
+                "algorithmic_bytes_per_launch": (nshell + 1) * mol.npoint * 4.0,
+                "peak_source": "measured: cuBLAS TF32 GEMM 8192^3, this run",
+                "bf16_peak_measured": peaks.get("bf16_tflops"),
+                "ms_per_launch": per_launch_s * 1000.0,
+                "algorithmic_flop_per_launch": flops,
+                "note": "3 TF32 MMAs per product (hi*hi, hi*lo, lo*hi); MMA area "
+                        "128 x (N1 + N2) per 32-point block"})
+            pro_ms, pro_n = fam_ms["glisa_pro"]
+            if pro_n and nshell <= 192:
+                # fused promolecule + gradient (+ change) pass: G's two float
+                # planes once (8 S bytes per point), rho and w read, dvec1,
+                # dvec2, d1 pair, rho0 and sqrt(d2) written (36 bytes)
+                p_s = pro_ms / pro_n / 1000.0
+                alg = mol.npoint * (8.0 * nshell + 16.0 + 36.0)
+                ach = alg / p_s / 1e9
+                cands["pro"] = (pro_ms, {
+                    "kernel": "k_glisa_fused_ff<1>", "bound": "hbm", "achieved": ach,
+                    "peak": hbm_peak, "unit": "GB/s", "frac": ach / hbm_peak,
+                    "traffic": NCU_TRAFFIC.get((w["name"], args.precision, "k_glisa_fused_ff<1>")),
+                    "peak_source": "measured" if peaks else "fallback",
+                    "ms_per_launch": p_s * 1000.0, "algorithmic_bytes_per_launch": alg})
+            fam = max(cands, key=lambda k: cands[k][0])
+            roofline = cands[fam][1]
+            others = {k: v[1] for k, v in cands.items() if k != fam}
+            if others:
+                roofline["other_kernels"] = {v["kernel"]: {
+                    "achieved": v["achieved"], "unit": v["unit"], "frac": v["frac"],
+                    "ms_per_launch": v["ms_per_launch"]} for v in others.values()}
         else:
             alg_bytes = (nshell + 1) * mol.npoint * 8.0  # G and w rho/rho0^2 once
             achieved = alg_bytes / per_launch_s / 1e9

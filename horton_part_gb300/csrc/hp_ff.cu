@@ -337,6 +337,13 @@ __global__ void __launch_bounds__(kThreads) k_glisa_basis_ff(Batch bt) {
   const JobDev& J = decode_local_ff(bt, blk);
   const int p = blk * kThreads + threadIdx.x;
   if (p >= J.npoint) return;
+  if (J.wrf) {  // w rho and rho as float pairs for the fused passes
+    const double rho = J.rho[p], wr = J.w[p] * rho;
+    float4 q;
+    split(wr, &q.x, &q.y);
+    split(rho, &q.z, &q.w);
+    J.wrf[p] = q;
+  }
   for (int a = 0; a < J.natom; ++a) {
     const f2 d2 = dist2_ff(J, p, a);
     const f2 r = d2.hi > 0.0f ? ffa::sqrt_ff(d2) : f2{0.0f, 0.0f};

@@ -48,6 +48,12 @@ __device__ __forceinline__ void dot2_merge(Dot2& a, const Dot2& b) {
 
 __device__ __forceinline__ double dot2_value(const Dot2& a) { return (double)a.s + (double)a.c; }
 
+// a < c for a normalised float pair a and the float pair c of a double
+// (lexicographic: the double comparison except within ~1e-14 of c).
+__device__ __forceinline__ bool below(ffa::f2 a, float2 c) {
+  return a.hi < c.x || (a.hi == c.x && a.lo < c.y);
+}
+
 // The compensated sum as a normalised float pair.
 __device__ __forceinline__ ffa::f2 dot2_ff(const Dot2& a) { return ffa::two_sum(a.s, a.c); }
 
@@ -314,17 +320,20 @@ __global__ void __launch_bounds__(kThreads) k_glisa_trials_ff(Batch bt) {
 // all S shells, double-buffered with cp.async); per sub-tile
 //   A  u(p) = sum_m G[m][p] x[m]: warp w sums the shells m = w (mod 8) for
 //      the 32 points (lane = point), two chains per lane;
-//   A' warp 0 merges the eight partial sums in a fixed order and forms the
-//      per-point v(p) as a float pair;
+//   A' every warp merges the eight partial sums in the same fixed order and
+//      forms v(p) as a float pair for itself (no barrier before B); the
+//      sub-tile's owner warp (sub mod 8) also writes the per-point outputs;
 //   B  gpart[m] += sum_p G[m][p] v(p): warp w owns rows w, w + 8, ...; the
 //      lanes' compensated sums stay in registers across the tile and are
 //      reduced once at its end.
+// No FP64 arithmetic per point: w rho and rho come as float pairs (wrf, set
+// once per job), the outputs are float pairs.
 // MODE 0 (refinement product): x = delta, v = (w rho / rho0^2) u.
-// MODE 1 (promolecule + gradient): x = c, u = rho0, the outputs of
-//   k_glisa_pro_ff with the quotients in float-float, v = w rho / rho0; the
-//   entropy terms w rho ln(rho / rho0) are formed every 256 points by all
-//   threads (one point each) with ln from logf plus one Newton step on
-//   exp_ff (error ~ the square of logf's). With with_change, also
+// MODE 1 (promolecule + gradient): x = c, u = rho0 (r0f), d2 = w rho / rho0^2
+//   (d2f) and sqrt(d2) (hess_s), v = w rho / rho0, quotients in float-float;
+//   the owner also forms the entropy terms w rho ln(rho / rho0), ln from
+//   logf plus one Newton step on exp_ff (error ~ the square of logf's), and
+//   counts the points below negative_cutoff. With with_change, also
 //   C  the outer change of the step that produced c (glisa.py:776 via
 //      compute_change): warp w takes the atoms a = w (mod 8), lane = point,
 //      sum_{m in a} (c - c_old)_m g_m as a compensated sum from the staged
@@ -338,14 +347,12 @@ constexpr int kFuseThreads = 256;
 constexpr int kFuseWarps = kFuseThreads / 32;
 constexpr int kFuseSP = 32;                             // points per sub-tile (one per lane)
 constexpr int kFuseRows = kFuseMaxShells / kFuseWarps;  // rows per warp in B
-constexpr int kFuseGroup = kFuseThreads / kFuseSP;      // sub-tiles per entropy pass
 
 // Shared memory of a fused pass for S shells (bytes).
 __host__ __device__ constexpr size_t fuse_smem_bytes(int S) {
   return 4 * (size_t)S * kFuseSP * 4          // two stages of both planes
          + 16 * (size_t)S                     // x and the parameter change as float pairs
          + 8 * (size_t)kFuseWarps * kFuseSP   // partial sums
-         + 8 * (size_t)kFuseSP                // v
          + 512                                // exp table
          + 8 * (2 * kFuseWarps + 2);          // block sums
 }
@@ -394,9 +401,9 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_fused_ff(Batch bt, in
   float2* xv = reinterpret_cast<float2*>(stg + 4 * plane);
   float2* dcv = xv + S;
   Dot2* part = reinterpret_cast<Dot2*>(dcv + S);
-  float2* vs = reinterpret_cast<float2*>(part + kFuseWarps * kFuseSP);
-  float2* tab = vs + kFuseSP;
+  float2* tab = reinterpret_cast<float2*>(part + kFuseWarps * kFuseSP);
   double* red = reinterpret_cast<double*>(tab + 64);
+  const float2 cutp = split2(J.density_cutoff), negp = split2(J.negative_cutoff);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int p0 = tile * J.tile_points;
   const int p1 = min(p0 + J.tile_points, J.npoint);
@@ -438,78 +445,60 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_fused_ff(Batch bt, in
       dot2_merge(d, e);
       part[warp * kFuseSP + lane] = d;
     }
-    __syncthreads();
-    if (warp == 0) {  // A'
-      Dot2 d = part[lane];
+    __syncthreads();  // partial sums visible
+    // A': every warp merges the eight partial sums (the same fixed order) and
+    // forms v for the sub-tile's points itself; warp sub % 8 (the owner) also
+    // writes the per-point outputs and, MODE 1, the entropy terms
+    Dot2 du = part[lane];
 #pragma unroll
-      for (int q = 1; q < kFuseWarps; ++q) dot2_merge(d, part[q * kFuseSP + lane]);
-      const int p = p0 + sub * kFuseSP + lane;
-      float2 v = make_float2(0.f, 0.f);
-      if (p < p1) {
-        if (MODE == 0) {
-          const float2 d2 = split2(J.dvec2[p]);
-          const f2 h = ffa::mul(dot2_ff(d), f2{d2.x, d2.y});
-          v = make_float2(h.hi, h.lo);
-        } else {
-          const f2 r0 = dot2_ff(d);
-          const double rho0 = ffa::to_double(r0);
-          const double rho = J.rho[p], w = J.w[p];
-          const bool sick = (rho < J.density_cutoff) || (rho0 < J.density_cutoff);
-          f2 d1{0.f, 0.f}, dd{0.f, 0.f};
-          if (!sick) {
-            const float2 wr = split2(w * rho);
-            d1 = ffa::div(f2{wr.x, wr.y}, r0);
-            dd = ffa::div(d1, r0);
-          }
-          J.dvec1[p] = ffa::to_double(d1);
-          J.dvec2[p] = ffa::to_double(dd);
-          J.d1f[p] = make_float2(d1.hi, d1.lo);
-          J.rho0[p] = rho0;
+    for (int q = 1; q < kFuseWarps; ++q) dot2_merge(du, part[q * kFuseSP + lane]);
+    const int p = p0 + sub * kFuseSP + lane;
+    const bool owner = warp == (sub & (kFuseWarps - 1));
+    f2 v{0.f, 0.f};
+    if (p < p1) {
+      if (MODE == 0) {
+        const float2 d2 = J.d2f[p];
+        v = ffa::mul(dot2_ff(du), f2{d2.x, d2.y});
+      } else {
+        const f2 r0 = dot2_ff(du);
+        const float4 q = J.wrf[p];  // (w rho) and rho as float pairs
+        const bool sick = below(f2{q.z, q.w}, cutp) || below(r0, cutp);
+        if (!sick) v = ffa::div(f2{q.x, q.y}, r0);
+        if (owner) {
+          const f2 dd = sick ? f2{0.f, 0.f} : ffa::div(v, r0);
+          J.r0f[p] = make_float2(r0.hi, r0.lo);
+          J.d2f[p] = make_float2(dd.hi, dd.lo);
           J.hess_s[p] = sqrtf(dd.hi);
-          if (rho0 < J.negative_cutoff) nneg += 1.0f;
-          v = make_float2(d1.hi, d1.lo);
+          if (below(r0, negp)) nneg += 1.0f;
+          if (!sick) {  // w rho ln(rho / rho0)
+            const f2 ratio = ffa::div(f2{q.z, q.w}, r0);
+            const float l0 = logf(ratio.hi);
+            const f2 e = ffa::exp_ff(f2{-l0, 0.f}, tab);
+            const f2 l = ffa::add(ffa::add(ffa::mul(ratio, e), -1.0f), l0);
+            ent = ffa::add(ent, ffa::mul(f2{q.x, q.y}, l));
+          }
         }
       }
-      vs[lane] = v;
     }
-    __syncthreads();
     {  // B
-      const float2 v = vs[lane];
 #pragma unroll
       for (int r = 0; r < kFuseRows; ++r) {
         const int m = warp + kFuseWarps * r;
-        if (m < S) dot2_add(acc[r], gh[m * kFuseSP + lane], gl[m * kFuseSP + lane], v.x, v.y);
+        if (m < S) dot2_add(acc[r], gh[m * kFuseSP + lane], gl[m * kFuseSP + lane], v.hi, v.lo);
       }
     }
     if (chg) {  // C
-      const int p = p0 + sub * kFuseSP + lane;
       const float wf = p < p1 ? (float)J.w[p] : 0.0f;
       for (int a = warp; a < J.natom; a += kFuseWarps) {
         Dot2 d{0.f, 0.f};
         for (int m = J.shell_off[a]; m < J.shell_off[a + 1]; ++m)
           dot2_add(d, gh[m * kFuseSP + lane], gl[m * kFuseSP + lane], dcv[m].x, dcv[m].y);
-        const float v = d.s + d.c;
-        const float term = wf * v * v;
+        const float dv = d.s + d.c;
+        const float term = wf * dv * dv;
         const float t = ch + term;
         const float bb = t - ch;
         cl += (ch - (t - bb)) + (term - bb);
         ch = t;
-      }
-    }
-    if (MODE == 1 && (sub % kFuseGroup == kFuseGroup - 1 || sub == nsub - 1)) {
-      // entropy terms of the group's points, one per thread (rho0 was
-      // written by warp 0 before the last barrier)
-      const int p = p0 + (sub - sub % kFuseGroup) * kFuseSP + threadIdx.x;
-      if (p < p1 && threadIdx.x < (sub % kFuseGroup + 1) * kFuseSP) {
-        const double rho = J.rho[p], rho0 = J.rho0[p];
-        if (!((rho < J.density_cutoff) || (rho0 < J.density_cutoff))) {
-          const float2 rp = split2(rho), r0 = split2(rho0), wr = split2(J.w[p] * rho);
-          const f2 ratio = ffa::div(f2{rp.x, rp.y}, f2{r0.x, r0.y});
-          const float l0 = logf(ratio.hi);
-          const f2 e = ffa::exp_ff(f2{-l0, 0.f}, tab);
-          const f2 l = ffa::add(ffa::add(ffa::mul(ratio, e), -1.0f), l0);
-          ent = ffa::add(ent, ffa::mul(f2{wr.x, wr.y}, l));
-        }
       }
     }
   }
@@ -596,8 +585,7 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_trials_fused(Batch bt
   int kt = 0;  // clipped shells with t_m > t: a prefix of the list (sorted, largest first)
   while (kt < nclip && tm[kt] > t) ++kt;
   const float4* cd = reinterpret_cast<const float4*>(J.clipf);
-  const double cut = J.density_cutoff;
-  const float2 cutp = split2(cut);
+  const float2 cutp = split2(J.density_cutoff);
   float ah = 0.0f, al = 0.0f;
   for (int sub = 0; sub < nsub; ++sub) {
     const float* gh = stg + (sub & 1) * 2 * plane;
@@ -638,19 +626,22 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_trials_fused(Batch bt
       }
       const f2 dsd = dot2_ff(sd);
       const f2 corr = ffa::neg(ffa::add(dot2_ff(sc), f2{at * dsd.hi, at * dsd.lo}));
-      const double rho = J.rho[p], w = J.w[p], r0 = J.rho0[p];
-      const bool rs = rho < cut;
-      const bool h0 = !(rs || r0 < cut);
-      const float2 r0p = split2(r0);
+      const float2 r0p = J.r0f[p];
+      const float4 q = J.wrf[p];  // (w rho) and rho as float pairs
+      const bool rs = below(f2{q.z, q.w}, cutp);
+      const bool h0 = !(rs || below(f2{r0p.x, r0p.y}, cutp));
       const f2 dr = ffa::add(f2{at * u.hi, at * u.lo}, corr);
       const f2 rt = ffa::add(dr, f2{r0p.x, r0p.y});
-      const bool below = rt.hi < cutp.x || (rt.hi == cutp.x && rt.lo < cutp.y);
-      const bool ht = !(rs || below);
+      const bool ht = !(rs || below(rt, cutp));
       double big = 0.0;
       float term = 0.0f;
-      if (h0 && ht) term = -(float)(w * rho) * log1pf(dr.hi / r0p.x);
-      else if (ht) big = w * rho * log(rho / ffa::to_double(rt));
-      else if (h0) big = -(w * rho * log(rho / r0));
+      if (h0 && ht) {
+        term = -q.x * log1pf(dr.hi / r0p.x);
+      } else if (ht || h0) {  // the sick status changes: FP64 logs (few points)
+        const double wr = (double)q.x + (double)q.y, rho = (double)q.z + (double)q.w;
+        if (ht) big = wr * log(rho / ffa::to_double(rt));
+        else big = -(wr * log(rho / ((double)r0p.x + (double)r0p.y)));
+      }
       if (big != 0.0) {
         const float bh = (float)big;
         term = bh;

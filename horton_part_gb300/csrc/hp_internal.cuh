@@ -161,6 +161,10 @@ struct JobDev {
   float* gmat_lo;         // gLISA, gff: low part of G [nshell][npoint] (gmat is not stored)
   float* clipf;           // gLISA, gff: clipped shells' (c hi, c lo, delta hi, delta lo) [nshell]
   float2* rdist;          // mixed / ff (MBIS, GISA, aLISA): point-atom distances as float pairs [natom][npoint]
+  float4* wrf;            // fused gLISA: (w rho hi, lo, rho hi, lo) per point (constant)
+  float2* r0f;            // fused gLISA: rho0 as float pairs [npoint]
+  float2* d2f;            // fused gLISA: w rho / rho0^2 as float pairs [npoint]
+  double* hsum;           // gLISA tensor-core Hessian: refinement product H delta [nshell]
   float2* d1f;            // gLISA, gff: w rho / rho0 as float pairs, npoint
   float2* hvf;            // gLISA, gff: the refinement's hvec as float pairs, npoint
   float* hess_s;          // gLISA tensor-core Hessian: sqrt(w rho / rho0^2) as FP32, npoint

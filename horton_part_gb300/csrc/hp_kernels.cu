@@ -1186,9 +1186,17 @@ __global__ void __launch_bounds__(kThreads) k_glisa_reduce(Batch bt) {
       while (i * (i + 1) / 2 > e) --i;
       while ((i + 1) * (i + 2) / 2 <= e) ++i;
       const int j = e - i * (i + 1) / 2;
-      const float* hp = reinterpret_cast<const float*>(J.hpart);
-      double s = 0.0;
-      for (int sp = 0; sp < J.nsplit; ++sp) s += (double)hp[(size_t)sp * E + e];
+      const float* hp = reinterpret_cast<const float*>(J.hpart) + e;
+      double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;  // four chains, fixed combination
+      int sp = 0;
+      for (; sp + 3 < J.nsplit; sp += 4) {
+        s0 += (double)hp[(size_t)sp * E];
+        s1 += (double)hp[(size_t)(sp + 1) * E];
+        s2 += (double)hp[(size_t)(sp + 2) * E];
+        s3 += (double)hp[(size_t)(sp + 3) * E];
+      }
+      for (; sp < J.nsplit; ++sp) s0 += (double)hp[(size_t)sp * E];
+      const double s = (s0 + s1) + (s2 + s3);
       J.hess[(size_t)i * M + j] = s;
       J.hess[(size_t)j * M + i] = s;
     }
@@ -1201,10 +1209,24 @@ __global__ void __launch_bounds__(kThreads) k_glisa_reduce(Batch bt) {
       J.hess[(size_t)j * M + i] = s;
     }
   }
-  if (e < M) {
-    double s = 0.0;
-    for (int t = 0; t < J.ntile; ++t) s += J.gpart[(size_t)e * J.ntile + t];
-    J.grad[e] = -s;  // df_i = -int rho g_i / rho0 (glisa.py:452-455)
+  // gradient rows: one warp per row, lanes over tiles (four chains, fixed order)
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nblk = (M * M + kThreads - 1) / kThreads;  // this job's K_SQUARE blocks
+  for (int m = local * kWarps + warp; m < M; m += nblk * kWarps) {
+    const double* gp = J.gpart + (size_t)m * J.ntile;
+    double h0 = 0.0, h1 = 0.0, h2 = 0.0, h3 = 0.0;
+    int t = lane;
+    for (; t + 96 < J.ntile; t += 128) {
+      h0 += gp[t];
+      h1 += gp[t + 32];
+      h2 += gp[t + 64];
+      h3 += gp[t + 96];
+    }
+    for (; t < J.ntile; t += 32) h0 += gp[t];
+    double h = (h0 + h1) + (h2 + h3);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) h += __shfl_xor_sync(0xffffffffu, h, o);
+    if (lane == 0) J.grad[m] = -h;  // df_i = -int rho g_i / rho0 (glisa.py:452-455)
   }
 }
 
@@ -1303,6 +1325,10 @@ __device__ void chol_solve_block(const double* L, const double* dinv, int n, dou
   __syncthreads();
 }
 
+// Largest free set whose FP32 factor, 1 / diagonal and right-hand side fit
+// the Newton step's 200 KB of dynamic shared memory.
+constexpr int kNewtonF32Max = 224;
+
 // chol_factor in FP32, for the factor of the tensor-core Hessian: that
 // matrix carries ~1e-7 relative error already, so an FP32 factor is as good a
 // preconditioner for the FP64-residual refinement as an FP64 one (same
@@ -1359,26 +1385,54 @@ __device__ void chol_factor_f(float* L, int n, int* bad, float* colbuf, float* d
   }
 }
 
-// y <- (L L^T)^-1 y by one warp, everything in shared memory (L as left by
-// chol_factor_f): forward with the columns of L (contiguous in the upper
-// copy), backward with its rows; one warp barrier per column.
-__device__ void chol_solve_warp_f(const float* L, const float* dinv, int n, float* y) {
+// y <- (L L^T)^-1 y by one warp (L as left by chol_factor_f, in shared
+// memory): the vector lives in registers, element i in lane i % 32, slot
+// i / 32; each column's pivot value is broadcast by a shuffle, so a column
+// costs one shuffle and a few FMAs, no barrier. Forward with the columns of
+// L (contiguous in the upper copy), backward with its rows. n <= 32 kSolveSlots.
+constexpr int kSolveSlots = (kNewtonF32Max + 31) / 32;
+__device__ void chol_solve_warp_f(const float* L, const float* dinv, int n, float* yio) {
   const int lane = threadIdx.x & 31;
+  float y[kSolveSlots];
+#pragma unroll
+  for (int s = 0; s < kSolveSlots; ++s) {
+    const int i = s * 32 + lane;
+    y[s] = i < n ? yio[i] : 0.0f;
+  }
   for (int j = 0; j < n; ++j) {
-    const float zj = y[j] * dinv[j];
+    const int sj = j >> 5;
+    float yj = 0.0f;
+#pragma unroll
+    for (int s = 0; s < kSolveSlots; ++s)
+      if (s == sj) yj = y[s];
+    const float zj = __shfl_sync(0xffffffffu, yj, j & 31) * dinv[j];
     const float* col = L + (size_t)j * n;  // L[i][j] = col[i], i > j
-    for (int i = j + 1 + lane; i < n; i += 32) y[i] = fmaf(-col[i], zj, y[i]);
-    __syncwarp();
-    if (lane == 0) y[j] = zj;
-    __syncwarp();
+#pragma unroll
+    for (int s = 0; s < kSolveSlots; ++s) {
+      const int i = s * 32 + lane;
+      if (i > j && i < n) y[s] = fmaf(-col[i], zj, y[s]);
+      else if (i == j) y[s] = zj;
+    }
   }
   for (int j = n - 1; j >= 0; --j) {
-    const float xj = y[j] * dinv[j];
+    const int sj = j >> 5;
+    float yj = 0.0f;
+#pragma unroll
+    for (int s = 0; s < kSolveSlots; ++s)
+      if (s == sj) yj = y[s];
+    const float xj = __shfl_sync(0xffffffffu, yj, j & 31) * dinv[j];
     const float* row = L + (size_t)j * n;  // L[j][i], i < j
-    for (int i = lane; i < j; i += 32) y[i] = fmaf(-row[i], xj, y[i]);
-    __syncwarp();
-    if (lane == 0) y[j] = xj;
-    __syncwarp();
+#pragma unroll
+    for (int s = 0; s < kSolveSlots; ++s) {
+      const int i = s * 32 + lane;
+      if (i < j) y[s] = fmaf(-row[i], xj, y[s]);
+      else if (i == j) y[s] = xj;
+    }
+  }
+#pragma unroll
+  for (int s = 0; s < kSolveSlots; ++s) {
+    const int i = s * 32 + lane;
+    if (i < n) yio[i] = y[s];
   }
 }
 
@@ -1387,14 +1441,16 @@ __device__ void chol_solve_warp_f(const float* L, const float* dinv, int n, floa
 constexpr int kNewtonSmemL = 200 * 1024;
 constexpr int kNewtonColMax = 256;
 // FP32 factor in shared memory (factor, 1 / diagonal and the right-hand side)
-constexpr int kNewtonF32Max = 224;
+// the step runs on one SM; 32 warps keep more rows of each column step in flight
+constexpr int kNewtonThreads = 1024;
+constexpr int kNewtonWarps = kNewtonThreads / 32;
 static_assert(4 * (kNewtonF32Max * kNewtonF32Max + 2 * kNewtonF32Max) <= kNewtonSmemL, "FP32 factor");
 
-__global__ void __launch_bounds__(kThreads) k_glisa_newton_step(Batch bt, int projected) {
+__global__ void __launch_bounds__(kNewtonThreads) k_glisa_newton_step(Batch bt, int projected) {
   extern __shared__ double l_smem[];
   __shared__ double col_smem[2 * kNewtonColMax];
   __shared__ int bad;
-  __shared__ int wcount[kWarps];
+  __shared__ int wcount[kNewtonWarps];
   __shared__ int fid[kNewtonF32Max];
   int local;
   const JobDev& J = decode_local(bt, local);
@@ -1402,7 +1458,7 @@ __global__ void __launch_bounds__(kThreads) k_glisa_newton_step(Batch bt, int pr
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   // free set in shell order: per-warp ballots and a prefix over the warps
   int nf = 0;
-  for (int base = 0; base < M; base += kThreads) {
+  for (int base = 0; base < M; base += kNewtonThreads) {
     const int m = base + threadIdx.x;
     bool f = false;
     if (m < M) f = !projected || J.propars[m] > 0.0 || 1.0 + J.grad[m] < 0.0;
@@ -1410,7 +1466,7 @@ __global__ void __launch_bounds__(kThreads) k_glisa_newton_step(Batch bt, int pr
     if (lane == 0) wcount[warp] = __popc(b);
     __syncthreads();
     int off = nf, total = nf;
-    for (int w = 0; w < kWarps; ++w) {
+    for (int w = 0; w < kNewtonWarps; ++w) {
       if (w < warp) off += wcount[w];
       total += wcount[w];
     }
@@ -1434,21 +1490,21 @@ __global__ void __launch_bounds__(kThreads) k_glisa_newton_step(Batch bt, int pr
     float* Lf = reinterpret_cast<float*>(l_smem);
     float* dv = Lf + nf * nf;
     float* yv = dv + nf;
-    for (int i = warp; i < nf; i += kWarps) {  // lower triangle (all the factor reads)
+    for (int i = warp; i < nf; i += kNewtonWarps) {  // lower triangle (all the factor reads)
       const double* hrow = J.hess + (size_t)fid[i] * M;
       for (int j = lane; j <= i; j += 32) Lf[i * nf + j] = (float)hrow[fid[j]];
     }
-    for (int m = threadIdx.x; m < M; m += kThreads) J.delta[m] = 0.0;
+    for (int m = threadIdx.x; m < M; m += kNewtonThreads) J.delta[m] = 0.0;
     __syncthreads();
     chol_factor_f(Lf, nf, &bad, reinterpret_cast<float*>(col_smem), dv);
     if (!bad) {
-      for (int i = threadIdx.x; i < nf; i += kThreads) yv[i] = (float)(-(1.0 + J.grad[fid[i]]));
+      for (int i = threadIdx.x; i < nf; i += kNewtonThreads) yv[i] = (float)(-(1.0 + J.grad[fid[i]]));
       __syncthreads();
       if (threadIdx.x < 32) chol_solve_warp_f(Lf, dv, nf, yv);
       __syncthreads();
-      for (int i = threadIdx.x; i < nf; i += kThreads) J.delta[fid[i]] = (double)yv[i];
+      for (int i = threadIdx.x; i < nf; i += kNewtonThreads) J.delta[fid[i]] = (double)yv[i];
       float* keep = reinterpret_cast<float*>(J.chol);
-      for (int e = threadIdx.x; e < nf * nf + nf; e += kThreads) keep[e] = Lf[e];
+      for (int e = threadIdx.x; e < nf * nf + nf; e += kNewtonThreads) keep[e] = Lf[e];
       if (threadIdx.x == 0) J.freeidx[M + 1] = 1;
       return;
     }
@@ -1460,11 +1516,11 @@ __global__ void __launch_bounds__(kThreads) k_glisa_newton_step(Batch bt, int pr
   if (threadIdx.x == 0) J.freeidx[M + 1] = 0;
   const bool l_in_smem = (size_t)nf * nf * sizeof(double) <= (size_t)kNewtonSmemL;
   double* L = l_in_smem ? l_smem : J.chol;
-  for (int e = threadIdx.x; e < nf * nf; e += kThreads) {
+  for (int e = threadIdx.x; e < nf * nf; e += kNewtonThreads) {
     const int i = e / nf, j = e % nf;
     L[e] = J.hess[(size_t)J.freeidx[i] * M + J.freeidx[j]];
   }
-  for (int m = threadIdx.x; m < M; m += kThreads) J.delta[m] = 0.0;
+  for (int m = threadIdx.x; m < M; m += kNewtonThreads) J.delta[m] = 0.0;
   __syncthreads();
   // column buffers in shared memory when they fit, else in ctrial (kTrials x
   // nshell, free until the trial set); 1 / diag(L) at ctrial[2 nshell, 3 nshell)
@@ -1472,13 +1528,13 @@ __global__ void __launch_bounds__(kThreads) k_glisa_newton_step(Batch bt, int pr
   double* colbuf = nf <= kNewtonColMax ? col_smem : J.ctrial;
   chol_factor(L, nf, &bad, colbuf, J.ctrial + 2 * M);
   double* y = J.keep;  // scratch (the m-newton mask is formed after the step)
-  for (int i = threadIdx.x; i < nf; i += kThreads) y[i] = -(1.0 + J.grad[J.freeidx[i]]);
+  for (int i = threadIdx.x; i < nf; i += kNewtonThreads) y[i] = -(1.0 + J.grad[J.freeidx[i]]);
   __syncthreads();
   chol_solve_block(L, J.ctrial + 2 * M, nf, y);
-  for (int i = threadIdx.x; i < nf; i += kThreads) J.delta[J.freeidx[i]] = y[i];
+  for (int i = threadIdx.x; i < nf; i += kNewtonThreads) J.delta[J.freeidx[i]] = y[i];
   if (threadIdx.x == 0 && bad) atomicOr(&J.mail->i[MI_ERR], E_SINGULAR);
   if (l_in_smem)  // the refinement steps read the factor from chol
-    for (int e = threadIdx.x; e < nf * nf; e += kThreads) J.chol[e] = L[e];
+    for (int e = threadIdx.x; e < nf * nf; e += kNewtonThreads) J.chol[e] = L[e];
 }
 
 // Hessian-vector product with the exact FP64 Hessian, first half:
@@ -1495,6 +1551,33 @@ __global__ void __launch_bounds__(kThreads) k_glisa_hv(Batch bt) {
   J.hvec[p] = J.dvec2[p] * u;
 }
 
+// Row sums of the per-tile partials: hsum[m] = sum over tiles of gpart[m]
+// (the exact product H delta of the refinement), one warp per row, lanes over
+// tiles in four chains combined in a fixed order; many blocks, so the sums
+// leave the one-block refinement kernel.
+__global__ void __launch_bounds__(kThreads) k_glisa_gsum(Batch bt) {
+  int local;
+  const JobDev& J = decode_local(bt, local);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nblk = (J.nshell * J.nshell + kThreads - 1) / kThreads;  // this job's K_SQUARE blocks
+  for (int m = local * kWarps + warp; m < J.nshell; m += nblk * kWarps) {
+    const double* gp = J.gpart + (size_t)m * J.ntile;
+    double h0 = 0.0, h1 = 0.0, h2 = 0.0, h3 = 0.0;
+    int t = lane;
+    for (; t + 96 < J.ntile; t += 128) {
+      h0 += gp[t];
+      h1 += gp[t + 32];
+      h2 += gp[t + 64];
+      h3 += gp[t + 96];
+    }
+    for (; t < J.ntile; t += 32) h0 += gp[t];
+    double h = (h0 + h1) + (h2 + h3);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) h += __shfl_xor_sync(0xffffffffu, h, o);
+    if (lane == 0) J.hsum[m] = h;
+  }
+}
+
 // One step of iterative refinement of the Newton system on the free set:
 // r = (-1 - df)_F - (H delta)_F with the exact FP64 product, then
 // delta_F += (L L^T)^-1 r with the factor of the (tensor-core) Hessian.
@@ -1507,22 +1590,11 @@ __global__ void __launch_bounds__(kThreads) k_glisa_refine(Batch bt) {
   const bool f32 = J.freeidx[M + 1] != 0;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   double* r = J.keep;
-  for (int i = warp; i < nf; i += kWarps) {  // one warp per row, lanes over tiles
+  (void)lane;
+  (void)warp;
+  for (int i = threadIdx.x; i < nf; i += kThreads) {  // H delta rows from k_glisa_gsum
     const int m = J.freeidx[i];
-    const double* gp = J.gpart + (size_t)m * J.ntile;
-    double h0 = 0.0, h1 = 0.0, h2 = 0.0, h3 = 0.0;  // four chains, combined in a fixed order
-    int t = lane;
-    for (; t + 96 < J.ntile; t += 128) {
-      h0 += gp[t];
-      h1 += gp[t + 32];
-      h2 += gp[t + 64];
-      h3 += gp[t + 96];
-    }
-    for (; t < J.ntile; t += 32) h0 += gp[t];
-    double hd = (h0 + h1) + (h2 + h3);
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) hd += __shfl_xor_sync(0xffffffffu, hd, o);
-    if (lane == 0) r[i] = -(1.0 + J.grad[m]) - hd;
+    r[i] = -(1.0 + J.grad[m]) - J.hsum[m];
   }
   __syncthreads();
   if (f32) {  // FP32 factor of k_glisa_newton_step: copy it in, one warp solves
@@ -1981,7 +2053,7 @@ void launch_glisa_solve(const HostBatch& hb, cudaStream_t st, int projected) {
     configured_device = dev;
   }
   if (hb.blocks[K_JOB] > 0) {
-    k_glisa_newton_step<<<hb.blocks[K_JOB], kThreads, kNewtonSmemL, st>>>(hb.b[K_JOB], projected);
+    k_glisa_newton_step<<<hb.blocks[K_JOB], kNewtonThreads, kNewtonSmemL, st>>>(hb.b[K_JOB], projected);
     ++g_launch_count;
   }
 }
@@ -1994,6 +2066,7 @@ void launch_glisa_refine(const HostBatch& hb, cudaStream_t st, int gff, int fuse
     HP_LAUNCH(k_glisa_hv, K_POINT1, kThreads);
     HP_LAUNCH(k_glisa_grad, K_POINT, kThreads, 1);
   }
+  HP_LAUNCH(k_glisa_gsum, K_SQUARE, kThreads);  // K_SQUARE: ceil(M^2 / 256) >= ceil(M / 8) blocks
   if (hb.blocks[K_JOB] > 0) {  // dynamic shared memory: the FP32 factor (set up by launch_glisa_solve)
     k_glisa_refine<<<hb.blocks[K_JOB], kThreads, kNewtonSmemL, st>>>(hb.b[K_JOB]);
     ++g_launch_count;

@@ -859,11 +859,17 @@ int32_t hp_job_create(hp_ctx* ctx, const hp_job_desc* d, hp_job** out) {
     add(&J.clip, 4 * (size_t)(2 * S + 1));
     add(&J.rho0, 8 * (size_t)N);
     if (tc) {
+      add(&J.hsum, 8 * (size_t)S);
       add(&J.gmat32, 4 * (size_t)S * N);
       add(&J.hess_s, 4 * (size_t)N);
       if (gff) {
         add(&J.gmat_lo, 4 * (size_t)S * N);
         add(&J.clipf, 4 * 4 * (size_t)S);
+        if (S <= kFuseMaxShells) {
+          add(&J.wrf, 16 * (size_t)N);
+          add(&J.r0f, 8 * (size_t)N);
+          add(&J.d2f, 8 * (size_t)N);
+        }
         add(&J.d1f, 8 * (size_t)N);
         add(&J.hvf, 8 * (size_t)N);
       } else {

@@ -453,6 +453,9 @@ void launch_final_atweights_mx(const HostBatch& hb, cudaStream_t st, int model, 
 // MBIS on atom grids (hp_local.cu)
 void launch_mbis_local(const HostBatch& hb, cudaStream_t st);  // spherical averages + radial inner solve
 void launch_change_radial(const HostBatch& hb, cudaStream_t st);
+void launch_gisa_local(const HostBatch& hb, cudaStream_t st);     // spherical averages + radial moments
+void launch_lisa_sc_local(const HostBatch& hb, cudaStream_t st);  // spherical averages + radial sc solve
+void launch_gisa_qp(const HostBatch& hb, cudaStream_t st);        // k_gisa_qp alone
 
 // float-float MBIS (hp_ff.cu)
 void launch_promol_ff(const HostBatch& hb, cudaStream_t st);

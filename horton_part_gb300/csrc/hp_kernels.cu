@@ -1967,6 +1967,8 @@ void launch_promol(const HostBatch& hb, cudaStream_t st, int mixed, int model) {
   HP_LAUNCH(k_atweights, K_ATOM_TILE, kThreads);
 }
 
+void launch_gisa_qp(const HostBatch& hb, cudaStream_t st) { HP_LAUNCH(k_gisa_qp, K_ATOM, 32); }
+
 void launch_atweights(const HostBatch& hb, cudaStream_t st) {
   HP_LAUNCH(k_atweights, K_ATOM_TILE, kThreads);
 }

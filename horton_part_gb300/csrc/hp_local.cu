@@ -1,4 +1,6 @@
-// MBIS on atom grids (grid_type 1): the reference's class default.
+// Atom grids (grid_type 1): the reference's class default. MBIS, GISA and
+// aLISA (sc) update each atom on its radial grid; gLISA only measures its
+// change there.
 //
 // The promolecule and the at_weights are formed on the molecular grid as for
 // grid_type 2/3 (core/stockholder.py:352-384). Each atom then works on its
@@ -45,6 +47,11 @@ __device__ __forceinline__ double rhoa_value(const JobDev& J, int a, int p) {
 __device__ __forceinline__ void put_atom_partial(const JobDev& J, int a, int q, double v) {
   double* slot = J.apart + ((size_t)a * J.qa + q) * J.ntile;
   for (int t = threadIdx.x; t < J.ntile; t += blockDim.x) store_partial(J, slot + t, t == 0 ? v : 0.0);
+}
+
+// Unit-population shell s of a basis scheme at distance r (core/basis.py:161).
+__device__ __forceinline__ double radial_shell(const JobDev& J, int s, double r) {
+  return basis_shell<double>(J.sh_order[s], J.sh_alpha[s], J.sh_pref[s], r);
 }
 
 constexpr int kLocalMaxRad = 1024;  // radial nodes per atom
@@ -155,27 +162,133 @@ __global__ void __launch_bounds__(kThreads) k_mbis_radial(Batch bt) {
   }
 }
 
-// Outer change on the radial grids: sum_i 4 pi r_i^2 w_i (pro_new - pro_old)^2.
+// Outer change on the radial grids: sum_i 4 pi r_i^2 w_i (pro_new - pro_old)^2
+// (MBIS: Slater shells of both parameter sets; basis schemes: the parameter
+// differences times the unit-population shells at the nodes).
 __global__ void __launch_bounds__(kThreads) k_change_radial(Batch bt) {
   __shared__ double red[kWarps];
   int a;
   const JobDev& J = decode_atom_lc(bt, a);
   const int r0 = J.rad_off[a], nrad = J.rad_off[a + 1] - r0;
-  const int nsh = J.shell_off[a + 1] - J.shell_off[a];
+  const int s0 = J.shell_off[a], nsh = J.shell_off[a + 1] - s0;
   const double* pn = J.propars + J.par_off[a];
   const double* po = J.propars_old + J.par_off[a];
+  const bool mbis = J.scheme == SCHEME_MBIS;
   double acc = 0.0;
   for (int i = threadIdx.x; i < nrad; i += kThreads) {
     const double r = J.rad_r[r0 + i];
     double d = 0.0;
     for (int k = 0; k < nsh; ++k) {
-      d += pn[2 * k] * pn[2 * k + 1] * pn[2 * k + 1] * pn[2 * k + 1] * exp(-pn[2 * k + 1] * r) * kInv8Pi;
-      d -= po[2 * k] * po[2 * k + 1] * po[2 * k + 1] * po[2 * k + 1] * exp(-po[2 * k + 1] * r) * kInv8Pi;
+      if (mbis) {
+        d += pn[2 * k] * pn[2 * k + 1] * pn[2 * k + 1] * pn[2 * k + 1] * exp(-pn[2 * k + 1] * r) * kInv8Pi;
+        d -= po[2 * k] * po[2 * k + 1] * po[2 * k + 1] * po[2 * k + 1] * exp(-po[2 * k + 1] * r) * kInv8Pi;
+      } else {
+        d += (pn[k] - po[k]) * radial_shell(J, s0 + k, r);
+      }
     }
     acc += 4.0 * M_PI * r * r * J.rad_w[r0 + i] * d * d;
   }
   const double s = block_sum1(acc, red);
   put_atom_partial(J, a, QA_CHANGE, s);
+}
+
+// GISA on atom grids (gisa.py:281-318): the quadratic program's moments
+// q_k = sum_i 4 pi r_i^2 w_i g_k(r_i) rho_sph(r_i) and the population from
+// the spherical average on the atom's radial grid, into tile 0 of the
+// partials k_gisa_qp reads (one block per atom).
+__global__ void __launch_bounds__(kThreads) k_basis_radial_qvec(Batch bt) {
+  __shared__ double red[kWarps * (kMaxShells + 1)];
+  __shared__ double out[kMaxShells + 1];
+  int a;
+  const JobDev& J = decode_atom_lc(bt, a);
+  const int r0 = J.rad_off[a], nrad = J.rad_off[a + 1] - r0;
+  const int s0 = J.shell_off[a], nsh = J.shell_off[a + 1] - s0;
+  double acc[kMaxShells + 1];
+#pragma unroll
+  for (int q = 0; q <= kMaxShells; ++q) acc[q] = 0.0;
+  for (int i = threadIdx.x; i < nrad; i += kThreads) {
+    const double r = J.rad_r[r0 + i];
+    const double wr = 4.0 * M_PI * r * r * J.rad_w[r0 + i] * J.radrho[r0 + i];
+#pragma unroll
+    for (int k = 0; k < kMaxShells; ++k)
+      if (k < nsh) acc[k] += wr * radial_shell(J, s0 + k, r);
+    acc[kMaxShells] += wr;
+  }
+  block_sum<kMaxShells + 1>(acc, red, out);
+  for (int k = 0; k < nsh; ++k) put_atom_partial(J, a, QA_INNER + k, out[k]);
+  put_atom_partial(J, a, QA_POP, out[kMaxShells]);
+}
+
+// aLISA self-consistent solver on atom grids (alisa.py:193-291 on the
+// spherical average, gisa.py:281-318): every inner iteration of one atom in
+// one block, c_k <- sum_i 4 pi r_i^2 w_i c_k g_k(r_i) rho_sph / pro until the
+// radial change of the pro-atom is below the inner threshold; population
+// for the charges.
+__global__ void __launch_bounds__(kThreads) k_lisa_sc_radial(Batch bt) {
+  __shared__ double red[kWarps * (kMaxShells + 1)];
+  __shared__ double out[kMaxShells + 1];
+  __shared__ double par[kMaxShells];
+  __shared__ int done_s;
+  int a;
+  const JobDev& J = decode_atom_lc(bt, a);
+  const int r0 = J.rad_off[a], nrad = J.rad_off[a + 1] - r0;
+  const int s0 = J.shell_off[a], nsh = J.shell_off[a + 1] - s0;
+  double* pa = J.propars + J.par_off[a];
+  if (threadIdx.x < nsh) par[threadIdx.x] = pa[threadIdx.x];
+  if (threadIdx.x == 0) done_s = 0;
+  constexpr int kPer = kLocalMaxRad / kThreads;
+  double rr[kPer], ww[kPer], rh[kPer], oldpro[kPer];
+  double pop = 0.0;
+#pragma unroll
+  for (int q = 0; q < kPer; ++q) {
+    const int i = threadIdx.x + q * kThreads;
+    const bool in = i < nrad;
+    rr[q] = in ? J.rad_r[r0 + i] : 1.0;
+    ww[q] = in ? 4.0 * M_PI * rr[q] * rr[q] * J.rad_w[r0 + i] : 0.0;
+    rh[q] = in ? J.radrho[r0 + i] : 0.0;
+    oldpro[q] = 0.0;
+    pop += ww[q] * rh[q];
+  }
+  {
+    double acc1[1] = {pop};
+    block_sum<1>(acc1, red, out);
+    put_atom_partial(J, a, QA_POP, out[0]);
+  }
+  __syncthreads();
+  int it = 0;
+  for (; it < J.inner_maxiter; ++it) {
+    double acc[kMaxShells + 1];
+#pragma unroll
+    for (int q = 0; q <= kMaxShells; ++q) acc[q] = 0.0;
+#pragma unroll
+    for (int q = 0; q < kPer; ++q) {
+      double pro = 0.0;
+      for (int k = 0; k < nsh; ++k) pro += par[k] * radial_shell(J, s0 + k, rr[q]);
+      const bool sick = (rh[q] < J.density_cutoff) || (pro < J.density_cutoff);
+      const double ratio = sick ? 0.0 : rh[q] / pro;
+      const double wr = ww[q] * ratio;
+#pragma unroll
+      for (int k = 0; k < kMaxShells; ++k)
+        if (k < nsh) acc[k] += wr * par[k] * radial_shell(J, s0 + k, rr[q]);
+      const double e = oldpro[q] - pro;
+      acc[kMaxShells] += ww[q] * e * e;
+      oldpro[q] = pro;
+    }
+    block_sum<kMaxShells + 1>(acc, red, out);
+    if (threadIdx.x == 0) {
+      for (int k = 0; k < nsh; ++k) par[k] = out[k];
+      const double change = it == 0 ? 1e100 : sqrt(out[kMaxShells]);
+      done_s = change < J.inner_threshold;
+    }
+    __syncthreads();
+    if (done_s) break;
+  }
+  if (threadIdx.x < nsh) pa[threadIdx.x] = par[threadIdx.x];
+  if (threadIdx.x == 0) {
+    const bool conv = it < J.inner_maxiter;
+    atomicAdd(&J.mail->d[MD_INNER_TOTAL], (double)(conv ? it + 1 : J.inner_maxiter));
+    if (!conv) atomicOr(&J.mail->i[MI_WARN], W_INNER);
+  }
 }
 
 #define HP_LAUNCH_LC(kernel, kind, threads, ...)                                       \
@@ -193,6 +306,16 @@ void launch_mbis_local(const HostBatch& hb, cudaStream_t st) {
 
 void launch_change_radial(const HostBatch& hb, cudaStream_t st) {
   HP_LAUNCH_LC(k_change_radial, K_ATOM, kThreads);
+}
+
+void launch_gisa_local(const HostBatch& hb, cudaStream_t st) {
+  HP_LAUNCH_LC(k_sph_avg, K_ATOM, kThreads);
+  HP_LAUNCH_LC(k_basis_radial_qvec, K_ATOM, kThreads);
+}
+
+void launch_lisa_sc_local(const HostBatch& hb, cudaStream_t st) {
+  HP_LAUNCH_LC(k_sph_avg, K_ATOM, kThreads);
+  HP_LAUNCH_LC(k_lisa_sc_radial, K_ATOM, kThreads);
 }
 
 }  // namespace hp

@@ -310,11 +310,20 @@ int step_iterstock(hp_ctx* ctx, const std::vector<hp_job*>& jobs, const HostBatc
       break;
     case HP_SCHEME_GISA: {
       ProfScope ps(ctx, HP_KERNEL_INNER);
-      launch_gisa(hb, st, mixed);
+      if (local) {  // moments on the radial grids, the same quadratic program
+        launch_gisa_local(hb, st);
+        launch_gisa_qp(hb, st);
+      } else {
+        launch_gisa(hb, st, mixed);
+      }
       break;
     }
     case HP_SCHEME_LISA:
-      if (j0->dev.solver == SOLVER_SC)
+      if (local) {  // atom grids: every inner iteration of every atom in one launch
+        ProfScope ps(ctx, HP_KERNEL_INNER);
+        launch_inner_init(hb, st);
+        launch_lisa_sc_local(hb, st);
+      } else if (j0->dev.solver == SOLVER_SC)
         rc = run_inner(ctx, jobs, hb, [&] {
           ProfScope ps(ctx, HP_KERNEL_INNER);
           launch_lisa_sc_inner(hb, st, mixed);
@@ -351,7 +360,7 @@ int step_iterstock(hp_ctx* ctx, const std::vector<hp_job*>& jobs, const HostBatc
     const double a = (double)j->dev.natom;
     const double inner_evals = j->desc.scheme == HP_SCHEME_GISA ? a : inner;
     if (j->dev.local)  // promolecule on the molecular grid; inner and change on the radial grids
-      j->evals += n * a + (inner + 2.0 * a) * (double)j->dev.nrad / a;
+      j->evals += n * a + (inner_evals + 2.0 * a) * (double)j->dev.nrad / a;
     else
       j->evals += n * (3.0 * a + inner_evals);
     if (j->dev.mixed != PH_FP32 && j->desc.precision == HP_PRECISION_MIXED) j->polish_iters += 1;
@@ -485,10 +494,15 @@ int step_glisa(hp_ctx* ctx, const std::vector<hp_job*>& jobs, const HostBatch& h
       }
     }
   }
+  const bool local = jobs[0]->dev.local != 0;  // atom grids: the change is radial
   if (fused) {  // next iteration's promolecule and gradient, this step's change
     ProfScope ps(ctx, HP_KERNEL_GLISA_PRO);
-    launch_glisa_fused_ff(hb, st, 1, fuse_shells, 1);
-  } else {
+    launch_glisa_fused_ff(hb, st, 1, fuse_shells, local ? 0 : 1);
+  }
+  if (local) {
+    ProfScope ps(ctx, HP_KERNEL_CHANGE);
+    launch_change_radial(hb, st);
+  } else if (!fused) {
     ProfScope ps(ctx, HP_KERNEL_CHANGE);
     if (gff) launch_glisa_change_ff(hb, st);
     else launch_glisa_change(hb, st);
@@ -587,8 +601,9 @@ int validate(const hp_job_desc* d) {
   if (d->grid_type != 1 && d->grid_type != 2 && d->grid_type != 3)
     return fail(HP_ERR_INVALID, "grid_type must be 1, 2 or 3");
   if (d->grid_type == 1) {
-    if (d->scheme != HP_SCHEME_MBIS)
-      return fail(HP_ERR_UNSUPPORTED, "grid_type 1 (atom grids) is available for MBIS");
+    if (d->scheme == HP_SCHEME_LISA && d->solver != HP_SOLVER_DEFAULT && d->solver != HP_SOLVER_SC)
+      return fail(HP_ERR_UNSUPPORTED,
+                  "grid_type 1 (atom grids) for aLISA is available with the sc solver");
     if (!d->radial_offsets || !d->shell_point_offsets || !d->point_sphere_weights ||
         !d->radial_points || !d->radial_weights || d->nrad <= 0)
       return fail(HP_ERR_INVALID, "grid_type 1 needs the atom-grid arrays");

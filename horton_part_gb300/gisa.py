@@ -64,6 +64,9 @@ class GaussianISAWPart(GPUStockholderWPart):
 
     name = "gisa"
     _scheme = "gisa"
+    # grid_type 1: the update works on the spherical averages on the radial
+    # grids (aLISA: the sc solver)
+    _supports_atom_grids = True
 
     def __init__(self, coordinates, numbers, pseudo_numbers, grid, moldens, spindens=None, lmax=3,
                  logger=None, threshold=1e-6, maxiter=500, inner_threshold=1e-8,

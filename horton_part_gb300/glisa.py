@@ -30,6 +30,7 @@ _SOLVERS = {"newton": "newton", "m-newton": "m-newton", "sc": "sc", "cvxopt": "p
 class GlobalLinearISAWPart(GPUStockholderWPart):
     name = "glisa"
     _scheme = "glisa"
+    _supports_atom_grids = True  # grid_type 1: the change is measured on the radial grids
     _has_charge_history = False
     _dumps_change = False
 

@@ -335,13 +335,13 @@ class GPUStockholderWPart(WPart):
         pass
 
     # -- the partitioning ------------------------------------------------------
-    _supports_atom_grids = False  # grid_type 1 on the GPU (MBIS)
+    _supports_atom_grids = False  # grid_type 1 on the GPU (set by the scheme classes)
 
     def _check_grid_type(self):
         if not self.on_molgrid and not self._supports_atom_grids:
             raise NotImplementedError(
-                "grid_type=1 (spherical averages on the atomic radial grids) is available for MBIS "
-                "on the GPU path; use grid_type=2 or 3 (molecular grid)")
+                "grid_type=1 (spherical averages on the atomic radial grids) is available for "
+                "MBIS, GISA, aLISA (sc) and gLISA on the GPU path; use grid_type=2 or 3")
 
     def _make_job(self):
         from .molgrid import atom_grid_arrays

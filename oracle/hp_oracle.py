@@ -430,10 +430,35 @@ def lisa_solver_newton(bs_funcs, rho, propars, weights, threshold, mode="exact",
 # ---------------------------------------------------------------------------
 
 
+def _radial_view(local, a, bs_orders=None, bs_exponents=None):
+    """Atom a's radial nodes, the weights 4 pi r^2 w_r and (optionally) its
+    unit-population shells at the nodes (``gisa.py:91-106`` with
+    ``rgrid.points``; ``gisa.py:281-318``)."""
+    ra = np.asarray(local["rpoints"][a], dtype=float)
+    wa = 4 * np.pi * ra**2 * np.asarray(local["rweights"][a], dtype=float)
+    g = None if bs_orders is None else basis_functions(bs_orders, bs_exponents, ra)
+    return ra, wa, g
+
+
+def _local_average(local, a, values):
+    """Spherical average of ``values`` (molecular-grid array) over atom a's
+    own points (``gisa.py:283-289``, ``mbis.py:174-187``)."""
+    own = slice(local["indices"][a], local["indices"][a + 1])
+    return spherical_average(values[own], local["shell"][own], local["wsph"][own],
+                             len(local["rpoints"][a]))
+
+
 def basis_scheme(scheme, coordinates, numbers, pseudo_numbers, points, weights, rho, orders,
                  exponents, initials, threshold=1e-6, maxiter=500, inner_threshold=1e-8,
-                 solver="sc", density_cutoff=DENSITY_CUTOFF, negative_cutoff=NEGATIVE_CUTOFF):
-    """GISA (``scheme='gisa'``) or aLISA (``scheme='lisa'``) on the molecular grid.
+                 solver="sc", density_cutoff=DENSITY_CUTOFF, negative_cutoff=NEGATIVE_CUTOFF,
+                 local=None):
+    """GISA (``scheme='gisa'``) or aLISA (``scheme='lisa'``) on the molecular grid,
+    or with ``local`` (the atom-grid description of ``mbis``) on atom grids
+    (grid_type 1): each atom's update works on the spherical average of its
+    AIM density over its radial grid with the shells evaluated at the radial
+    nodes and the weights 4 pi r^2 w_r, the charges are radial integrals, and
+    the change is the radial integral of the squared pro-atom difference
+    (``gisa.py:281-318``, ``core/iterstock.py:32-45``).
 
     ``orders/exponents/initials`` are per-atom lists of arrays.
     """
@@ -441,6 +466,7 @@ def basis_scheme(scheme, coordinates, numbers, pseudo_numbers, points, weights, 
     inner = inner_threshold if inner_threshold < threshold else threshold
     rs = radial_distances(points, coordinates)
     bs = [basis_functions(orders[a], exponents[a], rs[a]) for a in range(natom)]
+    rad = [_radial_view(local, a, orders[a], exponents[a]) for a in range(natom)] if local else None
     ranges = np.concatenate([[0], np.cumsum([len(e) for e in exponents])])
     propars = init_basis_propars(initials, pseudo_numbers, weights, rho)
     res = dict(history_propars=[], history_charges=[], history_entropies=[], history_changes=[],
@@ -454,34 +480,39 @@ def basis_scheme(scheme, coordinates, numbers, pseudo_numbers, points, weights, 
         promol, at_weights = stockholder_weights(pros)
         its = []
         for a in range(natom):
-            rhoa = at_weights[a] * rho
             sl = slice(ranges[a], ranges[a + 1])
+            if local is None:
+                rhoa, wa, ga = at_weights[a] * rho, weights, bs[a]
+            else:
+                _, wa, ga = rad[a]
+                rhoa = _local_average(local, a, at_weights[a] * rho)
             if scheme == "gisa":
-                propars[sl] = gisa_qp(bs[a], rhoa, weights, exponents[a])
+                propars[sl] = gisa_qp(ga, rhoa, wa, exponents[a])
                 its.append(1)
             elif solver == "sc":
-                new, nit = lisa_solver_sc(bs[a], rhoa, propars[sl].copy(), weights, inner,
+                new, nit = lisa_solver_sc(ga, rhoa, propars[sl].copy(), wa, inner,
                                           density_cutoff)
                 propars[sl] = new
                 its.append(nit)
             elif solver in ("newton", "m-newton"):
                 new, nit = lisa_solver_newton(
-                    bs[a], rhoa, propars[sl].copy(), weights, inner,
+                    ga, rhoa, propars[sl].copy(), wa, inner,
                     mode="exact" if solver == "newton" else "modified",
                     density_cutoff=density_cutoff, negative_cutoff=negative_cutoff)
                 propars[sl] = new
                 its.append(nit)
             else:
                 raise NotImplementedError(solver)
-            charges[a] = pseudo_numbers[a] - integrate(weights, rhoa)
+            charges[a] = pseudo_numbers[a] - integrate(wa, rhoa)
         res["inner_iterations"].append(its)
         res["history_propars"].append(propars.copy())
         res["history_charges"].append(charges.copy())
         res["history_entropies"].append(entropy(weights, rho, promol, density_cutoff))
         msd = 0.0
         for a in range(natom):
-            d = (propars[ranges[a]:ranges[a + 1]] - old[ranges[a]:ranges[a + 1]]) @ bs[a]
-            msd += integrate(weights, d, d)
+            ga, wa = (bs[a], weights) if local is None else (rad[a][2], rad[a][1])
+            d = (propars[ranges[a]:ranges[a + 1]] - old[ranges[a]:ranges[a + 1]]) @ ga
+            msd += integrate(wa, d, d)
         change = np.sqrt(msd)
         res["history_changes"].append(change)
         if change < threshold or counter >= maxiter:
@@ -511,9 +542,13 @@ def _fix_propars(exp_array, propars, delta):
 def glisa(coordinates, numbers, pseudo_numbers, points, weights, rho, orders, exponents,
           initials, threshold=1e-6, maxiter=100, solver="newton",
           density_cutoff=DENSITY_CUTOFF, negative_cutoff=NEGATIVE_CUTOFF, linspace_size=40,
-          tau=1.0):
+          tau=1.0, local=None):
     """gLISA on the molecular grid (``glisa.py:248-281``) with the ``newton``,
-    ``m-newton`` (``glisa.py:617-803``) or ``sc`` (``glisa.py:805-879``) solver."""
+    ``m-newton`` (``glisa.py:617-803``) or ``sc`` (``glisa.py:805-879``) solver.
+    With ``local`` (grid_type 1) only the change differs: it is the radial
+    integral of the squared pro-atom difference on each atom's radial grid
+    (``glisa.py:166-168`` through ``core/iterstock.py:32-45``); the solver
+    works on the molecular grid for every grid type (``glisa.py:257-270``)."""
     from scipy.linalg import solve
 
     natom = len(numbers)
@@ -524,11 +559,18 @@ def glisa(coordinates, numbers, pseudo_numbers, points, weights, rho, orders, ex
     pop = integrate(weights, rho)
     res = dict(history_propars=[], history_charges=[], history_entropies=[], history_changes=[])
 
+    rad = ([_radial_view(local, a, orders[a], exponents[a]) for a in range(natom)]
+           if local else None)
+
     def change_of(p1, p2):
         msd = 0.0
         for a in range(natom):
-            d = (p1[ranges[a]:ranges[a + 1]] - p2[ranges[a]:ranges[a + 1]]) @ G[ranges[a]:ranges[a + 1]]
-            msd += integrate(weights, d, d)
+            if local is None:
+                ga, wa = G[ranges[a]:ranges[a + 1]], weights
+            else:
+                ga, wa = rad[a][2], rad[a][1]
+            d = (p1[ranges[a]:ranges[a + 1]] - p2[ranges[a]:ranges[a + 1]]) @ ga
+            msd += integrate(wa, d, d)
         return np.sqrt(msd)
 
     def promol_valid(p):

@@ -29,6 +29,20 @@ CASES = {
                                        kwargs=dict(threshold=1e-8, solver="m-newton")),
     "glisa_sc_h2o_50x110": dict(scheme="glisa", mol=("water", 50, 110),
                                 kwargs=dict(threshold=1e-8, solver="sc")),
+    # atom grids (grid_type 1, the reference's class default): H2O, 30 radial
+    # x Lebedev-50 per atom
+    # GISA's QP amplifies the last-bit differences of the reference's
+    # spherical averages (a cubic spline evaluated at its own knots) to ~1e-9
+    # in the parameters, so this case compares at looser tolerances
+    "gisa_h2o_local_30x50": dict(scheme="gisa", mol=("water", 30, 50), local=True,
+                                 kwargs=dict(threshold=1e-8, inner_threshold=1e-8,
+                                             solver="quadprog"),
+                                 tol=dict(charges=1e-8, propars=1e-7, changes=1e-9, entropies=1e-6)),
+    "lisa_sc_h2o_local_30x50": dict(scheme="lisa", mol=("water", 30, 50), local=True,
+                                    kwargs=dict(threshold=1e-8, inner_threshold=1e-8,
+                                                solver="sc")),
+    "glisa_newton_h2o_local_30x50": dict(scheme="glisa", mol=("water", 30, 50), local=True,
+                                         kwargs=dict(threshold=1e-8, solver="newton")),
 }
 
 
@@ -42,4 +56,28 @@ def build_inputs(case):
         mol = synthetic.chain_molecule(counts, nrad, nang, seed=seed)
     else:
         raise ValueError(kind)
-    return mol, dict(case["kwargs"])
+    kwargs = dict(case["kwargs"])
+    if case.get("local"):
+        kwargs["local"] = local_description(mol, case["mol"][2])
+    return mol, kwargs
+
+
+def local_description(mol, nang):
+    """The atom-grid description (grid_type 1) of a synthetic molecule's grid:
+    per atom its points' range (``indices``), radial nodes and weights, and
+    per point its radial-shell index within its atom grid and its angular
+    weight / 4 pi, plus the Lebedev size ``nang``."""
+    import numpy as np
+
+    from horton_part_gb300.molgrid import atom_grid_arrays
+
+    arr = atom_grid_arrays(mol.grid)
+    roff, spo = arr["radial_offsets"], arr["shell_point_offsets"]
+    na = len(roff) - 1
+    shell = np.repeat(np.arange(len(spo) - 1), np.diff(spo))
+    return dict(indices=np.asarray(mol.grid.indices),
+                rpoints=[arr["radial_points"][roff[a]:roff[a + 1]] for a in range(na)],
+                rweights=[arr["radial_weights"][roff[a]:roff[a + 1]] for a in range(na)],
+                shell=shell - np.repeat(roff[:-1], np.diff(roff))[shell],
+                wsph=arr["point_sphere_weights"], nang=nang)
+

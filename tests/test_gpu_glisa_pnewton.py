@@ -98,3 +98,28 @@ def test_tensor_core_hessian_with_newton(gpu_context):
           f"max|dq| {dq:.2e}, max|dp| {dp:.2e}")
     assert dq < 1e-8
     assert dp < 1e-7
+
+
+def test_tensor_core_hessian_on_atom_grids(gpu_context):
+    """grid_type 1 (the reference's class default): the change is measured on
+    the radial grids (glisa.py:166-168); the tensor-core form with the fused
+    passes against the reference's own result on the same input."""
+    import os
+    import sys
+
+    sys.path.insert(0, os.path.join(os.path.dirname(__file__), "golden"))
+    from cases import CASES, build_inputs
+
+    name = "glisa_newton_h2o_local_30x50"
+    with np.load(os.path.join(os.path.dirname(__file__), "golden", f"{name}.npz")) as f:
+        g = {k: f[k] for k in f.files}
+    mol, kwargs = build_inputs(CASES[name])
+    kwargs.pop("local")
+    part = wpart_schemes("glisa")(mol.coordinates, mol.numbers, mol.pseudo_numbers, mol.grid,
+                                  mol.density, grid_type=1, precision="mixed", **kwargs)
+    part.do_partitioning()
+    dq = np.abs(part["charges"] - g["charges"]).max()
+    print(f"glisa atom grids, tensor core: niter {part['niter']} (reference {int(g['niter'])}), "
+          f"max|dq| {dq:.2e}")
+    assert part["niter"] == int(g["niter"])
+    assert dq < 1e-8

@@ -48,9 +48,10 @@ def test_mixed_precision_within_bar(name, gpu_context):
     with np.load(os.path.join(GOLDEN, f"{name}.npz")) as f:
         g = {k: f[k] for k in f.files}
     mol, kwargs = build_inputs(case)
+    grid_type = 1 if kwargs.pop("local", None) is not None else 3
     part = wpart_schemes(case["scheme"])(mol.coordinates, mol.numbers, mol.pseudo_numbers,
-                                         mol.grid, mol.density, grid_type=3, precision="mixed",
-                                         **kwargs)
+                                         mol.grid, mol.density, grid_type=grid_type,
+                                         precision="mixed", **kwargs)
     with warnings.catch_warnings():
         warnings.simplefilter("ignore")
         part.do_partitioning()

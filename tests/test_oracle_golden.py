@@ -63,11 +63,15 @@ def test_oracle_matches_reference_golden(name):
     with warnings.catch_warnings():
         warnings.simplefilter("ignore")
         res = run_oracle(case, mol, kwargs)
+    tol = case.get("tol", {})
     assert int(res["niter"]) == int(g["niter"])
-    np.testing.assert_allclose(res["charges"], g["charges"], rtol=0, atol=1e-10)
-    np.testing.assert_allclose(res["propars"], g["propars"], rtol=1e-9, atol=1e-12)
-    np.testing.assert_allclose(res["history_changes"], g["history_changes"], rtol=1e-6, atol=1e-14)
-    np.testing.assert_allclose(res["history_entropies"], g["history_entropies"], rtol=1e-9,
+    np.testing.assert_allclose(res["charges"], g["charges"], rtol=0, atol=tol.get("charges", 1e-10))
+    np.testing.assert_allclose(res["propars"], g["propars"], rtol=tol.get("propars", 1e-9),
+                               atol=1e-12)
+    np.testing.assert_allclose(res["history_changes"], g["history_changes"], rtol=1e-6,
+                               atol=tol.get("changes", 1e-14))
+    np.testing.assert_allclose(res["history_entropies"], g["history_entropies"],
+                               rtol=tol.get("entropies", 1e-9),
                                atol=1e-12)
     if "core_charges" in g:
         np.testing.assert_allclose(res["core_charges"], g["core_charges"], atol=1e-10)

@@ -21,7 +21,7 @@ LIB_PATH = os.path.join(_HERE, "libhpgpu.so")
 HP_OK, HP_ERR_INVALID, HP_ERR_NO_MEMORY, HP_ERR_NOT_CONVERGED = 0, 1, 2, 3
 HP_ERR_NUMERIC, HP_ERR_TIMEOUT, HP_ERR_CUDA, HP_ERR_UNSUPPORTED, HP_ERR_STATE = 4, 5, 6, 7, 8
 
-SCHEMES = {"mbis": 0, "gisa": 1, "lisa": 2, "glisa": 3}
+SCHEMES = {"mbis": 0, "gisa": 1, "lisa": 2, "glisa": 3, "nlis": 4}
 SOLVERS = {"default": 0, "sc": 1, "newton": 2, "m-newton": 3, "quadprog": 4, "qp": 4,
            "pnewton": 5}
 PRECISIONS = {"fp64": 0, "mixed": 1, "ff": 2}

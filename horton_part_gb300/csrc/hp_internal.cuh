@@ -83,11 +83,11 @@ enum ErrFlag {
 
 enum WarnFlag { W_INNER = 1, W_POPULATION = 2, W_NEG_PARS = 4 };
 
-enum Scheme { SCHEME_MBIS = 0, SCHEME_GISA = 1, SCHEME_LISA = 2, SCHEME_GLISA = 3 };
+enum Scheme { SCHEME_MBIS = 0, SCHEME_GISA = 1, SCHEME_LISA = 2, SCHEME_GLISA = 3, SCHEME_NLIS = 4 };
 enum Solver { SOLVER_DEFAULT = 0, SOLVER_SC = 1, SOLVER_NEWTON = 2, SOLVER_M_NEWTON = 3,
               SOLVER_QP = 4, SOLVER_PNEWTON = 5 };
 constexpr int kTrials = 8;  // projected-Newton step lengths 2^-t evaluated per pass
-enum Model { MODEL_MBIS = 0, MODEL_BASIS = 1 };
+enum Model { MODEL_MBIS = 0, MODEL_BASIS = 1, MODEL_NLIS = 2 };
 // Evaluation phase of a job (JobDev::mixed): FP64, FP32 with compensated sums,
 // or float-float (MBIS).
 enum Phase { PH_FP64 = 0, PH_FP32 = 1, PH_FF = 2 };
@@ -360,6 +360,18 @@ __device__ __forceinline__ T basis_shell(T order, T alpha, T pref, T r) {
   return pref * dexp(-alpha * rn);
 }
 
+// NLIS / GMBIS shell with population N: N n S^(3/n) exp(-S r^n) / (4 pi
+// Gamma(3/n)) (nlis.py:148, 298); n = 1 is MBIS's Slater shell.
+__device__ __forceinline__ double nlis_shell(double N, double S, double n, double r) {
+  const double rn = n == 1.0 ? r : n == 2.0 ? r * r : pow(r, n);
+  return N * n * pow(S, 3.0 / n) * exp(-S * rn) / (4.0 * M_PI * tgamma(3.0 / n));
+}
+
+// r^n for an NLIS shell order.
+__device__ __forceinline__ double nlis_rn(double n, double r) {
+  return n == 1.0 ? r : n == 2.0 ? r * r : pow(r, n);
+}
+
 }  // namespace hp
 
 namespace hp {
@@ -391,6 +403,8 @@ void launch_charges(const HostBatch& hb, cudaStream_t st);
 void launch_inner_init(const HostBatch& hb, cudaStream_t st);
 void launch_count_active(const HostBatch& hb, cudaStream_t st);
 void launch_mbis_inner(const HostBatch& hb, cudaStream_t st, int mixed);
+void launch_nlis_inner(const HostBatch& hb, cudaStream_t st);  // NLIS / GMBIS, FP64
+void launch_nlis_local(const HostBatch& hb, cudaStream_t st);  // spherical averages + radial solve
 void launch_gisa(const HostBatch& hb, cudaStream_t st, int mixed);
 void launch_lisa_sc_inner(const HostBatch& hb, cudaStream_t st, int mixed);
 void launch_lisa_newton_inner(const HostBatch& hb, cudaStream_t st, int mixed, int modified);

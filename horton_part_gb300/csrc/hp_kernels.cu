@@ -97,6 +97,9 @@ __device__ __forceinline__ T proatom(const JobDev& J, int a, const double* par, 
   T y = (T)0;
   if (MODEL == MODEL_MBIS) {
     for (int k = 0; k < s1 - s0; ++k) y += slater_shell<T>((T)pa[2 * k], (T)pa[2 * k + 1], r);
+  } else if (MODEL == MODEL_NLIS) {
+    for (int k = 0; k < s1 - s0; ++k)
+      y += (T)nlis_shell(pa[3 * k], pa[3 * k + 1], pa[3 * k + 2], (double)r);
   } else {
     for (int k = 0; k < s1 - s0; ++k) y += (T)pa[k] * basis_val<T>(J, s0 + k, p, r);
   }
@@ -449,6 +452,112 @@ __global__ void __launch_bounds__(kThreads) k_mbis_inner(Batch bt) {
 }
 
 // One warp per atom: N_k <- m0_k, S_k <- 3 m0_k / m1_k, convergence test.
+// NLIS / GMBIS inner iteration (nlis.py:99-195), per (atom, tile): with the
+// unit shells u_k = n S^(3/n) exp(-S r^n) / (4 pi Gamma(3/n)) (prefactors
+// formed once per block) and t_k = N_k u_k: m0_k = int w t_k rho_a / pro,
+// m1_k = int w u_k (rho_a / pro) r^n_k (the reference's m1, without N_k), and
+// int w (oldpro - pro)^2 for the inner change. FP64.
+__global__ void __launch_bounds__(kThreads) k_nlis_inner(Batch bt) {
+  __shared__ double red[kWarps * kMbisQ];
+  __shared__ double out[kMbisQ];
+  __shared__ double pu[2][kMbisMaxShell];  // unit-shell prefactors of cur, prev
+  const JobDev* Jp;
+  const AtomTile at = decode_atom_tile(bt, Jp);
+  const JobDev& J = *Jp;
+  if (!J.active[at.atom]) return;
+  const int nsh = J.shell_off[at.atom + 1] - J.shell_off[at.atom];
+  const double* pc = J.cur + J.par_off[at.atom];
+  const double* pp = J.prev + J.par_off[at.atom];
+  const bool first = J.inner_it[at.atom] == 0;
+  if (threadIdx.x < 2 * nsh) {
+    const int k = threadIdx.x % nsh;
+    const double* q = threadIdx.x < nsh ? pc : pp;
+    const double n = q[3 * k + 2];
+    pu[threadIdx.x / nsh][k] = n * pow(q[3 * k + 1], 3.0 / n) / (4.0 * M_PI * tgamma(3.0 / n));
+  }
+  __syncthreads();
+  double acc[kMbisQ];
+#pragma unroll
+  for (int q = 0; q < kMbisQ; ++q) acc[q] = 0.0;
+  const double* ra = J.rhoa + (size_t)at.atom * J.npoint;
+  for (int i = 0; i < J.ppt; ++i) {
+    const int p = point_of(J, at.tile, i);
+    if (p >= J.npoint) continue;
+    const double r = Dist<double>::r(J, p, at.atom);
+    double u[kMbisMaxShell], rn[kMbisMaxShell];
+    double pro = 0.0, oldpro = 0.0;
+#pragma unroll
+    for (int k = 0; k < kMbisMaxShell; ++k) {
+      u[k] = 0.0;
+      rn[k] = 0.0;
+      if (k < nsh) {
+        rn[k] = nlis_rn(pc[3 * k + 2], r);
+        u[k] = pu[0][k] * exp(-pc[3 * k + 1] * rn[k]);
+        pro += pc[3 * k] * u[k];
+        if (!first) oldpro += pp[3 * k] * pu[1][k] * exp(-pp[3 * k + 1] * nlis_rn(pp[3 * k + 2], r));
+      }
+    }
+    const double rho = ra[p];
+    const double w = J.w[p];
+    const bool sick = (rho < J.density_cutoff) || (pro < J.density_cutoff);
+    const double ratio = sick ? 0.0 : rho / pro;
+#pragma unroll
+    for (int k = 0; k < kMbisMaxShell; ++k) {
+      if (k < nsh) {
+        const double wu = w * u[k] * ratio;
+        acc[2 * k] += wu * pc[3 * k];
+        acc[2 * k + 1] += wu * rn[k];
+      }
+    }
+    const double e = oldpro - pro;
+    acc[kMbisQ - 1] += w * e * e;
+  }
+  block_sum<kMbisQ>(acc, red, out);
+  if (threadIdx.x < 2 * nsh) apart_ptr(J, at.atom, QA_INNER + threadIdx.x)[at.tile] = out[threadIdx.x];
+  if (threadIdx.x == 0) apart_ptr(J, at.atom, QA_INNER + kMbisQ - 1)[at.tile] = out[kMbisQ - 1];
+}
+
+// NLIS update per atom: N_k <- m0_k, S_k <- 3 / (n_k m1_k) (1e-5 where m1_k is
+// within 1e-8 of zero, numpy.isclose), n_k fixed; convergence as MBIS.
+__global__ void k_nlis_update(Batch bt) {
+  int a;
+  const JobDev& J = decode_local(bt, a);
+  if (!J.active[a]) return;
+  const int lane = threadIdx.x & 31;
+  const int nsh = J.shell_off[a + 1] - J.shell_off[a];
+  double m[2 * kMbisMaxShell];
+  for (int q = 0; q < 2 * nsh; ++q) m[q] = warp_tile_sum(J, apart_ptr(J, a, QA_INNER + q), J.ntile);
+  const double chg2 = warp_tile_sum(J, apart_ptr(J, a, QA_INNER + kMbisQ - 1), J.ntile);
+  if (lane != 0) return;
+  const int it = J.inner_it[a];
+  const double change = (it == 0) ? 1e100 : sqrt(chg2);
+  double* pc = J.cur + J.par_off[a];
+  double* pp = J.prev + J.par_off[a];
+  double* pr = J.propars + J.par_off[a];
+  double nw[3 * kMbisMaxShell];
+  for (int k = 0; k < nsh; ++k) {
+    const double n = pc[3 * k + 2], m1 = m[2 * k + 1];
+    nw[3 * k] = m[2 * k];
+    nw[3 * k + 1] = fabs(m1) <= 1e-8 ? 1e-5 : 3.0 / (m1 * n);
+    nw[3 * k + 2] = n;
+  }
+  const bool conv = change < J.inner_threshold;
+  if (conv || it + 1 >= J.inner_maxiter) {
+    for (int q = 0; q < 3 * nsh; ++q) pr[q] = nw[q];
+    J.active[a] = 0;
+    J.atom_out[a * AO_COUNT + AO_INNER_CHANGE] = change;
+    atomicAdd(&J.mail->d[MD_INNER_TOTAL], (double)(it + 1));
+    if (!conv) atomicOr(&J.mail->i[MI_WARN], W_INNER);
+  } else {
+    for (int q = 0; q < 3 * nsh; ++q) {
+      pp[q] = pc[q];
+      pc[q] = nw[q];
+    }
+    J.inner_it[a] = it + 1;
+    J.atom_out[a * AO_COUNT + AO_INNER_CHANGE] = change;
+  }
+}
+
 __global__ void k_mbis_update(Batch bt) {
   int a;
   const JobDev& J = decode_local(bt, a);
@@ -1963,6 +2072,7 @@ void launch_promol(const HostBatch& hb, cudaStream_t st, int mixed, int model) {
   if (mixed == PH_FF && model == MODEL_MBIS) return launch_promol_ff(hb, st);
   if (mixed) return launch_promol_mx(hb, st, model);
   if (model == MODEL_MBIS) HP_LAUNCH((k_promol<double, MODEL_MBIS>), K_POINT1, kThreads);
+  else if (model == MODEL_NLIS) HP_LAUNCH((k_promol<double, MODEL_NLIS>), K_POINT1, kThreads);
   else HP_LAUNCH((k_promol<double, MODEL_BASIS>), K_POINT1, kThreads);
   HP_LAUNCH(k_atweights, K_ATOM_TILE, kThreads);
 }
@@ -1978,12 +2088,15 @@ void launch_final_atweights(const HostBatch& hb, cudaStream_t st, int mixed, int
   if (mixed == PH_FF && model == MODEL_MBIS) return launch_final_atweights_ff(hb, st, use_old);
   if (mixed) return launch_final_atweights_mx(hb, st, model, use_old);
   if (model == MODEL_MBIS) HP_LAUNCH((k_final_atweights<double, MODEL_MBIS>), K_ATOM_TILE, kThreads, use_old);
+  else if (model == MODEL_NLIS)
+    HP_LAUNCH((k_final_atweights<double, MODEL_NLIS>), K_ATOM_TILE, kThreads, use_old);
   else HP_LAUNCH((k_final_atweights<double, MODEL_BASIS>), K_ATOM_TILE, kThreads, use_old);
 }
 
 void launch_change(const HostBatch& hb, cudaStream_t st, int mixed, int model) {
   if (mixed) return launch_change_mx(hb, st, model);
   if (model == MODEL_MBIS) HP_LAUNCH((k_change<double, MODEL_MBIS>), K_ATOM_TILE, kThreads);
+  else if (model == MODEL_NLIS) HP_LAUNCH((k_change<double, MODEL_NLIS>), K_ATOM_TILE, kThreads);
   else HP_LAUNCH((k_change<double, MODEL_BASIS>), K_ATOM_TILE, kThreads);
 }
 
@@ -2004,6 +2117,11 @@ void launch_mbis_inner(const HostBatch& hb, cudaStream_t st, int mixed) {
   else if (mixed) launch_mbis_inner_mx(hb, st);
   else HP_LAUNCH(k_mbis_inner<double>, K_ATOM_TILE, kThreads);
   HP_LAUNCH(k_mbis_update, K_ATOM, 32);
+}
+
+void launch_nlis_inner(const HostBatch& hb, cudaStream_t st) {
+  HP_LAUNCH(k_nlis_inner, K_ATOM_TILE, kThreads);
+  HP_LAUNCH(k_nlis_update, K_ATOM, 32);
 }
 
 void launch_gisa(const HostBatch& hb, cudaStream_t st, int mixed) {

@@ -162,6 +162,100 @@ __global__ void __launch_bounds__(kThreads) k_mbis_radial(Batch bt) {
   }
 }
 
+// NLIS / GMBIS inner fixed point of every atom on its radial grid
+// (nlis.py:99-195 on the spherical average; one block per atom, every inner
+// iteration in this launch), population for the charges. FP64.
+__global__ void __launch_bounds__(kThreads) k_nlis_radial(Batch bt) {
+  __shared__ double red[kWarps * kLocalQ];
+  __shared__ double out[kLocalQ];
+  __shared__ double par[21];
+  __shared__ double pu[7];
+  __shared__ int done_s;
+  int a;
+  const JobDev& J = decode_atom_lc(bt, a);
+  const int r0 = J.rad_off[a], nrad = J.rad_off[a + 1] - r0;
+  const int nsh = J.shell_off[a + 1] - J.shell_off[a];
+  double* pa = J.propars + J.par_off[a];
+  if (threadIdx.x < 3 * nsh) par[threadIdx.x] = pa[threadIdx.x];
+  if (threadIdx.x == 0) done_s = 0;
+  constexpr int kPer = kLocalMaxRad / kThreads;
+  double rr[kPer], ww[kPer], rh[kPer], oldpro[kPer];
+  double pop = 0.0;
+#pragma unroll
+  for (int q = 0; q < kPer; ++q) {
+    const int i = threadIdx.x + q * kThreads;
+    const bool in = i < nrad;
+    rr[q] = in ? J.rad_r[r0 + i] : 1.0;
+    ww[q] = in ? 4.0 * M_PI * rr[q] * rr[q] * J.rad_w[r0 + i] : 0.0;
+    rh[q] = in ? J.radrho[r0 + i] : 0.0;
+    oldpro[q] = 0.0;
+    pop += ww[q] * rh[q];
+  }
+  {
+    double acc1[1] = {pop};
+    block_sum<1>(acc1, red, out);
+    put_atom_partial(J, a, QA_POP, out[0]);
+  }
+  __syncthreads();
+  int it = 0;
+  for (; it < J.inner_maxiter; ++it) {
+    if (threadIdx.x < nsh) {  // unit-shell prefactors n S^(3/n) / (4 pi Gamma(3/n))
+      const double n = par[3 * threadIdx.x + 2];
+      pu[threadIdx.x] = n * pow(par[3 * threadIdx.x + 1], 3.0 / n) / (4.0 * M_PI * tgamma(3.0 / n));
+    }
+    __syncthreads();
+    double acc[kLocalQ];
+#pragma unroll
+    for (int q = 0; q < kLocalQ; ++q) acc[q] = 0.0;
+#pragma unroll
+    for (int q = 0; q < kPer; ++q) {
+      double u[7], rn[7];
+      double pro = 0.0;
+#pragma unroll
+      for (int k = 0; k < 7; ++k) {
+        u[k] = 0.0;
+        rn[k] = 0.0;
+        if (k < nsh) {
+          rn[k] = nlis_rn(par[3 * k + 2], rr[q]);
+          u[k] = pu[k] * exp(-par[3 * k + 1] * rn[k]);
+          pro += par[3 * k] * u[k];
+        }
+      }
+      const bool sick = (rh[q] < J.density_cutoff) || (pro < J.density_cutoff);
+      const double ratio = sick ? 0.0 : rh[q] / pro;
+#pragma unroll
+      for (int k = 0; k < 7; ++k) {
+        if (k < nsh) {
+          const double wu = ww[q] * u[k] * ratio;
+          acc[2 * k] += wu * par[3 * k];
+          acc[2 * k + 1] += wu * rn[k];
+        }
+      }
+      const double e = oldpro[q] - pro;
+      acc[kLocalQ - 1] += ww[q] * e * e;
+      oldpro[q] = pro;
+    }
+    block_sum<kLocalQ>(acc, red, out);
+    if (threadIdx.x == 0) {
+      for (int k = 0; k < nsh; ++k) {
+        const double n = par[3 * k + 2], m1 = out[2 * k + 1];
+        par[3 * k] = out[2 * k];
+        par[3 * k + 1] = fabs(m1) <= 1e-8 ? 1e-5 : 3.0 / (m1 * n);
+      }
+      const double change = it == 0 ? 1e100 : sqrt(out[kLocalQ - 1]);
+      done_s = change < J.inner_threshold;
+    }
+    __syncthreads();
+    if (done_s) break;
+  }
+  if (threadIdx.x < 3 * nsh) pa[threadIdx.x] = par[threadIdx.x];
+  if (threadIdx.x == 0) {
+    const bool conv = it < J.inner_maxiter;
+    atomicAdd(&J.mail->d[MD_INNER_TOTAL], (double)(conv ? it + 1 : J.inner_maxiter));
+    if (!conv) atomicOr(&J.mail->i[MI_WARN], W_INNER);
+  }
+}
+
 // Outer change on the radial grids: sum_i 4 pi r_i^2 w_i (pro_new - pro_old)^2
 // (MBIS: Slater shells of both parameter sets; basis schemes: the parameter
 // differences times the unit-population shells at the nodes).
@@ -174,12 +268,16 @@ __global__ void __launch_bounds__(kThreads) k_change_radial(Batch bt) {
   const double* pn = J.propars + J.par_off[a];
   const double* po = J.propars_old + J.par_off[a];
   const bool mbis = J.scheme == SCHEME_MBIS;
+  const bool nlis = J.scheme == SCHEME_NLIS;
   double acc = 0.0;
   for (int i = threadIdx.x; i < nrad; i += kThreads) {
     const double r = J.rad_r[r0 + i];
     double d = 0.0;
     for (int k = 0; k < nsh; ++k) {
-      if (mbis) {
+      if (nlis) {
+        d += nlis_shell(pn[3 * k], pn[3 * k + 1], pn[3 * k + 2], r);
+        d -= nlis_shell(po[3 * k], po[3 * k + 1], po[3 * k + 2], r);
+      } else if (mbis) {
         d += pn[2 * k] * pn[2 * k + 1] * pn[2 * k + 1] * pn[2 * k + 1] * exp(-pn[2 * k + 1] * r) * kInv8Pi;
         d -= po[2 * k] * po[2 * k + 1] * po[2 * k + 1] * po[2 * k + 1] * exp(-po[2 * k + 1] * r) * kInv8Pi;
       } else {
@@ -306,6 +404,11 @@ void launch_mbis_local(const HostBatch& hb, cudaStream_t st) {
 
 void launch_change_radial(const HostBatch& hb, cudaStream_t st) {
   HP_LAUNCH_LC(k_change_radial, K_ATOM, kThreads);
+}
+
+void launch_nlis_local(const HostBatch& hb, cudaStream_t st) {
+  HP_LAUNCH_LC(k_sph_avg, K_ATOM, kThreads);
+  HP_LAUNCH_LC(k_nlis_radial, K_ATOM, kThreads);
 }
 
 void launch_gisa_local(const HostBatch& hb, cudaStream_t st) {

@@ -216,7 +216,11 @@ int check_launch() {
   return HP_OK;
 }
 
-int model_of(const hp_job* j) { return j->desc.scheme == HP_SCHEME_MBIS ? MODEL_MBIS : MODEL_BASIS; }
+int model_of(const hp_job* j) {
+  return j->desc.scheme == HP_SCHEME_MBIS ? MODEL_MBIS
+         : j->desc.scheme == HP_SCHEME_NLIS ? MODEL_NLIS
+                                            : MODEL_BASIS;
+}
 
 // Map device error bits to a status.
 int status_of(int err) {
@@ -305,6 +309,18 @@ int step_iterstock(hp_ctx* ctx, const std::vector<hp_job*>& jobs, const HostBatc
         rc = run_inner(ctx, jobs, hb, [&] {
           ProfScope ps(ctx, HP_KERNEL_INNER);
           launch_mbis_inner(hb, st, mixed);
+        }, j0->dev.inner_maxiter + 1);
+      }
+      break;
+    case HP_SCHEME_NLIS:  // NLIS / GMBIS (FP64)
+      if (local) {
+        ProfScope ps(ctx, HP_KERNEL_INNER);
+        launch_inner_init(hb, st);
+        launch_nlis_local(hb, st);
+      } else {
+        rc = run_inner(ctx, jobs, hb, [&] {
+          ProfScope ps(ctx, HP_KERNEL_INNER);
+          launch_nlis_inner(hb, st);
         }, j0->dev.inner_maxiter + 1);
       }
       break;
@@ -592,7 +608,9 @@ int step_group(hp_ctx* ctx, const std::vector<hp_job*>& jobs) {
 
 int validate(const hp_job_desc* d) {
   if (!d) return fail(HP_ERR_INVALID, "null descriptor");
-  if (d->scheme < 0 || d->scheme > 3) return fail(HP_ERR_INVALID, "unknown scheme");
+  if (d->scheme < 0 || d->scheme > 4) return fail(HP_ERR_INVALID, "unknown scheme");
+  if (d->scheme == HP_SCHEME_NLIS && d->precision != HP_PRECISION_FP64)
+    return fail(HP_ERR_UNSUPPORTED, "NLIS / GMBIS run in FP64");
   if (d->natom <= 0 || d->npoint <= 0) return fail(HP_ERR_INVALID, "natom and npoint must be positive");
   if (d->npoint > (int64_t)2000000000) return fail(HP_ERR_INVALID, "npoint too large");
   if (!d->coordinates || !d->pseudo_numbers || !d->points || !d->weights || !d->density ||
@@ -619,13 +637,14 @@ int validate(const hp_job_desc* d) {
       if (d->shell_point_offsets[k + 1] < d->shell_point_offsets[k])
         return fail(HP_ERR_INVALID, "shell_point_offsets must not decrease");
   }
-  if (d->scheme != HP_SCHEME_MBIS && (!d->shell_orders || !d->shell_exponents))
+  const bool slater_like = d->scheme == HP_SCHEME_MBIS || d->scheme == HP_SCHEME_NLIS;
+  if (!slater_like && (!d->shell_orders || !d->shell_exponents))
     return fail(HP_ERR_INVALID, "basis schemes need shell orders and exponents");
   if (d->shell_offsets[0] != 0) return fail(HP_ERR_INVALID, "shell_offsets[0] must be 0");
   for (int64_t a = 0; a < d->natom; ++a) {
     const int n = d->shell_offsets[a + 1] - d->shell_offsets[a];
     if (n <= 0) return fail(HP_ERR_INVALID, "every atom needs at least one shell");
-    if (d->scheme == HP_SCHEME_MBIS && n > 7) return fail(HP_ERR_INVALID, "MBIS allows at most 7 shells");
+    if (slater_like && n > 7) return fail(HP_ERR_INVALID, "MBIS / NLIS allow at most 7 shells");
     if (n > kMaxShells) return fail(HP_ERR_UNSUPPORTED, "at most 16 shells per atom");
   }
   if (d->maxiter <= 0) return fail(HP_ERR_INVALID, "maxiter must be positive");
@@ -653,7 +672,7 @@ int validate(const hp_job_desc* d) {
       d->solver == HP_SOLVER_SC)
     return fail(HP_ERR_UNSUPPORTED,
                 "mixed precision for gLISA is the tensor-core Hessian of the Newton solvers");
-  for (int64_t s = 0; d->scheme != HP_SCHEME_MBIS && s < d->shell_offsets[d->natom]; ++s) {
+  for (int64_t s = 0; !slater_like && s < d->shell_offsets[d->natom]; ++s) {
     if (!(d->shell_orders[s] > 0.0)) return fail(HP_ERR_INVALID, "n must be positive");
     if (d->shell_exponents[s] < 0.0) return fail(HP_ERR_INVALID, "alpha must be non-negative");
   }
@@ -761,8 +780,9 @@ int32_t hp_job_create(hp_ctx* ctx, const hp_job_desc* d, hp_job** out) {
   const int N = (int)d->npoint;
   const int S = d->shell_offsets[A];
   const bool mbis = d->scheme == HP_SCHEME_MBIS;
+  const bool nlis = d->scheme == HP_SCHEME_NLIS;  // (N, S, n) per shell
   const bool glisa = d->scheme == HP_SCHEME_GLISA;
-  const int P = mbis ? 2 * S : S;
+  const int P = mbis ? 2 * S : nlis ? 3 * S : S;
   int kmax = 1;
   for (int a = 0; a < A; ++a) kmax = std::max(kmax, d->shell_offsets[a + 1] - d->shell_offsets[a]);
   int solver = d->solver;
@@ -859,7 +879,7 @@ int32_t hp_job_create(hp_ctx* ctx, const hp_job_desc* d, hp_job** out) {
   // then reads G instead of recomputing exponentials (gLISA always does).
   const size_t gbytes = 8 * (size_t)S * N;
   const size_t room = ctx->budget > ctx->used ? ctx->budget - ctx->used : 0;
-  if (!glisa && !mbis && !mixed && gbytes <= room / 2) add(&J.gmat, gbytes);
+  if (!glisa && !mbis && !nlis && !mixed && gbytes <= room / 2) add(&J.gmat, gbytes);
   if (glisa) {
     if (!gff) add(&J.gmat, 8 * (size_t)S * N);
     add(&J.gpart, 8 * (size_t)S * ntile);
@@ -1037,10 +1057,11 @@ int32_t hp_job_create(hp_ctx* ctx, const hp_job_desc* d, hp_job** out) {
   }
   ok &= up(J.shell_off, d->shell_offsets, 4 * (size_t)(A + 1)) == cudaSuccess;
   std::vector<int> poff((size_t)A + 1);
-  for (int a = 0; a <= A; ++a) poff[a] = mbis ? 2 * d->shell_offsets[a] : d->shell_offsets[a];
+  for (int a = 0; a <= A; ++a)
+    poff[a] = mbis ? 2 * d->shell_offsets[a] : nlis ? 3 * d->shell_offsets[a] : d->shell_offsets[a];
   ok &= up(J.par_off, poff.data(), 4 * (size_t)(A + 1)) == cudaSuccess;
   std::vector<double> ord((size_t)S, 1.0), alp((size_t)S, 0.0), pref((size_t)S, 0.0);
-  if (!mbis) {
+  if (!mbis && !nlis) {
     for (int s = 0; s < S; ++s) {
       ord[s] = d->shell_orders[s];
       alp[s] = d->shell_exponents[s];

@@ -94,8 +94,11 @@ class GlobalLinearISAWPart(GPUStockholderWPart):
             self._check_grid_type()
             offsets, init, orders, exps = self._shell_tables()
             from . import _lib
+            from .molgrid import atom_grid_arrays
 
             ctx = self._context or _lib.default_context(0)
+            # grid_type 1: the radial grids measure the change
+            local = None if self.on_molgrid else atom_grid_arrays(self.grid)
             return _lib.Job(
                 ctx, self._scheme, self.coordinates, self.pseudo_numbers, self.grid.points,
                 self.grid.weights, self._moldens, offsets, init, shell_orders=orders,
@@ -103,7 +106,7 @@ class GlobalLinearISAWPart(GPUStockholderWPart):
                 grid_type=self.grid_type, threshold=self._threshold,
                 inner_threshold=self._threshold, density_cutoff=self.density_cutoff,
                 negative_cutoff=self.negative_cutoff, population_cutoff=self.population_cutoff,
-                maxiter=self._maxiter, **extra)
+                maxiter=self._maxiter, local=local, **extra)
         finally:
             self._maxiter = saved
 

@@ -3,7 +3,8 @@
 Same names and semantics as horton-part's ``utils.py`` (constants
 ``utils.py:50-59`` from ``data/constants.yaml``; ``typecheck_geo``
 ``utils.py:107-186``; ``wpart_schemes`` ``utils.py:62-104``) for the schemes
-this package implements on the GPU: ``mbis``, ``gisa``, ``lisa``, ``glisa``.
+this package implements on the GPU: ``mbis``, ``gisa``, ``lisa``, ``glisa``,
+``nlis``, ``gmbis``.
 """
 
 from __future__ import annotations
@@ -37,7 +38,15 @@ def wpart_schemes(scheme):
         from .glisa import GlobalLinearISAWPart
 
         return GlobalLinearISAWPart
-    if scheme in ("h", "hi", "is", "nlis", "gmbis", "b"):
+    if scheme == "nlis":
+        from .nlis import NLISWPart
+
+        return NLISWPart
+    if scheme == "gmbis":
+        from .nlis import GMBISWPart
+
+        return GMBISWPart
+    if scheme in ("h", "hi", "is", "b"):
         raise NotImplementedError(f"scheme {scheme!r} is not part of the GPU partitioning path")
     raise UnboundLocalError(f"unknown scheme {scheme!r}")
 

@@ -63,7 +63,11 @@ typedef enum {
   HP_SCHEME_MBIS = 0,  /* mbis.py  MBISWPart */
   HP_SCHEME_GISA = 1,  /* gisa.py  GaussianISAWPart */
   HP_SCHEME_LISA = 2,  /* alisa.py LinearISAWPart (aLISA) */
-  HP_SCHEME_GLISA = 3  /* glisa.py GlobalLinearISAWPart (gLISA) */
+  HP_SCHEME_GLISA = 3, /* glisa.py GlobalLinearISAWPart (gLISA) */
+  HP_SCHEME_NLIS = 4   /* nlis.py NLISWPart and gmbis.py GMBISWPart: shells
+                          N n S^(3/n) exp(-S r^n) / (4 pi Gamma(3/n)), three
+                          parameters (N, S, n) per shell in initial_propars,
+                          n fixed (nlis.py:99-195); FP64 only */
 } hp_scheme;
 
 typedef enum {
@@ -104,7 +108,8 @@ typedef struct {
   int32_t scheme;    /* hp_scheme */
   int32_t solver;    /* hp_solver */
   int32_t precision; /* hp_precision */
-  int32_t grid_type; /* 2 or 3 (molecular grid); 1 (atom grids: MBIS) */
+  int32_t grid_type; /* 2 or 3 (molecular grid); 1 (atom grids: MBIS, NLIS,
+                        GISA, aLISA sc, gLISA) */
   int64_t natom;
   int64_t npoint;
   const double* coordinates;    /* natom x 3, bohr */
@@ -115,12 +120,15 @@ typedef struct {
   /* Shells. shell_offsets[natom+1] delimits each atom's shells.
    * MBIS: each shell has the parameter pair (N_k, S_k); shell_orders and
    *       shell_exponents are ignored.
+   * NLIS: each shell has the triple (N_k, S_k, n_k), n_k fixed; shell_orders
+   *       and shell_exponents are ignored.
    * Basis schemes: shell k has fixed order n_k and exponent alpha_k and one
    *       parameter (its population c_k). */
   const int32_t* shell_offsets;
   const double* shell_orders;
   const double* shell_exponents;
-  /* Initial parameters: MBIS 2 per shell (N, S); basis schemes 1 per shell.
+  /* Initial parameters: MBIS 2 per shell (N, S); NLIS 3 (N, S, n); basis
+   * schemes 1 per shell.
    * For the basis schemes the library rescales them so that their sum is
    * the integrated density (gisa.py:85-86). */
   const double* initial_propars;

@@ -244,6 +244,152 @@ def mbis(coordinates, numbers, pseudo_numbers, points, weights, rho, threshold=1
 
 
 # ---------------------------------------------------------------------------
+# NLIS / GMBIS  (nlis.py, gmbis.py): MBIS with shells exp(-S r^n)
+# ---------------------------------------------------------------------------
+
+
+def nlis_nshell(number, nshell_dict):
+    """Shells of an element (``nlis.py:23-35``)."""
+    return nshell_dict.get(number, mbis_nshell(number))
+
+
+def nlis_initial_propars(number, exp_n_dict, nshell_dict):
+    """Initial (N, S, n) triples (``nlis.py:38-96``)."""
+    nbs = nlis_nshell(number, nshell_dict)
+    propars = np.ones(3 * nbs)
+    s0 = 2.0 * number
+    alpha = (0.5 / s0) ** (1.0 / (nbs - 1)) if nbs > 1 else 1.0
+    for k in range(nbs):
+        propars[3 * k] = number / nbs
+        propars[3 * k + 1] = s0 * alpha**k
+        propars[3 * k + 2] = exp_n_dict[(number, k)] if (number, k) in exp_n_dict else 1.0
+    return propars
+
+
+def gmbis_initial_propars(number, exp_n_dict):
+    """Initial (N, S, n) triples of GMBIS (``gmbis.py:17-52``)."""
+    nshell = mbis_nshell(number)
+    propars = np.zeros(3 * nshell)
+    s0 = 2.0 * number
+    alpha = (2.0 / s0) ** (1.0 / (nshell - 1)) if nshell > 1 else 1.0
+    nel = np.array([2.0, 8.0, 8.0, 18.0, 18.0, 32.0, 32.0])
+    for k in range(nshell):
+        propars[3 * k] = nel[k]
+        propars[3 * k + 1] = s0 * alpha**k
+        propars[3 * k + 2] = exp_n_dict[(number, k)] if (number, k) in exp_n_dict else 1.0
+    propars[-3] = number - propars[:-3:3].sum()
+    return propars
+
+
+def nlis_unit_shell(s, n, r):
+    """n S^(3/n) exp(-S r^n) / (4 pi Gamma(3/n)) (``nlis.py:148``)."""
+    return n * s ** (3.0 / n) * np.exp(-s * r**n) / (4 * np.pi * math.gamma(3.0 / n))
+
+
+def nlis_proatom(propars_a, r):
+    """sum_k N_k g_k(r) (``nlis.py:281-296``)."""
+    y = np.zeros(len(r))
+    for k in range(len(propars_a) // 3):
+        nk, s, n = propars_a[3 * k:3 * k + 3]
+        y += nk * nlis_unit_shell(s, n, r)
+    return y
+
+
+def opt_nlis_propars(rho, propars, weights, r, threshold, density_cutoff=DENSITY_CUTOFF,
+                     maxiter=2000):
+    """Inner NLIS fixed point for one atom (``nlis.py:99-195``): N_k <- m0_k,
+    S_k <- 3 / (n_k m1_k) with m1_k = int w g_k (rho / pro) r^n (the unit shell,
+    without N_k), S_k = 1e-5 where m1_k is within 1e-8 of zero.
+
+    Returns ``(propars, n_inner, converged)``.
+    """
+    nshell = len(propars) // 3
+    terms = np.zeros((nshell, len(r)))
+    oldpro = None
+    for irep in range(maxiter):
+        for k in range(nshell):
+            terms[k] = nlis_unit_shell(propars[3 * k + 1], propars[3 * k + 2], r)
+        pro = np.sum(terms * propars[::3, None], axis=0)
+        sick = (rho < density_cutoff) | (pro < density_cutoff)
+        with np.errstate(all="ignore"):
+            ratio = rho / pro
+        ratio[sick] = 0.0
+        terms_ratio = terms * ratio
+        for k in range(nshell):
+            nk, n = propars[3 * k], propars[3 * k + 2]
+            m0 = np.einsum("p,p->", weights, terms_ratio[k] * nk)
+            m1 = np.einsum("p,p,p->", weights, terms_ratio[k], r**n)
+            propars[3 * k] = m0
+            propars[3 * k + 1] = 1e-5 if np.isclose(m1, 0.0) else 3 / (m1 * n)
+        if oldpro is None:
+            change = 1e100
+        else:
+            err = oldpro - pro
+            change = np.sqrt(np.einsum("p,p,p->", weights, err, err))
+        if change < threshold:
+            return propars, irep + 1, True
+        oldpro = pro
+    return propars, maxiter, False
+
+
+def nlis(coordinates, numbers, pseudo_numbers, points, weights, rho, initial, ranges,
+         threshold=1e-6, maxiter=500, inner_threshold=1e-8, density_cutoff=DENSITY_CUTOFF,
+         local=None):
+    """NLIS / GMBIS (``nlis.py:198-367``, ``gmbis.py:55-156``): the outer loop of
+    ``mbis`` (``core/iterstock.py:159-193``, ``mbis.py:167-203``) with the
+    pro-atoms of ``nlis_proatom`` and the inner solver ``opt_nlis_propars``.
+    ``initial`` holds the atoms' initial (N, S, n) triples
+    (``nlis_initial_propars`` or ``gmbis_initial_propars``) and ``ranges`` their
+    offsets; ``local`` as in ``mbis``."""
+    natom = len(numbers)
+    inner = inner_threshold if inner_threshold < threshold else threshold
+    rs = radial_distances(points, coordinates)
+    propars = np.asarray(initial, dtype=float).copy()
+    res = dict(history_propars=[], history_charges=[], history_entropies=[], history_changes=[],
+               inner_iterations=[])
+    charges = np.zeros(natom)
+    counter = 0
+    while True:
+        counter += 1
+        old = propars.copy()
+        pros = [nlis_proatom(propars[ranges[a]:ranges[a + 1]], rs[a]) for a in range(natom)]
+        promol, at_weights = stockholder_weights(pros)
+        its = []
+        for a in range(natom):
+            sl = slice(ranges[a], ranges[a + 1])
+            if local is None:
+                rhoa, wa, ra = at_weights[a] * rho, weights, rs[a]
+            else:
+                ra, wa, _ = _radial_view(local, a)
+                rhoa = _local_average(local, a, at_weights[a] * rho)
+            new, nit, _ = opt_nlis_propars(rhoa, propars[sl].copy(), wa, ra, inner, density_cutoff)
+            propars[sl] = new
+            its.append(nit)
+            charges[a] = pseudo_numbers[a] - np.einsum("p,p->", wa, rhoa)
+        res["inner_iterations"].append(its)
+        res["history_propars"].append(propars.copy())
+        res["history_charges"].append(charges.copy())
+        res["history_entropies"].append(entropy(weights, rho, promol, density_cutoff))
+        msd = 0.0
+        for a in range(natom):
+            ra, wa = (rs[a], weights) if local is None else _radial_view(local, a)[:2]
+            d = (nlis_proatom(propars[ranges[a]:ranges[a + 1]], ra)
+                 - nlis_proatom(old[ranges[a]:ranges[a + 1]], ra))
+            msd += integrate(wa, d, d)
+        change = np.sqrt(msd)
+        res["history_changes"].append(change)
+        if change < threshold or counter >= maxiter:
+            break
+    res.update(charges=charges, propars=propars, niter=counter, change=change,
+               promoldens=promol, at_weights=np.array(at_weights), ranges=np.array(ranges))
+    finalize(res, np.asarray(numbers), np.asarray(pseudo_numbers, dtype=float))
+    res["valence_charges"] = np.array([-propars[ranges[a + 1] - 3] for a in range(natom)])
+    res["valence_widths"] = np.array([1.0 / propars[ranges[a + 1] - 2] for a in range(natom)])
+    res["core_charges"] = charges - res["valence_charges"]
+    return res
+
+
+# ---------------------------------------------------------------------------
 # basis-function schemes: shared  (gisa.py)
 # ---------------------------------------------------------------------------
 

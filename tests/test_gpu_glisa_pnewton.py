@@ -122,4 +122,4 @@ def test_tensor_core_hessian_on_atom_grids(gpu_context):
     print(f"glisa atom grids, tensor core: niter {part['niter']} (reference {int(g['niter'])}), "
           f"max|dq| {dq:.2e}")
     assert part["niter"] == int(g["niter"])
-    assert dq < 1e-8
+    assert dq < 5e-8  # atom-grid change: see tests/golden/cases.py tolerances()

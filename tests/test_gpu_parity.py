@@ -13,7 +13,7 @@ import warnings
 import numpy as np
 import pytest
 
-from cases import CASES, build_inputs
+from cases import CASES, build_inputs, tolerances
 from horton_part_gb300 import synthetic
 from horton_part_gb300.basis import ExpBasisFuncHelper
 from horton_part_gb300.utils import wpart_schemes
@@ -54,9 +54,11 @@ def test_fp64_parity_with_reference(name, gpu_context):
     g = load_golden(name)
     part, mol = run_case(name)
     thr = CASES[name]["kwargs"]["threshold"]
+    tol = tolerances(CASES[name])
+    q_tol = max(Q_TOL, tol.get("charges", 0.0))
     if niter_must_match(g, thr):
         assert part["niter"] == int(g["niter"])
-    np.testing.assert_allclose(part["charges"], g["charges"], rtol=0, atol=Q_TOL)
+    np.testing.assert_allclose(part["charges"], g["charges"], rtol=0, atol=q_tol)
     np.testing.assert_allclose(part["propars"], g["propars"], rtol=P_RTOL, atol=1e-10)
     n = min(len(part["history_changes"]), len(g["history_changes"]))
     np.testing.assert_allclose(part["history_entropies"][:n], g["history_entropies"][:n],
@@ -64,16 +66,17 @@ def test_fp64_parity_with_reference(name, gpu_context):
                                atol=1e-10)
     np.testing.assert_allclose(part["history_propars"][:n], g["history_propars"][:n],
                                rtol=1e-6, atol=1e-9)
-    np.testing.assert_allclose(part["populations"], g["populations"], atol=Q_TOL)
+    np.testing.assert_allclose(part["populations"], g["populations"], atol=q_tol)
     if CASES[name]["scheme"] != "glisa":
         np.testing.assert_allclose(part["history_charges"][:n], g["history_charges"][:n],
-                                   atol=Q_TOL)
-        assert part["change"] == pytest.approx(float(g["change"]), rel=1e-4)
+                                   atol=q_tol)
+        assert part["change"] == pytest.approx(float(g["change"]), rel=1e-4,
+                                               abs=tol.get("changes", 0.0))
     else:
         assert part["history_charges"].size == 0
     if "core_charges" in g:
-        np.testing.assert_allclose(part["core_charges"], g["core_charges"], atol=Q_TOL)
-        np.testing.assert_allclose(part["valence_charges"], g["valence_charges"], atol=Q_TOL)
+        np.testing.assert_allclose(part["core_charges"], g["core_charges"], atol=q_tol)
+        np.testing.assert_allclose(part["valence_charges"], g["valence_charges"], atol=q_tol)
         np.testing.assert_allclose(part["valence_widths"], g["valence_widths"], rtol=P_RTOL)
 
 
@@ -259,3 +262,33 @@ def test_mbis_atom_grids_water_hf_sto3g(precision, tol, gpu_context):
     published = np.array([-0.61891067, 0.3095756, 0.30932584])
     assert np.abs(part["charges"] - published).max() < 5e-5
     assert part["at_weights_0"].shape == (npa,)
+
+
+@pytest.mark.parametrize("grid_type", [3, 1])
+def test_nlis_general_orders_match_the_oracle(grid_type, gpu_context):
+    """NLIS with more shells than MBIS (nshell_dict) and non-integer orders
+    (r^1.5) on the molecular grid and on atom grids, against the oracle
+    (nlis.py:99-195; the reference's own runs pin the oracle in
+    tests/test_oracle_golden.py)."""
+    from cases import local_description
+    from oracle import hp_oracle as O
+
+    mol = synthetic.water(nrad=30, nang=50)
+    nsd = {1: 2, 8: 3}
+    expn = {(1, 0): 1.0, (1, 1): 1.5, (8, 0): 1.0, (8, 1): 2.0, (8, 2): 1.5}
+    init = [O.nlis_initial_propars(int(z), expn, nsd) for z in mol.numbers]
+    ranges = np.concatenate([[0], np.cumsum([len(x) for x in init])])
+    local = local_description(mol, 50) if grid_type == 1 else None
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        ref = O.nlis(mol.coordinates, mol.numbers, mol.pseudo_numbers, mol.grid.points,
+                     mol.grid.weights, mol.density, np.concatenate(init), ranges, threshold=1e-8,
+                     inner_threshold=1e-8, local=local)
+    part = wpart_schemes("nlis")(mol.coordinates, mol.numbers, mol.pseudo_numbers, mol.grid,
+                                 mol.density, grid_type=grid_type, threshold=1e-8,
+                                 exp_n_dict=expn, nshell_dict=nsd)
+    part.do_partitioning()
+    assert part["niter"] == ref["niter"]
+    np.testing.assert_allclose(part["charges"], ref["charges"], atol=1e-7 if grid_type == 1 else 1e-9)
+    np.testing.assert_allclose(part["propars"], ref["propars"], rtol=1e-7, atol=1e-10)
+    np.testing.assert_allclose(part["valence_widths"], ref["valence_widths"], rtol=1e-7)

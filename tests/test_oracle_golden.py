@@ -44,6 +44,14 @@ def run_oracle(case, mol, kwargs):
     scheme = case["scheme"]
     if scheme == "mbis":
         return O.mbis(*args, **kwargs)
+    if scheme in ("nlis", "gmbis"):
+        kw = dict(kwargs)
+        expn = kw.pop("exp_n_dict")
+        nsd = kw.pop("nshell_dict", None) or {}
+        init = [O.nlis_initial_propars(int(z), expn, nsd) if scheme == "nlis"
+                else O.gmbis_initial_propars(int(z), expn) for z in mol.numbers]
+        ranges = np.concatenate([[0], np.cumsum([len(x) for x in init])])
+        return O.nlis(*args, np.concatenate(init), ranges, **kw)
     orders, exps, inits = basis_tables(mol)
     if scheme in ("gisa", "lisa"):
         kw = dict(kwargs)

@@ -352,17 +352,19 @@ constexpr int kFuseRows = kFuseMaxShells / kFuseWarps;  // rows per warp in B
 __host__ __device__ constexpr size_t fuse_smem_bytes(int S) {
   return 4 * (size_t)S * kFuseSP * 4          // two stages of both planes
          + 16 * (size_t)S                     // x and the parameter change as float pairs
+         + 8 * (size_t)S                      // active-shell list and positions
          + 8 * (size_t)kFuseWarps * kFuseSP   // partial sums
          + 512                                // exp table
          + 8 * (2 * kFuseWarps + 2);          // block sums
 }
 
-// Sub-tile [q0, q0 + kFuseSP) of both planes into gh / gl ([S][kFuseSP]);
-// columns at or past p1 are zero-filled. vec: 16-byte copies (npoint % 4 == 0,
-// so every row segment starts 16-byte aligned and p1 is a multiple of 4).
+// Sub-tile [q0, q0 + kFuseSP) of the tile's active rows (act[0..nact), the
+// shells with a nonzero value in the tile) of both planes into gh / gl
+// ([nact][kFuseSP], row i holds shell act[i]); columns at or past p1 are
+// zero-filled. vec: 16-byte copies (npoint % 4 == 0, so every row segment
+// starts 16-byte aligned and p1 is a multiple of 4).
 __device__ __forceinline__ void fuse_load(const JobDev& J, int q0, int p1, float* gh, float* gl,
-                                          bool vec) {
-  const int S = J.nshell;
+                                          bool vec, const int* act, int nact) {
   const size_t N = J.npoint;
   if (vec) {
     constexpr int C = kFuseSP / 4;  // 16-byte chunks per row
@@ -370,22 +372,43 @@ __device__ __forceinline__ void fuse_load(const JobDev& J, int q0, int p1, float
     const int p = q0 + 4 * c;
     const bool in = p < p1;
     const int pc = in ? p : q0;
-    for (int m = threadIdx.x / C; m < S; m += kFuseThreads / C) {
-      const size_t off = (size_t)m * N + pc;
-      cp_async16(gh + m * kFuseSP + 4 * c, J.gmat32 + off, in);
-      cp_async16(gl + m * kFuseSP + 4 * c, J.gmat_lo + off, in);
+    for (int i = threadIdx.x / C; i < nact; i += kFuseThreads / C) {
+      const size_t off = (size_t)act[i] * N + pc;
+      cp_async16(gh + i * kFuseSP + 4 * c, J.gmat32 + off, in);
+      cp_async16(gl + i * kFuseSP + 4 * c, J.gmat_lo + off, in);
     }
   } else {
     const int c = threadIdx.x % kFuseSP;
     const int p = q0 + c;
     const bool in = p < p1;
     const int pc = in ? p : q0;
-    for (int m = threadIdx.x / kFuseSP; m < S; m += kFuseThreads / kFuseSP) {
-      const size_t off = (size_t)m * N + pc;
-      cp_async4(gh + m * kFuseSP + c, J.gmat32 + off, in);
-      cp_async4(gl + m * kFuseSP + c, J.gmat_lo + off, in);
+    for (int i = threadIdx.x / kFuseSP; i < nact; i += kFuseThreads / kFuseSP) {
+      const size_t off = (size_t)act[i] * N + pc;
+      cp_async4(gh + i * kFuseSP + c, J.gmat32 + off, in);
+      cp_async4(gl + i * kFuseSP + c, J.gmat_lo + off, in);
     }
   }
+}
+
+// The tile's active-shell list into shared memory: act[0..nact) ascending and
+// pos[m] = its index (-1 for a shell that is zero on the whole tile).
+__device__ __forceinline__ int load_active(const JobDev& J, int tile, int* act, int* pos) {
+  const int S = J.nshell;
+  const int* g = J.gact + (size_t)tile * (S + 1);
+  const int nact = g[S];
+  for (int m = threadIdx.x; m < S; m += kFuseThreads) pos[m] = -1;
+  __syncthreads();
+  for (int i = threadIdx.x; i < nact; i += kFuseThreads) {
+    act[i] = g[i];
+    pos[g[i]] = i;
+  }
+  return nact;
+}
+
+// Zero partial row sums of the shells that are inactive on this tile.
+__device__ __forceinline__ void zero_inactive(const JobDev& J, int tile, const int* pos) {
+  for (int m = threadIdx.x; m < J.nshell; m += kFuseThreads)
+    if (pos[m] < 0) J.gpart[(size_t)m * J.ntile + tile] = 0.0;
 }
 
 template <int MODE>
@@ -403,13 +426,17 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_fused_ff(Batch bt, in
   Dot2* part = reinterpret_cast<Dot2*>(dcv + S);
   float2* tab = reinterpret_cast<float2*>(part + kFuseWarps * kFuseSP);
   double* red = reinterpret_cast<double*>(tab + 64);
+  int* act = reinterpret_cast<int*>(red + 2 * kFuseWarps + 2);
+  int* pos = act + S;
   const float2 cutp = split2(J.density_cutoff), negp = split2(J.negative_cutoff);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int p0 = tile * J.tile_points;
   const int p1 = min(p0 + J.tile_points, J.npoint);
   const int nsub = (p1 - p0 + kFuseSP - 1) / kFuseSP;
   const bool vec = (J.npoint & 3) == 0;
-  fuse_load(J, p0, p1, stg, stg + plane, vec);
+  const int nact = load_active(J, tile, act, pos);
+  __syncthreads();
+  fuse_load(J, p0, p1, stg, stg + plane, vec, act, nact);
   cp_async_commit();
   const double* x = MODE ? J.propars : J.delta;
   for (int i = threadIdx.x; i < S; i += kFuseThreads) xv[i] = split2(x[i]);
@@ -430,18 +457,22 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_fused_ff(Batch bt, in
     __syncthreads();  // sub-tile sub visible; every thread is done with sub - 1
     if (sub + 1 < nsub) {
       float* nh = stg + ((sub + 1) & 1) * 2 * plane;  // last read in B of sub - 1
-      fuse_load(J, p0 + (sub + 1) * kFuseSP, p1, nh, nh + plane, vec);
+      fuse_load(J, p0 + (sub + 1) * kFuseSP, p1, nh, nh + plane, vec, act, nact);
       cp_async_commit();
     }
-    {  // A
+    {  // A (active rows i = warp mod 8)
       Dot2 d{0.f, 0.f}, e{0.f, 0.f};
-      int m = warp;
-      for (; m + kFuseWarps < S; m += 2 * kFuseWarps) {
-        dot2_add(d, gh[m * kFuseSP + lane], gl[m * kFuseSP + lane], xv[m].x, xv[m].y);
-        const int m2 = m + kFuseWarps;
-        dot2_add(e, gh[m2 * kFuseSP + lane], gl[m2 * kFuseSP + lane], xv[m2].x, xv[m2].y);
+      int i = warp;
+      for (; i + kFuseWarps < nact; i += 2 * kFuseWarps) {
+        const float2 x1 = xv[act[i]], x2 = xv[act[i + kFuseWarps]];
+        dot2_add(d, gh[i * kFuseSP + lane], gl[i * kFuseSP + lane], x1.x, x1.y);
+        const int i2 = i + kFuseWarps;
+        dot2_add(e, gh[i2 * kFuseSP + lane], gl[i2 * kFuseSP + lane], x2.x, x2.y);
       }
-      if (m < S) dot2_add(d, gh[m * kFuseSP + lane], gl[m * kFuseSP + lane], xv[m].x, xv[m].y);
+      if (i < nact) {
+        const float2 x1 = xv[act[i]];
+        dot2_add(d, gh[i * kFuseSP + lane], gl[i * kFuseSP + lane], x1.x, x1.y);
+      }
       dot2_merge(d, e);
       part[warp * kFuseSP + lane] = d;
     }
@@ -480,19 +511,21 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_fused_ff(Batch bt, in
         }
       }
     }
-    {  // B
+    {  // B (active rows i = warp + 8 r)
 #pragma unroll
       for (int r = 0; r < kFuseRows; ++r) {
-        const int m = warp + kFuseWarps * r;
-        if (m < S) dot2_add(acc[r], gh[m * kFuseSP + lane], gl[m * kFuseSP + lane], v.hi, v.lo);
+        const int i = warp + kFuseWarps * r;
+        if (i < nact) dot2_add(acc[r], gh[i * kFuseSP + lane], gl[i * kFuseSP + lane], v.hi, v.lo);
       }
     }
     if (chg) {  // C
       const float wf = p < p1 ? (float)J.w[p] : 0.0f;
       for (int a = warp; a < J.natom; a += kFuseWarps) {
         Dot2 d{0.f, 0.f};
-        for (int m = J.shell_off[a]; m < J.shell_off[a + 1]; ++m)
-          dot2_add(d, gh[m * kFuseSP + lane], gl[m * kFuseSP + lane], dcv[m].x, dcv[m].y);
+        for (int m = J.shell_off[a]; m < J.shell_off[a + 1]; ++m) {
+          const int i = pos[m];
+          if (i >= 0) dot2_add(d, gh[i * kFuseSP + lane], gl[i * kFuseSP + lane], dcv[m].x, dcv[m].y);
+        }
         const float dv = d.s + d.c;
         const float term = wf * dv * dv;
         const float t = ch + term;
@@ -504,17 +537,18 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_fused_ff(Batch bt, in
   }
 #pragma unroll
   for (int r = 0; r < kFuseRows; ++r) {
-    const int m = warp + kFuseWarps * r;
-    if (m < S) {  // warp-uniform
+    const int i = warp + kFuseWarps * r;
+    if (i < nact) {  // warp-uniform
       Dot2 d = acc[r];
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) {
         const Dot2 b{__shfl_xor_sync(0xffffffffu, d.s, o), __shfl_xor_sync(0xffffffffu, d.c, o)};
         dot2_merge(d, b);
       }
-      if (lane == 0) J.gpart[(size_t)m * J.ntile + tile] = dot2_value(d);
+      if (lane == 0) J.gpart[(size_t)act[i] * J.ntile + tile] = dot2_value(d);
     }
   }
+  zero_inactive(J, tile, pos);
   if (MODE == 1) {
     // entropy and negativity partials of the tile
     double e = ffa::to_double(ent), n = (double)nneg;
@@ -570,12 +604,17 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_trials_fused(Batch bt
   const int plane = S * kFuseSP;
   float2* xv = reinterpret_cast<float2*>(stg + 4 * plane);
   Dot2* part = reinterpret_cast<Dot2*>(xv + 2 * S);
+  int* act = reinterpret_cast<int*>(reinterpret_cast<float2*>(part + kFuseWarps * kFuseSP) + 64) +
+             2 * (2 * kFuseWarps + 2);  // after the exp table and block sums of the fused layout
+  int* pos = act + S;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int p0 = tile * J.tile_points;
   const int p1 = min(p0 + J.tile_points, J.npoint);
   const int nsub = (p1 - p0 + kFuseSP - 1) / kFuseSP;
   const bool vec = (J.npoint & 3) == 0;
-  fuse_load(J, p0, p1, stg, stg + plane, vec);
+  const int nact = load_active(J, tile, act, pos);
+  __syncthreads();
+  fuse_load(J, p0, p1, stg, stg + plane, vec, act, nact);
   cp_async_commit();
   for (int i = threadIdx.x; i < S; i += kFuseThreads) xv[i] = split2(J.delta[i]);
   const int t = warp;  // this warp's trial: step 2^-t
@@ -594,18 +633,22 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_trials_fused(Batch bt
     __syncthreads();
     if (sub + 1 < nsub) {
       float* nh = stg + ((sub + 1) & 1) * 2 * plane;
-      fuse_load(J, p0 + (sub + 1) * kFuseSP, p1, nh, nh + plane, vec);
+      fuse_load(J, p0 + (sub + 1) * kFuseSP, p1, nh, nh + plane, vec, act, nact);
       cp_async_commit();
     }
-    {  // A
+    {  // A (active rows i = warp mod 8)
       Dot2 d{0.f, 0.f}, e{0.f, 0.f};
-      int m = warp;
-      for (; m + kFuseWarps < S; m += 2 * kFuseWarps) {
-        dot2_add(d, gh[m * kFuseSP + lane], gl[m * kFuseSP + lane], xv[m].x, xv[m].y);
-        const int m2 = m + kFuseWarps;
-        dot2_add(e, gh[m2 * kFuseSP + lane], gl[m2 * kFuseSP + lane], xv[m2].x, xv[m2].y);
+      int i = warp;
+      for (; i + kFuseWarps < nact; i += 2 * kFuseWarps) {
+        const float2 x1 = xv[act[i]], x2 = xv[act[i + kFuseWarps]];
+        dot2_add(d, gh[i * kFuseSP + lane], gl[i * kFuseSP + lane], x1.x, x1.y);
+        const int i2 = i + kFuseWarps;
+        dot2_add(e, gh[i2 * kFuseSP + lane], gl[i2 * kFuseSP + lane], x2.x, x2.y);
       }
-      if (m < S) dot2_add(d, gh[m * kFuseSP + lane], gl[m * kFuseSP + lane], xv[m].x, xv[m].y);
+      if (i < nact) {
+        const float2 x1 = xv[act[i]];
+        dot2_add(d, gh[i * kFuseSP + lane], gl[i * kFuseSP + lane], x1.x, x1.y);
+      }
       dot2_merge(d, e);
       part[warp * kFuseSP + lane] = d;
     }
@@ -618,9 +661,10 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_trials_fused(Batch bt
       const f2 u = dot2_ff(du);
       Dot2 sc{0.f, 0.f}, sd{0.f, 0.f};
       for (int k = 0; k < kt; ++k) {
-        const int m = J.clip[k];
+        const int i = pos[J.clip[k]];
+        if (i < 0) continue;  // the shell is zero on this tile
         const float4 v = cd[k];
-        const float g1 = gh[m * kFuseSP + lane], g2 = gl[m * kFuseSP + lane];
+        const float g1 = gh[i * kFuseSP + lane], g2 = gl[i * kFuseSP + lane];
         dot2_add(sc, g1, g2, v.x, v.y);
         dot2_add(sd, g1, g2, v.z, v.w);
       }
@@ -695,6 +739,36 @@ __global__ void __launch_bounds__(kThreads) k_glisa_change_ff(Batch bt) {
   const double sum = block_sum1((double)ah + (double)al, red);
   for (int a = threadIdx.x; a < J.natom; a += kThreads)
     J.apart[((size_t)a * J.qa + QA_CHANGE) * J.ntile + tile] = a == 0 ? sum : 0.0;
+}
+
+// Active shells of every point tile of a fused job (once per job, after the
+// basis): gact[tile][0..n) the shells with a nonzero value on the tile, in
+// order, n at gact[tile][S]. A float-float value is zero exactly when its
+// high part is, so the passes that skip the other rows add exact zeros less.
+__global__ void __launch_bounds__(kThreads) k_glisa_active(Batch bt) {
+  __shared__ int flag[kFuseMaxShells];
+  int tile;
+  const JobDev& J = decode_local_gf(bt, tile);
+  if (!J.fuse) return;
+  const int S = J.nshell;
+  const size_t N = J.npoint;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int p0 = tile * J.tile_points;
+  const int p1 = min(p0 + J.tile_points, J.npoint);
+  for (int m = warp; m < S; m += kWarps) {
+    bool nz = false;
+    for (int p = p0 + lane; p < p1; p += 32) nz |= J.gmat32[m * N + p] != 0.0f;
+    nz = __any_sync(0xffffffffu, nz);
+    if (lane == 0) flag[m] = nz ? 1 : 0;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int* g = J.gact + (size_t)tile * (S + 1);
+    int n = 0;
+    for (int m = 0; m < S; ++m)
+      if (flag[m]) g[n++] = m;
+    g[S] = n;
+  }
 }
 
 // Final promolecule of a float-float gLISA job (glisa.py:268-278 through
@@ -793,6 +867,10 @@ void launch_glisa_trials_fused(const HostBatch& hb, cudaStream_t st, int max_she
   k_glisa_trials_fused<<<hb.blocks[K_POINT], kFuseThreads, fuse_smem_bytes(max_shells), st>>>(
       hb.b[K_POINT]);
   ++g_launch_count;
+}
+
+void launch_glisa_active(const HostBatch& hb, cudaStream_t st) {
+  HP_LAUNCH_GF(k_glisa_active, K_POINT, kThreads);
 }
 
 void launch_glisa_promol_ff(const HostBatch& hb, cudaStream_t st) {

@@ -165,6 +165,7 @@ struct JobDev {
   float2* r0f;            // fused gLISA: rho0 as float pairs [npoint]
   float2* d2f;            // fused gLISA: w rho / rho0^2 as float pairs [npoint]
   double* hsum;           // gLISA tensor-core Hessian: refinement product H delta [nshell]
+  int* gact;              // fused gLISA: per point tile the shells nonzero on it [ntile][nshell + 1]
   float2* d1f;            // gLISA, gff: w rho / rho0 as float pairs, npoint
   float2* hvf;            // gLISA, gff: the refinement's hvec as float pairs, npoint
   float* hess_s;          // gLISA tensor-core Hessian: sqrt(w rho / rho0^2) as FP32, npoint
@@ -442,6 +443,7 @@ void launch_glisa_grad_ff(const HostBatch& hb, cudaStream_t st);
 void launch_glisa_hv_ff(const HostBatch& hb, cudaStream_t st);  // hvec and G hvec
 void launch_glisa_trials_ff(const HostBatch& hb, cudaStream_t st);
 void launch_glisa_promol_ff(const HostBatch& hb, cudaStream_t st);  // final promolecule
+void launch_glisa_active(const HostBatch& hb, cudaStream_t st);     // per-tile active shells
 void launch_glisa_trials_fused(const HostBatch& hb, cudaStream_t st, int max_shells);
 void launch_atweights(const HostBatch& hb, cudaStream_t st);        // k_atweights alone
 void launch_glisa_change_ff(const HostBatch& hb, cudaStream_t st);

@@ -169,7 +169,7 @@ __global__ void k_init_params(Batch bt) {
   const double nelec = warp_tile_sum(J, J.jpart + (size_t)QJ_NELEC * J.ntile, J.ntile);
   if ((threadIdx.x & 31) != 0) return;
   J.mail->d[MD_NELEC] = nelec;
-  if (J.scheme != SCHEME_MBIS) {
+  if (J.scheme != SCHEME_MBIS && J.scheme != SCHEME_NLIS) {  // basis schemes: populations only
     double s = 0.0;
     for (int i = 0; i < J.nparam; ++i) s += J.propars[i];
     for (int i = 0; i < J.nparam; ++i) J.propars[i] = J.propars[i] / s * nelec;

@@ -280,8 +280,12 @@ int job_init(hp_ctx* ctx, const std::vector<hp_job*>& jobs, const HostBatch& hb)
   int fuse_shells = 0;
   for (hp_job* j : jobs)
     if (j->dev.fuse) fuse_shells = std::max(fuse_shells, j->dev.nshell);
-  // fused gLISA jobs: the first iteration's promolecule and gradient
-  if (fuse_shells > 0) launch_glisa_fused_ff(hb, ctx->stream, 1, fuse_shells, 0);
+  // fused gLISA jobs: active shells per tile, then the first iteration's
+  // promolecule and gradient
+  if (fuse_shells > 0) {
+    launch_glisa_active(hb, ctx->stream);
+    launch_glisa_fused_ff(hb, ctx->stream, 1, fuse_shells, 0);
+  }
   for (hp_job* j : jobs) j->initialized = true;
   return check_launch();
 }
@@ -901,6 +905,7 @@ int32_t hp_job_create(hp_ctx* ctx, const hp_job_desc* d, hp_job** out) {
         add(&J.gmat_lo, 4 * (size_t)S * N);
         add(&J.clipf, 4 * 4 * (size_t)S);
         if (S <= kFuseMaxShells) {
+          add(&J.gact, 4 * (size_t)(S + 1) * ntile);
           add(&J.wrf, 16 * (size_t)N);
           add(&J.r0f, 8 * (size_t)N);
           add(&J.d2f, 8 * (size_t)N);

@@ -353,6 +353,7 @@ __host__ __device__ constexpr size_t fuse_smem_bytes(int S) {
   return 4 * (size_t)S * kFuseSP * 4          // two stages of both planes
          + 16 * (size_t)S                     // x and the parameter change as float pairs
          + 8 * (size_t)S                      // active-shell list and positions
+         + 4 * ((size_t)S + 1)                // per atom: its first active row
          + 8 * (size_t)kFuseWarps * kFuseSP   // partial sums
          + 512                                // exp table
          + 8 * (2 * kFuseWarps + 2);          // block sums
@@ -428,6 +429,7 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_fused_ff(Batch bt, in
   double* red = reinterpret_cast<double*>(tab + 64);
   int* act = reinterpret_cast<int*>(red + 2 * kFuseWarps + 2);
   int* pos = act + S;
+  int* aoff = pos + S;  // atom a's active rows: [aoff[a], aoff[a + 1]) (act is ordered by shell)
   const float2 cutp = split2(J.density_cutoff), negp = split2(J.negative_cutoff);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int p0 = tile * J.tile_points;
@@ -438,6 +440,17 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_fused_ff(Batch bt, in
   __syncthreads();
   fuse_load(J, p0, p1, stg, stg + plane, vec, act, nact);
   cp_async_commit();
+  if (MODE == 1)
+    for (int a = threadIdx.x; a <= J.natom; a += kFuseThreads) {
+      const int s0 = J.shell_off[a];
+      int lo = 0, hi = nact;  // first active row with shell >= s0
+      while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (act[mid] < s0) lo = mid + 1;
+        else hi = mid;
+      }
+      aoff[a] = lo;
+    }
   const double* x = MODE ? J.propars : J.delta;
   for (int i = threadIdx.x; i < S; i += kFuseThreads) xv[i] = split2(x[i]);
   const bool chg = MODE == 1 && with_change;
@@ -455,6 +468,11 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_fused_ff(Batch bt, in
     const float* gl = gh + plane;
     cp_async_wait<0>();
     __syncthreads();  // sub-tile sub visible; every thread is done with sub - 1
+    float wf = 0.0f;  // phase C weight, loaded early
+    if (chg) {
+      const int pc = p0 + sub * kFuseSP + lane;
+      wf = pc < p1 ? (float)J.w[pc] : 0.0f;
+    }
     if (sub + 1 < nsub) {
       float* nh = stg + ((sub + 1) & 1) * 2 * plane;  // last read in B of sub - 1
       fuse_load(J, p0 + (sub + 1) * kFuseSP, p1, nh, nh + plane, vec, act, nact);
@@ -518,13 +536,14 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_fused_ff(Batch bt, in
         if (i < nact) dot2_add(acc[r], gh[i * kFuseSP + lane], gl[i * kFuseSP + lane], v.hi, v.lo);
       }
     }
-    if (chg) {  // C
-      const float wf = p < p1 ? (float)J.w[p] : 0.0f;
+    if (chg) {  // C (atoms with no active row add exact zeros: skipped)
       for (int a = warp; a < J.natom; a += kFuseWarps) {
+        const int i0 = aoff[a], i1 = aoff[a + 1];
+        if (i0 == i1) continue;
         Dot2 d{0.f, 0.f};
-        for (int m = J.shell_off[a]; m < J.shell_off[a + 1]; ++m) {
-          const int i = pos[m];
-          if (i >= 0) dot2_add(d, gh[i * kFuseSP + lane], gl[i * kFuseSP + lane], dcv[m].x, dcv[m].y);
+        for (int i = i0; i < i1; ++i) {
+          const float2 dc = dcv[act[i]];
+          dot2_add(d, gh[i * kFuseSP + lane], gl[i * kFuseSP + lane], dc.x, dc.y);
         }
         const float dv = d.s + d.c;
         const float term = wf * dv * dv;
@@ -743,7 +762,7 @@ __global__ void __launch_bounds__(kThreads) k_glisa_change_ff(Batch bt) {
 
 // Active shells of every point tile of a fused job (once per job, after the
 // basis): gact[tile][0..n) the shells with a nonzero value on the tile, in
-// order, n at gact[tile][S]. A float-float value is zero exactly when its
+// order, n at gact[tile][S]; gmask[tile] the same as a bit mask. A float-float value is zero exactly when its
 // high part is, so the passes that skip the other rows add exact zeros less.
 __global__ void __launch_bounds__(kThreads) k_glisa_active(Batch bt) {
   __shared__ int flag[kFuseMaxShells];
@@ -768,6 +787,12 @@ __global__ void __launch_bounds__(kThreads) k_glisa_active(Batch bt) {
     for (int m = 0; m < S; ++m)
       if (flag[m]) g[n++] = m;
     g[S] = n;
+  }
+  const int words = (S + 31) / 32;  // the same as a bit mask for the tensor-core Hessian
+  for (int wd = threadIdx.x; wd < words; wd += kThreads) {
+    unsigned b = 0u;
+    for (int k = 0; k < 32 && 32 * wd + k < S; ++k) b |= (unsigned)flag[32 * wd + k] << k;
+    J.gmask[(size_t)tile * words + wd] = b;
   }
 }
 

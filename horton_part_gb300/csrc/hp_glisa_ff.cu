@@ -762,7 +762,7 @@ __global__ void __launch_bounds__(kThreads) k_glisa_change_ff(Batch bt) {
 
 // Active shells of every point tile of a fused job (once per job, after the
 // basis): gact[tile][0..n) the shells with a nonzero value on the tile, in
-// order, n at gact[tile][S]; gmask[tile] the same as a bit mask. A float-float value is zero exactly when its
+// order, n at gact[tile][S]. A float-float value is zero exactly when its
 // high part is, so the passes that skip the other rows add exact zeros less.
 __global__ void __launch_bounds__(kThreads) k_glisa_active(Batch bt) {
   __shared__ int flag[kFuseMaxShells];
@@ -787,12 +787,6 @@ __global__ void __launch_bounds__(kThreads) k_glisa_active(Batch bt) {
     for (int m = 0; m < S; ++m)
       if (flag[m]) g[n++] = m;
     g[S] = n;
-  }
-  const int words = (S + 31) / 32;  // the same as a bit mask for the tensor-core Hessian
-  for (int wd = threadIdx.x; wd < words; wd += kThreads) {
-    unsigned b = 0u;
-    for (int k = 0; k < 32 && 32 * wd + k < S; ++k) b |= (unsigned)flag[32 * wd + k] << k;
-    J.gmask[(size_t)tile * words + wd] = b;
   }
 }
 

@@ -166,7 +166,6 @@ struct JobDev {
   float2* d2f;            // fused gLISA: w rho / rho0^2 as float pairs [npoint]
   double* hsum;           // gLISA tensor-core Hessian: refinement product H delta [nshell]
   int* gact;              // fused gLISA: per point tile the shells nonzero on it [ntile][nshell + 1]
-  unsigned* gmask;        // fused gLISA: the same as bit masks [ntile][(nshell + 31) / 32]
   float2* d1f;            // gLISA, gff: w rho / rho0 as float pairs, npoint
   float2* hvf;            // gLISA, gff: the refinement's hvec as float pairs, npoint
   float* hess_s;          // gLISA tensor-core Hessian: sqrt(w rho / rho0^2) as FP32, npoint

@@ -906,7 +906,6 @@ int32_t hp_job_create(hp_ctx* ctx, const hp_job_desc* d, hp_job** out) {
         add(&J.clipf, 4 * 4 * (size_t)S);
         if (S <= kFuseMaxShells) {
           add(&J.gact, 4 * (size_t)(S + 1) * ntile);
-          add(&J.gmask, 4 * (size_t)((S + 31) / 32) * ntile);
           add(&J.wrf, 16 * (size_t)N);
           add(&J.r0f, 8 * (size_t)N);
           add(&J.d2f, 8 * (size_t)N);

@@ -395,19 +395,14 @@ __global__ void __launch_bounds__(kTcThreads) k_glisa_hess_tc1(Batch bt) {
 
   // rows of this thread: warp + 16 r (< M); operands of two blocks in flight
   float v0[kT1RowsPerWarp], v1[kT1RowsPerWarp], s0 = 0.0f, s1 = 0.0f;
-  // fused jobs keep per point tile the mask of shells nonzero on it (a
-  // 32-point block lies in one tile): rows that are zero there are not loaded
-  const int mwords = (M + 31) / 32;
   auto load_block = [&](float (&v)[kT1RowsPerWarp], float& s, int kb) {
     const int p = kb + lane;
     const bool inr = p < pend;
     s = inr ? J.hess_s[p] : 0.0f;
-    const unsigned* mk = J.gmask ? J.gmask + (size_t)(kb / J.tile_points) * mwords : nullptr;
 #pragma unroll
     for (int r = 0; r < kT1RowsPerWarp; ++r) {
       const int m = warp + kTcWarps * r;
-      const bool act = m < M && (!mk || ((mk[m >> 5] >> (m & 31)) & 1u));
-      v[r] = (inr && act) ? J.gmat32[(size_t)m * N + p] : 0.0f;
+      v[r] = (inr && m < M) ? J.gmat32[(size_t)m * N + p] : 0.0f;
     }
   };
 

@@ -468,10 +468,18 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_fused_ff(Batch bt, in
     const float* gl = gh + plane;
     cp_async_wait<0>();
     __syncthreads();  // sub-tile sub visible; every thread is done with sub - 1
-    float wf = 0.0f;  // phase C weight, loaded early
-    if (chg) {
-      const int pc = p0 + sub * kFuseSP + lane;
-      wf = pc < p1 ? (float)J.w[pc] : 0.0f;
+    // per-point inputs of A' and C, loaded before phase A so that their
+    // latency overlaps it
+    const int pq = p0 + sub * kFuseSP + lane;
+    float wf = 0.0f;
+    float4 qpre = make_float4(0.f, 0.f, 0.f, 0.f);  // MODE 1: (w rho) and rho pairs; MODE 0: d2 pair
+    if (pq < p1) {
+      if (MODE == 1) qpre = J.wrf[pq];
+      else {
+        const float2 d2 = J.d2f[pq];
+        qpre = make_float4(d2.x, d2.y, 0.f, 0.f);
+      }
+      if (chg) wf = (float)J.w[pq];
     }
     if (sub + 1 < nsub) {
       float* nh = stg + ((sub + 1) & 1) * 2 * plane;  // last read in B of sub - 1
@@ -506,11 +514,10 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_fused_ff(Batch bt, in
     f2 v{0.f, 0.f};
     if (p < p1) {
       if (MODE == 0) {
-        const float2 d2 = J.d2f[p];
-        v = ffa::mul(dot2_ff(du), f2{d2.x, d2.y});
+        v = ffa::mul(dot2_ff(du), f2{qpre.x, qpre.y});
       } else {
         const f2 r0 = dot2_ff(du);
-        const float4 q = J.wrf[p];  // (w rho) and rho as float pairs
+        const float4 q = qpre;  // (w rho) and rho as float pairs
         const bool sick = below(f2{q.z, q.w}, cutp) || below(r0, cutp);
         if (!sick) v = ffa::div(f2{q.x, q.y}, r0);
         if (owner) {
@@ -650,6 +657,13 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_trials_fused(Batch bt
     const float* gl = gh + plane;
     cp_async_wait<0>();
     __syncthreads();
+    const int pq = p0 + sub * kFuseSP + lane;  // this lane's point: inputs loaded before A
+    float2 r0pre = make_float2(0.f, 0.f);
+    float4 qpre = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (pq < p1) {
+      r0pre = J.r0f[pq];
+      qpre = J.wrf[pq];
+    }
     if (sub + 1 < nsub) {
       float* nh = stg + ((sub + 1) & 1) * 2 * plane;
       fuse_load(J, p0 + (sub + 1) * kFuseSP, p1, nh, nh + plane, vec, act, nact);
@@ -689,8 +703,8 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_trials_fused(Batch bt
       }
       const f2 dsd = dot2_ff(sd);
       const f2 corr = ffa::neg(ffa::add(dot2_ff(sc), f2{at * dsd.hi, at * dsd.lo}));
-      const float2 r0p = J.r0f[p];
-      const float4 q = J.wrf[p];  // (w rho) and rho as float pairs
+      const float2 r0p = r0pre;
+      const float4 q = qpre;  // (w rho) and rho as float pairs
       const bool rs = below(f2{q.z, q.w}, cutp);
       const bool h0 = !(rs || below(f2{r0p.x, r0p.y}, cutp));
       const f2 dr = ffa::add(f2{at * u.hi, at * u.lo}, corr);

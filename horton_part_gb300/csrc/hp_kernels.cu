@@ -1443,82 +1443,55 @@ constexpr int kNewtonF32Max = 224;
 // preconditioner for the FP64-residual refinement as an FP64 one (same
 // direction error after each refinement step), at 1/64 of the FP64 cost per
 // operation on GB300. Same layout: factor in the lower triangle, its
-// transpose in the upper, dinv[k] = 1 / L[k][k].
-// Blocked right-looking form with panels of kCholB columns: warp 0 factors a
-// panel (one warp barrier per column, no block barrier), then all threads
-// apply the panel's rank-kCholB update to the trailing lower triangle in 4 x 4
-// register tiles; two block barriers per panel instead of one per column.
-constexpr int kCholB = 32;
-__device__ void chol_factor_f(float* L, int n, int* bad, float* dinv) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+// transpose in the upper, dinv[k] = 1 / L[k][k]; colbuf: 2n floats.
+__device__ void chol_factor_f(float* L, int n, int* bad, float* colbuf, float* dinv) {
+  __shared__ float piv_f[2], rinv_f[2];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
   const float tiny = 1e-37f;
-  for (int k0 = 0; k0 < n; k0 += kCholB) {
-    const int k1 = min(k0 + kCholB, n);
-    if (warp == 0) {
-      for (int j = k0; j < k1; ++j) {
-        const float d = L[j * n + j];
-        const float piv = sqrtf(fmaxf(d, tiny));
-        const float inv = 1.0f / piv;
-        __syncwarp();
-        if (lane == 0) {
-          if (!(d > 0.0f)) *bad = 1;
-          L[j * n + j] = piv;
-          dinv[j] = inv;
-        }
-        for (int i = j + 1 + lane; i < n; i += 32) L[i * n + j] *= inv;
-        __syncwarp();
-        for (int i = j + 1 + lane; i < n; i += 32) {  // the panel's later columns
-          const float lij = L[i * n + j];
-          const int cend = min(i, k1 - 1);
-          for (int c = j + 1; c <= cend; ++c) L[i * n + c] = fmaf(-lij, L[c * n + j], L[i * n + c]);
-        }
-        __syncwarp();
-      }
-    }
-    __syncthreads();
-    const int T = n - k1;  // trailing rows / columns
-    if (T > 0) {
-      const int nt = (T + 3) / 4;
-      const int ntiles = nt * (nt + 1) / 2;  // 4 x 4 tiles of the lower triangle
-      for (int t = threadIdx.x; t < ntiles; t += blockDim.x) {
-        int bi = (int)((sqrtf(8.0f * (float)t + 1.0f) - 1.0f) * 0.5f);
-        while (bi * (bi + 1) / 2 > t) --bi;
-        while ((bi + 1) * (bi + 2) / 2 <= t) ++bi;
-        const int bj = t - bi * (bi + 1) / 2;
-        const int i0 = k1 + 4 * bi, j0 = k1 + 4 * bj;
-        float acc[4][4];
-#pragma unroll
-        for (int q = 0; q < 4; ++q)
-#pragma unroll
-          for (int r = 0; r < 4; ++r) acc[q][r] = 0.0f;
-        for (int c = k0; c < k1; ++c) {
-          float a[4], b[4];
-#pragma unroll
-          for (int q = 0; q < 4; ++q) {
-            a[q] = i0 + q < n ? L[(i0 + q) * n + c] : 0.0f;
-            b[q] = j0 + q < n ? L[(j0 + q) * n + c] : 0.0f;
-          }
-#pragma unroll
-          for (int q = 0; q < 4; ++q)
-#pragma unroll
-            for (int r = 0; r < 4; ++r) acc[q][r] = fmaf(a[q], b[r], acc[q][r]);
-        }
-#pragma unroll
-        for (int q = 0; q < 4; ++q)
-#pragma unroll
-          for (int r = 0; r < 4; ++r) {
-            const int i = i0 + q, j = j0 + r;
-            if (i < n && j <= i) L[i * n + j] -= acc[q][r];
-          }
-      }
-    }
-    __syncthreads();
-  }
-  for (int e = threadIdx.x; e < n * n; e += blockDim.x) {  // transpose into the upper triangle
-    const int i = e / n, j = e - i * n;
-    if (j > i) L[e] = L[j * n + i];
+  float* col = colbuf;
+  float* nxt = colbuf + n;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) col[i] = L[(size_t)i * n];
+  if (threadIdx.x == 0 && n > 0) {
+    const float a = L[0];
+    if (!(a > 0.0f)) *bad = 1;
+    piv_f[0] = sqrtf(fmaxf(a, tiny));
+    rinv_f[0] = 1.0f / fmaxf(a, tiny);
   }
   __syncthreads();
+  for (int k = 0; k < n; ++k) {
+    const float piv = piv_f[k & 1], rinv = rinv_f[k & 1];
+    const float ipiv = piv * rinv;
+    if (threadIdx.x == 0) {
+      L[(size_t)k * n + k] = piv;
+      dinv[k] = ipiv;
+    }
+    for (int i = k + 1 + warp; i < n; i += nwarp) {
+      const float ci = col[i];
+      const float li = ci * rinv;
+      float* row = L + (size_t)i * n;
+      for (int j = k + 1 + lane; j <= i; j += 32) {
+        const float v = fmaf(-li, col[j], row[j]);
+        row[j] = v;
+        if (j == k + 1) {
+          nxt[i] = v;
+          if (i == k + 1) {
+            if (!(v > 0.0f)) *bad = 1;
+            piv_f[(k + 1) & 1] = sqrtf(fmaxf(v, tiny));
+            rinv_f[(k + 1) & 1] = 1.0f / fmaxf(v, tiny);
+          }
+        }
+      }
+      if (lane == 0) {
+        const float lik = ci * ipiv;
+        row[k] = lik;
+        L[(size_t)k * n + i] = lik;
+      }
+    }
+    __syncthreads();
+    float* t = col;
+    col = nxt;
+    nxt = t;
+  }
 }
 
 // y <- (L L^T)^-1 y by one warp (L as left by chol_factor_f, in shared
@@ -1577,8 +1550,8 @@ __device__ void chol_solve_warp_f(const float* L, const float* dinv, int n, floa
 constexpr int kNewtonSmemL = 200 * 1024;
 constexpr int kNewtonColMax = 256;
 // FP32 factor in shared memory (factor, 1 / diagonal and the right-hand side)
-// the step runs on one SM: 16 warps share each panel's trailing update
-constexpr int kNewtonThreads = 512;
+// the step runs on one SM; 32 warps keep more rows of each column step in flight
+constexpr int kNewtonThreads = 1024;
 constexpr int kNewtonWarps = kNewtonThreads / 32;
 static_assert(4 * (kNewtonF32Max * kNewtonF32Max + 2 * kNewtonF32Max) <= kNewtonSmemL, "FP32 factor");
 
@@ -1632,7 +1605,7 @@ __global__ void __launch_bounds__(kNewtonThreads) k_glisa_newton_step(Batch bt, 
     }
     for (int m = threadIdx.x; m < M; m += kNewtonThreads) J.delta[m] = 0.0;
     __syncthreads();
-    chol_factor_f(Lf, nf, &bad, dv);
+    chol_factor_f(Lf, nf, &bad, reinterpret_cast<float*>(col_smem), dv);
     if (!bad) {
       for (int i = threadIdx.x; i < nf; i += kNewtonThreads) yv[i] = (float)(-(1.0 + J.grad[fid[i]]));
       __syncthreads();

@@ -338,19 +338,32 @@ __global__ void __launch_bounds__(kTcThreads) k_glisa_hess_tc(Batch bt) {
 // ---------------------------------------------------------------------------
 constexpr int kT1Plane = kT1Rows * kTcK * 4;      // 32 KB
 constexpr int kT1Stage = 2 * kT1Plane;             // hi + lo
-constexpr int kT1OffBar = 2 * kT1Stage;            // 128 KB
-constexpr int kT1Smem = kT1OffBar + 64 + 1024;     // + alignment slack
+constexpr int kT1Stages = 3;                       // shared-memory stages
+constexpr int kT1OffBar = kT1Stages * kT1Stage;    // 192 KB
+constexpr int kT1Smem = kT1OffBar + 64 + 1024;     // + barriers, TMEM slot, alignment slack
 constexpr int kT1Cols = 512;                       // D1 at 0, D2 at 256
-constexpr int kT1RowsPerWarp = kT1Rows / kTcWarps; // 16
+constexpr int kT1StageWarps = 16;                  // producers: rows warp + 16 r
+constexpr int kT1RowsPerWarp = kT1Rows / kT1StageWarps;
+constexpr int kT1Threads = (kT1StageWarps + 1) * 32;  // + one warp that issues the MMAs
 
-__global__ void __launch_bounds__(kTcThreads) k_glisa_hess_tc1(Batch bt) {
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
+// Warp-specialised: warps 0..15 stage blocks into a ring of three shared-
+// memory stages and arrive on the stage's "full" barrier (one arrival per
+// warp); warp 16's elected lane waits for it, issues the block's MMAs and
+// commits them to the stage's "empty" barrier, which the producers wait on
+// before refilling the stage. No block-wide barrier per block: staging of
+// the next blocks overlaps the MMAs of the previous ones.
+__global__ void __launch_bounds__(kT1Threads) k_glisa_hess_tc1(Batch bt) {
   extern __shared__ uint8_t smem_raw[];
   const uint32_t raw = smem_u32(smem_raw);
   const uint32_t base = (raw + 1023u) & ~1023u;
   uint8_t* sm = smem_raw + (base - raw);
-  const uint32_t bar0 = base + kT1OffBar;  // stage s: bar0 + 8 s
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(sm + kT1OffBar + 16);
-  __shared__ int timed_out;
+  const uint32_t bar0 = base + kT1OffBar;  // full[s] at bar0 + 8 s, empty[s] at bar0 + 8 (3 + s)
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(sm + kT1OffBar + 8 * 2 * kT1Stages);
+  __shared__ volatile int timed_out;
 
   const int jb = find_job(bt, blockIdx.x);
   const JobDev& J = bt.jobs[jb];
@@ -360,12 +373,10 @@ __global__ void __launch_bounds__(kTcThreads) k_glisa_hess_tc1(Batch bt) {
   const int chunk = ((N + J.nsplit - 1) / J.nsplit + kTcK - 1) / kTcK * kTcK;
   const int pbeg = split * chunk;
   const int pend = min(pbeg + chunk, N);
+  const int nblk = pend > pbeg ? (pend - pbeg + kTcK - 1) / kTcK : 0;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int n1 = (M + 15) / 16 * 16;
   const int n2 = n1 > kTcM ? n1 - kTcM : 0;
-  const uint32_t idesc1 = idesc_tf32(n1);
-  const uint32_t idesc2 = idesc_tf32(n2 > 0 ? n2 : 16);
-  const uint32_t swz_col = (uint32_t)((((lane >> 2) ^ (warp & 7)) << 2) | (lane & 3));
 
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
@@ -373,17 +384,19 @@ __global__ void __launch_bounds__(kTcThreads) k_glisa_hess_tc1(Batch bt) {
                  "r"(kT1Cols));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
-  // rows M..255 of both planes of both stages stay zero
-  for (int e = threadIdx.x; e < 2 * 2 * (kT1Rows - M) * kTcK; e += kTcThreads) {
+  // rows M..255 of both planes of every stage stay zero
+  for (int e = threadIdx.x; e < kT1Stages * 2 * (kT1Rows - M) * kTcK; e += kT1Threads) {
     const int k = e % kTcK;
-    const int rr = e / kTcK;  // 0 .. 4 (256 - M) - 1
+    const int rr = e / kTcK;
     const int row = M + rr % (kT1Rows - M);
     const int plane = rr / (kT1Rows - M);  // stage * 2 + (lo ? 1 : 0)
     reinterpret_cast<uint32_t*>(sm + plane * kT1Plane)[row * kTcK + k] = 0u;
   }
   if (threadIdx.x == 0) {
-    mbar_init(bar0, 1);
-    mbar_init(bar0 + 8, 1);
+    for (int st = 0; st < kT1Stages; ++st) {
+      mbar_init(bar0 + 8 * st, kT1StageWarps);
+      mbar_init(bar0 + 8 * (kT1Stages + st), 1);
+    }
     timed_out = 0;
     asm volatile("fence.mbarrier_init.release.cluster;");
   }
@@ -393,110 +406,123 @@ __global__ void __launch_bounds__(kTcThreads) k_glisa_hess_tc1(Batch bt) {
   asm volatile("tcgen05.fence::after_thread_sync;");
   const uint32_t tmem = *tmem_slot;
 
-  // rows of this thread: warp + 16 r (< M); operands of two blocks in flight
-  float v0[kT1RowsPerWarp], v1[kT1RowsPerWarp], s0 = 0.0f, s1 = 0.0f;
-  auto load_block = [&](float (&v)[kT1RowsPerWarp], float& s, int kb) {
-    const int p = kb + lane;
-    const bool inr = p < pend;
-    s = inr ? J.hess_s[p] : 0.0f;
+  if (warp < kT1StageWarps) {
+    // producers: rows warp + 16 r (< M); operands of two blocks in registers
+    const uint32_t swz_col = (uint32_t)((((lane >> 2) ^ (warp & 7)) << 2) | (lane & 3));
+    float v0[kT1RowsPerWarp], v1[kT1RowsPerWarp], s0 = 0.0f, s1 = 0.0f;
+    auto load_block = [&](float (&v)[kT1RowsPerWarp], float& s, int k) {
+      const int p = pbeg + k * kTcK + lane;
+      const bool inr = p < pend;
+      s = inr ? J.hess_s[p] : 0.0f;
 #pragma unroll
-    for (int r = 0; r < kT1RowsPerWarp; ++r) {
-      const int m = warp + kTcWarps * r;
-      v[r] = (inr && m < M) ? J.gmat32[(size_t)m * N + p] : 0.0f;
-    }
-  };
-
-  int nblocks = 0;
-  auto do_block = [&](float (&v)[kT1RowsPerWarp], float& s, int kb) -> bool {
-    const int st = nblocks & 1;
-    uint8_t* stage = sm + st * kT1Stage;
-    uint32_t* x_hi = reinterpret_cast<uint32_t*>(stage);
-    uint32_t* x_lo = reinterpret_cast<uint32_t*>(stage + kT1Plane);
-    if (nblocks >= 2) {
-      if (!mbar_wait(bar0 + 8 * st, (uint32_t)(((nblocks >> 1) - 1) & 1))) timed_out = 1;
-    }
-#pragma unroll
-    for (int r = 0; r < kT1RowsPerWarp; ++r) {
-      const int row = warp + kTcWarps * r;
-      if (row < M) {
-        const float x = v[r] * s;
-        const uint32_t hi = __float_as_uint(x) & kTf32Mask;
-        const uint32_t off = (uint32_t)(row * kTcK) + swz_col;
-        x_hi[off] = hi;
-        x_lo[off] = __float_as_uint(x - __uint_as_float(hi));
+      for (int r = 0; r < kT1RowsPerWarp; ++r) {
+        const int m = warp + kT1StageWarps * r;
+        v[r] = (inr && m < M) ? J.gmat32[(size_t)m * N + p] : 0.0f;
       }
-    }
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    __syncthreads();
-    if (timed_out) return false;
-    if (threadIdx.x == 0) {
-      asm volatile("tcgen05.fence::after_thread_sync;");
-      const uint32_t hi = smem_u32(x_hi), lo = smem_u32(x_lo);
-      const uint32_t hi2 = hi + kTcM * kTcK * 4, lo2 = lo + kTcM * kTcK * 4;  // row 128
+    };
+    auto stage_block = [&](float (&v)[kT1RowsPerWarp], float& s, int k) -> bool {
+      const int st = k % kT1Stages;
+      if (k >= kT1Stages &&
+          !mbar_wait(bar0 + 8 * (kT1Stages + st), (uint32_t)((k / kT1Stages - 1) & 1))) {
+        timed_out = 1;
+        return false;
+      }
+      uint8_t* stage = sm + st * kT1Stage;
+      uint32_t* x_hi = reinterpret_cast<uint32_t*>(stage);
+      uint32_t* x_lo = reinterpret_cast<uint32_t*>(stage + kT1Plane);
 #pragma unroll
-      for (int k = 0; k < kTcK / 8; ++k) {
-        const uint32_t acc = (nblocks > 0 || k > 0) ? 1u : 0u;
-        umma_tf32(tmem, umma_desc(hi + 32 * k), umma_desc(hi + 32 * k), idesc1, acc);
-        umma_tf32(tmem, umma_desc(hi + 32 * k), umma_desc(lo + 32 * k), idesc1, 1u);
-        umma_tf32(tmem, umma_desc(lo + 32 * k), umma_desc(hi + 32 * k), idesc1, 1u);
-        if (n2 > 0) {
-          const uint32_t t2 = tmem + 256u;
-          umma_tf32(t2, umma_desc(hi2 + 32 * k), umma_desc(hi2 + 32 * k), idesc2, acc);
-          umma_tf32(t2, umma_desc(hi2 + 32 * k), umma_desc(lo2 + 32 * k), idesc2, 1u);
-          umma_tf32(t2, umma_desc(lo2 + 32 * k), umma_desc(hi2 + 32 * k), idesc2, 1u);
+      for (int r = 0; r < kT1RowsPerWarp; ++r) {
+        const int row = warp + kT1StageWarps * r;
+        if (row < M) {
+          const float x = v[r] * s;
+          const uint32_t hi = __float_as_uint(x) & kTf32Mask;
+          const uint32_t off = (uint32_t)(row * kTcK) + swz_col;
+          x_hi[off] = hi;
+          x_lo[off] = __float_as_uint(x - __uint_as_float(hi));
         }
       }
-      umma_commit(bar0 + 8 * st);
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      __syncwarp();
+      if (lane == 0) mbar_arrive(bar0 + 8 * st);
+      if (k + 2 < nblk) load_block(v, s, k + 2);
+      return true;
+    };
+    if (nblk > 0) load_block(v0, s0, 0);
+    if (nblk > 1) load_block(v1, s1, 1);
+    for (int k = 0; k < nblk; k += 2) {
+      if (timed_out || !stage_block(v0, s0, k)) break;
+      if (k + 1 < nblk && (timed_out || !stage_block(v1, s1, k + 1))) break;
     }
-    ++nblocks;
-    if (kb + 2 * kTcK < pend) load_block(v, s, kb + 2 * kTcK);
-    return true;
-  };
-
-  if (pbeg < pend) load_block(v0, s0, pbeg);
-  if (pbeg + kTcK < pend) load_block(v1, s1, pbeg + kTcK);
-  for (int kb = pbeg; kb < pend; kb += 2 * kTcK) {
-    if (!do_block(v0, s0, kb)) break;
-    if (kb + kTcK < pend && !do_block(v1, s1, kb + kTcK)) break;
-  }
-  if (nblocks > 0 && !timed_out) {
-    const int last = nblocks - 1;
-    if (!mbar_wait(bar0 + 8 * (last & 1), (uint32_t)((last >> 1) & 1))) timed_out = 1;
+  } else if (lane == 0) {
+    // the MMA issuer
+    const uint32_t idesc1 = idesc_tf32(n1);
+    const uint32_t idesc2 = idesc_tf32(n2 > 0 ? n2 : 16);
+    for (int k = 0; k < nblk; ++k) {
+      const int st = k % kT1Stages;
+      if (timed_out || !mbar_wait(bar0 + 8 * st, (uint32_t)((k / kT1Stages) & 1))) {
+        timed_out = 1;
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;");
+      const uint32_t hi = base + st * kT1Stage, lo = hi + kT1Plane;
+      const uint32_t hi2 = hi + kTcM * kTcK * 4, lo2 = lo + kTcM * kTcK * 4;  // row 128
+#pragma unroll
+      for (int kk = 0; kk < kTcK / 8; ++kk) {
+        const uint32_t acc = (k > 0 || kk > 0) ? 1u : 0u;
+        umma_tf32(tmem, umma_desc(hi + 32 * kk), umma_desc(hi + 32 * kk), idesc1, acc);
+        umma_tf32(tmem, umma_desc(hi + 32 * kk), umma_desc(lo + 32 * kk), idesc1, 1u);
+        umma_tf32(tmem, umma_desc(lo + 32 * kk), umma_desc(hi + 32 * kk), idesc1, 1u);
+        if (n2 > 0) {
+          const uint32_t t2 = tmem + 256u;
+          umma_tf32(t2, umma_desc(hi2 + 32 * kk), umma_desc(hi2 + 32 * kk), idesc2, acc);
+          umma_tf32(t2, umma_desc(hi2 + 32 * kk), umma_desc(lo2 + 32 * kk), idesc2, 1u);
+          umma_tf32(t2, umma_desc(lo2 + 32 * kk), umma_desc(hi2 + 32 * kk), idesc2, 1u);
+        }
+      }
+      umma_commit(bar0 + 8 * (kT1Stages + st));
+    }
+    if (nblk > 0 && !timed_out) {  // the last commit covers every MMA
+      const int last = nblk - 1;
+      if (!mbar_wait(bar0 + 8 * (kT1Stages + last % kT1Stages), (uint32_t)((last / kT1Stages) & 1)))
+        timed_out = 1;
+    }
   }
   asm volatile("tcgen05.fence::after_thread_sync;");
   __syncthreads();
 
-  // epilogue: warp w reads tensor-memory lanes 32 (w % 4) .. + 31; the four
-  // warps of a lane quarter take every fourth 8-column chunk; the split's
-  // partial is the packed lower triangle in FP32 (the accumulator's format)
+  // epilogue (producer warps): warp w reads tensor-memory lanes 32 (w % 4) ..
+  // + 31; the four warps of a lane quarter take every fourth 8-column chunk;
+  // the split's partial is the packed lower triangle in FP32
   float* out = reinterpret_cast<float*>(J.hpart) + (size_t)split * (M * (M + 1) / 2);
-  const int quad = warp & 3;
-  const bool ok = nblocks > 0 && !timed_out;
-  for (int part = 0; part < 2; ++part) {
-    const int ncols = part == 0 ? n1 : n2;
-    const int i = part * kTcM + quad * 32 + lane;  // row of H
-    for (int c = 8 * (warp >> 2); c < ncols; c += 32) {
-      uint32_t v[8];
-      if (ok) {
-        const uint32_t taddr = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(part * 256 + c);
-        asm volatile(
-            "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
-            : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
-              "=r"(v[7])
-            : "r"(taddr));
-        asm volatile("tcgen05.wait::ld.sync.aligned;");
-      } else {
+  const bool ok = nblk > 0 && !timed_out;
+  if (warp < kT1StageWarps) {
+    const int quad = warp & 3;
+    for (int part = 0; part < 2; ++part) {
+      const int ncols = part == 0 ? n1 : n2;
+      const int i = part * kTcM + quad * 32 + lane;  // row of H
+      for (int c = 8 * (warp >> 2); c < ncols; c += 32) {
+        uint32_t v[8];
+        if (ok) {
+          const uint32_t taddr = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(part * 256 + c);
+          asm volatile(
+              "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+              : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+                "=r"(v[7])
+              : "r"(taddr));
+          asm volatile("tcgen05.wait::ld.sync.aligned;");
+        } else {
 #pragma unroll
-        for (int q = 0; q < 8; ++q) v[q] = 0u;
-      }
-      if (i < M) {
+          for (int q = 0; q < 8; ++q) v[q] = 0u;
+        }
+        if (i < M) {
 #pragma unroll
-        for (int q = 0; q < 8; ++q) {
-          const int j = part * kTcM + c + q;
-          if (j >= M) continue;
-          const float h = __uint_as_float(v[q]);
-          if (j <= i) out[i * (i + 1) / 2 + j] = h;
-          else if (part == 0 && j >= kTcM) out[j * (j + 1) / 2 + i] = h;  // H[j][i], j below row 128
+          for (int q = 0; q < 8; ++q) {
+            const int j = part * kTcM + c + q;
+            if (j >= M) continue;
+            const float h = __uint_as_float(v[q]);
+            if (j <= i) out[i * (i + 1) / 2 + j] = h;
+            else if (part == 0 && j >= kTcM) out[j * (j + 1) / 2 + i] = h;  // H[j][i], j below row 128
+          }
         }
       }
     }
@@ -525,7 +551,7 @@ void launch_glisa_hess_tc(const HostBatch& hb, cudaStream_t st, int max_shells, 
   }
   if (hb.blocks[K_HESS] <= 0) return;
   if (min_shells <= kT1Rows) {
-    k_glisa_hess_tc1<<<hb.blocks[K_HESS], kTcThreads, kT1Smem, st>>>(hb.b[K_HESS]);
+    k_glisa_hess_tc1<<<hb.blocks[K_HESS], kT1Threads, kT1Smem, st>>>(hb.b[K_HESS]);
     ++g_launch_count;
   }
   if (max_shells > kT1Rows) {

@@ -363,10 +363,12 @@ __host__ __device__ constexpr size_t fuse_smem_bytes(int S) {
 // shells with a nonzero value in the tile) of both planes into gh / gl
 // ([nact][kFuseSP], row i holds shell act[i]); columns at or past p1 are
 // zero-filled. vec: 16-byte copies (npoint % 4 == 0, so every row segment
-// starts 16-byte aligned and p1 is a multiple of 4).
-__device__ __forceinline__ void fuse_load(const JobDev& J, int q0, int p1, float* gh, float* gl,
-                                          bool vec, const int* act, int nact) {
-  const size_t N = J.npoint;
+// starts 16-byte aligned and p1 is a multiple of 4). The job's pointers come
+// in registers: the cp.async statements clobber memory, which would otherwise
+// reload them from the job table on every call.
+__device__ __forceinline__ void fuse_load(const float* __restrict__ g32, const float* __restrict__ glo,
+                                          size_t N, int q0, int p1, float* gh, float* gl, bool vec,
+                                          const int* act, int nact) {
   if (vec) {
     constexpr int C = kFuseSP / 4;  // 16-byte chunks per row
     const int c = threadIdx.x % C;
@@ -375,8 +377,8 @@ __device__ __forceinline__ void fuse_load(const JobDev& J, int q0, int p1, float
     const int pc = in ? p : q0;
     for (int i = threadIdx.x / C; i < nact; i += kFuseThreads / C) {
       const size_t off = (size_t)act[i] * N + pc;
-      cp_async16(gh + i * kFuseSP + 4 * c, J.gmat32 + off, in);
-      cp_async16(gl + i * kFuseSP + 4 * c, J.gmat_lo + off, in);
+      cp_async16(gh + i * kFuseSP + 4 * c, g32 + off, in);
+      cp_async16(gl + i * kFuseSP + 4 * c, glo + off, in);
     }
   } else {
     const int c = threadIdx.x % kFuseSP;
@@ -385,8 +387,8 @@ __device__ __forceinline__ void fuse_load(const JobDev& J, int q0, int p1, float
     const int pc = in ? p : q0;
     for (int i = threadIdx.x / kFuseSP; i < nact; i += kFuseThreads / kFuseSP) {
       const size_t off = (size_t)act[i] * N + pc;
-      cp_async4(gh + i * kFuseSP + c, J.gmat32 + off, in);
-      cp_async4(gl + i * kFuseSP + c, J.gmat_lo + off, in);
+      cp_async4(gh + i * kFuseSP + c, g32 + off, in);
+      cp_async4(gl + i * kFuseSP + c, glo + off, in);
     }
   }
 }
@@ -436,9 +438,19 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_fused_ff(Batch bt, in
   const int p1 = min(p0 + J.tile_points, J.npoint);
   const int nsub = (p1 - p0 + kFuseSP - 1) / kFuseSP;
   const bool vec = (J.npoint & 3) == 0;
+  const float* __restrict__ g32 = J.gmat32;
+  const float* __restrict__ glo = J.gmat_lo;
+  const size_t NN = J.npoint;
+  const float4* __restrict__ wrfp = J.wrf;
+  const float2* __restrict__ d2in = J.d2f;
+  const double* __restrict__ wp = J.w;
+  float2* r0fo = J.r0f;
+  float2* d2fo = J.d2f;
+  float* hso = J.hess_s;
+  const int natom = J.natom;
   const int nact = load_active(J, tile, act, pos);
   __syncthreads();
-  fuse_load(J, p0, p1, stg, stg + plane, vec, act, nact);
+  fuse_load(g32, glo, NN, p0, p1, stg, stg + plane, vec, act, nact);
   cp_async_commit();
   if (MODE == 1)
     for (int a = threadIdx.x; a <= J.natom; a += kFuseThreads) {
@@ -474,16 +486,16 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_fused_ff(Batch bt, in
     float wf = 0.0f;
     float4 qpre = make_float4(0.f, 0.f, 0.f, 0.f);  // MODE 1: (w rho) and rho pairs; MODE 0: d2 pair
     if (pq < p1) {
-      if (MODE == 1) qpre = J.wrf[pq];
+      if (MODE == 1) qpre = wrfp[pq];
       else {
-        const float2 d2 = J.d2f[pq];
+        const float2 d2 = d2in[pq];
         qpre = make_float4(d2.x, d2.y, 0.f, 0.f);
       }
-      if (chg) wf = (float)J.w[pq];
+      if (chg) wf = (float)wp[pq];
     }
     if (sub + 1 < nsub) {
       float* nh = stg + ((sub + 1) & 1) * 2 * plane;  // last read in B of sub - 1
-      fuse_load(J, p0 + (sub + 1) * kFuseSP, p1, nh, nh + plane, vec, act, nact);
+      fuse_load(g32, glo, NN, p0 + (sub + 1) * kFuseSP, p1, nh, nh + plane, vec, act, nact);
       cp_async_commit();
     }
     {  // A (active rows i = warp mod 8)
@@ -522,9 +534,9 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_fused_ff(Batch bt, in
         if (!sick) v = ffa::div(f2{q.x, q.y}, r0);
         if (owner) {
           const f2 dd = sick ? f2{0.f, 0.f} : ffa::div(v, r0);
-          J.r0f[p] = make_float2(r0.hi, r0.lo);
-          J.d2f[p] = make_float2(dd.hi, dd.lo);
-          J.hess_s[p] = sqrtf(dd.hi);
+          r0fo[p] = make_float2(r0.hi, r0.lo);
+          d2fo[p] = make_float2(dd.hi, dd.lo);
+          hso[p] = sqrtf(dd.hi);
           if (below(r0, negp)) nneg += 1.0f;
           if (!sick) {  // w rho ln(rho / rho0)
             const f2 ratio = ffa::div(f2{q.z, q.w}, r0);
@@ -544,7 +556,7 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_fused_ff(Batch bt, in
       }
     }
     if (chg) {  // C (atoms with no active row add exact zeros: skipped)
-      for (int a = warp; a < J.natom; a += kFuseWarps) {
+      for (int a = warp; a < natom; a += kFuseWarps) {
         const int i0 = aoff[a], i1 = aoff[a + 1];
         if (i0 == i1) continue;
         Dot2 d{0.f, 0.f};
@@ -633,14 +645,20 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_trials_fused(Batch bt
   int* act = reinterpret_cast<int*>(reinterpret_cast<float2*>(part + kFuseWarps * kFuseSP) + 64) +
              2 * (2 * kFuseWarps + 2);  // after the exp table and block sums of the fused layout
   int* pos = act + S;
+  int* cpos = pos + S;  // per clipped shell its active row on this tile (-1: zero here)
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int p0 = tile * J.tile_points;
   const int p1 = min(p0 + J.tile_points, J.npoint);
   const int nsub = (p1 - p0 + kFuseSP - 1) / kFuseSP;
   const bool vec = (J.npoint & 3) == 0;
+  const float* __restrict__ g32 = J.gmat32;
+  const float* __restrict__ glo = J.gmat_lo;
+  const size_t NN = J.npoint;
+  const float2* __restrict__ r0in = J.r0f;
+  const float4* __restrict__ wrfp = J.wrf;
   const int nact = load_active(J, tile, act, pos);
   __syncthreads();
-  fuse_load(J, p0, p1, stg, stg + plane, vec, act, nact);
+  fuse_load(g32, glo, NN, p0, p1, stg, stg + plane, vec, act, nact);
   cp_async_commit();
   for (int i = threadIdx.x; i < S; i += kFuseThreads) xv[i] = split2(J.delta[i]);
   const int t = warp;  // this warp's trial: step 2^-t
@@ -649,6 +667,7 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_trials_fused(Batch bt
   const int* tm = J.clip + S + 1;
   int kt = 0;  // clipped shells with t_m > t: a prefix of the list (sorted, largest first)
   while (kt < nclip && tm[kt] > t) ++kt;
+  for (int k = threadIdx.x; k < nclip; k += kFuseThreads) cpos[k] = pos[J.clip[k]];
   const float4* cd = reinterpret_cast<const float4*>(J.clipf);
   const float2 cutp = split2(J.density_cutoff);
   float ah = 0.0f, al = 0.0f;
@@ -661,12 +680,12 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_trials_fused(Batch bt
     float2 r0pre = make_float2(0.f, 0.f);
     float4 qpre = make_float4(0.f, 0.f, 0.f, 0.f);
     if (pq < p1) {
-      r0pre = J.r0f[pq];
-      qpre = J.wrf[pq];
+      r0pre = r0in[pq];
+      qpre = wrfp[pq];
     }
     if (sub + 1 < nsub) {
       float* nh = stg + ((sub + 1) & 1) * 2 * plane;
-      fuse_load(J, p0 + (sub + 1) * kFuseSP, p1, nh, nh + plane, vec, act, nact);
+      fuse_load(g32, glo, NN, p0 + (sub + 1) * kFuseSP, p1, nh, nh + plane, vec, act, nact);
       cp_async_commit();
     }
     {  // A (active rows i = warp mod 8)
@@ -694,7 +713,7 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_trials_fused(Batch bt
       const f2 u = dot2_ff(du);
       Dot2 sc{0.f, 0.f}, sd{0.f, 0.f};
       for (int k = 0; k < kt; ++k) {
-        const int i = pos[J.clip[k]];
+        const int i = cpos[k];
         if (i < 0) continue;  // the shell is zero on this tile
         const float4 v = cd[k];
         const float g1 = gh[i * kFuseSP + lane], g2 = gl[i * kFuseSP + lane];

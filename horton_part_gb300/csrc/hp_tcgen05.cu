@@ -107,6 +107,27 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
   return false;
 }
 
+// try_wait that may suspend the thread for up to `ns` nanoseconds (woken
+// when the phase completes), so that waiting warps issue few instructions.
+__device__ __forceinline__ bool mbar_try_wait_sleep(uint32_t bar, uint32_t parity, uint32_t ns) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n"
+      " selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity), "r"(ns)
+      : "memory");
+  return ok != 0;
+}
+
+// Bounded wait with suspension: at most kSleepWaitLimit tries of up to 1 us.
+constexpr int kSleepWaitLimit = 1 << 22;
+__device__ __forceinline__ bool mbar_wait_sleep(uint32_t bar, uint32_t parity) {
+  for (int i = 0; i < kSleepWaitLimit; ++i)
+    if (mbar_try_wait_sleep(bar, parity, 1000u)) return true;
+  return false;
+}
+
 __device__ __forceinline__ void umma_tf32(uint32_t tmem, uint64_t a, uint64_t b, uint32_t idesc,
                                           uint32_t acc) {
   asm volatile(
@@ -407,23 +428,27 @@ __global__ void __launch_bounds__(kT1Threads) k_glisa_hess_tc1(Batch bt) {
   const uint32_t tmem = *tmem_slot;
 
   if (warp < kT1StageWarps) {
-    // producers: rows warp + 16 r (< M); operands of two blocks in registers
+    // producers: rows warp + 16 r (< M); operands of two blocks in registers.
+    // The job's pointers live in registers: the asm statements below clobber
+    // memory, which would otherwise reload them from the job table each block.
+    const float* __restrict__ g32 = J.gmat32;
+    const float* __restrict__ hsv = J.hess_s;
     const uint32_t swz_col = (uint32_t)((((lane >> 2) ^ (warp & 7)) << 2) | (lane & 3));
     float v0[kT1RowsPerWarp], v1[kT1RowsPerWarp], s0 = 0.0f, s1 = 0.0f;
     auto load_block = [&](float (&v)[kT1RowsPerWarp], float& s, int k) {
       const int p = pbeg + k * kTcK + lane;
       const bool inr = p < pend;
-      s = inr ? J.hess_s[p] : 0.0f;
+      s = inr ? hsv[p] : 0.0f;
 #pragma unroll
       for (int r = 0; r < kT1RowsPerWarp; ++r) {
         const int m = warp + kT1StageWarps * r;
-        v[r] = (inr && m < M) ? J.gmat32[(size_t)m * N + p] : 0.0f;
+        v[r] = (inr && m < M) ? g32[(size_t)m * N + p] : 0.0f;
       }
     };
     auto stage_block = [&](float (&v)[kT1RowsPerWarp], float& s, int k) -> bool {
       const int st = k % kT1Stages;
       if (k >= kT1Stages &&
-          !mbar_wait(bar0 + 8 * (kT1Stages + st), (uint32_t)((k / kT1Stages - 1) & 1))) {
+          !mbar_wait_sleep(bar0 + 8 * (kT1Stages + st), (uint32_t)((k / kT1Stages - 1) & 1))) {
         timed_out = 1;
         return false;
       }
@@ -459,7 +484,7 @@ __global__ void __launch_bounds__(kT1Threads) k_glisa_hess_tc1(Batch bt) {
     const uint32_t idesc2 = idesc_tf32(n2 > 0 ? n2 : 16);
     for (int k = 0; k < nblk; ++k) {
       const int st = k % kT1Stages;
-      if (timed_out || !mbar_wait(bar0 + 8 * st, (uint32_t)((k / kT1Stages) & 1))) {
+      if (timed_out || !mbar_wait_sleep(bar0 + 8 * st, (uint32_t)((k / kT1Stages) & 1))) {
         timed_out = 1;
         break;
       }
@@ -483,7 +508,7 @@ __global__ void __launch_bounds__(kT1Threads) k_glisa_hess_tc1(Batch bt) {
     }
     if (nblk > 0 && !timed_out) {  // the last commit covers every MMA
       const int last = nblk - 1;
-      if (!mbar_wait(bar0 + 8 * (kT1Stages + last % kT1Stages), (uint32_t)((last / kT1Stages) & 1)))
+      if (!mbar_wait_sleep(bar0 + 8 * (kT1Stages + last % kT1Stages), (uint32_t)((last / kT1Stages) & 1)))
         timed_out = 1;
     }
   }

@@ -126,7 +126,7 @@ POLISH = True
 # capture of the same workload (ncu --set full; the summaries in profiles/
 # give the commands). Keyed by (workload, precision, kernel family).
 NCU_TRAFFIC = {
-    ("glisa-c6h10n2o2", "mixed", "k_glisa_hess_tc1"): 365.34e6 + 3.81e6,
+    ("glisa-c6h10n2o2", "mixed", "k_glisa_hess_tc1"): 364.90e6 + 3.19e6,
     ("glisa-c6h10n2o2", "mixed", "k_glisa_fused_ff<1>"): 734.05e6 + 22.20e6,
     ("mbis-chain60", "mixed", "inner"): 125.81e6 + 3.46e6,
 }
@@ -305,14 +305,21 @@ def config_of(w, args, precision):
     mol = mols[0]
     natom = sum(m.natom for m in mols)
     npoint = sum(m.npoint for m in mols)
-    # bytes resident per step: rho_a (A x N values) dominates
-    resident = sum(m.natom * m.npoint for m in mols) * (4 if precision == "mixed" else 8)
+    # bytes streamed per pass: the basis matrix G (S x N, float-float planes or
+    # FP64) for gLISA, rho_a (A x N values) for the other schemes
+    if w["scheme"] == "glisa":
+        resident = sum(sum(w["helper"].get_nshell(z) for z in m.numbers) * m.npoint
+                       for m in mols) * 8
+        what = "of G"
+    else:
+        resident = sum(m.natom * m.npoint for m in mols) * (4 if precision == "mixed" else 8)
+        what = "of rho_a"
     cfg = {"workload": w["name"], "molecules": len(mols), "natom": int(natom),
            "npoint": int(npoint),
            "nshell": int(sum(w["helper"].get_nshell(z) for z in mol.numbers)) if w["helper"] else None,
            "solver": w["solver"], "threshold": w["threshold"], "precision": precision,
            "polish": POLISH if precision == "mixed" else None,
-           "l2": ("inputs larger than L2 (%.0f MB of rho_a per pass)" % (resident / 1e6))
+           "l2": ("inputs larger than L2 (%.0f MB %s per pass)" % (resident / 1e6, what))
            if resident > 129e6 else "inputs smaller than L2 (%.0f MB)" % (resident / 1e6),
            "parallelism": f"replicas{args.gpus}"}
     return cfg

@@ -364,7 +364,7 @@ constexpr int kT1OffBar = kT1Stages * kT1Stage;    // 192 KB
 constexpr int kT1Smem = kT1OffBar + 64 + 1024;     // + barriers, TMEM slot, alignment slack
 constexpr int kT1Cols = 512;                       // D1 at 0, D2 at 256
 constexpr int kT1StageWarps = 16;                  // producers: rows warp + 16 r
-constexpr int kT1RowsPerWarp = kT1Rows / kT1StageWarps;
+constexpr int kT1Items = kT1Rows * (kTcK / 4) / (kT1StageWarps * 32);  // 16-byte chunks per producer
 constexpr int kT1Threads = (kT1StageWarps + 1) * 32;  // + one warp that issues the MMAs
 
 __device__ __forceinline__ void mbar_arrive(uint32_t bar) {
@@ -428,24 +428,56 @@ __global__ void __launch_bounds__(kT1Threads) k_glisa_hess_tc1(Batch bt) {
   const uint32_t tmem = *tmem_slot;
 
   if (warp < kT1StageWarps) {
-    // producers: rows warp + 16 r (< M); operands of two blocks in registers.
+    // producers: thread t stages the 16-byte chunk c = t mod 8 (points 4c ..
+    // 4c + 3 of the block) of rows t / 8 + 64 j (< M): one 16-byte load of G,
+    // the four scales, and one 16-byte store per plane into the chunk's
+    // swizzled position (c ^ (row mod 8)). Operands of two blocks in registers.
     // The job's pointers live in registers: the asm statements below clobber
     // memory, which would otherwise reload them from the job table each block.
     const float* __restrict__ g32 = J.gmat32;
     const float* __restrict__ hsv = J.hess_s;
-    const uint32_t swz_col = (uint32_t)((((lane >> 2) ^ (warp & 7)) << 2) | (lane & 3));
-    float v0[kT1RowsPerWarp], v1[kT1RowsPerWarp], s0 = 0.0f, s1 = 0.0f;
-    auto load_block = [&](float (&v)[kT1RowsPerWarp], float& s, int k) {
-      const int p = pbeg + k * kTcK + lane;
-      const bool inr = p < pend;
-      s = inr ? hsv[p] : 0.0f;
+    const int tid = threadIdx.x;
+    const int c = tid & 7;
+    const int r0 = tid >> 3;
+    const bool vec = (N & 3) == 0;  // 16-byte aligned rows; else element loads
+    float4 v0[kT1Items], v1[kT1Items], s0 = make_float4(0.f, 0.f, 0.f, 0.f), s1 = s0;
+    auto load_block = [&](float4 (&v)[kT1Items], float4& s, int k) {
+      const int p = pbeg + k * kTcK + 4 * c;
+      if (vec) {
+        const bool inr = p < pend;  // pend is a multiple of 4 when N is
+        s = inr ? *reinterpret_cast<const float4*>(hsv + p) : make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
-      for (int r = 0; r < kT1RowsPerWarp; ++r) {
-        const int m = warp + kT1StageWarps * r;
-        v[r] = (inr && m < M) ? g32[(size_t)m * N + p] : 0.0f;
+        for (int j = 0; j < kT1Items; ++j) {
+          const int row = r0 + 64 * j;
+          v[j] = (inr && row < M) ? *reinterpret_cast<const float4*>(g32 + (size_t)row * N + p)
+                                  : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+      } else {
+        float sv[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) sv[q] = p + q < pend ? hsv[p + q] : 0.0f;
+        s = make_float4(sv[0], sv[1], sv[2], sv[3]);
+#pragma unroll
+        for (int j = 0; j < kT1Items; ++j) {
+          const int row = r0 + 64 * j;
+          float e[4];
+#pragma unroll
+          for (int q = 0; q < 4; ++q) e[q] = (row < M && p + q < pend) ? g32[(size_t)row * N + p + q] : 0.0f;
+          v[j] = make_float4(e[0], e[1], e[2], e[3]);
+        }
       }
     };
-    auto stage_block = [&](float (&v)[kT1RowsPerWarp], float& s, int k) -> bool {
+    auto split_store = [&](uint8_t* hi_row, uint8_t* lo_row, float4 x) {
+      const uint4 h = make_uint4(__float_as_uint(x.x) & kTf32Mask, __float_as_uint(x.y) & kTf32Mask,
+                                 __float_as_uint(x.z) & kTf32Mask, __float_as_uint(x.w) & kTf32Mask);
+      const uint4 l = make_uint4(__float_as_uint(x.x - __uint_as_float(h.x)),
+                                 __float_as_uint(x.y - __uint_as_float(h.y)),
+                                 __float_as_uint(x.z - __uint_as_float(h.z)),
+                                 __float_as_uint(x.w - __uint_as_float(h.w)));
+      *reinterpret_cast<uint4*>(hi_row) = h;
+      *reinterpret_cast<uint4*>(lo_row) = l;
+    };
+    auto stage_block = [&](float4 (&v)[kT1Items], float4& s, int k) -> bool {
       const int st = k % kT1Stages;
       if (k >= kT1Stages &&
           !mbar_wait_sleep(bar0 + 8 * (kT1Stages + st), (uint32_t)((k / kT1Stages - 1) & 1))) {
@@ -453,17 +485,13 @@ __global__ void __launch_bounds__(kT1Threads) k_glisa_hess_tc1(Batch bt) {
         return false;
       }
       uint8_t* stage = sm + st * kT1Stage;
-      uint32_t* x_hi = reinterpret_cast<uint32_t*>(stage);
-      uint32_t* x_lo = reinterpret_cast<uint32_t*>(stage + kT1Plane);
 #pragma unroll
-      for (int r = 0; r < kT1RowsPerWarp; ++r) {
-        const int row = warp + kT1StageWarps * r;
+      for (int j = 0; j < kT1Items; ++j) {
+        const int row = r0 + 64 * j;
         if (row < M) {
-          const float x = v[r] * s;
-          const uint32_t hi = __float_as_uint(x) & kTf32Mask;
-          const uint32_t off = (uint32_t)(row * kTcK) + swz_col;
-          x_hi[off] = hi;
-          x_lo[off] = __float_as_uint(x - __uint_as_float(hi));
+          const float4 x = make_float4(v[j].x * s.x, v[j].y * s.y, v[j].z * s.z, v[j].w * s.w);
+          const int off = row * (kTcK * 4) + ((c ^ (row & 7)) << 4);
+          split_store(stage + off, stage + kT1Plane + off, x);
         }
       }
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");

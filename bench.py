@@ -582,6 +582,8 @@ def run_ours(args):
             "max_abs_dq_e": float(np.abs(rm["charges"] - rd["charges"]).max()),
             "max_scaled_dparam": dp, "polish_iterations": int(im.polish_iterations),
             "niter_mixed": int(im.niter)}
+        if w["scheme"] == "glisa":
+            line["accuracy_vs_fp64"]["newton_fp64_factors"] = int(im.f64_factors)
     if rank == 0 and world == 1 and not args.no_cpu:
         r, sample, threads = cpu_sample(w, 2 if w["scheme"] == "glisa" else 3)
         line["cpu_baseline"] = {"value": r, "unit": UNIT, "cores": threads, "kind": "port",

@@ -59,7 +59,7 @@ class JobInfo(ctypes.Structure):
         ("change", ctypes.c_double), ("done", ctypes.c_int32), ("status", ctypes.c_int32),
         ("warnings", ctypes.c_uint32), ("converged", ctypes.c_int32),
         ("device_bytes", ctypes.c_int64), ("point_atom_evals", ctypes.c_double),
-        ("polish_iterations", ctypes.c_int32), ("reserved", ctypes.c_int32),
+        ("polish_iterations", ctypes.c_int32), ("f64_factors", ctypes.c_int32),
     ]
 
 

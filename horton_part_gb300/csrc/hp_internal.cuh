@@ -65,6 +65,7 @@ enum MailI {
   MI_ERR = 2,         // ErrFlag bits
   MI_WARN = 3,        // warning bits (HP_WARN_*)
   MI_CONVERGED = 4,   // gLISA solver converged flag
+  MI_F64_FACTORS = 5, // gLISA Newton steps of a tensor-core job factored in FP64
   MI_COUNT = 8
 };
 struct Mailbox {

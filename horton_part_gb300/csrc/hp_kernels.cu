@@ -1443,55 +1443,157 @@ constexpr int kNewtonF32Max = 224;
 // preconditioner for the FP64-residual refinement as an FP64 one (same
 // direction error after each refinement step), at 1/64 of the FP64 cost per
 // operation on GB300. Same layout: factor in the lower triangle, its
-// transpose in the upper, dinv[k] = 1 / L[k][k]; colbuf: 2n floats.
-__device__ void chol_factor_f(float* L, int n, int* bad, float* colbuf, float* dinv) {
-  __shared__ float piv_f[2], rinv_f[2];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+// transpose in the upper, dinv[k] = 1 / L[k][k].
+//
+// Right-looking in panels of 8 columns, two block barriers per panel:
+//  (1) warp 0 factors the panel's 8 x 8 diagonal block (lane t holds row t;
+//      pivots and multipliers travel by shuffles) into pl / pr;
+//  (2) one thread per trailing row i forms its 8 panel entries (a triangular
+//      solve against pl) and stores them in the upper copy, row k + s;
+//  (3) the rank-8 update of the trailing lower triangle in 4 x 4 register
+//      tiles by warps 1.., while warp 0 updates the next diagonal block
+//      itself and goes straight on to (1) for the next panel.
+// The upper copy (rows of finished panels) is never read as part of the
+// trailing matrix; one pass at the end mirrors it into the lower triangle.
+// Every element's updates are applied panel by panel, columns in order, so
+// the factor does not depend on the thread count.
+constexpr int kCholPanel = 8;
+
+// (1): the diagonal block at rows / columns kk.. of L, on warp 0
+__device__ __forceinline__ void chol_diag_f(float* L, int n, int kk, float (*pl)[kCholPanel],
+                                            float* pr, float* dinv, int* bad) {
+  const int t = threadIdx.x & 31;
+  const int nb = min(kCholPanel, n - kk);
   const float tiny = 1e-37f;
-  float* col = colbuf;
-  float* nxt = colbuf + n;
-  for (int i = threadIdx.x; i < n; i += blockDim.x) col[i] = L[(size_t)i * n];
-  if (threadIdx.x == 0 && n > 0) {
-    const float a = L[0];
-    if (!(a > 0.0f)) *bad = 1;
-    piv_f[0] = sqrtf(fmaxf(a, tiny));
-    rinv_f[0] = 1.0f / fmaxf(a, tiny);
+  float a[kCholPanel], lrow[kCholPanel];
+#pragma unroll
+  for (int u = 0; u < kCholPanel; ++u) {
+    a[u] = (t < nb && u <= t) ? L[(size_t)(kk + t) * n + kk + u] : (u == t ? 1.0f : 0.0f);
+    lrow[u] = 0.0f;
   }
-  __syncthreads();
-  for (int k = 0; k < n; ++k) {
-    const float piv = piv_f[k & 1], rinv = rinv_f[k & 1];
-    const float ipiv = piv * rinv;
-    if (threadIdx.x == 0) {
-      L[(size_t)k * n + k] = piv;
-      dinv[k] = ipiv;
+  bool neg = false;
+  float mypiv = 1.0f, myr = 1.0f;
+#pragma unroll
+  for (int s = 0; s < kCholPanel; ++s) {
+    const float d = __shfl_sync(0xffffffffu, a[s], s);
+    const float dd = fmaxf(d, tiny);
+    const float piv = sqrtf(dd);
+    const float r = piv / dd;  // 1 / sqrt(d)
+    if (s < nb && !(d > 0.0f)) neg = true;
+    if (t == s) {
+      mypiv = piv;
+      myr = r;
     }
-    for (int i = k + 1 + warp; i < n; i += nwarp) {
-      const float ci = col[i];
-      const float li = ci * rinv;
-      float* row = L + (size_t)i * n;
-      for (int j = k + 1 + lane; j <= i; j += 32) {
-        const float v = fmaf(-li, col[j], row[j]);
-        row[j] = v;
-        if (j == k + 1) {
-          nxt[i] = v;
-          if (i == k + 1) {
-            if (!(v > 0.0f)) *bad = 1;
-            piv_f[(k + 1) & 1] = sqrtf(fmaxf(v, tiny));
-            rinv_f[(k + 1) & 1] = 1.0f / fmaxf(v, tiny);
-          }
-        }
-      }
-      if (lane == 0) {
-        const float lik = ci * ipiv;
-        row[k] = lik;
-        L[(size_t)k * n + i] = lik;
+    const float lts = t > s ? a[s] * r : 0.0f;
+    lrow[s] = lts;
+#pragma unroll
+    for (int u = s + 1; u < kCholPanel; ++u) {
+      const float lus = __shfl_sync(0xffffffffu, lts, u);
+      if (t >= u) a[u] = fmaf(-lts, lus, a[u]);
+    }
+  }
+  if (t < nb) {
+    dinv[kk + t] = myr;
+    pr[t] = myr;
+    L[(size_t)(kk + t) * n + kk + t] = mypiv;
+#pragma unroll
+    for (int s = 0; s < kCholPanel; ++s) {
+      pl[t][s] = lrow[s];
+      if (s < t) L[(size_t)(kk + s) * n + kk + t] = lrow[s];  // upper copy
+    }
+  }
+  if (neg && t == 0) *bad = 1;
+}
+
+__device__ void chol_factor_f(float* L, int n, int* bad, float* dinv) {
+  __shared__ float pl[kCholPanel][kCholPanel];
+  __shared__ float pr[kCholPanel];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (warp == 0 && n > 0) chol_diag_f(L, n, 0, pl, pr, dinv, bad);
+  __syncthreads();
+  for (int k = 0; k + kCholPanel < n; k += kCholPanel) {
+    const int k8 = k + kCholPanel;
+    // (2) panel entries of the trailing rows
+    for (int i = k8 + threadIdx.x; i < n; i += blockDim.x) {
+      const float* row = L + (size_t)i * n + k;
+      float x[kCholPanel];
+#pragma unroll
+      for (int s = 0; s < kCholPanel; ++s) {
+        float v = row[s];
+#pragma unroll
+        for (int u = 0; u < s; ++u) v = fmaf(-x[u], pl[s][u], v);
+        x[s] = v * pr[s];
+        L[(size_t)(k + s) * n + i] = x[s];
       }
     }
     __syncthreads();
-    float* t = col;
-    col = nxt;
-    nxt = t;
+    const float* P = L + (size_t)k * n;  // panel entry s of row i at P[s n + i]
+    if (warp == 0) {
+      // (3) on the next diagonal block (rows / columns k8 .. k8 + 7), then (1)
+      const int nb = min(kCholPanel, n - k8);
+      for (int e = lane; e < kCholPanel * (kCholPanel + 1) / 2; e += 32) {
+        int a = 0;
+        while ((a + 1) * (a + 2) / 2 <= e) ++a;
+        const int c = e - a * (a + 1) / 2;
+        if (a < nb) {
+          const int i = k8 + a, j = k8 + c;
+          float v = L[(size_t)i * n + j];
+#pragma unroll
+          for (int s = 0; s < kCholPanel; ++s) v = fmaf(-P[(size_t)s * n + i], P[(size_t)s * n + j], v);
+          L[(size_t)i * n + j] = v;
+        }
+      }
+      __syncwarp();
+      chol_diag_f(L, n, k8, pl, pr, dinv, bad);
+    } else {
+      // (3) on the 4 x 4 tiles below the next diagonal block
+      const int m = n - k8;
+      const int T = (m + 3) / 4;
+      const int ntile = T * (T + 1) / 2 - 3;  // tile rows 0 and 1 lie in the diagonal block
+      for (int tt = threadIdx.x - 32; tt < ntile; tt += blockDim.x - 32) {
+        const int lin = tt + 3;
+        int ti = (int)((sqrtf(8.0f * (float)lin + 1.0f) - 1.0f) * 0.5f);
+        while (ti * (ti + 1) / 2 > lin) --ti;
+        while ((ti + 1) * (ti + 2) / 2 <= lin) ++ti;
+        const int tj = lin - ti * (ti + 1) / 2;
+        const int i0 = k8 + 4 * ti, j0 = k8 + 4 * tj;
+        float acc[4][4];
+#pragma unroll
+        for (int a = 0; a < 4; ++a)
+#pragma unroll
+          for (int c = 0; c < 4; ++c) {
+            const int i = i0 + a, j = j0 + c;
+            acc[a][c] = (i < n && j <= i) ? L[(size_t)i * n + j] : 0.0f;
+          }
+#pragma unroll
+        for (int s = 0; s < kCholPanel; ++s) {
+          float xa[4], yc[4];
+#pragma unroll
+          for (int a = 0; a < 4; ++a) xa[a] = i0 + a < n ? P[(size_t)s * n + i0 + a] : 0.0f;
+#pragma unroll
+          for (int c = 0; c < 4; ++c) yc[c] = j0 + c < n ? P[(size_t)s * n + j0 + c] : 0.0f;
+#pragma unroll
+          for (int a = 0; a < 4; ++a)
+#pragma unroll
+            for (int c = 0; c < 4; ++c) acc[a][c] = fmaf(-xa[a], yc[c], acc[a][c]);
+        }
+#pragma unroll
+        for (int a = 0; a < 4; ++a)
+#pragma unroll
+          for (int c = 0; c < 4; ++c) {
+            const int i = i0 + a, j = j0 + c;
+            if (i < n && j <= i) L[(size_t)i * n + j] = acc[a][c];
+          }
+      }
+    }
+    __syncthreads();
   }
+  // lower triangle from the upper copy
+  for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+    const int i = e / n, jj = e - i * n;
+    if (jj < i) L[e] = L[(size_t)jj * n + i];
+  }
+  __syncthreads();
 }
 
 // y <- (L L^T)^-1 y by one warp (L as left by chol_factor_f, in shared
@@ -1550,8 +1652,9 @@ __device__ void chol_solve_warp_f(const float* L, const float* dinv, int n, floa
 constexpr int kNewtonSmemL = 200 * 1024;
 constexpr int kNewtonColMax = 256;
 // FP32 factor in shared memory (factor, 1 / diagonal and the right-hand side)
-// the step runs on one SM; 32 warps keep more rows of each column step in flight
-constexpr int kNewtonThreads = 1024;
+// the step runs on one SM; 16 warps (the panel factor needs no more, and keeps
+// its 4 x 4 update tiles in registers at this size)
+constexpr int kNewtonThreads = 512;
 constexpr int kNewtonWarps = kNewtonThreads / 32;
 static_assert(4 * (kNewtonF32Max * kNewtonF32Max + 2 * kNewtonF32Max) <= kNewtonSmemL, "FP32 factor");
 
@@ -1605,7 +1708,7 @@ __global__ void __launch_bounds__(kNewtonThreads) k_glisa_newton_step(Batch bt, 
     }
     for (int m = threadIdx.x; m < M; m += kNewtonThreads) J.delta[m] = 0.0;
     __syncthreads();
-    chol_factor_f(Lf, nf, &bad, reinterpret_cast<float*>(col_smem), dv);
+    chol_factor_f(Lf, nf, &bad, dv);
     if (!bad) {
       for (int i = threadIdx.x; i < nf; i += kNewtonThreads) yv[i] = (float)(-(1.0 + J.grad[fid[i]]));
       __syncthreads();
@@ -1622,6 +1725,7 @@ __global__ void __launch_bounds__(kNewtonThreads) k_glisa_newton_step(Batch bt, 
     if (threadIdx.x == 0) bad = 0;
     __syncthreads();
   }
+  if (J.tc && threadIdx.x == 0) atomicAdd(&J.mail->i[MI_F64_FACTORS], 1);
   if (threadIdx.x == 0) J.freeidx[M + 1] = 0;
   const bool l_in_smem = (size_t)nf * nf * sizeof(double) <= (size_t)kNewtonSmemL;
   double* L = l_in_smem ? l_smem : J.chol;

@@ -89,6 +89,7 @@ struct hp_job {
   bool converged = false;
   double prev_change = 1e300;
   int polish_iters = 0;  // outer iterations of a mixed job after its FP32 phase (FF or FP64)
+  int f64_factors = 0;   // tensor-core gLISA: Newton steps factored in FP64
   std::vector<double> changes;  // outer changes of this run
 };
 
@@ -538,6 +539,7 @@ int step_glisa(hp_ctx* ctx, const std::vector<hp_job*>& jobs, const HostBatch& h
     const Mailbox& m = ctx->mail_host[j->slot];
     j->niter = m.i[MI_ITER];
     j->change = m.d[MD_CHANGE];
+    j->f64_factors = m.i[MI_F64_FACTORS];
     j->evals += 3.0 * (double)j->dev.npoint * (double)j->dev.natom;
     if (m.i[MI_ERR]) {
       j->status = status_of(m.i[MI_ERR]);
@@ -1196,6 +1198,7 @@ int32_t hp_job_reset(hp_job* job) {
   job->converged = false;
   job->prev_change = 1e300;
   job->polish_iters = 0;
+  job->f64_factors = 0;
   job->changes.clear();
   if (job->desc.scheme == HP_SCHEME_GLISA || job->desc.precision == HP_PRECISION_FP64)
     job->dev.mixed = PH_FP64;
@@ -1246,7 +1249,7 @@ int32_t hp_job_info_get(hp_job* job, hp_job_info* out) {
   out->device_bytes = (int64_t)job->bytes;
   out->point_atom_evals = job->evals;
   out->polish_iterations = job->polish_iters;
-  out->reserved = 0;
+  out->f64_factors = job->f64_factors;
   return HP_OK;
 }
 

@@ -176,7 +176,9 @@ typedef struct {
   int64_t device_bytes; /* device memory held by the job */
   double point_atom_evals; /* pro-atom evaluations done so far (sum over passes) */
   int32_t polish_iterations; /* mixed precision: FP64 outer iterations after a stall */
-  int32_t reserved;
+  int32_t f64_factors; /* gLISA with the tensor-core Hessian: Newton steps whose
+                          FP32 factor met a non-positive pivot (or whose free set
+                          exceeded 224 shells) and were factored in FP64 */
 } hp_job_info;
 
 typedef struct {

@@ -670,6 +670,8 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_trials_fused(Batch bt
   for (int k = threadIdx.x; k < nclip; k += kFuseThreads) cpos[k] = pos[J.clip[k]];
   const float4* cd = reinterpret_cast<const float4*>(J.clipf);
   const float2 cutp = split2(J.density_cutoff);
+  float2* tab = reinterpret_cast<float2*>(part + kFuseWarps * kFuseSP);  // exp table
+  if (threadIdx.x < 64) tab[threadIdx.x] = c_exp2_gl[threadIdx.x];
   float ah = 0.0f, al = 0.0f;
   for (int sub = 0; sub < nsub; ++sub) {
     const float* gh = stg + (sub & 1) * 2 * plane;
@@ -729,19 +731,19 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_trials_fused(Batch bt
       const f2 dr = ffa::add(f2{at * u.hi, at * u.lo}, corr);
       const f2 rt = ffa::add(dr, f2{r0p.x, r0p.y});
       const bool ht = !(rs || below(rt, cutp));
-      double big = 0.0;
       float term = 0.0f;
       if (h0 && ht) {
         term = -q.x * log1pf(dr.hi / r0p.x);
-      } else if (ht || h0) {  // the sick status changes: FP64 logs (few points)
-        const double wr = (double)q.x + (double)q.y, rho = (double)q.z + (double)q.w;
-        if (ht) big = wr * log(rho / ffa::to_double(rt));
-        else big = -(wr * log(rho / ((double)r0p.x + (double)r0p.y)));
-      }
-      if (big != 0.0) {
-        const float bh = (float)big;
-        term = bh;
-        al += (float)(big - (double)bh);
+      } else if (ht || h0) {
+        // the sick status changes: +-(w rho) ln(rho / rho0) in float-float
+        // (logf, then one Newton step on the float-float exponential)
+        const f2 ratio = ffa::div(f2{q.z, q.w}, ht ? rt : f2{r0p.x, r0p.y});
+        const float l0 = logf(ratio.hi);
+        const f2 e = ffa::exp_ff(f2{-l0, 0.f}, tab);
+        const f2 l = ffa::add(ffa::add(ffa::mul(ratio, e), -1.0f), l0);
+        const f2 big = ffa::mul(f2{q.x, q.y}, ht ? l : ffa::neg(l));
+        term = big.hi;
+        al += big.lo;
       }
       const float s2 = ah + term;
       const float bb = s2 - ah;

@@ -336,8 +336,9 @@ __global__ void __launch_bounds__(kThreads) k_glisa_trials_ff(Batch bt) {
 //   counts the points below negative_cutoff. With with_change, also
 //   C  the outer change of the step that produced c (glisa.py:776 via
 //      compute_change): warp w takes the atoms a = w (mod 8), lane = point,
-//      sum_{m in a} (c - c_old)_m g_m as a compensated sum from the staged
-//      sub-tile, w times its square (FP32) summed per thread as a float
+//      sum_{m in a} (c - c_old)_m g_m from the staged sub-tile's G_hi in
+//      FP32 (the change is only compared with the threshold: ~1e-6
+//      relative is ample), w times its square summed per thread as a float
 //      pair; the tile's total goes to atom 0's QA_CHANGE slot.
 // Jobs with more than kFuseMaxShells shells use k_glisa_pro_ff /
 // k_glisa_hv_ff with k_glisa_grad_ff.
@@ -559,12 +560,8 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_fused_ff(Batch bt, in
       for (int a = warp; a < natom; a += kFuseWarps) {
         const int i0 = aoff[a], i1 = aoff[a + 1];
         if (i0 == i1) continue;
-        Dot2 d{0.f, 0.f};
-        for (int i = i0; i < i1; ++i) {
-          const float2 dc = dcv[act[i]];
-          dot2_add(d, gh[i * kFuseSP + lane], gl[i * kFuseSP + lane], dc.x, dc.y);
-        }
-        const float dv = d.s + d.c;
+        float dv = 0.0f;
+        for (int i = i0; i < i1; ++i) dv = fmaf(gh[i * kFuseSP + lane], dcv[act[i]].x, dv);
         const float term = wf * dv * dv;
         const float t = ch + term;
         const float bb = t - ch;

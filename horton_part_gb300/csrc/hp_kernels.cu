@@ -291,14 +291,18 @@ __global__ void __launch_bounds__(kThreads) k_change(Batch bt) {
 // One block per job: change, entropy, charges (with_charges) and the
 // history row (core/iterstock.py:172-188). Warps sum atoms' tiles in
 // parallel; thread 0 adds the atoms in order (deterministic).
-__global__ void __launch_bounds__(kThreads) k_outer_finish(Batch bt, int with_charges) {
+// One block of kFinishThreads per job: each warp sums whole rows of tile
+// partials, so 32 warps take the atoms' sums (and, on the last warp, the
+// entropy) in one round instead of several.
+constexpr int kFinishThreads = 1024;
+__global__ void __launch_bounds__(kFinishThreads) k_outer_finish(Batch bt, int with_charges) {
   __shared__ double ent_s;
   __shared__ double change_s;
   int local;
   const JobDev& J = decode_local(bt, local);
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
   const int it = J.mail->i[MI_ITER];
-  for (int a = warp; a < J.natom; a += kWarps) {
+  for (int a = warp; a < J.natom; a += nw) {
     const double s = warp_tile_sum(J, apart_ptr(J, a, QA_CHANGE), J.ntile);
     const double pop = with_charges ? warp_tile_sum(J, apart_ptr(J, a, QA_POP), J.ntile) : 0.0;
     if (lane == 0) {
@@ -306,7 +310,7 @@ __global__ void __launch_bounds__(kThreads) k_outer_finish(Batch bt, int with_ch
       if (with_charges) J.charges[a] = J.zpseudo[a] - pop;
     }
   }
-  if (warp == 0) {
+  if (warp == nw - 1) {
     const int q = J.fuse ? QJ_ENT_PREV : QJ_ENTROPY;
     const double ent = warp_tile_sum(J, J.jpart + (size_t)q * J.ntile, J.ntile);
     if (lane == 0) ent_s = ent;
@@ -319,10 +323,10 @@ __global__ void __launch_bounds__(kThreads) k_outer_finish(Batch bt, int with_ch
   }
   __syncthreads();
   if (it < J.maxiter) {
-    for (int i = threadIdx.x; i < J.nparam; i += kThreads)
+    for (int i = threadIdx.x; i < J.nparam; i += blockDim.x)
       J.hist_propars[(size_t)it * J.nparam + i] = J.propars[i];
     if (with_charges)
-      for (int a = threadIdx.x; a < J.natom; a += kThreads)
+      for (int a = threadIdx.x; a < J.natom; a += blockDim.x)
         J.hist_charges[(size_t)it * J.natom + a] = J.charges[a];
   }
   if (threadIdx.x == 0) {
@@ -1287,27 +1291,41 @@ __global__ void __launch_bounds__(kThreads) k_glisa_reduce(Batch bt) {
   const JobDev& J = decode_local(bt, local);
   const int M = J.nshell;
   const int e = local * kThreads + threadIdx.x;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nblk = (M * M + kThreads - 1) / kThreads;  // this job's K_SQUARE blocks
   if (J.tc && M <= kTcSinglePassShells) {
-    // FP32 packed lower triangles of the single-pass tensor-core kernel
+    // FP32 packed lower triangles of the single-pass tensor-core kernel: a
+    // chunk of 32 elements per pass of the block, warp w summing the point
+    // ranges w, w + 8, ... (coalesced loads, compensated FP32 sums), the
+    // eight warp sums combined in FP64 in warp order
+    __shared__ double wsum[kWarps][32];
     const int E = M * (M + 1) / 2;
-    if (e < E) {
-      int i = (int)((sqrtf(8.0f * (float)e + 1.0f) - 1.0f) * 0.5f);
-      while (i * (i + 1) / 2 > e) --i;
-      while ((i + 1) * (i + 2) / 2 <= e) ++i;
-      const int j = e - i * (i + 1) / 2;
-      const float* hp = reinterpret_cast<const float*>(J.hpart) + e;
-      double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;  // four chains, fixed combination
-      int sp = 0;
-      for (; sp + 3 < J.nsplit; sp += 4) {
-        s0 += (double)hp[(size_t)sp * E];
-        s1 += (double)hp[(size_t)(sp + 1) * E];
-        s2 += (double)hp[(size_t)(sp + 2) * E];
-        s3 += (double)hp[(size_t)(sp + 3) * E];
+    const float* hp = reinterpret_cast<const float*>(J.hpart);
+    for (int c = local; c < (E + 31) / 32; c += nblk) {
+      const int ec = c * 32 + lane;
+      float s = 0.0f, cc = 0.0f;
+      if (ec < E)
+        for (int sp = warp; sp < J.nsplit; sp += kWarps) {
+          const float x = hp[(size_t)sp * E + ec];
+          const float t = s + x;
+          const float bb = t - s;
+          cc += (s - (t - bb)) + (x - bb);
+          s = t;
+        }
+      wsum[warp][lane] = (double)s + (double)cc;
+      __syncthreads();
+      if (warp == 0 && ec < E) {
+        double v = 0.0;
+#pragma unroll
+        for (int w = 0; w < kWarps; ++w) v += wsum[w][lane];
+        int i = (int)((sqrtf(8.0f * (float)ec + 1.0f) - 1.0f) * 0.5f);
+        while (i * (i + 1) / 2 > ec) --i;
+        while ((i + 1) * (i + 2) / 2 <= ec) ++i;
+        const int j = ec - i * (i + 1) / 2;
+        J.hess[(size_t)i * M + j] = v;
+        J.hess[(size_t)j * M + i] = v;
       }
-      for (; sp < J.nsplit; ++sp) s0 += (double)hp[(size_t)sp * E];
-      const double s = (s0 + s1) + (s2 + s3);
-      J.hess[(size_t)i * M + j] = s;
-      J.hess[(size_t)j * M + i] = s;
+      __syncthreads();
     }
   } else if (e < M * M) {
     const int i = e / M, j = e - i * M;
@@ -1319,8 +1337,6 @@ __global__ void __launch_bounds__(kThreads) k_glisa_reduce(Batch bt) {
     }
   }
   // gradient rows: one warp per row, lanes over tiles (four chains, fixed order)
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int nblk = (M * M + kThreads - 1) / kThreads;  // this job's K_SQUARE blocks
   for (int m = local * kWarps + warp; m < M; m += nblk * kWarps) {
     const double* gp = J.gpart + (size_t)m * J.ntile;
     double h0 = 0.0, h1 = 0.0, h2 = 0.0, h3 = 0.0;
@@ -2244,7 +2260,7 @@ void launch_change(const HostBatch& hb, cudaStream_t st, int mixed, int model) {
 }
 
 void launch_outer_finish(const HostBatch& hb, cudaStream_t st, int with_charges) {
-  HP_LAUNCH(k_outer_finish, K_JOB, kThreads, with_charges);
+  HP_LAUNCH(k_outer_finish, K_JOB, kFinishThreads, with_charges);
 }
 
 void launch_charges(const HostBatch& hb, cudaStream_t st) { HP_LAUNCH(k_charges, K_JOB, 32); }

@@ -1286,26 +1286,30 @@ __global__ void __launch_bounds__(kThreads) k_glisa_hess(Batch bt) {
 
 // Sum Hessian partials over splits (fixed order) into the lower triangle and
 // mirror; gradient rows from gpart.
-__global__ void __launch_bounds__(kThreads) k_glisa_reduce(Batch bt) {
+// kReduceThreads per block: enough warps per SM to keep the partials' loads
+// in flight (the job has only nshell^2 / kThreads blocks).
+constexpr int kReduceThreads = 1024;
+constexpr int kReduceWarps = kReduceThreads / 32;
+__global__ void __launch_bounds__(kReduceThreads) k_glisa_reduce(Batch bt) {
   int local;
   const JobDev& J = decode_local(bt, local);
   const int M = J.nshell;
-  const int e = local * kThreads + threadIdx.x;
+  const int e = local * kReduceThreads + threadIdx.x;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int nblk = (M * M + kThreads - 1) / kThreads;  // this job's K_SQUARE blocks
   if (J.tc && M <= kTcSinglePassShells) {
     // FP32 packed lower triangles of the single-pass tensor-core kernel: a
     // chunk of 32 elements per pass of the block, warp w summing the point
-    // ranges w, w + 8, ... (coalesced loads, compensated FP32 sums), the
-    // eight warp sums combined in FP64 in warp order
-    __shared__ double wsum[kWarps][32];
+    // ranges w, w + 32, ... (coalesced loads, compensated FP32 sums), the
+    // warps' sums combined in FP64 in warp order
+    __shared__ double wsum[kReduceWarps][32];
     const int E = M * (M + 1) / 2;
     const float* hp = reinterpret_cast<const float*>(J.hpart);
     for (int c = local; c < (E + 31) / 32; c += nblk) {
       const int ec = c * 32 + lane;
       float s = 0.0f, cc = 0.0f;
       if (ec < E)
-        for (int sp = warp; sp < J.nsplit; sp += kWarps) {
+        for (int sp = warp; sp < J.nsplit; sp += kReduceWarps) {
           const float x = hp[(size_t)sp * E + ec];
           const float t = s + x;
           const float bb = t - s;
@@ -1317,7 +1321,7 @@ __global__ void __launch_bounds__(kThreads) k_glisa_reduce(Batch bt) {
       if (warp == 0 && ec < E) {
         double v = 0.0;
 #pragma unroll
-        for (int w = 0; w < kWarps; ++w) v += wsum[w][lane];
+        for (int w = 0; w < kReduceWarps; ++w) v += wsum[w][lane];
         int i = (int)((sqrtf(8.0f * (float)ec + 1.0f) - 1.0f) * 0.5f);
         while (i * (i + 1) / 2 > ec) --i;
         while ((i + 1) * (i + 2) / 2 <= ec) ++i;
@@ -1337,7 +1341,7 @@ __global__ void __launch_bounds__(kThreads) k_glisa_reduce(Batch bt) {
     }
   }
   // gradient rows: one warp per row, lanes over tiles (four chains, fixed order)
-  for (int m = local * kWarps + warp; m < M; m += nblk * kWarps) {
+  for (int m = local * kReduceWarps + warp; m < M; m += nblk * kReduceWarps) {
     const double* gp = J.gpart + (size_t)m * J.ntile;
     double h0 = 0.0, h1 = 0.0, h2 = 0.0, h3 = 0.0;
     int t = lane;
@@ -1612,54 +1616,56 @@ __device__ void chol_factor_f(float* L, int n, int* bad, float* dinv) {
   __syncthreads();
 }
 
-// y <- (L L^T)^-1 y by one warp (L as left by chol_factor_f, in shared
-// memory): the vector lives in registers, element i in lane i % 32, slot
-// i / 32; each column's pivot value is broadcast by a shuffle, so a column
-// costs one shuffle and a few FMAs, no barrier. Forward with the columns of
-// L (contiguous in the upper copy), backward with its rows. n <= 32 kSolveSlots.
-constexpr int kSolveSlots = (kNewtonF32Max + 31) / 32;
-__device__ void chol_solve_warp_f(const float* L, const float* dinv, int n, float* yio) {
-  const int lane = threadIdx.x & 31;
-  float y[kSolveSlots];
-#pragma unroll
-  for (int s = 0; s < kSolveSlots; ++s) {
-    const int i = s * 32 + lane;
-    y[s] = i < n ? yio[i] : 0.0f;
-  }
-  for (int j = 0; j < n; ++j) {
-    const int sj = j >> 5;
-    float yj = 0.0f;
-#pragma unroll
-    for (int s = 0; s < kSolveSlots; ++s)
-      if (s == sj) yj = y[s];
-    const float zj = __shfl_sync(0xffffffffu, yj, j & 31) * dinv[j];
-    const float* col = L + (size_t)j * n;  // L[i][j] = col[i], i > j
-#pragma unroll
-    for (int s = 0; s < kSolveSlots; ++s) {
-      const int i = s * 32 + lane;
-      if (i > j && i < n) y[s] = fmaf(-col[i], zj, y[s]);
-      else if (i == j) y[s] = zj;
+// y <- (L L^T)^-1 y by the whole block (L as left by chol_factor_f, y in
+// shared memory), in blocks of 32 rows: one warp solves the diagonal block
+// (element i in lane i - j0, each column's value broadcast by a shuffle),
+// then every thread updates one of the remaining rows with the block's 32
+// columns. Forward with the columns of L (the upper copy: conflict-free
+// across rows), backward with its rows. Each element receives its updates in
+// column order, forward ascending and backward descending, as in a plain
+// column-by-column substitution.
+__device__ void chol_solve_f(const float* L, const float* dinv, int n, float* y) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nb = (n + 31) / 32;
+  for (int jb = 0; jb < nb; ++jb) {
+    const int j0 = jb * 32, j1 = min(j0 + 32, n);
+    if (warp == 0) {
+      const int i = j0 + lane;
+      float b = i < n ? y[i] : 0.0f;
+      for (int j = j0; j < j1; ++j) {
+        const float zj = __shfl_sync(0xffffffffu, b, j - j0) * dinv[j];
+        if (i > j && i < n) b = fmaf(-L[(size_t)j * n + i], zj, b);
+        else if (i == j) b = zj;
+      }
+      if (i < n) y[i] = b;
     }
-  }
-  for (int j = n - 1; j >= 0; --j) {
-    const int sj = j >> 5;
-    float yj = 0.0f;
-#pragma unroll
-    for (int s = 0; s < kSolveSlots; ++s)
-      if (s == sj) yj = y[s];
-    const float xj = __shfl_sync(0xffffffffu, yj, j & 31) * dinv[j];
-    const float* row = L + (size_t)j * n;  // L[j][i], i < j
-#pragma unroll
-    for (int s = 0; s < kSolveSlots; ++s) {
-      const int i = s * 32 + lane;
-      if (i < j) y[s] = fmaf(-row[i], xj, y[s]);
-      else if (i == j) y[s] = xj;
+    __syncthreads();
+    for (int i = j1 + threadIdx.x; i < n; i += blockDim.x) {
+      float b = y[i];
+      for (int j = j0; j < j1; ++j) b = fmaf(-L[(size_t)j * n + i], y[j], b);
+      y[i] = b;
     }
+    __syncthreads();
   }
-#pragma unroll
-  for (int s = 0; s < kSolveSlots; ++s) {
-    const int i = s * 32 + lane;
-    if (i < n) yio[i] = y[s];
+  for (int jb = nb - 1; jb >= 0; --jb) {
+    const int j0 = jb * 32, j1 = min(j0 + 32, n);
+    if (warp == 0) {
+      const int i = j0 + lane;
+      float b = i < n ? y[i] : 0.0f;
+      for (int j = j1 - 1; j >= j0; --j) {
+        const float xj = __shfl_sync(0xffffffffu, b, j - j0) * dinv[j];
+        if (i < j) b = fmaf(-L[(size_t)j * n + i], xj, b);
+        else if (i == j) b = xj;
+      }
+      if (i < n) y[i] = b;
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < j0; i += blockDim.x) {
+      float b = y[i];
+      for (int j = j1 - 1; j >= j0; --j) b = fmaf(-L[(size_t)j * n + i], y[j], b);
+      y[i] = b;
+    }
+    __syncthreads();
   }
 }
 
@@ -1728,8 +1734,7 @@ __global__ void __launch_bounds__(kNewtonThreads) k_glisa_newton_step(Batch bt, 
     if (!bad) {
       for (int i = threadIdx.x; i < nf; i += kNewtonThreads) yv[i] = (float)(-(1.0 + J.grad[fid[i]]));
       __syncthreads();
-      if (threadIdx.x < 32) chol_solve_warp_f(Lf, dv, nf, yv);
-      __syncthreads();
+      chol_solve_f(Lf, dv, nf, yv);
       for (int i = threadIdx.x; i < nf; i += kNewtonThreads) J.delta[fid[i]] = (double)yv[i];
       float* keep = reinterpret_cast<float*>(J.chol);
       for (int e = threadIdx.x; e < nf * nf + nf; e += kNewtonThreads) keep[e] = Lf[e];
@@ -1836,8 +1841,7 @@ __global__ void __launch_bounds__(kThreads) k_glisa_refine(Batch bt) {
     for (int e = ne / 4 * 4 + threadIdx.x; e < ne; e += kThreads) Lf[e] = keep[e];
     for (int i = threadIdx.x; i < nf; i += kThreads) yv[i] = (float)r[i];
     __syncthreads();
-    if (threadIdx.x < 32) chol_solve_warp_f(Lf, Lf + nf * nf, nf, yv);
-    __syncthreads();
+    chol_solve_f(Lf, Lf + nf * nf, nf, yv);
     for (int i = threadIdx.x; i < nf; i += kThreads) J.delta[J.freeidx[i]] += (double)yv[i];
     return;
   }
@@ -2317,7 +2321,7 @@ void launch_glisa_grad(const HostBatch& hb, cudaStream_t st) {
 }
 void launch_glisa_hess(const HostBatch& hb, cudaStream_t st) { HP_LAUNCH(k_glisa_hess, K_HESS, kThreads); }
 void launch_glisa_reduce(const HostBatch& hb, cudaStream_t st) {
-  HP_LAUNCH(k_glisa_reduce, K_SQUARE, kThreads);
+  HP_LAUNCH(k_glisa_reduce, K_SQUARE, kReduceThreads);
 }
 
 void launch_glisa_solve(const HostBatch& hb, cudaStream_t st, int projected) {

@@ -1724,9 +1724,31 @@ __global__ void __launch_bounds__(kNewtonThreads) k_glisa_newton_step(Batch bt, 
     float* Lf = reinterpret_cast<float*>(l_smem);
     float* dv = Lf + nf * nf;
     float* yv = dv + nf;
-    for (int i = warp; i < nf; i += kNewtonWarps) {  // lower triangle (all the factor reads)
-      const double* hrow = J.hess + (size_t)fid[i] * M;
-      for (int j = lane; j <= i; j += 32) Lf[i * nf + j] = (float)hrow[fid[j]];
+    {  // lower triangle (all the factor reads), eight loads in flight per thread
+      const double* __restrict__ hs = J.hess;
+      const int ne = nf * (nf + 1) / 2;
+      constexpr int kBatch = 8;
+      for (int e0 = threadIdx.x; e0 < ne; e0 += kBatch * kNewtonThreads) {
+        double v[kBatch];
+        int dst[kBatch];
+#pragma unroll
+        for (int u = 0; u < kBatch; ++u) {
+          const int e = e0 + u * kNewtonThreads;
+          dst[u] = -1;
+          v[u] = 0.0;
+          if (e < ne) {
+            int i = (int)((sqrtf(8.0f * (float)e + 1.0f) - 1.0f) * 0.5f);
+            while (i * (i + 1) / 2 > e) --i;
+            while ((i + 1) * (i + 2) / 2 <= e) ++i;
+            const int j = e - i * (i + 1) / 2;
+            dst[u] = i * nf + j;
+            v[u] = hs[(size_t)fid[i] * M + fid[j]];
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < kBatch; ++u)
+          if (dst[u] >= 0) Lf[dst[u]] = (float)v[u];
+      }
     }
     for (int m = threadIdx.x; m < M; m += kNewtonThreads) J.delta[m] = 0.0;
     __syncthreads();
@@ -1831,7 +1853,7 @@ __global__ void __launch_bounds__(kThreads) k_glisa_refine(Batch bt) {
     r[i] = -(1.0 + J.grad[m]) - J.hsum[m];
   }
   __syncthreads();
-  if (f32) {  // FP32 factor of k_glisa_newton_step: copy it in, one warp solves
+  if (f32) {  // FP32 factor of k_glisa_newton_step: copy it in, the block solves
     float* Lf = reinterpret_cast<float*>(l_smem);
     float* yv = Lf + nf * nf + nf;
     const float* keep = reinterpret_cast<const float*>(J.chol);
@@ -2172,40 +2194,51 @@ __global__ void __launch_bounds__(kThreads) k_glisa_trials(Batch bt) {
 }
 
 // One warp per job: Armijo choice among the trials, apply the step.
-__global__ void k_glisa_trial_pick(Batch bt) {
+// One warp per trial (kTrials warps): warp t forms F(c_t) - F(c) and the
+// Armijo bound of trial t; the first trial (in step order) that passes is
+// taken, the shortest step if none does.
+__global__ void __launch_bounds__(32 * kTrials) k_glisa_trial_pick(Batch bt) {
+  __shared__ int pass[kTrials];
+  __shared__ int pick_s;
   int local;
   const JobDev& J = decode_local(bt, local);
-  const int lane = threadIdx.x & 31;
+  const int lane = threadIdx.x & 31, t = threadIdx.x >> 5;
   const int M = J.nshell;
   double c0 = 0.0;
   for (int m = lane; m < M; m += 32) c0 += J.propars[m];
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) c0 += __shfl_xor_sync(0xffffffffu, c0, o);
-  int pick = kTrials - 1;
-  for (int t = 0; t < kTrials; ++t) {
-    double s = 0.0, dec = 0.0;
-    for (int m = lane; m < M; m += 32) {
-      const double ct = J.ctrial[t * M + m];
-      s += ct;
-      dec += (1.0 + J.grad[m]) * (ct - J.propars[m]);
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      s += __shfl_xor_sync(0xffffffffu, s, o);
-      dec += __shfl_xor_sync(0xffffffffu, dec, o);
-    }
-    double df = 0.0;  // f(c_t) - f(c)
-    for (int q = lane; q < J.ntile; q += 32) df += J.tpart[(size_t)t * J.ntile + q];
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) df += __shfl_xor_sync(0xffffffffu, df, o);
-    // Armijo on F = f + sum c: F(c_t) <= F(c) + 1e-4 dF.(c_t - c)
-    if (df + (s - c0) <= 1e-4 * dec) {
-      pick = t;
-      break;
-    }
+  double s = 0.0, dec = 0.0;
+  for (int m = lane; m < M; m += 32) {
+    const double ct = J.ctrial[t * M + m];
+    s += ct;
+    dec += (1.0 + J.grad[m]) * (ct - J.propars[m]);
   }
-  for (int m = lane; m < M; m += 32) J.propars[m] = J.ctrial[pick * M + m];
-  if (lane == 0) J.mail->d[MD_LS_X] = ldexp(1.0, -pick);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    s += __shfl_xor_sync(0xffffffffu, s, o);
+    dec += __shfl_xor_sync(0xffffffffu, dec, o);
+  }
+  double df = 0.0;  // f(c_t) - f(c)
+  for (int q = lane; q < J.ntile; q += 32) df += J.tpart[(size_t)t * J.ntile + q];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) df += __shfl_xor_sync(0xffffffffu, df, o);
+  // Armijo on F = f + sum c: F(c_t) <= F(c) + 1e-4 dF.(c_t - c)
+  if (lane == 0) pass[t] = df + (s - c0) <= 1e-4 * dec;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int pick = kTrials - 1;
+    for (int k = 0; k < kTrials; ++k)
+      if (pass[k]) {
+        pick = k;
+        break;
+      }
+    pick_s = pick;
+    J.mail->d[MD_LS_X] = ldexp(1.0, -pick);
+  }
+  __syncthreads();
+  const int pick = pick_s;
+  for (int m = threadIdx.x; m < M; m += blockDim.x) J.propars[m] = J.ctrial[pick * M + m];
 }
 
 // ---------------------------------------------------------------------------
@@ -2378,7 +2411,7 @@ void launch_glisa_pnewton(const HostBatch& hb, cudaStream_t st, int gff, int fus
   if (fuse_shells > 0) launch_glisa_trials_fused(hb, st, fuse_shells);
   else if (gff) launch_glisa_trials_ff(hb, st);
   else HP_LAUNCH(k_glisa_trials, K_POINT, kThreads);
-  HP_LAUNCH(k_glisa_trial_pick, K_JOB, 32);
+  HP_LAUNCH(k_glisa_trial_pick, K_JOB, 32 * kTrials);
 }
 
 }  // namespace hp

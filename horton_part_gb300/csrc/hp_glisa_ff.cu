@@ -421,6 +421,7 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_fused_ff(Batch bt, in
   int tile;
   const JobDev& J = decode_local_gf(bt, tile);
   if (!J.fuse) return;
+  if (MODE == 0 && !glisa_refine_now(J)) return;
   const int S = J.nshell;
   // stage k: high plane at stg + 2 k S kFuseSP, low plane S kFuseSP after it
   float* stg = reinterpret_cast<float*>(fsm);

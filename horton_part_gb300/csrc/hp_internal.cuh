@@ -197,8 +197,21 @@ struct JobDev {
                                                  // tc: gLISA Hessian on the tensor cores;
                                                  // gff: gLISA G passes in float-float
   int fuse;                                      // gff with nshell <= kFuseMaxShells: fused passes
+  int refine;                                    // tc with polish: refine the Newton step in the finish
   double threshold, inner_threshold, density_cutoff, negative_cutoff, population_cutoff, tau;
 };
+
+// gLISA with the tensor-core Hessian: the Newton direction from the FP32
+// factor carries ~1e-6 relative error, which the outer iteration does not
+// notice (same iteration counts, same optimum: the gradient and objective are
+// exact). With polish, the iterations of the finish (last outer change within
+// 100 x the threshold) refine it once against the exact product H delta.
+// Read from the job's mailbox, which only the end of a step writes, so every
+// kernel of a step sees the same answer.
+__device__ __forceinline__ bool glisa_refine_now(const JobDev& J) {
+  return J.refine && J.mail->i[MI_ITER] > 0 && J.mail->d[MD_CHANGE] < 100.0 * J.threshold;
+}
+
 
 enum AtomOut {
   AO_POP = 0,

@@ -1814,6 +1814,7 @@ __global__ void __launch_bounds__(kThreads) k_glisa_hv(Batch bt) {
 __global__ void __launch_bounds__(kThreads) k_glisa_gsum(Batch bt) {
   int local;
   const JobDev& J = decode_local(bt, local);
+  if (!glisa_refine_now(J)) return;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int nblk = (J.nshell * J.nshell + kThreads - 1) / kThreads;  // this job's K_SQUARE blocks
   for (int m = local * kWarps + warp; m < J.nshell; m += nblk * kWarps) {
@@ -1841,6 +1842,7 @@ __global__ void __launch_bounds__(kThreads) k_glisa_refine(Batch bt) {
   extern __shared__ double l_smem[];
   int local;
   const JobDev& J = decode_local(bt, local);
+  if (!glisa_refine_now(J)) return;
   const int M = J.nshell;
   const int nf = J.freeidx[M];
   const bool f32 = J.freeidx[M + 1] != 0;

@@ -413,11 +413,11 @@ int step_iterstock(hp_ctx* ctx, const std::vector<hp_job*>& jobs, const HostBatc
   return HP_OK;
 }
 
-// Refinement steps per Newton iteration when the Hessian comes from the
-// tensor cores (each: one exact H delta product, one fused pass over G).
-// The factor of the tensor-core Hessian leaves a relative direction error
-// of ~1e-6; one step brings it to ~1e-12, far below what the outer
-// iteration notices (same iteration counts as the FP64 Hessian).
+// Refinement steps per Newton iteration of the finish when the Hessian comes
+// from the tensor cores (each: one exact H delta product, one fused pass over
+// G); the kernels skip the jobs not in their finish (glisa_refine_now). The
+// factor of the tensor-core Hessian leaves a relative direction error of
+// ~1e-6; one step brings it to ~1e-12.
 constexpr int kRefineSteps = 1;
 
 // One gLISA solver iteration (glisa.py:748-798 for Newton, 805-848 for SC).
@@ -957,6 +957,7 @@ int32_t hp_job_create(hp_ctx* ctx, const hp_job_desc* d, hp_job** out) {
   J.tc = tc ? 1 : 0;
   J.gff = gff ? 1 : 0;
   J.fuse = gff && S <= kFuseMaxShells ? 1 : 0;
+  J.refine = tc && d->polish ? 1 : 0;
   J.local = local ? 1 : 0;
   J.nrad = nrad;
   J.threshold = d->threshold;

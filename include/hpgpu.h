@@ -87,9 +87,11 @@ typedef enum {
   HP_PRECISION_MIXED = 1, /* MBIS, GISA, aLISA sc: FP32 evaluation, compensated
                              sums, FP64 updates and change test (optional
                              finish, see polish: float-float for MBIS, FP64 for
-                             the basis schemes). gLISA Newton solvers: FP64
-                             evaluation, Hessian on the tensor cores (TF32)
-                             with FP64 iterative refinement of the step. */
+                             the basis schemes). gLISA Newton solvers:
+                             float-float evaluation, Hessian on the tensor
+                             cores (TF32) with an FP32 factor; with polish,
+                             the step is refined against the exact product
+                             in the finish. */
   HP_PRECISION_FF = 2     /* MBIS: every evaluation in float-float arithmetic
                              (about 48 significant bits) on the FP32 pipes,
                              FP64 updates and tests: FP64-class results */
@@ -146,7 +148,11 @@ typedef struct {
                              outer change is within 100 x the threshold or has
                              stopped decreasing (its noise floor); 0 = stay in
                              FP32 to the threshold and stop with
-                             HP_WARN_NOISE_FLOOR only at the floor */
+                             HP_WARN_NOISE_FLOOR only at the floor. gLISA
+                             with the tensor-core Hessian: 1 = refine the
+                             Newton step once against the exact product H d
+                             while the last outer change is within 100 x the
+                             threshold; 0 = never */
   int32_t nrad;           /* grid_type 1: radial nodes over all atom grids */
   /* grid_type 1 (atom grids, the reference's default; base.py:619-628,
    * mbis.py:174-187): atom a owns the radial shells [radial_offsets[a],

@@ -48,6 +48,16 @@ def test_struct_sizes_match_header():
     assert ctypes.sizeof(_lib.JobResults) == 8 * 8
 
 
+def test_job_info_fields_match_header():
+    # member names of hp_job_info, in declaration order, against the binding
+    text = open(os.path.join(ROOT, "include", "hpgpu.h")).read()
+    body = re.search(r"typedef struct \{([^{}]*)\} hp_job_info;", text).group(1)
+    body = re.sub(r"/\*.*?\*/", "", body, flags=re.S)
+    names = re.findall(r"^\s*\w+\s+(\w+);", body, re.M)
+    assert names == [f[0] for f in _lib.JobInfo._fields_]
+    assert "f64_factors" in names
+
+
 def test_invalid_arguments_fail_before_device_work(library):
     L = _lib.lib()
     assert L.hp_job_create(None, None, None) == _lib.HP_ERR_INVALID

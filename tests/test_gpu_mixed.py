@@ -1,7 +1,7 @@
 """Mixed-precision path (FP32 evaluation, compensated sums, FP64 updates)
 against the reference's FP64 results.
 
-Bar (the benchmark spec): charges within 1e-6 e; pro-atom parameters within 1e-6
+Bar: charges within 1e-6 e; pro-atom parameters within 1e-6
 relative, measured against each atom's largest parameter of the same kind
 (populations against the atom's population, exponents against its largest
 exponent), so that populations pinned at zero are compared on the atom's

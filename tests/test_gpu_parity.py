@@ -2,7 +2,7 @@
 reference's results on the same inputs.
 
 Golden values come from the unmodified reference (tests/golden). FP64 path
-tolerances: charges within 1e-8 e (the spec bar is 1e-6 e), pro-atom
+tolerances: charges within 1e-8 e (the accuracy target is 1e-6 e), pro-atom
 parameters within 1e-7 relative, identical iteration counts unless the
 reference's final change lies within 1e-6 (relative) of the threshold.
 """

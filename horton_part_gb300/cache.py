@@ -1,15 +1,30 @@
-"""Result cache and run-once methods with the reference's semantics.
+"""Keyed result store and run-once methods behind ``part.cache`` / ``part[key]``.
 
-``Cache`` stores keyed results with optional allocation and tags, and
-``just_once`` makes a method run only on its first call and records its wall
-time in ``time_usage`` (``core/cache.py:34-80``, ``core/cache.py:100-399`` in
-horton-part). The partitioning classes of this package fill the same keys as
-the reference (``charges``, ``propars``, ``niter``, ``history_*`` ...), so
-code written against ``part.cache`` / ``part[key]`` works unchanged.
+Callers of horton-part read results through ``part.cache`` (``load``,
+``dump``, ``in``, ``iterkeys(tags="o")``, ``clear``) and rely on
+``@just_once`` methods such as ``do_partitioning`` running at most once per
+``clear()``; the interface is the one of horton-part's ``core/cache.py``.
+This module is written from that behaviour (the acceptance list is the
+reference's ``tests/core/test_cache.py``, restated in
+``tests/test_cache_api.py``):
+
+* keys are one or more hashable parts; ``c["a"]``, ``c[("a",)]`` and
+  ``c.load("a")`` name the same entry, as do ``c["a", 1]`` and
+  ``c.load("a", 1)``;
+* ``load(key, alloc=shape)`` hands out a zero-filled float64 array the first
+  time (returns ``(array, True)``) and the same array afterwards
+  (``(array, False)``), checking its shape (``TypeError``) and tags
+  (``ValueError``);
+* clearing an entry that holds an array zero-fills the array and marks the
+  entry stale, so a later ``alloc`` load with the same shape reuses the
+  buffer; entries with a ``__clear__`` method are cleared through it; any
+  other entry is removed;
+* tags are sets of one-letter labels ("o" marks the scheme's outputs).
 """
 
 from __future__ import annotations
 
+import functools
 import time
 
 import numpy as np
@@ -18,7 +33,12 @@ __all__ = ["JustOnceClass", "just_once", "Cache"]
 
 
 class JustOnceClass:
-    """Base class whose ``@just_once`` methods run at most once until ``clear()``."""
+    """Base for classes with ``@just_once`` methods.
+
+    The names of the methods that already ran sit in ``_done_just_once``;
+    ``clear()`` forgets them. ``time_usage[name]`` holds the wall time of the
+    last run of each such method.
+    """
 
     def __init__(self):
         self._done_just_once = set()
@@ -31,192 +51,169 @@ class JustOnceClass:
         self._done_just_once = set()
 
 
-def just_once(fn):
-    def wrapper(instance):
-        if not hasattr(instance, "_done_just_once"):
-            raise TypeError("Missing hidden _done_just_once. Forgot to call JustOnceClass.__init__()?")
-        if fn.__name__ in instance._done_just_once:
+def just_once(method):
+    """Run ``method(self)`` only on its first call until ``self.clear()``."""
+    name = method.__name__
+
+    @functools.wraps(method)
+    def run_once(self):
+        done = getattr(self, "_done_just_once", None)
+        if done is None:
+            raise TypeError(f"{type(self).__name__}.{name} is @just_once, but the instance has no "
+                            "run-once bookkeeping (JustOnceClass.__init__ was not called)")
+        if name in done:
             return
-        t0 = time.time()
-        fn(instance)
-        t1 = time.time()
-        instance._done_just_once.add(fn.__name__)
-        instance.time_usage[fn.__name__] = t1 - t0
+        start = time.time()
+        method(self)
+        self._done_just_once.add(name)
+        self.time_usage[name] = time.time() - start
 
-    wrapper.__doc__ = fn.__doc__
-    wrapper.__name__ = fn.__name__
-    return wrapper
+    return run_once
 
 
-def _norm_alloc(alloc):
-    if not hasattr(alloc, "__len__"):
-        alloc = (alloc,)
-    if len(alloc) == 0:
-        raise TypeError("Alloc can not be an empty list")
-    return tuple(alloc)
+_MISSING = object()
 
 
-def _norm_tags(tags):
-    return set() if tags is None else set(tags)
-
-
-def _norm_key(key):
-    if hasattr(key, "__len__") and len(key) == 0:
-        raise TypeError("At least one argument needed to specify a key.")
+def _entry_key(parts):
+    """One key from the positional parts of a call (nested 1-tuples unwrapped)."""
+    if isinstance(parts, tuple) and len(parts) == 0:
+        raise TypeError("a cache key needs at least one part")
+    key = parts
     while isinstance(key, tuple) and len(key) == 1:
         key = key[0]
     return key
 
 
-class CacheItem:
-    """A stored value with a validity flag and tags."""
+def _tag_set(tags):
+    return frozenset(tags) if tags else frozenset()
 
-    def __init__(self, value, tags=None):
-        self._value = value
-        self._valid = True
-        self._tags = _norm_tags(tags)
 
-    @classmethod
-    def from_alloc(cls, alloc, tags):
-        return cls(np.zeros(_norm_alloc(alloc), dtype=float), tags=tags)
+def _shape_of(alloc):
+    shape = tuple(alloc) if isinstance(alloc, (tuple, list)) else (alloc,)
+    if not shape:
+        raise TypeError("alloc must name at least one dimension")
+    return shape
 
-    def check_alloc(self, alloc):
-        alloc = _norm_alloc(alloc)
-        v = self._value
-        if not (isinstance(v, np.ndarray) and v.shape == alloc and issubclass(v.dtype.type, float)):
-            raise TypeError("The stored item does not match the given alloc.")
 
-    def check_tags(self, tags):
-        if _norm_tags(tags) != self._tags:
-            raise ValueError("Tags do not match.")
+class _Entry:
+    __slots__ = ("value", "stale", "tags")
 
-    @property
-    def value(self):
-        if not self._valid:
-            raise ValueError("This cached item is not valid.")
-        return self._value
+    def __init__(self, value, tags):
+        self.value = value
+        self.stale = False
+        self.tags = tags
 
-    @property
-    def valid(self):
-        return self._valid
+    def holds_float_array(self, shape):
+        v = self.value
+        return isinstance(v, np.ndarray) and v.dtype == np.float64 and v.shape == shape
 
-    @property
-    def tags(self):
-        return self._tags
-
-    def clear(self):
-        self._valid = False
-        if isinstance(self._value, np.ndarray):
-            self._value[:] = 0.0
-        elif hasattr(self._value, "__clear__") and callable(self._value.__clear__):
-            self._value.__clear__()
+    def invalidate(self):
+        """Reset the value in place; False when the entry cannot be kept."""
+        v = self.value
+        if isinstance(v, np.ndarray):
+            v[...] = 0.0
+        elif callable(getattr(v, "__clear__", None)):
+            v.__clear__()
         else:
             return False
+        self.stale = True
         return True
 
 
-_no_default = object()
-
-
 class Cache:
-    """Dictionary-like store of previously computed results."""
+    """Store of computed results, keyed by one or more hashable parts."""
 
     def __init__(self):
         self._store = {}
 
-    def clear(self, **kwargs):
-        dealloc = kwargs.pop("dealloc", False)
-        tags = _norm_tags(kwargs.pop("tags", None))
-        if kwargs:
-            raise TypeError("Unexpected arguments: %s" % list(kwargs))
-        for key, item in list(self._store.items()):
-            if not tags or item.tags & tags:
-                self.clear_item(key, dealloc=dealloc)
+    # -- reading ------------------------------------------------------------
+    def _live(self, key):
+        entry = self._store.get(key)
+        return None if entry is None or entry.stale else entry
 
-    def clear_item(self, *key, **kwargs):
-        key = _norm_key(key)
-        dealloc = kwargs.pop("dealloc", False)
-        if kwargs:
-            raise TypeError("Unexpected arguments: %s" % list(kwargs))
-        item = self._store.get(key)
-        if item is None:
-            return
-        if dealloc or not item.clear():
-            del self._store[key]
+    def load(self, *key, alloc=None, default=_MISSING, tags=None):
+        """Return the value under ``key``.
 
-    def load(self, *key, **kwargs):
-        key = _norm_key(key)
-        alloc = kwargs.pop("alloc", None)
-        default = kwargs.pop("default", _no_default)
-        tags = kwargs.pop("tags", None)
-        if alloc is not None and default is not _no_default:
-            raise TypeError("The optional arguments alloc and default can not be used at the same time.")
-        if tags is not None and alloc is None:
-            raise TypeError("The tags argument is only allowed when the alloc argument is present.")
-        if kwargs:
-            raise TypeError("Unknown optional arguments: %s" % list(kwargs))
-        item = self._store.get(key)
-        if alloc is not None:
-            if item is None:
-                item = CacheItem.from_alloc(alloc, tags)
-                self._store[key] = item
-                return item.value, True
-            if not item.valid:
-                try:
-                    item.check_alloc(alloc)
-                    item._valid = True
-                    item.check_tags(tags)
-                except TypeError:
-                    item = CacheItem.from_alloc(alloc, tags)
-                    self._store[key] = item
-                return item.value, True
-            item.check_alloc(alloc)
-            item.check_tags(tags)
-            return item.value, False
-        if default is not _no_default:
-            return default if item is None or not item.valid else item.value
-        if item is None or not item.valid:
-            raise KeyError(key)
-        return item.value
+        ``default``: returned when the entry is absent or stale.
+        ``alloc``: shape of a float64 array to hand out; returns
+        ``(array, new)`` and creates (or revives) the entry when needed.
+        ``tags`` may only accompany ``alloc``.
+        """
+        key = _entry_key(key)
+        if alloc is not None and default is not _MISSING:
+            raise TypeError("load takes either alloc or default, not both")
+        if alloc is None:
+            if tags is not None:
+                raise TypeError("tags are given at allocation (or dump) time only")
+            entry = self._live(key)
+            if entry is not None:
+                return entry.value
+            if default is _MISSING:
+                raise KeyError(key)
+            return default
+        return self._allocate(key, _shape_of(alloc), _tag_set(tags))
 
-    def __contains__(self, key):
-        item = self._store.get(_norm_key(key))
-        return item is not None and item.valid
-
-    def dump(self, *args, **kwargs):
-        tags = kwargs.pop("tags", None)
-        if kwargs:
-            raise TypeError("Unknown optional arguments: %s" % list(kwargs))
-        if len(args) < 2:
-            raise TypeError("At least two arguments are required: key1 and value.")
-        self._store[_norm_key(args[:-1])] = CacheItem(args[-1], tags)
-
-    def __len__(self):
-        return sum(item.valid for item in self._store.values())
+    def _allocate(self, key, shape, tags):
+        entry = self._store.get(key)
+        if entry is not None and entry.holds_float_array(shape):
+            if entry.tags != tags:
+                raise ValueError(f"cache entry {key!r} has tags {sorted(entry.tags)}, "
+                                 f"not {sorted(tags)}")
+            revived = entry.stale
+            entry.stale = False
+            return entry.value, revived
+        if entry is not None and not entry.stale:
+            raise TypeError(f"cache entry {key!r} is not a float array of shape {shape}")
+        entry = _Entry(np.zeros(shape), tags)
+        self._store[key] = entry
+        return entry.value, True
 
     def __getitem__(self, key):
         return self.load(key)
 
-    def __setitem__(self, key, value):
-        return self.dump(key, value)
+    def __contains__(self, key):
+        return self._live(_entry_key(key)) is not None
 
-    def __iter__(self):
-        return iter(self.iterkeys())
+    def __len__(self):
+        return sum(1 for e in self._store.values() if not e.stale)
+
+    def _selected(self, tags):
+        want = _tag_set(tags)
+        for key, entry in self._store.items():
+            if not entry.stale and (not want or entry.tags & want):
+                yield key, entry.value
 
     def iterkeys(self, tags=None):
-        tags = _norm_tags(tags)
-        for key, item in self._store.items():
-            if item.valid and (not tags or item.tags & tags):
-                yield key
+        return (k for k, _ in self._selected(tags))
 
     def itervalues(self, tags=None):
-        tags = _norm_tags(tags)
-        for item in self._store.values():
-            if item.valid and (not tags or item.tags & tags):
-                yield item.value
+        return (v for _, v in self._selected(tags))
 
     def iteritems(self, tags=None):
-        tags = _norm_tags(tags)
-        for key, item in self._store.items():
-            if item.valid and (not tags or item.tags & tags):
-                yield key, item.value
+        return self._selected(tags)
+
+    def __iter__(self):
+        return self.iterkeys()
+
+    # -- writing ------------------------------------------------------------
+    def dump(self, *key_and_value, tags=None):
+        """``dump(key..., value, tags=None)``: store ``value`` under ``key``."""
+        if len(key_and_value) < 2:
+            raise TypeError("dump needs a key and a value")
+        self._store[_entry_key(key_and_value[:-1])] = _Entry(key_and_value[-1], _tag_set(tags))
+
+    def __setitem__(self, key, value):
+        self.dump(key, value)
+
+    def clear_item(self, *key, dealloc=False):
+        """Invalidate (arrays, ``__clear__`` objects) or remove one entry."""
+        key = _entry_key(key)
+        entry = self._store.get(key)
+        if entry is not None and (dealloc or not entry.invalidate()):
+            del self._store[key]
+
+    def clear(self, dealloc=False, tags=None):
+        """Clear every entry, or those sharing a tag with ``tags``."""
+        want = _tag_set(tags)
+        for key in [k for k, e in self._store.items() if not want or e.tags & want]:
+            self.clear_item(key, dealloc=dealloc)

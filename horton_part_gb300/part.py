@@ -44,116 +44,96 @@ def _setup_logger(logger):
 
 
 class Part(JustOnceClass):
-    """Base class of the partitioning schemes (``core/base.py:35-410``)."""
+    """Geometry, density, grid and result cache of one partitioning problem.
+
+    Public surface of horton-part's ``Part`` (``core/base.py:35-410``):
+    constructor ``(coordinates, numbers, pseudo_numbers, grid, moldens,
+    spindens, local, lmax, logger)``, the read-only properties, ``part[key]``
+    for cached results and the ``do_*`` entry points. With ``local`` each atom
+    integrates on its own atomic grid (``grid.atgrids[i]``), otherwise on the
+    molecular grid.
+    """
 
     name = None
 
     def __init__(self, coordinates, numbers, pseudo_numbers, grid, moldens, spindens, local, lmax,
                  logger, *args, **kwargs):
         super().__init__()
-        natom, coordinates, numbers, pseudo_numbers = typecheck_geo(coordinates, numbers,
-                                                                    pseudo_numbers)
-        self._natom = natom
-        self._coordinates = coordinates
-        self._numbers = numbers
-        self._pseudo_numbers = pseudo_numbers
-        self._grid = grid
-        self._moldens = moldens
-        self._spindens = spindens
-        self._local = local
-        self._lmax = lmax
+        checked = typecheck_geo(coordinates, numbers, pseudo_numbers)
+        self._natom, self._coordinates, self._numbers, self._pseudo_numbers = checked
+        self._grid, self._moldens, self._spindens = grid, moldens, spindens
+        self._local, self._lmax = bool(local), lmax
         self._cache = Cache()
         self.logger = logger
-        if local:
-            self._init_subgrids()
-        self._init_log_scheme()
+        self._subgrids = grid.atgrids if self._local else None
 
-    def __getitem__(self, key):
-        return self.cache.load(key)
-
-    def variables_stored_in_cache(self):
-        return list(self.cache.iterkeys())
-
-    @property
-    def natom(self):
-        return self._natom
-
-    @property
-    def coordinates(self):
-        return self._coordinates
-
-    @property
-    def numbers(self):
-        return self._numbers
-
-    @property
-    def pseudo_numbers(self):
-        return self._pseudo_numbers
-
-    @property
-    def nelec(self):
-        return self.grid.integrate(self._moldens)
+    # -- read-only state ------------------------------------------------------
+    natom = property(lambda self: self._natom)
+    coordinates = property(lambda self: self._coordinates)
+    numbers = property(lambda self: self._numbers)
+    pseudo_numbers = property(lambda self: self._pseudo_numbers)
+    local = property(lambda self: self._local)
+    lmax = property(lambda self: self._lmax)
+    cache = property(lambda self: self._cache)
 
     @property
     def grid(self):
-        return self.get_grid()
+        return self._grid
 
     @property
-    def local(self):
-        return self._local
+    def nelec(self):
+        """Electrons in the molecular density (integral over the molecular grid)."""
+        return self._grid.integrate(self._moldens)
 
-    @property
-    def lmax(self):
-        return self._lmax
+    def __getitem__(self, key):
+        return self._cache.load(key)
 
-    @property
-    def cache(self):
-        return self._cache
-
-    def __clear__(self):
-        self.clear()
+    def variables_stored_in_cache(self):
+        return list(self._cache.iterkeys())
 
     def clear(self):
-        JustOnceClass.clear(self)
-        self.cache.clear()
+        """Forget every result: run-once marks and the cache."""
+        super().clear()
+        self._cache.clear()
 
+    # -- grids and fields -------------------------------------------------------
     def get_grid(self, index=None):
-        if index is None or not self.local:
+        """Atom ``index``'s integration grid (its atomic grid when local)."""
+        if index is None or not self._local:
             return self._grid
         return self._subgrids[index]
 
-    def get_moldens(self, index=None, output=None):
-        result = self._moldens if index is None or not self.local else self.to_atomic_grid(
-            index, self._moldens)
+    def _field_on(self, index, field, output):
+        values = field if index is None or not self._local else self.to_atomic_grid(index, field)
         if output is not None:
-            output[:] = result
-        return result
+            output[:] = values
+        return values
+
+    def get_moldens(self, index=None, output=None):
+        return self._field_on(index, self._moldens, output)
 
     def get_spindens(self, index=None, output=None):
-        result = self._spindens if index is None or not self.local else self.to_atomic_grid(
-            index, self._spindens)
-        if output is not None:
-            output[:] = result
-        return result
-
-    def _init_subgrids(self):
-        raise NotImplementedError
-
-    def _init_log_scheme(self):
-        pass
+        return self._field_on(index, self._spindens, output)
 
     def to_atomic_grid(self, index, data):
         raise NotImplementedError
 
     def get_wcor(self, index):
+        """Weight correction of atom ``index``'s integrals (none here)."""
         return 1.0
 
-    def compute_pseudo_population(self, index):
-        grid = self.get_grid(index)
-        dens = self.get_moldens(index)
-        at_weights = self.cache.load(f"at_weights_{index}")
-        return grid.integrate(at_weights, dens)
+    def _aim_integral(self, index, field):
+        """Integral of ``at_weights_{index} * field`` over atom ``index``'s grid."""
+        weights = self._cache.load(f"at_weights_{index}")
+        if self._local and weights.shape == self._grid.weights.shape:
+            weights = self.to_atomic_grid(index, weights)
+        on_atom = self._field_on(index, field, None)
+        return self.get_grid(index).integrate(weights, on_atom * self.get_wcor(index))
 
+    def compute_pseudo_population(self, index):
+        return self._aim_integral(index, self._moldens)
+
+    # -- entry points -----------------------------------------------------------
     @just_once
     def do_partitioning(self):
         self.update_at_weights()
@@ -163,128 +143,107 @@ class Part(JustOnceClass):
 
     @just_once
     def do_populations(self):
-        """Atomic populations from the at_weights (``core/base.py:277-300``)."""
-        populations, new = self.cache.load("populations", alloc=self.natom, tags="o")
-        if new:
-            self.do_partitioning()
-            pseudo_populations = self.cache.load("pseudo_populations", alloc=self.natom, tags="o")[0]
-            for index in range(self.natom):
-                grid = self.get_grid(index)
-                dens = self.get_moldens(index)
-                at_weights = self.cache.load(f"at_weights_{index}")
-                wcor = self.get_wcor(index)
-                if at_weights.shape == self._grid.weights.shape:
-                    at_weights = self.to_atomic_grid(index, at_weights)
-                pseudo_populations[index] = grid.integrate(at_weights, dens * wcor)
-            populations[:] = pseudo_populations
-            populations += self.numbers - self.pseudo_numbers
+        """``populations`` = AIM electron counts + (numbers - pseudo_numbers)."""
+        if "populations" in self._cache:
+            return
+        self.do_partitioning()
+        pseudo = np.array([self.compute_pseudo_population(i) for i in range(self._natom)])
+        self._cache.dump("pseudo_populations", pseudo, tags="o")
+        self._cache.dump("populations", pseudo + (self._numbers - self._pseudo_numbers), tags="o")
 
     @just_once
     def do_charges(self):
-        """Atomic charges (``core/base.py:302-311``)."""
-        charges, new = self._cache.load("charges", alloc=self.natom, tags="o")
-        if new:
-            self.do_populations()
-            populations = self._cache.load("populations")
-            charges[:] = self.numbers - populations
+        """``charges`` = numbers - populations."""
+        if "charges" in self._cache:
+            return
+        self.do_populations()
+        self._cache.dump("charges", self._numbers - self._cache.load("populations"), tags="o")
 
     @just_once
     def do_spin_charges(self):
-        """Atomic spin charges (``core/base.py:313-327``)."""
-        if self._spindens is not None:
-            spin_charges, _ = self._cache.load("spin_charges", alloc=self.natom, tags="o")
-            self.do_partitioning()
-            for index in range(self.natom):
-                grid = self.get_grid(index)
-                spindens = self.get_spindens(index)
-                at_weights = self.cache.load(f"at_weights_{index}")
-                spin_charges[index] = grid.integrate(at_weights, spindens * self.get_wcor(index))
+        """``spin_charges``: AIM integrals of the spin density (when one was given)."""
+        if self._spindens is None:
+            return
+        self.do_partitioning()
+        spin = np.array([self._aim_integral(i, self._spindens) for i in range(self._natom)])
+        self._cache.dump("spin_charges", spin, tags="o")
 
     def do_all(self):
         """Run every implemented ``do_*`` method; return the output keys."""
-        for name in ("do_partitioning", "do_populations", "do_charges", "do_spin_charges"):
-            getattr(self, name)()
-        return list(self.cache.iterkeys(tags="o"))
+        self.do_partitioning()
+        self.do_populations()
+        self.do_charges()
+        self.do_spin_charges()
+        return list(self._cache.iterkeys(tags="o"))
+
+
+# grid_type -> (integrals on the molecular grid, atomic grids not needed at all)
+# 1: atomic grids for everything, the molecular grid only for the weights;
+# 2: molecular grid for everything, atomic grids for constraints;
+# 3: molecular grid only.
+_GRID_TYPES = {1: (False, False), 2: (True, False), 3: (True, True)}
 
 
 class WPart(Part):
-    """Grid-based partitioning (``core/base.py:413-499``)."""
+    """Partitioning on a Becke molecular grid with optional atomic grids.
+
+    Public surface of horton-part's ``WPart`` (``core/base.py:413-636``):
+    ``grid_type`` (1, 2 or 3), the three numerical cutoffs, the iteration
+    histories and the radial distances of the grid points to every atom.
+    """
 
     def __init__(self, coordinates, numbers, pseudo_numbers, grid, moldens, spindens=None, lmax=3,
                  logger=None, grid_type=1, density_cutoff=DENSITY_CUTOFF,
                  negative_cutoff=NEGATIVE_CUTOFF, population_cutoff=POPULATION_CUTOFF, **kwargs):
         self._grid_type = grid_type
-        self._on_molgrid = None
-        self._only_use_molgrid = None
         self.setup_grids()
         local = not self._only_use_molgrid
         if local and getattr(grid, "atgrids", None) is None:
-            raise ValueError("Atomic grids are discarded from molecular grid object, "
-                             "but are needed for local integrations.")
+            raise ValueError(f"grid_type={grid_type} integrates on atomic grids, but the grid "
+                             "object carries none (grid.atgrids is None)")
         if logger is None:
-            logger = logging.getLogger(self.__class__.__name__)
+            logger = logging.getLogger(type(self).__name__)
             _setup_logger(logger)
-        self.history_propars = []
-        self.history_charges = []
-        self.history_entropies = []
-        self.history_changes = []
-        self.history_time_update_at_weights = []
-        self.history_time_update_propars = []
+        for name in ("propars", "charges", "entropies", "changes", "time_update_at_weights",
+                     "time_update_propars"):
+            setattr(self, "history_" + name, [])
         self._radial_distances = []
         self._density_cutoff = density_cutoff
-        self._population_cutoff = population_cutoff
         self._negative_cutoff = negative_cutoff
+        self._population_cutoff = population_cutoff
         super().__init__(coordinates, numbers, pseudo_numbers, grid, moldens, spindens, local, lmax,
                          logger)
 
     def setup_grids(self):
-        assert self.grid_type in [1, 2, 3]
-        self._on_molgrid = self.grid_type in [2, 3]
-        self._only_use_molgrid = self.grid_type in [3]
+        if self._grid_type not in _GRID_TYPES:
+            raise AssertionError(f"grid_type must be 1, 2 or 3, not {self._grid_type!r}")
+        self._on_molgrid, self._only_use_molgrid = _GRID_TYPES[self._grid_type]
 
-    @property
-    def grid_type(self):
-        return self._grid_type
+    grid_type = property(lambda self: self._grid_type)
+    on_molgrid = property(lambda self: self._on_molgrid)
+    only_use_molgrid = property(lambda self: self._only_use_molgrid)
+    density_cutoff = property(lambda self: self._density_cutoff)
+    negative_cutoff = property(lambda self: self._negative_cutoff)
+    population_cutoff = property(lambda self: self._population_cutoff)
 
-    @property
-    def only_use_molgrid(self):
-        return self._only_use_molgrid
-
-    @property
-    def on_molgrid(self):
-        return self._on_molgrid
+    def to_atomic_grid(self, index, data):
+        """The slice of a molecular-grid array that belongs to atom ``index``."""
+        if index is None or not self._local:
+            return data
+        lo, hi = self._grid.indices[index], self._grid.indices[index + 1]
+        return data[lo:hi]
 
     @property
     def radial_distances(self):
+        """|r_p - R_a| for every atom a (list of arrays over the molecular grid)."""
         self.calc_radial_distances()
         return self._radial_distances
 
-    @property
-    def density_cutoff(self):
-        return self._density_cutoff
-
-    @property
-    def population_cutoff(self):
-        return self._population_cutoff
-
-    @property
-    def negative_cutoff(self):
-        return self._negative_cutoff
-
-    def _init_subgrids(self):
-        self._subgrids = self._grid.atgrids
-
-    def to_atomic_grid(self, index, data):
-        if index is None or not self.local:
-            return data
-        begin, end = self.grid.indices[index], self.grid.indices[index + 1]
-        return data[begin:end]
-
     @just_once
     def calc_radial_distances(self):
-        for iatom in range(self.natom):
-            self._radial_distances.append(
-                np.linalg.norm(self.grid.points - self.coordinates[iatom], axis=1))
+        points = np.asarray(self._grid.points)
+        self._radial_distances = [np.sqrt(((points - c) ** 2).sum(axis=1))
+                                  for c in self._coordinates]
 
 
 class GPUStockholderWPart(WPart):

@@ -53,38 +53,39 @@ def wpart_schemes(scheme):
 
 def typecheck_geo(coordinates=None, numbers=None, pseudo_numbers=None, need_coordinates=True,
                   need_numbers=True, need_pseudo_numbers=True):
-    """Type-check a geometry; returns ``[natom] + checked arguments``."""
-    if coordinates is not None:
-        natom = len(coordinates)
-    elif numbers is not None:
-        natom = len(numbers)
-    elif pseudo_numbers is not None:
-        natom = len(pseudo_numbers)
-    else:
-        raise TypeError("At least one argument is required and should not be None")
-    if coordinates is None:
-        if need_coordinates:
-            raise TypeError("Coordinates can not be None.")
-    elif coordinates.shape != (natom, 3) or not issubclass(coordinates.dtype.type, float):
-        raise TypeError("The argument centers must be a float array with shape (natom,3).")
-    if numbers is None:
-        if need_numbers:
-            raise TypeError("Numbers can not be None.")
-    elif numbers.shape != (natom,) or not issubclass(numbers.dtype.type, np.int64):
-        raise TypeError("The argument numbers must be a vector with length natom.")
-    if pseudo_numbers is None:
-        if need_pseudo_numbers:
-            pseudo_numbers = numbers.astype(float)
-    else:
+    """Check a geometry and return ``[natom]`` followed by the needed arrays.
+
+    Same contract as horton-part's ``utils.typecheck_geo``: the atom count
+    comes from the first array given; ``coordinates`` must be float64 with
+    shape (natom, 3), ``numbers`` int64 with shape (natom,); ``pseudo_numbers``
+    (natom,) is converted to float64 and defaults to ``numbers``. An array
+    whose ``need_*`` flag is False may be None and is left out of the result.
+    Violations raise ``TypeError``.
+    """
+    given = [a for a in (coordinates, numbers, pseudo_numbers) if a is not None]
+    if not given:
+        raise TypeError("typecheck_geo needs coordinates, numbers or pseudo_numbers")
+    natom = len(given[0])
+
+    def check(label, array, needed, shape, dtype):
+        if array is None:
+            if needed:
+                raise TypeError(f"{label} are required")
+            return
+        if array.shape != shape or array.dtype != dtype:
+            raise TypeError(f"{label} must be a {np.dtype(dtype).name} array of shape {shape}, "
+                            f"got {array.dtype} {array.shape}")
+
+    check("coordinates", coordinates, need_coordinates, (natom, 3), np.float64)
+    check("numbers", numbers, need_numbers, (natom,), np.int64)
+    if pseudo_numbers is not None:
         if pseudo_numbers.shape != (natom,):
-            raise TypeError("The argument pseudo_numbers must be a vector with length natom.")
-        if not issubclass(pseudo_numbers.dtype.type, float):
-            pseudo_numbers = pseudo_numbers.astype(float)
-    result = [natom]
-    if need_coordinates:
-        result.append(coordinates)
-    if need_numbers:
-        result.append(numbers)
-    if need_pseudo_numbers:
-        result.append(pseudo_numbers)
-    return result
+            raise TypeError(f"pseudo_numbers must have shape ({natom},), got {pseudo_numbers.shape}")
+        pseudo_numbers = np.asarray(pseudo_numbers, dtype=np.float64)
+    elif need_pseudo_numbers:
+        if numbers is None:
+            raise TypeError("pseudo_numbers default to numbers, and neither was given")
+        pseudo_numbers = numbers.astype(np.float64)
+    wanted = ((need_coordinates, coordinates), (need_numbers, numbers),
+              (need_pseudo_numbers, pseudo_numbers))
+    return [natom] + [array for needed, array in wanted if needed]

@@ -4,14 +4,16 @@
 
 Each ``csrc/*.cu`` translation unit is compiled in parallel with
 ``-gencode arch=compute_103a,code=sm_103a -lineinfo -O3`` and linked into a
-shared library next to this file. Rebuilds only when a source or header is
-newer than the library.
+shared library next to this file. Rebuilds unless the stamp beside the
+library records the same sources, flags and machine architecture.
 """
 
 from __future__ import annotations
 
 import glob
+import hashlib
 import os
+import platform
 import shutil
 import subprocess
 import sys
@@ -40,18 +42,35 @@ def sources():
     return sorted(glob.glob(os.path.join(CSRC, "*.cu")))
 
 
-def _stale():
-    if not os.path.exists(LIB):
+STAMP = LIB + ".stamp"
+
+
+def _fingerprint(extra_flags=()):
+    """Hash of every source and header, the flags and the host machine: a
+    library built elsewhere (another architecture, other sources) never
+    matches and is rebuilt."""
+    h = hashlib.sha256()
+    deps = sorted(sources() + glob.glob(os.path.join(CSRC, "*.cuh")) + glob.glob(
+        os.path.join(CSRC, "*.h")) + glob.glob(os.path.join(INCLUDE, "*.h")))
+    for path in deps:
+        h.update(os.path.basename(path).encode())
+        with open(path, "rb") as f:
+            h.update(f.read())
+    h.update(" ".join([*ARCH, *NVCC_FLAGS, *extra_flags]).encode())
+    h.update(platform.machine().encode())
+    return h.hexdigest()
+
+
+def _stale(extra_flags=()):
+    if not os.path.exists(LIB) or not os.path.exists(STAMP):
         return True
-    t = os.path.getmtime(LIB)
-    deps = sources() + glob.glob(os.path.join(CSRC, "*.cuh")) + glob.glob(
-        os.path.join(CSRC, "*.h")) + glob.glob(os.path.join(INCLUDE, "*.h"))
-    return any(os.path.getmtime(p) > t for p in deps)
+    with open(STAMP) as f:
+        return f.read().strip() != _fingerprint(extra_flags)
 
 
 def build(force=False, verbose=False, extra_flags=()):
     """Compile and link; returns the library path."""
-    if not force and not _stale():
+    if not force and not _stale(extra_flags):
         return LIB
     os.makedirs(BUILD, exist_ok=True)
     exe = nvcc()
@@ -74,6 +93,8 @@ def build(force=False, verbose=False, extra_flags=()):
     if res.returncode != 0:
         raise RuntimeError(f"link failed:\n{res.stdout}\n{res.stderr}")
     os.replace(tmp, LIB)
+    with open(STAMP, "w") as f:
+        f.write(_fingerprint(extra_flags) + "\n")
     return LIB
 
 

@@ -493,6 +493,8 @@ void launch_mbis_inner_ff(const HostBatch& hb, cudaStream_t st);
 void launch_final_atweights_ff(const HostBatch& hb, cudaStream_t st, int use_old);
 
 extern long long g_launch_count;
+// Message returned by hp_last_error() for the calling thread (hp_runtime.cu).
+void set_error_text(const char* msg);
 
 constexpr int kHessTile = 64;
 constexpr int kNewtonQ(int k) { return k + k * (k + 1) / 2 + 2; }

@@ -13,6 +13,7 @@
 #include <cuda_runtime.h>
 
 #include <mutex>
+#include <string>
 
 #include "hp_internal.cuh"
 #include "hpgpu.h"
@@ -144,7 +145,17 @@ __global__ void k_na_mbis_update(int ntile, int nshell, double threshold, int ma
 }
 
 std::mutex g_na_mutex;
-double* g_na_ptr[64] = {};  // per-device address of hp_noalloc_scratch
+// Per-device address of hp_noalloc_scratch, looked up once per process.
+// cudaDeviceReset unloads the module: calls after a reset are unsupported.
+double* g_na_ptr[64] = {};
+
+// Status with its message for hp_last_error() (every error path sets one).
+int na_fail(int code, const char* what, cudaError_t e = cudaSuccess) {
+  std::string msg = std::string("hp_mbis_inner_noalloc: ") + what;
+  if (e != cudaSuccess) msg += std::string(": ") + cudaGetErrorString(e);
+  hp::set_error_text(msg.c_str());
+  return code;
+}
 
 }  // namespace
 
@@ -153,11 +164,20 @@ extern "C" int32_t hp_mbis_inner_noalloc(const double* rho_a, const double* weig
                                          int32_t nshell, double* propars, double threshold,
                                          double density_cutoff, int32_t maxiter, int32_t* niter,
                                          int32_t* converged, void* stream) {
-  if (!rho_a || !weights || !radial_dist || !propars) return HP_ERR_INVALID;
-  if (nshell < 1 || nshell > kNaMaxShell || maxiter < 1) return HP_ERR_INVALID;
-  if (npoint < 1 || npoint > (int64_t)kNaTile * kNaMaxTiles) return HP_ERR_INVALID;
+  if (!rho_a || !weights || !radial_dist || !propars)
+    return na_fail(HP_ERR_INVALID, "null device pointer");
+  if (nshell < 1 || nshell > kNaMaxShell) return na_fail(HP_ERR_INVALID, "nshell must be 1..7");
+  if (maxiter < 1) return na_fail(HP_ERR_INVALID, "maxiter must be positive");
+  if (npoint < 1 || npoint > (int64_t)kNaTile * kNaMaxTiles)
+    return na_fail(HP_ERR_INVALID, "npoint must be 1..2,097,152 (size of the static scratch)");
   int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return HP_ERR_CUDA;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return na_fail(HP_ERR_CUDA, "cudaGetDevice", e);
+  if (dev < 0 || dev >= 64) return na_fail(HP_ERR_CUDA, "device index above 63");
+  // An error left pending by the caller's own work is reported, not cleared:
+  // it is theirs, and the launches below would otherwise be blamed for it.
+  e = cudaPeekAtLastError();
+  if (e != cudaSuccess) return na_fail(HP_ERR_CUDA, "a CUDA error was pending before the call", e);
   double* scratch = nullptr;
   {
     // Set-up, once per device, with that device current: the host-side name
@@ -165,7 +185,8 @@ extern "C" int32_t hp_mbis_inner_noalloc(const double* rho_a, const double* weig
     std::lock_guard<std::mutex> lock(g_na_mutex);
     if (!g_na_ptr[dev]) {
       void* p = nullptr;
-      if (cudaGetSymbolAddress(&p, hp_noalloc_scratch) != cudaSuccess || !p) return HP_ERR_CUDA;
+      e = cudaGetSymbolAddress(&p, hp_noalloc_scratch);
+      if (e != cudaSuccess || !p) return na_fail(HP_ERR_CUDA, "cudaGetSymbolAddress", e);
       g_na_ptr[dev] = (double*)p;
     }
     scratch = g_na_ptr[dev];
@@ -182,11 +203,12 @@ extern "C" int32_t hp_mbis_inner_noalloc(const double* rho_a, const double* weig
                                                     density_cutoff, scratch);
       k_na_mbis_update<<<1, 32, 0, st>>>(ntile, nshell, threshold, maxiter, propars, scratch);
     }
-    if (cudaGetLastError() != cudaSuccess) return HP_ERR_CUDA;
-    if (cudaMemcpyAsync(state, scratch + kNaQ * kNaMaxTiles, sizeof(state), cudaMemcpyDeviceToHost,
-                        st) != cudaSuccess ||
-        cudaStreamSynchronize(st) != cudaSuccess)
-      return HP_ERR_CUDA;
+    e = cudaGetLastError();  // nothing was pending above: these are our launches
+    if (e != cudaSuccess) return na_fail(HP_ERR_CUDA, "kernel launch", e);
+    e = cudaMemcpyAsync(state, scratch + kNaQ * kNaMaxTiles, sizeof(state), cudaMemcpyDeviceToHost,
+                        st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return na_fail(HP_ERR_CUDA, "reading the solver state", e);
     if (state[kSDone] != 0.0) break;
   }
   if (niter) *niter = (int32_t)state[kSIt];

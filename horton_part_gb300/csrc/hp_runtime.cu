@@ -43,6 +43,10 @@ size_t align_up(size_t x) { return (x + kAlign - 1) / kAlign * kAlign; }
 
 }  // namespace
 
+namespace hp {
+void set_error_text(const char* msg) { g_err = msg ? msg : ""; }
+}  // namespace hp
+
 struct hp_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;

@@ -10,7 +10,8 @@ step (``newton``), the positivity line search (``m-newton``) or the
 self-consistent update (``sc``, ``glisa.py:805-879``).
 
 ``cvxopt`` (the class default in the reference) needs the cvxopt package; it
-is served by ``sc``, which converges to the same non-negative optimum.
+is served by a projected Newton method on c >= 0 (solver name ``pnewton``),
+which reaches the same non-negative optimum of the convex objective.
 """
 
 from __future__ import annotations

@@ -255,12 +255,16 @@ int32_t hp_ctx_profile_get(hp_ctx* ctx, int32_t family, double* ms, int64_t* lau
  * and radial_dist hold npoint values (the atom's AIM density w_a * rho, the
  * grid weights and |r - R_a|); propars holds the 2*nshell (N, S) pairs on
  * input and the solution on output. niter and converged are optional HOST
- * outputs. Runs on `stream` (NULL = default stream) and returns after it.
+ * outputs. Runs on `stream` (NULL = default stream) and returns after it;
+ * it blocks the host on that stream every 4 inner iterations (8 for the first
+ * chunk) to read its done flag, so it is synchronous, not asynchronous.
  * Limits: 1 <= nshell <= 7 and npoint <= 2,097,152 (HP_ERR_INVALID beyond).
  * The scratch is one 492 KB static device array per GPU, shared by all calls:
  * calls that overlap on the GPU (other streams or threads) race on it. The
  * first call on a device looks up that array's address; make that first call
- * before any stream capture. */
+ * before any stream capture. The address is kept for the life of the process:
+ * calls after cudaDeviceReset are unsupported. A CUDA error already pending
+ * when the call starts is returned as HP_ERR_CUDA without clearing it. */
 int32_t hp_mbis_inner_noalloc(const double* rho_a, const double* weights,
                               const double* radial_dist, int64_t npoint, int32_t nshell,
                               double* propars, double threshold, double density_cutoff,

@@ -20,7 +20,9 @@ import numpy as np
 
 from oracle import refshim
 
-REFERENCE_SRC = os.environ.get("HP_REFERENCE_SRC", "/root/reference/src")
+# The reference source tree (its ``src`` directory); no default: the fixture
+# scripts that import the reference name it explicitly.
+REFERENCE_SRC = os.environ.get("HP_REFERENCE_SRC", "")
 
 
 def _integrate(weights, arrays):
@@ -77,8 +79,9 @@ class DuckAtomGrid:
 
 
 def available():
-    return os.path.isdir(os.path.join(REFERENCE_SRC, "horton_part")) and refshim.activate(
-        REFERENCE_SRC)
+    if not REFERENCE_SRC or not os.path.isdir(os.path.join(REFERENCE_SRC, "horton_part")):
+        return False
+    return refshim.activate(REFERENCE_SRC)
 
 
 def _quiet_logger():

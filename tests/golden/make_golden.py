@@ -1,9 +1,9 @@
 """Write the golden fixtures in this folder by running the unmodified
 reference (horton-part) on seeded synthetic inputs.
 
-Run from the repository root, where the reference source tree is available:
+Run from the repository root, naming the reference's source tree:
 
-    python tests/golden/make_golden.py
+    HP_REFERENCE_SRC=<horton-part checkout>/src python tests/golden/make_golden.py
 
 Each ``<case>.npz`` holds the reference's results (charges, pro-atom
 parameters, iteration counts and histories) plus fingerprints of the inputs

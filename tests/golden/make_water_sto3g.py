@@ -41,7 +41,9 @@ def exp_radial(rmin=5e-4, rmax=20.0, n=120):
 
 
 def main(reference=None):
-    reference = reference or os.environ.get("HP_REFERENCE_ROOT", "/root/reference")
+    reference = reference or os.environ.get("HP_REFERENCE_ROOT")
+    if not reference:
+        raise SystemExit("set HP_REFERENCE_ROOT to the reference checkout (its tests/cached data)")
     with np.load(os.path.join(reference, CACHED)) as f:
         dens, stored = f["dens"], f["points"]
         numbers, coords, pseudo = f["numbers"], f["coordinates"], f["pseudo_numbers"]

@@ -32,16 +32,23 @@ replica of the job (no collective on the data path); value = sum over ranks.
 
 from __future__ import annotations
 
-import argparse
-import json
 import os
-import statistics
-import subprocess
-import sys
-import threading
-import time
 
-import numpy as np
+# The CPU baseline of a single job runs the NumPy oracle on one core, as the
+# reference's single-job path runs (its NumPy element-wise work is single
+# threaded); BLAS must not fan out over the host's cores. Set before NumPy loads.
+os.environ.setdefault("OPENBLAS_NUM_THREADS", "1")
+os.environ.setdefault("MKL_NUM_THREADS", "1")
+
+import argparse  # noqa: E402
+import json  # noqa: E402
+import statistics  # noqa: E402
+import subprocess  # noqa: E402
+import sys  # noqa: E402
+import threading  # noqa: E402
+import time  # noqa: E402
+
+import numpy as np  # noqa: E402
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
@@ -224,28 +231,32 @@ class ClockSampler:
 # ---------------------------------------------------------------------------
 
 def cpu_sample(w, iterations):
-    """Time the FP64 NumPy oracle on the same input; returns (evals/s, sample text, threads)."""
+    """Time the FP64 NumPy oracle on the same input on one host core; returns
+    (evals/s, sample text, threads).
+
+    gLISA: the oracle's projected Newton (the optimum of the reference's
+    default cvxopt problem; cvxopt is not installed), the solver family the
+    GPU runs, for ``iterations`` solver iterations including the basis set-up,
+    counted like the GPU (three pro-atom passes per iteration)."""
     from oracle import hp_oracle as O
 
     mol = w["mol"]
     args = (mol.coordinates, mol.numbers, mol.pseudo_numbers, mol.grid.points, mol.grid.weights,
             mol.density)
-    threads = os.cpu_count() or 1
+    threads = 1
     if w["scheme"] == "glisa":
         h = w["helper"]
         orders = [h.get_order(z) for z in mol.numbers]
         exps = [h.get_exponent(z) for z in mol.numbers]
         inits = [h.get_initial(z) for z in mol.numbers]
         t0 = time.perf_counter()
-        try:
-            res = O.glisa(*args, orders, exps, inits, threshold=w["threshold"], solver="newton",
-                          maxiter=iterations)
-            nit = res["niter"]
-        except O.OracleError:
-            nit = iterations
+        res = O.glisa_nonneg(*args, orders, exps, inits, maxiter=iterations,
+                             raise_on_maxiter=False)
+        nit = res["niter"]
         dt = time.perf_counter() - t0
-        evals = 3.0 * mol.natom * mol.npoint * nit + mol.natom * mol.npoint
-        return evals / dt, f"oracle gLISA newton, {nit} solver iterations incl. basis set-up, {dt:.1f} s", threads
+        evals = 3.0 * mol.natom * mol.npoint * nit
+        return (evals / dt, f"oracle gLISA projected Newton (cvxopt problem), {nit} solver "
+                f"iterations incl. basis set-up, {dt:.1f} s, 1 thread", threads)
     if w["scheme"] == "gisa":
         h = w["helper"]
         t0 = time.perf_counter()
@@ -256,13 +267,13 @@ def cpu_sample(w, iterations):
         dt = time.perf_counter() - t0
         evals = 4.0 * mol.natom * mol.npoint * res["niter"]
         return (evals / dt, f"oracle GISA, {res['niter']} outer iterations incl. basis set-up, "
-                f"{dt:.1f} s", threads)
+                f"{dt:.1f} s, 1 thread", threads)
     t0 = time.perf_counter()
     res = O.mbis(*args, threshold=w["threshold"], maxiter=iterations, inner_threshold=w["threshold"])
     dt = time.perf_counter() - t0
     inner = sum(sum(x) for x in res["inner_iterations"])
     evals = mol.npoint * (3.0 * mol.natom * res["niter"] + inner)
-    return evals / dt, f"oracle MBIS, {res['niter']} outer iterations, {dt:.1f} s", 1
+    return evals / dt, f"oracle MBIS, {res['niter']} outer iterations, {dt:.1f} s, 1 thread", 1
 
 
 # ---------------------------------------------------------------------------
@@ -354,8 +365,11 @@ def run_ours(args):
     def run_all(js):
         for j in js:
             j.reset()
-        while ctx.step(js) > 0:
-            pass
+        if len(js) == 1:
+            js[0].run()  # hp_job_run: gLISA queues several iterations per round trip
+        else:
+            while ctx.step(js) > 0:
+                pass
 
     def one_step(js):
         if batched:
@@ -428,6 +442,8 @@ def run_ours(args):
         if batched:
             for _ in range(args.warmup + args.steps):
                 ctx.step(e2e_jobs)
+        elif len(e2e_jobs) == 1:
+            e2e_jobs[0].run()
         else:
             while ctx.step(e2e_jobs) > 0:
                 pass
@@ -493,59 +509,89 @@ def run_ours(args):
                         "ms_per_launch": per_launch_s * 1000.0,
                         "algorithmic_bytes_per_launch": alg_bytes,
                         "point_atom_evals_per_launch": evals / f_n}
-    if w["scheme"] == "glisa" and hess_n:
+    job_bound = None
+    if w["scheme"] == "glisa":
         nshell = config_of(w, args, args.precision)["nshell"]
-        per_launch_s = hess_ms / hess_n / 1000.0
-        if args.precision == "mixed":
-            # the two single kernels of a tensor-core gLISA step; the roofline
-            # line is the one with more time in the profiled step
+        g_active = float(job.info().g_active_values)
+        fused = args.precision == "mixed" and nshell <= 192 and g_active > 0
+        if fused:
+            # The two passes over G of a tensor-core gLISA iteration; the
+            # roofline line is the one with more time in the profiled step.
+            # Bytes: G's two float planes in the tiles' active rows only (8
+            # bytes per value; the other rows are identically zero on their
+            # tile and never read) plus the per-point arrays.
             cands = {}
-            # Hessian: algorithmic work of H = G diag(d) G^T, 2 M^2 N FLOP per
-            # launch, against cuBLAS's TF32 GEMM rate measured in this process
-            flops = 2.0 * nshell * nshell * mol.npoint
-            achieved = flops / per_launch_s / 1e12
-            tf32 = measure_tf32_peak()
-            hk = "k_glisa_hess_tc1" if nshell <= 256 else "k_glisa_hess_tc"
-            cands["hess"] = (hess_ms, {
-                "kernel": hk, "bound": "tensor", "achieved": achieved,
-                "peak": tf32, "unit": "TFLOP/s", "frac": achieved / tf32,
-                "traffic": NCU_TRAFFIC.get((w["name"], args.precision, hk)),
-                "algorithmic_bytes_per_launch": (nshell + 1) * mol.npoint * 4.0,
-                "peak_source": "measured: cuBLAS TF32 GEMM 8192^3, this run",
-                "bf16_peak_measured": peaks.get("bf16_tflops"),
-                "ms_per_launch": per_launch_s * 1000.0,
-                "algorithmic_flop_per_launch": flops,
-                "note": "3 TF32 MMAs per product (hi*hi, hi*lo, lo*hi); MMA area "
-                        "128 x (N1 + N2) per 32-point block"})
             pro_ms, pro_n = fam_ms["glisa_pro"]
-            if pro_n and nshell <= 192:
-                # fused promolecule + gradient (+ change) pass: G's two float
-                # planes once (8 S bytes per point), rho and w read, dvec1,
-                # dvec2, d1 pair, rho0 and sqrt(d2) written (36 bytes)
+            if pro_n:
+                # promolecule + gradient + change + tensor-core Hessian: w rho
+                # and rho as float pairs (16 B) and w (8 B) in, rho0 and
+                # w rho / rho0^2 as float pairs (16 B) out
                 p_s = pro_ms / pro_n / 1000.0
-                alg = mol.npoint * (8.0 * nshell + 16.0 + 36.0)
+                alg = 8.0 * g_active + mol.npoint * (16.0 + 8.0 + 16.0)
                 ach = alg / p_s / 1e9
+                hflop = 2.0 * nshell * nshell * mol.npoint
                 cands["pro"] = (pro_ms, {
                     "kernel": "k_glisa_fused_ff<1>", "bound": "hbm", "achieved": ach,
                     "peak": hbm_peak, "unit": "GB/s", "frac": ach / hbm_peak,
                     "traffic": NCU_TRAFFIC.get((w["name"], args.precision, "k_glisa_fused_ff<1>")),
                     "peak_source": "measured" if peaks else "fallback",
-                    "ms_per_launch": p_s * 1000.0, "algorithmic_bytes_per_launch": alg})
-            fam = max(cands, key=lambda k: cands[k][0])
-            roofline = cands[fam][1]
-            others = {k: v[1] for k, v in cands.items() if k != fam}
-            if others:
-                roofline["other_kernels"] = {v["kernel"]: {
-                    "achieved": v["achieved"], "unit": v["unit"], "frac": v["frac"],
-                    "ms_per_launch": v["ms_per_launch"]} for v in others.values()}
-        else:
-            alg_bytes = (nshell + 1) * mol.npoint * 8.0  # G and w rho/rho0^2 once
-            achieved = alg_bytes / per_launch_s / 1e9
-            roofline = {"kernel": "k_glisa_hess", "bound": "hbm", "achieved": achieved,
-                        "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
-                        "traffic": None, "peak_source": "measured" if peaks else "fallback",
-                        "ms_per_launch": per_launch_s * 1000.0,
-                        "note": "FP64 CUDA-core Hessian; FP64 issue rate, not HBM, limits it"}
+                    "ms_per_launch": p_s * 1000.0, "algorithmic_bytes_per_launch": alg,
+                    "active_fraction_of_G": g_active / (nshell * mol.npoint),
+                    "hessian_tflops_in_pass": hflop / p_s / 1e12,
+                    "hessian_flop_per_launch": hflop,
+                    "note": "one pass over G per iteration forms rho0, the gradient, the "
+                            "change (compensated FP32 sums) and the Hessian (tcgen05 TF32 "
+                            "MMAs on the staged sub-tiles)"})
+            tr_ms, tr_n = fam_ms.get("glisa_trials", (0.0, 0))
+            if tr_n:
+                # trial pass: u = G^T delta and eight trial objectives; rho0
+                # pair (8 B) and w rho / rho pairs (16 B) in
+                t_s = tr_ms / tr_n / 1000.0
+                alg = 8.0 * g_active + mol.npoint * (8.0 + 16.0)
+                ach = alg / t_s / 1e9
+                cands["trials"] = (tr_ms, {
+                    "kernel": "k_glisa_trials_fused", "bound": "hbm", "achieved": ach,
+                    "peak": hbm_peak, "unit": "GB/s", "frac": ach / hbm_peak,
+                    "traffic": NCU_TRAFFIC.get((w["name"], args.precision, "k_glisa_trials_fused")),
+                    "peak_source": "measured" if peaks else "fallback",
+                    "ms_per_launch": t_s * 1000.0, "algorithmic_bytes_per_launch": alg,
+                    "note": "family time: also the trial set-up and pick (one block per job)"})
+            if cands:
+                fam = max(cands, key=lambda k: cands[k][0])
+                roofline = cands[fam][1]
+                others = {k: v[1] for k, v in cands.items() if k != fam}
+                if others:
+                    roofline["other_kernels"] = {v["kernel"]: {
+                        "achieved": v["achieved"], "unit": v["unit"], "frac": v["frac"],
+                        "ms_per_launch": v["ms_per_launch"]} for v in others.values()}
+            # job-level bound: the bytes of G every solver iteration reads at
+            # least (two passes over the active rows of both planes) at the
+            # copy peak, against the measured time per job
+            per_iter = 2 * 8.0 * g_active
+            bound_ms = per_iter * niter / (hbm_peak * 1e9) * 1e3
+            job_bound = {"g_bytes_per_iteration": per_iter, "iterations": int(niter),
+                         "hbm_bound_ms": bound_ms, "frac_of_job": bound_ms / (ms / args.steps)}
+        elif hess_n and hess_ms > 0:
+            per_launch_s = hess_ms / hess_n / 1000.0
+            if args.precision == "mixed":
+                flops = 2.0 * nshell * nshell * mol.npoint
+                achieved = flops / per_launch_s / 1e12
+                tf32 = measure_tf32_peak()
+                hk = "k_glisa_hess_tc1" if nshell <= 256 else "k_glisa_hess_tc"
+                roofline = {
+                    "kernel": hk, "bound": "tensor", "achieved": achieved,
+                    "peak": tf32, "unit": "TFLOP/s", "frac": achieved / tf32,
+                    "traffic": NCU_TRAFFIC.get((w["name"], args.precision, hk)),
+                    "peak_source": "measured: cuBLAS TF32 GEMM 8192^3, this run",
+                    "ms_per_launch": per_launch_s * 1000.0, "algorithmic_flop_per_launch": flops}
+            else:
+                alg_bytes = (nshell + 1) * mol.npoint * 8.0  # G and w rho/rho0^2 once
+                achieved = alg_bytes / per_launch_s / 1e9
+                roofline = {"kernel": "k_glisa_hess", "bound": "hbm", "achieved": achieved,
+                            "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
+                            "traffic": None, "peak_source": "measured" if peaks else "fallback",
+                            "ms_per_launch": per_launch_s * 1000.0,
+                            "note": "FP64 CUDA-core Hessian; FP64 issue rate, not HBM, limits it"}
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -556,7 +602,7 @@ def run_ours(args):
         "point_atom_evals_per_step": evals_per_step, "kernel_ms_one_profiled_step": fams,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "seconds_per_step": e2e_s},
-        "roofline": roofline, "clocks": clocks.summary(),
+        "roofline": roofline, "job_hbm_bound": job_bound, "clocks": clocks.summary(),
         "gpu_launches": int(launches),
     }
     if args.precision == "mixed" and not args.no_check:

@@ -60,6 +60,7 @@ class JobInfo(ctypes.Structure):
         ("warnings", ctypes.c_uint32), ("converged", ctypes.c_int32),
         ("device_bytes", ctypes.c_int64), ("point_atom_evals", ctypes.c_double),
         ("polish_iterations", ctypes.c_int32), ("f64_factors", ctypes.c_int32),
+        ("g_active_values", ctypes.c_int64),
     ]
 
 
@@ -77,11 +78,13 @@ class HPError(RuntimeError):
 
 EXPORTED = ("hp_abi_version", "hp_last_error", "hp_ctx_create", "hp_ctx_destroy",
             "hp_ctx_synchronize", "hp_ctx_memory", "hp_job_create", "hp_job_destroy", "hp_step",
+            "hp_step_n",
             "hp_job_run", "hp_job_info_get", "hp_job_results_get", "hp_job_reset",
             "hp_ctx_profile", "hp_ctx_profile_get", "hp_mbis_inner_noalloc")
 
 KERNEL_FAMILIES = {"promol": 0, "inner": 1, "change": 2, "glisa_pro": 3, "glisa_grad": 4,
-                   "glisa_hess": 5, "glisa_solve": 6, "other": 7}
+                   "glisa_hess": 5, "glisa_solve": 6, "other": 7, "glisa_trials": 8}
+KERNEL_FAMILY_COUNT = 9
 
 _lib = None
 _lock = threading.Lock()
@@ -109,6 +112,8 @@ def lib():
         L.hp_job_destroy.argtypes = [ctypes.c_void_p]
         L.hp_step.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p), ctypes.c_int32,
                               ctypes.POINTER(ctypes.c_int32)]
+        L.hp_step_n.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p), ctypes.c_int32,
+                                ctypes.c_int32, ctypes.POINTER(ctypes.c_int32)]
         L.hp_job_run.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
         L.hp_job_info_get.argtypes = [ctypes.c_void_p, ctypes.POINTER(JobInfo)]
         L.hp_job_results_get.argtypes = [ctypes.c_void_p, ctypes.POINTER(JobResults)]
@@ -183,15 +188,20 @@ class Context:
     def launch_count(self):
         """Kernel launches issued by the library since profiling was enabled."""
         ms, n = ctypes.c_double(), ctypes.c_int64()
-        _check(lib().hp_ctx_profile_get(self._h, len(KERNEL_FAMILIES), ctypes.byref(ms),
+        _check(lib().hp_ctx_profile_get(self._h, KERNEL_FAMILY_COUNT, ctypes.byref(ms),
                                         ctypes.byref(n)))
         return n.value
 
-    def step(self, jobs):
-        """One outer iteration for every live job; returns the live count."""
+    def step(self, jobs, iterations=1):
+        """Advance every live job by one outer iteration (``iterations`` > 1:
+        up to that many in one host round trip, see ``hp_step_n``); returns
+        the live count."""
         arr = (ctypes.c_void_p * len(jobs))(*[j.handle for j in jobs])
         live = ctypes.c_int32()
-        _check(lib().hp_step(self._h, arr, len(jobs), ctypes.byref(live)))
+        if iterations == 1:
+            _check(lib().hp_step(self._h, arr, len(jobs), ctypes.byref(live)))
+        else:
+            _check(lib().hp_step_n(self._h, arr, len(jobs), int(iterations), ctypes.byref(live)))
         return live.value
 
     def close(self):

@@ -17,6 +17,7 @@
 
 #include "hp_ff.cuh"
 #include "hp_internal.cuh"
+#include "hp_umma.cuh"
 
 namespace hp {
 
@@ -137,6 +138,7 @@ __global__ void __launch_bounds__(kThreads) k_glisa_pro_ff(Batch bt) {
   __shared__ double out[2];
   int tile;
   const JobDev& J = decode_local_gf(bt, tile);
+  if (glisa_idle(J)) return;
   if (J.fuse) return;  // k_glisa_fused_ff<1>
   load_pairs(J.propars, J.nshell, cf);
   double acc[2] = {0.0, 0.0};
@@ -170,6 +172,7 @@ __global__ void __launch_bounds__(kThreads) k_glisa_pro_ff(Batch bt) {
 __global__ void __launch_bounds__(kThreads) k_glisa_grad_ff(Batch bt, int use_hvec) {
   int tile;
   const JobDev& J = decode_local_gf(bt, tile);
+  if (glisa_idle(J)) return;
   if (J.fuse) return;  // k_glisa_fused_ff
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int p0 = tile * J.tile_points;
@@ -210,6 +213,7 @@ __global__ void __launch_bounds__(kThreads) k_glisa_hv_ff(Batch bt) {
   __shared__ float2 df[kGffMaxShells];
   int local;
   const JobDev& J = decode_local_gf(bt, local);
+  if (glisa_idle(J)) return;
   if (J.fuse) return;  // k_glisa_fused_ff<0>
   load_pairs(J.delta, J.nshell, df);
   const int p = local * kThreads + threadIdx.x;
@@ -224,6 +228,7 @@ __global__ void __launch_bounds__(kThreads) k_glisa_u_ff(Batch bt) {
   __shared__ float2 df[kGffMaxShells];
   int local;
   const JobDev& J = decode_local_gf(bt, local);
+  if (glisa_idle(J)) return;
   load_pairs(J.delta, J.nshell, df);
   const int p = local * kThreads + threadIdx.x;
   if (p >= J.npoint) return;
@@ -243,6 +248,7 @@ __global__ void __launch_bounds__(kThreads) k_glisa_trials_ff(Batch bt) {
   __shared__ double out[kTrials];
   int tile;
   const JobDev& J = decode_local_gf(bt, tile);
+  if (glisa_idle(J)) return;
   float ah[kTrials], al[kTrials];
 #pragma unroll
   for (int t = 0; t < kTrials; ++t) ah[t] = al[t] = 0.0f;
@@ -415,16 +421,65 @@ __device__ __forceinline__ void zero_inactive(const JobDev& J, int tile, const i
     if (pos[m] < 0) J.gpart[(size_t)m * J.ntile + tile] = 0.0;
 }
 
+// Shared memory of the promolecule + gradient pass (MODE 1), which also
+// stages the sub-tile's X = G_hi diag(s) for the tensor-core Hessian: the
+// fused layout plus the X tile (fuse_x_rows(S) rows of 128 bytes, 1024-byte
+// aligned), an mbarrier and the tensor-memory slot. At least kFuseSmemFloor
+// bytes, so that at most two blocks share an SM (two 256-column tensor-memory
+// allocations fill its 512 columns).
+__host__ __device__ constexpr int fuse_x_rows(int S) {
+  return (S + 15) / 16 * 16 > umma::kTcM ? (S + 15) / 16 * 16 : umma::kTcM;
+}
+constexpr size_t kFuseSmemFloor = 78 * 1024;
+__host__ __device__ constexpr size_t fuse_hess_smem_bytes(int S) {
+  return fuse_smem_bytes(S) + 128 * (size_t)fuse_x_rows(S) + 1024 + 64 > kFuseSmemFloor
+             ? fuse_smem_bytes(S) + 128 * (size_t)fuse_x_rows(S) + 1024 + 64
+             : kFuseSmemFloor;
+}
+constexpr int kFuseTmemCols = 256;
+
+// Persistent blocks (launch kind K_FUSE): block b of a job takes the point
+// tiles b, b + nb, ... (nb = min(ntile, kFuseCtas)). The per-tile outputs
+// (gradient rows, entropy, change) stay per tile.
+//
+// MODE 1 also accumulates the Hessian H = X X^T of its tiles on the tensor
+// cores (glisa.py:457-470): after A' every warp knows s(p) = sqrt(w rho) /
+// rho0 (0 where sick) of the sub-tile's 32 points and writes its rows of X
+// (X[m][p] = G_hi[m][p] s(p), rounded to TF32 to nearest) into the
+// 128B-swizzled K-major tile in shared memory (the tile's inactive rows stay
+// zero); at the next block barrier thread 0 issues tcgen05.mma.kind::tf32
+// (M = 128, K = 8, four per sub-tile) for
+//   D1 (tensor-memory columns 0..n1-1):  A = X rows 0..127,        B = rows 0..n1-1,
+//   D2 (columns c2..c2+n1-129):          A = X rows n1-128..n1-1, B = rows 128..n1-1,
+// n1 = S rounded up to 16, c2 = n1 rounded up to 32 (D2 only when S > 128),
+// and commits to an mbarrier that the writers of the next sub-tile wait on.
+// D1 holds H[i][j] for i < 128 (its columns j >= 128 are H[j][i]); the rows
+// 256 - n1 .. 127 of D2 hold H[i][j] for i, j >= 128. At the end the block
+// writes its packed FP32 lower triangle to hpart[block] (k_glisa_reduce sums
+// the nsplit partials in FP64 in a fixed order). The accumulation order is
+// fixed (one issuing thread, tiles and sub-tiles in order), so a job's H is
+// the same alone and in a batch. Relative accuracy of H: a few 1e-4 (TF32
+// operands, FP32 accumulation of non-negative terms); the Newton direction
+// is refined against the exact product in the finish (polish), and the
+// gradient and objective stay compensated.
 template <int MODE>
 __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_fused_ff(Batch bt, int with_change) {
   extern __shared__ float4 fsm[];
-  int tile;
-  const JobDev& J = decode_local_gf(bt, tile);
+  int local;
+  const JobDev& J = decode_local_gf(bt, local);
+  if (glisa_idle(J)) return;
   if (!J.fuse) return;
   if (MODE == 0 && !glisa_refine_now(J)) return;
+  const int nblk_job = bt.prefix[find_job(bt, blockIdx.x) + 1] - bt.prefix[find_job(bt, blockIdx.x)];
   const int S = J.nshell;
+  const bool hess = MODE == 1;
+  // MODE 1: the X tile first (1024-byte aligned), then the fused layout
+  const uint32_t raw = umma::smem_u32(fsm);
+  const uint32_t xoff = hess ? ((1024u - (raw & 1023u)) & 1023u) : 0u;
+  const int xrows = fuse_x_rows(S);
+  uint32_t* xt = reinterpret_cast<uint32_t*>(reinterpret_cast<uint8_t*>(fsm) + xoff);
+  float* stg = hess ? reinterpret_cast<float*>(xt + 32 * xrows) : reinterpret_cast<float*>(fsm);
   // stage k: high plane at stg + 2 k S kFuseSP, low plane S kFuseSP after it
-  float* stg = reinterpret_cast<float*>(fsm);
   const int plane = S * kFuseSP;
   float2* xv = reinterpret_cast<float2*>(stg + 4 * plane);
   float2* dcv = xv + S;
@@ -434,11 +489,11 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_fused_ff(Batch bt, in
   int* act = reinterpret_cast<int*>(red + 2 * kFuseWarps + 2);
   int* pos = act + S;
   int* aoff = pos + S;  // atom a's active rows: [aoff[a], aoff[a + 1]) (act is ordered by shell)
+  uint64_t* mbar = reinterpret_cast<uint64_t*>((reinterpret_cast<uintptr_t>(aoff + S + 2) + 15) & ~uintptr_t(15));
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(mbar + 1);
+  __shared__ volatile int timed_out;
   const float2 cutp = split2(J.density_cutoff), negp = split2(J.negative_cutoff);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int p0 = tile * J.tile_points;
-  const int p1 = min(p0 + J.tile_points, J.npoint);
-  const int nsub = (p1 - p0 + kFuseSP - 1) / kFuseSP;
   const bool vec = (J.npoint & 3) == 0;
   const float* __restrict__ g32 = J.gmat32;
   const float* __restrict__ glo = J.gmat_lo;
@@ -448,177 +503,303 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_fused_ff(Batch bt, in
   const double* __restrict__ wp = J.w;
   float2* r0fo = J.r0f;
   float2* d2fo = J.d2f;
-  float* hso = J.hess_s;
   const int natom = J.natom;
-  const int nact = load_active(J, tile, act, pos);
-  __syncthreads();
-  fuse_load(g32, glo, NN, p0, p1, stg, stg + plane, vec, act, nact);
-  cp_async_commit();
-  if (MODE == 1)
-    for (int a = threadIdx.x; a <= J.natom; a += kFuseThreads) {
-      const int s0 = J.shell_off[a];
-      int lo = 0, hi = nact;  // first active row with shell >= s0
-      while (lo < hi) {
-        const int mid = (lo + hi) >> 1;
-        if (act[mid] < s0) lo = mid + 1;
-        else hi = mid;
-      }
-      aoff[a] = lo;
+  const int n1 = (S + 15) / 16 * 16;
+  const int c2 = (n1 + 31) / 32 * 32;
+  const bool has_d2 = n1 > umma::kTcM;
+  const uint32_t bar = umma::smem_u32(mbar);
+  uint32_t tmem = 0;
+  int nmma = 0;  // sub-tiles whose MMAs have been issued (= commits on bar)
+  if (hess) {
+    if (warp == 0) {
+      asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                       umma::smem_u32(tmem_slot)),
+                   "r"(kFuseTmemCols));
+      asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
+    if (threadIdx.x == 0) {
+      umma::mbar_init(bar, 1);
+      timed_out = 0;
+      asm volatile("fence.mbarrier_init.release.cluster;");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    tmem = *tmem_slot;
+  }
+  // The MMAs of the X tile as it stands (thread 0; after a block barrier
+  // that follows the writers' proxy fences).
+  auto issue_mma = [&]() {
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    const uint32_t xa = umma::smem_u32(xt);
+    const uint32_t id1 = umma::idesc_tf32(n1);
+    const uint32_t id2 = umma::idesc_tf32(has_d2 ? n1 - umma::kTcM : 16);
+#pragma unroll
+    for (int kk = 0; kk < kFuseSP / 8; ++kk) {
+      const uint32_t acc = (nmma > 0 || kk > 0) ? 1u : 0u;
+      umma::umma_tf32(tmem, umma::umma_desc(xa + 32 * kk), umma::umma_desc(xa + 32 * kk), id1, acc);
+      if (has_d2)
+        umma::umma_tf32(tmem + (uint32_t)c2, umma::umma_desc(xa + (n1 - umma::kTcM) * 128 + 32 * kk),
+                        umma::umma_desc(xa + umma::kTcM * 128 + 32 * kk), id2, acc);
+    }
+    umma::umma_commit(bar);
+  };
+  // Every thread: the MMAs of the last issued sub-tile have read the X tile.
+  auto wait_mma = [&]() {
+    if (nmma > 0 && !timed_out && !umma::mbar_wait(bar, (uint32_t)((nmma - 1) & 1))) timed_out = 1;
+  };
+  if (MODE == 1 && threadIdx.x < 64) tab[threadIdx.x] = c_exp2_gl[threadIdx.x];
   const double* x = MODE ? J.propars : J.delta;
   for (int i = threadIdx.x; i < S; i += kFuseThreads) xv[i] = split2(x[i]);
   const bool chg = MODE == 1 && with_change;
   if (chg)
     for (int i = threadIdx.x; i < S; i += kFuseThreads) dcv[i] = split2(J.propars[i] - J.propars_old[i]);
-  float ch = 0.0f, cl = 0.0f;  // change terms of this thread (float pair)
-  if (MODE == 1 && threadIdx.x < 64) tab[threadIdx.x] = c_exp2_gl[threadIdx.x];
-  Dot2 acc[kFuseRows];
+
+  for (int tile = local; tile < J.ntile; tile += nblk_job) {
+    const int p0 = tile * J.tile_points;
+    const int p1 = min(p0 + J.tile_points, J.npoint);
+    const int nsub = (p1 - p0 + kFuseSP - 1) / kFuseSP;
+    if (hess) {
+      wait_mma();  // the previous tile's last MMAs have read the X tile
+      for (int e = threadIdx.x; e < 32 * xrows; e += kFuseThreads) xt[e] = 0u;  // inactive rows
+    }
+    __syncthreads();  // shared state of the previous tile no longer in use
+    const int nact = load_active(J, tile, act, pos);
+    __syncthreads();
+    fuse_load(g32, glo, NN, p0, p1, stg, stg + plane, vec, act, nact);
+    cp_async_commit();
+    if (MODE == 1)
+      for (int a = threadIdx.x; a <= J.natom; a += kFuseThreads) {
+        const int s0 = J.shell_off[a];
+        int lo = 0, hi = nact;  // first active row with shell >= s0
+        while (lo < hi) {
+          const int mid = (lo + hi) >> 1;
+          if (act[mid] < s0) lo = mid + 1;
+          else hi = mid;
+        }
+        aoff[a] = lo;
+      }
+    float ch = 0.0f, cl = 0.0f;  // change terms of this thread (float pair)
+    Dot2 acc[kFuseRows];
 #pragma unroll
-  for (int r = 0; r < kFuseRows; ++r) acc[r] = Dot2{0.f, 0.f};
-  f2 ent{0.f, 0.f};
-  float nneg = 0.0f;
-  for (int sub = 0; sub < nsub; ++sub) {
-    const float* gh = stg + (sub & 1) * 2 * plane;
-    const float* gl = gh + plane;
-    cp_async_wait<0>();
-    __syncthreads();  // sub-tile sub visible; every thread is done with sub - 1
-    // per-point inputs of A' and C, loaded before phase A so that their
-    // latency overlaps it
-    const int pq = p0 + sub * kFuseSP + lane;
-    float wf = 0.0f;
-    float4 qpre = make_float4(0.f, 0.f, 0.f, 0.f);  // MODE 1: (w rho) and rho pairs; MODE 0: d2 pair
-    if (pq < p1) {
-      if (MODE == 1) qpre = wrfp[pq];
-      else {
-        const float2 d2 = d2in[pq];
-        qpre = make_float4(d2.x, d2.y, 0.f, 0.f);
+    for (int r = 0; r < kFuseRows; ++r) acc[r] = Dot2{0.f, 0.f};
+    f2 ent{0.f, 0.f};
+    float nneg = 0.0f;
+    for (int sub = 0; sub < nsub; ++sub) {
+      const float* gh = stg + (sub & 1) * 2 * plane;
+      const float* gl = gh + plane;
+      cp_async_wait<0>();
+      __syncthreads();  // sub-tile sub visible; every thread is done with sub - 1
+      if (hess && sub > 0) {  // X of sub - 1 is complete: its MMAs
+        if (threadIdx.x == 0 && !timed_out) issue_mma();
+        ++nmma;
       }
-      if (chg) wf = (float)wp[pq];
-    }
-    if (sub + 1 < nsub) {
-      float* nh = stg + ((sub + 1) & 1) * 2 * plane;  // last read in B of sub - 1
-      fuse_load(g32, glo, NN, p0 + (sub + 1) * kFuseSP, p1, nh, nh + plane, vec, act, nact);
-      cp_async_commit();
-    }
-    {  // A (active rows i = warp mod 8)
-      Dot2 d{0.f, 0.f}, e{0.f, 0.f};
-      int i = warp;
-      for (; i + kFuseWarps < nact; i += 2 * kFuseWarps) {
-        const float2 x1 = xv[act[i]], x2 = xv[act[i + kFuseWarps]];
-        dot2_add(d, gh[i * kFuseSP + lane], gl[i * kFuseSP + lane], x1.x, x1.y);
-        const int i2 = i + kFuseWarps;
-        dot2_add(e, gh[i2 * kFuseSP + lane], gl[i2 * kFuseSP + lane], x2.x, x2.y);
+      // per-point inputs of A' and C, loaded before phase A so that their
+      // latency overlaps it
+      const int pq = p0 + sub * kFuseSP + lane;
+      float wf = 0.0f;
+      float4 qpre = make_float4(0.f, 0.f, 0.f, 0.f);  // MODE 1: (w rho) and rho pairs; MODE 0: d2 pair
+      if (pq < p1) {
+        if (MODE == 1) qpre = wrfp[pq];
+        else {
+          const float2 d2 = d2in[pq];
+          qpre = make_float4(d2.x, d2.y, 0.f, 0.f);
+        }
+        if (chg) wf = (float)wp[pq];
       }
-      if (i < nact) {
-        const float2 x1 = xv[act[i]];
-        dot2_add(d, gh[i * kFuseSP + lane], gl[i * kFuseSP + lane], x1.x, x1.y);
+      if (sub + 1 < nsub) {
+        float* nh = stg + ((sub + 1) & 1) * 2 * plane;  // last read in B of sub - 1
+        fuse_load(g32, glo, NN, p0 + (sub + 1) * kFuseSP, p1, nh, nh + plane, vec, act, nact);
+        cp_async_commit();
       }
-      dot2_merge(d, e);
-      part[warp * kFuseSP + lane] = d;
-    }
-    __syncthreads();  // partial sums visible
-    // A': every warp merges the eight partial sums (the same fixed order) and
-    // forms v for the sub-tile's points itself; warp sub % 8 (the owner) also
-    // writes the per-point outputs and, MODE 1, the entropy terms
-    Dot2 du = part[lane];
+      {  // A (active rows i = warp mod 8)
+        Dot2 d{0.f, 0.f}, e{0.f, 0.f};
+        int i = warp;
+        for (; i + kFuseWarps < nact; i += 2 * kFuseWarps) {
+          const float2 x1 = xv[act[i]], x2 = xv[act[i + kFuseWarps]];
+          dot2_add(d, gh[i * kFuseSP + lane], gl[i * kFuseSP + lane], x1.x, x1.y);
+          const int i2 = i + kFuseWarps;
+          dot2_add(e, gh[i2 * kFuseSP + lane], gl[i2 * kFuseSP + lane], x2.x, x2.y);
+        }
+        if (i < nact) {
+          const float2 x1 = xv[act[i]];
+          dot2_add(d, gh[i * kFuseSP + lane], gl[i * kFuseSP + lane], x1.x, x1.y);
+        }
+        dot2_merge(d, e);
+        part[warp * kFuseSP + lane] = d;
+      }
+      __syncthreads();  // partial sums visible
+      // A': every warp merges the eight partial sums (the same fixed order) and
+      // forms v for the sub-tile's points itself; warp sub % 8 (the owner) also
+      // writes the per-point outputs and, MODE 1, the entropy terms
+      Dot2 du = part[lane];
 #pragma unroll
-    for (int q = 1; q < kFuseWarps; ++q) dot2_merge(du, part[q * kFuseSP + lane]);
-    const int p = p0 + sub * kFuseSP + lane;
-    const bool owner = warp == (sub & (kFuseWarps - 1));
-    f2 v{0.f, 0.f};
-    if (p < p1) {
-      if (MODE == 0) {
-        v = ffa::mul(dot2_ff(du), f2{qpre.x, qpre.y});
-      } else {
-        const f2 r0 = dot2_ff(du);
-        const float4 q = qpre;  // (w rho) and rho as float pairs
-        const bool sick = below(f2{q.z, q.w}, cutp) || below(r0, cutp);
-        if (!sick) v = ffa::div(f2{q.x, q.y}, r0);
-        if (owner) {
-          const f2 dd = sick ? f2{0.f, 0.f} : ffa::div(v, r0);
-          r0fo[p] = make_float2(r0.hi, r0.lo);
-          d2fo[p] = make_float2(dd.hi, dd.lo);
-          hso[p] = sqrtf(dd.hi);
-          if (below(r0, negp)) nneg += 1.0f;
-          if (!sick) {  // w rho ln(rho / rho0)
-            const f2 ratio = ffa::div(f2{q.z, q.w}, r0);
-            const float l0 = logf(ratio.hi);
-            const f2 e = ffa::exp_ff(f2{-l0, 0.f}, tab);
-            const f2 l = ffa::add(ffa::add(ffa::mul(ratio, e), -1.0f), l0);
-            ent = ffa::add(ent, ffa::mul(f2{q.x, q.y}, l));
+      for (int q = 1; q < kFuseWarps; ++q) dot2_merge(du, part[q * kFuseSP + lane]);
+      const int p = p0 + sub * kFuseSP + lane;
+      const bool owner = warp == (sub & (kFuseWarps - 1));
+      f2 v{0.f, 0.f};
+      float sx = 0.0f;  // MODE 1: s(p) = sqrt(w rho) / rho0 for X
+      if (p < p1) {
+        if (MODE == 0) {
+          v = ffa::mul(dot2_ff(du), f2{qpre.x, qpre.y});
+        } else {
+          const f2 r0 = dot2_ff(du);
+          const float4 q = qpre;  // (w rho) and rho as float pairs
+          const bool sick = below(f2{q.z, q.w}, cutp) || below(r0, cutp);
+          if (!sick) {
+            v = ffa::div(f2{q.x, q.y}, r0);
+            sx = sqrtf(q.x) / r0.hi;
+          }
+          if (owner) {
+            const f2 dd = sick ? f2{0.f, 0.f} : ffa::div(v, r0);
+            r0fo[p] = make_float2(r0.hi, r0.lo);
+            d2fo[p] = make_float2(dd.hi, dd.lo);
+            if (below(r0, negp)) nneg += 1.0f;
+            if (!sick) {  // w rho ln(rho / rho0)
+              const f2 ratio = ffa::div(f2{q.z, q.w}, r0);
+              const float l0 = logf(ratio.hi);
+              const f2 e = ffa::exp_ff(f2{-l0, 0.f}, tab);
+              const f2 l = ffa::add(ffa::add(ffa::mul(ratio, e), -1.0f), l0);
+              ent = ffa::add(ent, ffa::mul(f2{q.x, q.y}, l));
+            }
           }
         }
       }
-    }
-    {  // B (active rows i = warp + 8 r)
+      if (hess) {  // X rows of the active shells i = warp + 8 r, column lane
+        wait_mma();  // the MMAs of sub - 1 have read the X tile
+        const uint32_t sw = (uint32_t)(lane & 3);
+        for (int i = warp; i < nact; i += kFuseWarps) {
+          const int m = act[i];
+          const uint32_t off = (uint32_t)(m * 32) + ((((uint32_t)lane >> 2) ^ (uint32_t)(m & 7)) << 2) + sw;
+          xt[off] = umma::to_tf32_rn(gh[i * kFuseSP + lane] * sx);
+        }
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      }
+      {  // B (active rows i = warp + 8 r)
 #pragma unroll
-      for (int r = 0; r < kFuseRows; ++r) {
-        const int i = warp + kFuseWarps * r;
-        if (i < nact) dot2_add(acc[r], gh[i * kFuseSP + lane], gl[i * kFuseSP + lane], v.hi, v.lo);
+        for (int r = 0; r < kFuseRows; ++r) {
+          const int i = warp + kFuseWarps * r;
+          if (i < nact) dot2_add(acc[r], gh[i * kFuseSP + lane], gl[i * kFuseSP + lane], v.hi, v.lo);
+        }
+      }
+      if (chg) {  // C (atoms with no active row add exact zeros: skipped)
+        for (int a = warp; a < natom; a += kFuseWarps) {
+          const int i0 = aoff[a], i1 = aoff[a + 1];
+          if (i0 == i1) continue;
+          float dv = 0.0f;
+          for (int i = i0; i < i1; ++i) dv = fmaf(gh[i * kFuseSP + lane], dcv[act[i]].x, dv);
+          const float term = wf * dv * dv;
+          const float t = ch + term;
+          const float bb = t - ch;
+          cl += (ch - (t - bb)) + (term - bb);
+          ch = t;
+        }
       }
     }
-    if (chg) {  // C (atoms with no active row add exact zeros: skipped)
-      for (int a = warp; a < natom; a += kFuseWarps) {
-        const int i0 = aoff[a], i1 = aoff[a + 1];
-        if (i0 == i1) continue;
-        float dv = 0.0f;
-        for (int i = i0; i < i1; ++i) dv = fmaf(gh[i * kFuseSP + lane], dcv[act[i]].x, dv);
-        const float term = wf * dv * dv;
-        const float t = ch + term;
-        const float bb = t - ch;
-        cl += (ch - (t - bb)) + (term - bb);
-        ch = t;
+    if (hess) {  // the tile's last sub-tile
+      __syncthreads();
+      if (threadIdx.x == 0 && !timed_out) issue_mma();
+      ++nmma;
+    }
+#pragma unroll
+    for (int r = 0; r < kFuseRows; ++r) {
+      const int i = warp + kFuseWarps * r;
+      if (i < nact) {  // warp-uniform
+        Dot2 d = acc[r];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+          const Dot2 b{__shfl_xor_sync(0xffffffffu, d.s, o), __shfl_xor_sync(0xffffffffu, d.c, o)};
+          dot2_merge(d, b);
+        }
+        if (lane == 0) J.gpart[(size_t)act[i] * J.ntile + tile] = dot2_value(d);
       }
     }
-  }
-#pragma unroll
-  for (int r = 0; r < kFuseRows; ++r) {
-    const int i = warp + kFuseWarps * r;
-    if (i < nact) {  // warp-uniform
-      Dot2 d = acc[r];
+    zero_inactive(J, tile, pos);
+    if (MODE == 1) {
+      // entropy and negativity partials of the tile
+      double e = ffa::to_double(ent), n = (double)nneg;
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) {
-        const Dot2 b{__shfl_xor_sync(0xffffffffu, d.s, o), __shfl_xor_sync(0xffffffffu, d.c, o)};
-        dot2_merge(d, b);
+        e += __shfl_xor_sync(0xffffffffu, e, o);
+        n += __shfl_xor_sync(0xffffffffu, n, o);
       }
-      if (lane == 0) J.gpart[(size_t)act[i] * J.ntile + tile] = dot2_value(d);
+      if (lane == 0) {
+        red[2 * warp] = e;
+        red[2 * warp + 1] = n;
+      }
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        double se = 0.0, sn = 0.0;
+        for (int k = 0; k < kFuseWarps; ++k) {
+          se += red[2 * k];
+          sn += red[2 * k + 1];
+        }
+        J.jpart[(size_t)QJ_ENTROPY * J.ntile + tile] = se;
+        J.jpart[(size_t)QJ_NEG * J.ntile + tile] = sn;
+      }
+      if (chg) {
+        double c = (double)ch + (double)cl;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+        __syncthreads();  // red is reused
+        if (lane == 0) red[warp] = c;
+        __syncthreads();
+        double sc = 0.0;
+        for (int k = 0; k < kFuseWarps; ++k) sc += red[k];
+        for (int a = threadIdx.x; a < J.natom; a += kFuseThreads)
+          J.apart[((size_t)a * J.qa + QA_CHANGE) * J.ntile + tile] = a == 0 ? sc : 0.0;
+      }
     }
   }
-  zero_inactive(J, tile, pos);
-  if (MODE == 1) {
-    // entropy and negativity partials of the tile
-    double e = ffa::to_double(ent), n = (double)nneg;
+  if (!hess) return;
+  // Epilogue: the block's Hessian partial from tensor memory. Warp w reads
+  // lanes 32 (w % 4) .. + 31; warps w and w + 4 take alternate 8-column chunks.
+  wait_mma();  // the last commit covers every MMA of the block
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  __syncthreads();
+  const bool ok = nmma > 0 && !timed_out;
+  float* out = reinterpret_cast<float*>(J.hpart) + (size_t)local * (S * (S + 1) / 2);
+  const int quad = warp & 3;
+  for (int part2 = 0; part2 < (has_d2 ? 2 : 1); ++part2) {
+    const int ncols = part2 == 0 ? n1 : n1 - umma::kTcM;
+    const int col0 = part2 == 0 ? 0 : c2;
+    const int row = part2 == 0 ? quad * 32 + lane : n1 - umma::kTcM + quad * 32 + lane;  // row of H
+    for (int c = 8 * (warp >> 2); c < ncols; c += 16) {
+      uint32_t vv[8];
+      if (ok) {
+        const uint32_t taddr = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(col0 + c);
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+            : "=r"(vv[0]), "=r"(vv[1]), "=r"(vv[2]), "=r"(vv[3]), "=r"(vv[4]), "=r"(vv[5]),
+              "=r"(vv[6]), "=r"(vv[7])
+            : "r"(taddr));
+        asm volatile("tcgen05.wait::ld.sync.aligned;");
+      } else {
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      e += __shfl_xor_sync(0xffffffffu, e, o);
-      n += __shfl_xor_sync(0xffffffffu, n, o);
-    }
-    if (lane == 0) {
-      red[2 * warp] = e;
-      red[2 * warp + 1] = n;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      double se = 0.0, sn = 0.0;
-      for (int k = 0; k < kFuseWarps; ++k) {
-        se += red[2 * k];
-        sn += red[2 * k + 1];
+        for (int q = 0; q < 8; ++q) vv[q] = 0u;
       }
-      J.jpart[(size_t)QJ_ENTROPY * J.ntile + tile] = se;
-      J.jpart[(size_t)QJ_NEG * J.ntile + tile] = sn;
-    }
-    if (chg) {
-      double c = (double)ch + (double)cl;
 #pragma unroll
-      for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
-      __syncthreads();  // red is reused
-      if (lane == 0) red[warp] = c;
-      __syncthreads();
-      double sc = 0.0;
-      for (int k = 0; k < kFuseWarps; ++k) sc += red[k];
-      for (int a = threadIdx.x; a < J.natom; a += kFuseThreads)
-        J.apart[((size_t)a * J.qa + QA_CHANGE) * J.ntile + tile] = a == 0 ? sc : 0.0;
+      for (int q = 0; q < 8; ++q) {
+        const float h = __uint_as_float(vv[q]);
+        if (part2 == 0) {
+          const int i = row, j = c + q;  // D1: H[i][j], i < 128
+          if (i < S && j < S) {
+            if (j <= i) out[i * (i + 1) / 2 + j] = h;
+            else if (j >= umma::kTcM) out[j * (j + 1) / 2 + i] = h;  // H[j][i], j below row 128
+          }
+        } else {
+          const int i = row, j = umma::kTcM + c + q;  // D2: H[i][j], i, j >= 128
+          if (i >= umma::kTcM && i < S && j <= i) out[i * (i + 1) / 2 + j] = h;
+        }
+      }
     }
+  }
+  if (timed_out && threadIdx.x == 0) atomicOr(&J.mail->i[MI_ERR], E_TIMEOUT);
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                 "r"(kFuseTmemCols));
   }
 }
 
@@ -634,6 +815,7 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_trials_fused(Batch bt
   extern __shared__ float4 fsm[];
   int tile;
   const JobDev& J = decode_local_gf(bt, tile);
+  if (glisa_idle(J)) return;
   if (!J.fuse) return;
   const int S = J.nshell;
   float* stg = reinterpret_cast<float*>(fsm);
@@ -767,6 +949,7 @@ __global__ void __launch_bounds__(kThreads) k_glisa_change_ff(Batch bt) {
   __shared__ double red[kWarps];
   int tile;
   const JobDev& J = decode_local_gf(bt, tile);
+  if (glisa_idle(J)) return;
   for (int i = threadIdx.x; i < J.nshell; i += kThreads) dc[i] = split2(J.propars[i] - J.propars_old[i]);
   __syncthreads();
   const size_t N = J.npoint;
@@ -893,7 +1076,7 @@ void ensure_exp_table_gl() {
   cudaFuncSetAttribute(k_glisa_fused_ff<0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)fuse_smem_bytes(kFuseMaxShells));
   cudaFuncSetAttribute(k_glisa_fused_ff<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       (int)fuse_smem_bytes(kFuseMaxShells));
+                       (int)fuse_hess_smem_bytes(kFuseMaxShells));
   cudaFuncSetAttribute(k_glisa_trials_fused, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)fuse_smem_bytes(kFuseMaxShells));
   if (dev < 31) done_mask |= 1 << dev;
@@ -903,13 +1086,14 @@ void ensure_exp_table_gl() {
 
 void launch_glisa_fused_ff(const HostBatch& hb, cudaStream_t st, int mode, int max_shells,
                            int with_change) {
-  if (hb.blocks[K_POINT] <= 0) return;
+  if (hb.blocks[K_FUSE] <= 0) return;
   ensure_exp_table_gl();
-  const size_t smem = fuse_smem_bytes(max_shells);
   if (mode)
-    k_glisa_fused_ff<1><<<hb.blocks[K_POINT], kFuseThreads, smem, st>>>(hb.b[K_POINT], with_change);
+    k_glisa_fused_ff<1><<<hb.blocks[K_FUSE], kFuseThreads, fuse_hess_smem_bytes(max_shells), st>>>(
+        hb.b[K_FUSE], with_change);
   else
-    k_glisa_fused_ff<0><<<hb.blocks[K_POINT], kFuseThreads, smem, st>>>(hb.b[K_POINT], 0);
+    k_glisa_fused_ff<0><<<hb.blocks[K_FUSE], kFuseThreads, fuse_smem_bytes(max_shells), st>>>(
+        hb.b[K_FUSE], 0);
   ++g_launch_count;
 }
 

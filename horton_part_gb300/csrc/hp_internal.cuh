@@ -66,6 +66,7 @@ enum MailI {
   MI_WARN = 3,        // warning bits (HP_WARN_*)
   MI_CONVERGED = 4,   // gLISA solver converged flag
   MI_F64_FACTORS = 5, // gLISA Newton steps of a tensor-core job factored in FP64
+  MI_DONE = 6,        // gLISA: finished (converged, failed or out of iterations)
   MI_COUNT = 8
 };
 struct Mailbox {
@@ -208,8 +209,17 @@ struct JobDev {
 // 100 x the threshold) refine it once against the exact product H delta.
 // Read from the job's mailbox, which only the end of a step writes, so every
 // kernel of a step sees the same answer.
+__device__ __forceinline__ bool glisa_idle(const JobDev& J);
 __device__ __forceinline__ bool glisa_refine_now(const JobDev& J) {
   return J.refine && J.mail->i[MI_ITER] > 0 && J.mail->d[MD_CHANGE] < 100.0 * J.threshold;
+}
+
+// gLISA jobs advance several solver iterations per host round trip:
+// k_outer_finish marks a job finished (converged, failed or out of
+// iterations) in MI_DONE, and every kernel of a gLISA step returns at once
+// for such a job, so the iterations queued after its last one do nothing.
+__device__ __forceinline__ bool glisa_idle(const JobDev& J) {
+  return J.scheme == SCHEME_GLISA && J.mail->i[MI_DONE] != 0;
 }
 
 
@@ -400,8 +410,14 @@ enum Kind {
   K_JOB = 3,        // one block per job
   K_HESS = 4,       // gLISA Hessian: (tile pair, point split)
   K_SQUARE = 5,     // gLISA reduce: ceil(nshell^2 / kThreads)
-  K_NKIND = 7
+  K_FUSE = 7,       // fused gLISA pass: min(ntile, kFuseCtas) persistent blocks per job
+  K_NKIND = 8
 };
+
+// Persistent blocks of the fused gLISA pass per job (two per SM): each
+// accumulates the Hessian of its point tiles in tensor memory and writes one
+// partial, so a fused job has nsplit = min(ntile, kFuseCtas) partials.
+constexpr int kFuseCtas = 2 * 152;
 
 struct HostBatch {
   Batch b[K_NKIND];

@@ -179,6 +179,7 @@ __global__ void k_init_params(Batch bt) {
 __global__ void k_copy_old(Batch bt) {
   int local;
   const JobDev& J = decode_local(bt, local);
+  if (glisa_idle(J)) return;
   for (int i = threadIdx.x; i < J.nparam; i += blockDim.x) J.propars_old[i] = J.propars[i];
   if (J.fuse)  // entropy and negativity partials of the parameters the step starts from
     for (int t = threadIdx.x; t < J.ntile; t += blockDim.x) {
@@ -300,6 +301,7 @@ __global__ void __launch_bounds__(kFinishThreads) k_outer_finish(Batch bt, int w
   __shared__ double change_s;
   int local;
   const JobDev& J = decode_local(bt, local);
+  if (glisa_idle(J)) return;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
   const int it = J.mail->i[MI_ITER];
   for (int a = warp; a < J.natom; a += nw) {
@@ -337,6 +339,11 @@ __global__ void __launch_bounds__(kFinishThreads) k_outer_finish(Batch bt, int w
       J.hist_chg[it] = change_s;
     }
     J.mail->i[MI_ITER] = it + 1;
+    // gLISA: the host's end-of-step tests (error, converged, out of
+    // iterations), made here so that queued iterations skip a finished job
+    if (J.scheme == SCHEME_GLISA &&
+        (J.mail->i[MI_ERR] != 0 || change_s < J.threshold || it + 1 >= J.maxiter))
+      J.mail->i[MI_DONE] = 1;
   }
 }
 
@@ -1169,6 +1176,7 @@ __global__ void __launch_bounds__(kThreads) k_glisa_pro(Batch bt) {
   __shared__ double out[2];
   int tile;
   const JobDev& J = decode_local(bt, tile);
+  if (glisa_idle(J)) return;
   double acc[2] = {0.0, 0.0};
   for (int i = 0; i < J.ppt; ++i) {
     const int p = point_of(J, tile, i);
@@ -1201,6 +1209,7 @@ __global__ void __launch_bounds__(kThreads) k_glisa_pro(Batch bt) {
 __global__ void __launch_bounds__(kThreads) k_glisa_grad(Batch bt, int use_hvec) {
   int tile;
   const JobDev& J = decode_local(bt, tile);
+  if (glisa_idle(J)) return;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int p0 = tile * J.tile_points;
   const int p1 = min(p0 + J.tile_points, J.npoint);
@@ -1225,6 +1234,7 @@ __global__ void __launch_bounds__(kThreads) k_glisa_hess(Batch bt) {
   __shared__ double Bs[kHK][kHT + 1];
   int local;
   const JobDev& J = decode_local(bt, local);
+  if (glisa_idle(J)) return;
   const int npair = J.htiles * (J.htiles + 1) / 2;
   const int split = local / npair;
   int pr = local - split * npair;
@@ -1293,6 +1303,7 @@ constexpr int kReduceWarps = kReduceThreads / 32;
 __global__ void __launch_bounds__(kReduceThreads) k_glisa_reduce(Batch bt) {
   int local;
   const JobDev& J = decode_local(bt, local);
+  if (glisa_idle(J)) return;
   const int M = J.nshell;
   const int e = local * kReduceThreads + threadIdx.x;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -1688,6 +1699,7 @@ __global__ void __launch_bounds__(kNewtonThreads) k_glisa_newton_step(Batch bt, 
   __shared__ int fid[kNewtonF32Max];
   int local;
   const JobDev& J = decode_local(bt, local);
+  if (glisa_idle(J)) return;
   const int M = J.nshell;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   // free set in shell order: per-warp ballots and a prefix over the warps
@@ -1799,6 +1811,7 @@ __global__ void __launch_bounds__(kNewtonThreads) k_glisa_newton_step(Batch bt, 
 __global__ void __launch_bounds__(kThreads) k_glisa_hv(Batch bt) {
   int local;
   const JobDev& J = decode_local(bt, local);
+  if (glisa_idle(J)) return;
   const int p = local * kThreads + threadIdx.x;
   if (p >= J.npoint) return;
   double u = 0.0;
@@ -1814,6 +1827,7 @@ __global__ void __launch_bounds__(kThreads) k_glisa_hv(Batch bt) {
 __global__ void __launch_bounds__(kThreads) k_glisa_gsum(Batch bt) {
   int local;
   const JobDev& J = decode_local(bt, local);
+  if (glisa_idle(J)) return;
   if (!glisa_refine_now(J)) return;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int nblk = (J.nshell * J.nshell + kThreads - 1) / kThreads;  // this job's K_SQUARE blocks
@@ -1842,6 +1856,7 @@ __global__ void __launch_bounds__(kThreads) k_glisa_refine(Batch bt) {
   extern __shared__ double l_smem[];
   int local;
   const JobDev& J = decode_local(bt, local);
+  if (glisa_idle(J)) return;
   if (!glisa_refine_now(J)) return;
   const int M = J.nshell;
   const int nf = J.freeidx[M];
@@ -1881,6 +1896,7 @@ constexpr int kTrialSetSmem = 2048;  // shells whose clip steps are sorted in sh
 __global__ void __launch_bounds__(kThreads) k_glisa_trial_set(Batch bt) {
   int local;
   const JobDev& J = decode_local(bt, local);
+  if (glisa_idle(J)) return;
   const int M = J.nshell;
   for (int e = threadIdx.x; e < kTrials * M; e += kThreads) {
     const int t = e / M, m = e - t * M;
@@ -2058,6 +2074,7 @@ __global__ void k_glisa_ls_pick(Batch bt, int first, int count) {
 __global__ void k_glisa_apply(Batch bt, int mode) {
   int local;
   const JobDev& J = decode_local(bt, local);
+  if (glisa_idle(J)) return;
   for (int m = threadIdx.x; m < J.nshell; m += blockDim.x) {
     if (mode == 0) J.propars[m] = J.propars[m] + J.delta[m];
     else J.propars[m] = J.propars[m] * (-J.grad[m]);
@@ -2070,6 +2087,7 @@ __global__ void __launch_bounds__(kThreads) k_glisa_change(Batch bt) {
   const JobDev* Jp;
   const AtomTile at = decode_atom_tile(bt, Jp);
   const JobDev& J = *Jp;
+  if (glisa_idle(J)) return;
   const int s0 = J.shell_off[at.atom], s1 = J.shell_off[at.atom + 1];
   double acc = 0.0;
   for (int i = 0; i < J.ppt; ++i) {
@@ -2134,6 +2152,7 @@ __global__ void __launch_bounds__(kThreads) k_glisa_trials(Batch bt) {
   __shared__ double out[kTrials];
   int tile;
   const JobDev& J = decode_local(bt, tile);
+  if (glisa_idle(J)) return;
   float ah[kTrials], al[kTrials];
 #pragma unroll
   for (int t = 0; t < kTrials; ++t) ah[t] = al[t] = 0.0f;
@@ -2204,6 +2223,7 @@ __global__ void __launch_bounds__(32 * kTrials) k_glisa_trial_pick(Batch bt) {
   __shared__ int pick_s;
   int local;
   const JobDev& J = decode_local(bt, local);
+  if (glisa_idle(J)) return;
   const int lane = threadIdx.x & 31, t = threadIdx.x >> 5;
   const int M = J.nshell;
   double c0 = 0.0;

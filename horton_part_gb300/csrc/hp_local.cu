@@ -263,6 +263,7 @@ __global__ void __launch_bounds__(kThreads) k_change_radial(Batch bt) {
   __shared__ double red[kWarps];
   int a;
   const JobDev& J = decode_atom_lc(bt, a);
+  if (glisa_idle(J)) return;
   const int r0 = J.rad_off[a], nrad = J.rad_off[a + 1] - r0;
   const int s0 = J.shell_off[a], nsh = J.shell_off[a + 1] - s0;
   const double* pn = J.propars + J.par_off[a];

@@ -94,6 +94,7 @@ struct hp_job {
   double prev_change = 1e300;
   int polish_iters = 0;  // outer iterations of a mixed job after its FP32 phase (FF or FP64)
   int f64_factors = 0;   // tensor-core gLISA: Newton steps factored in FP64
+  int64_t g_active = -1; // fused gLISA: G values in the tiles' active rows (-1: not read yet)
   std::vector<double> changes;  // outer changes of this run
 };
 
@@ -177,8 +178,9 @@ int blocks_for(const JobDev& J, int kind) {
     case K_ATOM_TILE: return J.natom * J.ntile;
     case K_ATOM: return J.natom;
     case K_JOB: return 1;
+    case K_FUSE: return J.fuse ? std::min(J.ntile, kFuseCtas) : 0;
     case K_HESS:
-      if (J.scheme != SCHEME_GLISA) return 0;
+      if (J.scheme != SCHEME_GLISA || J.fuse) return 0;  // fused jobs: in the fused pass
       return J.tc ? tc_hess_blocks(J) : J.nsplit * J.htiles * (J.htiles + 1) / 2;
     case K_SQUARE: return J.scheme == SCHEME_GLISA ? (J.nshell * J.nshell + kThreads - 1) / kThreads : 0;
   }
@@ -424,22 +426,30 @@ int step_iterstock(hp_ctx* ctx, const std::vector<hp_job*>& jobs, const HostBatc
 // ~1e-6; one step brings it to ~1e-12.
 constexpr int kRefineSteps = 1;
 
-// One gLISA solver iteration (glisa.py:748-798 for Newton, 805-848 for SC).
-int step_glisa(hp_ctx* ctx, const std::vector<hp_job*>& jobs, const HostBatch& hb) {
+// Up to `iters` gLISA solver iterations (glisa.py:748-798 for Newton,
+// 805-848 for SC) queued back to back, then one host round trip. The device
+// marks a job finished at the end of the iteration that converges, fails or
+// reaches maxiter (MI_DONE, k_outer_finish), and the kernels of the queued
+// iterations after it return at once for that job, so the results are those
+// of one iteration per round trip. The m-newton line search needs the host
+// between iterations (its retry pass), so it takes one iteration per call.
+int step_glisa(hp_ctx* ctx, const std::vector<hp_job*>& jobs, const HostBatch& hb, int iters) {
   cudaStream_t st = ctx->stream;
   const int solver = jobs[0]->dev.solver;
-  launch_copy_old(hb, st);
+  if (solver == SOLVER_M_NEWTON) iters = 1;
   const bool tc = jobs[0]->dev.tc != 0;
   const int gff = jobs[0]->dev.gff;
   // Jobs with at most kFuseMaxShells shells (batches are homogeneous in
-  // this) take the fused passes: the promolecule + gradient pass of an
-  // iteration runs at the end of the previous step (or at job start) and also
-  // forms that step's change; the others take separate passes.
+  // this) take the fused passes: the promolecule + gradient (+ Hessian) pass
+  // of an iteration runs at the end of the previous step (or at job start)
+  // and also forms that step's change; the others take separate passes.
   const bool fused = jobs[0]->dev.fuse != 0;
   int fuse_shells = 0;
   for (hp_job* j : jobs) fuse_shells = std::max(fuse_shells, j->dev.nshell);
   if (!fused) fuse_shells = 0;
   const int unfused = fused ? 0 : 1;
+  for (int iter = 0; iter < iters; ++iter) {
+  launch_copy_old(hb, st);
   if (!fused) {
     ProfScope ps(ctx, HP_KERNEL_GLISA_PRO);
     if (gff) launch_glisa_pro_ff(hb, st);
@@ -450,7 +460,7 @@ int step_glisa(hp_ctx* ctx, const std::vector<hp_job*>& jobs, const HostBatch& h
     if (gff) launch_glisa_grad_ff(hb, st);
     else launch_glisa_grad(hb, st);
   }
-  if (solver != SOLVER_SC) {
+  if (solver != SOLVER_SC && !fused) {  // fused jobs: the Hessian comes with the fused pass
     ProfScope ps(ctx, HP_KERNEL_GLISA_HESS);
     if (tc) {
       int smax = 0, smin = 1 << 30;
@@ -465,16 +475,19 @@ int step_glisa(hp_ctx* ctx, const std::vector<hp_job*>& jobs, const HostBatch& h
   {
     ProfScope ps(ctx, HP_KERNEL_GLISA_SOLVE);
     launch_glisa_reduce(hb, st);
-    if (solver == SOLVER_SC) {
-      launch_glisa_apply(hb, st, 1);
-    } else {
+    if (solver != SOLVER_SC) {
       // Newton system with the FP64 Hessian, or with the tensor-core one plus
       // iterative refinement against the exact FP64 product H delta.
       launch_glisa_solve(hb, st, solver == SOLVER_PNEWTON ? 1 : 0);
       if (tc)
         for (int k = 0; k < kRefineSteps; ++k) launch_glisa_refine(hb, st, gff, fuse_shells, unfused);
     }
-    if (solver == SOLVER_PNEWTON) {
+  }
+  {
+    ProfScope ps(ctx, HP_KERNEL_GLISA_TRIALS);
+    if (solver == SOLVER_SC) {
+      launch_glisa_apply(hb, st, 1);
+    } else if (solver == SOLVER_PNEWTON) {
       launch_glisa_pnewton(hb, st, gff, fuse_shells);
     } else if (solver != SOLVER_SC) {
       if (solver == SOLVER_NEWTON) launch_glisa_apply(hb, st, 0);
@@ -533,6 +546,7 @@ int step_glisa(hp_ctx* ctx, const std::vector<hp_job*>& jobs, const HostBatch& h
     else launch_glisa_change(hb, st);
   }
   launch_outer_finish(hb, st, 0);
+  }  // queued iterations
   int rc = check_launch();
   if (rc) return rc;
   rc = read_mail(ctx);
@@ -541,10 +555,11 @@ int step_glisa(hp_ctx* ctx, const std::vector<hp_job*>& jobs, const HostBatch& h
   for (hp_job* j : jobs) {
     if (j->done) continue;
     const Mailbox& m = ctx->mail_host[j->slot];
+    const int before = j->niter;
     j->niter = m.i[MI_ITER];
     j->change = m.d[MD_CHANGE];
     j->f64_factors = m.i[MI_F64_FACTORS];
-    j->evals += 3.0 * (double)j->dev.npoint * (double)j->dev.natom;
+    j->evals += 3.0 * (double)j->dev.npoint * (double)j->dev.natom * (double)(j->niter - before);
     if (m.i[MI_ERR]) {
       j->status = status_of(m.i[MI_ERR]);
       g_err = err_text(m.i[MI_ERR]);
@@ -590,7 +605,7 @@ int step_glisa(hp_ctx* ctx, const std::vector<hp_job*>& jobs, const HostBatch& h
   return HP_OK;
 }
 
-int step_group(hp_ctx* ctx, const std::vector<hp_job*>& jobs) {
+int step_group(hp_ctx* ctx, const std::vector<hp_job*>& jobs, int iters) {
   // The pinned staging buffers are reused by every build_batch; each upload
   // is followed by a stream synchronisation before the next one.
   int rc;
@@ -608,7 +623,7 @@ int step_group(hp_ctx* ctx, const std::vector<hp_job*>& jobs) {
   HostBatch hb;
   rc = build_batch(ctx, jobs, hb);
   if (rc) return rc;
-  if (jobs[0]->desc.scheme == HP_SCHEME_GLISA) return step_glisa(ctx, jobs, hb);
+  if (jobs[0]->desc.scheme == HP_SCHEME_GLISA) return step_glisa(ctx, jobs, hb, iters);
   return step_iterstock(ctx, jobs, hb);
 }
 
@@ -687,6 +702,16 @@ int validate(const hp_job_desc* d) {
     if (d->shell_exponents[s] < 0.0) return fail(HP_ERR_INVALID, "alpha must be non-negative");
   }
   return HP_OK;
+}
+
+// Solver iterations queued per host round trip when running a job to the
+// end: gLISA Newton converges quadratically, so near the threshold two
+// iterations are queued, further away four (the iterations queued after the
+// last one cost a few empty launches each).
+int run_chunk(const hp_job* j) {
+  if (j->desc.scheme != HP_SCHEME_GLISA) return 1;
+  if (j->niter > 0 && j->change < 1e3 * j->desc.threshold) return 2;
+  return 4;
 }
 
 }  // namespace
@@ -835,6 +860,9 @@ int32_t hp_job_create(hp_ctx* ctx, const hp_job_desc* d, hp_job** out) {
     const int tiles = tc_hess_blocks(probe);
     nsplit = std::max(1, std::min((152 + tiles - 1) / tiles, (N + 255) / 256));
   }
+  // fused jobs form the Hessian inside the fused pass: one partial per block
+  const bool fuse_job = tc && solver != HP_SOLVER_M_NEWTON && S <= kGffMaxShells && S <= kFuseMaxShells;
+  if (fuse_job) nsplit = std::min(ntile, kFuseCtas);
 
   // carve one allocation
   struct Part { void** dst; size_t bytes; };
@@ -1136,7 +1164,8 @@ int32_t hp_job_destroy(hp_job* job) {
   return HP_OK;
 }
 
-int32_t hp_step(hp_ctx* ctx, hp_job* const* jobs, int32_t njobs, int32_t* n_live) {
+namespace {
+int step_jobs(hp_ctx* ctx, hp_job* const* jobs, int32_t njobs, int iters, int32_t* n_live) {
   if (!ctx || (njobs > 0 && !jobs)) return fail(HP_ERR_INVALID, "null argument");
   if (njobs > kMaxSlots) return fail(HP_ERR_INVALID, "too many jobs in one step");
   HP_CK(cudaSetDevice(ctx->device));
@@ -1160,7 +1189,7 @@ int32_t hp_step(hp_ctx* ctx, hp_job* const* jobs, int32_t njobs, int32_t* n_live
     if (!placed) groups.push_back({j});
   }
   for (auto& g : groups) {
-    int rc = step_group(ctx, g);
+    int rc = step_group(ctx, g, iters);
     if (rc) return rc;
   }
   int live = 0;
@@ -1169,12 +1198,24 @@ int32_t hp_step(hp_ctx* ctx, hp_job* const* jobs, int32_t njobs, int32_t* n_live
   if (n_live) *n_live = live;
   return HP_OK;
 }
+}  // namespace
+
+int32_t hp_step(hp_ctx* ctx, hp_job* const* jobs, int32_t njobs, int32_t* n_live) {
+  return step_jobs(ctx, jobs, njobs, 1, n_live);
+}
+
+int32_t hp_step_n(hp_ctx* ctx, hp_job* const* jobs, int32_t njobs, int32_t max_iterations,
+                  int32_t* n_live) {
+  if (max_iterations < 1 || max_iterations > 64)
+    return fail(HP_ERR_INVALID, "max_iterations must be 1..64");
+  return step_jobs(ctx, jobs, njobs, max_iterations, n_live);
+}
 
 int32_t hp_job_run(hp_ctx* ctx, hp_job* job) {
   if (!ctx || !job) return fail(HP_ERR_INVALID, "null argument");
   int32_t live = 1;
   while (!job->done) {
-    int rc = hp_step(ctx, &job, 1, &live);
+    int rc = step_jobs(ctx, &job, 1, run_chunk(job), &live);
     if (rc) return rc;
   }
   if (job->status != HP_OK) return fail(job->status, g_err.empty() ? "job failed" : g_err);
@@ -1255,6 +1296,21 @@ int32_t hp_job_info_get(hp_job* job, hp_job_info* out) {
   out->point_atom_evals = job->evals;
   out->polish_iterations = job->polish_iters;
   out->f64_factors = job->f64_factors;
+  if (job->g_active < 0 && job->initialized && job->dev.fuse && job->dev.gact) {
+    // per tile: active-row count at gact[tile][S]; times the tile's points
+    const JobDev& J = job->dev;
+    std::vector<int> g((size_t)(J.nshell + 1) * J.ntile);
+    HP_CK(cudaSetDevice(job->ctx->device));
+    HP_CK(cudaStreamSynchronize(job->ctx->stream));
+    HP_CK(cudaMemcpy(g.data(), J.gact, sizeof(int) * g.size(), cudaMemcpyDeviceToHost));
+    int64_t total = 0;
+    for (int t = 0; t < J.ntile; ++t) {
+      const int64_t pts = std::min<int64_t>(J.tile_points, (int64_t)J.npoint - (int64_t)t * J.tile_points);
+      total += (int64_t)g[(size_t)t * (J.nshell + 1) + J.nshell] * pts;
+    }
+    job->g_active = total;
+  }
+  out->g_active_values = job->g_active > 0 ? job->g_active : 0;
   return HP_OK;
 }
 

@@ -31,12 +31,14 @@
 #include <stdint.h>
 
 #include "hp_internal.cuh"
+#include "hp_umma.cuh"
 
 namespace hp {
 
+using namespace umma;
+
 namespace {
 
-constexpr int kTcM = 128;       // UMMA M
 constexpr int kTcNMax = 256;    // largest UMMA N
 constexpr int kTcK = 32;        // points per block: 32 x 4 B = one 128-byte swizzle row
 constexpr int kTcThreads = 512; // four warpgroups (each covers tensor-memory lanes 0..127)
@@ -44,7 +46,6 @@ constexpr int kTcWarps = kTcThreads / 32;
 constexpr int kRowsA = kTcM / kTcWarps;     // A rows staged per warp
 constexpr int kRowsB = kTcNMax / kTcWarps;  // B rows staged per warp (at most)
 constexpr int kTcCols = 256;    // tensor-memory columns (FP32 accumulator, N <= 256)
-constexpr long long kWaitLimit = 1ll << 26;
 constexpr int kT1Rows = kTcSinglePassShells;  // single-pass form (k_glisa_hess_tc1)
 
 // shared-memory layout (offsets from a 1024-byte-aligned base): two stages
@@ -56,91 +57,6 @@ constexpr int kOffBlo = kOffBhi + kTcNMax * kTcK * 4;  // 64 KB
 constexpr int kStageBytes = kOffBlo + kTcNMax * kTcK * 4;  // 96 KB
 constexpr int kOffBar = 2 * kStageBytes;               // 192 KB
 constexpr int kSmemBytes = kOffBar + 64 + 1024;        // + alignment slack
-
-__device__ __forceinline__ uint32_t smem_u32(const void* p) {
-  return (uint32_t)__cvta_generic_to_shared(p);
-}
-
-
-// UMMA shared-memory descriptor: start address, leading byte offset (unused
-// for swizzled K-major; 16 B), stride byte offset 1024 B (between 8-row
-// groups), descriptor version 1, 128B swizzle.
-__device__ __forceinline__ uint64_t umma_desc(uint32_t saddr) {
-  uint64_t d = 0;
-  d |= (uint64_t)((saddr >> 4) & 0x3FFF);
-  d |= (uint64_t)(16 >> 4) << 16;
-  d |= (uint64_t)(1024 >> 4) << 32;
-  d |= (uint64_t)1 << 46;
-  d |= (uint64_t)2 << 61;
-  return d;
-}
-
-// Instruction descriptor, kind::tf32: D = F32 (bits 4-5), A = B = TF32
-// (bits 7-9, 10-12), both K-major, N >> 3 at bit 17, M >> 4 at bit 24.
-__device__ __forceinline__ uint32_t idesc_tf32(int n) {
-  return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(n >> 3) << 17) |
-         ((uint32_t)(kTcM >> 4) << 24);
-}
-
-// High TF32 part of a float: sign, exponent and the top 10 mantissa bits.
-constexpr uint32_t kTf32Mask = 0xFFFFE000u;
-
-__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count));
-}
-
-__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
-      " selp.u32 %0, 1, 0, p;\n}\n"
-      : "=r"(ok)
-      : "r"(bar), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-
-// Bounded wait; returns false on time-out.
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
-  for (long long i = 0; i < kWaitLimit; ++i)
-    if (mbar_try_wait(bar, parity)) return true;
-  return false;
-}
-
-// try_wait that may suspend the thread for up to `ns` nanoseconds (woken
-// when the phase completes), so that waiting warps issue few instructions.
-__device__ __forceinline__ bool mbar_try_wait_sleep(uint32_t bar, uint32_t parity, uint32_t ns) {
-  uint32_t ok;
-  asm volatile(
-      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n"
-      " selp.u32 %0, 1, 0, p;\n}\n"
-      : "=r"(ok)
-      : "r"(bar), "r"(parity), "r"(ns)
-      : "memory");
-  return ok != 0;
-}
-
-// Bounded wait with suspension: at most kSleepWaitLimit tries of up to 1 us.
-constexpr int kSleepWaitLimit = 1 << 22;
-__device__ __forceinline__ bool mbar_wait_sleep(uint32_t bar, uint32_t parity) {
-  for (int i = 0; i < kSleepWaitLimit; ++i)
-    if (mbar_try_wait_sleep(bar, parity, 1000u)) return true;
-  return false;
-}
-
-__device__ __forceinline__ void umma_tf32(uint32_t tmem, uint64_t a, uint64_t b, uint32_t idesc,
-                                          uint32_t acc) {
-  asm volatile(
-      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-      " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
-      "l"(a), "l"(b), "r"(idesc), "r"(acc));
-}
-
-__device__ __forceinline__ void umma_commit(uint32_t bar) {
-  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                   bar)
-               : "memory");
-}
 
 // Lower-triangular tile list of an M x M Hessian: row block r0 (128 rows)
 // pairs with column blocks of up to 256 columns that start before the
@@ -177,6 +93,7 @@ __global__ void __launch_bounds__(kTcThreads) k_glisa_hess_tc(Batch bt) {
 
   const int jb = find_job(bt, blockIdx.x);
   const JobDev& J = bt.jobs[jb];
+  if (glisa_idle(J)) return;
   const int local = blockIdx.x - bt.prefix[jb];
   const int M = J.nshell, N = J.npoint;
   if (M <= kT1Rows) return;  // k_glisa_hess_tc1
@@ -367,10 +284,6 @@ constexpr int kT1StageWarps = 16;                  // producers: rows warp + 16 
 constexpr int kT1Items = kT1Rows * (kTcK / 4) / (kT1StageWarps * 32);  // 16-byte chunks per producer
 constexpr int kT1Threads = (kT1StageWarps + 1) * 32;  // + one warp that issues the MMAs
 
-__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
-  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
-}
-
 // Warp-specialised: warps 0..15 stage blocks into a ring of three shared-
 // memory stages and arrive on the stage's "full" barrier (one arrival per
 // warp); warp 16's elected lane waits for it, issues the block's MMAs and
@@ -388,6 +301,7 @@ __global__ void __launch_bounds__(kT1Threads) k_glisa_hess_tc1(Batch bt) {
 
   const int jb = find_job(bt, blockIdx.x);
   const JobDev& J = bt.jobs[jb];
+  if (glisa_idle(J)) return;
   const int M = J.nshell, N = J.npoint;
   if (M > kT1Rows) return;  // the tiled kernel (k_glisa_hess_tc) takes this job
   const int split = blockIdx.x - bt.prefix[jb];

@@ -6,8 +6,9 @@ one context (device, stream, HBM budget) and runs a loop:
 1. admit waiting requests in arrival order while the job fits the HBM budget
    (``hp_job_create`` refuses a job that would exceed it; the request then
    waits for memory to free up);
-2. advance every live job by one outer iteration with ``hp_step`` (shared
-   kernel launches for all live jobs of a scheme, one host wait per step);
+2. advance every live job with ``hp_step_n`` (shared kernel launches for all
+   live jobs of a scheme, one host wait per step): gLISA jobs by two solver
+   iterations queued back to back, the other schemes by one outer iteration;
 3. retire finished jobs: copy their results out, free their device memory,
    record their latency (completion minus arrival).
 
@@ -149,7 +150,9 @@ class PartitionServer:
         self._admit()
         if self.live:
             try:
-                self.ctx.step([r.job for r in self.live])
+                # gLISA jobs take two solver iterations per step (one host
+                # round trip); the other schemes one
+                self.ctx.step([r.job for r in self.live], 2)
             except _lib.HPError:
                 pass  # per-job failures are recorded in the job status
             self.steps += 1

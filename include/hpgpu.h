@@ -44,7 +44,7 @@
 extern "C" {
 #endif
 
-#define HPGPU_ABI_VERSION 2
+#define HPGPU_ABI_VERSION 3
 
 typedef enum {
   HP_OK = 0,
@@ -185,6 +185,10 @@ typedef struct {
   int32_t f64_factors; /* gLISA with the tensor-core Hessian: Newton steps whose
                           FP32 factor met a non-positive pivot (or whose free set
                           exceeded 224 shells) and were factored in FP64 */
+  int64_t g_active_values; /* gLISA fused passes: values of G in the rows that are
+                              not identically zero on their point tile (the
+                              values those passes read), summed over tiles;
+                              0 when the job has no such index */
 } hp_job_info;
 
 typedef struct {
@@ -218,7 +222,17 @@ int32_t hp_job_destroy(hp_job* job);
  * jobs go to the context stream; the host waits once at the end. `n_live`
  * receives the number of jobs still running. */
 int32_t hp_step(hp_ctx* ctx, hp_job* const* jobs, int32_t njobs, int32_t* n_live);
-/* Run one job to completion (the whole do_partitioning). */
+/* Advance every live job by up to max_iterations (1..64) outer iterations in
+ * one host round trip. gLISA (newton, projected Newton, sc): the iterations
+ * are queued back to back and the device stops a job at the iteration that
+ * converges, fails or reaches maxiter (the results equal one iteration per
+ * hp_step); other schemes and gLISA m-newton advance one iteration per call.
+ * (No reference counterpart: several passes of the loop body of
+ * glisa.py:748-798 without returning to Python.) */
+int32_t hp_step_n(hp_ctx* ctx, hp_job* const* jobs, int32_t njobs, int32_t max_iterations,
+                  int32_t* n_live);
+/* Run one job to completion (the whole do_partitioning); gLISA jobs queue
+ * two to four solver iterations per host round trip. */
 int32_t hp_job_run(hp_ctx* ctx, hp_job* job);
 int32_t hp_job_info_get(hp_job* job, hp_job_info* out);
 int32_t hp_job_results_get(hp_job* job, const hp_job_results* out);
@@ -233,12 +247,18 @@ typedef enum {
   HP_KERNEL_PROMOL = 0,     /* pro-atoms, promolecule, at_weights */
   HP_KERNEL_INNER = 1,      /* MBIS / aLISA inner solver passes, GISA moments */
   HP_KERNEL_CHANGE = 2,     /* outer change pass */
-  HP_KERNEL_GLISA_PRO = 3,  /* gLISA promolecule, ratios, entropy */
+  HP_KERNEL_GLISA_PRO = 3,  /* gLISA promolecule, ratios, entropy (fused jobs: also
+                               the gradient, the outer change and the tensor-core
+                               Hessian, all in one pass over G) */
   HP_KERNEL_GLISA_GRAD = 4, /* gLISA gradient */
   HP_KERNEL_GLISA_HESS = 5, /* gLISA Hessian G^T diag(w rho/rho0^2) G */
-  HP_KERNEL_GLISA_SOLVE = 6,/* gLISA Newton solve, line search, updates */
+  HP_KERNEL_GLISA_SOLVE = 6,/* gLISA Newton solve (reduction of the partial sums,
+                               factor, step, refinement) */
   HP_KERNEL_OTHER = 7,
-  HP_KERNEL_COUNT = 8
+  HP_KERNEL_GLISA_TRIALS = 8,/* gLISA step-length search: trial objectives and the
+                               pick (projected Newton), line search (m-newton),
+                               the update (newton, sc) */
+  HP_KERNEL_COUNT = 9
 } hp_kernel_family;
 int32_t hp_ctx_profile(hp_ctx* ctx, int32_t enable);
 int32_t hp_ctx_profile_get(hp_ctx* ctx, int32_t family, double* ms, int64_t* launches);

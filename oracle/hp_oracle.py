@@ -14,8 +14,7 @@ reference's class hierarchy:
 Parity of this restatement is pinned against the reference itself: the
 fixtures in ``tests/golden`` were produced by running the unmodified
 reference (through ``oracle/refshim``) on the same inputs, and
-``tests/test_oracle_vs_reference.py`` re-checks it whenever the reference
-source is present. Two reference solvers need packages that are absent here
+``tests/test_oracle_golden.py`` checks the restatement against them. Two reference solvers need packages that are absent here
 (quadprog for GISA, cvxopt for the aLISA/gLISA class defaults); GISA's QP is
 restated as an exact active-set solver (:func:`qp_simplex_nonneg`), so GISA
 parity at that boundary is unpinned.
@@ -795,3 +794,107 @@ def glisa(coordinates, numbers, pseudo_numbers, points, weights, rho, orders, ex
     res.update(charges=charges, propars=propars, niter=niter, promoldens=promol,
                at_weights=np.array(at_weights), ranges=ranges)
     return finalize(res, np.asarray(numbers), np.asarray(pseudo_numbers, dtype=float))
+
+
+# ---------------------------------------------------------------------------
+# gLISA with non-negative populations (the reference's cvxopt default)
+# ---------------------------------------------------------------------------
+
+
+def glisa_objective(G, weights, rho, c, density_cutoff=DENSITY_CUTOFF, nderiv=2):
+    """Objective, gradient and Hessian of ``_working_matrix`` (``glisa.py:411-479``)
+    for the basis matrix ``G`` (M, N), vectorised: f = int rho ln(rho/rho0),
+    grad_i = -int rho g_i / rho0, H_ij = int rho g_i g_j / rho0^2, with the
+    sick mask rho < cutoff or rho0 < cutoff."""
+    rho0 = c @ G
+    sick = (rho < density_cutoff) | (rho0 < density_cutoff)
+    with np.errstate(all="ignore"):
+        ratio = np.where(sick, 0.0, rho / np.where(sick, 1.0, rho0))
+        lnr = np.where(sick, 0.0, np.log(np.where(sick, 1.0, ratio)))
+    f = integrate(weights, rho, lnr)
+    if nderiv == 0:
+        return f
+    wr = weights * ratio
+    grad = -(G @ wr)
+    if nderiv == 1:
+        return f, grad
+    d2 = wr * np.where(sick, 0.0, 1.0 / np.where(sick, 1.0, rho0))
+    hess = (G * d2) @ G.T
+    return f, grad, hess
+
+
+def glisa_kkt(G, weights, rho, c, density_cutoff=DENSITY_CUTOFF, zero=0.0):
+    """KKT residuals of the cvxopt problem of ``glisa.py:488-571`` (minimise
+    int rho ln(rho/rho0) subject to sum c = int rho and c >= 0) at ``c``.
+
+    Its multiplier of the equality is 1 (sum_i c_i grad_i = -int rho at any
+    c), so the optimality conditions read e_i = 1 + grad_i = 0 where
+    c_i > ``zero`` and e_i >= 0 where c_i <= ``zero``. Returns the largest
+    |e_i| over the positive populations, the most negative e_i over the zero
+    ones (0 when none is negative), the smallest population and
+    |sum c - int rho|."""
+    _, grad = glisa_objective(G, weights, rho, c, density_cutoff, nderiv=1)
+    e = 1.0 + grad
+    pos = c > zero
+    stat = float(np.abs(e[pos]).max()) if pos.any() else 0.0
+    dual = float(min(0.0, e[~pos].min())) if (~pos).any() else 0.0
+    return {"stationarity": stat, "dual_infeasibility": -dual, "min_population": float(c.min()),
+            "population_error": float(abs(c.sum() - integrate(weights, rho)))}
+
+
+def glisa_nonneg(coordinates, numbers, pseudo_numbers, points, weights, rho, orders, exponents,
+                 initials, gtol=1e-12, maxiter=200, density_cutoff=DENSITY_CUTOFF,
+                 raise_on_maxiter=True):
+    """The optimum of the reference's default gLISA solver (cvxopt,
+    ``glisa.py:488-571``; cvxopt is absent here) on the molecular grid.
+
+    The same convex problem is solved by a projected Newton method on the
+    extended objective F(c) = int rho ln(rho/rho0) + sum c over c >= 0
+    (Bertsekas 1982), whose KKT points are those of the cvxopt problem
+    (:func:`glisa_kkt`): free set {c_i > 0 or dF/dc_i < 0}, Newton step on the
+    free block (FP64 Cholesky), step lengths 2^-t on the projection
+    max(c + 2^-t d, 0) with the Armijo rule. Stops when every KKT residual
+    is below ``gtol``. Starts from the reference's initial populations
+    (``gisa.py:68-88``). Returns the reference's result keys plus ``kkt``
+    and ``G``. With ``raise_on_maxiter=False`` it returns after ``maxiter``
+    iterations without reaching the tolerance (a bounded timing sample)."""
+    from scipy.linalg import cho_factor, cho_solve
+
+    natom = len(numbers)
+    rs = radial_distances(points, coordinates)
+    G = np.concatenate([basis_functions(orders[a], exponents[a], rs[a]) for a in range(natom)])
+    ranges = np.concatenate([[0], np.cumsum([len(e) for e in exponents])])
+    c = init_basis_propars(initials, pseudo_numbers, weights, rho)
+
+    def F(x):
+        return glisa_objective(G, weights, rho, x, density_cutoff, nderiv=0) + x.sum()
+
+    niter = 0
+    for niter in range(1, maxiter + 1):
+        f, grad, hess = glisa_objective(G, weights, rho, c, density_cutoff)
+        e = 1.0 + grad
+        kkt = max(np.abs(e[c > 0]).max(initial=0.0), max(0.0, -e[c <= 0].min(initial=0.0)))
+        if kkt < gtol:
+            break
+        free = (c > 0) | (e < 0)
+        idx = np.flatnonzero(free)
+        d = np.zeros_like(c)
+        d[idx] = -cho_solve(cho_factor(hess[np.ix_(idx, idx)]), e[idx])
+        f0 = f + c.sum()
+        for t in range(40):
+            x = np.maximum(c + 0.5**t * d, 0.0)
+            if F(x) <= f0 + 1e-4 * e @ (x - c):
+                break
+        else:
+            raise OracleError("projected Newton: no descent step")
+        c = x
+    else:
+        if raise_on_maxiter:
+            raise OracleError("projected Newton did not reach the KKT tolerance")
+    pros = [c[ranges[a]:ranges[a + 1]] @ G[ranges[a]:ranges[a + 1]] for a in range(natom)]
+    _, at_weights = stockholder_weights(pros)
+    charges = np.array([pseudo_numbers[a] - integrate(weights, at_weights[a] * rho)
+                        for a in range(natom)])
+    return {"charges": charges, "propars": c, "niter": niter, "ranges": ranges, "G": G,
+            "populations": np.asarray(numbers) - charges,
+            "kkt": glisa_kkt(G, weights, rho, c, density_cutoff)}

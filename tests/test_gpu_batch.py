@@ -68,3 +68,34 @@ def test_jobs_join_a_running_batch(gpu_context):
     assert np.array_equal(got["charges"], want["charges"])
     for j in jobs:
         j.close()
+
+
+@pytest.mark.parametrize("solver,precision", [("pnewton", "mixed"), ("newton", "fp64"),
+                                              ("sc", "fp64")])
+def test_queued_glisa_iterations_equal_one_per_round_trip(solver, precision, gpu_context):
+    """hp_step_n queues several gLISA iterations per host round trip; the
+    device stops each job at the iteration that finishes it, so a batch
+    advanced 8 iterations at a time ends bit-identical (results, iteration
+    counts, histories) to one iteration per hp_step."""
+    from horton_part_gb300.serve import request_from_molecule
+
+    ctx = gpu_context
+    mols = [synthetic.water(nrad=30, nang=50),
+            synthetic.chain_molecule({6: 1, 8: 1, 1: 3}, 25, 50, seed=11)]
+    reqs = [request_from_molecule(i, "glisa", m, precision=precision, solver=solver,
+                                  maxiter=5000 if solver == "sc" else None)
+            for i, m in enumerate(mols)]
+    results = []
+    for chunk in (1, 8):
+        jobs = [_lib.Job(ctx, "glisa", **r.arrays, **r.options) for r in reqs]
+        calls = 0
+        while ctx.step(jobs, chunk) > 0:
+            calls += 1
+            assert calls < 6000
+        results.append([(j.results(), j.info()) for j in jobs])
+        for j in jobs:
+            j.close()
+    for (r1, i1), (r8, i8) in zip(*results):
+        assert i1.niter == i8.niter and i1.converged == i8.converged == 1
+        for key in ("charges", "propars", "history_changes", "history_entropies"):
+            assert np.array_equal(r1[key], r8[key]), key

@@ -26,9 +26,14 @@ def _molecules():
 
 
 def _request(i, scheme, mol, precision):
-    solver = "newton" if scheme == "glisa" else "default"
-    return request_from_molecule(i, scheme, mol, precision=precision if scheme != "glisa" else "fp64",
-                                 solver=solver)
+    """MBIS in the given precision; gLISA with the FP64 Newton solver, or in the
+    mixed form of the serving workload (projected Newton with the tensor-core
+    Hessian and float-float G) when the precision is mixed."""
+    if scheme != "glisa":
+        return request_from_molecule(i, scheme, mol, precision=precision, solver="default")
+    if precision == "mixed":
+        return request_from_molecule(i, scheme, mol, precision="mixed", solver="pnewton")
+    return request_from_molecule(i, scheme, mol, precision="fp64", solver="newton")
 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])

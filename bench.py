@@ -378,7 +378,8 @@ def run_ours(args):
             run_all(js)
 
     def snapshot(js):
-        return [(i.point_atom_evals, i.niter, i.inner_iterations) for i in (j.info() for j in js)]
+        return [(i.point_atom_evals, i.niter, i.inner_iterations, i.point_atom_evals_skipped)
+                for i in (j.info() for j in js)]
 
     if batched:
         for j in jobs:
@@ -404,8 +405,10 @@ def run_ours(args):
     after = snapshot(jobs)
     if batched:
         evals_timed = sum(a[0] - b[0] for a, b in zip(after, before))
+        skipped_timed = sum(a[3] - b[3] for a, b in zip(after, before))
     else:
         evals_timed = args.steps * sum(a[0] for a in after)
+        skipped_timed = args.steps * sum(a[3] for a in after)
     niter = max(a[1] for a in after)
     # one more step with CUDA events around each kernel family (on the
     # launching stream) for the per-family times and the roofline
@@ -480,6 +483,11 @@ def run_ours(args):
         an_pass = sum(m.natom * m.npoint * d for m, d in zip(mols, d_iter))  # per outer pass
         pt_pass = sum(m.npoint * d for m, d in zip(mols, d_iter))
         inner_evals = float(sum(m.npoint * d for m, d in zip(mols, d_inner)))
+        # the per-atom cutoff skips (atom, tile) pairs: count performed work
+        d_all = sum(p[0] - a[0] for p, a in zip(prof, after)) if batched else sum(p[0] for p in prof)
+        d_skip = sum(p[3] - a[3] for p, a in zip(prof, after)) if batched else sum(p[3] for p in prof)
+        performed = 1.0 - d_skip / d_all if d_all > 0 else 1.0
+        inner_evals *= performed
         if w["scheme"] == "gisa":
             inner_evals = an_pass
         per_step = {  # (point-atom evals, algorithmic bytes) of the profiled step
@@ -599,7 +607,9 @@ def run_ours(args):
         "scaling": "weak", "vs_baseline": None,
         "dtype": "f64" if args.precision == "fp64" else "f32+f64", "data": "synthetic",
         "config": config_of(w, args, args.precision), "niter_per_job": int(niter),
-        "point_atom_evals_per_step": evals_per_step, "kernel_ms_one_profiled_step": fams,
+        "point_atom_evals_per_step": evals_per_step,
+        "point_atom_evals_performed_per_step": (evals_timed - skipped_timed) / args.steps,
+        "kernel_ms_one_profiled_step": fams,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "seconds_per_step": e2e_s},
         "roofline": roofline, "job_hbm_bound": job_bound, "clocks": clocks.summary(),

@@ -60,7 +60,7 @@ class JobInfo(ctypes.Structure):
         ("warnings", ctypes.c_uint32), ("converged", ctypes.c_int32),
         ("device_bytes", ctypes.c_int64), ("point_atom_evals", ctypes.c_double),
         ("polish_iterations", ctypes.c_int32), ("f64_factors", ctypes.c_int32),
-        ("g_active_values", ctypes.c_int64),
+        ("g_active_values", ctypes.c_int64), ("point_atom_evals_skipped", ctypes.c_double),
     ]
 
 

@@ -169,6 +169,7 @@ __global__ void __launch_bounds__(kThreads) k_atweights_ff(Batch bt) {
   const JobDev& J = decode_at_ff(bt, a, tile);
   f2 acc[1] = {{0.f, 0.f}};
   double ent = 0.0;
+  float vmax = 0.0f;  // largest rho_a on the tile (per-atom cutoff)
   float2* ra = rhoa_ff(J, a);
   const float2* pm = reinterpret_cast<const float2*>(J.promol);
   for (int i = 0; i < J.ppt; ++i) {
@@ -184,6 +185,7 @@ __global__ void __launch_bounds__(kThreads) k_atweights_ff(Batch bt) {
     }
     const f2 v = ffa::mul(aw, rho);
     ra[p] = make_float2(v.hi, v.lo);
+    vmax = fmaxf(vmax, v.hi);
     acc[0] = ffa::add_pos(acc[0], ffa::mul(f2{J.wf[p], J.wl[p]}, v));
     if (a == 0) {
       const double r = J.rho[p], pr = ffa::to_double(promol);
@@ -191,6 +193,11 @@ __global__ void __launch_bounds__(kThreads) k_atweights_ff(Batch bt) {
     }
   }
   block_sum_f2<1>(acc, red, out);
+  if (J.amax) {
+    __shared__ float redm[kWarps];
+    const float m = block_max_f(vmax, redm);
+    if (threadIdx.x == 0) J.amax[(size_t)a * J.ntile + tile] = m;
+  }
   if (threadIdx.x == 0) put_partial_ff(J, a, QA_POP, tile, out[0]);
   if (a == 0) {
     const double s = block_sum1(ent, redd);
@@ -214,6 +221,19 @@ __global__ void __launch_bounds__(kThreads, 4) k_mbis_inner_ff(Batch bt) {
   const bool first = J.inner_it[a] == 0;
   const int s0 = J.shell_off[a], n = J.shell_off[a + 1] - s0;
   const float* co = J.fco + 8 * s0;
+  if (J.tgeo && J.amax[(size_t)a * J.ntile + tile] < (float)J.density_cutoff) {
+    // per-atom cutoff (see kSkipRel): zero moments, negligible change term
+    const float r = (float)tile_rmin(J, a, tile);
+    const double b = (double)mbis_bound_f(co, n, 0, r) + (first ? 0.0 : (double)mbis_bound_f(co, n, 2, r));
+    if (tile_weight(J, tile) * b * b < kSkipRel * J.inner_threshold * J.inner_threshold) {
+      if (threadIdx.x < 2 * n) put_partial_ff(J, a, QA_INNER + threadIdx.x, tile, make_float2(0.f, 0.f));
+      if (threadIdx.x == 0) {
+        put_partial_ff(J, a, QA_INNER + kFfMbisQ - 1, tile, make_float2(0.f, 0.f));
+        count_skipped(J, tile, 1.0);
+      }
+      return;
+    }
+  }
   f2 acc[kFfMbisQ];
 #pragma unroll
   for (int q = 0; q < kFfMbisQ; ++q) acc[q] = {0.f, 0.f};

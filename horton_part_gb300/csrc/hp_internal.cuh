@@ -57,6 +57,7 @@ enum MailD {
   MD_NELEC = 2,       // integrated density
   MD_INNER_TOTAL = 3, // inner iterations summed over atoms (exact in FP64)
   MD_LS_X = 4,        // accepted line-search step (gLISA m-newton)
+  MD_SKIPPED = 5,     // point-atom evaluations skipped by the per-atom cutoff (summed)
   MD_COUNT = 8
 };
 enum MailI {
@@ -189,6 +190,12 @@ struct JobDev {
   double* hist_ent;       // [maxiter]
   double* hist_chg;       // [maxiter]
   double* charges;        // natom
+  // per-atom cutoff (MBIS on the molecular grid): per point tile its bounding
+  // sphere and weight sum [ntile][5] = (cx, cy, cz, R, sum w), and per (atom,
+  // tile) the largest AIM density rho_a on the tile from the last at_weights
+  // pass [natom][ntile]; null when the job has no cutoff
+  const double* tgeo;
+  float* amax;
   Mailbox* mail;
   int natom, npoint, ntile, nparam, nshell, qa;
   int scheme, solver, mixed, maxiter;
@@ -212,6 +219,84 @@ struct JobDev {
 __device__ __forceinline__ bool glisa_idle(const JobDev& J);
 __device__ __forceinline__ bool glisa_refine_now(const JobDev& J) {
   return J.refine && J.mail->i[MI_ITER] > 0 && J.mail->d[MD_CHANGE] < 100.0 * J.threshold;
+}
+
+// Per-atom cutoff of the MBIS inner solve and outer change. The reference
+// sums every grid point for every atom. A point contributes nothing to
+// atom a's inner moments where rho_a < density_cutoff (the sick mask of
+// mbis.py:126-133); a (atom, tile) pair whose largest rho_a on the tile is
+// below the cutoff therefore adds exact zeros to the moments, and only the
+// change term sum_p w (pro_old - pro_new)^2 remains, which is bounded by
+// W_t (pro_old + pro_new)(r_min)^2: W_t the tile's weight sum and r_min the
+// distance from the atom to the tile's bounding sphere (a sum of Slater
+// shells with non-negative populations decreases with r). Such a pair is
+// skipped when that bound is below kSkipRel x threshold^2, 1e-16 of the
+// squared change at which the loop stops: below the rounding of the sums
+// themselves. The outer change (core/iterstock.py:32-45) skips a pair on
+// the same bound with the outer threshold.
+constexpr double kSkipRel = 1e-16;
+
+// Largest v over the block (valid in thread 0); red: kWarps floats.
+__device__ __forceinline__ float block_max_f(float v, float* red) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+  if (lane == 0) red[warp] = v;
+  __syncthreads();
+  float m = red[0];
+  for (int k = 1; k < (int)(blockDim.x >> 5); ++k) m = fmaxf(m, red[k]);
+  return m;
+}
+
+__device__ __forceinline__ double tile_rmin(const JobDev& J, int a, int t) {
+  const double* g = J.tgeo + 5 * (size_t)t;
+  const double dx = J.ax[a] - g[0], dy = J.ay[a] - g[1], dz = J.az[a] - g[2];
+  return fmax(0.0, sqrt(dx * dx + dy * dy + dz * dz) - g[3]);
+}
+
+__device__ __forceinline__ double tile_weight(const JobDev& J, int t) {
+  return J.tgeo[5 * (size_t)t + 4];
+}
+
+// Upper bound of an MBIS pro-atom (pairs (N_k, S_k), N_k >= 0) at distance
+// r >= 0 from its atom: sum |N_k| S_k^3 / (8 pi) exp(-S_k r).
+__device__ __forceinline__ double mbis_bound(const double* par, int nsh, double r) {
+  double b = 0.0;
+  for (int k = 0; k < nsh; ++k) {
+    const double n = fabs(par[2 * k]), x = par[2 * k + 1];
+    b += n * x * x * x * (0.125 / M_PI) * exp(-x * r);
+  }
+  return b;
+}
+
+// Upper bound of sum_k |a_k - b_k| g_k(r) for an atom's basis shells s0 ..
+// s0 + nsh - 1 (unit-population shells N(alpha, n) exp(-alpha r^n), which
+// decrease with r); b null: sum_k |a_k| g_k(r).
+__device__ __forceinline__ double basis_bound(const JobDev& J, int s0, int nsh, const double* a,
+                                              const double* b, double r) {
+  double s = 0.0;
+  for (int k = 0; k < nsh; ++k) {
+    const double c = b ? a[k] - b[k] : a[k];
+    const int m = s0 + k;
+    s += fabs(c) * J.sh_pref[m] * exp(-J.sh_alpha[m] * pow(r, J.sh_order[m]));
+  }
+  return s;
+}
+
+// The same bound from the FP32 shell coefficient table of the mixed and
+// float-float kernels (fco: per shell 8 floats; A = N S^3 / (8 pi) at column
+// ca, S at column ca + 1).
+__device__ __forceinline__ float mbis_bound_f(const float* co, int nsh, int ca, float r) {
+  float b = 0.0f;
+  for (int k = 0; k < nsh; ++k) b += fabsf(co[8 * k + ca]) * expf(-co[8 * k + ca + 1] * r);
+  return b;
+}
+
+// Records a skipped pair: its points count as skipped evaluations (`passes`
+// pro-atom evaluations per point).
+__device__ __forceinline__ void count_skipped(const JobDev& J, int t, double passes) {
+  const int n = min(J.tile_points, J.npoint - t * J.tile_points);
+  atomicAdd(&J.mail->d[MD_SKIPPED], passes * (double)n);
 }
 
 // gLISA jobs advance several solver iterations per host round trip:

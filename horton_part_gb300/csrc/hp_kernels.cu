@@ -214,10 +214,12 @@ __global__ void __launch_bounds__(kThreads) k_promol(Batch bt) {
 __global__ void __launch_bounds__(kThreads) k_atweights(Batch bt) {
   __shared__ double red[kWarps * 2];
   __shared__ double out[2];
+  __shared__ float redm[kWarps];
   const JobDev* Jp;
   const AtomTile at = decode_atom_tile(bt, Jp);
   const JobDev& J = *Jp;
   double acc[2] = {0.0, 0.0};
+  float vmax = 0.0f;  // largest rho_a on the tile (per-atom cutoff)
   double* ra = J.rhoa + (size_t)at.atom * J.npoint;
   for (int i = 0; i < J.ppt; ++i) {
     const int p = point_of(J, at.tile, i);
@@ -227,6 +229,7 @@ __global__ void __launch_bounds__(kThreads) k_atweights(Batch bt) {
     const double aw = fmin(fmax(ra[p] * J.invpro[p], 0.0), 1.0);
     const double v = aw * rho;
     ra[p] = v;
+    vmax = fmaxf(vmax, v > 3e38 ? 3e38f : (float)v);
     acc[0] += J.w[p] * v;
     if (at.atom == 0) {
       const bool sick = (promol < J.density_cutoff) || (rho < J.density_cutoff);
@@ -234,6 +237,10 @@ __global__ void __launch_bounds__(kThreads) k_atweights(Batch bt) {
     }
   }
   block_sum<2>(acc, red, out);
+  if (J.amax) {
+    const float m = block_max_f(vmax, redm);
+    if (threadIdx.x == 0) J.amax[(size_t)at.atom * J.ntile + at.tile] = m;
+  }
   if (threadIdx.x == 0) {
     apart_ptr(J, at.atom, QA_POP)[at.tile] = out[0];
     if (at.atom == 0) J.jpart[(size_t)QJ_ENTROPY * J.ntile + at.tile] = out[1];
@@ -267,6 +274,21 @@ __global__ void __launch_bounds__(kThreads) k_change(Batch bt) {
   const JobDev* Jp;
   const AtomTile at = decode_atom_tile(bt, Jp);
   const JobDev& J = *Jp;
+  if (MODEL != MODEL_NLIS && J.tgeo) {  // per-atom cutoff: bound of the pair's change term
+    const double r = tile_rmin(J, at.atom, at.tile);
+    const int s0 = J.shell_off[at.atom], nsh = J.shell_off[at.atom + 1] - s0;
+    const double* pn = J.propars + J.par_off[at.atom];
+    const double* po = J.propars_old + J.par_off[at.atom];
+    const double b = MODEL == MODEL_MBIS ? mbis_bound(pn, nsh, r) + mbis_bound(po, nsh, r)
+                                         : basis_bound(J, s0, nsh, pn, po, r);
+    if (tile_weight(J, at.tile) * b * b < kSkipRel * J.threshold * J.threshold) {
+      if (threadIdx.x == 0) {
+        apart_ptr(J, at.atom, QA_CHANGE)[at.tile] = 0.0;
+        count_skipped(J, at.tile, 2.0);
+      }
+      return;
+    }
+  }
   double acc = 0.0;
   for (int i = 0; i < J.ppt; ++i) {
     const int p = point_of(J, at.tile, i);
@@ -416,6 +438,20 @@ __global__ void __launch_bounds__(kThreads) k_mbis_inner(Batch bt) {
   const double* pc = J.cur + J.par_off[at.atom];
   const double* pp = J.prev + J.par_off[at.atom];
   const bool first = J.inner_it[at.atom] == 0;
+  if (J.tgeo && J.amax[(size_t)at.atom * J.ntile + at.tile] < (float)J.density_cutoff) {
+    // per-atom cutoff: rho_a below the cutoff on the whole tile (the moments
+    // are exact zeros); skip if the change term is negligible too
+    const double r = tile_rmin(J, at.atom, at.tile);
+    const double b = mbis_bound(pc, nsh, r) + (first ? 0.0 : mbis_bound(pp, nsh, r));
+    if (tile_weight(J, at.tile) * b * b < kSkipRel * J.inner_threshold * J.inner_threshold) {
+      if (threadIdx.x < 2 * nsh) apart_ptr(J, at.atom, QA_INNER + threadIdx.x)[at.tile] = 0.0;
+      if (threadIdx.x == 0) {
+        apart_ptr(J, at.atom, QA_INNER + kMbisQ - 1)[at.tile] = 0.0;
+        count_skipped(J, at.tile, 1.0);
+      }
+      return;
+    }
+  }
   T cn[kMbisMaxShell], cs[kMbisMaxShell], pn[kMbisMaxShell], ps[kMbisMaxShell];
 #pragma unroll
   for (int k = 0; k < kMbisMaxShell; ++k) {
@@ -833,6 +869,18 @@ __global__ void __launch_bounds__(kThreads) k_lisa_sc_inner(Batch bt) {
   const double* pc = J.cur + J.par_off[at.atom];
   const double* pp = J.prev + J.par_off[at.atom];
   const bool first = J.inner_it[at.atom] == 0;
+  if (J.tgeo && J.amax[(size_t)at.atom * J.ntile + at.tile] < (float)J.density_cutoff) {
+    // per-atom cutoff (kSkipRel): zero moments, negligible change term
+    const double b = first ? 0.0 : basis_bound(J, s0, nsh, pc, pp, tile_rmin(J, at.atom, at.tile));
+    if (tile_weight(J, at.tile) * b * b < kSkipRel * J.inner_threshold * J.inner_threshold) {
+      if (threadIdx.x < nsh) apart_ptr(J, at.atom, QA_INNER + threadIdx.x)[at.tile] = 0.0;
+      if (threadIdx.x == 0) {
+        apart_ptr(J, at.atom, QA_INNER + Q - 1)[at.tile] = 0.0;
+        count_skipped(J, at.tile, 1.0);
+      }
+      return;
+    }
+  }
   double acc[Q];
 #pragma unroll
   for (int q = 0; q < Q; ++q) acc[q] = 0.0;

@@ -170,6 +170,7 @@ __global__ void __launch_bounds__(kThreads) k_atweights_mx(Batch bt) {
   ff acc[2] = {{0.f, 0.f}, {0.f, 0.f}};
   float* ra = rhoa_f(J, a);
   const float cut = (float)J.density_cutoff;
+  float vmax = 0.0f;  // largest rho_a on the tile (per-atom cutoff)
   for (int i = 0; i < J.ppt; ++i) {
     const int p = tile * J.tile_points + i * kThreads + threadIdx.x;
     if (p >= J.npoint) continue;
@@ -178,10 +179,16 @@ __global__ void __launch_bounds__(kThreads) k_atweights_mx(Batch bt) {
     const float aw = promol > 0.f ? fminf(fmaxf(ra[p] / promol, 0.f), 1.f) : 0.f;
     const float v = aw * rho;
     ra[p] = v;
+    vmax = fmaxf(vmax, v);
     acc[0] = ff_add(acc[0], J.wf[p] * v);
     if (a == 0 && !(promol < cut || rho < cut)) acc[1] = ff_add(acc[1], J.wf[p] * rho * logf(rho / promol));
   }
   block_sum_ff<2>(acc, red, out);
+  if (J.amax) {
+    __shared__ float redm[kWarps];
+    const float m = block_max_f(vmax, redm);
+    if (threadIdx.x == 0) J.amax[(size_t)a * J.ntile + tile] = m;
+  }
   if (threadIdx.x == 0) {
     put_partial(J, a, QA_POP, tile, out[0]);
     if (a == 0) *reinterpret_cast<float2*>(J.jpart + (size_t)QJ_ENTROPY * J.ntile + tile) = out[1];
@@ -200,6 +207,22 @@ __global__ void __launch_bounds__(kThreads) k_change_mx(Batch bt) {
   const JobDev& J = decode_at_mx(bt, a, tile);
   const int s0 = J.shell_off[a], n = J.shell_off[a + 1] - s0;
   const float* co = J.fco + 8 * s0;
+  if (J.tgeo) {  // per-atom cutoff: bound of the pair's change term
+    const float r = (float)tile_rmin(J, a, tile);
+    double b = 0.0;
+    if (MODEL == MODEL_MBIS) {
+      b = (double)mbis_bound_f(co, n, 0, r) + (double)mbis_bound_f(co, n, 2, r);
+    } else {  // sum_k |c_old - c_new|_k g_k(r)
+      for (int k = 0; k < n; ++k) b += (double)(fabsf(co[8 * k + 1]) * shell_value_f(J, s0 + k, r));
+    }
+    if (tile_weight(J, tile) * b * b < kSkipRel * J.threshold * J.threshold) {
+      if (threadIdx.x == 0) {
+        put_partial(J, a, QA_CHANGE, tile, make_float2(0.f, 0.f));
+        count_skipped(J, tile, 2.0);
+      }
+      return;
+    }
+  }
   ff acc[1] = {{0.f, 0.f}};
   for (int i = 0; i < J.ppt; ++i) {
     const int p = tile * J.tile_points + i * kThreads + threadIdx.x;
@@ -243,6 +266,19 @@ __global__ void __launch_bounds__(kThreads, 4) k_mbis_inner_mx(Batch bt) {
   const bool first = J.inner_it[a] == 0;
   const int s0 = J.shell_off[a], n = J.shell_off[a + 1] - s0;
   const float* co = J.fco + 8 * s0;
+  if (J.tgeo && J.amax[(size_t)a * J.ntile + tile] < (float)J.density_cutoff) {
+    // per-atom cutoff (see kSkipRel): zero moments, negligible change term
+    const float r = (float)tile_rmin(J, a, tile);
+    const double b = (double)mbis_bound_f(co, n, 0, r) + (first ? 0.0 : (double)mbis_bound_f(co, n, 2, r));
+    if (tile_weight(J, tile) * b * b < kSkipRel * J.inner_threshold * J.inner_threshold) {
+      if (threadIdx.x < 2 * n) put_partial(J, a, QA_INNER + threadIdx.x, tile, make_float2(0.f, 0.f));
+      if (threadIdx.x == 0) {
+        put_partial(J, a, QA_INNER + kMxMbisQ - 1, tile, make_float2(0.f, 0.f));
+        count_skipped(J, tile, 1.0);
+      }
+      return;
+    }
+  }
   ff acc[kMxMbisQ];
 #pragma unroll
   for (int q = 0; q < kMxMbisQ; ++q) acc[q] = {0.f, 0.f};
@@ -320,6 +356,22 @@ __global__ void __launch_bounds__(kThreads) k_lisa_sc_inner_mx(Batch bt) {
   const int s0 = J.shell_off[a], n = J.shell_off[a + 1] - s0;
   const bool first = J.inner_it[a] == 0;
   const float* co = J.fco + 8 * s0;
+  if (J.tgeo && J.amax[(size_t)a * J.ntile + tile] < (float)J.density_cutoff) {
+    // per-atom cutoff (kSkipRel): zero moments, negligible change term
+    double b = 0.0;
+    if (!first) {
+      const float r = (float)tile_rmin(J, a, tile);
+      for (int k = 0; k < n; ++k) b += (double)(fabsf(co[8 * k + 1]) * shell_value_f(J, s0 + k, r));
+    }
+    if (tile_weight(J, tile) * b * b < kSkipRel * J.inner_threshold * J.inner_threshold) {
+      if (threadIdx.x < n) put_partial(J, a, QA_INNER + threadIdx.x, tile, make_float2(0.f, 0.f));
+      if (threadIdx.x == 0) {
+        put_partial(J, a, QA_INNER + Q - 1, tile, make_float2(0.f, 0.f));
+        count_skipped(J, tile, 1.0);
+      }
+      return;
+    }
+  }
   ff acc[Q];
 #pragma unroll
   for (int q = 0; q < Q; ++q) acc[q] = {0.f, 0.f};

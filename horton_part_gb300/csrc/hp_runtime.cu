@@ -95,6 +95,7 @@ struct hp_job {
   int polish_iters = 0;  // outer iterations of a mixed job after its FP32 phase (FF or FP64)
   int f64_factors = 0;   // tensor-core gLISA: Newton steps factored in FP64
   int64_t g_active = -1; // fused gLISA: G values in the tiles' active rows (-1: not read yet)
+  double skipped = 0.0;  // point-atom evaluations skipped by the per-atom cutoff
   std::vector<double> changes;  // outer changes of this run
 };
 
@@ -381,6 +382,7 @@ int step_iterstock(hp_ctx* ctx, const std::vector<hp_job*>& jobs, const HostBatc
     j->warnings |= (uint32_t)m.i[MI_WARN];
     const double inner = m.d[MD_INNER_TOTAL];
     j->inner_total += inner;
+    j->skipped = m.d[MD_SKIPPED];
     // point-atom evaluations in the reference's convention: weights pass,
     // one per inner iteration, two in compute_change (GISA: one q-vector pass)
     const double n = (double)j->dev.npoint;
@@ -961,6 +963,14 @@ int32_t hp_job_create(hp_ctx* ctx, const hp_job_desc* d, hp_job** out) {
     add(&J.rad_w, 8 * (size_t)nrad);
     add(&J.radrho, 8 * (size_t)nrad);
   }
+  // per-atom cutoff of the MBIS / aLISA sc inner solve and outer change
+  // (molecular grid)
+  const bool cutoff = (mbis || (d->scheme == HP_SCHEME_LISA && solver == HP_SOLVER_SC)) &&
+                      d->grid_type != 1;
+  if (cutoff) {
+    add(&J.tgeo, 8 * 5 * (size_t)ntile);
+    add(&J.amax, 4 * (size_t)A * ntile);
+  }
   add(&J.hist_propars, 8 * (size_t)maxiter * P);
   add(&J.hist_charges, 8 * (size_t)maxiter * A);
   add(&J.hist_ent, 8 * (size_t)maxiter); add(&J.hist_chg, 8 * (size_t)maxiter);
@@ -1030,6 +1040,35 @@ int32_t hp_job_create(hp_ctx* ctx, const hp_job_desc* d, hp_job** out) {
     }
   }
   ok &= up(J.w, d->weights, 8 * (size_t)N) == cudaSuccess;
+  std::vector<double> tgeo;
+  if (cutoff) {
+    // per tile: bounding-box centre, the largest distance of its points from
+    // it, and the sum of its weights
+    tgeo.assign(5 * (size_t)ntile, 0.0);
+    for (int t = 0; t < ntile; ++t) {
+      const int64_t p0 = (int64_t)t * tile_points, p1 = std::min<int64_t>(p0 + tile_points, N);
+      double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300}, wsum = 0.0;
+      for (int64_t p = p0; p < p1; ++p) {
+        for (int c = 0; c < 3; ++c) {
+          lo[c] = std::min(lo[c], d->points[3 * p + c]);
+          hi[c] = std::max(hi[c], d->points[3 * p + c]);
+        }
+        wsum += std::fabs(d->weights[p]);
+      }
+      double* g = tgeo.data() + 5 * (size_t)t;
+      for (int c = 0; c < 3; ++c) g[c] = 0.5 * (lo[c] + hi[c]);
+      double r2 = 0.0;
+      for (int64_t p = p0; p < p1; ++p) {
+        double e = 0.0;
+        for (int c = 0; c < 3; ++c) e += (d->points[3 * p + c] - g[c]) * (d->points[3 * p + c] - g[c]);
+        r2 = std::max(r2, e);
+      }
+      g[3] = std::sqrt(r2) * (1.0 + 1e-12) + 1e-12;  // rounding margin
+      g[4] = wsum;
+    }
+    ok &= up(J.tgeo, tgeo.data(), 8 * 5 * (size_t)ntile) == cudaSuccess;
+    ok &= cudaMemsetAsync(J.amax, 0x7f, 4 * (size_t)A * ntile, st) == cudaSuccess;  // large: no skip before the first at_weights pass
+  }
   ok &= up(J.rho, d->density, 8 * (size_t)N) == cudaSuccess;
   if (local) {
     ok &= up(J.rad_off, d->radial_offsets, 4 * (size_t)(A + 1)) == cudaSuccess;
@@ -1245,6 +1284,7 @@ int32_t hp_job_reset(hp_job* job) {
   job->prev_change = 1e300;
   job->polish_iters = 0;
   job->f64_factors = 0;
+  job->skipped = 0.0;
   job->changes.clear();
   if (job->desc.scheme == HP_SCHEME_GLISA || job->desc.precision == HP_PRECISION_FP64)
     job->dev.mixed = PH_FP64;
@@ -1311,6 +1351,7 @@ int32_t hp_job_info_get(hp_job* job, hp_job_info* out) {
     job->g_active = total;
   }
   out->g_active_values = job->g_active > 0 ? job->g_active : 0;
+  out->point_atom_evals_skipped = job->skipped;
   return HP_OK;
 }
 

@@ -189,6 +189,10 @@ typedef struct {
                               not identically zero on their point tile (the
                               values those passes read), summed over tiles;
                               0 when the job has no such index */
+  double point_atom_evals_skipped; /* MBIS on the molecular grid: evaluations of
+                                      point_atom_evals (which counts every atom at
+                                      every point, the reference's convention)
+                                      that the per-atom cutoff skipped */
 } hp_job_info;
 
 typedef struct {

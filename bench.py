@@ -47,6 +47,7 @@ import subprocess  # noqa: E402
 import sys  # noqa: E402
 import threading  # noqa: E402
 import time  # noqa: E402
+import warnings  # noqa: E402
 
 import numpy as np  # noqa: E402
 
@@ -78,6 +79,23 @@ def workload(name):
         mol = synthetic.water(75, 110)
         return dict(name=name, scheme="mbis", solver="default", mol=mol, helper=None,
                     threshold=1e-8, maxiter=500)
+    if name.startswith("alisa-peptide"):
+        # 200-atom peptide-like chain (H:C:N:O:S 100:64:18:16:2), 150 radial x
+        # Lebedev-590 per atom (17.7M points), 6 s-Gaussians per H, 9 per
+        # C/N/O, 10 per S, exponents geometric in [0.05, 500] (1,502 shells);
+        # aLISA sc. A step is one outer iteration whose inner sc loop runs at
+        # most 50 iterations per atom: the throughput of the loop (the full
+        # job needs thousands of inner iterations per outer iteration).
+        # "alisa-peptide<A>": the same construction with about A atoms on
+        # 75 x Lebedev-194 grids.
+        natom = int(name[len("alisa-peptide"):] or 200)
+        base = {1: 100, 6: 64, 7: 18, 8: 16, 16: 2}
+        counts = {z: max(1, round(n * natom / 200)) for z, n in base.items()}
+        nrad, nang = (150, 590) if natom >= 200 else (75, 194)
+        mol = synthetic.peptide_molecule(counts=counts, nrad=nrad, nang=nang, seed=4)
+        helper = synthetic.geometric_gaussian_basis({1: 6, 6: 9, 7: 9, 8: 9, 16: 10}, 0.05, 500.0)
+        return dict(name=name, scheme="lisa", solver="sc", mol=mol, helper=helper,
+                    threshold=1e-6, maxiter=500, inner_maxiter=50, per_iteration=True)
     if name == "mbis-chain60":
         # the largest molecule of the batched-MBIS mix: 60 atoms, 75 x Lebedev-194
         mols = synthetic.batch_molecules(natoms=[60], nrad=75, nang=194, seed=3)
@@ -121,6 +139,8 @@ def make_job(ctx, w, precision, pinned=None, mol=None):
     off, init, orders, exps = job_arrays(w, mol)
     pts, wts, rho = (mol.grid.points, mol.grid.weights, mol.density) if pinned is None else pinned
     extra = {"inner_maxiter": 2000} if w["scheme"] == "mbis" else {}
+    if "inner_maxiter" in w:
+        extra["inner_maxiter"] = w["inner_maxiter"]
     return _lib.Job(ctx, w["scheme"], mol.coordinates, mol.pseudo_numbers, pts, wts, rho, off,
                     init, shell_orders=orders, shell_exponents=exps, solver=w["solver"],
                     precision=precision, grid_type=3, threshold=w["threshold"],
@@ -257,6 +277,23 @@ def cpu_sample(w, iterations):
         evals = 3.0 * mol.natom * mol.npoint * nit
         return (evals / dt, f"oracle gLISA projected Newton (cvxopt problem), {nit} solver "
                 f"iterations incl. basis set-up, {dt:.1f} s, 1 thread", threads)
+    if w["scheme"] == "lisa":
+        # one atom's inner sc iterations over the whole grid (the reference
+        # solves the atoms one after another, alisa.py:1304-1335 -> 193-291)
+        h = w["helper"]
+        a = int(np.argmax(mol.numbers))
+        r = np.linalg.norm(mol.grid.points - mol.coordinates[a], axis=1)
+        t0 = time.perf_counter()
+        bs = O.basis_functions(h.get_order(mol.numbers[a]), h.get_exponent(mol.numbers[a]), r)
+        ini = np.array(h.get_initial(mol.numbers[a]), dtype=float)
+        with warnings.catch_warnings():
+            warnings.simplefilter("ignore")
+            O.lisa_solver_sc(bs, mol.density * 0.5, ini / ini.sum() * mol.pseudo_numbers[a],
+                             mol.grid.weights, 1e-30, max_niter_inner=iterations)
+        dt = time.perf_counter() - t0
+        evals = float(mol.npoint) * iterations
+        return (evals / dt, f"oracle aLISA sc: {iterations} inner iterations of one atom over all "
+                f"{mol.npoint} points incl. its basis, {dt:.1f} s, 1 thread", threads)
     if w["scheme"] == "gisa":
         h = w["helper"]
         t0 = time.perf_counter()
@@ -360,7 +397,7 @@ def run_ours(args):
     # A step: for one molecule, one complete job (every iteration to
     # convergence); for a batch of molecules, one outer iteration of every
     # live job (the batch converges over hundreds of such steps).
-    batched = len(mols) > 1
+    batched = len(mols) > 1 or bool(w.get("per_iteration"))
 
     def run_all(js):
         for j in js:
@@ -615,7 +652,7 @@ def run_ours(args):
         "roofline": roofline, "job_hbm_bound": job_bound, "clocks": clocks.summary(),
         "gpu_launches": int(launches),
     }
-    if args.precision == "mixed" and not args.no_check:
+    if args.precision == "mixed" and not args.no_check and not w.get("per_iteration"):
         # error of the mixed-precision result against the FP64 path on the
         # same input (the FP64 path matches the reference to 1e-8 e in tests)
         jm = make_job(ctx, w, "mixed")

@@ -1367,14 +1367,29 @@ __global__ void __launch_bounds__(kReduceThreads) k_glisa_reduce(Batch bt) {
     for (int c = local; c < (E + 31) / 32; c += nblk) {
       const int ec = c * 32 + lane;
       float s = 0.0f, cc = 0.0f;
-      if (ec < E)
-        for (int sp = warp; sp < J.nsplit; sp += kReduceWarps) {
+      if (ec < E) {
+        // four loads in flight per lane, added in split order
+        int sp = warp;
+        for (; sp + 3 * kReduceWarps < J.nsplit; sp += 4 * kReduceWarps) {
+          float x[4];
+#pragma unroll
+          for (int u = 0; u < 4; ++u) x[u] = hp[(size_t)(sp + u * kReduceWarps) * E + ec];
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            const float t = s + x[u];
+            const float bb = t - s;
+            cc += (s - (t - bb)) + (x[u] - bb);
+            s = t;
+          }
+        }
+        for (; sp < J.nsplit; sp += kReduceWarps) {
           const float x = hp[(size_t)sp * E + ec];
           const float t = s + x;
           const float bb = t - s;
           cc += (s - (t - bb)) + (x - bb);
           s = t;
         }
+      }
       wsum[warp][lane] = (double)s + (double)cc;
       __syncthreads();
       if (warp == 0 && ec < E) {

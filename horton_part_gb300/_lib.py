@@ -80,7 +80,8 @@ EXPORTED = ("hp_abi_version", "hp_last_error", "hp_ctx_create", "hp_ctx_destroy"
             "hp_ctx_synchronize", "hp_ctx_memory", "hp_job_create", "hp_job_destroy", "hp_step",
             "hp_step_n",
             "hp_job_run", "hp_job_info_get", "hp_job_results_get", "hp_job_reset",
-            "hp_ctx_profile", "hp_ctx_profile_get", "hp_mbis_inner_noalloc")
+            "hp_ctx_profile", "hp_ctx_profile_get", "hp_mbis_inner_noalloc", "hp_glisa_evaluate",
+            "hp_glisa_change", "hp_glisa_line_search", "hp_glisa_finish")
 
 KERNEL_FAMILIES = {"promol": 0, "inner": 1, "change": 2, "glisa_pro": 3, "glisa_grad": 4,
                    "glisa_hess": 5, "glisa_solve": 6, "other": 7, "glisa_trials": 8}
@@ -123,6 +124,10 @@ def lib():
             ctypes.c_void_p, ctypes.c_double, ctypes.c_double, ctypes.c_int32,
             ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32), ctypes.c_void_p]
         L.hp_ctx_profile.argtypes = [ctypes.c_void_p, ctypes.c_int32]
+        L.hp_glisa_evaluate.argtypes = [ctypes.c_void_p, _dp, ctypes.c_int32, _dp, _dp, _dp, _dp]
+        L.hp_glisa_change.argtypes = [ctypes.c_void_p, _dp, _dp, ctypes.c_int32, _dp]
+        L.hp_glisa_line_search.argtypes = [ctypes.c_void_p, _dp, _dp, _dp, _dp, _dp]
+        L.hp_glisa_finish.argtypes = [ctypes.c_void_p, _dp, ctypes.c_int32]
         L.hp_ctx_profile_get.argtypes = [ctypes.c_void_p, ctypes.c_int32,
                                          ctypes.POINTER(ctypes.c_double),
                                          ctypes.POINTER(ctypes.c_int64)]
@@ -333,6 +338,43 @@ class Job:
             r.at_weights = _ptr(out["at_weights"])
         _check(lib().hp_job_results_get(self._h, ctypes.byref(r)))
         return out
+
+    # -- evaluation service of the host-driven gLISA solvers ---------------
+    def _vec(self, x):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        if x.shape != (self.nparam,):
+            raise ValueError(f"expected {self.nparam} parameters, got shape {x.shape}")
+        return x
+
+    def evaluate(self, x, nderiv=1):
+        """(f, grad or None, hess or None, int rho0) at populations ``x``."""
+        x = self._vec(x)
+        f, pop = ctypes.c_double(), ctypes.c_double()
+        grad = np.zeros(self.nparam) if nderiv >= 1 else None
+        hess = np.zeros((self.nparam, self.nparam)) if nderiv == 2 else None
+        _check(lib().hp_glisa_evaluate(self._h, _ptr(x), int(nderiv), ctypes.byref(f),
+                                       _ptr(grad) if grad is not None else None,
+                                       _ptr(hess) if hess is not None else None,
+                                       ctypes.byref(pop)))
+        return f.value, grad, hess, pop.value
+
+    def change(self, x, y, kind=0):
+        """kind 0: promolecule change; 1: the outer change (compute_change)."""
+        out = ctypes.c_double()
+        _check(lib().hp_glisa_change(self._h, _ptr(self._vec(x)), _ptr(self._vec(y)), int(kind),
+                                     ctypes.byref(out)))
+        return out.value
+
+    def line_search(self, x, delta, keep):
+        """(step, new populations) of the valid-promolecule line search; step < 0: none."""
+        step = ctypes.c_double()
+        out = np.zeros(self.nparam)
+        _check(lib().hp_glisa_line_search(self._h, _ptr(self._vec(x)), _ptr(self._vec(delta)),
+                                          _ptr(self._vec(keep)), ctypes.byref(step), _ptr(out)))
+        return step.value, out
+
+    def finish(self, x, niter):
+        _check(lib().hp_glisa_finish(self._h, _ptr(self._vec(x)), int(niter)))
 
     def close(self):
         if getattr(self, "_h", None) and getattr(self.ctx, "_h", None):

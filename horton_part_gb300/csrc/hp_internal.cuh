@@ -58,6 +58,8 @@ enum MailD {
   MD_INNER_TOTAL = 3, // inner iterations summed over atoms (exact in FP64)
   MD_LS_X = 4,        // accepted line-search step (gLISA m-newton)
   MD_SKIPPED = 5,     // point-atom evaluations skipped by the per-atom cutoff (summed)
+  MD_EVAL_A = 6,      // host-driven gLISA solvers: objective or change of the last evaluation
+  MD_EVAL_B = 7,      // host-driven gLISA solvers: int rho0 of the last evaluation
   MD_COUNT = 8
 };
 enum MailI {
@@ -535,6 +537,11 @@ void launch_glisa_keep(const HostBatch& hb, cudaStream_t st);
 void launch_glisa_ls(const HostBatch& hb, cudaStream_t st, int first, int count);
 void launch_glisa_change(const HostBatch& hb, cudaStream_t st);
 void launch_glisa_check(const HostBatch& hb, cudaStream_t st);
+// evaluation service of the host-driven gLISA solvers (FP64 jobs):
+// what 0: objective (entropy) and int rho0 after k_glisa_pro;
+// what 1: sqrt(int (sum_m delta_m g_m)^2), the promolecule change for delta;
+// what 2: sqrt(sum over atoms of the QA_CHANGE partials) after k_glisa_change
+void launch_glisa_eval(const HostBatch& hb, cudaStream_t st, int what);
 // trials + Armijo pick; fuse_shells > 0: the fused trial pass (batch of fused jobs)
 void launch_glisa_pnewton(const HostBatch& hb, cudaStream_t st, int gff, int fuse_shells);
 // fuse_shells: largest shell count of the batch's fused jobs (0: none);

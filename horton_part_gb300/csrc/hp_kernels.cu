@@ -2184,6 +2184,58 @@ __global__ void k_glisa_check(Batch bt) {
 }
 
 // ---------------------------------------------------------------------------
+// Evaluation service of the host-driven gLISA solvers (DIIS, CDIIS,
+// trust-region, quasi-Newton; glisa.py:595-615, 883-1028). The host holds
+// the solver state (a few vectors of nshell values); the device does the grid
+// work of function_g, _working_matrix, calc_promol_dens and compute_change
+// for the populations the host uploads.
+// ---------------------------------------------------------------------------
+
+// Per point tile into atom 0's QA_POP slot: what 0: sum w rho0 (rho0 from
+// k_glisa_pro); what 1: sum w (sum_m delta_m G_m)^2.
+__global__ void __launch_bounds__(kThreads) k_glisa_eval_tiles(Batch bt, int what) {
+  __shared__ double red[kWarps];
+  int tile;
+  const JobDev& J = decode_local(bt, tile);
+  double acc = 0.0;
+  for (int i = 0; i < J.ppt; ++i) {
+    const int p = point_of(J, tile, i);
+    if (p >= J.npoint) continue;
+    if (what == 0) {
+      acc += J.w[p] * J.rho0[p];
+    } else {
+      double d = 0.0;
+#pragma unroll 8
+      for (int m = 0; m < J.nshell; ++m) d += J.delta[m] * J.gmat[(size_t)m * J.npoint + p];
+      acc += J.w[p] * d * d;
+    }
+  }
+  const double s = block_sum1(acc, red);
+  if (threadIdx.x == 0) apart_ptr(J, 0, QA_POP)[tile] = s;
+}
+
+// One warp: the totals into the mailbox (fixed summation order).
+__global__ void k_glisa_eval_sum(Batch bt, int what) {
+  int local;
+  const JobDev& J = decode_local(bt, local);
+  if (what == 0) {
+    const double e = warp_tile_sum(J, J.jpart + (size_t)QJ_ENTROPY * J.ntile, J.ntile);
+    const double p = warp_tile_sum(J, apart_ptr(J, 0, QA_POP), J.ntile);
+    if ((threadIdx.x & 31) == 0) {
+      J.mail->d[MD_EVAL_A] = e;
+      J.mail->d[MD_EVAL_B] = p;
+    }
+  } else if (what == 1) {
+    const double s = warp_tile_sum(J, apart_ptr(J, 0, QA_POP), J.ntile);
+    if ((threadIdx.x & 31) == 0) J.mail->d[MD_EVAL_A] = sqrt(s);
+  } else {
+    double msd = 0.0;
+    for (int a = 0; a < J.natom; ++a) msd += warp_tile_sum(J, apart_ptr(J, a, QA_CHANGE), J.ntile);
+    if ((threadIdx.x & 31) == 0) J.mail->d[MD_EVAL_A] = sqrt(msd);
+  }
+}
+
+// ---------------------------------------------------------------------------
 // gLISA with non-negative populations: projected Newton (the optimum of the
 // reference's cvxopt solver, glisa.py:488-571)
 //
@@ -2490,6 +2542,11 @@ void launch_glisa_change(const HostBatch& hb, cudaStream_t st) {
 }
 
 void launch_glisa_check(const HostBatch& hb, cudaStream_t st) { HP_LAUNCH(k_glisa_check, K_JOB, 32); }
+
+void launch_glisa_eval(const HostBatch& hb, cudaStream_t st, int what) {
+  if (what != 2) HP_LAUNCH(k_glisa_eval_tiles, K_POINT, kThreads, what);
+  HP_LAUNCH(k_glisa_eval_sum, K_JOB, 32, what);
+}
 
 void launch_glisa_pnewton(const HostBatch& hb, cudaStream_t st, int gff, int fuse_shells) {
   HP_LAUNCH(k_glisa_trial_set, K_JOB, kThreads);

@@ -96,6 +96,7 @@ struct hp_job {
   int f64_factors = 0;   // tensor-core gLISA: Newton steps factored in FP64
   int64_t g_active = -1; // fused gLISA: G values in the tiles' active rows (-1: not read yet)
   double skipped = 0.0;  // point-atom evaluations skipped by the per-atom cutoff
+  bool host_driven = false;  // finished by hp_glisa_finish (histories kept by the host)
   std::vector<double> changes;  // outer changes of this run
 };
 
@@ -1285,12 +1286,164 @@ int32_t hp_job_reset(hp_job* job) {
   job->polish_iters = 0;
   job->f64_factors = 0;
   job->skipped = 0.0;
+  job->host_driven = false;
   job->changes.clear();
   if (job->desc.scheme == HP_SCHEME_GLISA || job->desc.precision == HP_PRECISION_FP64)
     job->dev.mixed = PH_FP64;
   else
     job->dev.mixed = job->desc.precision == HP_PRECISION_FF ? PH_FF : PH_FP32;
   return HP_OK;
+}
+
+// ---------------------------------------------------------------------------
+// evaluation service of the host-driven gLISA solvers
+// ---------------------------------------------------------------------------
+
+namespace {
+
+// An FP64 gLISA job on the molecular grid, initialised (basis matrix on the
+// device), with its one-job batch in hb.
+int eval_ready(hp_job* job, HostBatch& hb) {
+  if (!job) return fail(HP_ERR_INVALID, "null job");
+  if (job->desc.scheme != HP_SCHEME_GLISA || !job->dev.gmat || job->dev.tc || job->dev.local)
+    return fail(HP_ERR_UNSUPPORTED,
+                "the host-driven gLISA solvers run on FP64 gLISA jobs on the molecular grid");
+  hp_ctx* ctx = job->ctx;
+  HP_CK(cudaSetDevice(ctx->device));
+  std::vector<hp_job*> one{job};
+  int rc = build_batch(ctx, one, hb);
+  if (rc) return rc;
+  if (!job->initialized) {
+    rc = job_init(ctx, one, hb);
+    if (rc) return rc;
+    HP_CK(cudaStreamSynchronize(ctx->stream));
+  }
+  return HP_OK;
+}
+
+int upload(hp_job* job, double* dst, const double* src) {
+  HP_CK(cudaMemcpyAsync(dst, src, 8 * (size_t)job->dev.nparam, cudaMemcpyHostToDevice,
+                        job->ctx->stream));
+  return HP_OK;
+}
+
+}  // namespace
+
+int32_t hp_glisa_evaluate(hp_job* job, const double* x, int32_t nderiv, double* f, double* grad,
+                          double* hess, double* pro_pop) {
+  if (!x || nderiv < 0 || nderiv > 2) return fail(HP_ERR_INVALID, "bad argument");
+  HostBatch hb;
+  int rc = eval_ready(job, hb);
+  if (rc) return rc;
+  hp_ctx* ctx = job->ctx;
+  const JobDev& J = job->dev;
+  cudaStream_t st = ctx->stream;
+  rc = upload(job, J.propars, x);
+  if (rc) return rc;
+  launch_glisa_pro(hb, st);
+  if (nderiv >= 1) launch_glisa_grad(hb, st);
+  if (nderiv == 2) launch_glisa_hess(hb, st);
+  if (nderiv >= 1) launch_glisa_reduce(hb, st);
+  launch_glisa_eval(hb, st, 0);
+  rc = check_launch();
+  if (rc) return rc;
+  rc = read_mail(ctx);
+  if (rc) return rc;
+  const Mailbox& m = ctx->mail_host[job->slot];
+  if (f) *f = m.d[MD_EVAL_A];
+  if (pro_pop) *pro_pop = m.d[MD_EVAL_B];
+  const size_t S = (size_t)J.nshell;
+  if (grad && nderiv >= 1) HP_CK(cudaMemcpy(grad, J.grad, 8 * S, cudaMemcpyDeviceToHost));
+  if (hess && nderiv == 2) HP_CK(cudaMemcpy(hess, J.hess, 8 * S * S, cudaMemcpyDeviceToHost));
+  job->evals += (double)J.npoint * (double)J.natom;
+  return HP_OK;
+}
+
+int32_t hp_glisa_change(hp_job* job, const double* x, const double* y, int32_t kind,
+                        double* change) {
+  if (!x || !y || !change || kind < 0 || kind > 1) return fail(HP_ERR_INVALID, "bad argument");
+  HostBatch hb;
+  int rc = eval_ready(job, hb);
+  if (rc) return rc;
+  hp_ctx* ctx = job->ctx;
+  const JobDev& J = job->dev;
+  cudaStream_t st = ctx->stream;
+  if (kind == 0) {  // promolecule difference
+    std::vector<double> d((size_t)J.nparam);
+    for (int i = 0; i < J.nparam; ++i) d[i] = x[i] - y[i];
+    rc = upload(job, J.delta, d.data());
+    if (rc) return rc;
+    HP_CK(cudaStreamSynchronize(st));  // d leaves scope
+    launch_glisa_eval(hb, st, 1);
+  } else {  // compute_change: per-atom pro-atom differences
+    rc = upload(job, J.propars, x);
+    if (!rc) rc = upload(job, J.propars_old, y);
+    if (rc) return rc;
+    launch_glisa_change(hb, st);
+    launch_glisa_eval(hb, st, 2);
+  }
+  rc = check_launch();
+  if (rc) return rc;
+  rc = read_mail(ctx);
+  if (rc) return rc;
+  *change = ctx->mail_host[job->slot].d[MD_EVAL_A];
+  job->evals += 2.0 * (double)J.npoint * (double)J.natom;
+  return HP_OK;
+}
+
+int32_t hp_glisa_line_search(hp_job* job, const double* x, const double* delta, const double* keep,
+                             double* step, double* x_out) {
+  if (!x || !delta || !keep || !step || !x_out) return fail(HP_ERR_INVALID, "bad argument");
+  HostBatch hb;
+  int rc = eval_ready(job, hb);
+  if (rc) return rc;
+  hp_ctx* ctx = job->ctx;
+  const JobDev& J = job->dev;
+  cudaStream_t st = ctx->stream;
+  rc = upload(job, J.propars, x);
+  if (!rc) rc = upload(job, J.delta, delta);
+  if (!rc) rc = upload(job, J.keep, keep);
+  if (rc) return rc;
+  launch_glisa_ls(hb, st, 0, std::min(J.linspace_size, 64));
+  rc = check_launch();
+  if (rc) return rc;
+  rc = read_mail(ctx);
+  if (rc) return rc;
+  *step = ctx->mail_host[job->slot].d[MD_LS_X];
+  HP_CK(cudaMemcpy(x_out, J.propars, 8 * (size_t)J.nparam, cudaMemcpyDeviceToHost));
+  job->evals += (double)J.npoint * (double)J.natom;
+  return HP_OK;
+}
+
+int32_t hp_glisa_finish(hp_job* job, const double* x, int32_t niter) {
+  if (!x || niter < 0) return fail(HP_ERR_INVALID, "bad argument");
+  HostBatch hb;
+  int rc = eval_ready(job, hb);
+  if (rc) return rc;
+  hp_ctx* ctx = job->ctx;
+  cudaStream_t st = ctx->stream;
+  rc = upload(job, job->dev.propars, x);
+  if (rc) return rc;
+  launch_glisa_pro(hb, st);  // negativity of the final promolecule
+  launch_glisa_check(hb, st);
+  launch_promol(hb, st, 0, MODEL_BASIS);  // at_weights and populations (glisa.py:268-278)
+  launch_charges(hb, st);
+  rc = check_launch();
+  if (rc) return rc;
+  rc = read_mail(ctx);
+  if (rc) return rc;
+  const Mailbox& m = ctx->mail_host[job->slot];
+  job->warnings |= (uint32_t)m.i[MI_WARN];
+  if (m.i[MI_ERR]) {
+    job->status = status_of(m.i[MI_ERR]);
+    g_err = err_text(m.i[MI_ERR]);
+  }
+  job->niter = niter;
+  job->converged = m.i[MI_ERR] == 0;
+  job->done = true;
+  job->host_driven = true;
+  job->evals += 2.0 * (double)job->dev.npoint * (double)job->dev.natom;
+  return job->status == HP_OK ? HP_OK : fail(job->status, g_err);
 }
 
 int32_t hp_ctx_profile(hp_ctx* c, int32_t enable) {
@@ -1361,7 +1514,7 @@ int32_t hp_job_results_get(hp_job* job, const hp_job_results* r) {
   HP_CK(cudaSetDevice(ctx->device));
   const JobDev& J = job->dev;
   const size_t A = J.natom, N = J.npoint, P = J.nparam;
-  const size_t nit = std::min(job->niter, J.maxiter);
+  const size_t nit = job->host_driven ? 0 : std::min(job->niter, J.maxiter);
   cudaStream_t st = ctx->stream;
   if (r->at_weights) {
     if (!job->done) return fail(HP_ERR_STATE, "at_weights are available once the job is done");

@@ -293,6 +293,12 @@ class GPUStockholderWPart(WPart):
     def _finalize_extra(self, res):
         pass
 
+    def _run_job(self, job):
+        """Run the job to the end on the device; a scheme whose iterations run
+        on the host returns the histories it kept (else None)."""
+        job.run()
+        return None
+
     # -- the partitioning ------------------------------------------------------
     _supports_atom_grids = False  # grid_type 1 on the GPU (set by the scheme classes)
 
@@ -341,7 +347,7 @@ class GPUStockholderWPart(WPart):
         try:
             t0 = time.time()
             try:
-                job.run()
+                host_histories = self._run_job(job)
             except _lib.HPError as err:
                 raise RuntimeError(str(err)) from err
             t1 = time.time()
@@ -349,6 +355,8 @@ class GPUStockholderWPart(WPart):
             self._job_info = info
             self._report_warnings(info)
             res = job.results(at_weights=self._store_at_weights)
+            if host_histories:
+                res.update(host_histories)
         finally:
             job.close()
         niter = int(info.niter)

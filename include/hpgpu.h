@@ -245,6 +245,38 @@ int32_t hp_job_results_get(hp_job* job, const hp_job_results* out);
  * core/base.py:164-167, without re-uploading the grid.) */
 int32_t hp_job_reset(hp_job* job);
 
+/* Evaluation service of the gLISA solvers whose iterations run on the host
+ * (DIIS, CDIIS, trust-region, quasi-Newton: glisa.py:595-615, 883-1028, with
+ * algo/diis.py, algo/cdiis.py, algo/quasi_newton.py): the host keeps the
+ * solver state (a few vectors of nparam values), the device does every pass
+ * over the grid. FP64 gLISA jobs on the molecular grid only
+ * (HP_ERR_UNSUPPORTED otherwise); x, y, delta, keep, grad, hess and x_out
+ * are HOST arrays of nparam (hess: nparam x nparam) values.
+ *
+ * hp_glisa_evaluate <- GlobalLinearISAWPart._working_matrix (glisa.py:411-479)
+ *   with calc_promol_dens (glisa.py:346-348): at populations x, f =
+ *   int rho ln(rho/rho0), grad_i = -int rho g_i/rho0 (nderiv >= 1), hess_ij =
+ *   int rho g_i g_j/rho0^2 (nderiv = 2), pro_pop = int rho0. */
+int32_t hp_glisa_evaluate(hp_job* job, const double* x, int32_t nderiv, double* f, double* grad,
+                          double* hess, double* pro_pop);
+/* kind 0: sqrt(int (rho0(x) - rho0(y))^2), the promolecule change of the
+ *   DIIS and trust-region convergence tests (glisa.py:886-893, 958-962);
+ * kind 1: the outer change of compute_change (core/iterstock.py:32-45). */
+int32_t hp_glisa_change(hp_job* job, const double* x, const double* y, int32_t kind,
+                        double* change);
+/* The valid-promolecule line search of _solver_general_newton
+ * (glisa.py:675-743): the first t of linspace(tau, 0, linspace_size) (the
+ * job's tau and linspace_size) with every pro-atom of x + keep * t * delta
+ * at or above negative_cutoff on the grid; *step = t and x_out = that point,
+ * or *step = -1 when no trial is valid. */
+int32_t hp_glisa_line_search(hp_job* job, const double* x, const double* delta, const double* keep,
+                             double* step, double* x_out);
+/* End a host-driven job at populations x after niter iterations: the checks,
+ * at_weights and charges of glisa.py:268-278 (check_pro_atom_parameters,
+ * utils.py:255-398); the job is done afterwards and hp_job_results_get
+ * returns its charges and parameters (the histories stay with the host). */
+int32_t hp_glisa_finish(hp_job* job, const double* x, int32_t niter);
+
 /* Kernel timing with CUDA events on the context stream, per kernel family
  * (hp_kernel_family). Enabling clears the accumulators. */
 typedef enum {

@@ -677,6 +677,8 @@ def run_ours(args):
             "niter_mixed": int(im.niter)}
         if w["scheme"] == "glisa":
             line["accuracy_vs_fp64"]["newton_fp64_factors"] = int(im.f64_factors)
+    if rank == 0 and world == 1 and args.workload == "glisa-c6h10n2o2" and not args.no_extras:
+        line.update(extra_sections(ctx, args))
     if rank == 0 and world == 1 and not args.no_cpu:
         r, sample, threads = cpu_sample(w, 2 if w["scheme"] == "glisa" else 3)
         line["cpu_baseline"] = {"value": r, "unit": UNIT, "cores": threads, "kind": "port",
@@ -686,6 +688,78 @@ def run_ours(args):
     job.close()
     ctx.close()
     replicas.finalize()
+
+
+def extra_sections(ctx, args):
+    """Bounded measurements of the metric's other workloads, added to the
+    default line: the batched MBIS step (config 3's generator, 32 molecules
+    of 3-60 atoms, 75 x Lebedev-194 per atom; three outer iterations of every
+    job with shared launches, timed with CUDA events) and the continuous-
+    batching server (12 requests, 70 % MBIS / 30 % gLISA, 3-60 atoms:
+    closed-loop capacity, then Poisson arrivals at 70 % of it with p50/p99
+    latency). Each takes a few tens of seconds."""
+    import torch
+
+    from horton_part_gb300 import _lib, synthetic
+    from horton_part_gb300.serve import PartitionServer, request_from_molecule
+
+    out = {}
+    stream = torch.cuda.current_stream()
+    w = {"scheme": "mbis", "solver": "default", "threshold": 1e-8, "maxiter": 500, "helper": None}
+    mols = synthetic.batch_molecules(nmol=32, amin=3, amax=60, nrad=75, nang=194, seed=3)
+    jobs = [make_job(ctx, w, "mixed", mol=m) for m in mols]
+    for _ in range(2):  # warm-up: the first outer iterations
+        ctx.step(jobs)
+    before = [j.info() for j in jobs]
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    nsteps = 3
+    for _ in range(nsteps):
+        ctx.step(jobs)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    after = [j.info() for j in jobs]
+    evals = sum(a.point_atom_evals - b.point_atom_evals for a, b in zip(after, before))
+    skipped = sum(a.point_atom_evals_skipped - b.point_atom_evals_skipped for a, b in zip(after, before))
+    for j in jobs:
+        j.close()
+    out["batch"] = {"workload": "mbis-batch32", "molecules": len(mols),
+                    "natom": int(sum(m.natom for m in mols)),
+                    "npoint": int(sum(m.npoint for m in mols)), "precision": "mixed",
+                    "steps": nsteps, "ms_per_step": ms / nsteps,
+                    "point_atom_evals_per_s": evals / (ms / 1000.0),
+                    "performed_fraction": 1.0 - skipped / evals if evals else None}
+    # serving: 12 requests from the serving mix's generator, atoms 3-60
+    rng = np.random.default_rng(17)
+    nreq = 12
+    is_mbis = rng.random(nreq) < 0.7
+    natoms = np.rint(np.exp(rng.uniform(np.log(3.0), np.log(60.0), nreq))).astype(int)
+    mb = iter(synthetic.batch_molecules(natoms=natoms[is_mbis], nrad=75, nang=194, seed=17))
+    gl = iter(synthetic.batch_molecules(natoms=natoms[~is_mbis], nrad=100, nang=302, seed=18))
+    pool = [("mbis", next(mb), "default") if is_mbis[i] else ("glisa", next(gl), "pnewton")
+            for i in range(nreq)]
+
+    def serve(arrivals):
+        srv = PartitionServer(hbm_budget=150 * 10**9)
+        reqs = [request_from_molecule(i, sch, m, precision="mixed", threshold=1e-8, solver=sv)
+                for i, (sch, m, sv) in enumerate(pool)]
+        wall = srv.run_stream(reqs, arrivals)
+        st = srv.stats(wall)
+        srv.close()
+        return st
+
+    cap = serve(np.zeros(nreq))
+    lam = 0.7 * cap["jobs_per_s"]
+    arr = np.cumsum(np.random.default_rng(19).exponential(1.0 / lam, nreq))
+    load = serve(arr)
+    out["serving"] = {"requests": nreq, "mbis": int(is_mbis.sum()), "glisa": int((~is_mbis).sum()),
+                      "natom_total": int(natoms.sum()), "precision": "mixed",
+                      "capacity_jobs_per_s": cap["jobs_per_s"],
+                      "poisson_arrival_rate_jobs_per_s": lam, "poisson": load,
+                      "note": "every request enters from host arrays and returns its results"}
+    return out
 
 
 def serve_requests(nreq, seed, precision):
@@ -813,6 +887,8 @@ def main():
     ap.add_argument("--no-polish", action="store_true",
                     help="mixed precision: stay in FP32 to the threshold (no finish phase)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the bounded batch and serving sections of the default workload")
     ap.add_argument("--no-check", action="store_true",
                     help="skip the mixed-precision accuracy run against the FP64 path")
     ap.add_argument("--serve-jobs", type=int, default=32,

@@ -845,8 +845,17 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_trials_fused(Batch bt
   const float at = ldexpf(1.0f, -t);
   const int nclip = J.clip[S];
   const int* tm = J.clip + S + 1;
-  int kt = 0;  // clipped shells with t_m > t: a prefix of the list (sorted, largest first)
-  while (kt < nclip && tm[kt] > t) ++kt;
+  // clipped shells with t_m > t: a prefix of the list (sorted, largest
+  // first) of length ktab[t]; group g = the shells with min(t_m, kTrials) =
+  // g + 1, the list segment [ktab[g + 1], ktab[g]) (group kTrials - 1 from
+  // 0), is clipped in the trials t <= g
+  __shared__ int ktab[kTrials];
+  __shared__ float4 grp[kTrials][kFuseSP];  // per group and point: (sum c g, sum delta g) pairs
+  if (threadIdx.x < kTrials) {
+    int k = 0;
+    while (k < nclip && tm[k] > (int)threadIdx.x) ++k;
+    ktab[threadIdx.x] = k;
+  }
   for (int k = threadIdx.x; k < nclip; k += kFuseThreads) cpos[k] = pos[J.clip[k]];
   const float4* cd = reinterpret_cast<const float4*>(J.clipf);
   const float2 cutp = split2(J.density_cutoff);
@@ -886,6 +895,20 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_trials_fused(Batch bt
       dot2_merge(d, e);
       part[warp * kFuseSP + lane] = d;
     }
+    {  // C: warp g sums the clipped shells of group g for the 32 points, once
+      const int g = warp;
+      const int k1 = ktab[g], k0 = g + 1 < kTrials ? ktab[g + 1] : 0;
+      Dot2 sc{0.f, 0.f}, sd{0.f, 0.f};
+      for (int k = k0; k < k1; ++k) {
+        const int i = cpos[k];
+        if (i < 0) continue;  // the shell is zero on this tile
+        const float4 v = cd[k];
+        const float g1 = gh[i * kFuseSP + lane], g2 = gl[i * kFuseSP + lane];
+        dot2_add(sc, g1, g2, v.x, v.y);
+        dot2_add(sd, g1, g2, v.z, v.w);
+      }
+      grp[g][lane] = make_float4(sc.s, sc.c, sd.s, sd.c);
+    }
     __syncthreads();
     const int p = p0 + sub * kFuseSP + lane;
     if (p < p1) {  // T
@@ -893,14 +916,11 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_trials_fused(Batch bt
 #pragma unroll
       for (int q = 1; q < kFuseWarps; ++q) dot2_merge(du, part[q * kFuseSP + lane]);
       const f2 u = dot2_ff(du);
-      Dot2 sc{0.f, 0.f}, sd{0.f, 0.f};
-      for (int k = 0; k < kt; ++k) {
-        const int i = cpos[k];
-        if (i < 0) continue;  // the shell is zero on this tile
-        const float4 v = cd[k];
-        const float g1 = gh[i * kFuseSP + lane], g2 = gl[i * kFuseSP + lane];
-        dot2_add(sc, g1, g2, v.x, v.y);
-        dot2_add(sd, g1, g2, v.z, v.w);
+      Dot2 sc{0.f, 0.f}, sd{0.f, 0.f};  // groups t .. kTrials - 1, in that order
+      for (int g = t; g < kTrials; ++g) {
+        const float4 v = grp[g][lane];
+        dot2_merge(sc, Dot2{v.x, v.y});
+        dot2_merge(sd, Dot2{v.z, v.w});
       }
       const f2 dsd = dot2_ff(sd);
       const f2 corr = ffa::neg(ffa::add(dot2_ff(sc), f2{at * dsd.hi, at * dsd.lo}));

@@ -2,9 +2,12 @@
 chain with S, 6-10 s-Gaussians per element up to exponent 500), at a size the
 oracle finishes: 11 atoms on 20 x Lebedev-50 points per atom.
 
-FP64 must match the oracle's iteration count and charges to 1e-8 e; the
-mixed form (FP32 bulk, FP64 finish) to 1e-6 e. The per-atom cutoff of the
-inner solve is active on both (the molecule is 18 bohr long).
+FP64 at the oracle's threshold (1e-6) must match its iteration count and
+charges to 1e-8 e. The self-consistent update converges slowly (about 200
+inner iterations per atom and outer iteration here), so two runs that stop
+at a change of 1e-6 after different paths can still differ by ~1e-4 e; the
+mixed form (FP32 bulk, FP64 finish) is therefore compared with FP64 at a
+threshold of 1e-9, where both must agree to 1e-6 e.
 """
 
 import os
@@ -22,20 +25,33 @@ sys.path.insert(0, GOLDEN)
 from make_lisa_peptide import build_peptide_inputs, fingerprint  # noqa: E402
 
 
-@pytest.mark.parametrize("precision,q_tol", [("fp64", 1e-8), ("mixed", 1e-6)])
-def test_lisa_sc_peptide_matches_the_oracle(precision, q_tol, gpu_context):
+def _run(mol, helper, precision, threshold):
+    part = wpart_schemes("lisa")(mol.coordinates, mol.numbers, mol.pseudo_numbers, mol.grid,
+                                 mol.density, grid_type=3, solver="sc", basis_func=helper,
+                                 threshold=threshold, inner_threshold=min(1e-8, threshold),
+                                 precision=precision)
+    part.do_partitioning()
+    return part
+
+
+def test_lisa_sc_peptide_matches_the_oracle(gpu_context):
     with np.load(os.path.join(GOLDEN, "lisa_sc_peptide11_20x50.npz")) as f:
         g = {k: f[k] for k in f.files}
     mol, helper = build_peptide_inputs()
     np.testing.assert_allclose(fingerprint(mol), g["fingerprint"], rtol=1e-10)
-    part = wpart_schemes("lisa")(mol.coordinates, mol.numbers, mol.pseudo_numbers, mol.grid,
-                                 mol.density, grid_type=3, solver="sc", basis_func=helper,
-                                 threshold=1e-6, inner_threshold=1e-8, precision=precision)
-    part.do_partitioning()
-    info = part.job_info
+    part = _run(mol, helper, "fp64", 1e-6)
     dq = float(np.abs(part["charges"] - g["charges"]).max())
-    print(f"aLISA sc peptide {precision}: niter {part['niter']} (oracle {int(g['niter'])}), "
-          f"max|dq| {dq:.2e} e, skipped {info.point_atom_evals_skipped / info.point_atom_evals:.1%}")
-    assert dq < q_tol
-    if precision == "fp64":
-        assert part["niter"] == int(g["niter"])
+    print(f"aLISA sc peptide fp64: niter {part['niter']} (oracle {int(g['niter'])}), "
+          f"max|dq| {dq:.2e} e")
+    assert dq < 1e-8
+    assert part["niter"] == int(g["niter"])
+
+
+def test_lisa_sc_peptide_mixed_reaches_the_fp64_result(gpu_context):
+    mol, helper = build_peptide_inputs()
+    fp = _run(mol, helper, "fp64", 1e-9)
+    mx = _run(mol, helper, "mixed", 1e-9)
+    dq = float(np.abs(mx["charges"] - fp["charges"]).max())
+    print(f"aLISA sc peptide at 1e-9: niter fp64 {fp['niter']} mixed {mx['niter']}, "
+          f"max|dq| {dq:.2e} e")
+    assert dq < 1e-6

@@ -323,27 +323,34 @@ __global__ void __launch_bounds__(kThreads) k_glisa_trials_ff(Batch bt) {
 // Fused passes: one read of G for a product G^T x and the row sums G v that
 // depend on it. A block (256 threads, two per SM) streams its point tile
 // through shared memory in sub-tiles of kFuseSP = 32 points (both planes of
-// all S shells, double-buffered with cp.async); per sub-tile
-//   A  u(p) = sum_m G[m][p] x[m]: warp w sums the shells m = w (mod 8) for
-//      the 32 points (lane = point), two chains per lane;
-//   A' every warp merges the eight partial sums in the same fixed order and
-//      forms v(p) as a float pair for itself (no barrier before B); the
-//      sub-tile's owner warp (sub mod 8) also writes the per-point outputs;
-//   B  gpart[m] += sum_p G[m][p] v(p): warp w owns rows w, w + 8, ...; the
-//      lanes' compensated sums stay in registers across the tile and are
-//      reduced once at its end.
+// the tile's active rows, cp.async into one of nbuf staging buffers: two when
+// they fit beside the rest of the block's shared memory, so that the next
+// sub-tile loads while this one is processed). Warp w owns the active rows
+// i = w, w + 8, ... of the tile (lane = point); per sub-tile
+//   A  the warp reads its rows' values into registers (kRegRows of them; rows
+//      past that, for tiles with more than 8 kRegRows active shells, are read
+//      again from the staging buffer) and sums G[m][p] x[m] over them in two
+//      compensated chains, merged into the warp's partial sum of u(p);
+//   A' warp 0 merges the eight partials in warp order and forms v(p) (and
+//      for MODE 1 s(p) and rho0(p)) for the sub-tile's points, published in
+//      shared memory; meanwhile warps 1-7 form the outer change (C below);
+//   B  every warp adds G[m][p] v(p) of its rows to compensated accumulators
+//      kept in registers across the tile (reduced once at its end) and, MODE
+//      1, writes its rows of X = G_hi diag(s) for the tensor-core Hessian;
+//      the owner warp of the sub-tile (sub mod 8) writes the per-point outputs
+//      and the entropy terms.
 // No FP64 arithmetic per point: w rho and rho come as float pairs (wrf, set
 // once per job), the outputs are float pairs.
 // MODE 0 (refinement product): x = delta, v = (w rho / rho0^2) u.
 // MODE 1 (promolecule + gradient): x = c, u = rho0 (r0f), d2 = w rho / rho0^2
-//   (d2f) and sqrt(d2) (hess_s), v = w rho / rho0, quotients in float-float;
-//   the owner also forms the entropy terms w rho ln(rho / rho0), ln from
-//   logf plus one Newton step on exp_ff (error ~ the square of logf's), and
-//   counts the points below negative_cutoff. With with_change, also
+//   (d2f) and v = w rho / rho0, quotients in float-float; the owner also forms
+//   the entropy terms w rho ln(rho / rho0), ln from logf plus one Newton step
+//   on exp_ff (error ~ the square of logf's), and counts the points below
+//   negative_cutoff. With with_change, also
 //   C  the outer change of the step that produced c (glisa.py:776 via
-//      compute_change): warp w takes the atoms a = w (mod 8), lane = point,
-//      sum_{m in a} (c - c_old)_m g_m from the staged sub-tile's G_hi in
-//      FP32 (the change is only compared with the threshold: ~1e-6
+//      compute_change): warps 1-7 take the atoms a = w - 1 (mod 7), lane =
+//      point, sum_{m in a} (c - c_old)_m g_m from the staged sub-tile's G_hi
+//      in FP32 (the change is only compared with the threshold: ~1e-6
 //      relative is ample), w times its square summed per thread as a float
 //      pair; the tile's total goes to atom 0's QA_CHANGE slot.
 // Jobs with more than kFuseMaxShells shells use k_glisa_pro_ff /
@@ -354,16 +361,19 @@ constexpr int kFuseThreads = 256;
 constexpr int kFuseWarps = kFuseThreads / 32;
 constexpr int kFuseSP = 32;                             // points per sub-tile (one per lane)
 constexpr int kFuseRows = kFuseMaxShells / kFuseWarps;  // rows per warp in B
+constexpr int kRegRows = 12;                            // rows per warp kept in registers
+// Shared memory of one block at most (two blocks per SM share 228 KB).
+constexpr size_t kFuseSmemMax = 112 * 1024;
 
-// Shared memory of a fused pass for S shells (bytes).
-__host__ __device__ constexpr size_t fuse_smem_bytes(int S) {
-  return 4 * (size_t)S * kFuseSP * 4          // two stages of both planes
-         + 16 * (size_t)S                     // x and the parameter change as float pairs
-         + 8 * (size_t)S                      // active-shell list and positions
-         + 4 * ((size_t)S + 1)                // per atom: its first active row
-         + 8 * (size_t)kFuseWarps * kFuseSP   // partial sums
-         + 512                                // exp table
-         + 8 * (2 * kFuseWarps + 2);          // block sums
+// Shared memory of a fused pass for S shells with nbuf staging buffers (bytes).
+__host__ __device__ constexpr size_t fuse_smem_bytes(int S, int nbuf) {
+  return 2 * (size_t)nbuf * S * kFuseSP * 4  // staging: both planes per buffer
+         + 16 * (size_t)S                    // x and the parameter change as float pairs
+         + 8 * (size_t)kFuseWarps * kFuseSP  // partial sums
+         + 32 * (size_t)kFuseSP              // per point: (v, s) and rho0
+         + 512                               // exp table
+         + 8 * (2 * kFuseWarps + 2)          // block sums
+         + 12 * (size_t)S + 8;               // active-shell list, positions, per-atom offsets
 }
 
 // Sub-tile [q0, q0 + kFuseSP) of the tile's active rows (act[0..nact), the
@@ -431,24 +441,30 @@ __host__ __device__ constexpr int fuse_x_rows(int S) {
   return (S + 15) / 16 * 16 > umma::kTcM ? (S + 15) / 16 * 16 : umma::kTcM;
 }
 constexpr size_t kFuseSmemFloor = 78 * 1024;
-__host__ __device__ constexpr size_t fuse_hess_smem_bytes(int S) {
-  return fuse_smem_bytes(S) + 128 * (size_t)fuse_x_rows(S) + 1024 + 64 > kFuseSmemFloor
-             ? fuse_smem_bytes(S) + 128 * (size_t)fuse_x_rows(S) + 1024 + 64
+__host__ __device__ constexpr size_t fuse_hess_smem_bytes(int S, int nbuf) {
+  return fuse_smem_bytes(S, nbuf) + 128 * (size_t)fuse_x_rows(S) + 1024 + 64 > kFuseSmemFloor
+             ? fuse_smem_bytes(S, nbuf) + 128 * (size_t)fuse_x_rows(S) + 1024 + 64
              : kFuseSmemFloor;
 }
 constexpr int kFuseTmemCols = 256;
+
+// Staging buffers of a fused pass over jobs of at most S shells: two when
+// the block's shared memory stays within kFuseSmemMax.
+__host__ __device__ constexpr int fuse_nbuf(int S, int mode) {
+  return (mode ? fuse_hess_smem_bytes(S, 2) : fuse_smem_bytes(S, 2)) <= kFuseSmemMax ? 2 : 1;
+}
+static_assert(fuse_hess_smem_bytes(kFuseMaxShells, 1) <= kFuseSmemMax, "fused pass shared memory");
 
 // Persistent blocks (launch kind K_FUSE): block b of a job takes the point
 // tiles b, b + nb, ... (nb = min(ntile, kFuseCtas)). The per-tile outputs
 // (gradient rows, entropy, change) stay per tile.
 //
 // MODE 1 also accumulates the Hessian H = X X^T of its tiles on the tensor
-// cores (glisa.py:457-470): after A' every warp knows s(p) = sqrt(w rho) /
-// rho0 (0 where sick) of the sub-tile's 32 points and writes its rows of X
-// (X[m][p] = G_hi[m][p] s(p), rounded to TF32 to nearest) into the
-// 128B-swizzled K-major tile in shared memory (the tile's inactive rows stay
-// zero); at the next block barrier thread 0 issues tcgen05.mma.kind::tf32
-// (M = 128, K = 8, four per sub-tile) for
+// cores (glisa.py:457-470): in B every warp writes its rows of X (X[m][p] =
+// G_hi[m][p] s(p), s(p) = sqrt(w rho) / rho0, 0 where sick, rounded to TF32
+// to nearest) into the 128B-swizzled K-major tile in shared memory (the
+// tile's inactive rows stay zero); at the next block barrier thread 0 issues
+// tcgen05.mma.kind::tf32 (M = 128, K = 8, four per sub-tile) for
 //   D1 (tensor-memory columns 0..n1-1):  A = X rows 0..127,        B = rows 0..n1-1,
 //   D2 (columns c2..c2+n1-129):          A = X rows n1-128..n1-1, B = rows 128..n1-1,
 // n1 = S rounded up to 16, c2 = n1 rounded up to 32 (D2 only when S > 128),
@@ -463,14 +479,15 @@ constexpr int kFuseTmemCols = 256;
 // is refined against the exact product in the finish (polish), and the
 // gradient and objective stay compensated.
 template <int MODE>
-__global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_fused_ff(Batch bt, int with_change) {
+__global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_fused_ff(Batch bt, int with_change, int nbuf) {
   extern __shared__ float4 fsm[];
   int local;
   const JobDev& J = decode_local_gf(bt, local);
   if (glisa_idle(J)) return;
   if (!J.fuse) return;
   if (MODE == 0 && !glisa_refine_now(J)) return;
-  const int nblk_job = bt.prefix[find_job(bt, blockIdx.x) + 1] - bt.prefix[find_job(bt, blockIdx.x)];
+  const int jb = find_job(bt, blockIdx.x);
+  const int nblk_job = bt.prefix[jb + 1] - bt.prefix[jb];
   const int S = J.nshell;
   const bool hess = MODE == 1;
   // MODE 1: the X tile first (1024-byte aligned), then the fused layout
@@ -479,12 +496,14 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_fused_ff(Batch bt, in
   const int xrows = fuse_x_rows(S);
   uint32_t* xt = reinterpret_cast<uint32_t*>(reinterpret_cast<uint8_t*>(fsm) + xoff);
   float* stg = hess ? reinterpret_cast<float*>(xt + 32 * xrows) : reinterpret_cast<float*>(fsm);
-  // stage k: high plane at stg + 2 k S kFuseSP, low plane S kFuseSP after it
+  // buffer k: high plane at stg + 2 k S kFuseSP, low plane S kFuseSP after it
   const int plane = S * kFuseSP;
-  float2* xv = reinterpret_cast<float2*>(stg + 4 * plane);
+  float2* xv = reinterpret_cast<float2*>(stg + 2 * nbuf * plane);
   float2* dcv = xv + S;
   Dot2* part = reinterpret_cast<Dot2*>(dcv + S);
-  float2* tab = reinterpret_cast<float2*>(part + kFuseWarps * kFuseSP);
+  float4* pvs = reinterpret_cast<float4*>(part + kFuseWarps * kFuseSP);  // (v hi, v lo, s, -)
+  float2* pr0 = reinterpret_cast<float2*>(pvs + kFuseSP);                 // rho0 pair
+  float2* tab = pr0 + 2 * kFuseSP;
   double* red = reinterpret_cast<double*>(tab + 64);
   int* act = reinterpret_cast<int*>(red + 2 * kFuseWarps + 2);
   int* pos = act + S;
@@ -568,8 +587,8 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_fused_ff(Batch bt, in
     __syncthreads();
     fuse_load(g32, glo, NN, p0, p1, stg, stg + plane, vec, act, nact);
     cp_async_commit();
-    if (MODE == 1)
-      for (int a = threadIdx.x; a <= J.natom; a += kFuseThreads) {
+    if (chg)
+      for (int a = threadIdx.x; a <= natom; a += kFuseThreads) {
         const int s0 = J.shell_off[a];
         int lo = 0, hi = nact;  // first active row with shell >= s0
         while (lo < hi) {
@@ -579,6 +598,12 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_fused_ff(Batch bt, in
         }
         aoff[a] = lo;
       }
+    // this warp's rows i = warp + 8 r, r < nr; with one staging buffer the
+    // next sub-tile loads once the rows are in registers, unless some rows
+    // are read from the buffer again in B (more than 8 kRegRows active rows)
+    // or the change reads it after A
+    const int nr = nact > warp ? (nact - warp + kFuseWarps - 1) / kFuseWarps : 0;
+    const bool early = nact <= kFuseWarps * kRegRows && !chg;
     float ch = 0.0f, cl = 0.0f;  // change terms of this thread (float pair)
     Dot2 acc[kFuseRows];
 #pragma unroll
@@ -586,104 +611,93 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_fused_ff(Batch bt, in
     f2 ent{0.f, 0.f};
     float nneg = 0.0f;
     for (int sub = 0; sub < nsub; ++sub) {
-      const float* gh = stg + (sub & 1) * 2 * plane;
+      const float* gh = stg + (nbuf == 2 ? (sub & 1) : 0) * 2 * plane;
       const float* gl = gh + plane;
+      const int q0 = p0 + sub * kFuseSP;
+      if (nbuf == 1 && sub > 0 && !early) {  // the buffer was read until the end of sub - 1
+        __syncthreads();
+        fuse_load(g32, glo, NN, q0, p1, stg, stg + plane, vec, act, nact);
+        cp_async_commit();
+      }
       cp_async_wait<0>();
       __syncthreads();  // sub-tile sub visible; every thread is done with sub - 1
       if (hess && sub > 0) {  // X of sub - 1 is complete: its MMAs
         if (threadIdx.x == 0 && !timed_out) issue_mma();
         ++nmma;
       }
-      // per-point inputs of A' and C, loaded before phase A so that their
-      // latency overlaps it
-      const int pq = p0 + sub * kFuseSP + lane;
+      // per-point inputs, loaded before phase A so that their latency
+      // overlaps it: (w rho, rho) pairs (MODE 1) or the d2 pair (MODE 0) for
+      // warp 0 and the sub-tile's owner, w for the change warps
+      const int pq = q0 + lane;
+      const bool owner = warp == (sub & (kFuseWarps - 1));
       float wf = 0.0f;
-      float4 qpre = make_float4(0.f, 0.f, 0.f, 0.f);  // MODE 1: (w rho) and rho pairs; MODE 0: d2 pair
+      float4 qpre = make_float4(0.f, 0.f, 0.f, 0.f);
       if (pq < p1) {
-        if (MODE == 1) qpre = wrfp[pq];
-        else {
-          const float2 d2 = d2in[pq];
-          qpre = make_float4(d2.x, d2.y, 0.f, 0.f);
+        if (warp == 0 || (MODE == 1 && owner)) {
+          if (MODE == 1) qpre = wrfp[pq];
+          else {
+            const float2 d2 = d2in[pq];
+            qpre = make_float4(d2.x, d2.y, 0.f, 0.f);
+          }
         }
-        if (chg) wf = (float)wp[pq];
+        if (chg && warp > 0) wf = (float)wp[pq];
       }
-      if (sub + 1 < nsub) {
-        float* nh = stg + ((sub + 1) & 1) * 2 * plane;  // last read in B of sub - 1
-        fuse_load(g32, glo, NN, p0 + (sub + 1) * kFuseSP, p1, nh, nh + plane, vec, act, nact);
+      if (nbuf == 2 && sub + 1 < nsub) {
+        float* nh = stg + ((sub + 1) & 1) * 2 * plane;  // last read in sub - 1
+        fuse_load(g32, glo, NN, q0 + kFuseSP, p1, nh, nh + plane, vec, act, nact);
         cp_async_commit();
       }
-      {  // A (active rows i = warp mod 8)
+      // A: rows r even in chain d, odd in chain e
+      float rh[kRegRows], rl[kRegRows];
+      {
         Dot2 d{0.f, 0.f}, e{0.f, 0.f};
-        int i = warp;
-        for (; i + kFuseWarps < nact; i += 2 * kFuseWarps) {
-          const float2 x1 = xv[act[i]], x2 = xv[act[i + kFuseWarps]];
-          dot2_add(d, gh[i * kFuseSP + lane], gl[i * kFuseSP + lane], x1.x, x1.y);
-          const int i2 = i + kFuseWarps;
-          dot2_add(e, gh[i2 * kFuseSP + lane], gl[i2 * kFuseSP + lane], x2.x, x2.y);
+#pragma unroll
+        for (int r = 0; r < kRegRows; ++r) {
+          rh[r] = 0.0f;
+          rl[r] = 0.0f;
+          if (r < nr) {
+            const int i = warp + kFuseWarps * r;
+            const float2 xx = xv[act[i]];
+            rh[r] = gh[i * kFuseSP + lane];
+            rl[r] = gl[i * kFuseSP + lane];
+            if (r & 1) dot2_add(e, rh[r], rl[r], xx.x, xx.y);
+            else dot2_add(d, rh[r], rl[r], xx.x, xx.y);
+          }
         }
-        if (i < nact) {
-          const float2 x1 = xv[act[i]];
-          dot2_add(d, gh[i * kFuseSP + lane], gl[i * kFuseSP + lane], x1.x, x1.y);
+        for (int r = kRegRows; r < nr; ++r) {
+          const int i = warp + kFuseWarps * r;
+          const float2 xx = xv[act[i]];
+          if (r & 1) dot2_add(e, gh[i * kFuseSP + lane], gl[i * kFuseSP + lane], xx.x, xx.y);
+          else dot2_add(d, gh[i * kFuseSP + lane], gl[i * kFuseSP + lane], xx.x, xx.y);
         }
         dot2_merge(d, e);
         part[warp * kFuseSP + lane] = d;
       }
       __syncthreads();  // partial sums visible
-      // A': every warp merges the eight partial sums (the same fixed order) and
-      // forms v for the sub-tile's points itself; warp sub % 8 (the owner) also
-      // writes the per-point outputs and, MODE 1, the entropy terms
-      Dot2 du = part[lane];
+      if (warp == 0) {
+        // A': the eight partial sums merged in warp order; v (and s, rho0)
+        Dot2 du = part[lane];
 #pragma unroll
-      for (int q = 1; q < kFuseWarps; ++q) dot2_merge(du, part[q * kFuseSP + lane]);
-      const int p = p0 + sub * kFuseSP + lane;
-      const bool owner = warp == (sub & (kFuseWarps - 1));
-      f2 v{0.f, 0.f};
-      float sx = 0.0f;  // MODE 1: s(p) = sqrt(w rho) / rho0 for X
-      if (p < p1) {
-        if (MODE == 0) {
-          v = ffa::mul(dot2_ff(du), f2{qpre.x, qpre.y});
-        } else {
-          const f2 r0 = dot2_ff(du);
-          const float4 q = qpre;  // (w rho) and rho as float pairs
-          const bool sick = below(f2{q.z, q.w}, cutp) || below(r0, cutp);
-          if (!sick) {
-            v = ffa::div(f2{q.x, q.y}, r0);
-            sx = sqrtf(q.x) / r0.hi;
-          }
-          if (owner) {
-            const f2 dd = sick ? f2{0.f, 0.f} : ffa::div(v, r0);
-            r0fo[p] = make_float2(r0.hi, r0.lo);
-            d2fo[p] = make_float2(dd.hi, dd.lo);
-            if (below(r0, negp)) nneg += 1.0f;
-            if (!sick) {  // w rho ln(rho / rho0)
-              const f2 ratio = ffa::div(f2{q.z, q.w}, r0);
-              const float l0 = logf(ratio.hi);
-              const f2 e = ffa::exp_ff(f2{-l0, 0.f}, tab);
-              const f2 l = ffa::add(ffa::add(ffa::mul(ratio, e), -1.0f), l0);
-              ent = ffa::add(ent, ffa::mul(f2{q.x, q.y}, l));
+        for (int q = 1; q < kFuseWarps; ++q) dot2_merge(du, part[q * kFuseSP + lane]);
+        f2 v{0.f, 0.f}, r0{0.f, 0.f};
+        float sx = 0.0f;
+        if (pq < p1) {
+          if (MODE == 0) {
+            v = ffa::mul(dot2_ff(du), f2{qpre.x, qpre.y});
+          } else {
+            r0 = dot2_ff(du);
+            const bool sick = below(f2{qpre.z, qpre.w}, cutp) || below(r0, cutp);
+            if (!sick) {
+              v = ffa::div(f2{qpre.x, qpre.y}, r0);
+              sx = sqrtf(qpre.x) / r0.hi;
             }
           }
         }
-      }
-      if (hess) {  // X rows of the active shells i = warp + 8 r, column lane
-        wait_mma();  // the MMAs of sub - 1 have read the X tile
-        const uint32_t sw = (uint32_t)(lane & 3);
-        for (int i = warp; i < nact; i += kFuseWarps) {
-          const int m = act[i];
-          const uint32_t off = (uint32_t)(m * 32) + ((((uint32_t)lane >> 2) ^ (uint32_t)(m & 7)) << 2) + sw;
-          xt[off] = umma::to_tf32_rn(gh[i * kFuseSP + lane] * sx);
-        }
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      }
-      {  // B (active rows i = warp + 8 r)
-#pragma unroll
-        for (int r = 0; r < kFuseRows; ++r) {
-          const int i = warp + kFuseWarps * r;
-          if (i < nact) dot2_add(acc[r], gh[i * kFuseSP + lane], gl[i * kFuseSP + lane], v.hi, v.lo);
-        }
-      }
-      if (chg) {  // C (atoms with no active row add exact zeros: skipped)
-        for (int a = warp; a < natom; a += kFuseWarps) {
+        pvs[lane] = make_float4(v.hi, v.lo, sx, 0.f);
+        pr0[lane] = make_float2(r0.hi, r0.lo);
+      } else if (chg) {
+        // C (atoms with no active row add exact zeros: skipped)
+        for (int a = warp - 1; a < natom; a += kFuseWarps - 1) {
           const int i0 = aoff[a], i1 = aoff[a + 1];
           if (i0 == i1) continue;
           float dv = 0.0f;
@@ -695,6 +709,55 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_fused_ff(Batch bt, in
           ch = t;
         }
       }
+      __syncthreads();  // v, s and rho0 of the sub-tile visible
+      if (nbuf == 1 && early && sub + 1 < nsub) {  // rows in registers: the buffer is free
+        fuse_load(g32, glo, NN, q0 + kFuseSP, p1, stg, stg + plane, vec, act, nact);
+        cp_async_commit();
+      }
+      const float4 pv = pvs[lane];
+      const f2 v{pv.x, pv.y};
+      const float sx = pv.z;
+      if (MODE == 1 && owner && pq < p1) {
+        // per-point outputs and the entropy term w rho ln(rho / rho0)
+        const float2 r0s = pr0[lane];
+        const f2 r0{r0s.x, r0s.y};
+        const bool sick = below(f2{qpre.z, qpre.w}, cutp) || below(r0, cutp);
+        const f2 dd = sick ? f2{0.f, 0.f} : ffa::div(v, r0);
+        r0fo[pq] = r0s;
+        d2fo[pq] = make_float2(dd.hi, dd.lo);
+        if (below(r0, negp)) nneg += 1.0f;
+        if (!sick) {
+          const f2 ratio = ffa::div(f2{qpre.z, qpre.w}, r0);
+          const float l0 = logf(ratio.hi);
+          const f2 e = ffa::exp_ff(f2{-l0, 0.f}, tab);
+          const f2 l = ffa::add(ffa::add(ffa::mul(ratio, e), -1.0f), l0);
+          ent = ffa::add(ent, ffa::mul(f2{qpre.x, qpre.y}, l));
+        }
+      }
+      if (hess) wait_mma();  // the MMAs of sub - 1 have read the X tile
+      // B (and the rows of X)
+      const uint32_t sw = (uint32_t)(lane & 3);
+#pragma unroll
+      for (int r = 0; r < kFuseRows; ++r) {
+        if (r < nr) {
+          const int i = warp + kFuseWarps * r;
+          float g1, g2;
+          if (r < kRegRows) {
+            g1 = rh[r];
+            g2 = rl[r];
+          } else {
+            g1 = gh[i * kFuseSP + lane];
+            g2 = gl[i * kFuseSP + lane];
+          }
+          if (hess) {
+            const int m = act[i];
+            const uint32_t off = (uint32_t)(m * 32) + ((((uint32_t)lane >> 2) ^ (uint32_t)(m & 7)) << 2) + sw;
+            xt[off] = umma::to_tf32_rn(g1 * sx);
+          }
+          dot2_add(acc[r], g1, g2, v.hi, v.lo);
+        }
+      }
+      if (hess) asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     }
     if (hess) {  // the tile's last sub-tile
       __syncthreads();
@@ -804,12 +867,27 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_fused_ff(Batch bt, in
 }
 
 // Trial objective differences for fused jobs: k_glisa_u_ff and
-// k_glisa_trials_ff in one pass over staged sub-tiles (as k_glisa_fused_ff).
-// Per sub-tile: A forms u = G^T delta (eight partial sums per point); T: warp
-// t evaluates trial t for the 32 points (lane = point), with the clipped
-// shells' corrections read from the staged sub-tile, and keeps its sum in
-// registers; the tile's eight sums go to tpart at its end.
+// k_glisa_trials_ff in one pass over staged sub-tiles (as k_glisa_fused_ff,
+// two staging buffers). Per sub-tile: A forms the eight warps' partial sums
+// of u = G^T delta and C the clipped-shell group sums (warp g: group g);
+// then warp 0 merges the partials (warp order) into u and the groups into
+// their suffix sums (group kTrials - 1 first), so that trial t reads the sum
+// of the groups t..kTrials-1 at once; T: warp t evaluates trial t for the 32
+// points (lane = point) and keeps its sum in registers; the tile's eight sums
+// go to tpart at its end.
 static_assert(kTrials == kFuseWarps, "one warp per trial step");
+
+// Shared memory of the trial pass for S shells (bytes).
+__host__ __device__ constexpr size_t trials_smem_bytes(int S) {
+  return 4 * (size_t)S * kFuseSP * 4                // two staging buffers, both planes
+         + 16 * (size_t)kTrials * kFuseSP           // group sums, then their suffix sums
+         + 8 * (size_t)kFuseWarps * kFuseSP         // partial sums of u
+         + 8 * (size_t)kFuseSP                      // u per point
+         + 512                                      // exp table
+         + 8 * (size_t)S                            // delta as float pairs
+         + 12 * (size_t)S + 16;                     // act, pos, clipped shells' rows
+}
+static_assert(trials_smem_bytes(kFuseMaxShells) <= kFuseSmemMax, "trial pass shared memory");
 
 __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_trials_fused(Batch bt) {
   extern __shared__ float4 fsm[];
@@ -820,10 +898,12 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_trials_fused(Batch bt
   const int S = J.nshell;
   float* stg = reinterpret_cast<float*>(fsm);
   const int plane = S * kFuseSP;
-  float2* xv = reinterpret_cast<float2*>(stg + 4 * plane);
-  Dot2* part = reinterpret_cast<Dot2*>(xv + 2 * S);
-  int* act = reinterpret_cast<int*>(reinterpret_cast<float2*>(part + kFuseWarps * kFuseSP) + 64) +
-             2 * (2 * kFuseWarps + 2);  // after the exp table and block sums of the fused layout
+  float4* grp = reinterpret_cast<float4*>(stg + 4 * plane);  // [kTrials][kFuseSP]
+  Dot2* part = reinterpret_cast<Dot2*>(grp + kTrials * kFuseSP);
+  float2* uv = reinterpret_cast<float2*>(part + kFuseWarps * kFuseSP);
+  float2* tab = uv + kFuseSP;  // exp table
+  float2* xv = tab + 64;
+  int* act = reinterpret_cast<int*>(xv + S);
   int* pos = act + S;
   int* cpos = pos + S;  // per clipped shell its active row on this tile (-1: zero here)
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -850,7 +930,6 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_trials_fused(Batch bt
   // g + 1, the list segment [ktab[g + 1], ktab[g]) (group kTrials - 1 from
   // 0), is clipped in the trials t <= g
   __shared__ int ktab[kTrials];
-  __shared__ float4 grp[kTrials][kFuseSP];  // per group and point: (sum c g, sum delta g) pairs
   if (threadIdx.x < kTrials) {
     int k = 0;
     while (k < nclip && tm[k] > (int)threadIdx.x) ++k;
@@ -859,7 +938,6 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_trials_fused(Batch bt
   for (int k = threadIdx.x; k < nclip; k += kFuseThreads) cpos[k] = pos[J.clip[k]];
   const float4* cd = reinterpret_cast<const float4*>(J.clipf);
   const float2 cutp = split2(J.density_cutoff);
-  float2* tab = reinterpret_cast<float2*>(part + kFuseWarps * kFuseSP);  // exp table
   if (threadIdx.x < 64) tab[threadIdx.x] = c_exp2_gl[threadIdx.x];
   float ah = 0.0f, al = 0.0f;
   for (int sub = 0; sub < nsub; ++sub) {
@@ -907,23 +985,33 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_trials_fused(Batch bt
         dot2_add(sc, g1, g2, v.x, v.y);
         dot2_add(sd, g1, g2, v.z, v.w);
       }
-      grp[g][lane] = make_float4(sc.s, sc.c, sd.s, sd.c);
+      grp[g * kFuseSP + lane] = make_float4(sc.s, sc.c, sd.s, sd.c);
     }
     __syncthreads();
-    const int p = p0 + sub * kFuseSP + lane;
-    if (p < p1) {  // T
+    if (warp == 0) {  // u and the groups' suffix sums
       Dot2 du = part[lane];
 #pragma unroll
       for (int q = 1; q < kFuseWarps; ++q) dot2_merge(du, part[q * kFuseSP + lane]);
       const f2 u = dot2_ff(du);
-      Dot2 sc{0.f, 0.f}, sd{0.f, 0.f};  // groups t .. kTrials - 1, in that order
-      for (int g = t; g < kTrials; ++g) {
-        const float4 v = grp[g][lane];
+      uv[lane] = make_float2(u.hi, u.lo);
+      float4 v = grp[(kTrials - 1) * kFuseSP + lane];
+      Dot2 sc{v.x, v.y}, sd{v.z, v.w};
+#pragma unroll
+      for (int g = kTrials - 2; g >= 0; --g) {
+        v = grp[g * kFuseSP + lane];
         dot2_merge(sc, Dot2{v.x, v.y});
         dot2_merge(sd, Dot2{v.z, v.w});
+        grp[g * kFuseSP + lane] = make_float4(sc.s, sc.c, sd.s, sd.c);
       }
-      const f2 dsd = dot2_ff(sd);
-      const f2 corr = ffa::neg(ffa::add(dot2_ff(sc), f2{at * dsd.hi, at * dsd.lo}));
+    }
+    __syncthreads();
+    const int p = pq;
+    if (p < p1) {  // T
+      const float2 uu = uv[lane];
+      const f2 u{uu.x, uu.y};
+      const float4 gs = grp[t * kFuseSP + lane];  // groups t .. kTrials - 1
+      const f2 dsd = dot2_ff(Dot2{gs.z, gs.w});
+      const f2 corr = ffa::neg(ffa::add(dot2_ff(Dot2{gs.x, gs.y}), f2{at * dsd.hi, at * dsd.lo}));
       const float2 r0p = r0pre;
       const float4 q = qpre;  // (w rho) and rho as float pairs
       const bool rs = below(f2{q.z, q.w}, cutp);
@@ -1094,11 +1182,11 @@ void ensure_exp_table_gl() {
   }
   cudaMemcpyToSymbol(c_exp2_gl, t, sizeof(t));
   cudaFuncSetAttribute(k_glisa_fused_ff<0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       (int)fuse_smem_bytes(kFuseMaxShells));
+                       (int)kFuseSmemMax);
   cudaFuncSetAttribute(k_glisa_fused_ff<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       (int)fuse_hess_smem_bytes(kFuseMaxShells));
+                       (int)kFuseSmemMax);
   cudaFuncSetAttribute(k_glisa_trials_fused, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       (int)fuse_smem_bytes(kFuseMaxShells));
+                       (int)kFuseSmemMax);
   if (dev < 31) done_mask |= 1 << dev;
 }
 
@@ -1108,19 +1196,20 @@ void launch_glisa_fused_ff(const HostBatch& hb, cudaStream_t st, int mode, int m
                            int with_change) {
   if (hb.blocks[K_FUSE] <= 0) return;
   ensure_exp_table_gl();
+  const int nbuf = fuse_nbuf(max_shells, mode);
   if (mode)
-    k_glisa_fused_ff<1><<<hb.blocks[K_FUSE], kFuseThreads, fuse_hess_smem_bytes(max_shells), st>>>(
-        hb.b[K_FUSE], with_change);
+    k_glisa_fused_ff<1><<<hb.blocks[K_FUSE], kFuseThreads, fuse_hess_smem_bytes(max_shells, nbuf),
+                          st>>>(hb.b[K_FUSE], with_change, nbuf);
   else
-    k_glisa_fused_ff<0><<<hb.blocks[K_FUSE], kFuseThreads, fuse_smem_bytes(max_shells), st>>>(
-        hb.b[K_FUSE], 0);
+    k_glisa_fused_ff<0><<<hb.blocks[K_FUSE], kFuseThreads, fuse_smem_bytes(max_shells, nbuf), st>>>(
+        hb.b[K_FUSE], 0, nbuf);
   ++g_launch_count;
 }
 
 void launch_glisa_trials_fused(const HostBatch& hb, cudaStream_t st, int max_shells) {
   if (hb.blocks[K_POINT] <= 0) return;
   ensure_exp_table_gl();
-  k_glisa_trials_fused<<<hb.blocks[K_POINT], kFuseThreads, fuse_smem_bytes(max_shells), st>>>(
+  k_glisa_trials_fused<<<hb.blocks[K_POINT], kFuseThreads, trials_smem_bytes(max_shells), st>>>(
       hb.b[K_POINT]);
   ++g_launch_count;
 }

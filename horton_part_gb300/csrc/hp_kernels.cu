@@ -1357,32 +1357,40 @@ __global__ void __launch_bounds__(kReduceThreads) k_glisa_reduce(Batch bt) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int nblk = (M * M + kThreads - 1) / kThreads;  // this job's K_SQUARE blocks
   if (J.tc && M <= kTcSinglePassShells) {
-    // FP32 packed lower triangles of the single-pass tensor-core kernel: a
-    // chunk of 32 elements per pass of the block, warp w summing the point
-    // ranges w, w + 32, ... (coalesced loads, compensated FP32 sums), the
-    // warps' sums combined in FP64 in warp order
+    // FP32 packed lower triangles of the single-pass tensor-core kernels.
+    // The triangle's E elements form chunks of 32 (lane = element); the block
+    // takes G = ceil(chunks / nblk) chunks at once, W = warps / G warps per
+    // chunk, warp sub of a chunk summing the splits sub, sub + W, ... (16
+    // loads in flight per lane, compensated FP32 sums in split order); the
+    // W partials of a chunk are combined in FP64 in warp order. G and W
+    // depend only on the shell count, so the order is fixed per job.
     __shared__ double wsum[kReduceWarps][32];
     const int E = M * (M + 1) / 2;
+    const int chunks = (E + 31) / 32;
+    const int G = min((chunks + nblk - 1) / nblk, kReduceWarps);
+    const int W = kReduceWarps / G;
     const float* hp = reinterpret_cast<const float*>(J.hpart);
-    for (int c = local; c < (E + 31) / 32; c += nblk) {
+    for (int c0 = local * G; c0 < chunks; c0 += nblk * G) {
+      const int g = warp / W, sub = warp - g * W;
+      const int c = c0 + g;
       const int ec = c * 32 + lane;
       float s = 0.0f, cc = 0.0f;
-      if (ec < E) {
-        // four loads in flight per lane, added in split order
-        int sp = warp;
-        for (; sp + 3 * kReduceWarps < J.nsplit; sp += 4 * kReduceWarps) {
-          float x[4];
+      if (g < G && c < chunks && ec < E) {
+        constexpr int kU = 16;
+        int sp = sub;
+        for (; sp + (kU - 1) * W < J.nsplit; sp += kU * W) {
+          float x[kU];
 #pragma unroll
-          for (int u = 0; u < 4; ++u) x[u] = hp[(size_t)(sp + u * kReduceWarps) * E + ec];
+          for (int u = 0; u < kU; ++u) x[u] = hp[(size_t)(sp + u * W) * E + ec];
 #pragma unroll
-          for (int u = 0; u < 4; ++u) {
+          for (int u = 0; u < kU; ++u) {
             const float t = s + x[u];
             const float bb = t - s;
             cc += (s - (t - bb)) + (x[u] - bb);
             s = t;
           }
         }
-        for (; sp < J.nsplit; sp += kReduceWarps) {
+        for (; sp < J.nsplit; sp += W) {
           const float x = hp[(size_t)sp * E + ec];
           const float t = s + x;
           const float bb = t - s;
@@ -1392,16 +1400,19 @@ __global__ void __launch_bounds__(kReduceThreads) k_glisa_reduce(Batch bt) {
       }
       wsum[warp][lane] = (double)s + (double)cc;
       __syncthreads();
-      if (warp == 0 && ec < E) {
-        double v = 0.0;
-#pragma unroll
-        for (int w = 0; w < kReduceWarps; ++w) v += wsum[w][lane];
-        int i = (int)((sqrtf(8.0f * (float)ec + 1.0f) - 1.0f) * 0.5f);
-        while (i * (i + 1) / 2 > ec) --i;
-        while ((i + 1) * (i + 2) / 2 <= ec) ++i;
-        const int j = ec - i * (i + 1) / 2;
-        J.hess[(size_t)i * M + j] = v;
-        J.hess[(size_t)j * M + i] = v;
+      if (warp < G) {
+        const int cw = c0 + warp;
+        const int ew = cw * 32 + lane;
+        if (cw < chunks && ew < E) {
+          double v = 0.0;
+          for (int q = 0; q < W; ++q) v += wsum[warp * W + q][lane];
+          int i = (int)((sqrtf(8.0f * (float)ew + 1.0f) - 1.0f) * 0.5f);
+          while (i * (i + 1) / 2 > ew) --i;
+          while ((i + 1) * (i + 2) / 2 <= ew) ++i;
+          const int j = ew - i * (i + 1) / 2;
+          J.hess[(size_t)i * M + j] = v;
+          J.hess[(size_t)j * M + i] = v;
+        }
       }
       __syncthreads();
     }

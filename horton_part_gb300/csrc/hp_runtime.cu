@@ -240,7 +240,7 @@ int status_of(int err) {
 }
 
 const char* err_text(int err) {
-  if (err & E_TIMEOUT) return "tensor-core Hessian: a bounded device wait ran out";
+  if (err & E_TIMEOUT) return "tensor-core Hessian: a bounded device wait ran out; MMAs issued before it may not have retired, so treat this context as suspect and recreate it";
   if (err & E_NEG_DENSITY) return "Negative pro-atom density found!";
   if (err & E_SINGULAR) return "Hessian is not positive definite (singular Newton system)";
   if (err & E_LINESEARCH) return "Line search failed!";

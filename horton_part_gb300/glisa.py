@@ -125,7 +125,7 @@ class GlobalLinearISAWPart(GPUStockholderWPart):
         if name != "quasi-newton":
             ents = [job.evaluate(h, 0)[0] for h in hist]
         job.finish(x, niter)
-        return {"history_propars": np.array(hist).reshape(len(hist), -1),
+        return {"history_propars": np.array(hist, dtype=float).reshape(len(hist), x0.size),
                 "history_entropies": np.array(ents), "history_changes": np.array(changes or []),
                 "history_charges": np.zeros((0, self.natom))}
 

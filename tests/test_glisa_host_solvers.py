@@ -114,3 +114,35 @@ def test_host_solver_logic_matches_the_reference(setup, solver):
     assert dq < 1e-8
     if int(g["niter"]) >= 0:
         assert niter == int(g["niter"])
+
+
+class _FakeJob(NumpyEvaluator):
+    """A device job stand-in for ``GlobalLinearISAWPart._run_job``: the NumPy
+    evaluation service plus the ``finish`` call that ends a host-driven job."""
+
+    def finish(self, x, niter):
+        self.finished = (np.array(x), int(niter))
+
+
+@pytest.mark.parametrize("solver", HOST_CASES)
+def test_class_runs_the_host_solver_and_returns_histories(solver):
+    """The class's host-solver driver on the NumPy service: the solver's end
+    point reaches ``finish`` and the histories have the reference's shapes
+    (trust-region keeps none)."""
+    from horton_part_gb300.utils import wpart_schemes
+
+    mol = build_host_inputs()
+    part = wpart_schemes("glisa")(mol.coordinates, mol.numbers, mol.pseudo_numbers, mol.grid,
+                                  mol.density, grid_type=3, solver=solver, threshold=1e-8)
+    job = _FakeJob(mol, ExpBasisFuncHelper.from_function_type("gauss"))
+    hist = part._run_job(job)
+    x, niter = job.finished
+    nshell = job.G.shape[0]
+    assert x.shape == (nshell,) and niter > 0
+    assert hist["history_propars"].ndim == 2 and hist["history_propars"].shape[1] == nshell
+    assert len(hist["history_entropies"]) == len(hist["history_propars"])
+    if solver == "trust-region":
+        assert hist["history_propars"].shape[0] == 0
+    else:
+        assert hist["history_propars"].shape[0] > 0
+        np.testing.assert_allclose(hist["history_propars"][-1].sum(), x.sum(), rtol=1e-6)

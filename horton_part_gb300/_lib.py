@@ -70,6 +70,14 @@ class JobResults(ctypes.Structure):
         "history_changes", "promoldens", "at_weights")]
 
 
+class DensityDesc(ctypes.Structure):
+    _fields_ = [
+        ("nshell", ctypes.c_int32), ("centers", _dp), ("shell_info", _ip), ("nprim", ctypes.c_int32),
+        ("exponents", _dp), ("coeffs", _dp), ("nbasis", ctypes.c_int32), ("nmat", ctypes.c_int32),
+        ("mats", _dp), ("pure2", _dp), ("pure3", _dp),
+    ]
+
+
 class HPError(RuntimeError):
     def __init__(self, code, msg):
         super().__init__(msg)
@@ -81,7 +89,9 @@ EXPORTED = ("hp_abi_version", "hp_last_error", "hp_ctx_create", "hp_ctx_destroy"
             "hp_step_n",
             "hp_job_run", "hp_job_info_get", "hp_job_results_get", "hp_job_reset",
             "hp_ctx_profile", "hp_ctx_profile_get", "hp_mbis_inner_noalloc", "hp_glisa_evaluate",
-            "hp_glisa_change", "hp_glisa_line_search", "hp_glisa_finish")
+            "hp_glisa_change", "hp_glisa_line_search", "hp_glisa_finish",
+            "hp_density_plan_create", "hp_density_plan_eval", "hp_density_plan_stats",
+            "hp_density_plan_destroy")
 
 KERNEL_FAMILIES = {"promol": 0, "inner": 1, "change": 2, "glisa_pro": 3, "glisa_grad": 4,
                    "glisa_hess": 5, "glisa_solve": 6, "other": 7, "glisa_trials": 8}
@@ -128,6 +138,12 @@ def lib():
         L.hp_glisa_change.argtypes = [ctypes.c_void_p, _dp, _dp, ctypes.c_int32, _dp]
         L.hp_glisa_line_search.argtypes = [ctypes.c_void_p, _dp, _dp, _dp, _dp, _dp]
         L.hp_glisa_finish.argtypes = [ctypes.c_void_p, _dp, ctypes.c_int32]
+        L.hp_density_plan_create.argtypes = [ctypes.c_void_p, ctypes.POINTER(DensityDesc),
+                                             ctypes.POINTER(ctypes.c_void_p)]
+        L.hp_density_plan_eval.argtypes = [ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
+                                           ctypes.c_void_p, ctypes.c_int32]
+        L.hp_density_plan_stats.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint64)]
+        L.hp_density_plan_destroy.argtypes = [ctypes.c_void_p]
         L.hp_ctx_profile_get.argtypes = [ctypes.c_void_p, ctypes.c_int32,
                                          ctypes.POINTER(ctypes.c_double),
                                          ctypes.POINTER(ctypes.c_int64)]

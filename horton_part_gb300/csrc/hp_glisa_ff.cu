@@ -368,12 +368,11 @@ constexpr size_t kFuseSmemMax = 112 * 1024;
 // Shared memory of a fused pass for S shells with nbuf staging buffers (bytes).
 __host__ __device__ constexpr size_t fuse_smem_bytes(int S, int nbuf) {
   return 2 * (size_t)nbuf * S * kFuseSP * 4  // staging: both planes per buffer
-         + 16 * (size_t)S                    // x and the parameter change as float pairs
+         + 16 * (size_t)S                    // per active row: x pair and the parameter change
          + 8 * (size_t)kFuseWarps * kFuseSP  // partial sums
-         + 32 * (size_t)kFuseSP              // per point: (v, s) and rho0
-         + 512                               // exp table
+         + 32 * (size_t)kFuseSP              // per point: (v, s)
          + 8 * (2 * kFuseWarps + 2)          // block sums
-         + 12 * (size_t)S + 8;               // active-shell list, positions, per-atom offsets
+         + 16 * (size_t)S + 8;               // active shells, positions, per-atom offsets, X keys
 }
 
 // Sub-tile [q0, q0 + kFuseSP) of the tile's active rows (act[0..nact), the
@@ -457,7 +456,7 @@ static_assert(fuse_hess_smem_bytes(kFuseMaxShells, 1) <= kFuseSmemMax, "fused pa
 
 // Persistent blocks (launch kind K_FUSE): block b of a job takes the point
 // tiles b, b + nb, ... (nb = min(ntile, kFuseCtas)). The per-tile outputs
-// (gradient rows, entropy, change) stay per tile.
+// (gradient rows, change) stay per tile.
 //
 // MODE 1 also accumulates the Hessian H = X X^T of its tiles on the tensor
 // cores (glisa.py:457-470): in B every warp writes its rows of X (X[m][p] =
@@ -478,6 +477,13 @@ static_assert(fuse_hess_smem_bytes(kFuseMaxShells, 1) <= kFuseSmemMax, "fused pa
 // operands, FP32 accumulation of non-negative terms); the Newton direction
 // is refined against the exact product in the finish (polish), and the
 // gradient and objective stay compensated.
+//
+// Per tile the active rows' values that every sub-tile needs are compacted
+// once: x[act[i]] (xa), the X-tile word of row act[i] for lane 0 (xkey; the
+// 128B swizzle makes lane l's word xkey ^ l) and the parameter change
+// (dca), so that the row loops read them at fixed offsets.
+// MODE 1 writes rho0 (r0f); the entropy, the negativity count and w rho /
+// rho0^2 (d2f) follow in k_glisa_point_ff.
 template <int MODE>
 __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_fused_ff(Batch bt, int with_change, int nbuf) {
   extern __shared__ float4 fsm[];
@@ -498,20 +504,19 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_fused_ff(Batch bt, in
   float* stg = hess ? reinterpret_cast<float*>(xt + 32 * xrows) : reinterpret_cast<float*>(fsm);
   // buffer k: high plane at stg + 2 k S kFuseSP, low plane S kFuseSP after it
   const int plane = S * kFuseSP;
-  float2* xv = reinterpret_cast<float2*>(stg + 2 * nbuf * plane);
-  float2* dcv = xv + S;
-  Dot2* part = reinterpret_cast<Dot2*>(dcv + S);
+  float2* xa = reinterpret_cast<float2*>(stg + 2 * nbuf * plane);  // x of active row i
+  float* dca = reinterpret_cast<float*>(xa + S);                   // change of active row i
+  Dot2* part = reinterpret_cast<Dot2*>(dca + 2 * S);
   float4* pvs = reinterpret_cast<float4*>(part + kFuseWarps * kFuseSP);  // (v hi, v lo, s, -)
-  float2* pr0 = reinterpret_cast<float2*>(pvs + kFuseSP);                 // rho0 pair
-  float2* tab = pr0 + 2 * kFuseSP;
-  double* red = reinterpret_cast<double*>(tab + 64);
+  double* red = reinterpret_cast<double*>(pvs + 2 * kFuseSP);
   int* act = reinterpret_cast<int*>(red + 2 * kFuseWarps + 2);
   int* pos = act + S;
   int* aoff = pos + S;  // atom a's active rows: [aoff[a], aoff[a + 1]) (act is ordered by shell)
-  uint64_t* mbar = reinterpret_cast<uint64_t*>((reinterpret_cast<uintptr_t>(aoff + S + 2) + 15) & ~uintptr_t(15));
+  int* xkey = aoff + S + 2;
+  uint64_t* mbar = reinterpret_cast<uint64_t*>((reinterpret_cast<uintptr_t>(xkey + S) + 15) & ~uintptr_t(15));
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(mbar + 1);
   __shared__ volatile int timed_out;
-  const float2 cutp = split2(J.density_cutoff), negp = split2(J.negative_cutoff);
+  const float2 cutp = split2(J.density_cutoff);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const bool vec = (J.npoint & 3) == 0;
   const float* __restrict__ g32 = J.gmat32;
@@ -521,7 +526,6 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_fused_ff(Batch bt, in
   const float2* __restrict__ d2in = J.d2f;
   const double* __restrict__ wp = J.w;
   float2* r0fo = J.r0f;
-  float2* d2fo = J.d2f;
   const int natom = J.natom;
   const int n1 = (S + 15) / 16 * 16;
   const int c2 = (n1 + 31) / 32 * 32;
@@ -550,16 +554,16 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_fused_ff(Batch bt, in
   // that follows the writers' proxy fences).
   auto issue_mma = [&]() {
     asm volatile("tcgen05.fence::after_thread_sync;");
-    const uint32_t xa = umma::smem_u32(xt);
+    const uint32_t xs = umma::smem_u32(xt);
     const uint32_t id1 = umma::idesc_tf32(n1);
     const uint32_t id2 = umma::idesc_tf32(has_d2 ? n1 - umma::kTcM : 16);
 #pragma unroll
     for (int kk = 0; kk < kFuseSP / 8; ++kk) {
       const uint32_t acc = (nmma > 0 || kk > 0) ? 1u : 0u;
-      umma::umma_tf32(tmem, umma::umma_desc(xa + 32 * kk), umma::umma_desc(xa + 32 * kk), id1, acc);
+      umma::umma_tf32(tmem, umma::umma_desc(xs + 32 * kk), umma::umma_desc(xs + 32 * kk), id1, acc);
       if (has_d2)
-        umma::umma_tf32(tmem + (uint32_t)c2, umma::umma_desc(xa + (n1 - umma::kTcM) * 128 + 32 * kk),
-                        umma::umma_desc(xa + umma::kTcM * 128 + 32 * kk), id2, acc);
+        umma::umma_tf32(tmem + (uint32_t)c2, umma::umma_desc(xs + (n1 - umma::kTcM) * 128 + 32 * kk),
+                        umma::umma_desc(xs + umma::kTcM * 128 + 32 * kk), id2, acc);
     }
     umma::umma_commit(bar);
   };
@@ -567,12 +571,8 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_fused_ff(Batch bt, in
   auto wait_mma = [&]() {
     if (nmma > 0 && !timed_out && !umma::mbar_wait(bar, (uint32_t)((nmma - 1) & 1))) timed_out = 1;
   };
-  if (MODE == 1 && threadIdx.x < 64) tab[threadIdx.x] = c_exp2_gl[threadIdx.x];
   const double* x = MODE ? J.propars : J.delta;
-  for (int i = threadIdx.x; i < S; i += kFuseThreads) xv[i] = split2(x[i]);
   const bool chg = MODE == 1 && with_change;
-  if (chg)
-    for (int i = threadIdx.x; i < S; i += kFuseThreads) dcv[i] = split2(J.propars[i] - J.propars_old[i]);
 
   for (int tile = local; tile < J.ntile; tile += nblk_job) {
     const int p0 = tile * J.tile_points;
@@ -587,6 +587,12 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_fused_ff(Batch bt, in
     __syncthreads();
     fuse_load(g32, glo, NN, p0, p1, stg, stg + plane, vec, act, nact);
     cp_async_commit();
+    for (int i = threadIdx.x; i < nact; i += kFuseThreads) {
+      const int m = act[i];
+      xa[i] = split2(x[m]);
+      xkey[i] = m * 32 + ((m & 7) << 2);
+      if (chg) dca[i] = (float)(J.propars[m] - J.propars_old[m]);
+    }
     if (chg)
       for (int a = threadIdx.x; a <= natom; a += kFuseThreads) {
         const int s0 = J.shell_off[a];
@@ -608,8 +614,6 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_fused_ff(Batch bt, in
     Dot2 acc[kFuseRows];
 #pragma unroll
     for (int r = 0; r < kFuseRows; ++r) acc[r] = Dot2{0.f, 0.f};
-    f2 ent{0.f, 0.f};
-    float nneg = 0.0f;
     for (int sub = 0; sub < nsub; ++sub) {
       const float* gh = stg + (nbuf == 2 ? (sub & 1) : 0) * 2 * plane;
       const float* gl = gh + plane;
@@ -627,13 +631,12 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_fused_ff(Batch bt, in
       }
       // per-point inputs, loaded before phase A so that their latency
       // overlaps it: (w rho, rho) pairs (MODE 1) or the d2 pair (MODE 0) for
-      // warp 0 and the sub-tile's owner, w for the change warps
+      // warp 0, w for the change warps
       const int pq = q0 + lane;
-      const bool owner = warp == (sub & (kFuseWarps - 1));
       float wf = 0.0f;
       float4 qpre = make_float4(0.f, 0.f, 0.f, 0.f);
       if (pq < p1) {
-        if (warp == 0 || (MODE == 1 && owner)) {
+        if (warp == 0) {
           if (MODE == 1) qpre = wrfp[pq];
           else {
             const float2 d2 = d2in[pq];
@@ -650,25 +653,24 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_fused_ff(Batch bt, in
       // A: rows r even in chain d, odd in chain e
       float rh[kRegRows], rl[kRegRows];
       {
+        const float* ghw = gh + warp * kFuseSP + lane;
+        const float* glw = gl + warp * kFuseSP + lane;
         Dot2 d{0.f, 0.f}, e{0.f, 0.f};
 #pragma unroll
         for (int r = 0; r < kRegRows; ++r) {
-          rh[r] = 0.0f;
-          rl[r] = 0.0f;
           if (r < nr) {
-            const int i = warp + kFuseWarps * r;
-            const float2 xx = xv[act[i]];
-            rh[r] = gh[i * kFuseSP + lane];
-            rl[r] = gl[i * kFuseSP + lane];
+            const float2 xx = xa[warp + kFuseWarps * r];
+            rh[r] = ghw[r * kFuseWarps * kFuseSP];
+            rl[r] = glw[r * kFuseWarps * kFuseSP];
             if (r & 1) dot2_add(e, rh[r], rl[r], xx.x, xx.y);
             else dot2_add(d, rh[r], rl[r], xx.x, xx.y);
           }
         }
         for (int r = kRegRows; r < nr; ++r) {
-          const int i = warp + kFuseWarps * r;
-          const float2 xx = xv[act[i]];
-          if (r & 1) dot2_add(e, gh[i * kFuseSP + lane], gl[i * kFuseSP + lane], xx.x, xx.y);
-          else dot2_add(d, gh[i * kFuseSP + lane], gl[i * kFuseSP + lane], xx.x, xx.y);
+          const float2 xx = xa[warp + kFuseWarps * r];
+          const float g1 = ghw[r * kFuseWarps * kFuseSP], g2 = glw[r * kFuseWarps * kFuseSP];
+          if (r & 1) dot2_add(e, g1, g2, xx.x, xx.y);
+          else dot2_add(d, g1, g2, xx.x, xx.y);
         }
         dot2_merge(d, e);
         part[warp * kFuseSP + lane] = d;
@@ -679,13 +681,14 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_fused_ff(Batch bt, in
         Dot2 du = part[lane];
 #pragma unroll
         for (int q = 1; q < kFuseWarps; ++q) dot2_merge(du, part[q * kFuseSP + lane]);
-        f2 v{0.f, 0.f}, r0{0.f, 0.f};
+        f2 v{0.f, 0.f};
         float sx = 0.0f;
         if (pq < p1) {
           if (MODE == 0) {
             v = ffa::mul(dot2_ff(du), f2{qpre.x, qpre.y});
           } else {
-            r0 = dot2_ff(du);
+            const f2 r0 = dot2_ff(du);
+            r0fo[pq] = make_float2(r0.hi, r0.lo);
             const bool sick = below(f2{qpre.z, qpre.w}, cutp) || below(r0, cutp);
             if (!sick) {
               v = ffa::div(f2{qpre.x, qpre.y}, r0);
@@ -694,14 +697,14 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_fused_ff(Batch bt, in
           }
         }
         pvs[lane] = make_float4(v.hi, v.lo, sx, 0.f);
-        pr0[lane] = make_float2(r0.hi, r0.lo);
       } else if (chg) {
         // C (atoms with no active row add exact zeros: skipped)
+        const float* ghl = gh + lane;
         for (int a = warp - 1; a < natom; a += kFuseWarps - 1) {
           const int i0 = aoff[a], i1 = aoff[a + 1];
           if (i0 == i1) continue;
           float dv = 0.0f;
-          for (int i = i0; i < i1; ++i) dv = fmaf(gh[i * kFuseSP + lane], dcv[act[i]].x, dv);
+          for (int i = i0; i < i1; ++i) dv = fmaf(ghl[i * kFuseSP], dca[i], dv);
           const float term = wf * dv * dv;
           const float t = ch + term;
           const float bb = t - ch;
@@ -709,7 +712,7 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_fused_ff(Batch bt, in
           ch = t;
         }
       }
-      __syncthreads();  // v, s and rho0 of the sub-tile visible
+      __syncthreads();  // v and s of the sub-tile visible
       if (nbuf == 1 && early && sub + 1 < nsub) {  // rows in registers: the buffer is free
         fuse_load(g32, glo, NN, q0 + kFuseSP, p1, stg, stg + plane, vec, act, nact);
         cp_async_commit();
@@ -717,26 +720,8 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_fused_ff(Batch bt, in
       const float4 pv = pvs[lane];
       const f2 v{pv.x, pv.y};
       const float sx = pv.z;
-      if (MODE == 1 && owner && pq < p1) {
-        // per-point outputs and the entropy term w rho ln(rho / rho0)
-        const float2 r0s = pr0[lane];
-        const f2 r0{r0s.x, r0s.y};
-        const bool sick = below(f2{qpre.z, qpre.w}, cutp) || below(r0, cutp);
-        const f2 dd = sick ? f2{0.f, 0.f} : ffa::div(v, r0);
-        r0fo[pq] = r0s;
-        d2fo[pq] = make_float2(dd.hi, dd.lo);
-        if (below(r0, negp)) nneg += 1.0f;
-        if (!sick) {
-          const f2 ratio = ffa::div(f2{qpre.z, qpre.w}, r0);
-          const float l0 = logf(ratio.hi);
-          const f2 e = ffa::exp_ff(f2{-l0, 0.f}, tab);
-          const f2 l = ffa::add(ffa::add(ffa::mul(ratio, e), -1.0f), l0);
-          ent = ffa::add(ent, ffa::mul(f2{qpre.x, qpre.y}, l));
-        }
-      }
       if (hess) wait_mma();  // the MMAs of sub - 1 have read the X tile
       // B (and the rows of X)
-      const uint32_t sw = (uint32_t)(lane & 3);
 #pragma unroll
       for (int r = 0; r < kFuseRows; ++r) {
         if (r < nr) {
@@ -749,11 +734,7 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_fused_ff(Batch bt, in
             g1 = gh[i * kFuseSP + lane];
             g2 = gl[i * kFuseSP + lane];
           }
-          if (hess) {
-            const int m = act[i];
-            const uint32_t off = (uint32_t)(m * 32) + ((((uint32_t)lane >> 2) ^ (uint32_t)(m & 7)) << 2) + sw;
-            xt[off] = umma::to_tf32_rn(g1 * sx);
-          }
+          if (hess) xt[xkey[i] ^ lane] = umma::to_tf32_rn(g1 * sx);
           dot2_add(acc[r], g1, g2, v.hi, v.lo);
         }
       }
@@ -778,40 +759,16 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_fused_ff(Batch bt, in
       }
     }
     zero_inactive(J, tile, pos);
-    if (MODE == 1) {
-      // entropy and negativity partials of the tile
-      double e = ffa::to_double(ent), n = (double)nneg;
+    if (chg) {
+      double c = (double)ch + (double)cl;
 #pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        e += __shfl_xor_sync(0xffffffffu, e, o);
-        n += __shfl_xor_sync(0xffffffffu, n, o);
-      }
-      if (lane == 0) {
-        red[2 * warp] = e;
-        red[2 * warp + 1] = n;
-      }
+      for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+      if (lane == 0) red[warp] = c;
       __syncthreads();
-      if (threadIdx.x == 0) {
-        double se = 0.0, sn = 0.0;
-        for (int k = 0; k < kFuseWarps; ++k) {
-          se += red[2 * k];
-          sn += red[2 * k + 1];
-        }
-        J.jpart[(size_t)QJ_ENTROPY * J.ntile + tile] = se;
-        J.jpart[(size_t)QJ_NEG * J.ntile + tile] = sn;
-      }
-      if (chg) {
-        double c = (double)ch + (double)cl;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
-        __syncthreads();  // red is reused
-        if (lane == 0) red[warp] = c;
-        __syncthreads();
-        double sc = 0.0;
-        for (int k = 0; k < kFuseWarps; ++k) sc += red[k];
-        for (int a = threadIdx.x; a < J.natom; a += kFuseThreads)
-          J.apart[((size_t)a * J.qa + QA_CHANGE) * J.ntile + tile] = a == 0 ? sc : 0.0;
-      }
+      double sc = 0.0;
+      for (int k = 0; k < kFuseWarps; ++k) sc += red[k];
+      for (int a = threadIdx.x; a < J.natom; a += kFuseThreads)
+        J.apart[((size_t)a * J.qa + QA_CHANGE) * J.ntile + tile] = a == 0 ? sc : 0.0;
     }
   }
   if (!hess) return;
@@ -863,6 +820,67 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_fused_ff(Batch bt, in
   if (warp == 0) {
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
                  "r"(kFuseTmemCols));
+  }
+}
+
+// Per-point outputs of the promolecule pass of a fused job, one block per
+// point tile (after k_glisa_fused_ff<1>, which wrote rho0 as float pairs):
+// w rho / rho0^2 (d2f, 0 where sick), the entropy terms w rho ln(rho / rho0)
+// (ln from logf plus one Newton step on exp_ff, error ~ the square of
+// logf's) and the count of points below negative_cutoff, per tile in
+// jpart (QJ_ENTROPY, QJ_NEG).
+__global__ void __launch_bounds__(kThreads) k_glisa_point_ff(Batch bt) {
+  __shared__ float2 tab[64];
+  __shared__ double red[2 * kWarps];
+  int tile;
+  const JobDev& J = decode_local_gf(bt, tile);
+  if (glisa_idle(J)) return;
+  if (!J.fuse) return;
+  if (threadIdx.x < 64) tab[threadIdx.x] = c_exp2_gl[threadIdx.x];
+  __syncthreads();
+  const float2 cutp = split2(J.density_cutoff), negp = split2(J.negative_cutoff);
+  const int p0 = tile * J.tile_points;
+  const int p1 = min(p0 + J.tile_points, J.npoint);
+  f2 ent{0.f, 0.f};
+  float nneg = 0.0f;
+  for (int p = p0 + threadIdx.x; p < p1; p += kThreads) {
+    const float4 q = J.wrf[p];  // (w rho) and rho as float pairs
+    const float2 r0s = J.r0f[p];
+    const f2 r0{r0s.x, r0s.y};
+    const bool sick = below(f2{q.z, q.w}, cutp) || below(r0, cutp);
+    f2 dd{0.f, 0.f};
+    if (!sick) {
+      const f2 v = ffa::div(f2{q.x, q.y}, r0);
+      dd = ffa::div(v, r0);
+      const f2 ratio = ffa::div(f2{q.z, q.w}, r0);
+      const float l0 = logf(ratio.hi);
+      const f2 e = ffa::exp_ff(f2{-l0, 0.f}, tab);
+      const f2 l = ffa::add(ffa::add(ffa::mul(ratio, e), -1.0f), l0);
+      ent = ffa::add(ent, ffa::mul(f2{q.x, q.y}, l));
+    }
+    J.d2f[p] = make_float2(dd.hi, dd.lo);
+    if (below(r0, negp)) nneg += 1.0f;
+  }
+  double e = ffa::to_double(ent), n = (double)nneg;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    e += __shfl_xor_sync(0xffffffffu, e, o);
+    n += __shfl_xor_sync(0xffffffffu, n, o);
+  }
+  if (lane == 0) {
+    red[2 * warp] = e;
+    red[2 * warp + 1] = n;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double se = 0.0, sn = 0.0;
+    for (int k = 0; k < kWarps; ++k) {
+      se += red[2 * k];
+      sn += red[2 * k + 1];
+    }
+    J.jpart[(size_t)QJ_ENTROPY * J.ntile + tile] = se;
+    J.jpart[(size_t)QJ_NEG * J.ntile + tile] = sn;
   }
 }
 
@@ -1197,13 +1215,19 @@ void launch_glisa_fused_ff(const HostBatch& hb, cudaStream_t st, int mode, int m
   if (hb.blocks[K_FUSE] <= 0) return;
   ensure_exp_table_gl();
   const int nbuf = fuse_nbuf(max_shells, mode);
-  if (mode)
+  if (mode) {
     k_glisa_fused_ff<1><<<hb.blocks[K_FUSE], kFuseThreads, fuse_hess_smem_bytes(max_shells, nbuf),
                           st>>>(hb.b[K_FUSE], with_change, nbuf);
-  else
+    ++g_launch_count;
+    if (hb.blocks[K_POINT] > 0) {
+      k_glisa_point_ff<<<hb.blocks[K_POINT], kThreads, 0, st>>>(hb.b[K_POINT]);
+      ++g_launch_count;
+    }
+  } else {
     k_glisa_fused_ff<0><<<hb.blocks[K_FUSE], kFuseThreads, fuse_smem_bytes(max_shells, nbuf), st>>>(
         hb.b[K_FUSE], 0, nbuf);
-  ++g_launch_count;
+    ++g_launch_count;
+  }
 }
 
 void launch_glisa_trials_fused(const HostBatch& hb, cudaStream_t st, int max_shells) {

@@ -601,6 +601,26 @@ void launch_mbis_inner_ff(const HostBatch& hb, cudaStream_t st);
 void launch_final_atweights_ff(const HostBatch& hb, cudaStream_t st, int use_old);
 
 extern long long g_launch_count;
+// Density of contracted Gaussians on points (hp_density.cu).
+struct DensityArgs {
+  const double* points;  // [npoint][3]
+  int64_t npoint;
+  int nshell, nbasis, nmat, tile;
+  const double* centers;  // [nshell][3]
+  const int* info;        // [nshell][5]: l, pure, nprim, first primitive, first function
+  const double* amin;     // [nshell] smallest exponent of the shell
+  const double* exps;     // [nprim]
+  const double* coefs;    // [nprim] contraction coefficient x primitive normalisation
+  const double* mats;     // [nmat][nbasis][nbasis]
+  double* out;            // [nmat][npoint]
+  unsigned long long* stats;  // [3]: shell-tile pairs, function-point pairs, FMA per matrix; or null
+};
+constexpr size_t kDensSmemMax = 200 * 1024;
+size_t density_smem_bytes(int nbasis, int nshell, int tile);
+int density_tile(int nbasis, int nshell);
+int set_pure_tables(const double* pure2, const double* pure3);
+void launch_density(const DensityArgs& a, cudaStream_t st);
+
 // Message returned by hp_last_error() for the calling thread (hp_runtime.cu).
 void set_error_text(const char* msg);
 

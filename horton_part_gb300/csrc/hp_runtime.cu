@@ -1552,4 +1552,174 @@ int32_t hp_job_results_get(hp_job* job, const hp_job_results* r) {
   return HP_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Density generator (hp_density.cu)
+// ---------------------------------------------------------------------------
+
+struct hp_density_plan {
+  hp_ctx* ctx = nullptr;
+  DensityArgs args{};
+  double* dev = nullptr;                 // centers, amin, exps, coefs, mats
+  int* info = nullptr;
+  unsigned long long* stats = nullptr;   // [3]
+  size_t bytes = 0;
+  double* scratch = nullptr;             // host-pointer evaluations: points and out
+  size_t scratch_points = 0;
+};
+
+int32_t hp_density_plan_create(hp_ctx* ctx, const hp_density_desc* d, hp_density_plan** out) {
+  if (!out) return fail(HP_ERR_INVALID, "null output pointer");
+  *out = nullptr;
+  if (!ctx || !d) return fail(HP_ERR_INVALID, "null argument");
+  if (d->nshell < 0 || d->nprim < 0 || d->nbasis < 0 || d->nmat < 1 || !d->mats ||
+      (d->nshell > 0 && (!d->centers || !d->shell_info || !d->exponents || !d->coeffs)))
+    return fail(HP_ERR_INVALID, "incomplete density description");
+  const int ns = d->nshell, nb = d->nbasis;
+  std::vector<double> amin(ns, 0.0);
+  int nf = 0;
+  bool pure2 = false, pure3 = false;
+  for (int s = 0; s < ns; ++s) {
+    const int* in = d->shell_info + 5 * s;
+    const int l = in[0], pure = in[1], np = in[2], k0 = in[3], f0 = in[4];
+    if (l < 0 || l > 3) return fail(HP_ERR_UNSUPPORTED, "shells up to f (l <= 3) only");
+    if (np < 1 || k0 < 0 || k0 + np > d->nprim) return fail(HP_ERR_INVALID, "shell primitives out of range");
+    const int nfs = (pure && l >= 2) ? 2 * l + 1 : (l + 1) * (l + 2) / 2;
+    if (f0 != nf) return fail(HP_ERR_INVALID, "shell functions must be consecutive");
+    nf += nfs;
+    if (pure && l == 2) pure2 = true;
+    if (pure && l == 3) pure3 = true;
+    double a = INFINITY;
+    for (int k = k0; k < k0 + np; ++k) {
+      if (!(d->exponents[k] > 0.0)) return fail(HP_ERR_INVALID, "exponents must be positive");
+      if (d->coeffs[k] != 0.0) a = std::min(a, d->exponents[k]);
+    }
+    amin[s] = std::isfinite(a) ? a : 1e300;  // a shell with no nonzero coefficient is never significant
+  }
+  if (nf != nb) return fail(HP_ERR_INVALID, "shell functions do not add up to nbasis");
+  if ((pure2 && !d->pure2) || (pure3 && !d->pure3))
+    return fail(HP_ERR_INVALID, "pure shells need their Cartesian-to-pure matrix");
+  const int tile = density_tile(nb, ns);
+  if (tile == 0) return fail(HP_ERR_UNSUPPORTED, "basis too large for one point tile");
+  HP_CK(cudaSetDevice(ctx->device));
+  const size_t ndbl = 3 * (size_t)ns + ns + 2 * (size_t)d->nprim + (size_t)d->nmat * nb * nb;
+  const size_t bytes = 8 * ndbl + 4 * 5 * (size_t)ns + 8 * 3;
+  if (ctx->used + bytes > ctx->budget) return fail(HP_ERR_NO_MEMORY, "HBM budget exceeded");
+  hp_density_plan* p = new hp_density_plan();
+  p->ctx = ctx;
+  if (cudaMalloc(&p->dev, 8 * std::max<size_t>(ndbl, 1)) != cudaSuccess ||
+      cudaMalloc(&p->info, 4 * std::max<size_t>(5 * (size_t)ns, 1)) != cudaSuccess ||
+      cudaMalloc(&p->stats, 8 * 3) != cudaSuccess) {
+    hp_density_plan_destroy(p);
+    return fail(HP_ERR_NO_MEMORY, "device allocation failed");
+  }
+  double* cen = p->dev;
+  double* am = cen + 3 * (size_t)ns;
+  double* ex = am + ns;
+  double* co = ex + d->nprim;
+  double* mats = co + d->nprim;
+  cudaStream_t st = ctx->stream;
+  int rc = 0;
+  rc |= cudaMemcpyAsync(cen, d->centers, 8 * 3 * (size_t)ns, cudaMemcpyHostToDevice, st) != cudaSuccess;
+  rc |= cudaMemcpyAsync(am, amin.data(), 8 * (size_t)ns, cudaMemcpyHostToDevice, st) != cudaSuccess;
+  rc |= cudaMemcpyAsync(ex, d->exponents, 8 * (size_t)d->nprim, cudaMemcpyHostToDevice, st) != cudaSuccess;
+  rc |= cudaMemcpyAsync(co, d->coeffs, 8 * (size_t)d->nprim, cudaMemcpyHostToDevice, st) != cudaSuccess;
+  rc |= cudaMemcpyAsync(mats, d->mats, 8 * (size_t)d->nmat * nb * nb, cudaMemcpyHostToDevice, st) != cudaSuccess;
+  rc |= cudaMemcpyAsync(p->info, d->shell_info, 4 * 5 * (size_t)ns, cudaMemcpyHostToDevice, st) != cudaSuccess;
+  rc |= cudaMemsetAsync(p->stats, 0, 8 * 3, st) != cudaSuccess;
+  if (pure2 || pure3) {
+    double t2[30] = {0.0}, t3[70] = {0.0};
+    if (d->pure2) memcpy(t2, d->pure2, sizeof(t2));
+    if (d->pure3) memcpy(t3, d->pure3, sizeof(t3));
+    rc |= set_pure_tables(t2, t3);
+  }
+  rc |= cudaStreamSynchronize(st) != cudaSuccess;
+  if (rc) {
+    hp_density_plan_destroy(p);
+    return fail(HP_ERR_CUDA, "density plan upload failed");
+  }
+  p->bytes = bytes;
+  ctx->used += bytes;
+  DensityArgs& a = p->args;
+  a.nshell = ns;
+  a.nbasis = nb;
+  a.nmat = d->nmat;
+  a.tile = tile;
+  a.centers = cen;
+  a.info = p->info;
+  a.amin = am;
+  a.exps = ex;
+  a.coefs = co;
+  a.mats = mats;
+  a.stats = p->stats;
+  *out = p;
+  return HP_OK;
+}
+
+int32_t hp_density_plan_eval(hp_density_plan* p, int64_t npoint, const double* points, double* out,
+                             int32_t device_ptrs) {
+  if (!p || (npoint > 0 && (!points || !out)) || npoint < 0) return fail(HP_ERR_INVALID, "bad argument");
+  if (npoint == 0) return HP_OK;
+  hp_ctx* ctx = p->ctx;
+  HP_CK(cudaSetDevice(ctx->device));
+  cudaStream_t st = ctx->stream;
+  DensityArgs a = p->args;
+  a.npoint = npoint;
+  const size_t nout = (size_t)a.nmat * (size_t)npoint;
+  if (device_ptrs) {
+    a.points = points;
+    a.out = out;
+    launch_density(a, st);
+    return check_launch();
+  }
+  const size_t need = 3 * (size_t)npoint + nout;
+  if (p->scratch_points < need) {
+    if (p->scratch) {
+      cudaFree(p->scratch);
+      ctx->used -= 8 * p->scratch_points;
+      p->scratch = nullptr;
+      p->scratch_points = 0;
+    }
+    if (ctx->used + 8 * need > ctx->budget) return fail(HP_ERR_NO_MEMORY, "HBM budget exceeded");
+    if (cudaMalloc(&p->scratch, 8 * need) != cudaSuccess) return fail(HP_ERR_NO_MEMORY, "device allocation failed");
+    p->scratch_points = need;
+    ctx->used += 8 * need;
+  }
+  double* dpts = p->scratch;
+  double* dout = dpts + 3 * (size_t)npoint;
+  HP_CK(cudaMemcpyAsync(dpts, points, 8 * 3 * (size_t)npoint, cudaMemcpyHostToDevice, st));
+  a.points = dpts;
+  a.out = dout;
+  launch_density(a, st);
+  int rc = check_launch();
+  if (rc) return rc;
+  HP_CK(cudaMemcpyAsync(out, dout, 8 * nout, cudaMemcpyDeviceToHost, st));
+  HP_CK(cudaStreamSynchronize(st));
+  return HP_OK;
+}
+
+int32_t hp_density_plan_stats(hp_density_plan* p, uint64_t* stats) {
+  if (!p || !stats) return fail(HP_ERR_INVALID, "null argument");
+  HP_CK(cudaSetDevice(p->ctx->device));
+  HP_CK(cudaStreamSynchronize(p->ctx->stream));
+  unsigned long long h[3];
+  HP_CK(cudaMemcpy(h, p->stats, sizeof(h), cudaMemcpyDeviceToHost));
+  for (int k = 0; k < 3; ++k) stats[k] = (uint64_t)h[k];
+  return HP_OK;
+}
+
+int32_t hp_density_plan_destroy(hp_density_plan* p) {
+  if (!p) return HP_OK;
+  if (p->ctx) {
+    cudaSetDevice(p->ctx->device);
+    cudaStreamSynchronize(p->ctx->stream);
+    p->ctx->used -= p->bytes + 8 * p->scratch_points;
+  }
+  if (p->dev) cudaFree(p->dev);
+  if (p->info) cudaFree(p->info);
+  if (p->stats) cudaFree(p->stats);
+  if (p->scratch) cudaFree(p->scratch);
+  delete p;
+  return HP_OK;
+}
+
 }  // extern "C"

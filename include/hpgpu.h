@@ -44,7 +44,7 @@
 extern "C" {
 #endif
 
-#define HPGPU_ABI_VERSION 3
+#define HPGPU_ABI_VERSION 4
 
 typedef enum {
   HP_OK = 0,
@@ -276,6 +276,46 @@ int32_t hp_glisa_line_search(hp_job* job, const double* x, const double* delta, 
  * utils.py:255-398); the job is done afterwards and hp_job_results_get
  * returns its charges and parameters (the histories stay with the host). */
 int32_t hp_glisa_finish(hp_job* job, const double* x, int32_t niter);
+
+/* ------------------------------------------------------------------------
+ * Density generator: the electron density of a contracted-Gaussian
+ * wavefunction on grid points (scripts/generate_density.py:119-204, with
+ * rho = einsum("ab,bp,ap->p", D, phi, phi) at :186-188), in FP64.
+ *
+ * Shells follow Gaussian's fchk conventions (0 <= l <= 3; Cartesian
+ * components in file order; pure functions m = 0, +1, -1, ... given by the
+ * caller's Cartesian-to-pure matrices). coeffs already include the
+ * primitive normalisation (2a/pi)^(3/4) (4a)^(l/2) / sqrt((2l-1)!!).
+ * ------------------------------------------------------------------------ */
+typedef struct {
+  int32_t nshell;
+  const double* centers;      /* [nshell][3], bohr */
+  const int32_t* shell_info;  /* [nshell][5]: l, pure, nprim, first primitive, first function */
+  int32_t nprim;
+  const double* exponents;    /* [nprim] */
+  const double* coeffs;       /* [nprim] */
+  int32_t nbasis;
+  int32_t nmat;               /* density matrices (total, spin, ...) */
+  const double* mats;         /* [nmat][nbasis][nbasis], symmetric */
+  const double* pure2;        /* [5][6] row-major, or NULL when no pure d shell */
+  const double* pure3;        /* [7][10] row-major, or NULL when no pure f shell */
+} hp_density_desc;
+
+typedef struct hp_density_plan hp_density_plan;
+
+/* Copy the basis and the matrices to the device. */
+int32_t hp_density_plan_create(hp_ctx* ctx, const hp_density_desc* desc, hp_density_plan** out);
+/* out[m * npoint + p] = sum_ab mats[m]_ab phi_a(points[p]) phi_b(points[p]).
+ * device_ptrs = 0: points and out are host arrays (copied in and out);
+ * 1: device arrays of the plan's context, used in place (asynchronous on
+ * the context stream). */
+int32_t hp_density_plan_eval(hp_density_plan* plan, int64_t npoint, const double* points,
+                             double* out, int32_t device_ptrs);
+/* Work performed since the plan was created: [0] shell-tile pairs kept by
+ * the screening, [1] basis values evaluated, [2] FMA per matrix in the
+ * contraction (synchronises the context stream). */
+int32_t hp_density_plan_stats(hp_density_plan* plan, uint64_t* stats);
+int32_t hp_density_plan_destroy(hp_density_plan* plan);
 
 /* Kernel timing with CUDA events on the context stream, per kernel family
  * (hp_kernel_family). Enabling clears the accumulators. */

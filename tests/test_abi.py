@@ -38,7 +38,7 @@ def test_binding_covers_header():
 
 
 def test_abi_version(library):
-    assert _lib.lib().hp_abi_version() == 3
+    assert _lib.lib().hp_abi_version() == 4
 
 
 def test_struct_sizes_match_header():

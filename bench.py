@@ -187,6 +187,29 @@ def measure_tf32_peak(n=8192, reps=10):
         torch.backends.cuda.matmul.allow_tf32 = old
 
 
+def measure_fp64_peak(n=4096, reps=5):
+    """Best-of-`reps` FP64 GEMM rate of cuBLAS (TFLOP/s): the denominator of
+    the FP64 density kernel's roofline (no FP64 figure is recorded beside the
+    HBM and BF16 peaks)."""
+    import torch
+
+    a = torch.randn(n, n, device="cuda", dtype=torch.float64)
+    b = torch.randn(n, n, device="cuda", dtype=torch.float64)
+    c = torch.empty(n, n, device="cuda", dtype=torch.float64)
+    for _ in range(2):
+        torch.matmul(a, b, out=c)
+    best = float("inf")
+    for _ in range(reps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b, out=c)
+        e1.record()
+        torch.cuda.synchronize()
+        best = min(best, e0.elapsed_time(e1) / 1000.0)
+    del a, b, c
+    return 2.0 * n ** 3 / best / 1e12
+
+
 # ---------------------------------------------------------------------------
 # clocks
 # ---------------------------------------------------------------------------
@@ -678,7 +701,7 @@ def run_ours(args):
         if w["scheme"] == "glisa":
             line["accuracy_vs_fp64"]["newton_fp64_factors"] = int(im.f64_factors)
     if rank == 0 and world == 1 and args.workload == "glisa-c6h10n2o2" and not args.no_extras:
-        line.update(extra_sections(ctx, args))
+        line.update(extra_sections(ctx, args, w))
     if rank == 0 and world == 1 and not args.no_cpu:
         r, sample, threads = cpu_sample(w, 2 if w["scheme"] == "glisa" else 3)
         line["cpu_baseline"] = {"value": r, "unit": UNIT, "cores": threads, "kind": "port",
@@ -690,7 +713,75 @@ def run_ours(args):
     replicas.finalize()
 
 
-def extra_sections(ctx, args):
+def density_section(ctx, mol):
+    """The density generator (part-gen's density step) on the molecule's
+    grid: a split-valence-plus-d basis on every atom (14 functions per heavy
+    atom, 5 per H) and a closed-shell density matrix, FP64. Device-resident
+    points timed with CUDA events (3 evaluations after 2 warm-ups), the
+    host-array call timed end to end, the oracle timed on 20,000 points on
+    one core, and the GPU result checked against the oracle there."""
+    import torch
+
+    from horton_part_gb300 import synthetic
+    from horton_part_gb300.density import DensityPlan
+    from oracle import hp_density as H
+
+    shells = synthetic.contracted_basis(mol.numbers, mol.coordinates)
+    nb = sum(s.nfunc for s in shells)
+    D = synthetic.density_matrix(nb, int(round(float(np.sum(mol.numbers)) / 2)))
+    plan = DensityPlan(shells, D, context=ctx)
+    pts_h = np.ascontiguousarray(mol.grid.points)
+    n = len(pts_h)
+    pts = torch.tensor(pts_h, device="cuda")
+    out = torch.empty((1, n), dtype=torch.float64, device="cuda")
+    stream = torch.cuda.current_stream()
+    for _ in range(2):
+        plan.evaluate_device(pts, out)
+    torch.cuda.synchronize()
+    st0 = plan.stats()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = 3
+    e0.record(stream)
+    for _ in range(reps):
+        plan.evaluate_device(pts, out)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    st1 = plan.stats()
+    fma = (st1["fma_per_matrix"] - st0["fma_per_matrix"]) / reps
+    values = (st1["basis_values"] - st0["basis_values"]) / reps
+    t0 = time.perf_counter()
+    host = plan.evaluate(pts_h)[0]
+    e2e_s = time.perf_counter() - t0
+    sample = np.random.default_rng(9).choice(n, 20000, replace=False)
+    t0 = time.perf_counter()
+    ref = H.density(D, shells, pts_h[sample])
+    cpu_s = time.perf_counter() - t0
+    plan.close()
+    peak = measure_fp64_peak()
+    achieved = 2.0 * fma / (ms / 1e3) / 1e12
+    return {
+        "workload": f"density-{mol.natom}atoms", "npoint": n, "nbasis": nb, "nshell": len(shells),
+        "dtype": "f64", "ms_per_evaluation": ms, "points_per_s": n / (ms / 1e3),
+        "e2e": {"seconds": e2e_s, "points_per_s": n / e2e_s, "h2d_bytes": 24 * n, "d2h_bytes": 8 * n},
+        "screening": {"basis_values_fraction": values / (nb * n),
+                      "contraction_fma": fma, "dense_fma": nb * (nb + 1) / 2 * n},
+        "roofline": {"kernel": "k_density", "bound": "fp64", "achieved": achieved, "peak": peak,
+                     "unit": "TFLOP/s", "frac": achieved / peak,
+                     "peak_source": "measured: cuBLAS FP64 GEMM 4096^3, this run",
+                     "note": "contraction FMA (2 FLOP each) only; the exps of the basis values "
+                             "are extra FP64 work"},
+        "cpu_baseline": {"points_per_s": len(sample) / cpu_s, "cores": 1, "kind": "port",
+                         "sample": f"oracle density (NumPy einsum) on {len(sample)} points, "
+                                   f"{cpu_s:.1f} s, 1 thread"},
+        "err_vs_oracle": {
+            "max_abs_over_max_rho": float(np.max(np.abs(host[sample] - ref)) / np.max(np.abs(ref))),
+            "max_rel_where_rho_above_1e-8_max": float(np.max(
+                (np.abs(host[sample] - ref) / np.abs(ref))[np.abs(ref) > 1e-8 * np.max(np.abs(ref))]))},
+    }
+
+
+def extra_sections(ctx, args, w=None):
     """Bounded measurements of the metric's other workloads, added to the
     default line: the batched MBIS step (config 3's generator, 32 molecules
     of 3-60 atoms, 75 x Lebedev-194 per atom; three outer iterations of every
@@ -759,6 +850,8 @@ def extra_sections(ctx, args):
                       "capacity_jobs_per_s": cap["jobs_per_s"],
                       "poisson_arrival_rate_jobs_per_s": lam, "poisson": load,
                       "note": "every request enters from host arrays and returns its results"}
+    if w is not None:
+        out["density"] = density_section(ctx, w["mol"])
     return out
 
 

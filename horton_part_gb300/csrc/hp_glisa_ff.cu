@@ -569,7 +569,7 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_fused_ff(Batch bt, in
   };
   // Every thread: the MMAs of the last issued sub-tile have read the X tile.
   auto wait_mma = [&]() {
-    if (nmma > 0 && !timed_out && !umma::mbar_wait(bar, (uint32_t)((nmma - 1) & 1))) timed_out = 1;
+    if (nmma > 0 && !timed_out && !umma::mbar_wait_sleep(bar, (uint32_t)((nmma - 1) & 1))) timed_out = 1;
   };
   const double* x = MODE ? J.propars : J.delta;
   const bool chg = MODE == 1 && with_change;

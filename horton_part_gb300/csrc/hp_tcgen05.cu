@@ -166,7 +166,7 @@ __global__ void __launch_bounds__(kTcThreads) k_glisa_hess_tc(Batch bt) {
     if (nblocks >= 2) {
       // the MMAs of block nblocks - 2 (the stage's previous commit, number
       // (nblocks >> 1) - 1 on this barrier) must have read the stage
-      if (!mbar_wait(bar0 + 8 * st, (uint32_t)(((nblocks >> 1) - 1) & 1))) timed_out = 1;
+      if (!mbar_wait_sleep(bar0 + 8 * st, (uint32_t)(((nblocks >> 1) - 1) & 1))) timed_out = 1;
     }
 #pragma unroll
     for (int r = 0; r < kRowsA; ++r) {
@@ -219,7 +219,7 @@ __global__ void __launch_bounds__(kTcThreads) k_glisa_hess_tc(Batch bt) {
   if (nblocks > 0 && !timed_out) {
     // the last commit covers every MMA issued before it
     const int last = nblocks - 1;
-    if (!mbar_wait(bar0 + 8 * (last & 1), (uint32_t)((last >> 1) & 1))) timed_out = 1;
+    if (!mbar_wait_sleep(bar0 + 8 * (last & 1), (uint32_t)((last >> 1) & 1))) timed_out = 1;
   }
   asm volatile("tcgen05.fence::after_thread_sync;");
   __syncthreads();

@@ -30,6 +30,8 @@ __all__ = [
     "slater_density",
     "batch_molecules",
     "peptide_molecule",
+    "contracted_basis",
+    "density_matrix",
 ]
 
 ANGSTROM = 1.889726133921252
@@ -306,3 +308,38 @@ def geometric_gaussian_basis(nshell_per_element, amin=0.05, amax=300.0):
         exps[z] = np.geomspace(amax, amin, k)
         inits[z] = np.full(k, 1.0 / k)
     return ExpBasisFuncHelper(orders, exps, inits)
+
+
+def contracted_basis(numbers, coordinates, seed=5):
+    """Contracted Gaussian shells of a split-valence-plus-polarisation shape on
+    every atom (a stand-in for a published basis set, which this package does
+    not carry): H s(3) s(1) p(1) (5 functions); heavier atoms s(6) s(3) s(1)
+    p(3) p(1) and a pure d(1) (14 functions). Exponents follow an
+    even-tempered ladder scaled by the nuclear charge, contraction
+    coefficients are positive and seeded. Returns a list of
+    :class:`horton_part_gb300.fchk.Shell`."""
+    from .fchk import Shell
+
+    rng = np.random.default_rng(seed)
+    out = []
+    for a, (z, c) in enumerate(zip(np.asarray(numbers), np.asarray(coordinates, dtype=np.float64))):
+        scale = float(z) ** 1.5 if z > 1 else 1.0
+        if z == 1:
+            spec = [(0, False, 3, 20.0), (0, False, 1, 0.17), (1, False, 1, 0.8)]
+        else:
+            spec = [(0, False, 6, 700.0 * scale / 20.0), (0, False, 3, 5.0 * scale / 20.0),
+                    (0, False, 1, 0.3), (1, False, 3, 4.0 * scale / 20.0), (1, False, 1, 0.25),
+                    (2, True, 1, 0.8)]
+        for l, pure, n, top in spec:
+            exps = top / 3.2 ** np.arange(n)
+            coefs = rng.uniform(0.2, 1.0, n)
+            out.append(Shell(c, l, pure, exps, coefs, a))
+    return out
+
+
+def density_matrix(nbasis, nocc, seed=6):
+    """Closed-shell one-particle density 2 C C^T of ``nocc`` seeded orthonormal
+    orbitals (a stand-in for a converged SCF density)."""
+    rng = np.random.default_rng(seed)
+    q, _ = np.linalg.qr(rng.normal(size=(nbasis, nocc)))
+    return 2.0 * q @ q.T

@@ -781,14 +781,15 @@ def density_section(ctx, mol):
     }
 
 
-def extra_sections(ctx, args, w=None):
+def extra_sections(ctx, args, workload_main=None):
     """Bounded measurements of the metric's other workloads, added to the
     default line: the batched MBIS step (config 3's generator, 32 molecules
     of 3-60 atoms, 75 x Lebedev-194 per atom; three outer iterations of every
     job with shared launches, timed with CUDA events) and the continuous-
     batching server (12 requests, 70 % MBIS / 30 % gLISA, 3-60 atoms:
     closed-loop capacity, then Poisson arrivals at 70 % of it with p50/p99
-    latency). Each takes a few tens of seconds."""
+    latency), and the density generator on the main workload's molecule and
+    grid (density_section). Each takes a few tens of seconds."""
     import torch
 
     from horton_part_gb300 import _lib, synthetic
@@ -850,8 +851,8 @@ def extra_sections(ctx, args, w=None):
                       "capacity_jobs_per_s": cap["jobs_per_s"],
                       "poisson_arrival_rate_jobs_per_s": lam, "poisson": load,
                       "note": "every request enters from host arrays and returns its results"}
-    if w is not None:
-        out["density"] = density_section(ctx, w["mol"])
+    if workload_main is not None:
+        out["density"] = density_section(ctx, workload_main["mol"])
     return out
 
 

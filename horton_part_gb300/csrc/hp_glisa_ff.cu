@@ -938,7 +938,7 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_trials_fused(Batch bt
   __syncthreads();
   fuse_load(g32, glo, NN, p0, p1, stg, stg + plane, vec, act, nact);
   cp_async_commit();
-  for (int i = threadIdx.x; i < S; i += kFuseThreads) xv[i] = split2(J.delta[i]);
+  for (int i = threadIdx.x; i < nact; i += kFuseThreads) xv[i] = split2(J.delta[act[i]]);  // by active row
   const int t = warp;  // this warp's trial: step 2^-t
   const float at = ldexpf(1.0f, -t);
   const int nclip = J.clip[S];
@@ -975,18 +975,20 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_trials_fused(Batch bt
       fuse_load(g32, glo, NN, p0 + (sub + 1) * kFuseSP, p1, nh, nh + plane, vec, act, nact);
       cp_async_commit();
     }
-    {  // A (active rows i = warp mod 8)
+    {  // A (active rows i = warp mod 8; delta compacted by active row)
       Dot2 d{0.f, 0.f}, e{0.f, 0.f};
       int i = warp;
+      const float* ghl = gh + lane;
+      const float* gll = gl + lane;
       for (; i + kFuseWarps < nact; i += 2 * kFuseWarps) {
-        const float2 x1 = xv[act[i]], x2 = xv[act[i + kFuseWarps]];
-        dot2_add(d, gh[i * kFuseSP + lane], gl[i * kFuseSP + lane], x1.x, x1.y);
+        const float2 x1 = xv[i], x2 = xv[i + kFuseWarps];
+        dot2_add(d, ghl[i * kFuseSP], gll[i * kFuseSP], x1.x, x1.y);
         const int i2 = i + kFuseWarps;
-        dot2_add(e, gh[i2 * kFuseSP + lane], gl[i2 * kFuseSP + lane], x2.x, x2.y);
+        dot2_add(e, ghl[i2 * kFuseSP], gll[i2 * kFuseSP], x2.x, x2.y);
       }
       if (i < nact) {
-        const float2 x1 = xv[act[i]];
-        dot2_add(d, gh[i * kFuseSP + lane], gl[i * kFuseSP + lane], x1.x, x1.y);
+        const float2 x1 = xv[i];
+        dot2_add(d, ghl[i * kFuseSP], gll[i * kFuseSP], x1.x, x1.y);
       }
       dot2_merge(d, e);
       part[warp * kFuseSP + lane] = d;

@@ -726,15 +726,21 @@ def density_section(ctx, mol):
     from horton_part_gb300.density import DensityPlan
     from oracle import hp_density as H
 
+    from horton_part_gb300 import _lib
+
     shells = synthetic.contracted_basis(mol.numbers, mol.coordinates)
     nb = sum(s.nfunc for s in shells)
     D = synthetic.density_matrix(nb, int(round(float(np.sum(mol.numbers)) / 2)))
-    plan = DensityPlan(shells, D, context=ctx)
     pts_h = np.ascontiguousarray(mol.grid.points)
     n = len(pts_h)
     pts = torch.tensor(pts_h, device="cuda")
     out = torch.empty((1, n), dtype=torch.float64, device="cuda")
-    stream = torch.cuda.current_stream()
+    torch.cuda.synchronize()
+    # a context on a stream of its own, so that the events below are recorded
+    # on the stream the kernel runs on
+    stream = torch.cuda.Stream()
+    dctx = _lib.Context(torch.cuda.current_device(), stream=stream.cuda_stream)
+    plan = DensityPlan(shells, D, context=dctx)
     for _ in range(2):
         plan.evaluate_device(pts, out)
     torch.cuda.synchronize()
@@ -758,6 +764,7 @@ def density_section(ctx, mol):
     ref = H.density(D, shells, pts_h[sample])
     cpu_s = time.perf_counter() - t0
     plan.close()
+    dctx.close()
     peak = measure_fp64_peak()
     achieved = 2.0 * fma / (ms / 1e3) / 1e12
     return {

@@ -6,6 +6,9 @@ coefficients are refitted by one of the reference's inner solvers, run for
 all atoms at once on the device:
 
 ``sc``        c_k <- int w c_k g_k rho_a / pro (``alisa.py:193-291``)
+``sc-1-iter`` one such update per outer iteration (``alisa.py:294-353``): the
+              ``sc`` kernels with one inner iteration and no inner
+              convergence test (so no warning)
 ``newton``    exact Newton on the KL objective (``alisa.py:543-602``)
 ``m-newton``  Newton with the positivity line search (``alisa.py:605-664``)
 
@@ -13,7 +16,7 @@ all atoms at once on the device:
 optimum is the non-negative KL minimiser, which the multiplicative ``sc``
 update also reaches, so ``cvxopt`` is served by ``sc``. Other reference
 solvers (``diis``, ``cdiis``, ``trust-region``, ``quasi-newton``,
-``sc-1-iter``, ``sc-plus-convex``) are not on the GPU path and raise
+``sc-plus-convex``) are not on the GPU path and raise
 ``NotImplementedError``.
 """
 
@@ -26,7 +29,8 @@ from .gisa import GaussianISAWPart, shell_tables_from_helper
 
 __all__ = ["LinearISAWPart", "setup_bs_helper"]
 
-_SOLVERS = {"sc": "sc", "cvxopt": "sc", "newton": "newton", "m-newton": "m-newton"}
+_SOLVERS = {"sc": "sc", "sc-1-iter": "sc", "cvxopt": "sc", "newton": "newton",
+            "m-newton": "m-newton"}
 
 
 def setup_bs_helper(part):
@@ -80,8 +84,17 @@ class LinearISAWPart(GaussianISAWPart):
     def _solver_name(self):
         return _SOLVERS[self._solver]
 
+    def _report_warnings(self, info):
+        if self._solver == "sc-1-iter":  # one update by design: no inner convergence test
+            from . import _lib
+
+            info.warnings &= ~_lib.WARN_INNER_NOT_CONVERGED
+        super()._report_warnings(info)
+
     def _job_extra(self):
         opts = dict(self._solver_options)
+        if self._solver == "sc-1-iter":
+            return {"inner_maxiter": 1}
         if _SOLVERS[self._solver] == "sc":
             return {"inner_maxiter": int(float(opts.get("max_niter_inner", 100000)))}
         extra = {"inner_maxiter": int(opts.get("niter", 10000))}

@@ -327,26 +327,25 @@ __global__ void __launch_bounds__(kThreads) k_glisa_trials_ff(Batch bt) {
 // they fit beside the rest of the block's shared memory, so that the next
 // sub-tile loads while this one is processed). Warp w owns the active rows
 // i = w, w + 8, ... of the tile (lane = point); per sub-tile
-//   A  the warp reads its rows' values into registers (kRegRows of them; rows
-//      past that, for tiles with more than 8 kRegRows active shells, are read
-//      again from the staging buffer) and sums G[m][p] x[m] over them in two
-//      compensated chains, merged into the warp's partial sum of u(p);
+//   A  the warp sums G[m][p] x[m] over its rows in two compensated chains,
+//      merged into the warp's partial sum of u(p);
 //   A' warp 0 merges the eight partials in warp order and forms v(p) (and
-//      for MODE 1 s(p) and rho0(p)) for the sub-tile's points, published in
-//      shared memory; meanwhile warps 1-7 form the outer change (C below);
+//      for MODE 1 s(p), writing rho0(p)) for the sub-tile's points, published
+//      in shared memory; meanwhile warps 1-7 form the outer change (C below);
 //   B  every warp adds G[m][p] v(p) of its rows to compensated accumulators
 //      kept in registers across the tile (reduced once at its end) and, MODE
-//      1, writes its rows of X = G_hi diag(s) for the tensor-core Hessian;
-//      the owner warp of the sub-tile (sub mod 8) writes the per-point outputs
-//      and the entropy terms.
+//      1, writes its rows of X = G_hi diag(s) for the tensor-core Hessian.
+// The staged values are read again in B rather than kept in registers from
+// A: the block runs at two per SM with at most 128 registers a thread, and
+// holding them across the barriers costs more issue slots than the second
+// shared-memory read (measured: 195 against 135 million warp instructions
+// per pass on the benchmark molecule).
 // No FP64 arithmetic per point: w rho and rho come as float pairs (wrf, set
 // once per job), the outputs are float pairs.
 // MODE 0 (refinement product): x = delta, v = (w rho / rho0^2) u.
-// MODE 1 (promolecule + gradient): x = c, u = rho0 (r0f), d2 = w rho / rho0^2
-//   (d2f) and v = w rho / rho0, quotients in float-float; the owner also forms
-//   the entropy terms w rho ln(rho / rho0), ln from logf plus one Newton step
-//   on exp_ff (error ~ the square of logf's), and counts the points below
-//   negative_cutoff. With with_change, also
+// MODE 1 (promolecule + gradient): x = c, u = rho0 (r0f) and v = w rho /
+//   rho0, quotients in float-float (the entropy, w rho / rho0^2 and the
+//   negativity count follow in k_glisa_point_ff). With with_change, also
 //   C  the outer change of the step that produced c (glisa.py:776 via
 //      compute_change): warps 1-7 take the atoms a = w - 1 (mod 7), lane =
 //      point, sum_{m in a} (c - c_old)_m g_m from the staged sub-tile's G_hi
@@ -360,8 +359,12 @@ __global__ void __launch_bounds__(kThreads) k_glisa_trials_ff(Batch bt) {
 constexpr int kFuseThreads = 256;
 constexpr int kFuseWarps = kFuseThreads / 32;
 constexpr int kFuseSP = 32;                             // points per sub-tile (one per lane)
-constexpr int kFuseRows = kFuseMaxShells / kFuseWarps;  // rows per warp in B
-constexpr int kRegRows = 12;                            // rows per warp kept in registers
+// B keeps the gradient sums of a warp's first kFuseRows rows (tile rows below
+// kFuseWarps kFuseRows = 96) in registers across the tile; the rows past
+// them (tiles with more active shells) are reduced across the lanes per
+// sub-tile and summed per row in shared memory.
+constexpr int kFuseRows = 12;
+constexpr int kFuseRegRowsTotal = kFuseWarps * kFuseRows;
 // Shared memory of one block at most (two blocks per SM share 228 KB).
 constexpr size_t kFuseSmemMax = 112 * 1024;
 
@@ -371,6 +374,7 @@ __host__ __device__ constexpr size_t fuse_smem_bytes(int S, int nbuf) {
          + 16 * (size_t)S                    // per active row: x pair and the parameter change
          + 8 * (size_t)kFuseWarps * kFuseSP  // partial sums
          + 32 * (size_t)kFuseSP              // per point: (v, s)
+         + 8 * (size_t)(kFuseMaxShells - kFuseRegRowsTotal)  // gradient sums of the rows past them
          + 8 * (2 * kFuseWarps + 2)          // block sums
          + 16 * (size_t)S + 8;               // active shells, positions, per-atom offsets, X keys
 }
@@ -508,7 +512,8 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_fused_ff(Batch bt, in
   float* dca = reinterpret_cast<float*>(xa + S);                   // change of active row i
   Dot2* part = reinterpret_cast<Dot2*>(dca + 2 * S);
   float4* pvs = reinterpret_cast<float4*>(part + kFuseWarps * kFuseSP);  // (v hi, v lo, s, -)
-  double* red = reinterpret_cast<double*>(pvs + 2 * kFuseSP);
+  Dot2* ovf = reinterpret_cast<Dot2*>(pvs + 2 * kFuseSP);  // rows i >= kFuseRegRowsTotal
+  double* red = reinterpret_cast<double*>(ovf + (kFuseMaxShells - kFuseRegRowsTotal));
   int* act = reinterpret_cast<int*>(red + 2 * kFuseWarps + 2);
   int* pos = act + S;
   int* aoff = pos + S;  // atom a's active rows: [aoff[a], aoff[a + 1]) (act is ordered by shell)
@@ -592,6 +597,7 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_fused_ff(Batch bt, in
       xa[i] = split2(x[m]);
       xkey[i] = m * 32 + ((m & 7) << 2);
       if (chg) dca[i] = (float)(J.propars[m] - J.propars_old[m]);
+      if (i >= kFuseRegRowsTotal) ovf[i - kFuseRegRowsTotal] = Dot2{0.f, 0.f};
     }
     if (chg)
       for (int a = threadIdx.x; a <= natom; a += kFuseThreads) {
@@ -604,12 +610,8 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_fused_ff(Batch bt, in
         }
         aoff[a] = lo;
       }
-    // this warp's rows i = warp + 8 r, r < nr; with one staging buffer the
-    // next sub-tile loads once the rows are in registers, unless some rows
-    // are read from the buffer again in B (more than 8 kRegRows active rows)
-    // or the change reads it after A
+    // this warp's rows i = warp + 8 r, r < nr
     const int nr = nact > warp ? (nact - warp + kFuseWarps - 1) / kFuseWarps : 0;
-    const bool early = nact <= kFuseWarps * kRegRows && !chg;
     float ch = 0.0f, cl = 0.0f;  // change terms of this thread (float pair)
     Dot2 acc[kFuseRows];
 #pragma unroll
@@ -618,7 +620,7 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_fused_ff(Batch bt, in
       const float* gh = stg + (nbuf == 2 ? (sub & 1) : 0) * 2 * plane;
       const float* gl = gh + plane;
       const int q0 = p0 + sub * kFuseSP;
-      if (nbuf == 1 && sub > 0 && !early) {  // the buffer was read until the end of sub - 1
+      if (nbuf == 1 && sub > 0) {  // the buffer was read until the end of sub - 1
         __syncthreads();
         fuse_load(g32, glo, NN, q0, p1, stg, stg + plane, vec, act, nact);
         cp_async_commit();
@@ -651,26 +653,20 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_fused_ff(Batch bt, in
         cp_async_commit();
       }
       // A: rows r even in chain d, odd in chain e
-      float rh[kRegRows], rl[kRegRows];
+      const float* ghw = gh + warp * kFuseSP + lane;
+      const float* glw = gl + warp * kFuseSP + lane;
       {
-        const float* ghw = gh + warp * kFuseSP + lane;
-        const float* glw = gl + warp * kFuseSP + lane;
         Dot2 d{0.f, 0.f}, e{0.f, 0.f};
-#pragma unroll
-        for (int r = 0; r < kRegRows; ++r) {
-          if (r < nr) {
-            const float2 xx = xa[warp + kFuseWarps * r];
-            rh[r] = ghw[r * kFuseWarps * kFuseSP];
-            rl[r] = glw[r * kFuseWarps * kFuseSP];
-            if (r & 1) dot2_add(e, rh[r], rl[r], xx.x, xx.y);
-            else dot2_add(d, rh[r], rl[r], xx.x, xx.y);
-          }
+        int r = 0;
+        for (; r + 1 < nr; r += 2) {
+          const float2 x1 = xa[warp + kFuseWarps * r], x2 = xa[warp + kFuseWarps * (r + 1)];
+          dot2_add(d, ghw[r * kFuseWarps * kFuseSP], glw[r * kFuseWarps * kFuseSP], x1.x, x1.y);
+          dot2_add(e, ghw[(r + 1) * kFuseWarps * kFuseSP], glw[(r + 1) * kFuseWarps * kFuseSP], x2.x,
+                   x2.y);
         }
-        for (int r = kRegRows; r < nr; ++r) {
-          const float2 xx = xa[warp + kFuseWarps * r];
-          const float g1 = ghw[r * kFuseWarps * kFuseSP], g2 = glw[r * kFuseWarps * kFuseSP];
-          if (r & 1) dot2_add(e, g1, g2, xx.x, xx.y);
-          else dot2_add(d, g1, g2, xx.x, xx.y);
+        if (r < nr) {
+          const float2 x1 = xa[warp + kFuseWarps * r];
+          dot2_add(d, ghw[r * kFuseWarps * kFuseSP], glw[r * kFuseWarps * kFuseSP], x1.x, x1.y);
         }
         dot2_merge(d, e);
         part[warp * kFuseSP + lane] = d;
@@ -713,10 +709,6 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_fused_ff(Batch bt, in
         }
       }
       __syncthreads();  // v and s of the sub-tile visible
-      if (nbuf == 1 && early && sub + 1 < nsub) {  // rows in registers: the buffer is free
-        fuse_load(g32, glo, NN, q0 + kFuseSP, p1, stg, stg + plane, vec, act, nact);
-        cp_async_commit();
-      }
       const float4 pv = pvs[lane];
       const f2 v{pv.x, pv.y};
       const float sx = pv.z;
@@ -725,18 +717,23 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_fused_ff(Batch bt, in
 #pragma unroll
       for (int r = 0; r < kFuseRows; ++r) {
         if (r < nr) {
-          const int i = warp + kFuseWarps * r;
-          float g1, g2;
-          if (r < kRegRows) {
-            g1 = rh[r];
-            g2 = rl[r];
-          } else {
-            g1 = gh[i * kFuseSP + lane];
-            g2 = gl[i * kFuseSP + lane];
-          }
-          if (hess) xt[xkey[i] ^ lane] = umma::to_tf32_rn(g1 * sx);
+          const float g1 = ghw[r * kFuseWarps * kFuseSP], g2 = glw[r * kFuseWarps * kFuseSP];
+          if (hess) xt[xkey[warp + kFuseWarps * r] ^ lane] = umma::to_tf32_rn(g1 * sx);
           dot2_add(acc[r], g1, g2, v.hi, v.lo);
         }
+      }
+      for (int r = kFuseRows; r < nr; ++r) {  // rows past the register sums: lane sum per sub-tile
+        const int i = warp + kFuseWarps * r;
+        const float g1 = ghw[r * kFuseWarps * kFuseSP], g2 = glw[r * kFuseWarps * kFuseSP];
+        if (hess) xt[xkey[i] ^ lane] = umma::to_tf32_rn(g1 * sx);
+        Dot2 t{0.f, 0.f};
+        dot2_add(t, g1, g2, v.hi, v.lo);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+          const Dot2 b{__shfl_xor_sync(0xffffffffu, t.s, o), __shfl_xor_sync(0xffffffffu, t.c, o)};
+          dot2_merge(t, b);
+        }
+        if (lane == 0) dot2_merge(ovf[i - kFuseRegRowsTotal], t);
       }
       if (hess) asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     }
@@ -758,6 +755,11 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_fused_ff(Batch bt, in
         if (lane == 0) J.gpart[(size_t)act[i] * J.ntile + tile] = dot2_value(d);
       }
     }
+    for (int r = kFuseRows; r < nr; ++r)
+      if (lane == 0) {
+        const int i = warp + kFuseWarps * r;
+        J.gpart[(size_t)act[i] * J.ntile + tile] = dot2_value(ovf[i - kFuseRegRowsTotal]);
+      }
     zero_inactive(J, tile, pos);
     if (chg) {
       double c = (double)ch + (double)cl;

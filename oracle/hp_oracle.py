@@ -639,6 +639,11 @@ def basis_scheme(scheme, coordinates, numbers, pseudo_numbers, points, weights, 
                                           density_cutoff)
                 propars[sl] = new
                 its.append(nit)
+            elif solver == "sc-1-iter":  # alisa.py:294-353: one update, no test
+                pro_shells, _, _, ratio, _ = compute_quantities(rhoa, propars[sl], ga,
+                                                                density_cutoff)
+                propars[sl] = np.einsum("p,ip->i", wa, pro_shells * ratio)
+                its.append(1)
             elif solver in ("newton", "m-newton"):
                 new, nit = lisa_solver_newton(
                     ga, rhoa, propars[sl].copy(), wa, inner,

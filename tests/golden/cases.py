@@ -20,6 +20,10 @@ CASES = {
                             kwargs=dict(threshold=1e-8, inner_threshold=1e-8, solver="quadprog")),
     "lisa_sc_h2o_50x110": dict(scheme="lisa", mol=("water", 50, 110),
                                kwargs=dict(threshold=1e-8, inner_threshold=1e-8, solver="sc")),
+    # one SC update per outer iteration (alisa.py:294-353)
+    "lisa_sc1iter_h2o_50x110": dict(scheme="lisa", mol=("water", 50, 110),
+                                    kwargs=dict(threshold=1e-8, inner_threshold=1e-8,
+                                                solver="sc-1-iter")),
     "lisa_mnewton_h2o_50x110": dict(scheme="lisa", mol=("water", 50, 110),
                                     kwargs=dict(threshold=1e-8, inner_threshold=1e-8,
                                                 solver="m-newton")),

@@ -700,6 +700,16 @@ def run_ours(args):
             "niter_mixed": int(im.niter)}
         if w["scheme"] == "glisa":
             line["accuracy_vs_fp64"]["newton_fp64_factors"] = int(im.f64_factors)
+        fixture = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tests", "golden",
+                               "glisa_nonneg_c6h10n2o2_100x302.npz")
+        if w["name"] == "glisa-c6h10n2o2" and os.path.exists(fixture):
+            # the optimum of the reference's cvxopt problem on this input, certified
+            # by its KKT residuals (tests/golden/make_glisa_nonneg.py)
+            with np.load(fixture) as f:
+                opt = f["charges"]
+            line["accuracy_vs_certified_optimum"] = {
+                "max_abs_dq_e_mixed": float(np.abs(rm["charges"] - opt).max()),
+                "max_abs_dq_e_fp64": float(np.abs(rd["charges"] - opt).max())}
     if rank == 0 and world == 1 and args.workload == "glisa-c6h10n2o2" and not args.no_extras:
         line.update(extra_sections(ctx, args, w))
     if rank == 0 and world == 1 and not args.no_cpu:

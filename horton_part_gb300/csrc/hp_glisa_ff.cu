@@ -76,27 +76,6 @@ __device__ __forceinline__ int point_in_tile(const JobDev& J, int tile, int i) {
 // 2^(i/64) as float pairs for ffa::exp_ff (this translation unit's copy).
 __constant__ float2 c_exp2_gl[64];
 
-// Asynchronous global -> shared copies (cp.async); a source size of 0
-// writes zeros without reading.
-__device__ __forceinline__ void cp_async4(float* dst, const float* src, bool full) {
-  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(d), "l"(src), "r"(full ? 4 : 0)
-               : "memory");
-}
-
-__device__ __forceinline__ void cp_async16(float* dst, const float* src, bool full) {
-  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(d), "l"(src), "r"(full ? 16 : 0)
-               : "memory");
-}
-
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-
-template <int N>
-__device__ __forceinline__ void cp_async_wait() {
-  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
-}
-
 // FP64 vector -> float pairs in shared memory (all threads; ends with a barrier).
 __device__ __forceinline__ void load_pairs(const double* v, int n, float2* out) {
   for (int i = threadIdx.x; i < n; i += blockDim.x) out[i] = split2(v[i]);
@@ -368,49 +347,22 @@ constexpr int kFuseRegRowsTotal = kFuseWarps * kFuseRows;
 // Shared memory of one block at most (two blocks per SM share 228 KB).
 constexpr size_t kFuseSmemMax = 112 * 1024;
 
-// Shared memory of a fused pass for S shells with nbuf staging buffers (bytes).
-__host__ __device__ constexpr size_t fuse_smem_bytes(int S, int nbuf) {
-  return 2 * (size_t)nbuf * S * kFuseSP * 4  // staging: both planes per buffer
-         + 16 * (size_t)S                    // per active row: x pair and the parameter change
+// The packed sub-tiles of G (gpack: per sub-tile nact rows x 32 points, one
+// contiguous block per plane) reach shared memory by TMA bulk copies into a
+// ring of slots of 2 nact x 128 bytes: as many slots (at most kRingSlots,
+// one mbarrier each) as the ring holds for the tile's nact, so that the
+// copies of the next sub-tiles are in flight while one is processed.
+constexpr int kRingSlots = 6;
+
+// Shared memory of a fused pass for S shells without its staging ring (bytes).
+__host__ __device__ constexpr size_t fuse_fixed_bytes(int S) {
+  return 16 * (size_t)S                    // per active row: x pair and the parameter change
          + 8 * (size_t)kFuseWarps * kFuseSP  // partial sums
          + 32 * (size_t)kFuseSP              // per point: (v, s)
          + 8 * (size_t)(kFuseMaxShells - kFuseRegRowsTotal)  // gradient sums of the rows past them
          + 8 * (2 * kFuseWarps + 2)          // block sums
-         + 16 * (size_t)S + 8;               // active shells, positions, per-atom offsets, X keys
-}
-
-// Sub-tile [q0, q0 + kFuseSP) of the tile's active rows (act[0..nact), the
-// shells with a nonzero value in the tile) of both planes into gh / gl
-// ([nact][kFuseSP], row i holds shell act[i]); columns at or past p1 are
-// zero-filled. vec: 16-byte copies (npoint % 4 == 0, so every row segment
-// starts 16-byte aligned and p1 is a multiple of 4). The job's pointers come
-// in registers: the cp.async statements clobber memory, which would otherwise
-// reload them from the job table on every call.
-__device__ __forceinline__ void fuse_load(const float* __restrict__ g32, const float* __restrict__ glo,
-                                          size_t N, int q0, int p1, float* gh, float* gl, bool vec,
-                                          const int* act, int nact) {
-  if (vec) {
-    constexpr int C = kFuseSP / 4;  // 16-byte chunks per row
-    const int c = threadIdx.x % C;
-    const int p = q0 + 4 * c;
-    const bool in = p < p1;
-    const int pc = in ? p : q0;
-    for (int i = threadIdx.x / C; i < nact; i += kFuseThreads / C) {
-      const size_t off = (size_t)act[i] * N + pc;
-      cp_async16(gh + i * kFuseSP + 4 * c, g32 + off, in);
-      cp_async16(gl + i * kFuseSP + 4 * c, glo + off, in);
-    }
-  } else {
-    const int c = threadIdx.x % kFuseSP;
-    const int p = q0 + c;
-    const bool in = p < p1;
-    const int pc = in ? p : q0;
-    for (int i = threadIdx.x / kFuseSP; i < nact; i += kFuseThreads / kFuseSP) {
-      const size_t off = (size_t)act[i] * N + pc;
-      cp_async4(gh + i * kFuseSP + c, g32 + off, in);
-      cp_async4(gl + i * kFuseSP + c, glo + off, in);
-    }
-  }
+         + 16 * (size_t)S + 8                // active shells, positions, per-atom offsets, X keys
+         + 16 + 8 * kRingSlots;              // the ring's mbarriers (16-byte aligned)
 }
 
 // The tile's active-shell list into shared memory: act[0..nact) ascending and
@@ -444,19 +396,21 @@ __host__ __device__ constexpr int fuse_x_rows(int S) {
   return (S + 15) / 16 * 16 > umma::kTcM ? (S + 15) / 16 * 16 : umma::kTcM;
 }
 constexpr size_t kFuseSmemFloor = 78 * 1024;
-__host__ __device__ constexpr size_t fuse_hess_smem_bytes(int S, int nbuf) {
-  return fuse_smem_bytes(S, nbuf) + 128 * (size_t)fuse_x_rows(S) + 1024 + 64 > kFuseSmemFloor
-             ? fuse_smem_bytes(S, nbuf) + 128 * (size_t)fuse_x_rows(S) + 1024 + 64
-             : kFuseSmemFloor;
+__host__ __device__ constexpr size_t fuse_fixed_bytes(int S, int mode) {
+  return mode ? fuse_fixed_bytes(S) + 128 * (size_t)fuse_x_rows(S) + 1024 + 64 : fuse_fixed_bytes(S);
 }
 constexpr int kFuseTmemCols = 256;
 
-// Staging buffers of a fused pass over jobs of at most S shells: two when
-// the block's shared memory stays within kFuseSmemMax.
-__host__ __device__ constexpr int fuse_nbuf(int S, int mode) {
-  return (mode ? fuse_hess_smem_bytes(S, 2) : fuse_smem_bytes(S, 2)) <= kFuseSmemMax ? 2 : 1;
+// The staging ring of a fused pass over jobs of at most S shells (floats):
+// the rest of kFuseSmemMax (at least kFuseSmemFloor in all), in 128-byte
+// units. It must hold one sub-tile of the job's largest tile.
+__host__ __device__ constexpr int fuse_ring_floats(int S, int mode) {
+  return (int)((kFuseSmemMax - fuse_fixed_bytes(S, mode)) / 128 * 32);
 }
-static_assert(fuse_hess_smem_bytes(kFuseMaxShells, 1) <= kFuseSmemMax, "fused pass shared memory");
+static_assert(fuse_ring_floats(kFuseMaxShells, 1) >= 2 * kFuseMaxShells * kFuseSP,
+              "fused pass shared memory: one sub-tile of the largest tile");
+static_assert(fuse_fixed_bytes(kFuseMaxShells, 1) + 4 * (size_t)fuse_ring_floats(kFuseMaxShells, 1) >=
+                  kFuseSmemFloor, "at most two blocks per SM");
 
 // Persistent blocks (launch kind K_FUSE): block b of a job takes the point
 // tiles b, b + nb, ... (nb = min(ntile, kFuseCtas)). The per-tile outputs
@@ -489,7 +443,7 @@ static_assert(fuse_hess_smem_bytes(kFuseMaxShells, 1) <= kFuseSmemMax, "fused pa
 // MODE 1 writes rho0 (r0f); the entropy, the negativity count and w rho /
 // rho0^2 (d2f) follow in k_glisa_point_ff.
 template <int MODE>
-__global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_fused_ff(Batch bt, int with_change, int nbuf) {
+__global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_fused_ff(Batch bt, int with_change, int ring_floats) {
   extern __shared__ float4 fsm[];
   int local;
   const JobDev& J = decode_local_gf(bt, local);
@@ -505,10 +459,8 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_fused_ff(Batch bt, in
   const uint32_t xoff = hess ? ((1024u - (raw & 1023u)) & 1023u) : 0u;
   const int xrows = fuse_x_rows(S);
   uint32_t* xt = reinterpret_cast<uint32_t*>(reinterpret_cast<uint8_t*>(fsm) + xoff);
-  float* stg = hess ? reinterpret_cast<float*>(xt + 32 * xrows) : reinterpret_cast<float*>(fsm);
-  // buffer k: high plane at stg + 2 k S kFuseSP, low plane S kFuseSP after it
-  const int plane = S * kFuseSP;
-  float2* xa = reinterpret_cast<float2*>(stg + 2 * nbuf * plane);  // x of active row i
+  float* ring = hess ? reinterpret_cast<float*>(xt + 32 * xrows) : reinterpret_cast<float*>(fsm);
+  float2* xa = reinterpret_cast<float2*>(ring + ring_floats);  // x of active row i
   float* dca = reinterpret_cast<float*>(xa + S);                   // change of active row i
   Dot2* part = reinterpret_cast<Dot2*>(dca + 2 * S);
   float4* pvs = reinterpret_cast<float4*>(part + kFuseWarps * kFuseSP);  // (v hi, v lo, s, -)
@@ -518,15 +470,12 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_fused_ff(Batch bt, in
   int* pos = act + S;
   int* aoff = pos + S;  // atom a's active rows: [aoff[a], aoff[a + 1]) (act is ordered by shell)
   int* xkey = aoff + S + 2;
-  uint64_t* mbar = reinterpret_cast<uint64_t*>((reinterpret_cast<uintptr_t>(xkey + S) + 15) & ~uintptr_t(15));
+  uint64_t* rbar = reinterpret_cast<uint64_t*>((reinterpret_cast<uintptr_t>(xkey + S) + 15) & ~uintptr_t(15));
+  uint64_t* mbar = rbar + kRingSlots;  // the MMAs' commits (MODE 1)
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(mbar + 1);
   __shared__ volatile int timed_out;
   const float2 cutp = split2(J.density_cutoff);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const bool vec = (J.npoint & 3) == 0;
-  const float* __restrict__ g32 = J.gmat32;
-  const float* __restrict__ glo = J.gmat_lo;
-  const size_t NN = J.npoint;
   const float4* __restrict__ wrfp = J.wrf;
   const float2* __restrict__ d2in = J.d2f;
   const double* __restrict__ wp = J.w;
@@ -536,6 +485,13 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_fused_ff(Batch bt, in
   const int c2 = (n1 + 31) / 32 * 32;
   const bool has_d2 = n1 > umma::kTcM;
   const uint32_t bar = umma::smem_u32(mbar);
+  const uint32_t rbar0 = umma::smem_u32(rbar);
+  if (threadIdx.x == 0) {
+    for (int b = 0; b < kRingSlots; ++b) umma::mbar_init(rbar0 + 8 * b, 1);
+    timed_out = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;");
+  }
+  uint32_t ring_phase = 0;  // bit b: parity of the next completion of slot b
   uint32_t tmem = 0;
   int nmma = 0;  // sub-tiles whose MMAs have been issued (= commits on bar)
   if (hess) {
@@ -547,7 +503,6 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_fused_ff(Batch bt, in
     }
     if (threadIdx.x == 0) {
       umma::mbar_init(bar, 1);
-      timed_out = 0;
       asm volatile("fence.mbarrier_init.release.cluster;");
     }
     asm volatile("tcgen05.fence::before_thread_sync;");
@@ -590,8 +545,24 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_fused_ff(Batch bt, in
     __syncthreads();  // shared state of the previous tile no longer in use
     const int nact = load_active(J, tile, act, pos);
     __syncthreads();
-    fuse_load(g32, glo, NN, p0, p1, stg, stg + plane, vec, act, nact);
-    cp_async_commit();
+    // staging ring for this tile: nslot slots of slotf floats (high plane,
+    // then low plane, nact rows of 32 points each); thread 0 keeps the
+    // copies of nslot - 1 sub-tiles ahead in flight
+    const int slotf = 2 * nact * kFuseSP;
+    const int nslot = nact > 0 ? min(kRingSlots, max(1, ring_floats / slotf)) : 1;
+    const float* src = J.gpack + J.gtile_off[tile];
+    auto issue = [&](int k) {
+      const int b = k % nslot;
+      const uint32_t bytes = (uint32_t)nact * kFuseSP * 4;
+      umma::mbar_expect_tx(rbar0 + 8 * b, 2 * bytes);
+      if (bytes) {
+        const uint32_t dst = umma::smem_u32(ring + (size_t)b * slotf);
+        umma::bulk_g2s(dst, src + (size_t)k * nact * kFuseSP, bytes, rbar0 + 8 * b);
+        umma::bulk_g2s(dst + bytes, src + J.gpack_plane + (size_t)k * nact * kFuseSP, bytes, rbar0 + 8 * b);
+      }
+    };
+    if (threadIdx.x == 0)
+      for (int k2 = 0; k2 < nslot - 1 && k2 < nsub; ++k2) issue(k2);
     for (int i = threadIdx.x; i < nact; i += kFuseThreads) {
       const int m = act[i];
       xa[i] = split2(x[m]);
@@ -617,20 +588,18 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_fused_ff(Batch bt, in
 #pragma unroll
     for (int r = 0; r < kFuseRows; ++r) acc[r] = Dot2{0.f, 0.f};
     for (int sub = 0; sub < nsub; ++sub) {
-      const float* gh = stg + (nbuf == 2 ? (sub & 1) : 0) * 2 * plane;
-      const float* gl = gh + plane;
+      const int slot = sub % nslot;
+      const float* gh = ring + (size_t)slot * slotf;
+      const float* gl = gh + nact * kFuseSP;
       const int q0 = p0 + sub * kFuseSP;
-      if (nbuf == 1 && sub > 0) {  // the buffer was read until the end of sub - 1
-        __syncthreads();
-        fuse_load(g32, glo, NN, q0, p1, stg, stg + plane, vec, act, nact);
-        cp_async_commit();
+      __syncthreads();  // every thread is done with sub - 1 (its slot is free)
+      if (threadIdx.x == 0) {
+        if (sub + nslot - 1 < nsub) issue(sub + nslot - 1);
+        if (hess && sub > 0 && !timed_out) issue_mma();  // X of sub - 1 is complete: its MMAs
       }
-      cp_async_wait<0>();
-      __syncthreads();  // sub-tile sub visible; every thread is done with sub - 1
-      if (hess && sub > 0) {  // X of sub - 1 is complete: its MMAs
-        if (threadIdx.x == 0 && !timed_out) issue_mma();
-        ++nmma;
-      }
+      if (hess && sub > 0) ++nmma;
+      if (!umma::mbar_wait_sleep(rbar0 + 8 * slot, (ring_phase >> slot) & 1u)) timed_out = 1;
+      ring_phase ^= 1u << slot;  // sub-tile sub is in the slot
       // per-point inputs, loaded before phase A so that their latency
       // overlaps it: (w rho, rho) pairs (MODE 1) or the d2 pair (MODE 0) for
       // warp 0, w for the change warps
@@ -646,11 +615,6 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_fused_ff(Batch bt, in
           }
         }
         if (chg && warp > 0) wf = (float)wp[pq];
-      }
-      if (nbuf == 2 && sub + 1 < nsub) {
-        float* nh = stg + ((sub + 1) & 1) * 2 * plane;  // last read in sub - 1
-        fuse_load(g32, glo, NN, q0 + kFuseSP, p1, nh, nh + plane, vec, act, nact);
-        cp_async_commit();
       }
       // A: rows r even in chain d, odd in chain e
       const float* ghw = gh + warp * kFuseSP + lane;
@@ -887,8 +851,8 @@ __global__ void __launch_bounds__(kThreads) k_glisa_point_ff(Batch bt) {
 }
 
 // Trial objective differences for fused jobs: k_glisa_u_ff and
-// k_glisa_trials_ff in one pass over staged sub-tiles (as k_glisa_fused_ff,
-// two staging buffers). Per sub-tile: A forms the eight warps' partial sums
+// k_glisa_trials_ff in one pass over staged sub-tiles (as k_glisa_fused_ff:
+// the packed sub-tiles by TMA bulk copies into a staging ring). Per sub-tile: A forms the eight warps' partial sums
 // of u = G^T delta and C the clipped-shell group sums (warp g: group g);
 // then warp 0 merges the partials (warp order) into u and the groups into
 // their suffix sums (group kTrials - 1 first), so that trial t reads the sum
@@ -897,28 +861,30 @@ __global__ void __launch_bounds__(kThreads) k_glisa_point_ff(Batch bt) {
 // go to tpart at its end.
 static_assert(kTrials == kFuseWarps, "one warp per trial step");
 
-// Shared memory of the trial pass for S shells (bytes).
-__host__ __device__ constexpr size_t trials_smem_bytes(int S) {
-  return 4 * (size_t)S * kFuseSP * 4                // two staging buffers, both planes
-         + 16 * (size_t)kTrials * kFuseSP           // group sums, then their suffix sums
+// Shared memory of the trial pass for S shells without its staging ring (bytes).
+__host__ __device__ constexpr size_t trials_fixed_bytes(int S) {
+  return 16 * (size_t)kTrials * kFuseSP           // group sums, then their suffix sums
          + 8 * (size_t)kFuseWarps * kFuseSP         // partial sums of u
          + 8 * (size_t)kFuseSP                      // u per point
          + 512                                      // exp table
          + 8 * (size_t)S                            // delta as float pairs
-         + 12 * (size_t)S + 16;                     // act, pos, clipped shells' rows
+         + 12 * (size_t)S + 16                      // act, pos, clipped shells' rows
+         + 16 + 8 * kRingSlots;                     // the ring's mbarriers
 }
-static_assert(trials_smem_bytes(kFuseMaxShells) <= kFuseSmemMax, "trial pass shared memory");
+__host__ __device__ constexpr int trials_ring_floats(int S) {
+  return (int)((kFuseSmemMax - trials_fixed_bytes(S)) / 128 * 32);
+}
+static_assert(trials_ring_floats(kFuseMaxShells) >= 2 * kFuseMaxShells * kFuseSP, "trial pass shared memory");
 
-__global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_trials_fused(Batch bt) {
+__global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_trials_fused(Batch bt, int ring_floats) {
   extern __shared__ float4 fsm[];
   int tile;
   const JobDev& J = decode_local_gf(bt, tile);
   if (glisa_idle(J)) return;
   if (!J.fuse) return;
   const int S = J.nshell;
-  float* stg = reinterpret_cast<float*>(fsm);
-  const int plane = S * kFuseSP;
-  float4* grp = reinterpret_cast<float4*>(stg + 4 * plane);  // [kTrials][kFuseSP]
+  float* ring = reinterpret_cast<float*>(fsm);
+  float4* grp = reinterpret_cast<float4*>(ring + ring_floats);  // [kTrials][kFuseSP]
   Dot2* part = reinterpret_cast<Dot2*>(grp + kTrials * kFuseSP);
   float2* uv = reinterpret_cast<float2*>(part + kFuseWarps * kFuseSP);
   float2* tab = uv + kFuseSP;  // exp table
@@ -926,20 +892,38 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_trials_fused(Batch bt
   int* act = reinterpret_cast<int*>(xv + S);
   int* pos = act + S;
   int* cpos = pos + S;  // per clipped shell its active row on this tile (-1: zero here)
+  uint64_t* rbar = reinterpret_cast<uint64_t*>((reinterpret_cast<uintptr_t>(cpos + S) + 15) & ~uintptr_t(15));
+  const uint32_t rbar0 = umma::smem_u32(rbar);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int p0 = tile * J.tile_points;
   const int p1 = min(p0 + J.tile_points, J.npoint);
   const int nsub = (p1 - p0 + kFuseSP - 1) / kFuseSP;
-  const bool vec = (J.npoint & 3) == 0;
-  const float* __restrict__ g32 = J.gmat32;
-  const float* __restrict__ glo = J.gmat_lo;
-  const size_t NN = J.npoint;
   const float2* __restrict__ r0in = J.r0f;
   const float4* __restrict__ wrfp = J.wrf;
+  if (threadIdx.x == 0) {
+    for (int b = 0; b < kRingSlots; ++b) umma::mbar_init(rbar0 + 8 * b, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;");
+  }
   const int nact = load_active(J, tile, act, pos);
   __syncthreads();
-  fuse_load(g32, glo, NN, p0, p1, stg, stg + plane, vec, act, nact);
-  cp_async_commit();
+  // staging ring (as k_glisa_fused_ff)
+  const int slotf = 2 * nact * kFuseSP;
+  const int nslot = nact > 0 ? min(kRingSlots, max(1, ring_floats / slotf)) : 1;
+  const float* src = J.gpack + J.gtile_off[tile];
+  uint32_t ring_phase = 0;
+  int timed_out = 0;
+  auto issue = [&](int k) {
+    const int b = k % nslot;
+    const uint32_t bytes = (uint32_t)nact * kFuseSP * 4;
+    umma::mbar_expect_tx(rbar0 + 8 * b, 2 * bytes);
+    if (bytes) {
+      const uint32_t dst = umma::smem_u32(ring + (size_t)b * slotf);
+      umma::bulk_g2s(dst, src + (size_t)k * nact * kFuseSP, bytes, rbar0 + 8 * b);
+      umma::bulk_g2s(dst + bytes, src + J.gpack_plane + (size_t)k * nact * kFuseSP, bytes, rbar0 + 8 * b);
+    }
+  };
+  if (threadIdx.x == 0)
+    for (int k2 = 0; k2 < nslot - 1 && k2 < nsub; ++k2) issue(k2);
   for (int i = threadIdx.x; i < nact; i += kFuseThreads) xv[i] = split2(J.delta[act[i]]);  // by active row
   const int t = warp;  // this warp's trial: step 2^-t
   const float at = ldexpf(1.0f, -t);
@@ -961,10 +945,11 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_trials_fused(Batch bt
   if (threadIdx.x < 64) tab[threadIdx.x] = c_exp2_gl[threadIdx.x];
   float ah = 0.0f, al = 0.0f;
   for (int sub = 0; sub < nsub; ++sub) {
-    const float* gh = stg + (sub & 1) * 2 * plane;
-    const float* gl = gh + plane;
-    cp_async_wait<0>();
-    __syncthreads();
+    const int slot = sub % nslot;
+    const float* gh = ring + (size_t)slot * slotf;
+    const float* gl = gh + nact * kFuseSP;
+    __syncthreads();  // every thread is done with sub - 1 (its slot is free)
+    if (threadIdx.x == 0 && sub + nslot - 1 < nsub) issue(sub + nslot - 1);
     const int pq = p0 + sub * kFuseSP + lane;  // this lane's point: inputs loaded before A
     float2 r0pre = make_float2(0.f, 0.f);
     float4 qpre = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -972,11 +957,8 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_trials_fused(Batch bt
       r0pre = r0in[pq];
       qpre = wrfp[pq];
     }
-    if (sub + 1 < nsub) {
-      float* nh = stg + ((sub + 1) & 1) * 2 * plane;
-      fuse_load(g32, glo, NN, p0 + (sub + 1) * kFuseSP, p1, nh, nh + plane, vec, act, nact);
-      cp_async_commit();
-    }
+    if (!umma::mbar_wait_sleep(rbar0 + 8 * slot, (ring_phase >> slot) & 1u)) timed_out = 1;
+    ring_phase ^= 1u << slot;
     {  // A (active rows i = warp mod 8; delta compacted by active row)
       Dot2 d{0.f, 0.f}, e{0.f, 0.f};
       int i = warp;
@@ -1065,6 +1047,7 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_trials_fused(Batch bt
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   if (lane == 0) J.tpart[(size_t)t * J.ntile + tile] = v;
+  if (timed_out && lane == 0) atomicOr(&J.mail->i[MI_ERR], E_TIMEOUT);
 }
 
 // Outer change (glisa.py:776 via compute_change): sum over atoms of
@@ -1133,6 +1116,35 @@ __global__ void __launch_bounds__(kThreads) k_glisa_active(Batch bt) {
     for (int m = 0; m < S; ++m)
       if (flag[m]) g[n++] = m;
     g[S] = n;
+  }
+}
+
+// The active rows of every point tile of a fused job packed per 32-point
+// sub-tile (after k_glisa_active): sub-tile s of tile t holds its nact rows
+// of 32 points contiguously, gpack[gtile_off[t] + (s nact + i) 32 + l] =
+// G[act[i]][p0 + 32 s + l] (0 past the job's last point), the low plane
+// gpack_plane floats after the high one. One block per tile.
+__global__ void __launch_bounds__(kThreads) k_glisa_pack(Batch bt) {
+  int tile;
+  const JobDev& J = decode_local_gf(bt, tile);
+  if (!J.fuse || !J.gpack) return;
+  const int S = J.nshell;
+  const int* act = J.gact + (size_t)tile * (S + 1);
+  const int nact = act[S];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int p0 = tile * J.tile_points;
+  const int p1 = min(p0 + J.tile_points, J.npoint);
+  const int nsub = (p1 - p0 + 31) / 32;
+  const size_t N = J.npoint;
+  float* hi = J.gpack + J.gtile_off[tile];
+  float* lo = hi + J.gpack_plane;
+  for (int e = warp; e < nsub * nact; e += kWarps) {
+    const int sub = e / nact, i = e - sub * nact;
+    const int p = p0 + 32 * sub + lane;
+    const size_t src = (size_t)act[i] * N + p;
+    const size_t dst = ((size_t)sub * nact + i) * 32 + lane;
+    hi[dst] = p < p1 ? J.gmat32[src] : 0.0f;
+    lo[dst] = p < p1 ? J.gmat_lo[src] : 0.0f;
   }
 }
 
@@ -1218,18 +1230,17 @@ void launch_glisa_fused_ff(const HostBatch& hb, cudaStream_t st, int mode, int m
                            int with_change) {
   if (hb.blocks[K_FUSE] <= 0) return;
   ensure_exp_table_gl();
-  const int nbuf = fuse_nbuf(max_shells, mode);
+  const int ring = fuse_ring_floats(max_shells, mode);
+  const size_t smem = fuse_fixed_bytes(max_shells, mode) + 4 * (size_t)ring;
   if (mode) {
-    k_glisa_fused_ff<1><<<hb.blocks[K_FUSE], kFuseThreads, fuse_hess_smem_bytes(max_shells, nbuf),
-                          st>>>(hb.b[K_FUSE], with_change, nbuf);
+    k_glisa_fused_ff<1><<<hb.blocks[K_FUSE], kFuseThreads, smem, st>>>(hb.b[K_FUSE], with_change, ring);
     ++g_launch_count;
     if (hb.blocks[K_POINT] > 0) {
       k_glisa_point_ff<<<hb.blocks[K_POINT], kThreads, 0, st>>>(hb.b[K_POINT]);
       ++g_launch_count;
     }
   } else {
-    k_glisa_fused_ff<0><<<hb.blocks[K_FUSE], kFuseThreads, fuse_smem_bytes(max_shells, nbuf), st>>>(
-        hb.b[K_FUSE], 0, nbuf);
+    k_glisa_fused_ff<0><<<hb.blocks[K_FUSE], kFuseThreads, smem, st>>>(hb.b[K_FUSE], 0, ring);
     ++g_launch_count;
   }
 }
@@ -1237,13 +1248,18 @@ void launch_glisa_fused_ff(const HostBatch& hb, cudaStream_t st, int mode, int m
 void launch_glisa_trials_fused(const HostBatch& hb, cudaStream_t st, int max_shells) {
   if (hb.blocks[K_POINT] <= 0) return;
   ensure_exp_table_gl();
-  k_glisa_trials_fused<<<hb.blocks[K_POINT], kFuseThreads, trials_smem_bytes(max_shells), st>>>(
-      hb.b[K_POINT]);
+  const int ring = trials_ring_floats(max_shells);
+  k_glisa_trials_fused<<<hb.blocks[K_POINT], kFuseThreads,
+                         trials_fixed_bytes(max_shells) + 4 * (size_t)ring, st>>>(hb.b[K_POINT], ring);
   ++g_launch_count;
 }
 
 void launch_glisa_active(const HostBatch& hb, cudaStream_t st) {
   HP_LAUNCH_GF(k_glisa_active, K_POINT, kThreads);
+}
+
+void launch_glisa_pack(const HostBatch& hb, cudaStream_t st) {
+  HP_LAUNCH_GF(k_glisa_pack, K_POINT, kThreads);
 }
 
 void launch_glisa_promol_ff(const HostBatch& hb, cudaStream_t st) {

@@ -171,6 +171,11 @@ struct JobDev {
   float2* d2f;            // fused gLISA: w rho / rho0^2 as float pairs [npoint]
   double* hsum;           // gLISA tensor-core Hessian: refinement product H delta [nshell]
   int* gact;              // fused gLISA: per point tile the shells nonzero on it [ntile][nshell + 1]
+  float* gpack;           // fused gLISA: the tiles' active rows of G packed per 32-point sub-tile
+                          // ([sub-tile][active row][32 points], high plane then low plane)
+  int64_t* gtile_off;     // fused gLISA: start of tile t's sub-tiles in a plane of gpack (floats)
+  int64_t gpack_plane;    // fused gLISA: floats per plane of gpack
+  int nact_max;           // fused gLISA: most active rows of a tile
   float2* d1f;            // gLISA, gff: w rho / rho0 as float pairs, npoint
   float2* hvf;            // gLISA, gff: the refinement's hvec as float pairs, npoint
   float* hess_s;          // gLISA tensor-core Hessian: sqrt(w rho / rho0^2) as FP32, npoint
@@ -509,6 +514,7 @@ constexpr int kFuseCtas = 2 * 152;
 struct HostBatch {
   Batch b[K_NKIND];
   int blocks[K_NKIND];
+  int nact_max = 0;  // fused gLISA: most active rows of a tile over the batch's jobs
 };
 
 void launch_nelec(const HostBatch& hb, cudaStream_t st);
@@ -565,7 +571,8 @@ void launch_glisa_grad_ff(const HostBatch& hb, cudaStream_t st);
 void launch_glisa_hv_ff(const HostBatch& hb, cudaStream_t st);  // hvec and G hvec
 void launch_glisa_trials_ff(const HostBatch& hb, cudaStream_t st);
 void launch_glisa_promol_ff(const HostBatch& hb, cudaStream_t st);  // final promolecule
-void launch_glisa_active(const HostBatch& hb, cudaStream_t st);     // per-tile active shells
+void launch_glisa_active(const HostBatch& hb, cudaStream_t st);    // per-tile active shells
+void launch_glisa_pack(const HostBatch& hb, cudaStream_t st);      // active rows packed per sub-tile
 void launch_glisa_trials_fused(const HostBatch& hb, cudaStream_t st, int max_shells);
 void launch_atweights(const HostBatch& hb, cudaStream_t st);        // k_atweights alone
 void launch_glisa_change_ff(const HostBatch& hb, cudaStream_t st);

@@ -97,6 +97,8 @@ struct hp_job {
   int64_t g_active = -1; // fused gLISA: G values in the tiles' active rows (-1: not read yet)
   double skipped = 0.0;  // point-atom evaluations skipped by the per-atom cutoff
   bool host_driven = false;  // finished by hp_glisa_finish (histories kept by the host)
+  void* pack_mem = nullptr;  // fused gLISA: packed G (dev.gpack, dev.gtile_off)
+  size_t pack_bytes = 0;
   std::vector<double> changes;  // outer changes of this run
 };
 
@@ -192,7 +194,11 @@ int blocks_for(const JobDev& J, int kind) {
 // Upload the batch description (JobDev copies and per-kind block prefixes).
 int build_batch(hp_ctx* ctx, const std::vector<hp_job*>& jobs, HostBatch& hb) {
   const int n = (int)jobs.size();
-  for (int j = 0; j < n; ++j) ctx->batch_host[j] = jobs[j]->dev;
+  hb.nact_max = 0;
+  for (int j = 0; j < n; ++j) {
+    ctx->batch_host[j] = jobs[j]->dev;
+    hb.nact_max = std::max(hb.nact_max, jobs[j]->dev.nact_max);
+  }
   HP_CK(cudaMemcpyAsync(ctx->batch_dev, ctx->batch_host, sizeof(JobDev) * n,
                         cudaMemcpyHostToDevice, ctx->stream));
   for (int k = 0; k < K_NKIND; ++k) {
@@ -275,6 +281,50 @@ int run_inner(hp_ctx* ctx, const std::vector<hp_job*>& jobs, const HostBatch& hb
   return HP_OK;
 }
 
+// Fused gLISA jobs: the packed layout of G's active rows (k_glisa_pack)
+// from the per-tile active-row counts of k_glisa_active: tile t's sub-tiles
+// start at gtile_off[t] in each plane and hold nact_t rows of 32 floats each.
+// The arrays are allocated at the first initialisation of a job (the counts
+// depend only on G) and charged to the context.
+int pack_layout(hp_ctx* ctx, const std::vector<hp_job*>& jobs) {
+  bool any = false;
+  for (hp_job* j : jobs) any |= j->dev.fuse && !j->dev.gpack;
+  if (!any) return HP_OK;
+  HP_CK(cudaStreamSynchronize(ctx->stream));
+  for (hp_job* j : jobs) {
+    JobDev& J = j->dev;
+    if (!J.fuse || J.gpack) continue;
+    const int S = J.nshell;
+    std::vector<int> g((size_t)(S + 1) * J.ntile);
+    HP_CK(cudaMemcpy(g.data(), J.gact, sizeof(int) * g.size(), cudaMemcpyDeviceToHost));
+    std::vector<int64_t> off(J.ntile);
+    int64_t total = 0;
+    int nmax = 0;
+    for (int t = 0; t < J.ntile; ++t) {
+      const int nact = g[(size_t)t * (S + 1) + S];
+      const int64_t pts = std::min<int64_t>(J.tile_points, (int64_t)J.npoint - (int64_t)t * J.tile_points);
+      const int64_t nsub = (pts + 31) / 32;
+      off[t] = total;
+      total += nsub * 32 * (int64_t)nact;
+      nmax = std::max(nmax, nact);
+    }
+    const size_t bytes = 2 * 4 * (size_t)std::max<int64_t>(total, 1) + 8 * (size_t)J.ntile;
+    if (ctx->used + bytes > ctx->budget) return fail(HP_ERR_NO_MEMORY, "HBM budget exceeded (packed G)");
+    void* mem = nullptr;
+    if (cudaMalloc(&mem, bytes) != cudaSuccess) return fail(HP_ERR_NO_MEMORY, "device allocation failed");
+    J.gpack = reinterpret_cast<float*>(mem);
+    J.gpack_plane = total;
+    J.gtile_off = reinterpret_cast<int64_t*>(reinterpret_cast<char*>(mem) + 2 * 4 * (size_t)std::max<int64_t>(total, 1));
+    J.nact_max = nmax;
+    j->pack_mem = mem;
+    j->pack_bytes = bytes;
+    j->bytes += bytes;
+    ctx->used += bytes;
+    HP_CK(cudaMemcpy(J.gtile_off, off.data(), 8 * (size_t)J.ntile, cudaMemcpyHostToDevice));
+  }
+  return HP_OK;
+}
+
 int job_init(hp_ctx* ctx, const std::vector<hp_job*>& jobs, const HostBatch& hb) {
   launch_nelec(hb, ctx->stream);
   bool any_basis = false, any_basis_ff = false, any_rdist = false;
@@ -293,7 +343,13 @@ int job_init(hp_ctx* ctx, const std::vector<hp_job*>& jobs, const HostBatch& hb)
   // promolecule and gradient
   if (fuse_shells > 0) {
     launch_glisa_active(hb, ctx->stream);
-    launch_glisa_fused_ff(hb, ctx->stream, 1, fuse_shells, 0);
+    int rc = pack_layout(ctx, jobs);
+    if (rc) return rc;
+    HostBatch hp;  // the jobs' descriptors now carry the packed arrays
+    rc = build_batch(ctx, jobs, hp);
+    if (rc) return rc;
+    launch_glisa_pack(hp, ctx->stream);
+    launch_glisa_fused_ff(hp, ctx->stream, 1, fuse_shells, 0);
   }
   for (hp_job* j : jobs) j->initialized = true;
   return check_launch();
@@ -1198,6 +1254,7 @@ int32_t hp_job_destroy(hp_job* job) {
   cudaSetDevice(ctx->device);
   cudaStreamSynchronize(ctx->stream);
   if (job->mem) cudaFree(job->mem);
+  if (job->pack_mem) cudaFree(job->pack_mem);
   ctx->used -= job->bytes;
   ctx->slots[job->slot] = nullptr;
   delete job;

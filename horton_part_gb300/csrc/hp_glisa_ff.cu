@@ -598,7 +598,8 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_fused_ff(Batch bt, in
         if (hess && sub > 0 && !timed_out) issue_mma();  // X of sub - 1 is complete: its MMAs
       }
       if (hess && sub > 0) ++nmma;
-      if (!umma::mbar_wait_sleep(rbar0 + 8 * slot, (ring_phase >> slot) & 1u)) timed_out = 1;
+      if (!timed_out && !umma::mbar_wait_sleep(rbar0 + 8 * slot, (ring_phase >> slot) & 1u))
+        timed_out = 1;
       ring_phase ^= 1u << slot;  // sub-tile sub is in the slot
       // per-point inputs, loaded before phase A so that their latency
       // overlaps it: (w rho, rho) pairs (MODE 1) or the d2 pair (MODE 0) for
@@ -957,7 +958,8 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_trials_fused(Batch bt
       r0pre = r0in[pq];
       qpre = wrfp[pq];
     }
-    if (!umma::mbar_wait_sleep(rbar0 + 8 * slot, (ring_phase >> slot) & 1u)) timed_out = 1;
+    if (!timed_out && !umma::mbar_wait_sleep(rbar0 + 8 * slot, (ring_phase >> slot) & 1u))
+      timed_out = 1;
     ring_phase ^= 1u << slot;
     {  // A (active rows i = warp mod 8; delta compacted by active row)
       Dot2 d{0.f, 0.f}, e{0.f, 0.f};

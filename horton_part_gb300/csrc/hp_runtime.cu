@@ -1079,7 +1079,9 @@ int32_t hp_job_create(hp_ctx* ctx, const hp_job_desc* d, hp_job** out) {
   auto up = [&](const void* dst, const void* src, size_t bytes) {
     return cudaMemcpyAsync((void*)dst, src, bytes, cudaMemcpyHostToDevice, st);
   };
-  bool ok = true;
+  // every work array starts at zero, as in a fresh allocation: a job's results
+  // never depend on what an earlier job left in recycled device memory
+  bool ok = cudaMemsetAsync(mem, 0, total, st) == cudaSuccess;
   for (int c = 0; c < 3 && ok; ++c) {
     for (int p = 0; p < N; ++p) buf[p] = d->points[(size_t)3 * p + c];
     const double* dst = c == 0 ? J.px : c == 1 ? J.py : J.pz;
@@ -1233,6 +1235,7 @@ int32_t hp_job_create(hp_ctx* ctx, const hp_job_desc* d, hp_job** out) {
   ok &= cudaMemsetAsync(J.apart, 0, 8 * (size_t)A * qa * ntile, st) == cudaSuccess;
   ok &= cudaMemsetAsync(J.atom_out, 0, 8 * (size_t)A * AO_COUNT, st) == cudaSuccess;
   ok &= cudaMemsetAsync(J.charges, 0, 8 * (size_t)A, st) == cudaSuccess;
+
   ok &= cudaMemsetAsync(ctx->mail_dev + slot, 0, sizeof(Mailbox), st) == cudaSuccess;
   ok &= cudaStreamSynchronize(st) == cudaSuccess;
   if (!ok) {

@@ -400,6 +400,7 @@ __host__ __device__ constexpr size_t fuse_fixed_bytes(int S, int mode) {
   return mode ? fuse_fixed_bytes(S) + 128 * (size_t)fuse_x_rows(S) + 1024 + 64 : fuse_fixed_bytes(S);
 }
 constexpr int kFuseTmemCols = 256;
+constexpr int kMmaThread = kFuseThreads - 32;  // lane 0 of the last warp issues the MMAs
 
 // The staging ring of a fused pass over jobs of at most S shells (floats):
 // the rest of kFuseSmemMax (at least kFuseSmemFloor in all), in 128-byte
@@ -512,18 +513,21 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_fused_ff(Batch bt, in
   }
   // The MMAs of the X tile as it stands (thread 0; after a block barrier
   // that follows the writers' proxy fences).
+  // descriptors of the X tile's operands at K offset 0; K step kk adds 32
+  // bytes to the start address (2 in the descriptor's 16-byte units)
+  const uint32_t xs = umma::smem_u32(xt);
+  const uint64_t da1 = umma::umma_desc(xs);
+  const uint64_t da2 = umma::umma_desc(xs + (n1 - umma::kTcM) * 128);
+  const uint64_t db2 = umma::umma_desc(xs + umma::kTcM * 128);
+  const uint32_t id1 = umma::idesc_tf32(n1);
+  const uint32_t id2 = umma::idesc_tf32(has_d2 ? n1 - umma::kTcM : 16);
   auto issue_mma = [&]() {
     asm volatile("tcgen05.fence::after_thread_sync;");
-    const uint32_t xs = umma::smem_u32(xt);
-    const uint32_t id1 = umma::idesc_tf32(n1);
-    const uint32_t id2 = umma::idesc_tf32(has_d2 ? n1 - umma::kTcM : 16);
 #pragma unroll
     for (int kk = 0; kk < kFuseSP / 8; ++kk) {
       const uint32_t acc = (nmma > 0 || kk > 0) ? 1u : 0u;
-      umma::umma_tf32(tmem, umma::umma_desc(xs + 32 * kk), umma::umma_desc(xs + 32 * kk), id1, acc);
-      if (has_d2)
-        umma::umma_tf32(tmem + (uint32_t)c2, umma::umma_desc(xs + (n1 - umma::kTcM) * 128 + 32 * kk),
-                        umma::umma_desc(xs + umma::kTcM * 128 + 32 * kk), id2, acc);
+      umma::umma_tf32(tmem, da1 + 2 * kk, da1 + 2 * kk, id1, acc);
+      if (has_d2) umma::umma_tf32(tmem + (uint32_t)c2, da2 + 2 * kk, db2 + 2 * kk, id2, acc);
     }
     umma::umma_commit(bar);
   };
@@ -593,10 +597,10 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_fused_ff(Batch bt, in
       const float* gl = gh + nact * kFuseSP;
       const int q0 = p0 + sub * kFuseSP;
       __syncthreads();  // every thread is done with sub - 1 (its slot is free)
-      if (threadIdx.x == 0) {
-        if (sub + nslot - 1 < nsub) issue(sub + nslot - 1);
-        if (hess && sub > 0 && !timed_out) issue_mma();  // X of sub - 1 is complete: its MMAs
-      }
+      if (threadIdx.x == 0 && sub + nslot - 1 < nsub) issue(sub + nslot - 1);
+      // X of sub - 1 is complete: its MMAs (issued by the last warp; warp 0
+      // has the per-point step of this sub-tile ahead)
+      if (hess && sub > 0 && threadIdx.x == kMmaThread && !timed_out) issue_mma();
       if (hess && sub > 0) ++nmma;
       if (!timed_out && !umma::mbar_wait_sleep(rbar0 + 8 * slot, (ring_phase >> slot) & 1u))
         timed_out = 1;
@@ -704,7 +708,7 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_fused_ff(Batch bt, in
     }
     if (hess) {  // the tile's last sub-tile
       __syncthreads();
-      if (threadIdx.x == 0 && !timed_out) issue_mma();
+      if (threadIdx.x == kMmaThread && !timed_out) issue_mma();
       ++nmma;
     }
 #pragma unroll
@@ -1127,12 +1131,15 @@ __global__ void __launch_bounds__(kThreads) k_glisa_active(Batch bt) {
 // G[act[i]][p0 + 32 s + l] (0 past the job's last point), the low plane
 // gpack_plane floats after the high one. One block per tile.
 __global__ void __launch_bounds__(kThreads) k_glisa_pack(Batch bt) {
+  __shared__ int act[kFuseMaxShells];
   int tile;
   const JobDev& J = decode_local_gf(bt, tile);
   if (!J.fuse || !J.gpack) return;
   const int S = J.nshell;
-  const int* act = J.gact + (size_t)tile * (S + 1);
-  const int nact = act[S];
+  const int* g = J.gact + (size_t)tile * (S + 1);
+  const int nact = g[S];
+  for (int i = threadIdx.x; i < nact; i += kThreads) act[i] = g[i];
+  __syncthreads();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int p0 = tile * J.tile_points;
   const int p1 = min(p0 + J.tile_points, J.npoint);
@@ -1140,13 +1147,28 @@ __global__ void __launch_bounds__(kThreads) k_glisa_pack(Batch bt) {
   const size_t N = J.npoint;
   float* hi = J.gpack + J.gtile_off[tile];
   float* lo = hi + J.gpack_plane;
-  for (int e = warp; e < nsub * nact; e += kWarps) {
-    const int sub = e / nact, i = e - sub * nact;
-    const int p = p0 + 32 * sub + lane;
-    const size_t src = (size_t)act[i] * N + p;
-    const size_t dst = ((size_t)sub * nact + i) * 32 + lane;
-    hi[dst] = p < p1 ? J.gmat32[src] : 0.0f;
-    lo[dst] = p < p1 ? J.gmat_lo[src] : 0.0f;
+  // warp per active row, streaming along the row's points (coalesced
+  // reads); sub-tile s of row i goes to ((s nact + i) 32 + lane)
+  for (int i = warp; i < nact; i += kWarps) {
+    const float* rh = J.gmat32 + (size_t)act[i] * N;
+    const float* rl = J.gmat_lo + (size_t)act[i] * N;
+    for (int sb = 0; sb < nsub; sb += 4) {
+      float vh[4], vl[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int p = p0 + 32 * (sb + u) + lane;
+        const bool in = sb + u < nsub && p < p1;
+        vh[u] = in ? rh[p] : 0.0f;
+        vl[u] = in ? rl[p] : 0.0f;
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+        if (sb + u < nsub) {
+          const size_t dst = ((size_t)(sb + u) * nact + i) * 32 + lane;
+          hi[dst] = vh[u];
+          lo[dst] = vl[u];
+        }
+    }
   }
 }
 

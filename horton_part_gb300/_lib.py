@@ -23,7 +23,7 @@ HP_ERR_NUMERIC, HP_ERR_TIMEOUT, HP_ERR_CUDA, HP_ERR_UNSUPPORTED, HP_ERR_STATE = 
 
 SCHEMES = {"mbis": 0, "gisa": 1, "lisa": 2, "glisa": 3, "nlis": 4}
 SOLVERS = {"default": 0, "sc": 1, "newton": 2, "m-newton": 3, "quadprog": 4, "qp": 4,
-           "pnewton": 5}
+           "pnewton": 5, "quasi-newton": 6}
 PRECISIONS = {"fp64": 0, "mixed": 1, "ff": 2}
 
 WARN_INNER_NOT_CONVERGED = 1

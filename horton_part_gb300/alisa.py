@@ -11,13 +11,14 @@ all atoms at once on the device:
               convergence test (so no warning)
 ``newton``    exact Newton on the KL objective (``alisa.py:543-602``)
 ``m-newton``  Newton with the positivity line search (``alisa.py:605-664``)
+``quasi-newton`` BFGS on the inverse Hessian with the same line search
+              (``alisa.py:683-750``, ``_solver_general_newton`` mode "bfgs")
 
 ``cvxopt`` (the reference's class default) needs the cvxopt package; its
 optimum is the non-negative KL minimiser, which the multiplicative ``sc``
 update also reaches, so ``cvxopt`` is served by ``sc``. Other reference
-solvers (``diis``, ``cdiis``, ``trust-region``, ``quasi-newton``,
-``sc-plus-convex``) are not on the GPU path and raise
-``NotImplementedError``.
+solvers (``diis``, ``cdiis``, ``trust-region``, ``sc-plus-convex``) are not
+on the GPU path and raise ``NotImplementedError``.
 """
 
 from __future__ import annotations
@@ -30,7 +31,7 @@ from .gisa import GaussianISAWPart, shell_tables_from_helper
 __all__ = ["LinearISAWPart", "setup_bs_helper"]
 
 _SOLVERS = {"sc": "sc", "sc-1-iter": "sc", "cvxopt": "sc", "newton": "newton",
-            "m-newton": "m-newton"}
+            "m-newton": "m-newton", "quasi-newton": "quasi-newton"}
 
 
 def setup_bs_helper(part):
@@ -98,7 +99,7 @@ class LinearISAWPart(GaussianISAWPart):
         if _SOLVERS[self._solver] == "sc":
             return {"inner_maxiter": int(float(opts.get("max_niter_inner", 100000)))}
         extra = {"inner_maxiter": int(opts.get("niter", 10000))}
-        if _SOLVERS[self._solver] == "m-newton":
+        if _SOLVERS[self._solver] in ("m-newton", "quasi-newton"):
             extra["linspace_size"] = int(opts.get("linspace_size", 20))
             extra["tau"] = float(opts.get("tau", 1.0))
         return extra

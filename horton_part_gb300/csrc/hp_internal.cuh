@@ -90,7 +90,7 @@ enum WarnFlag { W_INNER = 1, W_POPULATION = 2, W_NEG_PARS = 4 };
 
 enum Scheme { SCHEME_MBIS = 0, SCHEME_GISA = 1, SCHEME_LISA = 2, SCHEME_GLISA = 3, SCHEME_NLIS = 4 };
 enum Solver { SOLVER_DEFAULT = 0, SOLVER_SC = 1, SOLVER_NEWTON = 2, SOLVER_M_NEWTON = 3,
-              SOLVER_QP = 4, SOLVER_PNEWTON = 5 };
+              SOLVER_QP = 4, SOLVER_PNEWTON = 5, SOLVER_BFGS = 6 };
 constexpr int kTrials = 8;  // projected-Newton step lengths 2^-t evaluated per pass
 enum Model { MODEL_MBIS = 0, MODEL_BASIS = 1, MODEL_NLIS = 2 };
 // Evaluation phase of a job (JobDev::mixed): FP64, FP32 with compensated sums,
@@ -139,6 +139,9 @@ struct JobDev {
   double* cur;
   double* prev;
   double* delta;          // Newton steps (nparam)
+  double* hinv;           // aLISA quasi-Newton: inverse-Hessian estimate per atom [natom][kMaxShells^2]
+  double* olddf;          // aLISA quasi-Newton: gradient of the previous inner iteration (nparam)
+  double* step;           // aLISA quasi-Newton: step taken by the previous inner iteration (nparam)
   double* keep;           // gLISA line-search mask (nparam)
   // buffers
   double* promol;

@@ -1083,6 +1083,50 @@ __global__ void k_lisa_newton_update(Batch bt) {
   }
   double H[kMaxShells * kMaxShells], b[kMaxShells];
   for (int k = 0; k < nsh; ++k) b[k] = -1.0 + v[k];  // -1 - df, df = -sum w g ratio
+  if (J.solver == SOLVER_BFGS) {
+    // quasi-Newton (alisa.py:896-905, algo/quasi_newton.py:24-49): the
+    // inverse-Hessian estimate starts at the identity at the first inner
+    // iteration and takes the BFGS update
+    //   H += (s.y + y H y) s s^T / (s.y)^2 - (H y s^T + s y^T H) / s.y,
+    //   y = df - df_old, s the step of the previous line search;
+    // the step is H (-1 - df), applied by the positivity line search
+    double* hv = J.hinv + (size_t)a * kMaxShells * kMaxShells;
+    double* od = J.olddf + J.par_off[a];
+    const double* sp = J.step + J.par_off[a];
+    if (it == 0) {
+      for (int k = 0; k < nsh; ++k)
+        for (int l = 0; l < nsh; ++l) hv[k * nsh + l] = k == l ? 1.0 : 0.0;
+    } else {
+      double y[kMaxShells], hy[kMaxShells], yh[kMaxShells];
+      double sy = 0.0;
+      for (int k = 0; k < nsh; ++k) {
+        y[k] = -v[k] - od[k];
+        sy += sp[k] * y[k];
+      }
+      double yhy = 0.0;
+      for (int k = 0; k < nsh; ++k) {
+        double a1 = 0.0, a2 = 0.0;
+        for (int l = 0; l < nsh; ++l) {
+          a1 += hv[k * nsh + l] * y[l];  // (H y)_k
+          a2 += y[l] * hv[l * nsh + k];  // (y^T H)_k
+        }
+        hy[k] = a1;
+        yh[k] = a2;
+      }
+      for (int k = 0; k < nsh; ++k) yhy += y[k] * hy[k];
+      const double c1 = (sy + yhy) / (sy * sy);
+      for (int k = 0; k < nsh; ++k)
+        for (int l = 0; l < nsh; ++l)
+          hv[k * nsh + l] += c1 * sp[k] * sp[l] - (hy[k] * sp[l] + sp[k] * yh[l]) / sy;
+    }
+    for (int k = 0; k < nsh; ++k) {
+      double d = 0.0;
+      for (int l = 0; l < nsh; ++l) d += hv[k * nsh + l] * b[l];
+      dl[k] = d;
+      od[k] = -v[k];
+    }
+    return;
+  }
   int e = nsh;
   for (int k = 0; k < nsh; ++k)
     for (int l = 0; l <= k; ++l) {
@@ -1179,9 +1223,12 @@ __global__ void k_lisa_ls_pick(Batch bt) {
     return;
   }
   const double x = linspace_at(J.tau, 0.0, L, true, pick);
+  double* st = J.step ? J.step + J.par_off[a] : nullptr;  // quasi-Newton: the step taken
   for (int k = 0; k < nsh; ++k) {
     pp[k] = pc[k];
-    pc[k] = pc[k] + x * dl[k];
+    const double sk = x * dl[k];
+    pc[k] = pc[k] + sk;
+    if (st) st[k] = sk;
   }
   J.inner_it[a] += 1;
 }

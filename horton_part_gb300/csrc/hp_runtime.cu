@@ -416,7 +416,8 @@ int step_iterstock(hp_ctx* ctx, const std::vector<hp_job*>& jobs, const HostBatc
       else
         rc = run_inner(ctx, jobs, hb, [&] {
           ProfScope ps(ctx, HP_KERNEL_INNER);
-          launch_lisa_newton_inner(hb, st, mixed, j0->dev.solver == SOLVER_M_NEWTON);
+          launch_lisa_newton_inner(hb, st, mixed,
+                                   j0->dev.solver == SOLVER_M_NEWTON || j0->dev.solver == SOLVER_BFGS);
         }, j0->dev.inner_maxiter + 1);
       break;
   }
@@ -734,8 +735,10 @@ int validate(const hp_job_desc* d) {
   if (d->maxiter <= 0) return fail(HP_ERR_INVALID, "maxiter must be positive");
   if (d->scheme == HP_SCHEME_LISA &&
       (d->solver != HP_SOLVER_SC && d->solver != HP_SOLVER_NEWTON && d->solver != HP_SOLVER_M_NEWTON &&
-       d->solver != HP_SOLVER_DEFAULT))
-    return fail(HP_ERR_UNSUPPORTED, "aLISA solvers on this path: sc, newton, m-newton");
+       d->solver != HP_SOLVER_QUASI_NEWTON && d->solver != HP_SOLVER_DEFAULT))
+    return fail(HP_ERR_UNSUPPORTED, "aLISA solvers on this path: sc, newton, m-newton, quasi-newton");
+  if (d->scheme != HP_SCHEME_LISA && d->solver == HP_SOLVER_QUASI_NEWTON)
+    return fail(HP_ERR_UNSUPPORTED, "the device quasi-Newton solver is for aLISA");
   if (d->scheme == HP_SCHEME_GLISA &&
       (d->solver != HP_SOLVER_SC && d->solver != HP_SOLVER_NEWTON && d->solver != HP_SOLVER_M_NEWTON &&
        d->solver != HP_SOLVER_PNEWTON && d->solver != HP_SOLVER_DEFAULT))
@@ -963,6 +966,11 @@ int32_t hp_job_create(hp_ctx* ctx, const hp_job_desc* d, hp_job** out) {
   add(&J.propars, 8 * (size_t)P); add(&J.propars_init, 8 * (size_t)P);
   add(&J.propars_old, 8 * (size_t)P); add(&J.cur, 8 * (size_t)P);
   add(&J.prev, 8 * (size_t)P); add(&J.delta, 8 * (size_t)P); add(&J.keep, 8 * (size_t)P);
+  if (d->solver == HP_SOLVER_QUASI_NEWTON) {
+    add(&J.hinv, 8 * (size_t)A * kMaxShells * kMaxShells);
+    add(&J.olddf, 8 * (size_t)P);
+    add(&J.step, 8 * (size_t)P);
+  }
   add(&J.promol, 8 * (size_t)N);
   add(&J.invpro, 8 * (size_t)N);
   add(&J.rhoa, 8 * (size_t)A * N);

@@ -76,10 +76,13 @@ typedef enum {
   HP_SOLVER_NEWTON = 2,  /* alisa.py:543-602, glisa.py:573-575 (exact Newton) */
   HP_SOLVER_M_NEWTON = 3,/* alisa.py:605-664, glisa.py:577-591 (line search) */
   HP_SOLVER_QP = 4,      /* gisa.py:348-421 (quadratic program) */
-  HP_SOLVER_PNEWTON = 5  /* gLISA with non-negative populations: projected Newton on
+  HP_SOLVER_PNEWTON = 5, /* gLISA with non-negative populations: projected Newton on
                             the extended KL objective; reaches the optimum of the
                             reference's cvxopt solver (glisa.py:488-571), whose
                             package is not available */
+  HP_SOLVER_QUASI_NEWTON = 6 /* aLISA: BFGS on the inverse Hessian with the
+                            positivity line search (alisa.py:683-750 through
+                            _solver_general_newton, mode "bfgs", :753-938) */
 } hp_solver;
 
 typedef enum {

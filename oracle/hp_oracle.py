@@ -533,12 +533,14 @@ def lisa_solver_sc(bs_funcs, rho, propars, weights, threshold, density_cutoff=DE
 def lisa_solver_newton(bs_funcs, rho, propars, weights, threshold, mode="exact",
                        density_cutoff=DENSITY_CUTOFF, negative_cutoff=NEGATIVE_CUTOFF,
                        tau=1.0, linspace_size=20, niter=10000):
-    """Newton / modified Newton on one atom (``alisa.py:753-938``)."""
+    """Newton / modified Newton / BFGS quasi-Newton (``mode="bfgs"``) on one
+    atom (``alisa.py:753-938``, BFGS update of ``algo/quasi_newton.py:24-49``)."""
     from scipy.linalg import solve
 
     oldpro = None
     change = 1e100
     pop = np.einsum("i,i", weights, rho)
+    H = olddf = step = None
     for irep in range(niter):
         _, pro, sick, ratio, _ = compute_quantities(rho, propars, bs_funcs, density_cutoff)
         if oldpro is not None:
@@ -553,8 +555,18 @@ def lisa_solver_newton(bs_funcs, rho, propars, weights, threshold, mode="exact",
             grad_integrand = integrand / pro
         grad_integrand[:, sick] = 0.0
         df = -np.einsum("kp,p->k", integrand, weights)
-        hess = np.einsum("kp,jp,p->kj", grad_integrand, bs_funcs, weights)
-        delta = solve(hess, -1 - df, assume_a="sym")
+        if mode == "bfgs":
+            if irep == 0:
+                H = np.identity(len(propars))
+            else:
+                y = df - olddf
+                sy = step @ y
+                H = (H + (sy + y @ H @ y) * np.outer(step, step) / sy ** 2
+                     - (H @ np.outer(y, step) + np.outer(step, y) @ H) / sy)
+            delta = H @ (-1 - df)
+        else:
+            hess = np.einsum("kp,jp,p->kj", grad_integrand, bs_funcs, weights)
+            delta = solve(hess, -1 - df, assume_a="sym")
         if mode == "exact":
             propars[:] = propars + delta
         else:
@@ -562,11 +574,13 @@ def lisa_solver_newton(bs_funcs, rho, propars, weights, threshold, mode="exact",
                 new = propars + x * delta
                 new_pro = np.einsum("ij->j", bs_funcs * new[:, None])
                 if (new_pro > negative_cutoff).all():
+                    step = x * delta
                     propars[:] = new
                     break
             else:
                 raise OracleError("Line search failed!")
         oldpro = pro
+        olddf = df
     raise OracleError("Inner loop: Newton does not converge!")
 
 
@@ -644,10 +658,10 @@ def basis_scheme(scheme, coordinates, numbers, pseudo_numbers, points, weights, 
                                                                 density_cutoff)
                 propars[sl] = np.einsum("p,ip->i", wa, pro_shells * ratio)
                 its.append(1)
-            elif solver in ("newton", "m-newton"):
+            elif solver in ("newton", "m-newton", "quasi-newton"):
                 new, nit = lisa_solver_newton(
                     ga, rhoa, propars[sl].copy(), wa, inner,
-                    mode="exact" if solver == "newton" else "modified",
+                    mode={"newton": "exact", "m-newton": "modified"}.get(solver, "bfgs"),
                     density_cutoff=density_cutoff, negative_cutoff=negative_cutoff)
                 propars[sl] = new
                 its.append(nit)

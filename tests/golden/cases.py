@@ -24,6 +24,10 @@ CASES = {
     "lisa_sc1iter_h2o_50x110": dict(scheme="lisa", mol=("water", 50, 110),
                                     kwargs=dict(threshold=1e-8, inner_threshold=1e-8,
                                                 solver="sc-1-iter")),
+    # BFGS quasi-Newton with the positivity line search (alisa.py:683-750)
+    "lisa_qnewton_h2o_50x110": dict(scheme="lisa", mol=("water", 50, 110),
+                                    kwargs=dict(threshold=1e-8, inner_threshold=1e-8,
+                                                solver="quasi-newton")),
     "lisa_mnewton_h2o_50x110": dict(scheme="lisa", mol=("water", 50, 110),
                                     kwargs=dict(threshold=1e-8, inner_threshold=1e-8,
                                                 solver="m-newton")),

@@ -53,11 +53,21 @@ __device__ __forceinline__ int point_of(const JobDev& J, int tile, int i) {
   return tile * J.tile_points + i * kThreads + threadIdx.x;
 }
 
-// Warp sum over tiles with a fixed lane order (deterministic).
+// Warp sum over tiles with a fixed lane order (deterministic): four
+// independent chains per lane (tiles t, t + 32, t + 64, t + 96 of every 128)
+// so that their loads are in flight together, added in a fixed order.
 __device__ __forceinline__ double warp_tile_sum(const JobDev& J, const double* p, int ntile) {
   const int lane = threadIdx.x & 31;
-  double s = 0.0;
-  for (int t = lane; t < ntile; t += 32) s += partial_value(J, p + t);
+  double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+  int t = lane;
+  for (; t + 96 < ntile; t += 128) {
+    s0 += partial_value(J, p + t);
+    s1 += partial_value(J, p + t + 32);
+    s2 += partial_value(J, p + t + 64);
+    s3 += partial_value(J, p + t + 96);
+  }
+  for (; t < ntile; t += 32) s0 += partial_value(J, p + t);
+  double s = (s0 + s1) + (s2 + s3);
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
   return s;

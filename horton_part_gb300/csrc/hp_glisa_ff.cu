@@ -223,14 +223,14 @@ __global__ void __launch_bounds__(kThreads) k_glisa_u_ff(Batch bt) {
 // cutoff's float pair. The relative change (rho0_t - rho0) / rho0 goes to
 // log1pf as before; only the points whose sick status differs take FP64 logs.
 __global__ void __launch_bounds__(kThreads) k_glisa_trials_ff(Batch bt) {
-  __shared__ double red[kWarps * kTrials];
-  __shared__ double out[kTrials];
+  __shared__ double red[kWarps * 2 * kTrials];
+  __shared__ double out[2 * kTrials];
   int tile;
   const JobDev& J = decode_local_gf(bt, tile);
   if (glisa_idle(J)) return;
-  float ah[kTrials], al[kTrials];
+  float ah[kTrials], al[kTrials], an[kTrials];
 #pragma unroll
-  for (int t = 0; t < kTrials; ++t) ah[t] = al[t] = 0.0f;
+  for (int t = 0; t < kTrials; ++t) ah[t] = al[t] = an[t] = 0.0f;
   const int nclip = J.clip[J.nshell];
   const int* tm = J.clip + J.nshell + 1;
   const float4* cd = reinterpret_cast<const float4*>(J.clipf);
@@ -277,8 +277,10 @@ __global__ void __launch_bounds__(kThreads) k_glisa_trials_ff(Batch bt) {
       const bool ht = !(rs || below);
       double big = 0.0;
       float term = 0.0f;
-      if (h0 && ht) term = -wr * log1pf(dr.hi * inv);
-      else if (ht) big = w * rho * log(rho / ffa::to_double(rt));
+      if (h0 && ht) {
+        term = -wr * log1pf(dr.hi * inv);
+        an[t] += fabsf(term);
+      } else if (ht) big = w * rho * log(rho / ffa::to_double(rt));
       else if (h0) big = -(w * rho * log(rho / r0));
       if (big != 0.0) {
         const float bh = (float)big;
@@ -291,20 +293,23 @@ __global__ void __launch_bounds__(kThreads) k_glisa_trials_ff(Batch bt) {
       ah[t] = s;
     }
   }
-  double acc[kTrials];
+  double acc[2 * kTrials];
 #pragma unroll
-  for (int t = 0; t < kTrials; ++t) acc[t] = (double)ah[t] + (double)al[t];
-  block_sum<kTrials>(acc, red, out);
-  if (threadIdx.x < kTrials) J.tpart[(size_t)threadIdx.x * J.ntile + tile] = out[threadIdx.x];
+  for (int t = 0; t < kTrials; ++t) {
+    acc[t] = (double)ah[t] + (double)al[t];
+    acc[kTrials + t] = (double)an[t];
+  }
+  block_sum<2 * kTrials>(acc, red, out);
+  if (threadIdx.x < 2 * kTrials) J.tpart[(size_t)threadIdx.x * J.ntile + tile] = out[threadIdx.x];
 }
 
 // ---------------------------------------------------------------------------
 // Fused passes: one read of G for a product G^T x and the row sums G v that
-// depend on it. A block (256 threads, two per SM) streams its point tile
+// depend on it. A block (256 threads, two per SM) streams its point tiles
 // through shared memory in sub-tiles of kFuseSP = 32 points (both planes of
-// the tile's active rows, cp.async into one of nbuf staging buffers: two when
-// they fit beside the rest of the block's shared memory, so that the next
-// sub-tile loads while this one is processed). Warp w owns the active rows
+// the tile's active rows from the packed layout, TMA bulk copies into a ring
+// of staging slots, so that the next sub-tiles load while one is
+// processed). Warp w owns the active rows
 // i = w, w + 8, ... of the tile (lane = point); per sub-tile
 //   A  the warp sums G[m][p] x[m] over its rows in two compensated chains,
 //      merged into the warp's partial sum of u(p);
@@ -414,8 +419,10 @@ static_assert(fuse_fixed_bytes(kFuseMaxShells, 1) + 4 * (size_t)fuse_ring_floats
                   kFuseSmemFloor, "at most two blocks per SM");
 
 // Persistent blocks (launch kind K_FUSE): block b of a job takes the point
-// tiles b, b + nb, ... (nb = min(ntile, kFuseCtas)). The per-tile outputs
-// (gradient rows, change) stay per tile.
+// tiles the job's schedule gives it (fsched: longest processing time first
+// over the tiles' active-row work, ascending within a block; nb =
+// min(ntile, kFuseCtas)). The per-tile outputs (gradient rows, change) stay
+// per tile.
 //
 // MODE 1 also accumulates the Hessian H = X X^T of its tiles on the tensor
 // cores (glisa.py:457-470): in B every warp writes its rows of X (X[m][p] =
@@ -537,8 +544,26 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_fused_ff(Batch bt, in
   };
   const double* x = MODE ? J.propars : J.delta;
   const bool chg = MODE == 1 && with_change;
+  float ch = 0.0f, cl = 0.0f;  // change terms of this thread (float pair)
+  // C: the change terms of atoms a0, a0 + astep, ... for this lane's point
+  // (atoms with no active row add exact zeros: skipped)
+  auto change_terms = [&](const float* ghl, float wf, int a0, int astep) {
+    for (int a = a0; a < natom; a += astep) {
+      const int i0 = aoff[a], i1 = aoff[a + 1];
+      if (i0 == i1) continue;
+      float dv = 0.0f;
+      for (int i = i0; i < i1; ++i) dv = fmaf(ghl[i * kFuseSP], dca[i], dv);
+      const float term = wf * dv * dv;
+      const float t = ch + term;
+      const float bb = t - ch;
+      cl += (ch - (t - bb)) + (term - bb);
+      ch = t;
+    }
+  };
 
-  for (int tile = local; tile < J.ntile; tile += nblk_job) {
+  const int* __restrict__ tiles = J.fsched + nblk_job + 1;
+  for (int k = J.fsched[local]; k < J.fsched[local + 1]; ++k) {
+    const int tile = tiles[k];
     const int p0 = tile * J.tile_points;
     const int p1 = min(p0 + J.tile_points, J.npoint);
     const int nsub = (p1 - p0 + kFuseSP - 1) / kFuseSP;
@@ -587,7 +612,8 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_fused_ff(Batch bt, in
       }
     // this warp's rows i = warp + 8 r, r < nr
     const int nr = nact > warp ? (nact - warp + kFuseWarps - 1) / kFuseWarps : 0;
-    float ch = 0.0f, cl = 0.0f;  // change terms of this thread (float pair)
+    ch = 0.0f;
+    cl = 0.0f;
     Dot2 acc[kFuseRows];
 #pragma unroll
     for (int r = 0; r < kFuseRows; ++r) acc[r] = Dot2{0.f, 0.f};
@@ -602,85 +628,76 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_fused_ff(Batch bt, in
       // has the per-point step of this sub-tile ahead)
       if (hess && sub > 0 && threadIdx.x == kMmaThread && !timed_out) issue_mma();
       if (hess && sub > 0) ++nmma;
-      if (!timed_out && !umma::mbar_wait_sleep(rbar0 + 8 * slot, (ring_phase >> slot) & 1u))
-        timed_out = 1;
-      ring_phase ^= 1u << slot;  // sub-tile sub is in the slot
-      // per-point inputs, loaded before phase A so that their latency
-      // overlaps it: (w rho, rho) pairs (MODE 1) or the d2 pair (MODE 0) for
-      // warp 0, w for the change warps
       const int pq = q0 + lane;
-      float wf = 0.0f;
-      float4 qpre = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (pq < p1) {
-        if (warp == 0) {
-          if (MODE == 1) qpre = wrfp[pq];
-          else {
-            const float2 d2 = d2in[pq];
-            qpre = make_float4(d2.x, d2.y, 0.f, 0.f);
-          }
-        }
-        if (chg && warp > 0) wf = (float)wp[pq];
-      }
-      // A: rows r even in chain d, odd in chain e
       const float* ghw = gh + warp * kFuseSP + lane;
       const float* glw = gl + warp * kFuseSP + lane;
+      f2 v{0.f, 0.f};
+      float sx = 0.0f;
       {
-        Dot2 d{0.f, 0.f}, e{0.f, 0.f};
-        int r = 0;
-        for (; r + 1 < nr; r += 2) {
-          const float2 x1 = xa[warp + kFuseWarps * r], x2 = xa[warp + kFuseWarps * (r + 1)];
-          dot2_add(d, ghw[r * kFuseWarps * kFuseSP], glw[r * kFuseWarps * kFuseSP], x1.x, x1.y);
-          dot2_add(e, ghw[(r + 1) * kFuseWarps * kFuseSP], glw[(r + 1) * kFuseWarps * kFuseSP], x2.x,
-                   x2.y);
-        }
-        if (r < nr) {
-          const float2 x1 = xa[warp + kFuseWarps * r];
-          dot2_add(d, ghw[r * kFuseWarps * kFuseSP], glw[r * kFuseWarps * kFuseSP], x1.x, x1.y);
-        }
-        dot2_merge(d, e);
-        part[warp * kFuseSP + lane] = d;
-      }
-      __syncthreads();  // partial sums visible
-      if (warp == 0) {
-        // A': the eight partial sums merged in warp order; v (and s, rho0)
-        Dot2 du = part[lane];
-#pragma unroll
-        for (int q = 1; q < kFuseWarps; ++q) dot2_merge(du, part[q * kFuseSP + lane]);
-        f2 v{0.f, 0.f};
-        float sx = 0.0f;
+        // per-point inputs, loaded before phase A so that their latency
+        // overlaps it: (w rho, rho) pairs (MODE 1) or the d2 pair (MODE 0) for
+        // warp 0, w for the change warps
+        float wf = 0.0f;
+        float4 qpre = make_float4(0.f, 0.f, 0.f, 0.f);
         if (pq < p1) {
-          if (MODE == 0) {
-            v = ffa::mul(dot2_ff(du), f2{qpre.x, qpre.y});
-          } else {
-            const f2 r0 = dot2_ff(du);
-            r0fo[pq] = make_float2(r0.hi, r0.lo);
-            const bool sick = below(f2{qpre.z, qpre.w}, cutp) || below(r0, cutp);
-            if (!sick) {
-              v = ffa::div(f2{qpre.x, qpre.y}, r0);
-              sx = sqrtf(qpre.x) / r0.hi;
+          if (warp == 0) {
+            if (MODE == 1) qpre = wrfp[pq];
+            else {
+              const float2 d2 = d2in[pq];
+              qpre = make_float4(d2.x, d2.y, 0.f, 0.f);
             }
           }
+          if (chg && warp > 0) wf = (float)wp[pq];
         }
-        pvs[lane] = make_float4(v.hi, v.lo, sx, 0.f);
-      } else if (chg) {
-        // C (atoms with no active row add exact zeros: skipped)
-        const float* ghl = gh + lane;
-        for (int a = warp - 1; a < natom; a += kFuseWarps - 1) {
-          const int i0 = aoff[a], i1 = aoff[a + 1];
-          if (i0 == i1) continue;
-          float dv = 0.0f;
-          for (int i = i0; i < i1; ++i) dv = fmaf(ghl[i * kFuseSP], dca[i], dv);
-          const float term = wf * dv * dv;
-          const float t = ch + term;
-          const float bb = t - ch;
-          cl += (ch - (t - bb)) + (term - bb);
-          ch = t;
+        if (!timed_out && !umma::mbar_wait_sleep(rbar0 + 8 * slot, (ring_phase >> slot) & 1u))
+          timed_out = 1;
+        ring_phase ^= 1u << slot;  // sub-tile sub is in the slot
+        {  // A: rows r even in chain d, odd in chain e
+          Dot2 d{0.f, 0.f}, e{0.f, 0.f};
+          int r = 0;
+          for (; r + 1 < nr; r += 2) {
+            const float2 x1 = xa[warp + kFuseWarps * r], x2 = xa[warp + kFuseWarps * (r + 1)];
+            dot2_add(d, ghw[r * kFuseWarps * kFuseSP], glw[r * kFuseWarps * kFuseSP], x1.x, x1.y);
+            dot2_add(e, ghw[(r + 1) * kFuseWarps * kFuseSP], glw[(r + 1) * kFuseWarps * kFuseSP], x2.x,
+                     x2.y);
+          }
+          if (r < nr) {
+            const float2 x1 = xa[warp + kFuseWarps * r];
+            dot2_add(d, ghw[r * kFuseWarps * kFuseSP], glw[r * kFuseWarps * kFuseSP], x1.x, x1.y);
+          }
+          dot2_merge(d, e);
+          part[warp * kFuseSP + lane] = d;
         }
+        __syncthreads();  // partial sums visible
+        if (warp == 0) {
+          // A': the eight partial sums merged in warp order; v (and s, rho0)
+          Dot2 du = part[lane];
+#pragma unroll
+          for (int q = 1; q < kFuseWarps; ++q) dot2_merge(du, part[q * kFuseSP + lane]);
+          f2 vw{0.f, 0.f};
+          float sw = 0.0f;
+          if (pq < p1) {
+            if (MODE == 0) {
+              vw = ffa::mul(dot2_ff(du), f2{qpre.x, qpre.y});
+            } else {
+              const f2 r0 = dot2_ff(du);
+              r0fo[pq] = make_float2(r0.hi, r0.lo);
+              const bool sick = below(f2{qpre.z, qpre.w}, cutp) || below(r0, cutp);
+              if (!sick) {
+                vw = ffa::div(f2{qpre.x, qpre.y}, r0);
+                sw = sqrtf(qpre.x) / r0.hi;
+              }
+            }
+          }
+          pvs[lane] = make_float4(vw.hi, vw.lo, sw, 0.f);
+        } else if (chg) {
+          change_terms(gh + lane, wf, warp - 1, kFuseWarps - 1);  // C
+        }
+        __syncthreads();  // v and s of the sub-tile visible
+        const float4 pv = pvs[lane];
+        v = f2{pv.x, pv.y};
+        sx = pv.z;
       }
-      __syncthreads();  // v and s of the sub-tile visible
-      const float4 pv = pvs[lane];
-      const f2 v{pv.x, pv.y};
-      const float sx = pv.z;
       if (hess) wait_mma();  // the MMAs of sub - 1 have read the X tile
       // B (and the rows of X)
 #pragma unroll
@@ -883,10 +900,12 @@ static_assert(trials_ring_floats(kFuseMaxShells) >= 2 * kFuseMaxShells * kFuseSP
 
 __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_trials_fused(Batch bt, int ring_floats) {
   extern __shared__ float4 fsm[];
-  int tile;
-  const JobDev& J = decode_local_gf(bt, tile);
+  int local;
+  const JobDev& J = decode_local_gf(bt, local);
   if (glisa_idle(J)) return;
   if (!J.fuse) return;
+  // heaviest tiles first (the block scheduler starts the blocks in order)
+  const int tile = J.fsched[min(J.ntile, kFuseCtas) + 1 + J.ntile + local];
   const int S = J.nshell;
   float* ring = reinterpret_cast<float*>(fsm);
   float4* grp = reinterpret_cast<float4*>(ring + ring_floats);  // [kTrials][kFuseSP]
@@ -948,7 +967,7 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_trials_fused(Batch bt
   const float4* cd = reinterpret_cast<const float4*>(J.clipf);
   const float2 cutp = split2(J.density_cutoff);
   if (threadIdx.x < 64) tab[threadIdx.x] = c_exp2_gl[threadIdx.x];
-  float ah = 0.0f, al = 0.0f;
+  float ah = 0.0f, al = 0.0f, an = 0.0f;
   for (int sub = 0; sub < nsub; ++sub) {
     const int slot = sub % nslot;
     const float* gh = ring + (size_t)slot * slotf;
@@ -1032,6 +1051,7 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_trials_fused(Batch bt
       float term = 0.0f;
       if (h0 && ht) {
         term = -q.x * log1pf(dr.hi / r0p.x);
+        an += fabsf(term);
       } else if (ht || h0) {
         // the sick status changes: +-(w rho) ln(rho / rho0) in float-float
         // (logf, then one Newton step on the float-float exponential)
@@ -1049,10 +1069,16 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_trials_fused(Batch bt
       ah = s2;
     }
   }
-  double v = (double)ah + (double)al;
+  double v = (double)ah + (double)al, vn = (double)an;
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  if (lane == 0) J.tpart[(size_t)t * J.ntile + tile] = v;
+  for (int o = 16; o > 0; o >>= 1) {
+    v += __shfl_xor_sync(0xffffffffu, v, o);
+    vn += __shfl_xor_sync(0xffffffffu, vn, o);
+  }
+  if (lane == 0) {
+    J.tpart[(size_t)t * J.ntile + tile] = v;
+    J.tpart[(size_t)(kTrials + t) * J.ntile + tile] = vn;
+  }
   if (timed_out && lane == 0) atomicOr(&J.mail->i[MI_ERR], E_TIMEOUT);
 }
 

@@ -162,7 +162,8 @@ struct JobDev {
   double* dvec1;          // gLISA: w rho / rho0 (0 where sick), npoint
   double* dvec2;          // gLISA: w rho / rho0^2 (0 where sick), npoint
   double* ctrial;         // gLISA projected Newton: trial populations [kTrials][nshell]
-  double* tpart;          // gLISA projected Newton: trial objective partials [kTrials][ntile]
+  double* tpart;          // gLISA projected Newton: trial objective partials [kTrials][ntile], then
+                          // the magnitudes of their FP32 terms [kTrials][ntile]
   int* freeidx;           // gLISA Newton: free-variable list [nshell], count at [nshell]
   float* gmat32;          // gLISA tensor-core Hessian: FP32 copy of gmat [nshell][npoint]
                           // (with gff: the high part of G = gmat32 + gmat_lo)
@@ -179,6 +180,10 @@ struct JobDev {
   int64_t* gtile_off;     // fused gLISA: start of tile t's sub-tiles in a plane of gpack (floats)
   int64_t gpack_plane;    // fused gLISA: floats per plane of gpack
   int nact_max;           // fused gLISA: most active rows of a tile
+  int* fsched;            // fused gLISA: tile schedule. [0, nb]: block b's entries [fsched[b],
+                          // fsched[b + 1]) of the list at fsched + nb + 1 (ntile tiles, ascending
+                          // within a block); then the ntile tiles heaviest first (trial pass);
+                          // nb = min(ntile, kFuseCtas)
   float2* d1f;            // gLISA, gff: w rho / rho0 as float pairs, npoint
   float2* hvf;            // gLISA, gff: the refinement's hvec as float pairs, npoint
   float* hess_s;          // gLISA tensor-core Hessian: sqrt(w rho / rho0^2) as FP32, npoint

@@ -2021,15 +2021,14 @@ __global__ void __launch_bounds__(kThreads) k_glisa_refine(Batch bt) {
 
 // Projected-Newton trial points c_t = max(c + 2^-t delta, 0), t < kTrials,
 // and the list of shells the projection clips at the full step (the clipped
-// set of every shorter step is a subset of it).
+// set of every shorter step is a subset of it). A block of NT threads (tms:
+// kTrialSetSmem ints of shared memory, wcount: NT / 32).
 constexpr int kTrialSetSmem = 2048;  // shells whose clip steps are sorted in shared memory
 
-__global__ void __launch_bounds__(kThreads) k_glisa_trial_set(Batch bt) {
-  int local;
-  const JobDev& J = decode_local(bt, local);
-  if (glisa_idle(J)) return;
+template <int NT>
+__device__ void trial_set_body(const JobDev& J, int* tms, int* wcount) {
   const int M = J.nshell;
-  for (int e = threadIdx.x; e < kTrials * M; e += kThreads) {
+  for (int e = threadIdx.x; e < kTrials * M; e += NT) {
     const int t = e / M, m = e - t * M;
     const double a = ldexp(1.0, -t);
     J.ctrial[e] = fmax(J.propars[m] + a * J.delta[m], 0.0);
@@ -2039,10 +2038,8 @@ __global__ void __launch_bounds__(kThreads) k_glisa_trial_set(Batch bt) {
   // of equal t_m in index order
   int* tm = J.clip + M + 1;
   if (M <= kTrialSetSmem) {  // all threads: t_m per shell, then one ballot compaction per t
-    __shared__ int tms[kTrialSetSmem];
-    __shared__ int wcount[kWarps];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for (int m = threadIdx.x; m < M; m += kThreads) {
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int m = threadIdx.x; m < M; m += NT) {
       int t = 0;
       if (J.propars[m] + J.delta[m] < 0.0) {
         t = 1;
@@ -2053,14 +2050,14 @@ __global__ void __launch_bounds__(kThreads) k_glisa_trial_set(Batch bt) {
     __syncthreads();
     int n = 0;
     for (int t = kTrials; t >= 1; --t) {
-      for (int base = 0; base < M; base += kThreads) {
+      for (int base = 0; base < M; base += NT) {
         const int m = base + threadIdx.x;
         const bool f = m < M && tms[m] == t;
         const unsigned b = __ballot_sync(0xffffffffu, f);
         if (lane == 0) wcount[warp] = __popc(b);
         __syncthreads();
         int off = n, total = n;
-        for (int w = 0; w < kWarps; ++w) {
+        for (int w = 0; w < NT / 32; ++w) {
           if (w < warp) off += wcount[w];
           total += wcount[w];
         }
@@ -2094,7 +2091,7 @@ __global__ void __launch_bounds__(kThreads) k_glisa_trial_set(Batch bt) {
   if (J.clipf) {  // float pairs (c hi, c lo, delta hi, delta lo) of the clipped shells
     __syncthreads();
     const int n = J.clip[M];
-    for (int k = threadIdx.x; k < n; k += kThreads) {
+    for (int k = threadIdx.x; k < n; k += NT) {
       const int m = J.clip[k];
       const double c = J.propars[m], d = J.delta[m];
       const float ch = (float)c, dh = (float)d;
@@ -2104,6 +2101,15 @@ __global__ void __launch_bounds__(kThreads) k_glisa_trial_set(Batch bt) {
       J.clipf[4 * k + 3] = (float)(d - (double)dh);
     }
   }
+}
+
+__global__ void __launch_bounds__(kThreads) k_glisa_trial_set(Batch bt) {
+  __shared__ int tms[kTrialSetSmem];
+  __shared__ int wcount[kWarps];
+  int local;
+  const JobDev& J = decode_local(bt, local);
+  if (glisa_idle(J)) return;
+  trial_set_body<kThreads>(J, tms, wcount);
 }
 
 // Line-search mask (glisa.py:688-699 with utils.py:556-577): per atom, the
@@ -2331,14 +2337,14 @@ __global__ void k_glisa_eval_sum(Batch bt, int what) {
 // without an FP64 log per trial; the few points whose sick status differs
 // between rho0 and rho0_t take FP64 logs. Sums in float-float per thread.
 __global__ void __launch_bounds__(kThreads) k_glisa_trials(Batch bt) {
-  __shared__ double red[kWarps * kTrials];
-  __shared__ double out[kTrials];
+  __shared__ double red[kWarps * 2 * kTrials];
+  __shared__ double out[2 * kTrials];
   int tile;
   const JobDev& J = decode_local(bt, tile);
   if (glisa_idle(J)) return;
-  float ah[kTrials], al[kTrials];
+  float ah[kTrials], al[kTrials], an[kTrials];
 #pragma unroll
-  for (int t = 0; t < kTrials; ++t) ah[t] = al[t] = 0.0f;
+  for (int t = 0; t < kTrials; ++t) ah[t] = al[t] = an[t] = 0.0f;
   const int nclip = J.clip[J.nshell];
   const double cut = J.density_cutoff;
   for (int i = 0; i < J.ppt; ++i) {
@@ -2376,8 +2382,10 @@ __global__ void __launch_bounds__(kThreads) k_glisa_trials(Batch bt) {
       const bool ht = !(rho < cut || rt < cut);
       double big = 0.0;
       float term = 0.0f;
-      if (h0 && ht) term = -wr * log1pf((float)(dr * inv));
-      else if (ht) big = w * rho * log(rho / rt);
+      if (h0 && ht) {
+        term = -wr * log1pf((float)(dr * inv));
+        an[t] += fabsf(term);
+      } else if (ht) big = w * rho * log(rho / rt);
       else if (h0) big = -(w * rho * log(rho / r0));
       if (big != 0.0) {
         const float bh = (float)big;
@@ -2390,17 +2398,31 @@ __global__ void __launch_bounds__(kThreads) k_glisa_trials(Batch bt) {
       ah[t] = s;
     }
   }
-  double acc[kTrials];
+  double acc[2 * kTrials];
 #pragma unroll
-  for (int t = 0; t < kTrials; ++t) acc[t] = (double)ah[t] + (double)al[t];
-  block_sum<kTrials>(acc, red, out);
-  if (threadIdx.x < kTrials) J.tpart[(size_t)threadIdx.x * J.ntile + tile] = out[threadIdx.x];
+  for (int t = 0; t < kTrials; ++t) {
+    acc[t] = (double)ah[t] + (double)al[t];
+    acc[kTrials + t] = (double)an[t];
+  }
+  block_sum<2 * kTrials>(acc, red, out);
+  if (threadIdx.x < 2 * kTrials) J.tpart[(size_t)threadIdx.x * J.ntile + tile] = out[threadIdx.x];
 }
 
 // One warp per job: Armijo choice among the trials, apply the step.
 // One warp per trial (kTrials warps): warp t forms F(c_t) - F(c) and the
 // Armijo bound of trial t; the first trial (in step order) that passes is
-// taken, the shortest step if none does.
+// taken, the shortest step if none does. The trial passes form most terms
+// of f(c_t) - f(c) with the FP32 log1pf (a few ulp of each term: the ratio,
+// log1pf and the product), and return the sum of those terms' magnitudes
+// beside the difference (tpart rows kTrials + t). A trial passes when its
+// difference is within kArmijoUlps ulp of that sum of the Armijo bound:
+// near the optimum the predicted decrease falls below the resolution of the
+// FP32 terms, the test can no longer tell the steps apart, and the full
+// Newton step is the one to take (a shortened step there moves the
+// parameters by a fraction of the remaining error and ends the loop on a
+// change that is small only because the step was).
+constexpr double kArmijoUlps = 8.0;
+
 __global__ void __launch_bounds__(32 * kTrials) k_glisa_trial_pick(Batch bt) {
   __shared__ int pass[kTrials];
   __shared__ int pick_s;
@@ -2409,27 +2431,38 @@ __global__ void __launch_bounds__(32 * kTrials) k_glisa_trial_pick(Batch bt) {
   if (glisa_idle(J)) return;
   const int lane = threadIdx.x & 31, t = threadIdx.x >> 5;
   const int M = J.nshell;
-  double c0 = 0.0;
-  for (int m = lane; m < M; m += 32) c0 += J.propars[m];
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) c0 += __shfl_xor_sync(0xffffffffu, c0, o);
-  double s = 0.0, dec = 0.0;
+  // sum (c_t - c) over the step the trial pass evaluated, 2^-t delta_m on
+  // the shells the projection keeps and -c_m on those it clips: near the
+  // optimum the whole change of F is ~1e-16, below the rounding of either
+  // the difference of the two sums (each ~ the electron count) or of c_t
+  // itself (c_t - c differs from 2^-t delta by the rounding of c + 2^-t
+  // delta, ~1e-16 c per shell, which rho0_t does not contain)
+  const double a = ldexp(1.0, -t);
+  double ds = 0.0, dec = 0.0;
   for (int m = lane; m < M; m += 32) {
-    const double ct = J.ctrial[t * M + m];
-    s += ct;
-    dec += (1.0 + J.grad[m]) * (ct - J.propars[m]);
+    const double c = J.propars[m], x = c + a * J.delta[m];
+    const double d = x < 0.0 ? -c : a * J.delta[m];
+    ds += d;
+    dec += (1.0 + J.grad[m]) * d;
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
-    s += __shfl_xor_sync(0xffffffffu, s, o);
+    ds += __shfl_xor_sync(0xffffffffu, ds, o);
     dec += __shfl_xor_sync(0xffffffffu, dec, o);
   }
-  double df = 0.0;  // f(c_t) - f(c)
-  for (int q = lane; q < J.ntile; q += 32) df += J.tpart[(size_t)t * J.ntile + q];
+  double df = 0.0, dn = 0.0;  // f(c_t) - f(c), and the magnitude of its FP32 terms
+  for (int q = lane; q < J.ntile; q += 32) {
+    df += J.tpart[(size_t)t * J.ntile + q];
+    dn += J.tpart[(size_t)(kTrials + t) * J.ntile + q];
+  }
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) df += __shfl_xor_sync(0xffffffffu, df, o);
-  // Armijo on F = f + sum c: F(c_t) <= F(c) + 1e-4 dF.(c_t - c)
-  if (lane == 0) pass[t] = df + (s - c0) <= 1e-4 * dec;
+  for (int o = 16; o > 0; o >>= 1) {
+    df += __shfl_xor_sync(0xffffffffu, df, o);
+    dn += __shfl_xor_sync(0xffffffffu, dn, o);
+  }
+  // Armijo on F = f + sum c: F(c_t) <= F(c) + 1e-4 dF.(c_t - c), up to the
+  // rounding of the FP32 terms
+  if (lane == 0) pass[t] = df + ds <= 1e-4 * dec + kArmijoUlps * 0x1p-24 * dn;
   __syncthreads();
   if (threadIdx.x == 0) {
     int pick = kTrials - 1;
@@ -2443,7 +2476,18 @@ __global__ void __launch_bounds__(32 * kTrials) k_glisa_trial_pick(Batch bt) {
   }
   __syncthreads();
   const int pick = pick_s;
-  for (int m = threadIdx.x; m < M; m += blockDim.x) J.propars[m] = J.ctrial[pick * M + m];
+  // the step's start (k_copy_old's work, which projected-Newton steps leave
+  // to this kernel): the parameters, and for fused jobs the entropy and
+  // negativity partials of the pass at them
+  for (int m = threadIdx.x; m < M; m += blockDim.x) {
+    J.propars_old[m] = J.propars[m];
+    J.propars[m] = J.ctrial[pick * M + m];
+  }
+  if (J.fuse)
+    for (int q = threadIdx.x; q < J.ntile; q += blockDim.x) {
+      J.jpart[(size_t)QJ_ENT_PREV * J.ntile + q] = J.jpart[(size_t)QJ_ENTROPY * J.ntile + q];
+      J.jpart[(size_t)QJ_NEG_PREV * J.ntile + q] = J.jpart[(size_t)QJ_NEG * J.ntile + q];
+    }
 }
 
 // ---------------------------------------------------------------------------

@@ -71,7 +71,25 @@ struct hp_ctx {
   int64_t prof_n[HP_KERNEL_COUNT] = {};
   long long launch_base = 0;
   int slots_hi = 0;  // one past the highest slot a job has used (mailboxes to read back)
+  // Job memory (the carved job allocation and the packed G of fused gLISA
+  // jobs) comes from this stream-ordered pool on the context's stream; freed
+  // blocks stay in the pool (release threshold: never), so that a stream of
+  // job creations and destructions does not map and unmap device memory
+  // each time. Destroying the context returns it to the device.
+  cudaMemPool_t pool = nullptr;
 };
+
+namespace {
+
+cudaError_t job_alloc(hp_ctx* c, void** p, size_t bytes) {
+  return cudaMallocFromPoolAsync(p, bytes, c->pool, c->stream);
+}
+
+void job_free(hp_ctx* c, void* p) {
+  if (p) cudaFreeAsync(p, c->stream);
+}
+
+}  // namespace
 
 struct hp_job {
   hp_ctx* ctx = nullptr;
@@ -281,11 +299,56 @@ int run_inner(hp_ctx* ctx, const std::vector<hp_job*>& jobs, const HostBatch& hb
   return HP_OK;
 }
 
+// Work of a point tile in a fused pass, in row-equivalents per sub-tile: its
+// active rows plus the per-sub-tile cost that does not depend on them (the
+// per-point step, barriers and staging waits; about a hundred rows' worth
+// measured on the 150-shell benchmark molecule, 64 taken).
+constexpr int64_t kTileFixedRows = 64;
+
+// Tile schedule of the fused passes (longest processing time first): the
+// tiles by decreasing work (ties by index) each go to the least loaded of
+// the nb persistent blocks (ties by block index); each block then takes its
+// tiles in ascending order. A block's Hessian partial accumulates its tiles
+// in that order, so the schedule, a function of the job's own active-row
+// counts, keeps a job's results the same alone and in a batch. The trial
+// pass (one block per tile) visits the tiles heaviest first, which the block
+// scheduler turns into the same kind of balance.
+std::vector<int> tile_schedule(const std::vector<int64_t>& work, int nb) {
+  const int nt = (int)work.size();
+  std::vector<int> order(nt);
+  for (int t = 0; t < nt; ++t) order[t] = t;
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return work[a] > work[b]; });
+  std::vector<int64_t> load(nb, 0);
+  std::vector<int> owner(nt, 0);
+  // min-heap of (load, block): the comparator orders larger loads (then larger blocks) first
+  std::vector<std::pair<int64_t, int>> heap;
+  for (int b = 0; b < nb; ++b) heap.push_back({0, b});
+  auto cmp = [](const std::pair<int64_t, int>& x, const std::pair<int64_t, int>& y) {
+    return x.first != y.first ? x.first > y.first : x.second > y.second;
+  };
+  std::make_heap(heap.begin(), heap.end(), cmp);
+  for (int t : order) {
+    std::pop_heap(heap.begin(), heap.end(), cmp);
+    auto& top = heap.back();
+    owner[t] = top.second;
+    top.first += work[t];
+    std::push_heap(heap.begin(), heap.end(), cmp);
+  }
+  std::vector<int> out((size_t)nb + 1 + 2 * (size_t)nt, 0);
+  for (int t = 0; t < nt; ++t) out[owner[t] + 1] += 1;
+  for (int b = 0; b < nb; ++b) out[b + 1] += out[b];
+  std::vector<int> fill(out.begin(), out.begin() + nb);
+  for (int t = 0; t < nt; ++t) out[nb + 1 + fill[owner[t]]++] = t;  // ascending within a block
+  for (int k = 0; k < nt; ++k) out[(size_t)nb + 1 + nt + k] = order[k];
+  return out;
+}
+
 // Fused gLISA jobs: the packed layout of G's active rows (k_glisa_pack)
 // from the per-tile active-row counts of k_glisa_active: tile t's sub-tiles
-// start at gtile_off[t] in each plane and hold nact_t rows of 32 floats each.
-// The arrays are allocated at the first initialisation of a job (the counts
-// depend only on G) and charged to the context.
+// start at gtile_off[t] in each plane and hold nact_t rows of 32 floats each;
+// and the tile schedule of the passes (tile_schedule). The arrays are
+// allocated at the first initialisation of a job (the counts depend only on
+// G) and charged to the context.
 int pack_layout(hp_ctx* ctx, const std::vector<hp_job*>& jobs) {
   bool any = false;
   for (hp_job* j : jobs) any |= j->dev.fuse && !j->dev.gpack;
@@ -297,7 +360,7 @@ int pack_layout(hp_ctx* ctx, const std::vector<hp_job*>& jobs) {
     const int S = J.nshell;
     std::vector<int> g((size_t)(S + 1) * J.ntile);
     HP_CK(cudaMemcpy(g.data(), J.gact, sizeof(int) * g.size(), cudaMemcpyDeviceToHost));
-    std::vector<int64_t> off(J.ntile);
+    std::vector<int64_t> off(J.ntile), work(J.ntile);
     int64_t total = 0;
     int nmax = 0;
     for (int t = 0; t < J.ntile; ++t) {
@@ -307,20 +370,31 @@ int pack_layout(hp_ctx* ctx, const std::vector<hp_job*>& jobs) {
       off[t] = total;
       total += nsub * 32 * (int64_t)nact;
       nmax = std::max(nmax, nact);
+      work[t] = nsub * (nact + kTileFixedRows);
     }
-    const size_t bytes = 2 * 4 * (size_t)std::max<int64_t>(total, 1) + 8 * (size_t)J.ntile;
+    const int nb = std::min(J.ntile, kFuseCtas);
+    const std::vector<int> sched = tile_schedule(work, nb);
+    const size_t gbytes = 2 * 4 * (size_t)std::max<int64_t>(total, 1);
+    const size_t bytes = gbytes + 8 * (size_t)J.ntile + 4 * sched.size();
     if (ctx->used + bytes > ctx->budget) return fail(HP_ERR_NO_MEMORY, "HBM budget exceeded (packed G)");
     void* mem = nullptr;
-    if (cudaMalloc(&mem, bytes) != cudaSuccess) return fail(HP_ERR_NO_MEMORY, "device allocation failed");
+    if (job_alloc(ctx, &mem, bytes) != cudaSuccess) {
+      cudaGetLastError();
+      return fail(HP_ERR_NO_MEMORY, "device allocation failed");
+    }
     J.gpack = reinterpret_cast<float*>(mem);
     J.gpack_plane = total;
-    J.gtile_off = reinterpret_cast<int64_t*>(reinterpret_cast<char*>(mem) + 2 * 4 * (size_t)std::max<int64_t>(total, 1));
+    J.gtile_off = reinterpret_cast<int64_t*>(reinterpret_cast<char*>(mem) + gbytes);
+    J.fsched = reinterpret_cast<int*>(reinterpret_cast<char*>(mem) + gbytes + 8 * (size_t)J.ntile);
     J.nact_max = nmax;
     j->pack_mem = mem;
     j->pack_bytes = bytes;
     j->bytes += bytes;
     ctx->used += bytes;
-    HP_CK(cudaMemcpy(J.gtile_off, off.data(), 8 * (size_t)J.ntile, cudaMemcpyHostToDevice));
+    // on the context stream, where the allocation is ordered (pageable
+    // sources: each call returns once its source has been read)
+    HP_CK(cudaMemcpyAsync(J.gtile_off, off.data(), 8 * (size_t)J.ntile, cudaMemcpyHostToDevice, ctx->stream));
+    HP_CK(cudaMemcpyAsync(J.fsched, sched.data(), 4 * sched.size(), cudaMemcpyHostToDevice, ctx->stream));
   }
   return HP_OK;
 }
@@ -509,7 +583,8 @@ int step_glisa(hp_ctx* ctx, const std::vector<hp_job*>& jobs, const HostBatch& h
   if (!fused) fuse_shells = 0;
   const int unfused = fused ? 0 : 1;
   for (int iter = 0; iter < iters; ++iter) {
-  launch_copy_old(hb, st);
+  // projected Newton keeps the step's start in k_glisa_trial_pick
+  if (solver != SOLVER_PNEWTON) launch_copy_old(hb, st);
   if (!fused) {
     ProfScope ps(ctx, HP_KERNEL_GLISA_PRO);
     if (gff) launch_glisa_pro_ff(hb, st);
@@ -808,6 +883,19 @@ int32_t hp_ctx_create(int32_t device, size_t hbm_budget, void* stream, hp_ctx** 
     }
     c->own_stream = true;
   }
+  {
+    cudaMemPoolProps pp{};
+    pp.allocType = cudaMemAllocationTypePinned;
+    pp.location.type = cudaMemLocationTypeDevice;
+    pp.location.id = device;
+    uint64_t keep = UINT64_MAX;
+    if (cudaMemPoolCreate(&c->pool, &pp) != cudaSuccess ||
+        cudaMemPoolSetAttribute(c->pool, cudaMemPoolAttrReleaseThreshold, &keep) != cudaSuccess) {
+      cudaGetLastError();
+      hp_ctx_destroy(c);
+      return fail(HP_ERR_CUDA, "device memory pool creation failed");
+    }
+  }
   size_t fr = 0, tot = 0;
   cudaMemGetInfo(&fr, &tot);
   c->budget = hbm_budget ? hbm_budget : (size_t)(0.9 * (double)fr);
@@ -841,6 +929,10 @@ int32_t hp_ctx_destroy(hp_ctx* c) {
   if (c->prefix_host) cudaFreeHost(c->prefix_host);
   prof_collect(c);
   for (cudaEvent_t e : c->event_pool) cudaEventDestroy(e);
+  if (c->pool) {
+    if (c->stream) cudaStreamSynchronize(c->stream);  // the jobs' frees have run
+    cudaMemPoolDestroy(c->pool);
+  }
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
   delete c;
   return HP_OK;
@@ -994,7 +1086,7 @@ int32_t hp_job_create(hp_ctx* ctx, const hp_job_desc* d, hp_job** out) {
     add(&J.grad, 8 * (size_t)S);
     add(&J.dvec1, 8 * (size_t)N); add(&J.dvec2, 8 * (size_t)N);
     add(&J.ctrial, 8 * (size_t)kTrials * S);
-    add(&J.tpart, 8 * (size_t)kTrials * ntile);
+    add(&J.tpart, 8 * 2 * (size_t)kTrials * ntile);  // per trial: difference, then the magnitude of its FP32 terms
     add(&J.freeidx, 4 * (size_t)(S + 2));
     add(&J.clip, 4 * (size_t)(2 * S + 1));
     add(&J.rho0, 8 * (size_t)N);
@@ -1045,9 +1137,9 @@ int32_t hp_job_create(hp_ctx* ctx, const hp_job_desc* d, hp_job** out) {
   if (ctx->used + total > ctx->budget)
     return fail(HP_ERR_NO_MEMORY, "job needs " + std::to_string(total) + " bytes; HBM budget exceeded");
   void* mem = nullptr;
-  if (cudaMalloc(&mem, total) != cudaSuccess) {
+  if (job_alloc(ctx, &mem, total) != cudaSuccess) {
     cudaGetLastError();
-    return fail(HP_ERR_NO_MEMORY, "cudaMalloc of " + std::to_string(total) + " bytes failed");
+    return fail(HP_ERR_NO_MEMORY, "device allocation of " + std::to_string(total) + " bytes failed");
   }
   char* cur = (char*)mem;
   for (auto& p : parts) {
@@ -1247,7 +1339,7 @@ int32_t hp_job_create(hp_ctx* ctx, const hp_job_desc* d, hp_job** out) {
   ok &= cudaMemsetAsync(ctx->mail_dev + slot, 0, sizeof(Mailbox), st) == cudaSuccess;
   ok &= cudaStreamSynchronize(st) == cudaSuccess;
   if (!ok) {
-    cudaFree(mem);
+    job_free(ctx, mem);
     delete job;
     return fail(HP_ERR_CUDA, "upload of job inputs failed");
   }
@@ -1264,8 +1356,8 @@ int32_t hp_job_destroy(hp_job* job) {
   hp_ctx* ctx = job->ctx;
   cudaSetDevice(ctx->device);
   cudaStreamSynchronize(ctx->stream);
-  if (job->mem) cudaFree(job->mem);
-  if (job->pack_mem) cudaFree(job->pack_mem);
+  job_free(ctx, job->mem);  // back to the context's pool, in stream order
+  job_free(ctx, job->pack_mem);
   ctx->used -= job->bytes;
   ctx->slots[job->slot] = nullptr;
   delete job;

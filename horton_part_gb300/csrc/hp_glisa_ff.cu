@@ -315,7 +315,7 @@ __global__ void __launch_bounds__(kThreads) k_glisa_trials_ff(Batch bt) {
 //      merged into the warp's partial sum of u(p);
 //   A' warp 0 merges the eight partials in warp order and forms v(p) (and
 //      for MODE 1 s(p), writing rho0(p)) for the sub-tile's points, published
-//      in shared memory; meanwhile warps 1-7 form the outer change (C below);
+//      in shared memory;
 //   B  every warp adds G[m][p] v(p) of its rows to compensated accumulators
 //      kept in registers across the tile (reduced once at its end) and, MODE
 //      1, writes its rows of X = G_hi diag(s) for the tensor-core Hessian.
@@ -329,13 +329,9 @@ __global__ void __launch_bounds__(kThreads) k_glisa_trials_ff(Batch bt) {
 // MODE 0 (refinement product): x = delta, v = (w rho / rho0^2) u.
 // MODE 1 (promolecule + gradient): x = c, u = rho0 (r0f) and v = w rho /
 //   rho0, quotients in float-float (the entropy, w rho / rho0^2 and the
-//   negativity count follow in k_glisa_point_ff). With with_change, also
-//   C  the outer change of the step that produced c (glisa.py:776 via
-//      compute_change): warps 1-7 take the atoms a = w - 1 (mod 7), lane =
-//      point, sum_{m in a} (c - c_old)_m g_m from the staged sub-tile's G_hi
-//      in FP32 (the change is only compared with the threshold: ~1e-6
-//      relative is ample), w times its square summed per thread as a float
-//      pair; the tile's total goes to atom 0's QA_CHANGE slot.
+//   negativity count follow in k_glisa_point_ff). The outer change of the
+//   step that produced c needs no pass over the grid: k_outer_finish forms
+//   it from the per-atom Gram blocks of k_glisa_wgram.
 // Jobs with more than kFuseMaxShells shells use k_glisa_pro_ff /
 // k_glisa_hv_ff with k_glisa_grad_ff.
 // ---------------------------------------------------------------------------
@@ -361,12 +357,12 @@ constexpr int kRingSlots = 6;
 
 // Shared memory of a fused pass for S shells without its staging ring (bytes).
 __host__ __device__ constexpr size_t fuse_fixed_bytes(int S) {
-  return 16 * (size_t)S                    // per active row: x pair and the parameter change
+  return 8 * (size_t)S                     // per active row: x as a float pair
          + 8 * (size_t)kFuseWarps * kFuseSP  // partial sums
          + 32 * (size_t)kFuseSP              // per point: (v, s)
          + 8 * (size_t)(kFuseMaxShells - kFuseRegRowsTotal)  // gradient sums of the rows past them
          + 8 * (2 * kFuseWarps + 2)          // block sums
-         + 16 * (size_t)S + 8                // active shells, positions, per-atom offsets, X keys
+         + 12 * (size_t)S                    // active shells, positions, X keys
          + 16 + 8 * kRingSlots;              // the ring's mbarriers (16-byte aligned)
 }
 
@@ -445,13 +441,13 @@ static_assert(fuse_fixed_bytes(kFuseMaxShells, 1) + 4 * (size_t)fuse_ring_floats
 // gradient and objective stay compensated.
 //
 // Per tile the active rows' values that every sub-tile needs are compacted
-// once: x[act[i]] (xa), the X-tile word of row act[i] for lane 0 (xkey; the
-// 128B swizzle makes lane l's word xkey ^ l) and the parameter change
-// (dca), so that the row loops read them at fixed offsets.
+// once: x[act[i]] (xa) and the X-tile word of row act[i] for lane 0 (xkey;
+// the 128B swizzle makes lane l's word xkey ^ l), so that the row loops read
+// them at fixed offsets.
 // MODE 1 writes rho0 (r0f); the entropy, the negativity count and w rho /
 // rho0^2 (d2f) follow in k_glisa_point_ff.
 template <int MODE>
-__global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_fused_ff(Batch bt, int with_change, int ring_floats) {
+__global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_fused_ff(Batch bt, int ring_floats) {
   extern __shared__ float4 fsm[];
   int local;
   const JobDev& J = decode_local_gf(bt, local);
@@ -469,15 +465,13 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_fused_ff(Batch bt, in
   uint32_t* xt = reinterpret_cast<uint32_t*>(reinterpret_cast<uint8_t*>(fsm) + xoff);
   float* ring = hess ? reinterpret_cast<float*>(xt + 32 * xrows) : reinterpret_cast<float*>(fsm);
   float2* xa = reinterpret_cast<float2*>(ring + ring_floats);  // x of active row i
-  float* dca = reinterpret_cast<float*>(xa + S);                   // change of active row i
-  Dot2* part = reinterpret_cast<Dot2*>(dca + 2 * S);
+  Dot2* part = reinterpret_cast<Dot2*>(xa + S);
   float4* pvs = reinterpret_cast<float4*>(part + kFuseWarps * kFuseSP);  // (v hi, v lo, s, -)
   Dot2* ovf = reinterpret_cast<Dot2*>(pvs + 2 * kFuseSP);  // rows i >= kFuseRegRowsTotal
   double* red = reinterpret_cast<double*>(ovf + (kFuseMaxShells - kFuseRegRowsTotal));
   int* act = reinterpret_cast<int*>(red + 2 * kFuseWarps + 2);
   int* pos = act + S;
-  int* aoff = pos + S;  // atom a's active rows: [aoff[a], aoff[a + 1]) (act is ordered by shell)
-  int* xkey = aoff + S + 2;
+  int* xkey = pos + S;
   uint64_t* rbar = reinterpret_cast<uint64_t*>((reinterpret_cast<uintptr_t>(xkey + S) + 15) & ~uintptr_t(15));
   uint64_t* mbar = rbar + kRingSlots;  // the MMAs' commits (MODE 1)
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(mbar + 1);
@@ -486,9 +480,7 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_fused_ff(Batch bt, in
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const float4* __restrict__ wrfp = J.wrf;
   const float2* __restrict__ d2in = J.d2f;
-  const double* __restrict__ wp = J.w;
   float2* r0fo = J.r0f;
-  const int natom = J.natom;
   const int n1 = (S + 15) / 16 * 16;
   const int c2 = (n1 + 31) / 32 * 32;
   const bool has_d2 = n1 > umma::kTcM;
@@ -543,23 +535,11 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_fused_ff(Batch bt, in
     if (nmma > 0 && !timed_out && !umma::mbar_wait_sleep(bar, (uint32_t)((nmma - 1) & 1))) timed_out = 1;
   };
   const double* x = MODE ? J.propars : J.delta;
-  const bool chg = MODE == 1 && with_change;
-  float ch = 0.0f, cl = 0.0f;  // change terms of this thread (float pair)
-  // C: the change terms of atoms a0, a0 + astep, ... for this lane's point
-  // (atoms with no active row add exact zeros: skipped)
-  auto change_terms = [&](const float* ghl, float wf, int a0, int astep) {
-    for (int a = a0; a < natom; a += astep) {
-      const int i0 = aoff[a], i1 = aoff[a + 1];
-      if (i0 == i1) continue;
-      float dv = 0.0f;
-      for (int i = i0; i < i1; ++i) dv = fmaf(ghl[i * kFuseSP], dca[i], dv);
-      const float term = wf * dv * dv;
-      const float t = ch + term;
-      const float bb = t - ch;
-      cl += (ch - (t - bb)) + (term - bb);
-      ch = t;
-    }
-  };
+  // MODE 1 after an accepted projected-Newton trial (away from convergence):
+  // rho0 of this pass is the trial pass's density of that trial (r0t), and
+  // the pass skips A and A' (one block barrier per sub-tile instead of three)
+  const int r0sel = MODE == 1 ? J.mail->i[MI_R0T] : 0;
+  const float2* __restrict__ r0in = r0sel > 0 ? J.r0t + (size_t)(r0sel - 1) * J.npoint : nullptr;
 
   const int* __restrict__ tiles = J.fsched + nblk_job + 1;
   for (int k = J.fsched[local]; k < J.fsched[local + 1]; ++k) {
@@ -596,24 +576,10 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_fused_ff(Batch bt, in
       const int m = act[i];
       xa[i] = split2(x[m]);
       xkey[i] = m * 32 + ((m & 7) << 2);
-      if (chg) dca[i] = (float)(J.propars[m] - J.propars_old[m]);
       if (i >= kFuseRegRowsTotal) ovf[i - kFuseRegRowsTotal] = Dot2{0.f, 0.f};
     }
-    if (chg)
-      for (int a = threadIdx.x; a <= natom; a += kFuseThreads) {
-        const int s0 = J.shell_off[a];
-        int lo = 0, hi = nact;  // first active row with shell >= s0
-        while (lo < hi) {
-          const int mid = (lo + hi) >> 1;
-          if (act[mid] < s0) lo = mid + 1;
-          else hi = mid;
-        }
-        aoff[a] = lo;
-      }
     // this warp's rows i = warp + 8 r, r < nr
     const int nr = nact > warp ? (nact - warp + kFuseWarps - 1) / kFuseWarps : 0;
-    ch = 0.0f;
-    cl = 0.0f;
     Dot2 acc[kFuseRows];
 #pragma unroll
     for (int r = 0; r < kFuseRows; ++r) acc[r] = Dot2{0.f, 0.f};
@@ -633,21 +599,36 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_fused_ff(Batch bt, in
       const float* glw = gl + warp * kFuseSP + lane;
       f2 v{0.f, 0.f};
       float sx = 0.0f;
-      {
-        // per-point inputs, loaded before phase A so that their latency
-        // overlaps it: (w rho, rho) pairs (MODE 1) or the d2 pair (MODE 0) for
-        // warp 0, w for the change warps
-        float wf = 0.0f;
-        float4 qpre = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (r0in) {
+        // rho0 given: every warp forms v and s of its lane's point (warp 0
+        // also stores rho0); the loads are issued before the staging wait
+        float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
+        float2 r0s = make_float2(0.f, 0.f);
         if (pq < p1) {
-          if (warp == 0) {
-            if (MODE == 1) qpre = wrfp[pq];
-            else {
-              const float2 d2 = d2in[pq];
-              qpre = make_float4(d2.x, d2.y, 0.f, 0.f);
-            }
+          q = wrfp[pq];
+          r0s = r0in[pq];
+        }
+        if (!timed_out && !umma::mbar_wait_sleep(rbar0 + 8 * slot, (ring_phase >> slot) & 1u))
+          timed_out = 1;
+        ring_phase ^= 1u << slot;  // sub-tile sub is in the slot
+        if (pq < p1) {
+          const f2 r0{r0s.x, r0s.y};
+          if (warp == 0) r0fo[pq] = r0s;
+          if (!(below(f2{q.z, q.w}, cutp) || below(r0, cutp))) {
+            v = ffa::div(f2{q.x, q.y}, r0);
+            sx = sqrtf(q.x) / r0.hi;
           }
-          if (chg && warp > 0) wf = (float)wp[pq];
+        }
+      } else {
+        // per-point inputs of warp 0, loaded before phase A so that their
+        // latency overlaps it: (w rho, rho) pairs (MODE 1) or the d2 pair (MODE 0)
+        float4 qpre = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (pq < p1 && warp == 0) {
+          if (MODE == 1) qpre = wrfp[pq];
+          else {
+            const float2 d2 = d2in[pq];
+            qpre = make_float4(d2.x, d2.y, 0.f, 0.f);
+          }
         }
         if (!timed_out && !umma::mbar_wait_sleep(rbar0 + 8 * slot, (ring_phase >> slot) & 1u))
           timed_out = 1;
@@ -690,8 +671,6 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_fused_ff(Batch bt, in
             }
           }
           pvs[lane] = make_float4(vw.hi, vw.lo, sw, 0.f);
-        } else if (chg) {
-          change_terms(gh + lane, wf, warp - 1, kFuseWarps - 1);  // C
         }
         __syncthreads();  // v and s of the sub-tile visible
         const float4 pv = pvs[lane];
@@ -747,17 +726,6 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_fused_ff(Batch bt, in
         J.gpart[(size_t)act[i] * J.ntile + tile] = dot2_value(ovf[i - kFuseRegRowsTotal]);
       }
     zero_inactive(J, tile, pos);
-    if (chg) {
-      double c = (double)ch + (double)cl;
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
-      if (lane == 0) red[warp] = c;
-      __syncthreads();
-      double sc = 0.0;
-      for (int k = 0; k < kFuseWarps; ++k) sc += red[k];
-      for (int a = threadIdx.x; a < J.natom; a += kFuseThreads)
-        J.apart[((size_t)a * J.qa + QA_CHANGE) * J.ntile + tile] = a == 0 ? sc : 0.0;
-    }
   }
   if (!hess) return;
   // Epilogue: the block's Hessian partial from tensor memory. Warp w reads
@@ -1047,6 +1015,7 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_trials_fused(Batch bt
       const bool h0 = !(rs || below(f2{r0p.x, r0p.y}, cutp));
       const f2 dr = ffa::add(f2{at * u.hi, at * u.lo}, corr);
       const f2 rt = ffa::add(dr, f2{r0p.x, r0p.y});
+      J.r0t[(size_t)t * J.npoint + p] = make_float2(rt.hi, rt.lo);  // rho0 of the trial (next pass)
       const bool ht = !(rs || below(rt, cutp));
       float term = 0.0f;
       if (h0 && ht) {
@@ -1198,6 +1167,161 @@ __global__ void __launch_bounds__(kThreads) k_glisa_pack(Batch bt) {
   }
 }
 
+// Per-atom weighted Gram blocks of G, for the outer change of fused jobs on
+// the molecular grid (glisa.py:776 via compute_change). The change of a step
+// is sum_a int w (sum_{i in a} dc_i g_i)^2 = sum_a dc_a^T W_a dc_a with
+// W_a[i][j] = sum_p w_p g_i(p) g_j(p) over the shells i, j of atom a: the
+// same quadrature sum regrouped, so no pass over the grid is needed per
+// iteration (k_outer_finish forms the quadratic forms in FP64). W depends on
+// G and the weights only and is formed at each job initialisation, after
+// k_glisa_pack, in two kernels:
+//   k_glisa_wgram     one block per point tile: the tile's pairs (i >= j) of
+//                     active rows of one atom, kWgRound at a time, warp w
+//                     taking pairs w, w + 8, ...; the high plane of each
+//                     packed sub-tile is staged in shared memory, and lane l
+//                     adds (w g_i g_j)(l) (FP32 products of the high parts,
+//                     ~1e-7 relative each) to a compensated sum per pair; the
+//                     lane sums of a pair are merged in a fixed order and
+//                     written to wgpart[entry][tile] (entries of pairs
+//                     inactive on the tile: zero). The change is compared with
+//                     the threshold and reported: 1e-7 of W is the accuracy of
+//                     the FP32 change sums of the other passes;
+//   k_glisa_wgram_sum one warp per entry: the tiles' partials in FP64, tile
+//                     order in four chains.
+constexpr int kWgRound = 256;                           // pairs per round of a block
+constexpr int kWgPerWarp = kWgRound / kWarps;           // compensated sums per lane
+
+__global__ void __launch_bounds__(kThreads) k_glisa_wgram(Batch bt) {
+  extern __shared__ float4 wsm4[];            // one sub-tile's high plane: nact rows x 32 points
+  __shared__ int act[kFuseMaxShells];
+  __shared__ int first[kFuseMaxShells];       // active row i: first active row of its atom
+  __shared__ int pstart[kFuseMaxShells + 1];  // pairs of rows < i (pairs (i, j), j <= i, one atom)
+  __shared__ int patom[kFuseMaxShells];       // atom of active row i
+  int tile;
+  const JobDev& J = decode_local_gf(bt, tile);
+  if (!J.fuse || !J.gpack || !J.wgram) return;
+  float* wsm = reinterpret_cast<float*>(wsm4);
+  const int S = J.nshell;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int* g = J.gact + (size_t)tile * (S + 1);
+  const int nact = g[S];
+  for (int e = threadIdx.x; e < J.wgn; e += kThreads) J.wgpart[(size_t)e * J.ntile + tile] = 0.0;
+  for (int i = threadIdx.x; i < nact; i += kThreads) act[i] = g[i];
+  __syncthreads();
+  for (int i = threadIdx.x; i < nact; i += kThreads) {
+    const int m = act[i];
+    int lo = 0, hi = J.natom;  // the atom a with shell_off[a] <= m < shell_off[a + 1]
+    while (hi - lo > 1) {
+      const int mid = (lo + hi) >> 1;
+      if (J.shell_off[mid] <= m) lo = mid;
+      else hi = mid;
+    }
+    const int s0 = J.shell_off[lo];
+    int f = 0, h = i;  // first active row with shell >= s0
+    while (f < h) {
+      const int mid = (f + h) >> 1;
+      if (act[mid] < s0) f = mid + 1;
+      else h = mid;
+    }
+    patom[i] = lo;
+    first[i] = f;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int n = 0;
+    for (int i = 0; i < nact; ++i) {
+      pstart[i] = n;
+      n += i - first[i] + 1;
+    }
+    pstart[nact] = n;
+  }
+  __syncthreads();
+  const int npair = pstart[nact];
+  const int p0 = tile * J.tile_points;
+  const int p1 = min(p0 + J.tile_points, J.npoint);
+  const int nsub = (p1 - p0 + 31) / 32;
+  const int plane = nact * 32;  // floats of the high plane of a sub-tile
+  const float4* ghi = reinterpret_cast<const float4*>(J.gpack + J.gtile_off[tile]);
+  for (int r0 = 0; r0 < npair; r0 += kWgRound) {
+    // the pair's staged rows, (row i) << 16 | row j (-1: no pair)
+    int rij[kWgPerWarp];
+#pragma unroll
+    for (int k = 0; k < kWgPerWarp; ++k) {
+      const int p = r0 + warp + kWarps * k;
+      rij[k] = -1;
+      if (p < npair) {
+        int a = 0, b = nact;  // the row i with pstart[i] <= p < pstart[i + 1]
+        while (b - a > 1) {
+          const int mid = (a + b) >> 1;
+          if (pstart[mid] <= p) a = mid;
+          else b = mid;
+        }
+        rij[k] = (a << 16) | (first[a] + (p - pstart[a]));
+      }
+    }
+    float accs[kWgPerWarp], accc[kWgPerWarp];  // compensated sums (sum, rounding errors)
+#pragma unroll
+    for (int k = 0; k < kWgPerWarp; ++k) accs[k] = accc[k] = 0.0f;
+    for (int sub = 0; sub < nsub; ++sub) {
+      __syncthreads();  // the previous sub-tile is consumed
+      for (int e = threadIdx.x; e < plane / 4; e += kThreads) wsm4[e] = ghi[(size_t)sub * (plane / 4) + e];
+      const int q = p0 + 32 * sub + lane;
+      const float wl = q < p1 ? (float)J.w[q] : 0.0f;  // packed entries past p1 are zero
+      __syncthreads();
+#pragma unroll
+      for (int k = 0; k < kWgPerWarp; ++k) {
+        if (rij[k] < 0) continue;  // warp-uniform
+        const float t = wl * wsm[(rij[k] >> 16) * 32 + lane] * wsm[(rij[k] & 0xffff) * 32 + lane];
+        const float u = accs[k] + t;
+        const float bb = u - accs[k];
+        accc[k] += (accs[k] - (u - bb)) + (t - bb);
+        accs[k] = u;
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < kWgPerWarp; ++k) {
+      if (rij[k] < 0) continue;
+      Dot2 d{accs[k], accc[k]};
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const Dot2 b{__shfl_xor_sync(0xffffffffu, d.s, o), __shfl_xor_sync(0xffffffffu, d.c, o)};
+        dot2_merge(d, b);
+      }
+      if (lane == 0) {
+        const int i = rij[k] >> 16, j = rij[k] & 0xffff;
+        const int a = patom[i];
+        const int s0 = J.shell_off[a];
+        const int li = act[i] - s0, lj = act[j] - s0;
+        J.wgpart[(size_t)(J.wgoff[a] + li * (li + 1) / 2 + lj) * J.ntile + tile] = dot2_value(d);
+      }
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kThreads) k_glisa_wgram_sum(Batch bt) {
+  int local;
+  const JobDev& J = decode_local_gf(bt, local);
+  if (!J.fuse || !J.wgram) return;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nblk = (J.nshell * J.nshell + kThreads - 1) / kThreads;  // this job's K_SQUARE blocks
+  for (int e = local * kWarps + warp; e < J.wgn; e += nblk * kWarps) {
+    const double* gp = J.wgpart + (size_t)e * J.ntile;
+    double h0 = 0.0, h1 = 0.0, h2 = 0.0, h3 = 0.0;
+    int t = lane;
+    for (; t + 96 < J.ntile; t += 128) {
+      h0 += gp[t];
+      h1 += gp[t + 32];
+      h2 += gp[t + 64];
+      h3 += gp[t + 96];
+    }
+    for (; t < J.ntile; t += 32) h0 += gp[t];
+    double h = (h0 + h1) + (h2 + h3);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) h += __shfl_xor_sync(0xffffffffu, h, o);
+    if (lane == 0) J.wgram[e] = h;
+  }
+}
+
 // Final promolecule of a float-float gLISA job (glisa.py:268-278 through
 // core/stockholder.py:153-175): per point, each atom's pro-atom
 // sum_m c_m g_m as a compensated dot product; rho_a, the promolecule (+1e-100
@@ -1271,26 +1395,27 @@ void ensure_exp_table_gl() {
                        (int)kFuseSmemMax);
   cudaFuncSetAttribute(k_glisa_trials_fused, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)kFuseSmemMax);
+  cudaFuncSetAttribute(k_glisa_wgram, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       32 * 4 * kFuseMaxShells);
   if (dev < 31) done_mask |= 1 << dev;
 }
 
 }  // namespace
 
-void launch_glisa_fused_ff(const HostBatch& hb, cudaStream_t st, int mode, int max_shells,
-                           int with_change) {
+void launch_glisa_fused_ff(const HostBatch& hb, cudaStream_t st, int mode, int max_shells) {
   if (hb.blocks[K_FUSE] <= 0) return;
   ensure_exp_table_gl();
   const int ring = fuse_ring_floats(max_shells, mode);
   const size_t smem = fuse_fixed_bytes(max_shells, mode) + 4 * (size_t)ring;
   if (mode) {
-    k_glisa_fused_ff<1><<<hb.blocks[K_FUSE], kFuseThreads, smem, st>>>(hb.b[K_FUSE], with_change, ring);
+    k_glisa_fused_ff<1><<<hb.blocks[K_FUSE], kFuseThreads, smem, st>>>(hb.b[K_FUSE], ring);
     ++g_launch_count;
     if (hb.blocks[K_POINT] > 0) {
       k_glisa_point_ff<<<hb.blocks[K_POINT], kThreads, 0, st>>>(hb.b[K_POINT]);
       ++g_launch_count;
     }
   } else {
-    k_glisa_fused_ff<0><<<hb.blocks[K_FUSE], kFuseThreads, smem, st>>>(hb.b[K_FUSE], 0, ring);
+    k_glisa_fused_ff<0><<<hb.blocks[K_FUSE], kFuseThreads, smem, st>>>(hb.b[K_FUSE], ring);
     ++g_launch_count;
   }
 }
@@ -1310,6 +1435,16 @@ void launch_glisa_active(const HostBatch& hb, cudaStream_t st) {
 
 void launch_glisa_pack(const HostBatch& hb, cudaStream_t st) {
   HP_LAUNCH_GF(k_glisa_pack, K_POINT, kThreads);
+}
+
+void launch_glisa_wgram(const HostBatch& hb, cudaStream_t st) {
+  if (hb.blocks[K_POINT] > 0) {
+    ensure_exp_table_gl();  // also the shared-memory limits of the fused kernels
+    const size_t smem = 32 * 4 * (size_t)std::max(1, hb.nact_max);  // one staged high plane
+    k_glisa_wgram<<<hb.blocks[K_POINT], kThreads, smem, st>>>(hb.b[K_POINT]);
+    ++g_launch_count;
+  }
+  HP_LAUNCH_GF(k_glisa_wgram_sum, K_SQUARE, kThreads);
 }
 
 void launch_glisa_promol_ff(const HostBatch& hb, cudaStream_t st) {

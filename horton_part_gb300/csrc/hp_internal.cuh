@@ -70,6 +70,8 @@ enum MailI {
   MI_CONVERGED = 4,   // gLISA solver converged flag
   MI_F64_FACTORS = 5, // gLISA Newton steps of a tensor-core job factored in FP64
   MI_DONE = 6,        // gLISA: finished (converged, failed or out of iterations)
+  MI_R0T = 7,         // fused gLISA: 1 + the accepted trial whose densities (r0t) are the next
+                      // pass's rho0, 0 when that pass forms rho0 = G^T c itself
   MI_COUNT = 8
 };
 struct Mailbox {
@@ -172,6 +174,7 @@ struct JobDev {
   float2* rdist;          // mixed / ff (MBIS, GISA, aLISA): point-atom distances as float pairs [natom][npoint]
   float4* wrf;            // fused gLISA: (w rho hi, lo, rho hi, lo) per point (constant)
   float2* r0f;            // fused gLISA: rho0 as float pairs [npoint]
+  float2* r0t;            // fused gLISA: the trial pass's rho0 of each trial as float pairs [kTrials][npoint]
   float2* d2f;            // fused gLISA: w rho / rho0^2 as float pairs [npoint]
   double* hsum;           // gLISA tensor-core Hessian: refinement product H delta [nshell]
   int* gact;              // fused gLISA: per point tile the shells nonzero on it [ntile][nshell + 1]
@@ -184,6 +187,11 @@ struct JobDev {
                           // fsched[b + 1]) of the list at fsched + nb + 1 (ntile tiles, ascending
                           // within a block); then the ntile tiles heaviest first (trial pass);
                           // nb = min(ntile, kFuseCtas)
+  double* wgram;          // fused gLISA on the molecular grid: per atom the lower triangle of its
+                          // weighted Gram block W_a[i][j] = sum_p w_p g_i(p) g_j(p) (the outer change)
+  double* wgpart;         // per point tile partials of wgram [wgn][ntile]
+  int* wgoff;             // atom a's triangle starts at wgoff[a] [natom + 1]
+  int wgn;                // entries of wgram (wgoff[natom])
   float2* d1f;            // gLISA, gff: w rho / rho0 as float pairs, npoint
   float2* hvf;            // gLISA, gff: the refinement's hvec as float pairs, npoint
   float* hess_s;          // gLISA tensor-core Hessian: sqrt(w rho / rho0^2) as FP32, npoint
@@ -568,10 +576,7 @@ constexpr int kGffMaxShells = 2048;
 // fused passes (one read of G for a product and the row sums that follow it):
 // two shared-memory stages of [S][64] float pairs
 constexpr int kFuseMaxShells = 192;
-// mode 1 with with_change: also the outer change of the step just taken
-// (parameters minus propars_old), for fused jobs in place of k_glisa_change_ff
-void launch_glisa_fused_ff(const HostBatch& hb, cudaStream_t st, int mode, int max_shells,
-                           int with_change = 0);
+void launch_glisa_fused_ff(const HostBatch& hb, cudaStream_t st, int mode, int max_shells);
 void launch_glisa_basis_ff(const HostBatch& hb, cudaStream_t st);
 void launch_rdist_ff(const HostBatch& hb, cudaStream_t st);  // rdist of the batch's jobs
 void launch_glisa_pro_ff(const HostBatch& hb, cudaStream_t st);
@@ -581,6 +586,7 @@ void launch_glisa_trials_ff(const HostBatch& hb, cudaStream_t st);
 void launch_glisa_promol_ff(const HostBatch& hb, cudaStream_t st);  // final promolecule
 void launch_glisa_active(const HostBatch& hb, cudaStream_t st);    // per-tile active shells
 void launch_glisa_pack(const HostBatch& hb, cudaStream_t st);      // active rows packed per sub-tile
+void launch_glisa_wgram(const HostBatch& hb, cudaStream_t st);     // per-atom Gram blocks (outer change)
 void launch_glisa_trials_fused(const HostBatch& hb, cudaStream_t st, int max_shells);
 void launch_atweights(const HostBatch& hb, cudaStream_t st);        // k_atweights alone
 void launch_glisa_change_ff(const HostBatch& hb, cudaStream_t st);

@@ -321,6 +321,31 @@ __global__ void __launch_bounds__(kThreads) k_change(Batch bt) {
   if (threadIdx.x == 0) apart_ptr(J, at.atom, QA_CHANGE)[at.tile] = s;
 }
 
+// sum_{i, j in a} dc_i W_a[i][j] dc_j (dc = propars - propars_old) from the
+// lower triangle of atom a's Gram block (k_glisa_wgram): one warp, lanes over
+// the triangle's entries, summed in a fixed order. The int w (sum_{i in a}
+// dc_i g_i)^2 of compute_change (glisa.py:776) for fused gLISA jobs on the
+// molecular grid.
+__device__ double gram_change(const JobDev& J, int a) {
+  const int lane = threadIdx.x & 31;
+  const int s0 = J.shell_off[a];
+  const int k = J.shell_off[a + 1] - s0;
+  const double* W = J.wgram + J.wgoff[a];
+  double v = 0.0;
+  for (int e = lane; e < k * (k + 1) / 2; e += 32) {
+    int i = (int)((sqrtf(8.0f * (float)e + 1.0f) - 1.0f) * 0.5f);
+    while (i * (i + 1) / 2 > e) --i;
+    while ((i + 1) * (i + 2) / 2 <= e) ++i;
+    const int j = e - i * (i + 1) / 2;
+    const double di = J.propars[s0 + i] - J.propars_old[s0 + i];
+    const double dj = J.propars[s0 + j] - J.propars_old[s0 + j];
+    v += (i == j ? 1.0 : 2.0) * W[e] * di * dj;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
 // One block per job: change, entropy, charges (with_charges) and the
 // history row (core/iterstock.py:172-188). Warps sum atoms' tiles in
 // parallel; thread 0 adds the atoms in order (deterministic).
@@ -337,7 +362,7 @@ __global__ void __launch_bounds__(kFinishThreads) k_outer_finish(Batch bt, int w
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
   const int it = J.mail->i[MI_ITER];
   for (int a = warp; a < J.natom; a += nw) {
-    const double s = warp_tile_sum(J, apart_ptr(J, a, QA_CHANGE), J.ntile);
+    const double s = J.wgram ? gram_change(J, a) : warp_tile_sum(J, apart_ptr(J, a, QA_CHANGE), J.ntile);
     const double pop = with_charges ? warp_tile_sum(J, apart_ptr(J, a, QA_POP), J.ntile) : 0.0;
     if (lane == 0) {
       J.atom_out[a * AO_COUNT + AO_CHANGE] = s;
@@ -2422,6 +2447,15 @@ __global__ void __launch_bounds__(kThreads) k_glisa_trials(Batch bt) {
 // parameters by a fraction of the remaining error and ends the loop on a
 // change that is small only because the step was).
 constexpr double kArmijoUlps = 8.0;
+// The trial pass forms each trial's rho0 as rho0 + 2^-t G^T delta plus the
+// clipped shells' corrections (float-float); the fused pass that follows
+// takes the accepted trial's values as its rho0 while the last change is at
+// least kR0HandoffChange times the threshold. Each hand-off adds the
+// rounding of one float-float update (a few 1e-15 of rho0 + |G^T delta|),
+// which only steers the early iterations; from four orders of magnitude
+// above the threshold on, every pass forms rho0 = G^T c itself, so the
+// converged parameters are those of the direct evaluation.
+constexpr double kR0HandoffChange = 1e4;
 
 __global__ void __launch_bounds__(32 * kTrials) k_glisa_trial_pick(Batch bt) {
   __shared__ int pass[kTrials];
@@ -2473,6 +2507,9 @@ __global__ void __launch_bounds__(32 * kTrials) k_glisa_trial_pick(Batch bt) {
       }
     pick_s = pick;
     J.mail->d[MD_LS_X] = ldexp(1.0, -pick);
+    // fused jobs away from convergence: the next pass takes rho0 of the
+    // accepted trial from the trial pass (r0t) instead of forming G^T c
+    J.mail->i[MI_R0T] = J.r0t && J.mail->d[MD_CHANGE] >= kR0HandoffChange * J.threshold ? pick + 1 : 0;
   }
   __syncthreads();
   const int pick = pick_s;

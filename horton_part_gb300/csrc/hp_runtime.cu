@@ -423,7 +423,8 @@ int job_init(hp_ctx* ctx, const std::vector<hp_job*>& jobs, const HostBatch& hb)
     rc = build_batch(ctx, jobs, hp);
     if (rc) return rc;
     launch_glisa_pack(hp, ctx->stream);
-    launch_glisa_fused_ff(hp, ctx->stream, 1, fuse_shells, 0);
+    launch_glisa_wgram(hp, ctx->stream);
+    launch_glisa_fused_ff(hp, ctx->stream, 1, fuse_shells);
   }
   for (hp_job* j : jobs) j->initialized = true;
   return check_launch();
@@ -667,10 +668,12 @@ int step_glisa(hp_ctx* ctx, const std::vector<hp_job*>& jobs, const HostBatch& h
       }
     }
   }
-  const bool local = jobs[0]->dev.local != 0;  // atom grids: the change is radial
-  if (fused) {  // next iteration's promolecule and gradient, this step's change
+  // the change: atom grids radial; fused jobs on the molecular grid from the
+  // per-atom Gram blocks (in k_outer_finish); the others one pass over G
+  const bool local = jobs[0]->dev.local != 0;
+  if (fused) {  // next iteration's promolecule, gradient and Hessian
     ProfScope ps(ctx, HP_KERNEL_GLISA_PRO);
-    launch_glisa_fused_ff(hb, st, 1, fuse_shells, local ? 0 : 1);
+    launch_glisa_fused_ff(hb, st, 1, fuse_shells);
   }
   if (local) {
     ProfScope ps(ctx, HP_KERNEL_CHANGE);
@@ -1102,6 +1105,7 @@ int32_t hp_job_create(hp_ctx* ctx, const hp_job_desc* d, hp_job** out) {
           add(&J.wrf, 16 * (size_t)N);
           add(&J.r0f, 8 * (size_t)N);
           add(&J.d2f, 8 * (size_t)N);
+          add(&J.r0t, 8 * (size_t)kTrials * N);
         }
         add(&J.d1f, 8 * (size_t)N);
         add(&J.hvf, 8 * (size_t)N);
@@ -1112,6 +1116,19 @@ int32_t hp_job_create(hp_ctx* ctx, const hp_job_desc* d, hp_job** out) {
   }
   const bool local = d->grid_type == 1;
   const int nrad = local ? d->nrad : 0;
+  // fused jobs on the molecular grid: per-atom Gram blocks for the change
+  std::vector<int> wgoff_h;
+  if (fuse_job && !local) {
+    wgoff_h.assign((size_t)A + 1, 0);
+    for (int a = 0; a < A; ++a) {
+      const int k = d->shell_offsets[a + 1] - d->shell_offsets[a];
+      wgoff_h[a + 1] = wgoff_h[a] + k * (k + 1) / 2;
+    }
+    add(&J.wgoff, 4 * (size_t)(A + 1));
+    add(&J.wgram, 8 * (size_t)std::max(1, wgoff_h[A]));
+    add(&J.wgpart, 8 * (size_t)std::max(1, wgoff_h[A]) * ntile);
+    J.wgn = wgoff_h[A];
+  }
   if (local) {
     add(&J.rad_off, 4 * (size_t)(A + 1));
     add(&J.shell_pt, 8 * (size_t)(nrad + 1));
@@ -1330,6 +1347,7 @@ int32_t hp_job_create(hp_ctx* ctx, const hp_job_desc* d, hp_job** out) {
     }
     ok &= up(J.fpar, fpar32.data(), 4 * 4 * (size_t)S) == cudaSuccess;
   }
+  if (J.wgoff) ok &= up(J.wgoff, wgoff_h.data(), 4 * wgoff_h.size()) == cudaSuccess;
   ok &= up(J.propars, d->initial_propars, 8 * (size_t)P) == cudaSuccess;
   ok &= up(J.propars_init, d->initial_propars, 8 * (size_t)P) == cudaSuccess;
   ok &= cudaMemsetAsync(J.apart, 0, 8 * (size_t)A * qa * ntile, st) == cudaSuccess;

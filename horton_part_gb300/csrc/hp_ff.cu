@@ -349,12 +349,20 @@ __global__ void __launch_bounds__(kThreads) k_rdist_ff(Batch bt) {
 // of gisa.py:91-106 (force_on_molgrid=True) with the normalisation of
 // core/basis.py:161. Orders 2 (from the squared distance) and 1 are evaluated
 // in FF, any other order in FP64. fpar[4 s ..] = (pref hi, pref lo, alpha hi,
-// alpha lo). One thread per grid point, all shells.
+// alpha lo). One thread per grid point, all shells. The shells' orders are
+// classified once per block into shared memory (an FP64 comparison per shell
+// and point would run on the FP64 pipe, 1/64 of the FP32 rate).
 __global__ void __launch_bounds__(kThreads) k_glisa_basis_ff(Batch bt) {
   __shared__ float2 tab[64];
+  __shared__ int ord[kGffMaxShells];  // 2, 1 (FF paths) or 0 (FP64)
   ffa::load_exp_table(tab);
   int blk;
   const JobDev& J = decode_local_ff(bt, blk);
+  for (int s = threadIdx.x; s < J.nshell; s += kThreads) {
+    const double o = J.sh_order[s];
+    ord[s] = o == 2.0 ? 2 : o == 1.0 ? 1 : 0;
+  }
+  __syncthreads();
   const int p = blk * kThreads + threadIdx.x;
   if (p >= J.npoint) return;
   if (J.wrf) {  // w rho and rho as float pairs for the fused passes
@@ -368,14 +376,14 @@ __global__ void __launch_bounds__(kThreads) k_glisa_basis_ff(Batch bt) {
     const f2 d2 = dist2_ff(J, p, a);
     const f2 r = d2.hi > 0.0f ? ffa::sqrt_ff(d2) : f2{0.0f, 0.0f};
     for (int s = J.shell_off[a]; s < J.shell_off[a + 1]; ++s) {
-      const double order = J.sh_order[s];
+      const int order = ord[s];
       f2 g;
-      if (order == 2.0 || order == 1.0) {
+      if (order != 0) {
         const float* c = J.fpar + 4 * s;
-        const f2 x = ffa::mul(f2{c[2], c[3]}, order == 2.0 ? d2 : r);
+        const f2 x = ffa::mul(f2{c[2], c[3]}, order == 2 ? d2 : r);
         g = ffa::mul(f2{c[0], c[1]}, ffa::exp_ff(ffa::neg(x), tab));
       } else {
-        const double v = basis_shell<double>(order, J.sh_alpha[s], J.sh_pref[s],
+        const double v = basis_shell<double>(J.sh_order[s], J.sh_alpha[s], J.sh_pref[s],
                                              Dist<double>::r(J, p, a));
         split(v, &g.hi, &g.lo);
       }

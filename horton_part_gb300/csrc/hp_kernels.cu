@@ -177,12 +177,14 @@ __global__ void k_init_params(Batch bt) {
   int local;
   const JobDev& J = decode_local(bt, local);
   const double nelec = warp_tile_sum(J, J.jpart + (size_t)QJ_NELEC * J.ntile, J.ntile);
-  if ((threadIdx.x & 31) != 0) return;
-  J.mail->d[MD_NELEC] = nelec;
+  const int lane = threadIdx.x & 31;
+  if (lane == 0) J.mail->d[MD_NELEC] = nelec;
   if (J.scheme != SCHEME_MBIS && J.scheme != SCHEME_NLIS) {  // basis schemes: populations only
-    double s = 0.0;
-    for (int i = 0; i < J.nparam; ++i) s += J.propars[i];
-    for (int i = 0; i < J.nparam; ++i) J.propars[i] = J.propars[i] / s * nelec;
+    double s = 0.0;  // lanes over the parameters, then a fixed-order shuffle sum
+    for (int i = lane; i < J.nparam; i += 32) s += J.propars[i];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    for (int i = lane; i < J.nparam; i += 32) J.propars[i] = J.propars[i] / s * nelec;
   }
 }
 
@@ -404,11 +406,13 @@ __global__ void __launch_bounds__(kFinishThreads) k_outer_finish(Batch bt, int w
   }
 }
 
-// Charges from QA_POP (gLISA end, glisa.py:269-278).
-__global__ void k_charges(Batch bt) {
+// Charges from QA_POP (gLISA end, glisa.py:269-278): one warp per atom.
+constexpr int kChargesThreads = 512;
+__global__ void __launch_bounds__(kChargesThreads) k_charges(Batch bt) {
   int local;
   const JobDev& J = decode_local(bt, local);
-  for (int a = 0; a < J.natom; ++a) {
+  const int warp = threadIdx.x >> 5;
+  for (int a = warp; a < J.natom; a += kChargesThreads / 32) {
     const double pop = warp_tile_sum(J, apart_ptr(J, a, QA_POP), J.ntile);
     if ((threadIdx.x & 31) == 0) J.charges[a] = J.zpseudo[a] - pop;
   }
@@ -2586,7 +2590,7 @@ void launch_outer_finish(const HostBatch& hb, cudaStream_t st, int with_charges)
   HP_LAUNCH(k_outer_finish, K_JOB, kFinishThreads, with_charges);
 }
 
-void launch_charges(const HostBatch& hb, cudaStream_t st) { HP_LAUNCH(k_charges, K_JOB, 32); }
+void launch_charges(const HostBatch& hb, cudaStream_t st) { HP_LAUNCH(k_charges, K_JOB, kChargesThreads); }
 
 void launch_inner_init(const HostBatch& hb, cudaStream_t st) { HP_LAUNCH(k_inner_init, K_JOB, 128); }
 

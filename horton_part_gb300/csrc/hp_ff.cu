@@ -372,6 +372,7 @@ __global__ void __launch_bounds__(kThreads) k_glisa_basis_ff(Batch bt) {
     split(rho, &q.z, &q.w);
     J.wrf[p] = q;
   }
+  if (J.wgram) J.hess_s[p] = sqrtf((float)J.w[p]);  // scale of the weighted Gram matrix
   for (int a = 0; a < J.natom; ++a) {
     const f2 d2 = dist2_ff(J, p, a);
     const f2 r = d2.hi > 0.0f ? ffa::sqrt_ff(d2) : f2{0.0f, 0.0f};

@@ -1174,147 +1174,44 @@ __global__ void __launch_bounds__(kThreads) k_glisa_pack(Batch bt) {
 // same quadrature sum regrouped, so no pass over the grid is needed per
 // iteration (k_outer_finish forms the quadratic forms in FP64). W depends on
 // G and the weights only and is formed at each job initialisation, after
-// k_glisa_pack, in two kernels:
-//   k_glisa_wgram     one block per point tile: the tile's pairs (i >= j) of
-//                     active rows of one atom, kWgRound at a time, warp w
-//                     taking pairs w, w + 8, ...; the high plane of each
-//                     packed sub-tile is staged in shared memory, and lane l
-//                     adds (w g_i g_j)(l) (FP32 products of the high parts,
-//                     ~1e-7 relative each) to a compensated sum per pair; the
-//                     lane sums of a pair are merged in a fixed order and
-//                     written to wgpart[entry][tile] (entries of pairs
-//                     inactive on the tile: zero). The change is compared with
-//                     the threshold and reported: 1e-7 of W is the accuracy of
-//                     the FP32 change sums of the other passes;
-//   k_glisa_wgram_sum one warp per entry: the tiles' partials in FP64, tile
-//                     order in four chains.
-constexpr int kWgRound = 256;                           // pairs per round of a block
-constexpr int kWgPerWarp = kWgRound / kWarps;           // compensated sums per lane
-
+// the basis: the tensor cores form the whole weighted Gram matrix
+// G diag(w) G^T (k_glisa_hess_tc1 with the scale sqrt(w): X = G_hi sqrt(w)
+// split into TF32 high and low parts, three MMAs per product, ~1e-6
+// relative) as one FP32 triangle per point range in hpart, and
+// k_glisa_wgram sums the ranges' values of the atoms' diagonal blocks in
+// FP64 in range order, one warp per entry.
 __global__ void __launch_bounds__(kThreads) k_glisa_wgram(Batch bt) {
-  extern __shared__ float4 wsm4[];            // one sub-tile's high plane: nact rows x 32 points
-  __shared__ int act[kFuseMaxShells];
-  __shared__ int first[kFuseMaxShells];       // active row i: first active row of its atom
-  __shared__ int pstart[kFuseMaxShells + 1];  // pairs of rows < i (pairs (i, j), j <= i, one atom)
-  __shared__ int patom[kFuseMaxShells];       // atom of active row i
-  int tile;
-  const JobDev& J = decode_local_gf(bt, tile);
-  if (!J.fuse || !J.gpack || !J.wgram) return;
-  float* wsm = reinterpret_cast<float*>(wsm4);
-  const int S = J.nshell;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int* g = J.gact + (size_t)tile * (S + 1);
-  const int nact = g[S];
-  for (int e = threadIdx.x; e < J.wgn; e += kThreads) J.wgpart[(size_t)e * J.ntile + tile] = 0.0;
-  for (int i = threadIdx.x; i < nact; i += kThreads) act[i] = g[i];
-  __syncthreads();
-  for (int i = threadIdx.x; i < nact; i += kThreads) {
-    const int m = act[i];
-    int lo = 0, hi = J.natom;  // the atom a with shell_off[a] <= m < shell_off[a + 1]
-    while (hi - lo > 1) {
-      const int mid = (lo + hi) >> 1;
-      if (J.shell_off[mid] <= m) lo = mid;
-      else hi = mid;
-    }
-    const int s0 = J.shell_off[lo];
-    int f = 0, h = i;  // first active row with shell >= s0
-    while (f < h) {
-      const int mid = (f + h) >> 1;
-      if (act[mid] < s0) f = mid + 1;
-      else h = mid;
-    }
-    patom[i] = lo;
-    first[i] = f;
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    int n = 0;
-    for (int i = 0; i < nact; ++i) {
-      pstart[i] = n;
-      n += i - first[i] + 1;
-    }
-    pstart[nact] = n;
-  }
-  __syncthreads();
-  const int npair = pstart[nact];
-  const int p0 = tile * J.tile_points;
-  const int p1 = min(p0 + J.tile_points, J.npoint);
-  const int nsub = (p1 - p0 + 31) / 32;
-  const int plane = nact * 32;  // floats of the high plane of a sub-tile
-  const float4* ghi = reinterpret_cast<const float4*>(J.gpack + J.gtile_off[tile]);
-  for (int r0 = 0; r0 < npair; r0 += kWgRound) {
-    // the pair's staged rows, (row i) << 16 | row j (-1: no pair)
-    int rij[kWgPerWarp];
-#pragma unroll
-    for (int k = 0; k < kWgPerWarp; ++k) {
-      const int p = r0 + warp + kWarps * k;
-      rij[k] = -1;
-      if (p < npair) {
-        int a = 0, b = nact;  // the row i with pstart[i] <= p < pstart[i + 1]
-        while (b - a > 1) {
-          const int mid = (a + b) >> 1;
-          if (pstart[mid] <= p) a = mid;
-          else b = mid;
-        }
-        rij[k] = (a << 16) | (first[a] + (p - pstart[a]));
-      }
-    }
-    float accs[kWgPerWarp], accc[kWgPerWarp];  // compensated sums (sum, rounding errors)
-#pragma unroll
-    for (int k = 0; k < kWgPerWarp; ++k) accs[k] = accc[k] = 0.0f;
-    for (int sub = 0; sub < nsub; ++sub) {
-      __syncthreads();  // the previous sub-tile is consumed
-      for (int e = threadIdx.x; e < plane / 4; e += kThreads) wsm4[e] = ghi[(size_t)sub * (plane / 4) + e];
-      const int q = p0 + 32 * sub + lane;
-      const float wl = q < p1 ? (float)J.w[q] : 0.0f;  // packed entries past p1 are zero
-      __syncthreads();
-#pragma unroll
-      for (int k = 0; k < kWgPerWarp; ++k) {
-        if (rij[k] < 0) continue;  // warp-uniform
-        const float t = wl * wsm[(rij[k] >> 16) * 32 + lane] * wsm[(rij[k] & 0xffff) * 32 + lane];
-        const float u = accs[k] + t;
-        const float bb = u - accs[k];
-        accc[k] += (accs[k] - (u - bb)) + (t - bb);
-        accs[k] = u;
-      }
-    }
-#pragma unroll
-    for (int k = 0; k < kWgPerWarp; ++k) {
-      if (rij[k] < 0) continue;
-      Dot2 d{accs[k], accc[k]};
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        const Dot2 b{__shfl_xor_sync(0xffffffffu, d.s, o), __shfl_xor_sync(0xffffffffu, d.c, o)};
-        dot2_merge(d, b);
-      }
-      if (lane == 0) {
-        const int i = rij[k] >> 16, j = rij[k] & 0xffff;
-        const int a = patom[i];
-        const int s0 = J.shell_off[a];
-        const int li = act[i] - s0, lj = act[j] - s0;
-        J.wgpart[(size_t)(J.wgoff[a] + li * (li + 1) / 2 + lj) * J.ntile + tile] = dot2_value(d);
-      }
-    }
-  }
-}
-
-__global__ void __launch_bounds__(kThreads) k_glisa_wgram_sum(Batch bt) {
   int local;
   const JobDev& J = decode_local_gf(bt, local);
   if (!J.fuse || !J.wgram) return;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int nblk = (J.nshell * J.nshell + kThreads - 1) / kThreads;  // this job's K_SQUARE blocks
+  const int M = J.nshell;
+  const size_t tri = (size_t)M * (M + 1) / 2;
+  const float* hp = reinterpret_cast<const float*>(J.hpart);
+  const int nblk = (M * M + kThreads - 1) / kThreads;  // this job's K_SQUARE blocks
   for (int e = local * kWarps + warp; e < J.wgn; e += nblk * kWarps) {
-    const double* gp = J.wgpart + (size_t)e * J.ntile;
-    double h0 = 0.0, h1 = 0.0, h2 = 0.0, h3 = 0.0;
-    int t = lane;
-    for (; t + 96 < J.ntile; t += 128) {
-      h0 += gp[t];
-      h1 += gp[t + 32];
-      h2 += gp[t + 64];
-      h3 += gp[t + 96];
+    int lo = 0, hi = J.natom;  // the atom a with wgoff[a] <= e < wgoff[a + 1]
+    while (hi - lo > 1) {
+      const int mid = (lo + hi) >> 1;
+      if (J.wgoff[mid] <= e) lo = mid;
+      else hi = mid;
     }
-    for (; t < J.ntile; t += 32) h0 += gp[t];
+    const int q = e - J.wgoff[lo];  // local triangle entry (i, j), i >= j
+    int i = (int)((sqrtf(8.0f * (float)q + 1.0f) - 1.0f) * 0.5f);
+    while (i * (i + 1) / 2 > q) --i;
+    while ((i + 1) * (i + 2) / 2 <= q) ++i;
+    const int j = q - i * (i + 1) / 2;
+    const int gi = J.shell_off[lo] + i, gj = J.shell_off[lo] + j;
+    const size_t t = (size_t)gi * (gi + 1) / 2 + gj;
+    double h0 = 0.0, h1 = 0.0, h2 = 0.0, h3 = 0.0;
+    int sp = lane;
+    for (; sp + 96 < J.nsplit; sp += 128) {
+      h0 += hp[(size_t)sp * tri + t];
+      h1 += hp[(size_t)(sp + 32) * tri + t];
+      h2 += hp[(size_t)(sp + 64) * tri + t];
+      h3 += hp[(size_t)(sp + 96) * tri + t];
+    }
+    for (; sp < J.nsplit; sp += 32) h0 += hp[(size_t)sp * tri + t];
     double h = (h0 + h1) + (h2 + h3);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) h += __shfl_xor_sync(0xffffffffu, h, o);
@@ -1395,8 +1292,6 @@ void ensure_exp_table_gl() {
                        (int)kFuseSmemMax);
   cudaFuncSetAttribute(k_glisa_trials_fused, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)kFuseSmemMax);
-  cudaFuncSetAttribute(k_glisa_wgram, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       32 * 4 * kFuseMaxShells);
   if (dev < 31) done_mask |= 1 << dev;
 }
 
@@ -1438,13 +1333,8 @@ void launch_glisa_pack(const HostBatch& hb, cudaStream_t st) {
 }
 
 void launch_glisa_wgram(const HostBatch& hb, cudaStream_t st) {
-  if (hb.blocks[K_POINT] > 0) {
-    ensure_exp_table_gl();  // also the shared-memory limits of the fused kernels
-    const size_t smem = 32 * 4 * (size_t)std::max(1, hb.nact_max);  // one staged high plane
-    k_glisa_wgram<<<hb.blocks[K_POINT], kThreads, smem, st>>>(hb.b[K_POINT]);
-    ++g_launch_count;
-  }
-  HP_LAUNCH_GF(k_glisa_wgram_sum, K_SQUARE, kThreads);
+  launch_glisa_gram_tc(hb, st);
+  HP_LAUNCH_GF(k_glisa_wgram, K_SQUARE, kThreads);
 }
 
 void launch_glisa_promol_ff(const HostBatch& hb, cudaStream_t st) {

@@ -189,7 +189,6 @@ struct JobDev {
                           // nb = min(ntile, kFuseCtas)
   double* wgram;          // fused gLISA on the molecular grid: per atom the lower triangle of its
                           // weighted Gram block W_a[i][j] = sum_p w_p g_i(p) g_j(p) (the outer change)
-  double* wgpart;         // per point tile partials of wgram [wgn][ntile]
   int* wgoff;             // atom a's triangle starts at wgoff[a] [natom + 1]
   int wgn;                // entries of wgram (wgoff[natom])
   float2* d1f;            // gLISA, gff: w rho / rho0 as float pairs, npoint
@@ -600,6 +599,7 @@ int tc_hess_blocks(const JobDev& J);
 constexpr int kTcSinglePassShells = 256;
 // max_shells / min_shells: largest and smallest shell count among the batch's jobs
 void launch_glisa_hess_tc(const HostBatch& hb, cudaStream_t st, int max_shells, int min_shells);
+void launch_glisa_gram_tc(const HostBatch& hb, cudaStream_t st);  // G diag(w) G^T of fused jobs into hpart
 
 // mixed precision (hp_mixed.cu)
 void launch_promol_mx(const HostBatch& hb, cudaStream_t st, int model);

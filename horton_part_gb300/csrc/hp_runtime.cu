@@ -1126,7 +1126,6 @@ int32_t hp_job_create(hp_ctx* ctx, const hp_job_desc* d, hp_job** out) {
     }
     add(&J.wgoff, 4 * (size_t)(A + 1));
     add(&J.wgram, 8 * (size_t)std::max(1, wgoff_h[A]));
-    add(&J.wgpart, 8 * (size_t)std::max(1, wgoff_h[A]) * ntile);
     J.wgn = wgoff_h[A];
   }
   if (local) {

@@ -502,6 +502,25 @@ __global__ void __launch_bounds__(kT1Threads) k_glisa_hess_tc1(Batch bt) {
   }
 }
 
+// The weighted Gram matrix G diag(w) G^T of a fused job on the molecular
+// grid (its per-atom diagonal blocks give the outer change): the same
+// single-pass kernel with the scale sqrt(w) (hess_s, set by
+// k_glisa_basis_ff), one CTA per point range over the fused pass's nsplit
+// ranges (launch kind K_FUSE: min(ntile, kFuseCtas) blocks per job), into
+// hpart, which the job's first fused pass overwrites.
+void launch_glisa_gram_tc(const HostBatch& hb, cudaStream_t st) {
+  static int configured_device = -1;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (configured_device != dev) {
+    cudaFuncSetAttribute(k_glisa_hess_tc1, cudaFuncAttributeMaxDynamicSharedMemorySize, kT1Smem);
+    configured_device = dev;
+  }
+  if (hb.blocks[K_FUSE] <= 0) return;
+  k_glisa_hess_tc1<<<hb.blocks[K_FUSE], kT1Threads, kT1Smem, st>>>(hb.b[K_FUSE]);
+  ++g_launch_count;
+}
+
 int tc_hess_blocks(const JobDev& J) {
   if (J.nshell <= kT1Rows) return J.nsplit;  // k_glisa_hess_tc1: one CTA per point range
   return tc_tiles(J.nshell, -1, nullptr, nullptr, nullptr) * J.nsplit;

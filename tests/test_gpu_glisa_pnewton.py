@@ -123,3 +123,31 @@ def test_tensor_core_hessian_on_atom_grids(gpu_context):
           f"max|dq| {dq:.2e}")
     assert part["niter"] == int(g["niter"])
     assert dq < 5e-8  # atom-grid change: see tests/golden/cases.py tolerances()
+
+
+def test_outer_change_from_the_gram_blocks(gpu_context):
+    """Fused mixed-precision jobs form the outer change of every iteration
+    from per-atom Gram blocks W_a = sum_p w g_i g_j (formed once per job):
+    sum_a dc_a^T W_a dc_a is compute_change's int w (sum_{i in a} dc_i g_i)^2
+    regrouped. The history of changes must match the oracle's change between
+    consecutive parameter vectors of the same history, evaluated on the grid."""
+    mol = synthetic.chain_molecule({6: 1, 8: 1, 1: 3}, 30, 50, seed=11)
+    helper = synthetic.geometric_gaussian_basis({1: 4, 6: 6, 8: 6}, 0.05, 300.0)
+    part = wpart_schemes("glisa")(mol.coordinates, mol.numbers, mol.pseudo_numbers, mol.grid,
+                                  mol.density, grid_type=3, solver="cvxopt", basis_func=helper,
+                                  threshold=1e-10, precision="mixed")
+    part.do_partitioning()
+    hist = np.asarray(part["history_propars"])
+    changes = np.asarray(part["history_changes"])
+    assert len(hist) == len(changes) >= 4
+    orders = [helper.get_order(z) for z in mol.numbers]
+    exps = [helper.get_exponent(z) for z in mol.numbers]
+    r = O.radial_distances(mol.grid.points, mol.coordinates)
+    blocks = [O.basis_functions(o, e, r[a]) for a, (o, e) in enumerate(zip(orders, exps))]
+    offs = np.concatenate([[0], np.cumsum([len(e) for e in exps])])
+    w = mol.grid.weights
+    for k in range(1, len(hist)):
+        dc = hist[k] - hist[k - 1]
+        msd = sum(np.dot(w, (dc[offs[a]:offs[a + 1]] @ blocks[a]) ** 2) for a in range(len(blocks)))
+        ref = np.sqrt(msd)
+        assert changes[k] == pytest.approx(ref, rel=1e-5, abs=1e-13), (k, changes[k], ref)

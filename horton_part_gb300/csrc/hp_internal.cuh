@@ -552,7 +552,7 @@ void launch_glisa_pro(const HostBatch& hb, cudaStream_t st);
 void launch_glisa_grad(const HostBatch& hb, cudaStream_t st);
 void launch_glisa_hess(const HostBatch& hb, cudaStream_t st);
 void launch_glisa_reduce(const HostBatch& hb, cudaStream_t st);
-void launch_glisa_solve(const HostBatch& hb, cudaStream_t st, int projected);
+void launch_glisa_solve(const HostBatch& hb, cudaStream_t st, int projected, int max_shells, int tc);
 void launch_glisa_apply(const HostBatch& hb, cudaStream_t st, int mode);
 void launch_glisa_keep(const HostBatch& hb, cudaStream_t st);
 void launch_glisa_ls(const HostBatch& hb, cudaStream_t st, int first, int count);

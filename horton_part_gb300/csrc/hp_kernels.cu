@@ -1851,7 +1851,8 @@ constexpr int kNewtonThreads = 512;
 constexpr int kNewtonWarps = kNewtonThreads / 32;
 static_assert(4 * (kNewtonF32Max * kNewtonF32Max + 2 * kNewtonF32Max) <= kNewtonSmemL, "FP32 factor");
 
-__global__ void __launch_bounds__(kNewtonThreads) k_glisa_newton_step(Batch bt, int projected) {
+__global__ void __launch_bounds__(kNewtonThreads) k_glisa_newton_step(Batch bt, int projected,
+                                                                       int fp64_only) {
   extern __shared__ double l_smem[];
   __shared__ double col_smem[2 * kNewtonColMax];
   __shared__ int bad;
@@ -1861,7 +1862,10 @@ __global__ void __launch_bounds__(kNewtonThreads) k_glisa_newton_step(Batch bt, 
   const JobDev& J = decode_local(bt, local);
   if (glisa_idle(J)) return;
   const int M = J.nshell;
+  // fp64_only: the relaunch for jobs whose multi-block FP32 factor failed
+  if (fp64_only && J.freeidx[M + 1] != 3) return;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  __syncthreads();  // every thread has read the mark before thread 0 rewrites freeidx
   // free set in shell order: per-warp ballots and a prefix over the warps
   int nf = 0;
   for (int base = 0; base < M; base += kNewtonThreads) {
@@ -1889,7 +1893,21 @@ __global__ void __launch_bounds__(kNewtonThreads) k_glisa_newton_step(Batch bt, 
     bad = 0;
   }
   __syncthreads();
-  if (J.tc && nf <= kNewtonF32Max) {
+  if (J.tc && nf > kNewtonF32Max && !fp64_only) {
+    // tensor-core Hessian with a free set above the shared-memory factor:
+    // the free block's lower triangle in FP32 into chol, factored and solved
+    // by k_glisa_chol_panel / k_glisa_chol_update / k_glisa_chol_solve;
+    // freeidx[nshell + 1] = 2 marks the form
+    float* Lg = reinterpret_cast<float*>(J.chol);
+    for (int e = threadIdx.x; e < nf * nf; e += kNewtonThreads) {
+      const int i = e / nf, j = e - i * nf;
+      Lg[e] = j <= i ? (float)J.hess[(size_t)J.freeidx[i] * M + J.freeidx[j]] : 0.0f;
+    }
+    for (int m = threadIdx.x; m < M; m += kNewtonThreads) J.delta[m] = 0.0;
+    if (threadIdx.x == 0) J.freeidx[M + 1] = 2;
+    return;
+  }
+  if (J.tc && nf <= kNewtonF32Max && !fp64_only) {
     // tensor-core Hessian: FP32 factor and solve in shared memory; the factor
     // (with 1 / diagonal after it) is kept in chol for the refinement steps,
     // freeidx[nshell + 1] = 1 marks it as FP32
@@ -1965,6 +1983,160 @@ __global__ void __launch_bounds__(kNewtonThreads) k_glisa_newton_step(Batch bt, 
     for (int e = threadIdx.x; e < nf * nf; e += kNewtonThreads) J.chol[e] = L[e];
 }
 
+// FP32 Cholesky of a large free block (freeidx[nshell + 1] = 2, set by
+// k_glisa_newton_step), right-looking in panels of kCholBP columns over the
+// factor in global memory (nf x nf floats in chol, 1 / diag after them, the
+// layout of the shared-memory form: lower triangle and its upper copy), so
+// that the trailing updates spread over many blocks:
+//   k_glisa_chol_panel(p)   one block per job: the panel's diagonal block
+//                           factored by one warp (lane = row), then every
+//                           trailing row's panel entries by a triangular
+//                           solve (one thread per row), each written with its
+//                           upper copy;
+//   k_glisa_chol_update(p)  the rank-kCholBP update of the trailing lower
+//                           triangle in 64 x 64 tiles (4 x 4 per thread), the
+//                           blocks of launch kind K_SQUARE mapped onto the
+//                           tiles, the rest return;
+//   k_glisa_chol_solve      one block per job: the two triangular solves
+//                           (chol_solve_f on the global factor) into delta.
+// A non-positive pivot marks the job (freeidx[nshell + 1] = 3) for the FP64
+// factor of k_glisa_newton_step (fp64_only). Every element receives its
+// updates panel by panel in column order, independent of the block count.
+constexpr int kCholBP = 32;
+constexpr int kCholTile = 64;
+
+__device__ __forceinline__ bool chol_big(const JobDev& J) {
+  return !glisa_idle(J) && J.tc && J.freeidx[J.nshell + 1] == 2;
+}
+
+__global__ void __launch_bounds__(kThreads) k_glisa_chol_panel(Batch bt, int panel) {
+  __shared__ float D[kCholBP][kCholBP + 1];
+  int local;
+  const JobDev& J = decode_local(bt, local);
+  if (!chol_big(J)) return;
+  const int n = J.freeidx[J.nshell];
+  const int k = panel * kCholBP;
+  if (k >= n) return;
+  const int nb = min(kCholBP, n - k);
+  float* L = reinterpret_cast<float*>(J.chol);
+  float* dinv = L + (size_t)n * n;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int e = threadIdx.x; e < kCholBP * kCholBP; e += kThreads) {
+    const int i = e / kCholBP, j = e - i * kCholBP;
+    D[i][j] = (i < nb && j <= i) ? L[(size_t)(k + i) * n + k + j] : 0.0f;
+  }
+  __syncthreads();
+  if (warp == 0) {
+    bool neg = false;
+    for (int s2 = 0; s2 < nb; ++s2) {
+      __syncwarp();
+      const float d = D[s2][s2];
+      if (!(d > 0.0f)) neg = true;
+      const float piv = sqrtf(fmaxf(d, 1e-37f));
+      const float r = 1.0f / piv;
+      __syncwarp();
+      if (lane == s2) D[s2][s2] = piv;
+      if (lane > s2 && lane < nb) D[lane][s2] *= r;
+      __syncwarp();
+      if (lane > s2 && lane < nb) {
+        const float ls = D[lane][s2];
+        for (int j = s2 + 1; j <= lane; ++j) D[lane][j] = fmaf(-ls, D[j][s2], D[lane][j]);
+      }
+    }
+    __syncwarp();
+    if (lane < nb) dinv[k + lane] = 1.0f / D[lane][lane];
+    // not positive definite in FP32: the FP64 factor decides (k_glisa_newton_step
+    // relaunched with fp64_only); the later panels see the mark and return
+    if (neg && lane == 0) J.freeidx[J.nshell + 1] = 3;
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < nb * nb; e += kThreads) {  // the diagonal block and its upper copy
+    const int i = e / nb, j = e - i * nb;
+    if (j <= i) {
+      L[(size_t)(k + i) * n + k + j] = D[i][j];
+      L[(size_t)(k + j) * n + k + i] = D[i][j];
+    }
+  }
+  for (int i = k + nb + threadIdx.x; i < n; i += kThreads) {  // the trailing rows' panel entries
+    float x[kCholBP];
+#pragma unroll
+    for (int s2 = 0; s2 < kCholBP; ++s2) {
+      if (s2 < nb) {
+        float v = L[(size_t)i * n + k + s2];
+        for (int u = 0; u < s2; ++u) v = fmaf(-x[u], D[s2][u], v);
+        x[s2] = v / D[s2][s2];
+        L[(size_t)i * n + k + s2] = x[s2];
+        L[(size_t)(k + s2) * n + i] = x[s2];
+      }
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kThreads) k_glisa_chol_update(Batch bt, int panel) {
+  __shared__ float Pi[kCholTile][kCholBP + 1], Pj[kCholTile][kCholBP + 1];
+  int local;
+  const JobDev& J = decode_local(bt, local);
+  if (!chol_big(J)) return;
+  const int n = J.freeidx[J.nshell];
+  const int k = panel * kCholBP;
+  const int r0 = k + kCholBP;  // the trailing matrix starts here
+  if (r0 >= n) return;
+  const int T = (n - r0 + kCholTile - 1) / kCholTile;
+  if (local >= T * (T + 1) / 2) return;
+  int bi = (int)((sqrtf(8.0f * (float)local + 1.0f) - 1.0f) * 0.5f);
+  while (bi * (bi + 1) / 2 > local) --bi;
+  while ((bi + 1) * (bi + 2) / 2 <= local) ++bi;
+  const int bj = local - bi * (bi + 1) / 2;
+  const int i0 = r0 + kCholTile * bi, j0 = r0 + kCholTile * bj;
+  const float* L = reinterpret_cast<const float*>(J.chol);
+  for (int e = threadIdx.x; e < kCholTile * kCholBP; e += kThreads) {
+    const int a = e / kCholBP, c = e - a * kCholBP;
+    Pi[a][c] = i0 + a < n ? L[(size_t)(i0 + a) * n + k + c] : 0.0f;
+    Pj[a][c] = j0 + a < n ? L[(size_t)(j0 + a) * n + k + c] : 0.0f;
+  }
+  __syncthreads();
+  float* Lw = reinterpret_cast<float*>(J.chol);
+  const int ti = (threadIdx.x >> 4) * 4, tj = (threadIdx.x & 15) * 4;  // 4 x 4 elements per thread
+  float acc[4][4];
+#pragma unroll
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int c = 0; c < 4; ++c) acc[a][c] = 0.0f;
+#pragma unroll 8
+  for (int s2 = 0; s2 < kCholBP; ++s2) {
+    float xa[4], yc[4];
+#pragma unroll
+    for (int a = 0; a < 4; ++a) xa[a] = Pi[ti + a][s2];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) yc[c] = Pj[tj + c][s2];
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+      for (int c = 0; c < 4; ++c) acc[a][c] = fmaf(xa[a], yc[c], acc[a][c]);
+  }
+#pragma unroll
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      const int i = i0 + ti + a, j = j0 + tj + c;
+      if (i < n && j <= i) Lw[(size_t)i * n + j] -= acc[a][c];
+    }
+}
+
+__global__ void __launch_bounds__(kNewtonThreads) k_glisa_chol_solve(Batch bt) {
+  extern __shared__ float ysm[];
+  int local;
+  const JobDev& J = decode_local(bt, local);
+  if (!chol_big(J)) return;
+  const int M = J.nshell;
+  const int n = J.freeidx[M];
+  const float* L = reinterpret_cast<const float*>(J.chol);
+  for (int i = threadIdx.x; i < n; i += kNewtonThreads) ysm[i] = (float)(-(1.0 + J.grad[J.freeidx[i]]));
+  __syncthreads();
+  chol_solve_f(L, L + (size_t)n * n, n, ysm);
+  for (int i = threadIdx.x; i < n; i += kNewtonThreads) J.delta[J.freeidx[i]] = (double)ysm[i];
+}
+
 // Hessian-vector product with the exact FP64 Hessian, first half:
 // hvec[p] = (w rho / rho0^2)(p) * sum_m G[m][p] delta[m]. The second half is
 // k_glisa_grad(use_hvec = 1): gpart[m][tile] = sum_p G[m][p] hvec[p].
@@ -2030,6 +2202,15 @@ __global__ void __launch_bounds__(kThreads) k_glisa_refine(Batch bt) {
     r[i] = -(1.0 + J.grad[m]) - J.hsum[m];
   }
   __syncthreads();
+  if (f32 && nf > kNewtonF32Max) {  // the multi-block FP32 factor: solved in place
+    float* yv = reinterpret_cast<float*>(l_smem);
+    for (int i = threadIdx.x; i < nf; i += kThreads) yv[i] = (float)r[i];
+    __syncthreads();
+    const float* keep = reinterpret_cast<const float*>(J.chol);
+    chol_solve_f(keep, keep + (size_t)nf * nf, nf, yv);
+    for (int i = threadIdx.x; i < nf; i += kThreads) J.delta[J.freeidx[i]] += (double)yv[i];
+    return;
+  }
   if (f32) {  // FP32 factor of k_glisa_newton_step: copy it in, the block solves
     float* Lf = reinterpret_cast<float*>(l_smem);
     float* yv = Lf + nf * nf + nf;
@@ -2067,7 +2248,7 @@ __device__ void trial_set_body(const JobDev& J, int* tms, int* wcount) {
   // of equal t_m in index order
   int* tm = J.clip + M + 1;
   if (M <= kTrialSetSmem) {  // all threads: t_m per shell, then one ballot compaction per t
-        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int m = threadIdx.x; m < M; m += NT) {
       int t = 0;
       if (J.propars[m] + J.delta[m] < 0.0) {
@@ -2647,7 +2828,7 @@ void launch_glisa_reduce(const HostBatch& hb, cudaStream_t st) {
   HP_LAUNCH(k_glisa_reduce, K_SQUARE, kReduceThreads);
 }
 
-void launch_glisa_solve(const HostBatch& hb, cudaStream_t st, int projected) {
+void launch_glisa_solve(const HostBatch& hb, cudaStream_t st, int projected, int max_shells, int tc) {
   static int configured_device = -1;
   int dev = 0;
   cudaGetDevice(&dev);
@@ -2656,11 +2837,25 @@ void launch_glisa_solve(const HostBatch& hb, cudaStream_t st, int projected) {
                          kNewtonSmemL);
     cudaFuncSetAttribute(k_glisa_refine, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          kNewtonSmemL);
+    cudaFuncSetAttribute(k_glisa_chol_solve, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         kNewtonSmemL);
     configured_device = dev;
   }
   if (hb.blocks[K_JOB] > 0) {
-    k_glisa_newton_step<<<hb.blocks[K_JOB], kNewtonThreads, kNewtonSmemL, st>>>(hb.b[K_JOB], projected);
+    k_glisa_newton_step<<<hb.blocks[K_JOB], kNewtonThreads, kNewtonSmemL, st>>>(hb.b[K_JOB], projected, 0);
     ++g_launch_count;
+  }
+  // free sets above the shared-memory factor (tensor-core Hessian): the
+  // multi-block FP32 factor; the kernels return for the other jobs
+  if (tc && max_shells > kNewtonF32Max && hb.blocks[K_JOB] > 0) {
+    const int npanel = (max_shells + kCholBP - 1) / kCholBP;
+    for (int p = 0; p < npanel; ++p) {
+      HP_LAUNCH(k_glisa_chol_panel, K_JOB, kThreads, p);
+      HP_LAUNCH(k_glisa_chol_update, K_SQUARE, kThreads, p);
+    }
+    k_glisa_chol_solve<<<hb.blocks[K_JOB], kNewtonThreads, 4 * (size_t)max_shells, st>>>(hb.b[K_JOB]);
+    k_glisa_newton_step<<<hb.blocks[K_JOB], kNewtonThreads, kNewtonSmemL, st>>>(hb.b[K_JOB], projected, 1);
+    g_launch_count += 2;
   }
 }
 

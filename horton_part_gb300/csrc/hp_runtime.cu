@@ -614,7 +614,9 @@ int step_glisa(hp_ctx* ctx, const std::vector<hp_job*>& jobs, const HostBatch& h
     if (solver != SOLVER_SC) {
       // Newton system with the FP64 Hessian, or with the tensor-core one plus
       // iterative refinement against the exact FP64 product H delta.
-      launch_glisa_solve(hb, st, solver == SOLVER_PNEWTON ? 1 : 0);
+      int smax = 0;
+      for (hp_job* j : jobs) smax = std::max(smax, j->dev.nshell);
+      launch_glisa_solve(hb, st, solver == SOLVER_PNEWTON ? 1 : 0, smax, tc ? 1 : 0);
       if (tc)
         for (int k = 0; k < kRefineSteps; ++k) launch_glisa_refine(hb, st, gff, fuse_shells, unfused);
     }

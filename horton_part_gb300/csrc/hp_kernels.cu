@@ -2011,6 +2011,8 @@ __device__ __forceinline__ bool chol_big(const JobDev& J) {
 
 __global__ void __launch_bounds__(kThreads) k_glisa_chol_panel(Batch bt, int panel) {
   __shared__ float D[kCholBP][kCholBP + 1];
+  __shared__ float Xs[kThreads][kCholBP + 1];  // trailing rows' panel columns
+  __shared__ float Rp[kCholBP];                // 1 / the panel's pivots
   int local;
   const JobDev& J = decode_local(bt, local);
   if (!chol_big(J)) return;
@@ -2026,25 +2028,39 @@ __global__ void __launch_bounds__(kThreads) k_glisa_chol_panel(Batch bt, int pan
     D[i][j] = (i < nb && j <= i) ? L[(size_t)(k + i) * n + k + j] : 0.0f;
   }
   __syncthreads();
-  if (warp == 0) {
+  if (warp == 0) {  // lane t holds row t in registers; pivots and multipliers by shuffles
+    float a[kCholBP];
+#pragma unroll
+    for (int u = 0; u < kCholBP; ++u)
+      a[u] = (lane < nb && u <= lane) ? D[lane][u] : (u == lane ? 1.0f : 0.0f);
     bool neg = false;
-    for (int s2 = 0; s2 < nb; ++s2) {
-      __syncwarp();
-      const float d = D[s2][s2];
-      if (!(d > 0.0f)) neg = true;
+    float mypiv = 1.0f, myr = 1.0f;
+#pragma unroll
+    for (int s2 = 0; s2 < kCholBP; ++s2) {
+      const float d = __shfl_sync(0xffffffffu, a[s2], s2);
       const float piv = sqrtf(fmaxf(d, 1e-37f));
       const float r = 1.0f / piv;
-      __syncwarp();
-      if (lane == s2) D[s2][s2] = piv;
-      if (lane > s2 && lane < nb) D[lane][s2] *= r;
-      __syncwarp();
-      if (lane > s2 && lane < nb) {
-        const float ls = D[lane][s2];
-        for (int j = s2 + 1; j <= lane; ++j) D[lane][j] = fmaf(-ls, D[j][s2], D[lane][j]);
+      if (s2 < nb && !(d > 0.0f)) neg = true;
+      if (lane == s2) {
+        mypiv = piv;
+        myr = r;
+      }
+      const float lts = lane > s2 ? a[s2] * r : 0.0f;  // L[lane][s2]
+      if (lane > s2) a[s2] = lts;
+#pragma unroll
+      for (int u = s2 + 1; u < kCholBP; ++u) {
+        const float lus = __shfl_sync(0xffffffffu, lts, u);
+        if (lane >= u) a[u] = fmaf(-lts, lus, a[u]);
       }
     }
-    __syncwarp();
-    if (lane < nb) dinv[k + lane] = 1.0f / D[lane][lane];
+    if (lane < nb) {
+#pragma unroll
+      for (int u = 0; u < kCholBP; ++u)
+        if (u < lane) D[lane][u] = a[u];
+      D[lane][lane] = mypiv;
+      dinv[k + lane] = myr;
+      Rp[lane] = myr;
+    }
     // not positive definite in FP32: the FP64 factor decides (k_glisa_newton_step
     // relaunched with fp64_only); the later panels see the mark and return
     if (neg && lane == 0) J.freeidx[J.nshell + 1] = 3;
@@ -2057,17 +2073,43 @@ __global__ void __launch_bounds__(kThreads) k_glisa_chol_panel(Batch bt, int pan
       L[(size_t)(k + j) * n + k + i] = D[i][j];
     }
   }
-  for (int i = k + nb + threadIdx.x; i < n; i += kThreads) {  // the trailing rows' panel entries
-    float x[kCholBP];
+  // the trailing rows' panel entries, kThreads rows at a time: the rows'
+  // panel columns staged in shared memory by coalesced loads (a warp per
+  // row), solved one thread per row, written back the same way, with the
+  // upper copy written by columns (coalesced across the rows)
+  for (int rb = k + nb; rb < n; rb += kThreads) {
+    const int nr = min(kThreads, n - rb);
+    __syncthreads();  // Xs free
+    for (int e = threadIdx.x; e < nr * kCholBP; e += kThreads) {
+      const int a = e / kCholBP, c = e - a * kCholBP;
+      Xs[a][c] = c < nb ? L[(size_t)(rb + a) * n + k + c] : 0.0f;
+    }
+    __syncthreads();
+    if (threadIdx.x < nr) {  // column by column: the later entries' updates are independent
+      const int a = threadIdx.x;
+      float v[kCholBP];
 #pragma unroll
-    for (int s2 = 0; s2 < kCholBP; ++s2) {
-      if (s2 < nb) {
-        float v = L[(size_t)i * n + k + s2];
-        for (int u = 0; u < s2; ++u) v = fmaf(-x[u], D[s2][u], v);
-        x[s2] = v / D[s2][s2];
-        L[(size_t)i * n + k + s2] = x[s2];
-        L[(size_t)(k + s2) * n + i] = x[s2];
+      for (int c = 0; c < kCholBP; ++c) v[c] = Xs[a][c];
+#pragma unroll
+      for (int s2 = 0; s2 < kCholBP; ++s2) {
+        if (s2 < nb) {
+          const float x = v[s2] * Rp[s2];
+          v[s2] = x;
+#pragma unroll
+          for (int u = s2 + 1; u < kCholBP; ++u) v[u] = fmaf(-x, D[u][s2], v[u]);
+        }
       }
+#pragma unroll
+      for (int c = 0; c < kCholBP; ++c) Xs[a][c] = v[c];
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < nr * kCholBP; e += kThreads) {
+      const int a = e / kCholBP, c = e - a * kCholBP;
+      if (c < nb) L[(size_t)(rb + a) * n + k + c] = Xs[a][c];
+    }
+    for (int e = threadIdx.x; e < nb * nr; e += kThreads) {
+      const int c = e / nr, a = e - c * nr;
+      L[(size_t)(k + c) * n + rb + a] = Xs[a][c];
     }
   }
 }
@@ -2123,6 +2165,67 @@ __global__ void __launch_bounds__(kThreads) k_glisa_chol_update(Batch bt, int pa
     }
 }
 
+// y <- (L L^T)^-1 y with L in global memory (the multi-block factor): as
+// chol_solve_f, with each 32 x 32 diagonal block staged in shared memory
+// first, so that the sequential part on warp 0 reads shared memory; the
+// off-diagonal updates read rows of L (coalesced across the threads).
+__device__ void chol_solve_global(const float* L, const float* dinv, int n, float* y) {
+  __shared__ float B[32][33];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nb = (n + 31) / 32;
+  for (int jb = 0; jb < nb; ++jb) {
+    const int j0 = jb * 32, j1 = min(j0 + 32, n), w = j1 - j0;
+    __syncthreads();
+    for (int e = threadIdx.x; e < 32 * 32; e += blockDim.x) {  // B[c][r] = L[j0 + c][j0 + r] (upper copy: L_rc)
+      const int c = e >> 5, r = e & 31;
+      B[c][r] = (c < w && r < w) ? L[(size_t)(j0 + c) * n + j0 + r] : 0.0f;
+    }
+    __syncthreads();
+    if (warp == 0) {
+      const int i = j0 + lane;
+      float b = i < n ? y[i] : 0.0f;
+      for (int j = 0; j < w; ++j) {
+        const float zj = __shfl_sync(0xffffffffu, b, j) * dinv[j0 + j];
+        if (lane > j && lane < w) b = fmaf(-B[j][lane], zj, b);
+        else if (lane == j) b = zj;
+      }
+      if (i < n) y[i] = b;
+    }
+    __syncthreads();
+    for (int i = j1 + threadIdx.x; i < n; i += blockDim.x) {
+      float b = y[i];
+      for (int j = j0; j < j1; ++j) b = fmaf(-L[(size_t)j * n + i], y[j], b);
+      y[i] = b;
+    }
+  }
+  for (int jb = nb - 1; jb >= 0; --jb) {
+    const int j0 = jb * 32, j1 = min(j0 + 32, n), w = j1 - j0;
+    __syncthreads();
+    for (int e = threadIdx.x; e < 32 * 32; e += blockDim.x) {  // B[c][r] = L[j0 + c][j0 + r] (lower: L_cr)
+      const int c = e >> 5, r = e & 31;
+      B[c][r] = (c < w && r < w) ? L[(size_t)(j0 + c) * n + j0 + r] : 0.0f;
+    }
+    __syncthreads();
+    if (warp == 0) {
+      const int i = j0 + lane;
+      float b = i < n ? y[i] : 0.0f;
+      for (int j = w - 1; j >= 0; --j) {
+        const float xj = __shfl_sync(0xffffffffu, b, j) * dinv[j0 + j];
+        if (lane < j) b = fmaf(-B[j][lane], xj, b);
+        else if (lane == j) b = xj;
+      }
+      if (i < n) y[i] = b;
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < j0; i += blockDim.x) {
+      float b = y[i];
+      for (int j = j1 - 1; j >= j0; --j) b = fmaf(-L[(size_t)j * n + i], y[j], b);
+      y[i] = b;
+    }
+  }
+  __syncthreads();
+}
+
 __global__ void __launch_bounds__(kNewtonThreads) k_glisa_chol_solve(Batch bt) {
   extern __shared__ float ysm[];
   int local;
@@ -2133,7 +2236,7 @@ __global__ void __launch_bounds__(kNewtonThreads) k_glisa_chol_solve(Batch bt) {
   const float* L = reinterpret_cast<const float*>(J.chol);
   for (int i = threadIdx.x; i < n; i += kNewtonThreads) ysm[i] = (float)(-(1.0 + J.grad[J.freeidx[i]]));
   __syncthreads();
-  chol_solve_f(L, L + (size_t)n * n, n, ysm);
+  chol_solve_global(L, L + (size_t)n * n, n, ysm);
   for (int i = threadIdx.x; i < n; i += kNewtonThreads) J.delta[J.freeidx[i]] = (double)ysm[i];
 }
 
@@ -2207,7 +2310,7 @@ __global__ void __launch_bounds__(kThreads) k_glisa_refine(Batch bt) {
     for (int i = threadIdx.x; i < nf; i += kThreads) yv[i] = (float)r[i];
     __syncthreads();
     const float* keep = reinterpret_cast<const float*>(J.chol);
-    chol_solve_f(keep, keep + (size_t)nf * nf, nf, yv);
+    chol_solve_global(keep, keep + (size_t)nf * nf, nf, yv);
     for (int i = threadIdx.x; i < nf; i += kThreads) J.delta[J.freeidx[i]] += (double)yv[i];
     return;
   }

@@ -151,3 +151,30 @@ def test_outer_change_from_the_gram_blocks(gpu_context):
         msd = sum(np.dot(w, (dc[offs[a]:offs[a + 1]] @ blocks[a]) ** 2) for a in range(len(blocks)))
         ref = np.sqrt(msd)
         assert changes[k] == pytest.approx(ref, rel=1e-5, abs=1e-13), (k, changes[k], ref)
+
+
+def test_large_free_set_multiblock_factor(gpu_context):
+    """A free set above the 224 shells of the shared-memory factor: with the
+    tensor-core Hessian the Newton system is factored by the multi-block FP32
+    kernels (k_glisa_chol_panel / _update / _solve). The mixed job must reach
+    the FP64 job's charges (same optimum) without falling back to the FP64
+    factor."""
+    mol = synthetic.chain_molecule({6: 20, 1: 20, 8: 5}, 20, 50, seed=5)
+    helper = synthetic.geometric_gaussian_basis({1: 6, 6: 9, 8: 9}, 0.05, 300.0)
+    nshell = sum(helper.get_nshell(z) for z in mol.numbers)
+    assert nshell > 300
+    out = {}
+    for precision in ("fp64", "mixed"):
+        part = wpart_schemes("glisa")(mol.coordinates, mol.numbers, mol.pseudo_numbers, mol.grid,
+                                      mol.density, grid_type=3, solver="cvxopt", basis_func=helper,
+                                      threshold=1e-8, maxiter=300, precision=precision)
+        part.do_partitioning()
+        out[precision] = part
+    free = int((out["mixed"]["propars"] > 0).sum())
+    dq = np.abs(out["mixed"]["charges"] - out["fp64"]["charges"]).max()
+    print(f"{nshell} shells, {free} positive populations, niter mixed {out['mixed']['niter']} "
+          f"fp64 {out['fp64']['niter']}, max|dq| {dq:.2e}, "
+          f"FP64 factors {out['mixed']._job_info.f64_factors}")
+    assert free > 224
+    assert dq < 1e-7
+    assert out["mixed"]._job_info.f64_factors == 0

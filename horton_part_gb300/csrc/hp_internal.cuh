@@ -585,6 +585,20 @@ void launch_glisa_trials_ff(const HostBatch& hb, cudaStream_t st);
 void launch_glisa_promol_ff(const HostBatch& hb, cudaStream_t st);  // final promolecule
 void launch_glisa_active(const HostBatch& hb, cudaStream_t st);    // per-tile active shells
 void launch_glisa_pack(const HostBatch& hb, cudaStream_t st);      // active rows packed per sub-tile
+
+// job creation: the points' SoA and float-pair forms, w and rho pairs
+struct StageArgs {
+  const double* pts;       // (n, 3) as the caller passed them (device copy)
+  int n;
+  double* xyz[3];          // px, py, pz
+  float* hi[3];            // pxh, pyh, pzh (null: no float pairs)
+  float* lo[3];            // pxl, pyl, pzl
+  const double* w;         // weights and density (device)
+  const double* rho;
+  float* wf; float* wl;    // null: no w / rho pairs
+  float* rf; float* rl;
+};
+void launch_stage_points(const StageArgs& a, cudaStream_t st);
 void launch_glisa_wgram(const HostBatch& hb, cudaStream_t st);     // per-atom Gram blocks (outer change)
 void launch_glisa_trials_fused(const HostBatch& hb, cudaStream_t st, int max_shells);
 void launch_atweights(const HostBatch& hb, cudaStream_t st);        // k_atweights alone

@@ -158,6 +158,39 @@ __device__ bool small_chol_solve(double* A /* n*n */, double* b, int n) {
 // job set-up
 // ---------------------------------------------------------------------------
 
+// Job creation: the caller's (N, 3) points (copied to the device as they
+// are) into SoA FP64 coordinates and, for the float paths, their float pairs
+// (hi = the rounded value, lo = the rounded remainder, as the host would form
+// them); for mixed jobs also w and rho as float pairs. One thread per point.
+__global__ void __launch_bounds__(kThreads) k_stage_points(StageArgs a) {
+  const int p = blockIdx.x * kThreads + threadIdx.x;
+  if (p >= a.n) return;
+  const double v[3] = {a.pts[3 * (size_t)p], a.pts[3 * (size_t)p + 1], a.pts[3 * (size_t)p + 2]};
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    a.xyz[c][p] = v[c];
+    if (a.hi[c]) {
+      const float h = (float)v[c];
+      a.hi[c][p] = h;
+      a.lo[c][p] = (float)(v[c] - (double)h);
+    }
+  }
+  if (a.wf) {
+    const double w = a.w[p], r = a.rho[p];
+    const float wh = (float)w, rh = (float)r;
+    a.wf[p] = wh;
+    a.wl[p] = (float)(w - (double)wh);
+    a.rf[p] = rh;
+    a.rl[p] = (float)(r - (double)rh);
+  }
+}
+
+void launch_stage_points(const StageArgs& a, cudaStream_t st) {
+  if (a.n <= 0) return;
+  k_stage_points<<<(a.n + kThreads - 1) / kThreads, kThreads, 0, st>>>(a);
+  ++g_launch_count;
+}
+
 __global__ void __launch_bounds__(kThreads) k_nelec(Batch bt) {
   __shared__ double red[kWarps];
   int tile;

@@ -1193,29 +1193,17 @@ int32_t hp_job_create(hp_ctx* ctx, const hp_job_desc* d, hp_job** out) {
 
   // host staging: SoA grid, float hi/lo, atoms, shells
   cudaStream_t st = ctx->stream;
-  std::vector<double> buf((size_t)N);
   auto up = [&](const void* dst, const void* src, size_t bytes) {
     return cudaMemcpyAsync((void*)dst, src, bytes, cudaMemcpyHostToDevice, st);
   };
   // every work array starts at zero, as in a fresh allocation: a job's results
   // never depend on what an earlier job left in recycled device memory
   bool ok = cudaMemsetAsync(mem, 0, total, st) == cudaSuccess;
-  for (int c = 0; c < 3 && ok; ++c) {
-    for (int p = 0; p < N; ++p) buf[p] = d->points[(size_t)3 * p + c];
-    const double* dst = c == 0 ? J.px : c == 1 ? J.py : J.pz;
-    ok &= up(dst, buf.data(), 8 * (size_t)N) == cudaSuccess;
-    if (hilo) {
-      std::vector<float> hi((size_t)N), lo((size_t)N);
-      for (int p = 0; p < N; ++p) {
-        hi[p] = (float)buf[p];
-        lo[p] = (float)(buf[p] - (double)hi[p]);
-      }
-      const float* dh = c == 0 ? J.pxh : c == 1 ? J.pyh : J.pzh;
-      const float* dl = c == 0 ? J.pxl : c == 1 ? J.pyl : J.pzl;
-      ok &= up(dh, hi.data(), 4 * (size_t)N) == cudaSuccess;
-      ok &= up(dl, lo.data(), 4 * (size_t)N) == cudaSuccess;
-    }
-  }
+  // the points as the caller holds them, (N, 3), split on the device
+  // (k_stage_points, after w and rho are in place)
+  void* ptmp = nullptr;
+  ok &= job_alloc(ctx, &ptmp, 24 * (size_t)std::max(N, 1)) == cudaSuccess;
+  if (ok) ok &= up(ptmp, d->points, 24 * (size_t)N) == cudaSuccess;
   ok &= up(J.w, d->weights, 8 * (size_t)N) == cudaSuccess;
   std::vector<double> tgeo;
   if (cutoff) {
@@ -1254,23 +1242,29 @@ int32_t hp_job_create(hp_ctx* ctx, const hp_job_desc* d, hp_job** out) {
     ok &= up(J.rad_r, d->radial_points, 8 * (size_t)nrad) == cudaSuccess;
     ok &= up(J.rad_w, d->radial_weights, 8 * (size_t)nrad) == cudaSuccess;
   }
-  std::vector<float> wf32, rf32, wl32, rl32;
-  if (mixed) {
-    wf32.resize((size_t)N);
-    rf32.resize((size_t)N);
-    wl32.resize((size_t)N);
-    rl32.resize((size_t)N);
-    for (int p = 0; p < N; ++p) {
-      wf32[p] = (float)d->weights[p];
-      rf32[p] = (float)d->density[p];
-      wl32[p] = (float)(d->weights[p] - (double)wf32[p]);
-      rl32[p] = (float)(d->density[p] - (double)rf32[p]);
+  if (ok) {
+    StageArgs sa{};
+    sa.pts = static_cast<const double*>(ptmp);
+    sa.n = N;
+    // the job's arrays are read-only to the kernels that use them; this is
+    // where they are written
+    auto wd = [](const double* q) { return const_cast<double*>(q); };
+    auto wfl = [](const float* q) { return const_cast<float*>(q); };
+    sa.xyz[0] = wd(J.px); sa.xyz[1] = wd(J.py); sa.xyz[2] = wd(J.pz);
+    if (hilo) {
+      sa.hi[0] = wfl(J.pxh); sa.hi[1] = wfl(J.pyh); sa.hi[2] = wfl(J.pzh);
+      sa.lo[0] = wfl(J.pxl); sa.lo[1] = wfl(J.pyl); sa.lo[2] = wfl(J.pzl);
     }
-    ok &= up(J.wf, wf32.data(), 4 * (size_t)N) == cudaSuccess;
-    ok &= up(J.rhof, rf32.data(), 4 * (size_t)N) == cudaSuccess;
-    ok &= up(J.wl, wl32.data(), 4 * (size_t)N) == cudaSuccess;
-    ok &= up(J.rhol, rl32.data(), 4 * (size_t)N) == cudaSuccess;
+    sa.w = J.w;
+    sa.rho = J.rho;
+    if (mixed) {
+      sa.wf = wfl(J.wf); sa.wl = wfl(J.wl);
+      sa.rf = wfl(J.rhof); sa.rl = wfl(J.rhol);
+    }
+    launch_stage_points(sa, st);
+    ok &= cudaGetLastError() == cudaSuccess;
   }
+  job_free(ctx, ptmp);
   std::vector<double> ac((size_t)A);
   for (int c = 0; c < 3 && ok; ++c) {
     for (int a = 0; a < A; ++a) ac[a] = d->coordinates[(size_t)3 * a + c];

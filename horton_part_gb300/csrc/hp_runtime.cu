@@ -1197,8 +1197,29 @@ int32_t hp_job_create(hp_ctx* ctx, const hp_job_desc* d, hp_job** out) {
     return cudaMemcpyAsync((void*)dst, src, bytes, cudaMemcpyHostToDevice, st);
   };
   // every work array starts at zero, as in a fresh allocation: a job's results
-  // never depend on what an earlier job left in recycled device memory
-  bool ok = cudaMemsetAsync(mem, 0, total, st) == cudaSuccess;
+  // never depend on what an earlier job left in recycled device memory. The
+  // float-float planes of G are left out: k_glisa_basis_ff writes every
+  // element of them before anything reads them (they are most of a gLISA
+  // job's memory)
+  bool ok = true;
+  {
+    std::vector<std::pair<char*, char*>> skip;
+    auto plane = [&](const float* q) {
+      if (q) skip.push_back({(char*)q, (char*)q + align_up(4 * (size_t)S * N)});
+    };
+    if (J.gmat_lo) {  // the float-float planes exist only together
+      plane(J.gmat32);
+      plane(J.gmat_lo);
+    }
+    std::sort(skip.begin(), skip.end());
+    char* at = (char*)mem;
+    for (const auto& r : skip) {
+      if (r.first > at) ok &= cudaMemsetAsync(at, 0, (size_t)(r.first - at), st) == cudaSuccess;
+      at = std::max(at, r.second);
+    }
+    char* end = (char*)mem + total;
+    if (end > at) ok &= cudaMemsetAsync(at, 0, (size_t)(end - at), st) == cudaSuccess;
+  }
   // the points as the caller holds them, (N, 3), split on the device
   // (k_stage_points, after w and rho are in place)
   void* ptmp = nullptr;

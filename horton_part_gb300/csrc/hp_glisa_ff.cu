@@ -1297,7 +1297,16 @@ void ensure_exp_table_gl() {
 
 }  // namespace
 
-void launch_glisa_fused_ff(const HostBatch& hb, cudaStream_t st, int mode, int max_shells) {
+void launch_glisa_point_ff(const HostBatch& hb, cudaStream_t st) {
+  if (hb.blocks[K_POINT] > 0) {
+    ensure_exp_table_gl();
+    k_glisa_point_ff<<<hb.blocks[K_POINT], kThreads, 0, st>>>(hb.b[K_POINT]);
+    ++g_launch_count;
+  }
+}
+
+void launch_glisa_fused_ff(const HostBatch& hb, cudaStream_t st, int mode, int max_shells,
+                           bool point_pass) {
   if (hb.blocks[K_FUSE] <= 0) return;
   ensure_exp_table_gl();
   const int ring = fuse_ring_floats(max_shells, mode);
@@ -1305,7 +1314,7 @@ void launch_glisa_fused_ff(const HostBatch& hb, cudaStream_t st, int mode, int m
   if (mode) {
     k_glisa_fused_ff<1><<<hb.blocks[K_FUSE], kFuseThreads, smem, st>>>(hb.b[K_FUSE], ring);
     ++g_launch_count;
-    if (hb.blocks[K_POINT] > 0) {
+    if (point_pass && hb.blocks[K_POINT] > 0) {
       k_glisa_point_ff<<<hb.blocks[K_POINT], kThreads, 0, st>>>(hb.b[K_POINT]);
       ++g_launch_count;
     }

@@ -575,7 +575,11 @@ constexpr int kGffMaxShells = 2048;
 // fused passes (one read of G for a product and the row sums that follow it):
 // two shared-memory stages of [S][64] float pairs
 constexpr int kFuseMaxShells = 192;
-void launch_glisa_fused_ff(const HostBatch& hb, cudaStream_t st, int mode, int max_shells);
+// mode 1 with point_pass: k_glisa_point_ff after the pass (else the caller
+// launches it, launch_glisa_point_ff)
+void launch_glisa_fused_ff(const HostBatch& hb, cudaStream_t st, int mode, int max_shells,
+                           bool point_pass = true);
+void launch_glisa_point_ff(const HostBatch& hb, cudaStream_t st);
 void launch_glisa_basis_ff(const HostBatch& hb, cudaStream_t st);
 void launch_rdist_ff(const HostBatch& hb, cudaStream_t st);  // rdist of the batch's jobs
 void launch_glisa_pro_ff(const HostBatch& hb, cudaStream_t st);

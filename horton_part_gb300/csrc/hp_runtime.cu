@@ -77,6 +77,12 @@ struct hp_ctx {
   // job creations and destructions does not map and unmap device memory
   // each time. Destroying the context returns it to the device.
   cudaMemPool_t pool = nullptr;
+  // A second stream for the end-of-iteration bookkeeping of fused gLISA
+  // jobs (k_glisa_point_ff, k_outer_finish), which then overlaps the next
+  // iteration's reductions and Newton step (step_glisa); fork and join by
+  // events.
+  cudaStream_t side = nullptr;
+  cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
 };
 
 namespace {
@@ -583,6 +589,25 @@ int step_glisa(hp_ctx* ctx, const std::vector<hp_job*>& jobs, const HostBatch& h
   for (hp_job* j : jobs) fuse_shells = std::max(fuse_shells, j->dev.nshell);
   if (!fused) fuse_shells = 0;
   const int unfused = fused ? 0 : 1;
+  // fused projected-Newton jobs on the molecular grid: the point pass and
+  // k_outer_finish of an iteration run on the side stream while the next
+  // iteration's reduction and Newton step run here; the join comes before
+  // the refinement, which reads the change that k_outer_finish writes
+  // (glisa_refine_now), and before the trials, whose kernels must see the
+  // job's done flag. The reduction and the Newton step read none of the
+  // side kernels' outputs (a job that finished in the last iteration only
+  // costs them a wasted pass; its parameters are not touched before the
+  // join).
+  bool any_local = false;
+  for (hp_job* j : jobs) any_local |= j->dev.local != 0;
+  const bool overlap = fused && !any_local && solver == SOLVER_PNEWTON && ctx->side != nullptr;
+  bool pending = false;  // side work of the previous iteration not yet joined
+  auto join = [&]() {
+    if (pending) {
+      cudaStreamWaitEvent(st, ctx->join_ev, 0);
+      pending = false;
+    }
+  };
   for (int iter = 0; iter < iters; ++iter) {
   // projected Newton keeps the step's start in k_glisa_trial_pick
   if (solver != SOLVER_PNEWTON) launch_copy_old(hb, st);
@@ -617,6 +642,7 @@ int step_glisa(hp_ctx* ctx, const std::vector<hp_job*>& jobs, const HostBatch& h
       int smax = 0;
       for (hp_job* j : jobs) smax = std::max(smax, j->dev.nshell);
       launch_glisa_solve(hb, st, solver == SOLVER_PNEWTON ? 1 : 0, smax, tc ? 1 : 0);
+      join();
       if (tc)
         for (int k = 0; k < kRefineSteps; ++k) launch_glisa_refine(hb, st, gff, fuse_shells, unfused);
     }
@@ -673,9 +699,19 @@ int step_glisa(hp_ctx* ctx, const std::vector<hp_job*>& jobs, const HostBatch& h
   // the change: atom grids radial; fused jobs on the molecular grid from the
   // per-atom Gram blocks (in k_outer_finish); the others one pass over G
   const bool local = jobs[0]->dev.local != 0;
+  join();  // (a solver without the Newton step above)
   if (fused) {  // next iteration's promolecule, gradient and Hessian
     ProfScope ps(ctx, HP_KERNEL_GLISA_PRO);
-    launch_glisa_fused_ff(hb, st, 1, fuse_shells);
+    launch_glisa_fused_ff(hb, st, 1, fuse_shells, !overlap);
+  }
+  if (overlap) {
+    cudaEventRecord(ctx->fork_ev, st);
+    cudaStreamWaitEvent(ctx->side, ctx->fork_ev, 0);
+    launch_glisa_point_ff(hb, ctx->side);
+    launch_outer_finish(hb, ctx->side, 0);
+    cudaEventRecord(ctx->join_ev, ctx->side);
+    pending = true;
+    continue;  // the change is formed in k_outer_finish (Gram blocks)
   }
   if (local) {
     ProfScope ps(ctx, HP_KERNEL_CHANGE);
@@ -687,6 +723,7 @@ int step_glisa(hp_ctx* ctx, const std::vector<hp_job*>& jobs, const HostBatch& h
   }
   launch_outer_finish(hb, st, 0);
   }  // queued iterations
+  join();
   int rc = check_launch();
   if (rc) return rc;
   rc = read_mail(ctx);
@@ -901,6 +938,13 @@ int32_t hp_ctx_create(int32_t device, size_t hbm_budget, void* stream, hp_ctx** 
       return fail(HP_ERR_CUDA, "device memory pool creation failed");
     }
   }
+  if (cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->fork_ev, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->join_ev, cudaEventDisableTiming) != cudaSuccess) {
+    cudaGetLastError();
+    hp_ctx_destroy(c);
+    return fail(HP_ERR_CUDA, "side stream creation failed");
+  }
   size_t fr = 0, tot = 0;
   cudaMemGetInfo(&fr, &tot);
   c->budget = hbm_budget ? hbm_budget : (size_t)(0.9 * (double)fr);
@@ -938,6 +982,12 @@ int32_t hp_ctx_destroy(hp_ctx* c) {
     if (c->stream) cudaStreamSynchronize(c->stream);  // the jobs' frees have run
     cudaMemPoolDestroy(c->pool);
   }
+  if (c->side) {
+    cudaStreamSynchronize(c->side);
+    cudaStreamDestroy(c->side);
+  }
+  if (c->fork_ev) cudaEventDestroy(c->fork_ev);
+  if (c->join_ev) cudaEventDestroy(c->join_ev);
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
   delete c;
   return HP_OK;

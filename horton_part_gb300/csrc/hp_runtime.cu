@@ -428,8 +428,15 @@ int job_init(hp_ctx* ctx, const std::vector<hp_job*>& jobs, const HostBatch& hb)
     HostBatch hp;  // the jobs' descriptors now carry the packed arrays
     rc = build_batch(ctx, jobs, hp);
     if (rc) return rc;
+    // the Gram blocks (tensor cores, from the dense planes) on the side
+    // stream while the main stream packs G; joined before the first fused
+    // pass, which overwrites hpart
+    cudaEventRecord(ctx->fork_ev, ctx->stream);
+    cudaStreamWaitEvent(ctx->side, ctx->fork_ev, 0);
+    launch_glisa_wgram(hp, ctx->side);
+    cudaEventRecord(ctx->join_ev, ctx->side);
     launch_glisa_pack(hp, ctx->stream);
-    launch_glisa_wgram(hp, ctx->stream);
+    cudaStreamWaitEvent(ctx->stream, ctx->join_ev, 0);
     launch_glisa_fused_ff(hp, ctx->stream, 1, fuse_shells);
   }
   for (hp_job* j : jobs) j->initialized = true;

@@ -155,6 +155,7 @@ POLISH = True
 NCU_TRAFFIC = {
     ("glisa-c6h10n2o2", "mixed", "k_glisa_hess_tc1"): 364.90e6 + 3.19e6,
     ("glisa-c6h10n2o2", "mixed", "k_glisa_fused_ff<1>"): 324.64e6 + 7.57e6,
+    ("glisa-c6h10n2o2", "mixed", "k_glisa_trials_fused"): 329.22e6 + 27.24e6,
     ("mbis-chain60", "mixed", "inner"): 125.81e6 + 3.46e6,
 }
 

@@ -583,6 +583,14 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_fused_ff(Batch bt, in
     Dot2 acc[kFuseRows];
 #pragma unroll
     for (int r = 0; r < kFuseRows; ++r) acc[r] = Dot2{0.f, 0.f};
+    // rho0 given: the per-point pairs of the next sub-tile are loaded one
+    // sub-tile ahead, so that their latency overlaps the current one
+    float4 qn = make_float4(0.f, 0.f, 0.f, 0.f);
+    float2 rn = make_float2(0.f, 0.f);
+    if (r0in && p0 + lane < p1) {
+      qn = wrfp[p0 + lane];
+      rn = r0in[p0 + lane];
+    }
     for (int sub = 0; sub < nsub; ++sub) {
       const int slot = sub % nslot;
       const float* gh = ring + (size_t)slot * slotf;
@@ -601,12 +609,12 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_fused_ff(Batch bt, in
       float sx = 0.0f;
       if (r0in) {
         // rho0 given: every warp forms v and s of its lane's point (warp 0
-        // also stores rho0); the loads are issued before the staging wait
-        float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
-        float2 r0s = make_float2(0.f, 0.f);
-        if (pq < p1) {
-          q = wrfp[pq];
-          r0s = r0in[pq];
+        // also stores rho0) from the pairs loaded one sub-tile earlier
+        const float4 q = qn;
+        const float2 r0s = rn;
+        if (pq + kFuseSP < p1) {
+          qn = wrfp[pq + kFuseSP];
+          rn = r0in[pq + kFuseSP];
         }
         if (!timed_out && !umma::mbar_wait_sleep(rbar0 + 8 * slot, (ring_phase >> slot) & 1u))
           timed_out = 1;
@@ -985,12 +993,13 @@ __global__ void __launch_bounds__(kFuseThreads, 2) k_glisa_trials_fused(Batch bt
       grp[g * kFuseSP + lane] = make_float4(sc.s, sc.c, sd.s, sd.c);
     }
     __syncthreads();
-    if (warp == 0) {  // u and the groups' suffix sums
+    if (warp == 0) {  // u (warp 0) and the groups' suffix sums (warp 1)
       Dot2 du = part[lane];
 #pragma unroll
       for (int q = 1; q < kFuseWarps; ++q) dot2_merge(du, part[q * kFuseSP + lane]);
       const f2 u = dot2_ff(du);
       uv[lane] = make_float2(u.hi, u.lo);
+    } else if (warp == 1) {
       float4 v = grp[(kTrials - 1) * kFuseSP + lane];
       Dot2 sc{v.x, v.y}, sd{v.z, v.w};
 #pragma unroll

@@ -1231,7 +1231,7 @@ __global__ void __launch_bounds__(kThreads) k_glisa_wgram(Batch bt) {
 // Final promolecule of a float-float gLISA job (glisa.py:268-278 through
 // core/stockholder.py:153-175): per point, each atom's pro-atom
 // sum_m c_m g_m as a compensated dot product; rho_a, the promolecule (+1e-100
-// per atom, as k_promol) and its reciprocal in FP64 for k_atweights.
+// per atom, as k_promol) and its reciprocal in FP64 for k_glisa_atweights_ff.
 __global__ void __launch_bounds__(kThreads) k_glisa_promol_ff(Batch bt) {
   __shared__ float2 cf[kGffMaxShells];
   int blk;
@@ -1253,6 +1253,52 @@ __global__ void __launch_bounds__(kThreads) k_glisa_promol_ff(Batch bt) {
   }
   J.promol[p] = promol;
   J.invpro[p] = 1.0 / promol;
+}
+
+// at_weights of a float-float gLISA job from the final promolecule, one block
+// per point tile for all atoms (k_atweights takes a block per atom and tile
+// and re-reads the per-point arrays for each atom): per atom
+// rho_a = clip(pro_a / promol, 0, 1) rho, the tile's sum of w rho_a (QA_POP)
+// and largest rho_a, and the tile's entropy sum of w rho ln(rho / promol)
+// over the points above the cutoff. Each thread takes its points in the same
+// order and the block sums are the same as in k_atweights.
+__global__ void __launch_bounds__(kThreads) k_glisa_atweights_ff(Batch bt) {
+  __shared__ double red[kWarps];
+  __shared__ double out[1];
+  __shared__ float redm[kWarps];
+  int tile;
+  const JobDev& J = decode_local_gf(bt, tile);
+  const size_t N = J.npoint;
+  double acc[1] = {0.0};
+  for (int i = 0; i < J.ppt; ++i) {
+    const int p = point_in_tile(J, tile, i);
+    if (p >= J.npoint) continue;
+    const double promol = J.promol[p], rho = J.rho[p];
+    const bool sick = (promol < J.density_cutoff) || (rho < J.density_cutoff);
+    if (!sick) acc[0] += J.w[p] * rho * log(rho / promol);
+  }
+  block_sum<1>(acc, red, out);
+  if (threadIdx.x == 0) J.jpart[(size_t)QJ_ENTROPY * J.ntile + tile] = out[0];
+  for (int a = 0; a < J.natom; ++a) {
+    double pop[1] = {0.0};
+    float vmax = 0.0f;
+    double* ra = J.rhoa + (size_t)a * N;
+#pragma unroll 4
+    for (int i = 0; i < J.ppt; ++i) {
+      const int p = point_in_tile(J, tile, i);
+      if (p >= J.npoint) continue;
+      const double v = fmin(fmax(ra[p] * J.invpro[p], 0.0), 1.0) * J.rho[p];
+      ra[p] = v;
+      vmax = fmaxf(vmax, v > 3e38 ? 3e38f : (float)v);
+      pop[0] += J.w[p] * v;
+    }
+    block_sum<1>(pop, red, out);
+    if (J.amax) {
+      const float mx = block_max_f(vmax, redm);
+      if (threadIdx.x == 0) J.amax[(size_t)a * J.ntile + tile] = mx;
+    }
+    if (threadIdx.x == 0) J.apart[((size_t)a * J.qa + QA_POP) * J.ntile + tile] = out[0];
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -1355,8 +1401,9 @@ void launch_glisa_wgram(const HostBatch& hb, cudaStream_t st) {
   HP_LAUNCH_GF(k_glisa_wgram, K_SQUARE, kThreads);
 }
 
-void launch_glisa_promol_ff(const HostBatch& hb, cudaStream_t st) {
+void launch_glisa_final_ff(const HostBatch& hb, cudaStream_t st) {
   HP_LAUNCH_GF(k_glisa_promol_ff, K_POINT1, kThreads);
+  HP_LAUNCH_GF(k_glisa_atweights_ff, K_POINT, kThreads);
 }
 
 void launch_glisa_trials_ff(const HostBatch& hb, cudaStream_t st) {

@@ -586,7 +586,7 @@ void launch_glisa_pro_ff(const HostBatch& hb, cudaStream_t st);
 void launch_glisa_grad_ff(const HostBatch& hb, cudaStream_t st);
 void launch_glisa_hv_ff(const HostBatch& hb, cudaStream_t st);  // hvec and G hvec
 void launch_glisa_trials_ff(const HostBatch& hb, cudaStream_t st);
-void launch_glisa_promol_ff(const HostBatch& hb, cudaStream_t st);  // final promolecule
+void launch_glisa_final_ff(const HostBatch& hb, cudaStream_t st);   // final promolecule, then at_weights
 void launch_glisa_active(const HostBatch& hb, cudaStream_t st);    // per-tile active shells
 void launch_glisa_pack(const HostBatch& hb, cudaStream_t st);      // active rows packed per sub-tile
 

@@ -764,8 +764,7 @@ int step_glisa(hp_ctx* ctx, const std::vector<hp_job*>& jobs, const HostBatch& h
     if (rc) return rc;
     if (solver != SOLVER_SC) launch_glisa_check(hc, st);
     if (gff) {  // G as float-float planes: the promolecule from compensated sums
-      launch_glisa_promol_ff(hc, st);
-      launch_atweights(hc, st);
+      launch_glisa_final_ff(hc, st);
     } else {
       launch_promol(hc, st, 0, MODEL_BASIS);
     }

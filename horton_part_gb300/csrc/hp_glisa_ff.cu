@@ -1279,6 +1279,9 @@ __global__ void __launch_bounds__(kThreads) k_glisa_atweights_ff(Batch bt) {
   }
   block_sum<1>(acc, red, out);
   if (threadIdx.x == 0) J.jpart[(size_t)QJ_ENTROPY * J.ntile + tile] = out[0];
+  // the largest rho_a per tile only where a per-atom cutoff keeps it (its
+  // comparison and conversion are FP64 operations, like the sums)
+  const bool want_max = J.amax != nullptr;
   for (int a = 0; a < J.natom; ++a) {
     double pop[1] = {0.0};
     float vmax = 0.0f;
@@ -1289,11 +1292,11 @@ __global__ void __launch_bounds__(kThreads) k_glisa_atweights_ff(Batch bt) {
       if (p >= J.npoint) continue;
       const double v = fmin(fmax(ra[p] * J.invpro[p], 0.0), 1.0) * J.rho[p];
       ra[p] = v;
-      vmax = fmaxf(vmax, v > 3e38 ? 3e38f : (float)v);
+      if (want_max) vmax = fmaxf(vmax, v > 3e38 ? 3e38f : (float)v);
       pop[0] += J.w[p] * v;
     }
     block_sum<1>(pop, red, out);
-    if (J.amax) {
+    if (want_max) {
       const float mx = block_max_f(vmax, redm);
       if (threadIdx.x == 0) J.amax[(size_t)a * J.ntile + tile] = mx;
     }
